@@ -1,0 +1,76 @@
+"""Seeded synthetic meshes (cloth grids, tubes, boxes) used by the scenes."""
+from __future__ import annotations
+
+import numpy as np
+
+
+def grid(nx: int, ny: int, size_x: float = 1.0, size_y: float = 1.0):
+    """nx x ny vertex grid on [-sx/2, sx/2] x [-sy/2, sy/2] in the XZ plane
+    (y = 0), split into triangles along alternating diagonals.
+    Returns (vertices [n,3] f32, faces [f,3] u32)."""
+    xs = np.linspace(-0.5 * size_x, 0.5 * size_x, nx, dtype=np.float64)
+    zs = np.linspace(-0.5 * size_y, 0.5 * size_y, ny, dtype=np.float64)
+    X, Z = np.meshgrid(xs, zs, indexing="xy")  # [ny, nx]
+    v = np.stack([X.ravel(), np.zeros(X.size), Z.ravel()], axis=1).astype(np.float32)
+    faces = []
+    for j in range(ny - 1):
+        for i in range(nx - 1):
+            a = j * nx + i
+            b = a + 1
+            c = a + nx
+            d = c + 1
+            if (i + j) % 2 == 0:
+                faces.append((a, c, b))
+                faces.append((b, c, d))
+            else:
+                faces.append((a, c, d))
+                faces.append((a, d, b))
+    return v, np.asarray(faces, np.uint32)
+
+
+def tube(n_around: int, n_along: int, radius: float, length: float):
+    """Open cylinder along x: n_around x n_along vertices."""
+    th = np.linspace(0.0, 2.0 * np.pi, n_around, endpoint=False)
+    xs = np.linspace(-0.5 * length, 0.5 * length, n_along)
+    v = np.zeros((n_along * n_around, 3), np.float64)
+    for j, x in enumerate(xs):
+        v[j * n_around:(j + 1) * n_around, 0] = x
+        v[j * n_around:(j + 1) * n_around, 1] = radius * np.cos(th)
+        v[j * n_around:(j + 1) * n_around, 2] = radius * np.sin(th)
+    faces = []
+    for j in range(n_along - 1):
+        for i in range(n_around):
+            a = j * n_around + i
+            b = j * n_around + (i + 1) % n_around
+            c = a + n_around
+            d = b + n_around
+            faces.append((a, c, b))
+            faces.append((b, c, d))
+    return v.astype(np.float32), np.asarray(faces, np.uint32)
+
+
+def box(side: float, center=(0.0, 0.0, 0.0)):
+    """Closed axis-aligned cube, 8 vertices / 12 outward-facing triangles."""
+    h = 0.5 * side
+    c = np.asarray(center, np.float64)
+    v = np.array([[-h, -h, -h], [h, -h, -h], [h, h, -h], [-h, h, -h],
+                  [-h, -h, h], [h, -h, h], [h, h, h], [-h, h, h]]) + c
+    f = np.array([[0, 2, 1], [0, 3, 2], [4, 5, 6], [4, 6, 7], [0, 1, 5],
+                  [0, 5, 4], [2, 3, 7], [2, 7, 6], [1, 2, 6], [1, 6, 5],
+                  [0, 4, 7], [0, 7, 3]], np.uint32)
+    return v.astype(np.float32), f
+
+
+def edges_of(faces: np.ndarray) -> np.ndarray:
+    """Unique undirected edges in first-seen order (face order, then corner
+    order j -> j+1), each as (first-seen endpoint, next endpoint)."""
+    seen = {}
+    out = []
+    for f in faces:
+        for j in range(3):
+            a, b = int(f[j]), int(f[(j + 1) % 3])
+            key = (a, b) if a < b else (b, a)
+            if key not in seen:
+                seen[key] = len(out)
+                out.append((a, b))
+    return np.asarray(out, np.uint32).reshape(-1, 2)

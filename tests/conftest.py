@@ -1,0 +1,57 @@
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+PKG = ROOT / "ppf-contact-solver_gb300"
+for p in (str(PKG), str(ROOT)):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+# A fatal error inside the library returns a failed result to this process
+# instead of exiting it (the reference driver's exit(1) behaviour is the
+# default for every other host).
+os.environ.setdefault("PPF_RETURN_ON_FATAL", "1")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a)")
+    config.addinivalue_line("markers", "slow: long-running CPU test")
+
+
+@pytest.fixture(scope="session")
+def product_lib():
+    from ppf_gb300 import _lib, build
+
+    build.build_product()
+    return _lib.product()
+
+
+@pytest.fixture(scope="session")
+def oracle_lib():
+    from ppf_gb300 import _lib, build
+
+    build.build_oracle()
+    return _lib.oracle()
+
+
+@pytest.fixture(scope="session")
+def ref_lib():
+    from ppf_gb300 import _lib, build
+
+    try:
+        build.build_reference()
+    except Exception:
+        pass
+    lib = _lib.reference()
+    if lib is None:
+        pytest.skip("reference sources not present on this host")
+    return lib
+
+
+@pytest.fixture
+def rng():
+    return np.random.default_rng(1234)
