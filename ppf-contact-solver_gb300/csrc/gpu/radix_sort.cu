@@ -154,8 +154,10 @@ __global__ void __launch_bounds__(kSortThreads)
         const unsigned dd = dig[r];
         if (dd < kRadix) {
             unsigned pos = s_base[dd] + s_wcnt[warp][dd] + rank[r];
-            keys_out[pos] = key[r];
-            vals_out[pos] = val[r];
+            if (pos < n) {
+                keys_out[pos] = key[r];
+                vals_out[pos] = val[r];
+            }
         }
     }
 }

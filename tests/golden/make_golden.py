@@ -1,0 +1,34 @@
+"""Freezes golden vectors from the reference's own element code.
+
+Builds oracle/_ref/libppfref.so from the reference sources (oracle/Makefile),
+evaluates the seeded cases of tests/element_cases.py through it and writes the
+outputs to tests/golden/elements.npz. Run from the repository root:
+
+    python tests/golden/make_golden.py
+"""
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT / "tests"))
+sys.path.insert(0, str(ROOT / "ppf-contact-solver_gb300"))
+
+import element_cases as ec  # noqa: E402
+from ppf_gb300 import build  # noqa: E402
+
+
+def main():
+    lib_path = build.build_reference(force=True)
+    if lib_path is None:
+        raise SystemExit("reference sources not found")
+    ref = C.CDLL(str(lib_path))
+    out = ec.evaluate(ref, "ref_")
+    np.savez_compressed(Path(__file__).parent / "elements.npz", **out)
+    print("wrote", len(out), "arrays")
+
+
+if __name__ == "__main__":
+    main()
