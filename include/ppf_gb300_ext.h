@@ -48,6 +48,44 @@ int ppf_radix_sort_host(unsigned *keys, unsigned *vals, unsigned n,
 int ppf_radix_sort_device(unsigned *d_keys, unsigned *d_vals, unsigned n,
                           int key_bits, void *stream);
 
+/* ---- per-step statistics ------------------------------------------------
+ * The reference logs these per step through SimpleLog channels (newton_steps,
+ * pcg_iter, pcg_linsolve, toi: crates/ppf-cts-solver/src/cpp/main/main.cu:
+ * 1090-1111, 1354, 1547-1560); here they are returned to the host. */
+#define PPF_STATS_MAX_SOLVES 256
+typedef struct {
+    unsigned newton_iters;     /* Newton iterations of the last advance() */
+    unsigned pcg_iters_total;  /* PCG iterations summed over its solves */
+    unsigned pcg_solves;
+    float pcg_ms_total;        /* device time of the PCG solves */
+    float step_ms;             /* host wall time of advance() */
+    unsigned max_contacts;     /* largest active contact count of the step */
+    unsigned max_dyn_blocks;   /* largest number of contact-only blocks */
+    float pcg_ms[PPF_STATS_MAX_SOLVES];
+    unsigned pcg_iters[PPF_STATS_MAX_SOLVES];
+    float toi[PPF_STATS_MAX_SOLVES];
+} PpfStepStats;
+void ppf_step_stats(PpfStepStats *out);
+
+/* ---- stage inspection (parity checks) -------------------------------------
+ * Assembles and solves the first Newton system of a step at the current
+ * state (what advance() does before its first line search, main.cu:683-1120),
+ * writes the solution dx (3n floats) and keeps host copies of the system for
+ * ppf_debug_system. Returns the PCG state: 0 converged, 1 truncated, 2 failed. */
+int ppf_debug_newton_system(float *dx, unsigned *iters, float *resid);
+/* sizes[6]: fixed blocks, contact blocks, point-face, point-edge, point-point
+ * and edge-edge pairs of the system kept by ppf_debug_newton_system. */
+void ppf_debug_system_sizes(unsigned *sizes);
+/* Copies the kept system: fixed pattern (n+1 offsets, columns, 9 floats per
+ * block, per-vertex diagonal already folded in), contact blocks (offsets,
+ * columns, values), the per-vertex diagonal (9n), the right-hand side (3n)
+ * and the pair lists (pf: 2 u32, pe / pp: 3 u32 with the multiplicity and the
+ * friction flag in bit 31, ee: 2 u32 per pair). Any pointer may be NULL. */
+void ppf_debug_system(unsigned *f_off, unsigned *f_col, float *f_val,
+                      unsigned *d_off, unsigned *d_col, float *d_val,
+                      float *diag, float *force, unsigned *pf, unsigned *pe,
+                      unsigned *pp, unsigned *ee);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,92 @@
+/*
+ * ppf_gb300_scene.h -- host-side scene builder of libppf_gb300.so.
+ *
+ * Builds the DataSet / ParamSet / Constraint that initialize() consumes from
+ * plain meshes and material parameters, the way the reference's driver does
+ * before its first initialize() call (crates/ppf-cts-solver/src/builder.rs
+ * build() and make_param(), crates/ppf-cts-solver/src/scene.rs make_props(),
+ * crates/ppf-cts-solver/src/mesh.rs Mesh::new, and the face-edge props of
+ * crates/ppf-cts-solver/src/main.rs:205-250). Covered: shells (any model
+ * field, Baraff-Witkin evaluated), fix pins (static or kinematic), pull pins,
+ * analytic spheres and floors. Not covered: rods, tets, stitches, collision
+ * meshes, PDRD bodies, sand grains, UV anisotropy.
+ *
+ * Edge and hinge order: the reference extracts them from a hash map, whose
+ * iteration order is not reproducible; here they are listed in first-seen
+ * order over the faces, which is deterministic.
+ */
+#ifndef PPF_GB300_SCENE_H
+#define PPF_GB300_SCENE_H
+
+#include "ppf_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct PpfScene PpfScene;
+
+/* Per-object shell material, in the reference's parameter units
+ * (crates/ppf-cts-core/src/datamodel/params.rs object_param). */
+typedef struct {
+    int model;            /* PPF_MODEL_* ; default Baraff-Witkin */
+    float density;        /* kg/m^2 */
+    float young_mod;      /* Young's modulus pre-divided by density (Pa/rho) */
+    float poiss_rat;      /* (0, 0.5) */
+    float bend;           /* dimensionless bending stiffness */
+    float strain_limit;   /* 0 disables */
+    float contact_gap;    /* ghat */
+    float contact_offset;
+    float friction;
+} PpfShellMaterial;
+
+PpfScene *ppf_scene_create(void);
+void ppf_scene_destroy(PpfScene *scene);
+
+/* Reference defaults of every ParamSet field (params.rs app_param through
+ * builder.rs make_param), with dt = 1e-3. */
+void ppf_scene_default_param(PpfParamSet *out);
+
+/* Appends a shell object; returns the global index of its first vertex. */
+unsigned ppf_scene_add_shell(PpfScene *scene, const float *vertices,
+                             unsigned n_vertices, const unsigned *faces,
+                             unsigned n_faces, const PpfShellMaterial *mat);
+/* Initial velocity of every vertex (3 floats each); prev = curr - v dt. */
+void ppf_scene_set_velocity(PpfScene *scene, const float *velocity);
+/* Fix pins at the vertices' current positions. kinematic != 0 marks pins
+ * whose targets the host moves each step (ppf_scene_set_pin_targets). */
+void ppf_scene_pin(PpfScene *scene, const unsigned *indices, unsigned count,
+                   int kinematic);
+/* Soft pull pins toward the current positions with the given weight. */
+void ppf_scene_pull(PpfScene *scene, const unsigned *indices, unsigned count,
+                    float weight);
+void ppf_scene_add_sphere(PpfScene *scene, const float *center, float radius,
+                          float contact_gap, float friction, int reverse,
+                          int bowl);
+void ppf_scene_add_floor(PpfScene *scene, const float *ground, const float *up,
+                         float contact_gap, float friction);
+
+/* Builds the DataSet and ParamSet; `param` supplies the global parameters
+ * (dt, gravity, tolerances ...). Returns 0 on success. */
+int ppf_scene_build(PpfScene *scene, const PpfParamSet *param);
+PpfDataSet *ppf_scene_dataset(PpfScene *scene);
+PpfParamSet *ppf_scene_param(PpfScene *scene);
+PpfConstraint *ppf_scene_constraint(PpfScene *scene);
+/* Moves the kinematic pins: target positions at the end of the coming step
+ * and their displacement over it (3 floats per pin, in pin order). */
+void ppf_scene_set_pin_targets(PpfScene *scene, const float *position,
+                               const float *step_delta);
+unsigned ppf_scene_vertex_count(PpfScene *scene);
+/* Host copies of the built DataSet's vertex.curr / vertex.prev (3 floats per
+ * vertex). fetch() writes the device state into these arrays, so after it
+ * ppf_scene_positions returns the solver's state; ppf_scene_set_positions
+ * overwrites them before initialize(). Either pointer may be NULL. */
+void ppf_scene_positions(PpfScene *scene, float *curr, float *prev);
+void ppf_scene_set_positions(PpfScene *scene, const float *curr,
+                             const float *prev);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

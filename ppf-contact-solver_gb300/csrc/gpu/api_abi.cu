@@ -1,0 +1,251 @@
+// api_abi.cu -- the reference's extern "C" backend entry points
+// (crates/ppf-cts-solver/src/cpp/main/main.cu:1673-2350) and the stats /
+// stage-inspection extensions of include/ppf_gb300_ext.h.
+#include "../../../include/ppf_gb300_ext.h"
+#include "fatal.cuh"
+#include "solver.cuh"
+
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+using ppf::FatalError;
+using ppf::gpu::solver_instance;
+
+namespace {
+
+bool return_on_fatal() {
+    const char *e = std::getenv("PPF_RETURN_ON_FATAL");
+    return e && e[0] == '1';
+}
+
+// Records the error as the reference's fatal path does, then exits with
+// status 1 unless the host asked to get the failure back instead.
+void fatal(const FatalError &e) {
+    ppf::set_fatal(e.code, e.detail.c_str());
+    fprintf(stderr, "[ppf_gb300] fatal: %s\n", e.detail.c_str());
+    fflush(stderr);
+    if (!return_on_fatal()) std::exit(1);
+}
+
+struct DebugCache {
+    std::vector<unsigned> f_off, f_col, d_off, d_col, pf, pe, pp, ee;
+    std::vector<float> f_val, d_val, diag, force;
+} g_dbg;
+
+std::vector<unsigned char> g_window_dmap_active;
+struct Windows {
+    std::vector<unsigned> dmap;
+    std::vector<float> windows;
+    std::vector<unsigned> counts;
+    bool on = false;
+} g_win;
+constexpr unsigned kMaxCollisionWindows = 8; // main.cu:45
+
+} // namespace
+
+extern "C" {
+
+bool initialize(PpfDataSet *dataset, PpfParamSet *param) {
+    try {
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+            throw FatalError(PPF_FATAL_CUDA_DRIVER, "no CUDA device is visible to this process");
+        }
+        return solver_instance().initialize(dataset, param);
+    } catch (const FatalError &e) {
+        fatal(e);
+        return false;
+    }
+}
+
+void advance(PpfStepResult *result) {
+    try {
+        *result = solver_instance().advance();
+    } catch (const FatalError &e) {
+        fatal(e);
+        std::memset(result, 0, sizeof(*result));
+    }
+}
+
+void fetch(void) {
+    try {
+        solver_instance().fetch();
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+void fetch_inv_rest(void) {}
+
+void fetch_rest_angles(void) {}
+
+void fetch_dyn_counts(unsigned *n_value, unsigned *n_offset) {
+    try {
+        solver_instance().fetch_dyn_counts(n_value, n_offset);
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+void fetch_dyn(unsigned *index, PpfMat3x3f *value, unsigned *offset) {
+    try {
+        solver_instance().fetch_dyn(index, value, offset);
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+void update_dyn(unsigned *index, unsigned *offset) {
+    // The carried pattern only seeds capacity in the reference; here the
+    // contact blocks are re-derived every Newton iteration, so there is
+    // nothing to restore.
+    (void)index;
+    (void)offset;
+}
+
+void update_constraint(const PpfConstraint *constraint) {
+    try {
+        solver_instance().host->constraint = *constraint;
+        solver_instance().update_constraint(constraint);
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+void update_rest_shape(const PpfRestShapeUpdate *update) {
+    try {
+        solver_instance().update_rest_shape(update);
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+void override_velocity(const unsigned *indices, unsigned count, float vx, float vy,
+                       float vz, float dt) {
+    try {
+        solver_instance().override_velocity(indices, count, vx, vy, vz, dt);
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+void gather_current_positions(const unsigned *indices, unsigned count, float *out) {
+    try {
+        solver_instance().gather_current_positions(indices, count, out);
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+void override_angular_velocity(const unsigned *indices, unsigned count, float wx, float wy,
+                               float wz, float cx, float cy, float cz, float dt) {
+    try {
+        solver_instance().override_angular_velocity(indices, count, wx, wy, wz, cx, cy, cz, dt);
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+void init_collision_windows(const unsigned *vert_dmap, unsigned vert_count,
+                            const float *windows, const unsigned *window_counts,
+                            unsigned n_groups) {
+    g_win.dmap.assign(vert_dmap, vert_dmap + vert_count);
+    g_win.windows.assign(windows, windows + (size_t)n_groups * kMaxCollisionWindows * 2);
+    g_win.counts.assign(window_counts, window_counts + n_groups);
+    g_win.on = true;
+}
+
+void refresh_collision_active(float time) {
+    if (!g_win.on) return;
+    try {
+        std::vector<unsigned char> active(g_win.dmap.size());
+        for (size_t i = 0; i < g_win.dmap.size(); ++i) {
+            unsigned dm = g_win.dmap[i];
+            unsigned cnt = g_win.counts[dm];
+            bool a = cnt == 0;
+            for (unsigned w = 0; w < cnt && !a; ++w) {
+                float ts = g_win.windows[dm * kMaxCollisionWindows * 2 + w * 2];
+                float te = g_win.windows[dm * kMaxCollisionWindows * 2 + w * 2 + 1];
+                a = time >= ts && time < te;
+            }
+            active[i] = a ? 1 : 0;
+        }
+        solver_instance().set_active(active);
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+unsigned fetch_intersection_records(PpfIntersectionRecord *out, unsigned max_count) {
+    return solver_instance().fetch_intersection_records(out, max_count);
+}
+
+unsigned char ppf_fatal_code(void) { return g_ppf_fatal_code; }
+const char *ppf_fatal_detail(void) { return g_ppf_fatal_detail; }
+void set_log_path(const char *data_dir) { (void)data_dir; }
+
+// ---- extensions -------------------------------------------------------------
+void ppf_step_stats(PpfStepStats *out) {
+    const ppf::gpu::StepStats &s = solver_instance().stats();
+    std::memset(out, 0, sizeof(*out));
+    out->newton_iters = s.newton_iters;
+    out->pcg_iters_total = s.pcg_iters_total;
+    out->pcg_solves = s.pcg_solves;
+    out->pcg_ms_total = s.pcg_ms_total;
+    out->step_ms = s.step_ms;
+    out->max_contacts = s.max_contacts;
+    out->max_dyn_blocks = s.max_dyn_blocks;
+    unsigned k = s.pcg_solves < PPF_STATS_MAX_SOLVES ? s.pcg_solves : PPF_STATS_MAX_SOLVES;
+    for (unsigned i = 0; i < k; ++i) {
+        out->pcg_ms[i] = s.pcg_ms[i];
+        out->pcg_iters[i] = s.pcg_iters[i];
+        out->toi[i] = i < s.toi.size() ? s.toi[i] : 0.0f;
+    }
+}
+
+int ppf_debug_newton_system(float *dx, unsigned *iters, float *resid) {
+    try {
+        std::vector<float> d;
+        int state = solver_instance().debug_assemble_solve(d, *iters, *resid);
+        std::memcpy(dx, d.data(), d.size() * sizeof(float));
+        solver_instance().debug_matrix(g_dbg.f_off, g_dbg.f_col, g_dbg.f_val, g_dbg.d_off,
+                                       g_dbg.d_col, g_dbg.d_val, g_dbg.diag, g_dbg.force);
+        solver_instance().debug_pairs(g_dbg.pf, g_dbg.pe, g_dbg.pp, g_dbg.ee);
+        return state;
+    } catch (const FatalError &e) {
+        fatal(e);
+        return -1;
+    }
+}
+
+void ppf_debug_system_sizes(unsigned *sizes) {
+    sizes[0] = (unsigned)g_dbg.f_col.size();
+    sizes[1] = (unsigned)g_dbg.d_col.size();
+    sizes[2] = (unsigned)g_dbg.pf.size() / 2;
+    sizes[3] = (unsigned)g_dbg.pe.size() / 3;
+    sizes[4] = (unsigned)g_dbg.pp.size() / 3;
+    sizes[5] = (unsigned)g_dbg.ee.size() / 2;
+}
+
+void ppf_debug_system(unsigned *f_off, unsigned *f_col, float *f_val, unsigned *d_off,
+                      unsigned *d_col, float *d_val, float *diag, float *force,
+                      unsigned *pf, unsigned *pe, unsigned *pp, unsigned *ee) {
+    auto cp = [](void *dst, const auto &v) {
+        if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(v[0]));
+    };
+    cp(f_off, g_dbg.f_off);
+    cp(f_col, g_dbg.f_col);
+    cp(f_val, g_dbg.f_val);
+    cp(d_off, g_dbg.d_off);
+    cp(d_col, g_dbg.d_col);
+    cp(d_val, g_dbg.d_val);
+    cp(diag, g_dbg.diag);
+    cp(force, g_dbg.force);
+    cp(pf, g_dbg.pf);
+    cp(pe, g_dbg.pe);
+    cp(pp, g_dbg.pp);
+    cp(ee, g_dbg.ee);
+}
+
+} // extern "C"

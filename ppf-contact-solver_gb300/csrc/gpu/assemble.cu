@@ -1,0 +1,807 @@
+// assemble.cu -- Newton system assembly kernels.
+//
+// Stage order follows crates/ppf-cts-solver/src/cpp/main/main.cu:713-1049:
+// inertia / air / pull -> membrane + bending -> (copy elastic Hessian) ->
+// strain limit -> contact (detect, dedupe blocks, assemble) -> sphere / floor
+// -> Dirichlet elimination. Element formulas live in ../physics (shared with
+// the CPU oracle); these kernels gather, evaluate and scatter.
+#include "../physics/bw.cuh"
+#include "../physics/hinge.cuh"
+#include "../physics/strainlimit.cuh"
+#include "assemble.cuh"
+
+namespace ppf {
+namespace gpu {
+
+namespace {
+
+constexpr unsigned kB = 256;
+constexpr unsigned long long kEmptyKey = 0xFFFFFFFFFFFFFFFFull;
+
+__device__ __forceinline__ void atomic_add_block(float *dst, const Mat3 &m) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        float v = m.m[k];
+        if (v != 0.0f) atomicAdd(dst + k, v);
+    }
+}
+
+__device__ __forceinline__ Mat3 load_block(const float *p) { return load_mat3(p); }
+
+__device__ __forceinline__ Mat2 load_inv_rest(const float *p) {
+    Mat2 m;
+    m.m[0] = p[0];
+    m.m[1] = p[1];
+    m.m[2] = p[2];
+    m.m[3] = p[3];
+    return m;
+}
+
+// ---- inertia, air drag, pull pins (energy.cu:182-270, 700-716) ------------
+__global__ void k_vertex_energy(Scene s, StepParams p, AssemblyBuffers b) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) return;
+    const PpfVertexProp &vp = s.vprop[i];
+    if (vp.fix_index != 0) return;
+    const float dt = p.dt, dt2 = dt * dt;
+    Vec3 x = X(b.x0, i), y = X(b.x, i);
+    Vec3 normal = Vec3::zero();
+    for (unsigned k = s.vf_off[i]; k < s.vf_off[i + 1]; ++k) {
+        const unsigned *f = s.face + 3 * s.vf[k];
+        Vec3 z0 = X(b.x, f[0]), z1 = X(b.x, f[1]), z2 = X(b.x, f[2]);
+        normal += cross(z1 - z0, z2 - z0);
+    }
+    if (normal.squared_norm()) normal.normalize();
+    Vec3 wind = Vec3::zero();
+    if (!p.inactive_momentum) {
+        float ang = 30.0f * p.time;
+        float w = 0.25f * (0.5f * (1.0f + sinf(ang))) + (1.0f - 0.25f);
+        wind = w * vec3(p.wind[0], p.wind[1], p.wind[2]);
+    }
+    Vec3 f = Vec3::zero();
+    Mat3 H = Mat3::zero();
+    if (!normal.is_zero() && p.air_density) {
+        Vec3 z = (y - x) - dt * wind;
+        Mat3 P = Mat3::identity() - outer<3>(normal, normal);
+        Vec3 g = (normal * normal.dot(z)) / dt2 + ((p.air_friction * P) * z) / dt2;
+        Mat3 h = outer<3>(normal, normal) / dt2 + (p.air_friction * P) / dt2;
+        float s0 = vp.area * p.air_density;
+        f += s0 * g;
+        H += s0 * h;
+    }
+    bool pulled = false;
+    if (vp.pull_index > 0) {
+        const PpfPullPair &pp = s.pull[vp.pull_index - 1];
+        Vec3 pos = vec3(pp.position.v[0], pp.position.v[1], pp.position.v[2]);
+        f += pp.weight * (y - pos);
+        H += pp.weight * Mat3::identity();
+        pulled = true;
+    }
+    if (!pulled) {
+        Vec3 t = X(b.target, i);
+        f += vp.mass * ((y - t) / dt2);
+        H += vp.mass * (Mat3::identity() / dt2);
+    }
+    if (p.isotropic_air_friction) {
+        f += (p.isotropic_air_friction * (y - x)) / dt2;
+        H += (p.isotropic_air_friction / dt2) * Mat3::identity();
+    }
+    if (p.fix_xz && y[1] > p.fix_xz) {
+        float t = fminf(1.0f, y[1] - p.fix_xz);
+        Mat3 P = Mat3::identity();
+        P(1, 1) = 0.0f;
+        f += ((P * t) * vp.mass) * (y - x) / dt2;
+        H += (P * t) * vp.mass * dt2;
+    }
+    float *fo = b.force + 3 * i;
+    fo[0] += f[0];
+    fo[1] += f[1];
+    fo[2] += f[2];
+    float *d = b.diag + 9 * i;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) d[k] += H.m[k];
+}
+
+// ---- Baraff-Witkin membrane (energy.cu:304-364) ----------------------------
+__global__ void k_face_energy(Scene s, AssemblyBuffers b) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.nf) return;
+    const PpfFaceProp &pr = s.fprop[i];
+    if (pr.fixed || pr.rest_excluded || pr.collider) return;
+    const PpfFaceParam &fp = s.fparam[pr.param_index];
+    if (!(fp.mu > 0.0f)) return;
+    const unsigned *f = s.face + 3 * i;
+    Mat3 dedx;
+    Mat9 H;
+    bw::membrane(X(b.x, f[0]), X(b.x, f[1]), X(b.x, f[2]),
+                 load_inv_rest(s.inv_rest + 4 * i), fp.mu, fp.lambda, pr.mass, dedx, H);
+    for (int a = 0; a < 3; ++a) atomic_add3(b.force + 3 * f[a], dedx.col(a));
+    const unsigned *slot = s.face_slot + 9 * i;
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) {
+            unsigned sl = slot[3 * a + c];
+            if (sl != kSentinel)
+                atomic_add_block(b.fixed_val + 9 * (size_t)sl, H.block<3, 3>(3 * a, 3 * c));
+        }
+}
+
+// ---- dihedral bending (energy.cu:448-553) ----------------------------------
+__global__ void k_hinge_energy(Scene s, AssemblyBuffers b) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.nh) return;
+    const PpfHingeProp &pr = s.hprop[i];
+    if (pr.fixed || pr.collider) return;
+    const PpfHingeParam &hp = s.hparam[pr.param_index];
+    const unsigned *h = s.hinge + 4 * i;
+    float rho = 0.0f;
+    int cnt = 0;
+    for (int k = 0; k < 4; ++k) {
+        float a = s.vprop[h[k]].area;
+        if (a > 0.0f) {
+            rho += s.vprop[h[k]].mass / a;
+            ++cnt;
+        }
+    }
+    if (cnt > 0) rho /= cnt;
+    float k = hinge::stiffness(hp.bend, hp.bend_warp, hp.bend_weft, pr.uv_edge_sin2,
+                               pr.length, pr.area, rho);
+    if (!(k > 0.0f)) return;
+    const unsigned r[4] = {h[2], h[1], h[0], h[3]};
+    Mat3x4 dedx;
+    Mat12 H;
+    hinge::force_hessian(X(b.x, r[0]), X(b.x, r[1]), X(b.x, r[2]), X(b.x, r[3]),
+                         pr.rest_angle, dedx, H);
+    dedx *= k;
+    H *= k;
+    for (int a = 0; a < 4; ++a) atomic_add3(b.force + 3 * r[a], dedx.col(a));
+    const unsigned *slot = s.hinge_slot + 16 * i;
+    for (int a = 0; a < 4; ++a)
+        for (int c = 0; c < 4; ++c) {
+            unsigned sl = slot[4 * a + c];
+            if (sl != kSentinel)
+                atomic_add_block(b.fixed_val + 9 * (size_t)sl, H.block<3, 3>(3 * a, 3 * c));
+        }
+}
+
+// ---- strain-limit barrier (strainlimiting.cu:46-98) -------------------------
+__global__ void k_strain_limit(Scene s, StepParams p, AssemblyBuffers b) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.nf) return;
+    const PpfFaceProp &pr = s.fprop[i];
+    const PpfFaceParam &fp = s.fparam[pr.param_index];
+    if (pr.fixed || pr.rest_excluded || !(fp.strainlimit > 0.0f)) return;
+    float limit = strain::effective_limit(fp.strainlimit, fp.shrink_x, fp.shrink_y);
+    const unsigned *f = s.face + 3 * i;
+    Mat2 inv = load_inv_rest(s.inv_rest + 4 * i);
+    Mat3x2 F = bw::deformation_grad(X(b.x, f[0]), X(b.x, f[1]), X(b.x, f[2]), inv);
+    strain::Svd32 sv;
+    Mat3 dedx;
+    Mat9 H;
+    if (!strain::face_barrier(F, inv, fp.strainlimit, p.barrier, p.eiganalysis_eps, sv,
+                              dedx, H))
+        return;
+    Mat9 local;
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c)
+            local.set_block<3, 3>(3 * a, 3 * c, fixed_block(s, b.fixed_tmp, f[a], f[c]));
+    float k = strain::stiffness(X(b.x0, f[0]), X(b.x0, f[1]), X(b.x0, f[2]), local,
+                                pr.mass, sv.S.max_coeff(), limit);
+    Mat3 kf = k * dedx;
+    Mat9 kH = k * H;
+    for (int a = 0; a < 3; ++a) atomic_add3(b.force + 3 * f[a], kf.col(a));
+    const unsigned *slot = s.face_slot + 9 * i;
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) {
+            unsigned sl = slot[3 * a + c];
+            if (sl != kSentinel)
+                atomic_add_block(b.fixed_val + 9 * (size_t)sl, kH.block<3, 3>(3 * a, 3 * c));
+        }
+}
+
+// ---- contact detection (contact.cu:1398-1787, stage 0) ----------------------
+__device__ __forceinline__ unsigned push_pair(unsigned *ctr, unsigned cap) {
+    unsigned slot = atomicAdd(ctr, 1u);
+    return slot < cap ? slot : kSentinel;
+}
+
+struct VertexQueryOp {
+    const Scene &s;
+    const float *x;
+    unsigned v;
+    int kind; // 0 face, 1 edge, 2 vertex
+    PairLists &pl;
+    IterStatus *st;
+    unsigned found;
+    __device__ void operator()(unsigned prim) {
+        if (kind == 0) {
+            if (accept_point_face(s, x, v, prim)) {
+                unsigned k = push_pair(&st->n_pf, pl.cap_pf);
+                if (k != kSentinel) pl.pf[k] = make_uint2(v, prim);
+                ++found;
+            }
+        } else if (kind == 1) {
+            bool fr = true;
+            Vec2 c;
+            unsigned cnt = accept_point_edge(s, x, v, prim, &fr, &c);
+            if (cnt) {
+                unsigned k = push_pair(&st->n_pe, pl.cap_pe);
+                if (k != kSentinel) pl.pe[k] = make_uint3(v, prim, cnt | (fr ? 0x80000000u : 0u));
+                ++found;
+            }
+        } else {
+            bool fr = true;
+            unsigned cnt = accept_point_point(s, x, v, prim, &fr);
+            if (cnt) {
+                unsigned k = push_pair(&st->n_pp, pl.cap_pp);
+                if (k != kSentinel) pl.pp[k] = make_uint3(v, prim, cnt | (fr ? 0x80000000u : 0u));
+                ++found;
+            }
+        }
+    }
+};
+
+__global__ void k_detect_vertex(Scene s, BvhView fb, BvhView eb, BvhView vb,
+                                const float *x, PairLists pl, IterStatus *st) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= s.n_surf) return;
+    unsigned v = vb.node[t].x - 1u; // Morton order of the vertex tree
+    float m = s.margin_vert[v];
+    Vec3 p = X(x, v);
+    float4 qmin = make_float4(p[0] - m, p[1] - m, p[2] - m, 1.0f);
+    float4 qmax = make_float4(p[0] + m, p[1] + m, p[2] + m, 0.0f);
+    VertexQueryOp op{s, x, v, 0, pl, st, 0u};
+    bvh_query(fb, qmin, qmax, op, &st->status);
+    op.kind = 1;
+    bvh_query(eb, qmin, qmax, op, &st->status);
+    op.kind = 2;
+    bvh_query(vb, qmin, qmax, op, &st->status);
+    if (op.found) atomicAdd(&st->n_contact, op.found);
+}
+
+struct EdgeQueryOp {
+    const Scene &s;
+    const float *x;
+    unsigned e;
+    PairLists &pl;
+    IterStatus *st;
+    unsigned found;
+    __device__ void operator()(unsigned other) {
+        if (accept_edge_edge(s, x, e, other)) {
+            unsigned k = push_pair(&st->n_ee, pl.cap_ee);
+            if (k != kSentinel) pl.ee[k] = make_uint2(e, other);
+            ++found;
+        }
+    }
+};
+
+__global__ void k_detect_edge(Scene s, BvhView eb, const float *x, PairLists pl,
+                              IterStatus *st) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= s.ne) return;
+    unsigned e = eb.node[t].x - 1u;
+    const unsigned *ed = s.edge + 2 * e;
+    float m = s.margin_edge[e];
+    Vec3 a = X(x, ed[0]), c = X(x, ed[1]);
+    float4 qmin = make_float4(fminf(a[0], c[0]) - m, fminf(a[1], c[1]) - m,
+                              fminf(a[2], c[2]) - m, 1.0f);
+    float4 qmax = make_float4(fmaxf(a[0], c[0]) + m, fmaxf(a[1], c[1]) + m,
+                              fmaxf(a[2], c[2]) + m, 0.0f);
+    EdgeQueryOp op{s, x, e, pl, st, 0u};
+    bvh_query(eb, qmin, qmax, op, &st->status);
+    if (op.found) atomicAdd(&st->n_contact, op.found);
+}
+
+// ---- dynamic contact blocks: hash dedupe + CSR layout ----------------------
+__device__ __forceinline__ unsigned hash_key(unsigned long long k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return (unsigned)k;
+}
+
+__device__ void hash_insert(DynMatrix &dm, unsigned long long key, IterStatus *st) {
+    unsigned mask = dm.hcap - 1u;
+    unsigned h = hash_key(key) & mask;
+    for (unsigned probe = 0; probe < dm.hcap; ++probe) {
+        unsigned long long prev = atomicCAS(&dm.hkey[h], kEmptyKey, key);
+        if (prev == kEmptyKey) {
+            atomicAdd(&st->n_dyn, 1u);
+            return;
+        }
+        if (prev == key) return;
+        h = (h + 1u) & mask;
+    }
+    atomicOr(&st->status, STATUS_BLOCK_OVERFLOW);
+}
+
+__device__ unsigned hash_find(const DynMatrix &dm, unsigned long long key) {
+    unsigned mask = dm.hcap - 1u;
+    unsigned h = hash_key(key) & mask;
+    for (unsigned probe = 0; probe < dm.hcap; ++probe) {
+        unsigned long long k = dm.hkey[h];
+        if (k == key) return dm.hval[h];
+        if (k == kEmptyKey) return kSentinel;
+        h = (h + 1u) & mask;
+    }
+    return kSentinel;
+}
+
+template <int N>
+__device__ void insert_pair_keys(const Scene &s, DynMatrix &dm, const unsigned (&idx)[N],
+                                 IterStatus *st) {
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+            unsigned i = idx[a], j = idx[c];
+            if (i < j && fixed_slot(s, i, j) == kSentinel)
+                hash_insert(dm, ((unsigned long long)i << 32) | j, st);
+        }
+}
+
+__device__ __forceinline__ void pair_indices_pf(const Scene &s, uint2 pr, unsigned (&idx)[4]) {
+    const unsigned *f = s.face + 3 * pr.y;
+    idx[0] = pr.x;
+    idx[1] = f[0];
+    idx[2] = f[1];
+    idx[3] = f[2];
+}
+__device__ __forceinline__ void pair_indices_pe(const Scene &s, uint3 pr, unsigned (&idx)[3]) {
+    const unsigned *e = s.edge + 2 * pr.y;
+    idx[0] = pr.x;
+    idx[1] = e[0];
+    idx[2] = e[1];
+}
+__device__ __forceinline__ void pair_indices_ee(const Scene &s, uint2 pr, unsigned (&idx)[4]) {
+    const unsigned *a = s.edge + 2 * pr.x;
+    const unsigned *c = s.edge + 2 * pr.y;
+    idx[0] = a[0];
+    idx[1] = a[1];
+    idx[2] = c[0];
+    idx[3] = c[1];
+}
+
+__global__ void k_dyn_insert(Scene s, PairLists pl, unsigned n_pf, unsigned n_pe,
+                             unsigned n_pp, unsigned n_ee, DynMatrix dm, IterStatus *st) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n_pf) {
+        unsigned idx[4];
+        pair_indices_pf(s, pl.pf[t], idx);
+        insert_pair_keys<4>(s, dm, idx, st);
+        return;
+    }
+    t -= n_pf;
+    if (t < n_pe) {
+        unsigned idx[3];
+        pair_indices_pe(s, pl.pe[t], idx);
+        insert_pair_keys<3>(s, dm, idx, st);
+        return;
+    }
+    t -= n_pe;
+    if (t < n_pp) {
+        unsigned idx[2] = {pl.pp[t].x, pl.pp[t].y};
+        insert_pair_keys<2>(s, dm, idx, st);
+        return;
+    }
+    t -= n_pp;
+    if (t < n_ee) {
+        unsigned idx[4];
+        pair_indices_ee(s, pl.ee[t], idx);
+        insert_pair_keys<4>(s, dm, idx, st);
+    }
+}
+
+__global__ void k_dyn_count(DynMatrix dm) {
+    unsigned h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= dm.hcap) return;
+    unsigned long long k = dm.hkey[h];
+    if (k == kEmptyKey) return;
+    atomicAdd(&dm.cnt[(unsigned)(k >> 32)], 1u);
+    atomicAdd(&dm.cnt2[(unsigned)k], 1u);
+}
+
+__global__ void k_dyn_fill(DynMatrix dm) {
+    unsigned h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= dm.hcap) return;
+    unsigned long long k = dm.hkey[h];
+    if (k == kEmptyKey) return;
+    unsigned r = (unsigned)(k >> 32), c = (unsigned)k;
+    unsigned pos = dm.off[r] + atomicAdd(&dm.cnt[r], 1u);
+    dm.col[pos] = c;
+    dm.hval[h] = pos;
+    unsigned tpos = dm.tr_off[c] + atomicAdd(&dm.cnt2[c], 1u);
+    dm.tr[tpos] = make_uint2(r, pos);
+}
+
+// ---- contact pair assembly (contact.cu:262-354, stage 1) ---------------------
+template <int N>
+__device__ void scatter_pair(const Scene &s, const AssemblyBuffers &b, const DynMatrix &dm,
+                             const unsigned (&idx)[N], const Mat<3, N> &f,
+                             const Mat<3 * N, 3 * N> &H, IterStatus *st) {
+#pragma unroll
+    for (int a = 0; a < N; ++a) atomic_add3(b.force + 3 * idx[a], f.col(a));
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int c = 0; c < N; ++c) {
+            unsigned i = idx[a], j = idx[c];
+            if (i > j) continue;
+            Mat3 blk = H.template block<3, 3>(3 * a, 3 * c);
+            unsigned sl = fixed_slot(s, i, j);
+            if (sl != kSentinel) {
+                atomic_add_block(b.fixed_val + 9 * (size_t)sl, blk);
+            } else {
+                unsigned pos = hash_find(dm, ((unsigned long long)i << 32) | j);
+                if (pos == kSentinel) {
+                    atomicOr(&st->status, STATUS_BAD_SLOT);
+                } else {
+                    atomic_add_block(dm.val + 9 * (size_t)pos, blk);
+                }
+            }
+        }
+}
+
+template <int N>
+__device__ void assemble_pair(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+                              const DynMatrix &dm, const unsigned (&idx)[N],
+                              const float (&w)[N], float ghat, float offset, float mu,
+                              bool friction_on, float count) {
+    Vec3 x[N], x0[N];
+    float mass[N];
+    Mat<3 * N, 3 * N> local;
+#pragma unroll
+    for (int a = 0; a < N; ++a) {
+        x[a] = X(b.x, idx[a]);
+        x0[a] = X(b.x0, idx[a]);
+        mass[a] = s.vprop[idx[a]].mass;
+    }
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int c = 0; c < N; ++c)
+            local.template set_block<3, 3>(3 * a, 3 * c, fixed_block(s, b.fixed_tmp, idx[a], idx[c]));
+    Mat<3, N> f;
+    Mat<3 * N, 3 * N> H;
+    contact::pair_force_hessian<N>(x, x0, w, mass, local, ghat, offset, p.barrier,
+                                   friction_on, mu, p.friction_eps, count, f, H);
+    scatter_pair<N>(s, b, dm, idx, f, H, b.st);
+}
+
+__global__ void k_assemble_pf(Scene s, StepParams p, AssemblyBuffers b, PairLists pl,
+                              unsigned n, DynMatrix dm) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    uint2 pr = pl.pf[t];
+    unsigned idx[4];
+    pair_indices_pf(s, pr, idx);
+    Vec3 c = dist::point_triangle_coeff(X(b.x, idx[0]), X(b.x, idx[1]), X(b.x, idx[2]),
+                                        X(b.x, idx[3]));
+    float w[4] = {1.0f, -c[0], -c[1], -c[2]};
+    const PpfVertexParam &vp = s.vparam[s.vprop[pr.x].param_index];
+    const PpfFaceParam &fp = s.fparam[s.fprop[pr.y].param_index];
+    float offset = vp.offset + fp.offset;
+    float ghat = 0.5f * (vp.ghat + fp.ghat);
+    float mu = contact::combine_friction(vp.friction, fp.friction, p.friction_mode);
+    assemble_pair<4>(s, p, b, dm, idx, w, ghat, offset, mu, true, 1.0f);
+}
+
+__global__ void k_assemble_pe(Scene s, StepParams p, AssemblyBuffers b, PairLists pl,
+                              unsigned n, DynMatrix dm) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    uint3 pr = pl.pe[t];
+    unsigned idx[3];
+    pair_indices_pe(s, pr, idx);
+    Vec2 c = dist::point_edge_coeff(X(b.x, idx[0]), X(b.x, idx[1]), X(b.x, idx[2]));
+    float w[3] = {1.0f, -c[0], -c[1]};
+    const PpfVertexParam &vp = s.vparam[s.vprop[pr.x].param_index];
+    const PpfEdgeParam &ep = s.eparam[s.eprop[pr.y].param_index];
+    float offset = vp.offset + ep.offset;
+    float ghat = 0.5f * (vp.ghat + ep.ghat);
+    float mu = contact::combine_friction(vp.friction, ep.friction, p.friction_mode);
+    bool fr = (pr.z & 0x80000000u) != 0u;
+    float count = (float)(pr.z & 0x7fffffffu);
+    assemble_pair<3>(s, p, b, dm, idx, w, ghat, offset, mu, fr, count);
+}
+
+__global__ void k_assemble_pp(Scene s, StepParams p, AssemblyBuffers b, PairLists pl,
+                              unsigned n, DynMatrix dm) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    uint3 pr = pl.pp[t];
+    unsigned idx[2] = {pr.x, pr.y};
+    float w[2] = {1.0f, -1.0f};
+    const PpfVertexParam &a = s.vparam[s.vprop[pr.x].param_index];
+    const PpfVertexParam &c = s.vparam[s.vprop[pr.y].param_index];
+    float offset = a.offset + c.offset;
+    float ghat = 0.5f * (a.ghat + c.ghat);
+    float mu = contact::combine_friction(a.friction, c.friction, p.friction_mode);
+    bool fr = (pr.z & 0x80000000u) != 0u;
+    float count = (float)(pr.z & 0x7fffffffu);
+    assemble_pair<2>(s, p, b, dm, idx, w, ghat, offset, mu, fr, count);
+}
+
+__global__ void k_assemble_ee(Scene s, StepParams p, AssemblyBuffers b, PairLists pl,
+                              unsigned n, DynMatrix dm) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    uint2 pr = pl.ee[t];
+    unsigned idx[4];
+    pair_indices_ee(s, pr, idx);
+    Vec4 c = dist::edge_edge_coeff(X(b.x, idx[0]), X(b.x, idx[1]), X(b.x, idx[2]),
+                                   X(b.x, idx[3]));
+    float w[4] = {c[0], c[1], -c[2], -c[3]};
+    const PpfEdgeParam &pa = s.eparam[s.eprop[pr.x].param_index];
+    const PpfEdgeParam &pb = s.eparam[s.eprop[pr.y].param_index];
+    float offset = pa.offset + pb.offset;
+    float ghat = 0.5f * (pa.ghat + pb.ghat);
+    float mu = contact::combine_friction(pa.friction, pb.friction, p.friction_mode);
+    assemble_pair<4>(s, p, b, dm, idx, w, ghat, offset, mu, true, 1.0f);
+}
+
+// ---- analytic sphere / floor (contact.cu:1154-1381) --------------------------
+__global__ void k_vertex_constraints(Scene s, StepParams p, AssemblyBuffers b) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n_surf) return;
+    const PpfVertexProp &vp = s.vprop[i];
+    if (vp.fix_index > 0 || !(vp.mass > 0.0f)) return;
+    if (s.nsphere == 0 && s.nfloor == 0) return;
+    Mat3 local = load_block(b.fixed_tmp + 9 * (size_t)s.fixed_diag[i]);
+    Vec3 f = Vec3::zero();
+    Mat3 H = Mat3::zero();
+    const float vfr = s.vparam[vp.param_index].friction;
+    const Vec3 x = X(b.x, i), xs = X(b.x0, i);
+    unsigned nc = 0;
+    for (unsigned k = 0; k < s.nsphere; ++k) {
+        const PpfSphere &q = s.sphere[k];
+        contact::SphereC sp{vec3(q.center.v[0], q.center.v[1], q.center.v[2]), q.ghat,
+                            q.friction, q.radius, q.thickness, q.bowl, q.reverse,
+                            q.kinematic};
+        nc += contact::sphere_constraint(x, xs, vp.mass, vfr, local, sp, p.friction_mode,
+                                         p.friction_eps, f, H);
+    }
+    for (unsigned k = 0; k < s.nfloor; ++k) {
+        const PpfFloor &q = s.floor[k];
+        contact::FloorC fl{vec3(q.ground.v[0], q.ground.v[1], q.ground.v[2]), q.ghat,
+                           q.friction, q.thickness, vec3(q.up.v[0], q.up.v[1], q.up.v[2]),
+                           q.kinematic};
+        nc += contact::floor_constraint(x, xs, vp.mass, vfr, local, fl, p.friction_mode,
+                                        p.friction_eps, p.constraint_tol, f, H);
+    }
+    if (nc == 0) return;
+    atomic_add3(b.force + 3 * i, f);
+    atomic_add_block(b.fixed_val + 9 * (size_t)s.fixed_diag[i], H);
+    atomicAdd(&b.st->n_contact, nc);
+}
+
+// ---- Dirichlet elimination of pinned vertices (main.cu:954-1049) -------------
+__device__ __forceinline__ void lift_sub(float *force, unsigned row, const Mat3 &blk,
+                                         const Vec3 &pv, bool transposed) {
+    Vec3 c;
+    if (transposed) {
+        c[0] = blk(0, 0) * pv[0] + blk(1, 0) * pv[1] + blk(2, 0) * pv[2];
+        c[1] = blk(0, 1) * pv[0] + blk(1, 1) * pv[1] + blk(2, 1) * pv[2];
+        c[2] = blk(0, 2) * pv[0] + blk(1, 2) * pv[1] + blk(2, 2) * pv[2];
+    } else {
+        c[0] = blk(0, 0) * pv[0] + blk(0, 1) * pv[1] + blk(0, 2) * pv[2];
+        c[1] = blk(1, 0) * pv[0] + blk(1, 1) * pv[1] + blk(1, 2) * pv[2];
+        c[2] = blk(2, 0) * pv[0] + blk(2, 1) * pv[1] + blk(2, 2) * pv[2];
+    }
+    atomicAdd(force + 3 * row + 0, -c[0]);
+    atomicAdd(force + 3 * row + 1, -c[1]);
+    atomicAdd(force + 3 * row + 2, -c[2]);
+}
+
+__device__ __forceinline__ void eliminate_row(const Scene &s, const AssemblyBuffers &b,
+                                              unsigned i, unsigned k0, unsigned k1,
+                                              const unsigned *col, float *val) {
+    const bool mi = s.dof_mask[i] != 0u;
+    for (unsigned k = k0; k < k1; ++k) {
+        unsigned j = col[k];
+        const bool mj = s.dof_mask[j] != 0u;
+        float *blkp = val + 9 * (size_t)k;
+        if (mi != mj) {
+            Mat3 blk = load_block(blkp);
+            if (mj) lift_sub(b.force, i, blk, X(b.x, j) - X(b.target, j), false);
+            else lift_sub(b.force, j, blk, X(b.x, i) - X(b.target, i), true);
+        }
+        if (mi || mj)
+            for (int q = 0; q < 9; ++q) blkp[q] = 0.0f;
+    }
+}
+
+__global__ void k_dirichlet_lift(Scene s, AssemblyBuffers b, DynMatrix dm) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) return;
+    eliminate_row(s, b, i, dm.off[i], dm.off[i + 1], dm.col, dm.val);
+    eliminate_row(s, b, i, s.fixed_off[i], s.fixed_off[i + 1], s.fixed_col, b.fixed_val);
+}
+
+__global__ void k_dirichlet_rows(Scene s, AssemblyBuffers b) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n || s.dof_mask[i] == 0u) return;
+    float *d = b.diag + 9 * i;
+    for (int q = 0; q < 9; ++q) d[q] = (q % 4 == 0) ? 1.0f : 0.0f;
+    Vec3 pv = X(b.x, i) - X(b.target, i);
+    store3(b.force + 3 * i, pv);
+}
+
+// ---- exclusive scan ----------------------------------------------------------
+constexpr unsigned kScanBlock = 1024;
+
+__global__ void k_scan_blocks(const unsigned *in, unsigned *out, unsigned n,
+                              unsigned *block_sums) {
+    __shared__ unsigned s_warp[32];
+    unsigned i = blockIdx.x * kScanBlock + threadIdx.x;
+    unsigned v = i < n ? in[i] : 0u;
+    unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    unsigned x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+        unsigned y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= (unsigned)off) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = s_warp[lane];
+        for (int off = 1; off < 32; off <<= 1) {
+            unsigned y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= (unsigned)off) w += y;
+        }
+        s_warp[lane] = w;
+    }
+    __syncthreads();
+    unsigned incl = x + (warp ? s_warp[warp - 1] : 0u);
+    if (i < n) out[i] = incl - v;
+    if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = incl;
+}
+
+__global__ void k_scan_add(unsigned *out, unsigned n, const unsigned *block_offsets) {
+    unsigned i = blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < n && blockIdx.x > 0) out[i] += block_offsets[blockIdx.x];
+}
+
+__global__ void k_scan_total(const unsigned *in, unsigned *out, unsigned n) {
+    out[n] = (n ? out[n - 1] + in[n - 1] : 0u);
+}
+
+} // namespace
+
+size_t scan_tmp_size(unsigned n) {
+    // per level: block sums + their scanned offsets (+1), then the next level
+    size_t total = 0;
+    unsigned m = n;
+    do {
+        unsigned b = div_up(m < 1u ? 1u : m, kScanBlock);
+        total += 2 * (size_t)b + 1;
+        m = b;
+    } while (m > 1);
+    return total + 2;
+}
+
+static void scan_rec(const unsigned *in, unsigned *out, unsigned n, unsigned *tmp,
+                     cudaStream_t q) {
+    unsigned blocks = div_up(n, kScanBlock);
+    unsigned *sums = tmp;
+    unsigned *offs = tmp + blocks;
+    k_scan_blocks<<<blocks, kScanBlock, 0, q>>>(in, out, n, sums);
+    PPF_LAUNCH_CHECK();
+    if (blocks > 1) {
+        scan_rec(sums, offs, blocks, offs + blocks + 1, q);
+        k_scan_add<<<blocks, kScanBlock, 0, q>>>(out, n, offs);
+        PPF_LAUNCH_CHECK();
+    }
+}
+
+void exclusive_scan(const unsigned *in, unsigned *out, unsigned n, unsigned *tmp,
+                    cudaStream_t q) {
+    if (n > 0) scan_rec(in, out, n, tmp, q);
+    k_scan_total<<<1, 1, 0, q>>>(in, out, n);
+    PPF_LAUNCH_CHECK();
+}
+
+void launch_vertex_energy(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+                          cudaStream_t q) {
+    if (!s.n) return;
+    k_vertex_energy<<<div_up(s.n, kB), kB, 0, q>>>(s, p, b);
+    PPF_LAUNCH_CHECK();
+}
+
+void launch_elastic(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+                    cudaStream_t q) {
+    (void)p;
+    if (s.nf) {
+        k_face_energy<<<div_up(s.nf, kB), kB, 0, q>>>(s, b);
+        PPF_LAUNCH_CHECK();
+    }
+    if (s.nh) {
+        k_hinge_energy<<<div_up(s.nh, kB), kB, 0, q>>>(s, b);
+        PPF_LAUNCH_CHECK();
+    }
+}
+
+void launch_strain_limit(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+                         cudaStream_t q) {
+    if (!s.nf) return;
+    k_strain_limit<<<div_up(s.nf, kB), kB, 0, q>>>(s, p, b);
+    PPF_LAUNCH_CHECK();
+}
+
+void launch_detect(const Scene &s, const BvhView &fb, const BvhView &eb,
+                   const BvhView &vb, const AssemblyBuffers &b, PairLists &pl,
+                   cudaStream_t q) {
+    if (s.n_surf) {
+        k_detect_vertex<<<div_up(s.n_surf, 128u), 128, 0, q>>>(s, fb, eb, vb, b.x, pl, b.st);
+        PPF_LAUNCH_CHECK();
+    }
+    if (s.ne) {
+        k_detect_edge<<<div_up(s.ne, 128u), 128, 0, q>>>(s, eb, b.x, pl, b.st);
+        PPF_LAUNCH_CHECK();
+    }
+}
+
+void launch_dyn_build(const Scene &s, const AssemblyBuffers &b, const PairLists &pl,
+                      const unsigned counts[4], DynMatrix &dm, unsigned n_dyn_max,
+                      unsigned *d_scan_tmp, cudaStream_t q) {
+    (void)n_dyn_max;
+    PPF_CUDA(cudaMemsetAsync(dm.hkey, 0xff, (size_t)dm.hcap * sizeof(unsigned long long), q));
+    PPF_CUDA(cudaMemsetAsync(dm.cnt, 0, s.n * sizeof(unsigned), q));
+    PPF_CUDA(cudaMemsetAsync(dm.cnt2, 0, s.n * sizeof(unsigned), q));
+    unsigned total = counts[0] + counts[1] + counts[2] + counts[3];
+    if (total) {
+        k_dyn_insert<<<div_up(total, kB), kB, 0, q>>>(s, pl, counts[0], counts[1], counts[2],
+                                                      counts[3], dm, b.st);
+        PPF_LAUNCH_CHECK();
+    }
+    k_dyn_count<<<div_up(dm.hcap, kB), kB, 0, q>>>(dm);
+    PPF_LAUNCH_CHECK();
+    exclusive_scan(dm.cnt, dm.off, s.n, d_scan_tmp, q);
+    exclusive_scan(dm.cnt2, dm.tr_off, s.n, d_scan_tmp, q);
+    PPF_CUDA(cudaMemsetAsync(dm.cnt, 0, s.n * sizeof(unsigned), q));
+    PPF_CUDA(cudaMemsetAsync(dm.cnt2, 0, s.n * sizeof(unsigned), q));
+    k_dyn_fill<<<div_up(dm.hcap, kB), kB, 0, q>>>(dm);
+    PPF_LAUNCH_CHECK();
+}
+
+void launch_contact_assemble(const Scene &s, const StepParams &p,
+                             const AssemblyBuffers &b, const PairLists &pl,
+                             const unsigned counts[4], DynMatrix &dm, cudaStream_t q) {
+    if (counts[0]) {
+        k_assemble_pf<<<div_up(counts[0], 128u), 128, 0, q>>>(s, p, b, pl, counts[0], dm);
+        PPF_LAUNCH_CHECK();
+    }
+    if (counts[1]) {
+        k_assemble_pe<<<div_up(counts[1], 128u), 128, 0, q>>>(s, p, b, pl, counts[1], dm);
+        PPF_LAUNCH_CHECK();
+    }
+    if (counts[2]) {
+        k_assemble_pp<<<div_up(counts[2], 128u), 128, 0, q>>>(s, p, b, pl, counts[2], dm);
+        PPF_LAUNCH_CHECK();
+    }
+    if (counts[3]) {
+        k_assemble_ee<<<div_up(counts[3], 128u), 128, 0, q>>>(s, p, b, pl, counts[3], dm);
+        PPF_LAUNCH_CHECK();
+    }
+}
+
+void launch_vertex_constraints(const Scene &s, const StepParams &p,
+                               const AssemblyBuffers &b, cudaStream_t q) {
+    if (!s.n_surf || (s.nsphere == 0 && s.nfloor == 0)) return;
+    k_vertex_constraints<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, p, b);
+    PPF_LAUNCH_CHECK();
+}
+
+void launch_dirichlet(const Scene &s, const AssemblyBuffers &b, const DynMatrix &dm,
+                      float *dx, cudaStream_t q) {
+    (void)dx;
+    if (s.nfix == 0) return;
+    k_dirichlet_lift<<<div_up(s.n, kB), kB, 0, q>>>(s, b, dm);
+    PPF_LAUNCH_CHECK();
+    k_dirichlet_rows<<<div_up(s.n, kB), kB, 0, q>>>(s, b);
+    PPF_LAUNCH_CHECK();
+}
+
+} // namespace gpu
+} // namespace ppf

@@ -1,0 +1,116 @@
+// scene.cuh -- device-resident scene, per-step state and kernel entry points.
+//
+// Layout in HBM (one scene):
+//   positions         float[3n] (curr, prev, eval_x, target), AoS like the ABI
+//   topology          face u32[3F], edge u32[2E], hinge u32[4H] (hinge kept in
+//                     its DataSet order; kernels remap (h2, h1, h0, h3))
+//   props / params    the ABI structs, copied verbatim
+//   fixed Hessian     upper-triangle 3x3 BSR on the builder's pattern: row
+//                     offsets u32[n+1], columns u32[B_u], values float[9 B_u]
+//                     (column-major blocks), plus the transpose table
+//                     (row, slot) per lower entry for the symmetric SpMV
+//   contact Hessian   upper-triangle blocks outside the fixed pattern, deduped
+//                     per Newton iteration through a hash table, laid out as a
+//                     CSR (offsets, columns, values) and a transpose table
+//   diag              float[9n] (inertia, air, pull blocks)
+//   vectors           force, dx, PCG work vectors: float[3n] each
+#pragma once
+
+#include "../../../include/ppf_gb300.h"
+#include "common.cuh"
+#include "lbvh.cuh"
+
+namespace ppf {
+namespace gpu {
+
+constexpr unsigned kSentinel = 0xFFFFFFFFu;
+
+struct BvhView {
+    const uint2 *node;
+    const float4 *bmin;
+    const float4 *bmax;
+    unsigned root;
+    unsigned n;
+};
+
+struct CsrView {
+    const unsigned *offset;
+    const unsigned *col;
+    float *val; // 9 per block
+    const unsigned *tr_offset;
+    const uint2 *tr; // (row, block index)
+};
+
+// Everything a kernel needs to read the scene (device pointers, by value).
+struct Scene {
+    unsigned n, n_surf, nf, ne, nh;
+    const unsigned *face;
+    const unsigned *edge;
+    const unsigned *hinge;
+    const PpfVertexProp *vprop;
+    const PpfEdgeProp *eprop;
+    const PpfFaceProp *fprop;
+    const PpfHingeProp *hprop;
+    const PpfVertexParam *vparam;
+    const PpfEdgeParam *eparam;
+    const PpfFaceParam *fparam;
+    const PpfHingeParam *hparam;
+    const float *inv_rest; // 4 per face, column-major
+    const unsigned *vf_off, *vf; // vertex -> faces
+    const unsigned *ve_off, *ve; // vertex -> edges
+    const unsigned *ef_off, *ef; // edge -> faces
+    const unsigned *fixed_off, *fixed_col;
+    const unsigned *fixed_tr_off;
+    const uint2 *fixed_tr;
+    const unsigned *fixed_diag; // slot of (i, i)
+    const unsigned *face_slot;  // 9 per face
+    const unsigned *hinge_slot; // 16 per hinge, remapped order
+    const unsigned *dof_mask;   // 1 = Dirichlet vertex
+    const PpfFixPair *fix;
+    unsigned nfix;
+    const PpfPullPair *pull;
+    unsigned npull;
+    const PpfSphere *sphere;
+    unsigned nsphere;
+    const PpfFloor *floor;
+    unsigned nfloor;
+    const float *margin_face, *margin_edge, *margin_vert;
+    // collision-window activity (null when every element is active)
+    const unsigned char *vert_active, *edge_active;
+};
+
+struct StepParams {
+    float dt, prev_dt;
+    float time;
+    float air_friction, air_density, isotropic_air_friction;
+    float friction_eps, eiganalysis_eps, constraint_tol;
+    float line_search_max_t, ccd_eps;
+    float gravity[3], wind[3];
+    int barrier, friction_mode;
+    int inactive_momentum;
+    float fix_xz;
+};
+
+// Per-iteration scalars reduced on the device and read by the host once per
+// Newton iteration (one small D2H copy).
+struct IterStatus {
+    unsigned n_pf, n_pe, n_pp, n_ee;   // detected pairs (may exceed capacity)
+    unsigned n_dyn_keys, n_dyn;        // dynamic blocks: candidates, unique
+    unsigned status;                   // StatusBits
+    unsigned pin_infeasible;           // smallest pinned vertex index or ~0
+    unsigned overlap;                  // CCD "starts overlapping" flag
+    unsigned overlap_v0, overlap_v1, overlap_kind;
+    unsigned toi_bits;                 // min contact toi (float bits, >= 0)
+    unsigned toi_vf_bits;              // min vertex/face toi (seed for e-e)
+    unsigned sl_toi_bits;              // min strain-limit toi
+    unsigned max_dx_bits;              // max |dx_i|
+    unsigned n_contact;                // active contact + constraint count
+    unsigned n_isect;                  // intersection records found
+    unsigned pcg_iter;
+    float pcg_resid;
+    int pcg_state;                     // 0 converged, 1 truncated, 2 failed
+    float pcg_err0;
+};
+
+} // namespace gpu
+} // namespace ppf

@@ -1,0 +1,897 @@
+// solver.cu -- per-step Newton solve (crates/ppf-cts-solver/src/cpp/main/
+// main.cu:267-1649) on the device, driven from the host with two small
+// synchronizations per Newton iteration (contact-pair counts after detection,
+// the iteration's status block after the line search).
+#include "fatal.cuh"
+#include "solver.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+
+namespace ppf {
+namespace gpu {
+
+namespace {
+
+constexpr unsigned kB = 256;
+
+template <class T> void upload(DevBuf<T> &d, const T *h, size_t n) {
+    d.reserve(n ? n : 1);
+    if (n) PPF_CUDA(cudaMemcpy(d.data(), h, n * sizeof(T), cudaMemcpyHostToDevice));
+}
+template <class T> void upload(DevBuf<T> &d, const std::vector<T> &h) {
+    upload(d, h.data(), h.size());
+}
+
+// target = x + (x - x_prev) dt / dt_prev + dt^2 g; pinned: the pin's position
+// (main.cu:491-511).
+__global__ void k_compute_target(unsigned n, const float *curr, const float *prev,
+                                 const PpfVertexProp *vprop, const PpfFixPair *fix,
+                                 float *target, float dt, float prev_dt, float gx, float gy,
+                                 float gz, int inactive) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (vprop[i].fix_index > 0) {
+        const PpfFixPair &f = fix[vprop[i].fix_index - 1];
+        for (int d = 0; d < 3; ++d) target[3 * i + d] = f.position.v[d];
+        return;
+    }
+    float tr = dt / prev_dt, h2 = dt * dt;
+    const float g[3] = {gx, gy, gz};
+    for (int d = 0; d < 3; ++d) {
+        float x1 = curr[3 * i + d], x0 = prev[3 * i + d];
+        float y = (x1 - x0) * tr + h2 * g[d];
+        target[3 * i + d] = inactive ? x1 : x1 + y;
+    }
+}
+
+__global__ void k_rewind_fix(unsigned nfix, PpfFixPair *fix, float back) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nfix) return;
+    PpfFixPair &f = fix[i];
+    if (f.kinematic)
+        for (int d = 0; d < 3; ++d) f.position.v[d] = f.position.v[d] - back * f.step_delta.v[d];
+}
+
+__global__ void k_seed_dx(unsigned n, const PpfVertexProp *vprop, const float *x,
+                          const float *target, float *dx) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (vprop[i].fix_index > 0)
+        for (int d = 0; d < 3; ++d) dx[3 * i + d] = x[3 * i + d] - target[3 * i + d];
+}
+
+__global__ void k_fold_diag(unsigned n, const unsigned *diag_slot, const float *diag,
+                            float *fixed_val) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float *d = fixed_val + 9 * (size_t)diag_slot[i];
+    for (int k = 0; k < 9; ++k) d[k] += diag[9 * i + k];
+}
+
+__global__ void k_max_dx(unsigned n, const float *dx, IterStatus *st) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    float m = 0.0f;
+    if (i < n) {
+        float a = dx[3 * i], b = dx[3 * i + 1], c = dx[3 * i + 2];
+        m = sqrtf(a * a + b * b + c * c);
+    }
+    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31u) == 0 && m > 0.0f) atomicMax(&st->max_dx_bits, __float_as_uint(m));
+}
+
+// target <- eval_x; eval_x -= min(1, max_dx / |dx|_max) dx (main.cu:1142-1188)
+__global__ void k_apply_dx(unsigned n, float *x, float *target, const float *dx,
+                           const IterStatus *st, float max_dx_param, float *rescale_out) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    float mdx = __uint_as_float(st->max_dx_bits);
+    float rescale = fminf(1.0f, max_dx_param / mdx);
+    if (i == 0) *rescale_out = rescale;
+    if (i >= n) return;
+    for (int d = 0; d < 3; ++d) {
+        float v = x[3 * i + d];
+        target[3 * i + d] = v;
+        x[3 * i + d] = v - rescale * dx[3 * i + d];
+    }
+}
+
+__global__ void k_apply_toi(unsigned n, float *x, const float *target, float toi) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int d = 0; d < 3; ++d) {
+        float t = target[3 * i + d];
+        float dd = toi * (x[3 * i + d] - t);
+        x[3 * i + d] = t + dd;
+    }
+}
+
+__global__ void k_init_ls(IterStatus *st, float max_t, PcgResult *res) {
+    st->toi_bits = __float_as_uint(max_t);
+    st->toi_vf_bits = __float_as_uint(max_t);
+    st->sl_toi_bits = __float_as_uint(max_t);
+    st->pin_infeasible = 0xFFFFFFFFu;
+    st->overlap = 0u;
+    st->overlap_v0 = 0xFFFFFFFFu;
+    st->overlap_v1 = 0xFFFFFFFFu;
+    st->overlap_kind = 0xFFFFFFFFu;
+    st->pcg_iter = res->iter;
+    st->pcg_resid = res->resid;
+    st->pcg_state = res->state;
+    st->pcg_err0 = res->err0;
+    st->status |= res->status;
+}
+
+__global__ void k_override_velocity(const unsigned *idx, unsigned count, const float *curr,
+                                    float *prev, float vx, float vy, float vz) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    unsigned v = idx[i];
+    prev[3 * v] = curr[3 * v] - vx;
+    prev[3 * v + 1] = curr[3 * v + 1] - vy;
+    prev[3 * v + 2] = curr[3 * v + 2] - vz;
+}
+
+__global__ void k_override_angular(const unsigned *idx, unsigned count, const float *curr,
+                                   float *prev, float wx, float wy, float wz, float cx,
+                                   float cy, float cz, float dt) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    unsigned v = idx[i];
+    float rx = curr[3 * v] - cx, ry = curr[3 * v + 1] - cy, rz = curr[3 * v + 2] - cz;
+    float ux = wy * rz - wz * ry, uy = wz * rx - wx * rz, uz = wx * ry - wy * rx;
+    prev[3 * v] = prev[3 * v] - ux * dt;
+    prev[3 * v + 1] = prev[3 * v + 1] - uy * dt;
+    prev[3 * v + 2] = prev[3 * v + 2] - uz * dt;
+}
+
+float bits_to_float(unsigned u) {
+    float f;
+    std::memcpy(&f, &u, sizeof(f));
+    return f;
+}
+
+unsigned next_pow2(unsigned long long v) {
+    unsigned long long p = 1024;
+    while (p < v) p <<= 1;
+    return (unsigned)p;
+}
+
+} // namespace
+
+Solver &solver_instance() {
+    static Solver s;
+    return s;
+}
+
+Scene Solver::scene() const {
+    Scene s{};
+    s.n = n_;
+    s.n_surf = n_surf_;
+    s.nf = nf_;
+    s.ne = ne_;
+    s.nh = nh_;
+    s.face = face_.data();
+    s.edge = edge_.data();
+    s.hinge = hinge_.data();
+    s.vprop = vprop_.data();
+    s.eprop = eprop_.data();
+    s.fprop = fprop_.data();
+    s.hprop = hprop_.data();
+    s.vparam = vparam_.data();
+    s.eparam = eparam_.data();
+    s.fparam = fparam_.data();
+    s.hparam = hparam_.data();
+    s.inv_rest = inv_rest_.data();
+    s.vf_off = vf_off_.data();
+    s.vf = vf_.data();
+    s.ve_off = ve_off_.data();
+    s.ve = ve_.data();
+    s.ef_off = ef_off_.data();
+    s.ef = ef_.data();
+    s.fixed_off = fixed_off_.data();
+    s.fixed_col = fixed_col_.data();
+    s.fixed_tr_off = fixed_tr_off_.data();
+    s.fixed_tr = fixed_tr_.data();
+    s.fixed_diag = fixed_diag_.data();
+    s.face_slot = face_slot_.data();
+    s.hinge_slot = hinge_slot_.data();
+    s.dof_mask = dof_mask_.data();
+    s.fix = fix_.data();
+    s.nfix = nfix_;
+    s.pull = pull_.data();
+    s.npull = npull_;
+    s.sphere = sphere_.data();
+    s.nsphere = nsphere_;
+    s.floor = floor_.data();
+    s.nfloor = nfloor_;
+    s.margin_face = margin_face_.data();
+    s.margin_edge = margin_edge_.data();
+    s.margin_vert = margin_vert_.data();
+    s.vert_active = use_active_ ? vert_active_.data() : nullptr;
+    s.edge_active = use_active_ ? edge_active_.data() : nullptr;
+    return s;
+}
+
+StepParams Solver::step_params(float dt) const {
+    StepParams p{};
+    p.dt = dt;
+    p.prev_dt = param->prev_dt;
+    p.time = (float)param->time;
+    p.air_friction = param->air_friction;
+    p.air_density = param->air_density;
+    p.isotropic_air_friction = param->isotropic_air_friction;
+    p.friction_eps = param->friction_eps;
+    p.eiganalysis_eps = param->eiganalysis_eps;
+    p.constraint_tol = param->constraint_tol;
+    p.line_search_max_t = param->line_search_max_t;
+    p.ccd_eps = param->ccd_eps;
+    for (int d = 0; d < 3; ++d) {
+        p.gravity[d] = param->gravity.v[d];
+        p.wind[d] = param->wind.v[d];
+    }
+    p.barrier = param->barrier;
+    p.friction_mode = param->friction_mode;
+    p.inactive_momentum = param->inactive_momentum ? 1 : 0;
+    p.fix_xz = param->fix_xz;
+    return p;
+}
+
+AssemblyBuffers Solver::abuf() {
+    AssemblyBuffers b{};
+    b.force = force_.data();
+    b.diag = diag_.data();
+    b.fixed_val = fixed_val_.data();
+    b.fixed_tmp = fixed_tmp_.data();
+    b.x = eval_x_.data();
+    b.x0 = curr_.data();
+    b.target = target_.data();
+    b.st = st_.data();
+    return b;
+}
+
+PcgOperator Solver::pcg_operator() const {
+    PcgOperator A{};
+    A.n = n_;
+    A.f_off = fixed_off_.data();
+    A.f_col = fixed_col_.data();
+    A.f_val = fixed_val_.data();
+    A.f_tr_off = fixed_tr_off_.data();
+    A.f_tr = fixed_tr_.data();
+    A.d_off = dyn_.off;
+    A.d_col = dyn_.col;
+    A.d_val = dyn_.val;
+    A.d_tr_off = dyn_.tr_off;
+    A.d_tr = dyn_.tr;
+    A.inv_diag = inv_diag_.data();
+    return A;
+}
+
+BvhView Solver::view(const Lbvh &b) const {
+    return BvhView{b.node.data(), b.bmin.data(), b.bmax.data(), b.root, b.n};
+}
+
+void Solver::upload_props() {
+    upload(vprop_, h_vprop_);
+    upload(fprop_, h_fprop_);
+    upload(eprop_, h_eprop_);
+    upload(hprop_, h_hprop_);
+    std::vector<unsigned> mask(n_, 0u);
+    for (unsigned i = 0; i < n_; ++i)
+        mask[i] = (h_vprop_[i].fix_index > 0 && h_vprop_[i].pdrd_body_index == 0) ? 1u : 0u;
+    upload(dof_mask_, mask);
+}
+
+bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
+    host = ds;
+    param = prm;
+    n_ = ds->vertex.curr.size;
+    n_surf_ = ds->surface_vert_count;
+    nf_ = ds->mesh.mesh.face.size;
+    ne_ = ds->mesh.mesh.edge.size;
+    nh_ = ds->mesh.mesh.hinge.size;
+    if (!q_) PPF_CUDA(cudaStreamCreateWithFlags(&q_, cudaStreamNonBlocking));
+    if (!ev0_) {
+        PPF_CUDA(cudaEventCreate(&ev0_));
+        PPF_CUDA(cudaEventCreate(&ev1_));
+        PPF_CUDA(cudaEventCreate(&evs0_));
+        PPF_CUDA(cudaEventCreate(&evs1_));
+    }
+    // topology
+    upload(face_, (const unsigned *)ds->mesh.mesh.face.data, 3 * (size_t)nf_);
+    upload(edge_, (const unsigned *)ds->mesh.mesh.edge.data, 2 * (size_t)ne_);
+    upload(hinge_, (const unsigned *)ds->mesh.mesh.hinge.data, 4 * (size_t)nh_);
+    h_vprop_.assign(ds->prop.vertex.data, ds->prop.vertex.data + ds->prop.vertex.size);
+    h_fprop_.assign(ds->prop.face.data, ds->prop.face.data + ds->prop.face.size);
+    h_eprop_.assign(ds->prop.edge.data, ds->prop.edge.data + ds->prop.edge.size);
+    h_hprop_.assign(ds->prop.hinge.data, ds->prop.hinge.data + ds->prop.hinge.size);
+    upload_props();
+    upload(vparam_, ds->param_arrays.vertex.data, ds->param_arrays.vertex.size);
+    upload(eparam_, ds->param_arrays.edge.data, ds->param_arrays.edge.size);
+    upload(fparam_, ds->param_arrays.face.data, ds->param_arrays.face.size);
+    upload(hparam_, ds->param_arrays.hinge.data, ds->param_arrays.hinge.size);
+    upload(inv_rest_, (const float *)ds->inv_rest2x2.data, 4 * (size_t)ds->inv_rest2x2.size);
+    auto up_vv = [&](const PpfVecVecU32 &v, DevBuf<unsigned> &off, DevBuf<unsigned> &dat,
+                     unsigned rows) {
+        std::vector<unsigned> o(rows + 1, 0u);
+        if (v.size && v.offset)
+            for (unsigned i = 0; i <= rows && i <= v.size; ++i) o[i] = v.offset[i];
+        for (unsigned i = v.size + 1; i <= rows; ++i) o[i] = o[v.size];
+        upload(off, o);
+        upload(dat, v.data, v.nnz);
+    };
+    up_vv(ds->mesh.neighbor.vertex.face, vf_off_, vf_, n_);
+    up_vv(ds->mesh.neighbor.vertex.edge, ve_off_, ve_, n_);
+    up_vv(ds->mesh.neighbor.edge.face, ef_off_, ef_, ne_);
+    // fixed pattern (builder.rs:1244-1356), diagonal slots, element slots
+    const PpfVecVecU32 &ft = ds->fixed_index_table;
+    std::vector<unsigned> foff(ft.offset, ft.offset + n_ + 1);
+    std::vector<unsigned> fcol(ft.data, ft.data + foff[n_]);
+    nnz_fixed_ = foff[n_];
+    upload(fixed_off_, foff);
+    upload(fixed_col_, fcol);
+    const PpfVecVecVec2u &tt = ds->transpose_table;
+    std::vector<unsigned> toff(tt.offset, tt.offset + n_ + 1);
+    std::vector<uint2> tr(toff[n_]);
+    for (unsigned k = 0; k < toff[n_]; ++k) tr[k] = make_uint2(tt.data[k].v[0], tt.data[k].v[1]);
+    upload(fixed_tr_off_, toff);
+    upload(fixed_tr_, tr);
+    auto slot_of = [&](unsigned i, unsigned j) -> unsigned {
+        if (i > j) return kSentinel;
+        auto b = fcol.begin() + foff[i], e = fcol.begin() + foff[i + 1];
+        auto it = std::lower_bound(b, e, j);
+        if (it == e || *it != j) return kSentinel;
+        return (unsigned)(it - fcol.begin());
+    };
+    std::vector<unsigned> dslot(n_);
+    for (unsigned i = 0; i < n_; ++i) {
+        dslot[i] = slot_of(i, i);
+        if (dslot[i] == kSentinel) throw FatalError(4, "fixed pattern lacks a diagonal block");
+    }
+    upload(fixed_diag_, dslot);
+    std::vector<unsigned> fs(9 * (size_t)nf_), hs(16 * (size_t)nh_);
+    const unsigned *F = (const unsigned *)ds->mesh.mesh.face.data;
+    for (unsigned f = 0; f < nf_; ++f)
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) fs[9 * f + 3 * a + b] = slot_of(F[3 * f + a], F[3 * f + b]);
+    const unsigned *Hh = (const unsigned *)ds->mesh.mesh.hinge.data;
+    for (unsigned h = 0; h < nh_; ++h) {
+        const unsigned r[4] = {Hh[4 * h + 2], Hh[4 * h + 1], Hh[4 * h], Hh[4 * h + 3]};
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) hs[16 * h + 4 * a + b] = slot_of(r[a], r[b]);
+    }
+    upload(face_slot_, fs);
+    upload(hinge_slot_, hs);
+    // per-primitive margins 0.5 ghat + offset
+    std::vector<float> mf(nf_), me(ne_), mv(n_);
+    for (unsigned i = 0; i < nf_; ++i) {
+        const PpfFaceParam &p = ds->param_arrays.face.data[h_fprop_[i].param_index];
+        mf[i] = 0.5f * p.ghat + p.offset;
+    }
+    for (unsigned i = 0; i < ne_; ++i) {
+        const PpfEdgeParam &p = ds->param_arrays.edge.data[h_eprop_[i].param_index];
+        me[i] = 0.5f * p.ghat + p.offset;
+    }
+    for (unsigned i = 0; i < n_; ++i) {
+        const PpfVertexParam &p = ds->param_arrays.vertex.data[h_vprop_[i].param_index];
+        mv[i] = 0.5f * p.ghat + p.offset;
+    }
+    upload(margin_face_, mf);
+    upload(margin_edge_, me);
+    upload(margin_vert_, mv);
+    // constraints
+    update_constraint(&ds->constraint);
+    // state
+    upload(curr_, (const float *)ds->vertex.curr.data, 3 * (size_t)n_);
+    upload(prev_, (const float *)ds->vertex.prev.data, 3 * (size_t)n_);
+    const size_t n3 = 3 * (size_t)n_;
+    eval_x_.reserve(n3);
+    target_.reserve(n3);
+    force_.reserve(n3);
+    dx_.reserve(n3);
+    r_.reserve(n3);
+    diag_.reserve(9 * (size_t)n_);
+    inv_diag_.reserve(9 * (size_t)n_);
+    fixed_val_.reserve(9 * (size_t)nnz_fixed_);
+    fixed_tmp_.reserve(9 * (size_t)nnz_fixed_);
+    st_.reserve(1);
+    rescale_.reserve(1);
+    isect_.reserve(PPF_MAX_INTERSECTION_RECORDS);
+    if (!st_host_) PPF_CUDA(cudaMallocHost(&st_host_, sizeof(IterStatus)));
+    // pair lists and contact-block buffers start at a size proportional to the
+    // mesh and grow on demand
+    unsigned cap0 = std::max(1u << 14, 2 * std::max(n_, ne_));
+    pf_buf_.reserve(cap0);
+    pe_buf_.reserve(cap0);
+    pp_buf_.reserve(cap0);
+    ee_buf_.reserve(cap0);
+    pairs_.pf = pf_buf_.data();
+    pairs_.pe = pe_buf_.data();
+    pairs_.pp = pp_buf_.data();
+    pairs_.ee = ee_buf_.data();
+    pairs_.cap_pf = pairs_.cap_pe = pairs_.cap_pp = pairs_.cap_ee = cap0;
+    doff_buf_.reserve(n_ + 1);
+    dtroff_buf_.reserve(n_ + 1);
+    dcnt_buf_.reserve(n_ + 1);
+    dcnt2_buf_.reserve(n_ + 1);
+    scan_tmp_.reserve(scan_tmp_size(n_ + 1));
+    pcg_.reserve(n_);
+    initialized_ = true;
+    // initial trees and intersection check on prev and curr (main.cu:196-262)
+    if (!param->disable_contact) {
+        build_trees(curr_.data(), curr_.data(), 1.0f, true);
+        bool ok = check_intersection(prev_.data());
+        build_trees(curr_.data(), curr_.data(), 1.0f, false);
+        ok = ok && check_intersection(curr_.data());
+        if (!ok) {
+            set_fatal(1, "the scene is already self-intersecting at t=0; the solver "
+                         "advances from a separated configuration and cannot untangle one");
+            return false;
+        }
+    }
+    return true;
+}
+
+void Solver::update_constraint(const PpfConstraint *c) {
+    nfix_ = c->fix.size;
+    npull_ = c->pull.size;
+    nsphere_ = c->sphere.size;
+    nfloor_ = c->floor.size;
+    upload(fix_, c->fix.data, nfix_);
+    upload(pull_, c->pull.data, npull_);
+    upload(sphere_, c->sphere.data, nsphere_);
+    upload(floor_, c->floor.data, nfloor_);
+    if (h_vprop_.empty()) return;
+    // rebuild fix/pull indices and element `fixed` flags (main.cu:2012-2077)
+    for (auto &v : h_vprop_) v.fix_index = v.pull_index = 0;
+    for (unsigned i = 0; i < nfix_; ++i) h_vprop_[c->fix.data[i].index].fix_index = i + 1;
+    for (unsigned i = 0; i < npull_; ++i) h_vprop_[c->pull.data[i].index].pull_index = i + 1;
+    auto fixed = [&](unsigned v) { return h_vprop_[v].fix_index > 0; };
+    const unsigned *F = (const unsigned *)host->mesh.mesh.face.data;
+    for (unsigned i = 0; i < nf_; ++i)
+        h_fprop_[i].fixed = fixed(F[3 * i]) && fixed(F[3 * i + 1]) && fixed(F[3 * i + 2]);
+    const unsigned *E = (const unsigned *)host->mesh.mesh.edge.data;
+    for (unsigned i = 0; i < ne_; ++i) h_eprop_[i].fixed = fixed(E[2 * i]) && fixed(E[2 * i + 1]);
+    const unsigned *H = (const unsigned *)host->mesh.mesh.hinge.data;
+    for (unsigned i = 0; i < nh_; ++i)
+        h_hprop_[i].fixed = fixed(H[4 * i]) && fixed(H[4 * i + 1]) && fixed(H[4 * i + 2]) &&
+                            fixed(H[4 * i + 3]);
+    upload_props();
+    // mirror into the host DataSet props, as the reference does
+    std::memcpy(host->prop.vertex.data, h_vprop_.data(), n_ * sizeof(PpfVertexProp));
+    std::memcpy(host->prop.face.data, h_fprop_.data(), nf_ * sizeof(PpfFaceProp));
+    std::memcpy(host->prop.edge.data, h_eprop_.data(), ne_ * sizeof(PpfEdgeProp));
+    std::memcpy(host->prop.hinge.data, h_hprop_.data(), nh_ * sizeof(PpfHingeProp));
+}
+
+void Solver::update_rest_shape(const PpfRestShapeUpdate *u) {
+    if (u->inv_rest2x2.size)
+        PPF_CUDA(cudaMemcpy(inv_rest_.data(), u->inv_rest2x2.data,
+                            u->inv_rest2x2.size * sizeof(PpfMat2x2f), cudaMemcpyHostToDevice));
+    if (u->exclude_face.size) {
+        for (unsigned i = 0; i < u->exclude_face.size && i < nf_; ++i)
+            h_fprop_[i].rest_excluded = u->exclude_face.data[i] != 0;
+        upload(fprop_, h_fprop_);
+    }
+}
+
+void Solver::build_trees(const float *x0, const float *x1, float extrap, bool rebuild) {
+    PrimSet pf{PRIM_FACE, nf_, face_.data(), margin_face_.data(),
+               use_active_ ? face_active_.data() : nullptr};
+    PrimSet pe{PRIM_EDGE, ne_, edge_.data(), margin_edge_.data(),
+               use_active_ ? edge_active_.data() : nullptr};
+    PrimSet pv{PRIM_VERTEX, n_surf_, nullptr, margin_vert_.data(),
+               use_active_ ? vert_active_.data() : nullptr};
+    unsigned *status = &st_.data()->status;
+    if (rebuild) {
+        lbvh_build(bvh_face_, pf, x1, x0, x1, extrap, sort_ws_, status, q_);
+        lbvh_build(bvh_edge_, pe, x1, x0, x1, extrap, sort_ws_, status, q_);
+        lbvh_build(bvh_vert_, pv, x1, x0, x1, extrap, sort_ws_, status, q_);
+    } else {
+        lbvh_refit(bvh_face_, pf, x0, x1, extrap, status, q_);
+        lbvh_refit(bvh_edge_, pe, x0, x1, extrap, status, q_);
+        lbvh_refit(bvh_vert_, pv, x0, x1, extrap, status, q_);
+    }
+}
+
+void Solver::compute_target(float dt) {
+    k_compute_target<<<div_up(n_, kB), kB, 0, q_>>>(
+        n_, curr_.data(), prev_.data(), vprop_.data(), fix_.data(), target_.data(), dt,
+        param->prev_dt, param->gravity.v[0], param->gravity.v[1], param->gravity.v[2],
+        param->inactive_momentum ? 1 : 0);
+    PPF_LAUNCH_CHECK();
+}
+
+bool Solver::check_intersection(const float *x) {
+    PPF_CUDA(cudaMemsetAsync(&st_.data()->n_isect, 0, sizeof(unsigned), q_));
+    launch_intersection_check(scene(), view(bvh_face_), view(bvh_edge_), x, isect_.data(),
+                              st_.data(), q_);
+    unsigned cnt = 0;
+    PPF_CUDA(cudaMemcpyAsync(&cnt, &st_.data()->n_isect, sizeof(unsigned),
+                             cudaMemcpyDeviceToHost, q_));
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    isect_count_ = std::min(cnt, (unsigned)PPF_MAX_INTERSECTION_RECORDS);
+    isect_host_.resize(isect_count_);
+    if (isect_count_)
+        PPF_CUDA(cudaMemcpy(isect_host_.data(), isect_.data(),
+                            isect_count_ * sizeof(PpfIntersectionRecord), cudaMemcpyDeviceToHost));
+    return cnt == 0;
+}
+
+unsigned Solver::fetch_intersection_records(PpfIntersectionRecord *out, unsigned max_count) {
+    unsigned c = std::min(isect_count_, max_count);
+    if (c) std::memcpy(out, isect_host_.data(), c * sizeof(PpfIntersectionRecord));
+    return c;
+}
+
+void Solver::read_status() {
+    PPF_CUDA(cudaMemcpyAsync(st_host_, st_.data(), sizeof(IterStatus), cudaMemcpyDeviceToHost, q_));
+    PPF_CUDA(cudaStreamSynchronize(q_));
+}
+
+// Assembly of the Newton system at eval_x (main.cu:713-1049).
+void Solver::assemble(float dt) {
+    const Scene s = scene();
+    const StepParams p = step_params(dt);
+    const size_t n3 = 3 * (size_t)n_;
+    PPF_CUDA(cudaMemsetAsync(force_.data(), 0, n3 * sizeof(float), q_));
+    PPF_CUDA(cudaMemsetAsync(diag_.data(), 0, 9 * (size_t)n_ * sizeof(float), q_));
+    PPF_CUDA(cudaMemsetAsync(fixed_val_.data(), 0, 9 * (size_t)nnz_fixed_ * sizeof(float), q_));
+    PPF_CUDA(cudaMemsetAsync(dx_.data(), 0, n3 * sizeof(float), q_));
+    k_seed_dx<<<div_up(n_, kB), kB, 0, q_>>>(n_, vprop_.data(), eval_x_.data(), target_.data(),
+                                            dx_.data());
+    PPF_LAUNCH_CHECK();
+    AssemblyBuffers b = abuf();
+    launch_vertex_energy(s, p, b, q_);
+    launch_elastic(s, p, b, q_);
+    PPF_CUDA(cudaMemcpyAsync(fixed_tmp_.data(), fixed_val_.data(),
+                             9 * (size_t)nnz_fixed_ * sizeof(float), cudaMemcpyDeviceToDevice, q_));
+    launch_strain_limit(s, p, b, q_);
+    unsigned counts[4] = {0, 0, 0, 0};
+    if (!param->disable_contact) {
+        for (int attempt = 0; attempt < 3; ++attempt) {
+            PPF_CUDA(cudaMemsetAsync(st_.data(), 0, 4 * sizeof(unsigned), q_));
+            launch_detect(s, view(bvh_face_), view(bvh_edge_), view(bvh_vert_), b, pairs_, q_);
+            read_status();
+            counts[0] = st_host_->n_pf;
+            counts[1] = st_host_->n_pe;
+            counts[2] = st_host_->n_pp;
+            counts[3] = st_host_->n_ee;
+            bool grow = counts[0] > pairs_.cap_pf || counts[1] > pairs_.cap_pe ||
+                        counts[2] > pairs_.cap_pp || counts[3] > pairs_.cap_ee;
+            if (!grow) break;
+            auto grow_to = [](unsigned c) { return std::max(1u << 14, (unsigned)(2ull * c)); };
+            pf_buf_.reserve(grow_to(counts[0]));
+            pe_buf_.reserve(grow_to(counts[1]));
+            pp_buf_.reserve(grow_to(counts[2]));
+            ee_buf_.reserve(grow_to(counts[3]));
+            pairs_.pf = pf_buf_.data();
+            pairs_.pe = pe_buf_.data();
+            pairs_.pp = pp_buf_.data();
+            pairs_.ee = ee_buf_.data();
+            pairs_.cap_pf = (unsigned)pf_buf_.cap;
+            pairs_.cap_pe = (unsigned)pe_buf_.cap;
+            pairs_.cap_pp = (unsigned)pp_buf_.cap;
+            pairs_.cap_ee = (unsigned)ee_buf_.cap;
+            PPF_CUDA(cudaMemsetAsync(&st_.data()->n_contact, 0, sizeof(unsigned), q_));
+        }
+    }
+    // contact blocks outside the fixed pattern
+    unsigned long long keys = 6ull * counts[0] + 3ull * counts[1] + counts[2] + 6ull * counts[3];
+    unsigned hcap = next_pow2(2 * keys + 16);
+    hkey_buf_.reserve(hcap);
+    hval_buf_.reserve(hcap);
+    unsigned dcap = (unsigned)std::max<unsigned long long>(keys, 16ull);
+    dcol_buf_.reserve(dcap);
+    dtr_buf_.reserve(dcap);
+    dval_buf_.reserve(9 * (size_t)dcap);
+    dyn_.hkey = hkey_buf_.data();
+    dyn_.hval = hval_buf_.data();
+    dyn_.hcap = hcap;
+    dyn_.off = doff_buf_.data();
+    dyn_.col = dcol_buf_.data();
+    dyn_.val = dval_buf_.data();
+    dyn_.tr_off = dtroff_buf_.data();
+    dyn_.tr = dtr_buf_.data();
+    dyn_.cnt = dcnt_buf_.data();
+    dyn_.cnt2 = dcnt2_buf_.data();
+    dyn_.cap = dcap;
+    PPF_CUDA(cudaMemsetAsync(&st_.data()->n_dyn, 0, sizeof(unsigned), q_));
+    launch_dyn_build(s, b, pairs_, counts, dyn_, dcap, scan_tmp_.data(), q_);
+    PPF_CUDA(cudaMemsetAsync(dval_buf_.data(), 0, 9 * (size_t)dcap * sizeof(float), q_));
+    launch_contact_assemble(s, p, b, pairs_, counts, dyn_, q_);
+    launch_vertex_constraints(s, p, b, q_);
+    launch_dirichlet(s, b, dyn_, dx_.data(), q_);
+    k_fold_diag<<<div_up(n_, kB), kB, 0, q_>>>(n_, fixed_diag_.data(), diag_.data(),
+                                              fixed_val_.data());
+    PPF_LAUNCH_CHECK();
+}
+
+PpfStepResult Solver::advance() {
+    PpfStepResult result{};
+    result.ccd_success = result.pcg_success = result.intersection_free = true;
+    result.newton_progress = result.pin_feasible = result.contact_separated = true;
+    auto t_start = std::chrono::steady_clock::now();
+    stats_ = StepStats{};
+    const size_t n3 = 3 * (size_t)n_;
+    float dt = param->dt * param->playback;
+    const float max_t = param->line_search_max_t;
+    PPF_CUDA(cudaMemsetAsync(st_.data(), 0, sizeof(IterStatus), q_));
+    if (!param->disable_contact) build_trees(curr_.data(), curr_.data(), 1.0f, true);
+    compute_target(dt);
+    PPF_CUDA(cudaMemcpyAsync(eval_x_.data(), curr_.data(), n3 * sizeof(float),
+                             cudaMemcpyDeviceToDevice, q_));
+    double toi_advanced = 0.0;
+    unsigned step = 1;
+    bool final_step = false;
+    const Scene s = scene();
+    while (true) {
+        if (!final_step && param->max_newton_steps > 0 && step >= param->max_newton_steps) {
+            result.newton_progress = false;
+            return result;
+        }
+        if (final_step) {
+            if (toi_advanced < 1.0 && nfix_) {
+                k_rewind_fix<<<div_up(nfix_, kB), kB, 0, q_>>>(nfix_, fix_.data(),
+                                                               1.0f - (float)toi_advanced);
+                PPF_LAUNCH_CHECK();
+            }
+            dt *= (float)toi_advanced;
+            compute_target(dt);
+        }
+        PPF_CUDA(cudaMemsetAsync(st_.data(), 0, sizeof(IterStatus), q_));
+        assemble(dt);
+        // linear solve
+        PPF_CUDA(cudaMemcpyAsync(r_.data(), force_.data(), n3 * sizeof(float),
+                                 cudaMemcpyDeviceToDevice, q_));
+        PcgOperator A = pcg_operator();
+        launch_block_jacobi(A, fixed_diag_.data(), inv_diag_.data(), &st_.data()->status, q_);
+        PPF_CUDA(cudaEventRecord(ev0_, q_));
+        launch_pcg(A, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_);
+        PPF_CUDA(cudaEventRecord(ev1_, q_));
+        // rescaled Newton step, swept boxes, line search
+        k_max_dx<<<div_up(n_, kB), kB, 0, q_>>>(n_, dx_.data(), st_.data());
+        PPF_LAUNCH_CHECK();
+        k_apply_dx<<<div_up(n_, kB), kB, 0, q_>>>(n_, eval_x_.data(), target_.data(), dx_.data(),
+                                                   st_.data(), param->max_dx, rescale_.data());
+        PPF_LAUNCH_CHECK();
+        k_init_ls<<<1, 1, 0, q_>>>(st_.data(), max_t, pcg_.result.data());
+        PPF_LAUNCH_CHECK();
+        LineSearchArgs la{target_.data(), eval_x_.data(), curr_.data(), st_.data(), max_t,
+                          param->ccd_eps};
+        if (!param->disable_contact) {
+            build_trees(target_.data(), eval_x_.data(), max_t, false);
+            launch_contact_line_search(s, view(bvh_face_), view(bvh_edge_), view(bvh_vert_), la,
+                                       q_);
+        } else {
+            launch_constraint_line_search(s, la, q_);
+        }
+        launch_strain_line_search(s, la, q_);
+        float rescale = 1.0f;
+        PPF_CUDA(cudaMemcpyAsync(st_host_, st_.data(), sizeof(IterStatus),
+                                 cudaMemcpyDeviceToHost, q_));
+        PPF_CUDA(cudaMemcpyAsync(&rescale, rescale_.data(), sizeof(float), cudaMemcpyDeviceToHost, q_));
+        PPF_CUDA(cudaStreamSynchronize(q_));
+        const IterStatus st = *st_host_;
+        float pcg_ms = 0.0f;
+        PPF_CUDA(cudaEventElapsedTime(&pcg_ms, ev0_, ev1_));
+        stats_.newton_iters++;
+        stats_.pcg_solves++;
+        stats_.pcg_iters_total += st.pcg_iter;
+        stats_.pcg_ms_total += pcg_ms;
+        stats_.pcg_ms.push_back(pcg_ms);
+        stats_.pcg_iters.push_back(st.pcg_iter);
+        stats_.max_contacts = std::max(stats_.max_contacts, st.n_contact);
+        stats_.max_dyn_blocks = std::max(stats_.max_dyn_blocks, st.n_dyn);
+        if (st.status & (STATUS_BVH_STACK_OVERFLOW | STATUS_BLOCK_OVERFLOW | STATUS_BAD_SLOT |
+                         STATUS_SORT_LOOKBACK_TIMEOUT | STATUS_REFIT_CYCLE)) {
+            char buf[160];
+            snprintf(buf, sizeof(buf), "device status 0x%x during the Newton step", st.status);
+            throw FatalError(4, buf);
+        }
+        if (st.pcg_state == 2) {
+            result.pcg_success = false;
+            return result;
+        }
+        if (st.pin_infeasible != 0xFFFFFFFFu) {
+            result.pin_feasible = false;
+            return result;
+        }
+        if (st.overlap) {
+            result.contact_separated = false;
+            return result;
+        }
+        float toi = std::min(1.0f, bits_to_float(st.toi_bits) / max_t);
+        float sl_toi = bits_to_float(st.sl_toi_bits) / max_t;
+        toi = std::min(toi, sl_toi);
+        stats_.toi.push_back(toi);
+        if (toi <= 1.19209290e-7f) {
+            result.ccd_success = false;
+            return result;
+        }
+        if (!final_step)
+            toi_advanced += std::max(0.0, 1.0 - toi_advanced) * (double)(rescale * toi);
+        k_apply_toi<<<div_up(n_, kB), kB, 0, q_>>>(n_, eval_x_.data(), target_.data(), toi);
+        PPF_LAUNCH_CHECK();
+        if (final_step) break;
+        if (toi_advanced >= param->target_toi && step >= param->min_newton_steps) {
+            final_step = true;
+        } else {
+            ++step;
+            compute_target(dt);
+        }
+    }
+    if (!param->disable_contact) {
+        build_trees(eval_x_.data(), eval_x_.data(), 1.0f, false);
+        if (!check_intersection(eval_x_.data())) result.intersection_free = false;
+    }
+    param->prev_dt = dt;
+    param->time += (double)(param->prev_dt / param->playback);
+    PPF_CUDA(cudaMemcpyAsync(prev_.data(), curr_.data(), n3 * sizeof(float),
+                             cudaMemcpyDeviceToDevice, q_));
+    PPF_CUDA(cudaMemcpyAsync(curr_.data(), eval_x_.data(), n3 * sizeof(float),
+                             cudaMemcpyDeviceToDevice, q_));
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    result.time = param->time;
+    stats_.step_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() -
+                                                              t_start)
+                         .count();
+    return result;
+}
+
+void Solver::fetch() {
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    PPF_CUDA(cudaMemcpy(host->vertex.curr.data, curr_.data(), 3 * (size_t)n_ * sizeof(float),
+                        cudaMemcpyDeviceToHost));
+    PPF_CUDA(cudaMemcpy(host->vertex.prev.data, prev_.data(), 3 * (size_t)n_ * sizeof(float),
+                        cudaMemcpyDeviceToHost));
+}
+
+void Solver::fetch_dyn_counts(unsigned *n_value, unsigned *n_offset) {
+    *n_offset = n_ + 1;
+    unsigned v = 0;
+    if (dyn_.off) PPF_CUDA(cudaMemcpy(&v, dyn_.off + n_, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    *n_value = v;
+}
+
+void Solver::fetch_dyn(unsigned *index, PpfMat3x3f *value, unsigned *offset) {
+    std::vector<unsigned> off(n_ + 1, 0u);
+    if (dyn_.off)
+        PPF_CUDA(cudaMemcpy(off.data(), dyn_.off, (n_ + 1) * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    std::vector<unsigned> col(off[n_]);
+    std::vector<float> val(9 * (size_t)off[n_]);
+    if (off[n_]) {
+        PPF_CUDA(cudaMemcpy(col.data(), dyn_.col, off[n_] * sizeof(unsigned), cudaMemcpyDeviceToHost));
+        PPF_CUDA(cudaMemcpy(val.data(), dyn_.val, 9 * (size_t)off[n_] * sizeof(float),
+                            cudaMemcpyDeviceToHost));
+    }
+    // rows sorted by column, as the reference's carried pattern is
+    for (unsigned i = 0; i < n_; ++i) {
+        std::vector<unsigned> order(off[i + 1] - off[i]);
+        for (unsigned k = 0; k < order.size(); ++k) order[k] = off[i] + k;
+        std::sort(order.begin(), order.end(), [&](unsigned a, unsigned b) { return col[a] < col[b]; });
+        for (unsigned k = 0; k < order.size(); ++k) {
+            index[off[i] + k] = col[order[k]];
+            if (value) std::memcpy(value[off[i] + k].m, &val[9 * (size_t)order[k]], 9 * sizeof(float));
+        }
+    }
+    std::memcpy(offset, off.data(), (n_ + 1) * sizeof(unsigned));
+}
+
+void Solver::override_velocity(const unsigned *idx, unsigned count, float vx, float vy,
+                               float vz, float dt) {
+    if (count == 0 || dt <= 0.0f) return;
+    DevBuf<unsigned> d;
+    upload(d, idx, count);
+    k_override_velocity<<<div_up(count, kB), kB, 0, q_>>>(d.data(), count, curr_.data(),
+                                                         prev_.data(), vx * dt, vy * dt, vz * dt);
+    PPF_LAUNCH_CHECK();
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    d.release();
+}
+
+void Solver::override_angular_velocity(const unsigned *idx, unsigned count, float wx, float wy,
+                                       float wz, float cx, float cy, float cz, float dt) {
+    if (count == 0 || dt <= 0.0f) return;
+    DevBuf<unsigned> d;
+    upload(d, idx, count);
+    k_override_angular<<<div_up(count, kB), kB, 0, q_>>>(d.data(), count, curr_.data(),
+                                                        prev_.data(), wx, wy, wz, cx, cy, cz, dt);
+    PPF_LAUNCH_CHECK();
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    d.release();
+}
+
+void Solver::gather_current_positions(const unsigned *idx, unsigned count, float *out) {
+    std::vector<float> all(3 * (size_t)n_);
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    PPF_CUDA(cudaMemcpy(all.data(), curr_.data(), all.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (unsigned i = 0; i < count; ++i)
+        for (int d = 0; d < 3; ++d) out[3 * i + d] = all[3 * idx[i] + d];
+}
+
+void Solver::set_active(const std::vector<unsigned char> &va) {
+    std::vector<unsigned char> fa(nf_), ea(ne_);
+    const unsigned *F = (const unsigned *)host->mesh.mesh.face.data;
+    const unsigned *E = (const unsigned *)host->mesh.mesh.edge.data;
+    for (unsigned i = 0; i < nf_; ++i) fa[i] = va[F[3 * i]] || va[F[3 * i + 1]] || va[F[3 * i + 2]];
+    for (unsigned i = 0; i < ne_; ++i) ea[i] = va[E[2 * i]] || va[E[2 * i + 1]];
+    upload(vert_active_, va);
+    upload(face_active_, fa);
+    upload(edge_active_, ea);
+    use_active_ = true;
+}
+
+void Solver::debug_matrix(std::vector<unsigned> &f_off, std::vector<unsigned> &f_col,
+                          std::vector<float> &f_val, std::vector<unsigned> &d_off,
+                          std::vector<unsigned> &d_col, std::vector<float> &d_val,
+                          std::vector<float> &diag, std::vector<float> &force) {
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    f_off.resize(n_ + 1);
+    PPF_CUDA(cudaMemcpy(f_off.data(), fixed_off_.data(), (n_ + 1) * 4, cudaMemcpyDeviceToHost));
+    f_col.resize(nnz_fixed_);
+    PPF_CUDA(cudaMemcpy(f_col.data(), fixed_col_.data(), nnz_fixed_ * 4, cudaMemcpyDeviceToHost));
+    f_val.resize(9 * (size_t)nnz_fixed_);
+    PPF_CUDA(cudaMemcpy(f_val.data(), fixed_val_.data(), f_val.size() * 4, cudaMemcpyDeviceToHost));
+    d_off.assign(n_ + 1, 0u);
+    if (dyn_.off) PPF_CUDA(cudaMemcpy(d_off.data(), dyn_.off, (n_ + 1) * 4, cudaMemcpyDeviceToHost));
+    d_col.resize(d_off[n_]);
+    d_val.resize(9 * (size_t)d_off[n_]);
+    if (d_off[n_]) {
+        PPF_CUDA(cudaMemcpy(d_col.data(), dyn_.col, d_off[n_] * 4, cudaMemcpyDeviceToHost));
+        PPF_CUDA(cudaMemcpy(d_val.data(), dyn_.val, d_val.size() * 4, cudaMemcpyDeviceToHost));
+    }
+    diag.resize(9 * (size_t)n_);
+    PPF_CUDA(cudaMemcpy(diag.data(), diag_.data(), diag.size() * 4, cudaMemcpyDeviceToHost));
+    force.resize(3 * (size_t)n_);
+    PPF_CUDA(cudaMemcpy(force.data(), force_.data(), force.size() * 4, cudaMemcpyDeviceToHost));
+}
+
+void Solver::debug_pairs(std::vector<unsigned> &pf, std::vector<unsigned> &pe,
+                         std::vector<unsigned> &pp, std::vector<unsigned> &ee) {
+    read_status();
+    unsigned c[4] = {std::min(st_host_->n_pf, pairs_.cap_pf), std::min(st_host_->n_pe, pairs_.cap_pe),
+                     std::min(st_host_->n_pp, pairs_.cap_pp), std::min(st_host_->n_ee, pairs_.cap_ee)};
+    pf.resize(2 * (size_t)c[0]);
+    pe.resize(3 * (size_t)c[1]);
+    pp.resize(3 * (size_t)c[2]);
+    ee.resize(2 * (size_t)c[3]);
+    if (c[0]) PPF_CUDA(cudaMemcpy(pf.data(), pairs_.pf, pf.size() * 4, cudaMemcpyDeviceToHost));
+    if (c[1]) PPF_CUDA(cudaMemcpy(pe.data(), pairs_.pe, pe.size() * 4, cudaMemcpyDeviceToHost));
+    if (c[2]) PPF_CUDA(cudaMemcpy(pp.data(), pairs_.pp, pp.size() * 4, cudaMemcpyDeviceToHost));
+    if (c[3]) PPF_CUDA(cudaMemcpy(ee.data(), pairs_.ee, ee.size() * 4, cudaMemcpyDeviceToHost));
+}
+
+// One assembly + linear solve at the current state (target from curr/prev,
+// eval_x = curr), exposing the first Newton iteration of a step.
+int Solver::debug_assemble_solve(std::vector<float> &dx, unsigned &iters, float &resid) {
+    const size_t n3 = 3 * (size_t)n_;
+    float dt = param->dt * param->playback;
+    PPF_CUDA(cudaMemsetAsync(st_.data(), 0, sizeof(IterStatus), q_));
+    if (!param->disable_contact) build_trees(curr_.data(), curr_.data(), 1.0f, true);
+    compute_target(dt);
+    PPF_CUDA(cudaMemcpyAsync(eval_x_.data(), curr_.data(), n3 * sizeof(float),
+                             cudaMemcpyDeviceToDevice, q_));
+    assemble(dt);
+    PPF_CUDA(cudaMemcpyAsync(r_.data(), force_.data(), n3 * sizeof(float),
+                             cudaMemcpyDeviceToDevice, q_));
+    PcgOperator A = pcg_operator();
+    launch_block_jacobi(A, fixed_diag_.data(), inv_diag_.data(), &st_.data()->status, q_);
+    launch_pcg(A, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_);
+    PcgResult res;
+    PPF_CUDA(cudaMemcpyAsync(&res, pcg_.result.data(), sizeof(PcgResult), cudaMemcpyDeviceToHost, q_));
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    dx.resize(n3);
+    PPF_CUDA(cudaMemcpy(dx.data(), dx_.data(), n3 * sizeof(float), cudaMemcpyDeviceToHost));
+    iters = res.iter;
+    resid = res.resid;
+    return res.state;
+}
+
+void Solver::release() {
+    if (q_) cudaStreamSynchronize(q_);
+    initialized_ = false;
+}
+
+} // namespace gpu
+} // namespace ppf

@@ -1,0 +1,132 @@
+// solver.cuh -- the per-step solve behind the reference's C ABI.
+#pragma once
+
+#include <vector>
+
+#include "assemble.cuh"
+#include "lbvh.cuh"
+#include "linesearch.cuh"
+#include "pcg.cuh"
+
+namespace ppf {
+namespace gpu {
+
+// Per-step statistics (GB300 extension, ppf_step_stats in ppf_gb300_ext.h).
+struct StepStats {
+    unsigned newton_iters = 0;
+    unsigned pcg_iters_total = 0;
+    unsigned pcg_solves = 0;
+    float pcg_ms_total = 0.0f;
+    float step_ms = 0.0f;
+    unsigned max_contacts = 0;
+    unsigned max_dyn_blocks = 0;
+    std::vector<float> pcg_ms;        // per solve
+    std::vector<unsigned> pcg_iters;  // per solve
+    std::vector<float> toi;           // per Newton iteration
+};
+
+class Solver {
+  public:
+    bool initialize(PpfDataSet *ds, PpfParamSet *param);
+    PpfStepResult advance();
+    void fetch();
+    void update_constraint(const PpfConstraint *c);
+    void update_rest_shape(const PpfRestShapeUpdate *u);
+    void fetch_dyn_counts(unsigned *n_value, unsigned *n_offset);
+    void fetch_dyn(unsigned *index, PpfMat3x3f *value, unsigned *offset);
+    void override_velocity(const unsigned *idx, unsigned count, float vx, float vy,
+                           float vz, float dt);
+    void override_angular_velocity(const unsigned *idx, unsigned count, float wx,
+                                   float wy, float wz, float cx, float cy, float cz,
+                                   float dt);
+    void gather_current_positions(const unsigned *idx, unsigned count, float *out);
+    void set_active(const std::vector<unsigned char> &vert_active);
+    unsigned fetch_intersection_records(PpfIntersectionRecord *out, unsigned max_count);
+    const StepStats &stats() const { return stats_; }
+    // debug views (host copies) for stage parity checks
+    void debug_matrix(std::vector<unsigned> &f_off, std::vector<unsigned> &f_col,
+                      std::vector<float> &f_val, std::vector<unsigned> &d_off,
+                      std::vector<unsigned> &d_col, std::vector<float> &d_val,
+                      std::vector<float> &diag, std::vector<float> &force);
+    void debug_pairs(std::vector<unsigned> &pf, std::vector<unsigned> &pe,
+                     std::vector<unsigned> &pp, std::vector<unsigned> &ee);
+    // one assembly + solve at the current positions, without line search
+    int debug_assemble_solve(std::vector<float> &dx, unsigned &iters, float &resid);
+    void release();
+
+    PpfDataSet *host = nullptr;
+    PpfParamSet *param = nullptr;
+
+  private:
+    Scene scene() const;
+    StepParams step_params(float dt) const;
+    AssemblyBuffers abuf();
+    PcgOperator pcg_operator() const;
+    void upload_props();
+    void build_trees(const float *x0, const float *x1, float extrap, bool rebuild);
+    BvhView view(const Lbvh &b) const;
+    void compute_target(float dt);
+    void assemble(float dt);
+    bool check_intersection(const float *x);
+    void read_status();
+
+    unsigned n_ = 0, n_surf_ = 0, nf_ = 0, ne_ = 0, nh_ = 0;
+    cudaStream_t q_ = nullptr;
+    // topology / props / params
+    DevBuf<unsigned> face_, edge_, hinge_;
+    DevBuf<PpfVertexProp> vprop_;
+    DevBuf<PpfEdgeProp> eprop_;
+    DevBuf<PpfFaceProp> fprop_;
+    DevBuf<PpfHingeProp> hprop_;
+    DevBuf<PpfVertexParam> vparam_;
+    DevBuf<PpfEdgeParam> eparam_;
+    DevBuf<PpfFaceParam> fparam_;
+    DevBuf<PpfHingeParam> hparam_;
+    DevBuf<float> inv_rest_;
+    DevBuf<unsigned> vf_off_, vf_, ve_off_, ve_, ef_off_, ef_;
+    DevBuf<unsigned> fixed_off_, fixed_col_, fixed_tr_off_, fixed_diag_;
+    DevBuf<uint2> fixed_tr_;
+    DevBuf<unsigned> face_slot_, hinge_slot_, dof_mask_;
+    DevBuf<PpfFixPair> fix_;
+    DevBuf<PpfPullPair> pull_;
+    DevBuf<PpfSphere> sphere_;
+    DevBuf<PpfFloor> floor_;
+    unsigned nfix_ = 0, npull_ = 0, nsphere_ = 0, nfloor_ = 0;
+    DevBuf<float> margin_face_, margin_edge_, margin_vert_;
+    DevBuf<unsigned char> vert_active_, edge_active_, face_active_;
+    bool use_active_ = false;
+    std::vector<PpfVertexProp> h_vprop_;
+    std::vector<PpfFaceProp> h_fprop_;
+    std::vector<PpfEdgeProp> h_eprop_;
+    std::vector<PpfHingeProp> h_hprop_;
+    unsigned nnz_fixed_ = 0;
+    // state
+    DevBuf<float> curr_, prev_, eval_x_, target_, force_, dx_, diag_, r_;
+    DevBuf<float> fixed_val_, fixed_tmp_, inv_diag_;
+    Lbvh bvh_face_, bvh_edge_, bvh_vert_;
+    RadixSortWorkspace sort_ws_;
+    PairLists pairs_;
+    DevBuf<uint2> pf_buf_, ee_buf_;
+    DevBuf<uint3> pe_buf_, pp_buf_;
+    DynMatrix dyn_;
+    DevBuf<unsigned long long> hkey_buf_;
+    DevBuf<unsigned> hval_buf_, doff_buf_, dcol_buf_, dtroff_buf_, dcnt_buf_, dcnt2_buf_;
+    DevBuf<uint2> dtr_buf_;
+    DevBuf<float> dval_buf_;
+    DevBuf<unsigned> scan_tmp_;
+    PcgWorkspace pcg_;
+    DevBuf<IterStatus> st_;
+    IterStatus *st_host_ = nullptr;
+    DevBuf<float> rescale_;
+    DevBuf<PpfIntersectionRecord> isect_;
+    std::vector<PpfIntersectionRecord> isect_host_;
+    unsigned isect_count_ = 0;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evs0_ = nullptr, evs1_ = nullptr;
+    StepStats stats_;
+    bool initialized_ = false;
+};
+
+Solver &solver_instance();
+
+} // namespace gpu
+} // namespace ppf

@@ -1,0 +1,575 @@
+// builder.cpp -- host-side scene builder: meshes + materials -> DataSet.
+//
+// Restates, for shells, the reference driver's preparation of the DataSet:
+//   mesh topology (edges, hinges, neighbor tables)   mesh.rs:66-293
+//   face / vertex / hinge / edge props and params    scene.rs:1655-1840,
+//                                                   builder.rs:339-1020,
+//                                                   main.rs:205-250
+//   inverse rest matrices (tangent-plane frame)      builder.rs:157-230
+//   fixed sparsity, transpose table, slot tables     builder.rs:1244-1420
+//   ParamSet defaults                                params.rs:207-289,
+//                                                   builder.rs:1629-1681
+#include "../../../include/ppf_gb300_scene.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+template <class T> void set_vec(T *&data, unsigned &size, unsigned &alloc,
+                                std::vector<T> &src) {
+    data = src.empty() ? nullptr : src.data();
+    size = (unsigned)src.size();
+    alloc = size;
+}
+
+struct VecVecStore {
+    std::vector<unsigned> data;
+    std::vector<unsigned> offset;
+    void from(const std::vector<std::vector<unsigned>> &rows) {
+        data.clear();
+        offset.assign(1, 0u);
+        for (auto &r : rows) {
+            data.insert(data.end(), r.begin(), r.end());
+            offset.push_back((unsigned)data.size());
+        }
+    }
+    void fill(PpfVecVecU32 &v) {
+        v.data = data.empty() ? nullptr : data.data();
+        v.offset = offset.data();
+        v.size = (unsigned)offset.size() - 1;
+        v.nnz = (unsigned)data.size();
+        v.nnz_allocated = v.nnz;
+        v.offset_allocated = (unsigned)offset.size();
+    }
+};
+
+template <class P> unsigned dedup(std::vector<P> &store, const P &p) {
+    for (size_t i = 0; i < store.size(); ++i)
+        if (std::memcmp(&store[i], &p, sizeof(P)) == 0) return (unsigned)i;
+    store.push_back(p);
+    return (unsigned)store.size() - 1;
+}
+
+struct V3 {
+    float x, y, z;
+};
+V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+V3 crs(V3 a, V3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+float nrm(V3 a) { return std::sqrt(dot(a, a)); }
+V3 scale(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+
+} // namespace
+
+struct PpfScene {
+    // inputs
+    std::vector<float> x;                 // 3 n
+    std::vector<float> vel;               // 3 n
+    std::vector<unsigned> faces;          // 3 F
+    std::vector<unsigned> face_material;  // per face
+    std::vector<PpfShellMaterial> materials;
+    std::vector<unsigned> pin_index;
+    std::vector<unsigned char> pin_kinematic;
+    std::vector<std::pair<unsigned, float>> pulls;
+    std::vector<PpfSphere> spheres;
+    std::vector<PpfFloor> floors;
+
+    // outputs
+    std::vector<PpfVec3f> curr, prev;
+    std::vector<PpfVec3u> face;
+    std::vector<PpfVec2u> edge;
+    std::vector<PpfVec4u> hinge;
+    VecVecStore nb_vface, nb_vhinge, nb_vedge, nb_vrod, nb_hface, nb_eface;
+    std::vector<char> type_face, type_vertex, type_hinge;
+    std::vector<PpfVertexProp> vprop;
+    std::vector<PpfEdgeProp> eprop;
+    std::vector<PpfFaceProp> fprop;
+    std::vector<PpfHingeProp> hprop;
+    std::vector<PpfVertexParam> vparam;
+    std::vector<PpfEdgeParam> eparam;
+    std::vector<PpfFaceParam> fparam;
+    std::vector<PpfHingeParam> hparam;
+    std::vector<PpfMat2x2f> inv_rest;
+    std::vector<PpfFixPair> fix;
+    std::vector<PpfPullPair> pull;
+    VecVecStore fixed_table;
+    std::vector<PpfVec2u> transpose_data;
+    std::vector<unsigned> transpose_offset;
+    std::vector<unsigned> face_slots, hinge_slots;
+    PpfDataSet ds;
+    PpfParamSet param;
+    bool built = false;
+};
+
+extern "C" {
+
+PpfScene *ppf_scene_create(void) { return new PpfScene(); }
+void ppf_scene_destroy(PpfScene *s) { delete s; }
+unsigned ppf_scene_vertex_count(PpfScene *s) { return (unsigned)s->x.size() / 3; }
+
+void ppf_scene_positions(PpfScene *s, float *curr, float *prev) {
+    if (curr && !s->curr.empty()) std::memcpy(curr, s->curr.data(), s->curr.size() * sizeof(PpfVec3f));
+    if (prev && !s->prev.empty()) std::memcpy(prev, s->prev.data(), s->prev.size() * sizeof(PpfVec3f));
+}
+
+void ppf_scene_set_positions(PpfScene *s, const float *curr, const float *prev) {
+    if (curr && !s->curr.empty()) std::memcpy(s->curr.data(), curr, s->curr.size() * sizeof(PpfVec3f));
+    if (prev && !s->prev.empty()) std::memcpy(s->prev.data(), prev, s->prev.size() * sizeof(PpfVec3f));
+}
+
+void ppf_scene_default_param(PpfParamSet *p) {
+    std::memset(p, 0, sizeof(*p));
+    const float dt = 1e-3f;
+    p->time = 0.0;
+    p->air_friction = 0.2f;
+    p->air_density = 1e-3f;
+    p->constraint_tol = 0.01f;
+    p->prev_dt = dt;
+    p->dt = dt;
+    p->playback = 1.0f;
+    p->min_newton_steps = 0;
+    p->target_toi = 0.25f;
+    p->stitch_length_factor = 10.0f;
+    p->cg_max_iter = 10000;
+    p->cg_tol = 1e-3f;
+    p->line_search_max_t = 1.25f;
+    p->ccd_eps = 1e-7f;
+    p->max_dx = 1.0f;
+    p->eiganalysis_eps = 1e-2f;
+    p->friction_eps = 1e-5f;
+    p->isotropic_air_friction = 0.0f;
+    p->gravity = {{0.0f, -9.8f, 0.0f}};
+    p->wind = {{0.0f, 0.0f, 0.0f}};
+    p->barrier = PPF_BARRIER_CUBIC;
+    p->friction_mode = PPF_FRICTION_MIN;
+    p->csrmat_max_nnz = 10000000u;
+    p->fix_xz = 0.0f;
+    p->disable_contact = false;
+    p->inactive_momentum = false;
+    p->precond = 0;
+    p->schwarz_levels = 2;
+    p->max_newton_steps = 2048;
+    p->disable_pin_dof_removal = false;
+}
+
+unsigned ppf_scene_add_shell(PpfScene *s, const float *v, unsigned nv,
+                             const unsigned *f, unsigned nf,
+                             const PpfShellMaterial *mat) {
+    unsigned base = (unsigned)s->x.size() / 3;
+    s->x.insert(s->x.end(), v, v + 3 * nv);
+    s->vel.insert(s->vel.end(), 3 * nv, 0.0f);
+    unsigned mi = (unsigned)s->materials.size();
+    s->materials.push_back(*mat);
+    for (unsigned i = 0; i < 3 * nf; ++i) s->faces.push_back(base + f[i]);
+    s->face_material.insert(s->face_material.end(), nf, mi);
+    s->built = false;
+    return base;
+}
+
+void ppf_scene_set_velocity(PpfScene *s, const float *velocity) {
+    std::memcpy(s->vel.data(), velocity, s->vel.size() * sizeof(float));
+}
+
+void ppf_scene_pin(PpfScene *s, const unsigned *idx, unsigned n, int kinematic) {
+    for (unsigned i = 0; i < n; ++i) {
+        s->pin_index.push_back(idx[i]);
+        s->pin_kinematic.push_back(kinematic ? 1 : 0);
+    }
+}
+
+void ppf_scene_pull(PpfScene *s, const unsigned *idx, unsigned n, float weight) {
+    for (unsigned i = 0; i < n; ++i) s->pulls.push_back({idx[i], weight});
+}
+
+void ppf_scene_add_sphere(PpfScene *s, const float *c, float r, float gap,
+                          float friction, int reverse, int bowl) {
+    PpfSphere sp{};
+    sp.center = {{c[0], c[1], c[2]}};
+    sp.ghat = gap;
+    sp.friction = friction;
+    sp.radius = r;
+    sp.thickness = 0.0f;
+    sp.bowl = bowl != 0;
+    sp.reverse = reverse != 0;
+    sp.kinematic = false;
+    s->spheres.push_back(sp);
+}
+
+void ppf_scene_add_floor(PpfScene *s, const float *g, const float *up, float gap,
+                         float friction) {
+    PpfFloor fl{};
+    fl.ground = {{g[0], g[1], g[2]}};
+    fl.ghat = gap;
+    fl.friction = friction;
+    fl.thickness = 0.0f;
+    fl.up = {{up[0], up[1], up[2]}};
+    fl.kinematic = false;
+    s->floors.push_back(fl);
+}
+
+int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
+    const unsigned n = (unsigned)s->x.size() / 3;
+    const unsigned nf = (unsigned)s->faces.size() / 3;
+    auto X = [&](unsigned i) { return V3{s->x[3 * i], s->x[3 * i + 1], s->x[3 * i + 2]}; };
+    s->param = *prm;
+    const float dt = prm->dt;
+
+    // positions
+    s->curr.resize(n);
+    s->prev.resize(n);
+    for (unsigned i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            s->curr[i].v[d] = s->x[3 * i + d];
+            s->prev[i].v[d] = s->x[3 * i + d] - s->vel[3 * i + d] * dt;
+        }
+
+    // faces
+    s->face.resize(nf);
+    for (unsigned i = 0; i < nf; ++i)
+        for (int k = 0; k < 3; ++k) s->face[i].v[k] = s->faces[3 * i + k];
+
+    // edges in first-seen order with their incident faces (mesh.rs:188-229)
+    std::map<std::pair<unsigned, unsigned>, unsigned> edge_id;
+    std::vector<std::vector<unsigned>> edge_faces;
+    s->edge.clear();
+    for (unsigned i = 0; i < nf; ++i)
+        for (int j = 0; j < 3; ++j) {
+            unsigned a = s->faces[3 * i + j], b = s->faces[3 * i + (j + 1) % 3];
+            auto key = std::make_pair(std::min(a, b), std::max(a, b));
+            auto it = edge_id.find(key);
+            if (it == edge_id.end()) {
+                edge_id[key] = (unsigned)s->edge.size();
+                s->edge.push_back({{a, b}});
+                edge_faces.push_back({i});
+            } else if (edge_faces[it->second].size() < 2) {
+                edge_faces[it->second].push_back(i);
+            }
+        }
+    // hinges (mesh.rs:231-293): shared edge as seen in its first face, the
+    // first face's opposite corner, then the second face's opposite corner;
+    // edges with more than two faces carry no hinge.
+    struct HingeAcc {
+        unsigned e0, e1, o0, o1, f0, f1, count;
+    };
+    std::map<std::pair<unsigned, unsigned>, unsigned> hinge_key;
+    std::vector<HingeAcc> hacc;
+    for (unsigned i = 0; i < nf; ++i)
+        for (int j = 0; j < 3; ++j) {
+            unsigned a = s->faces[3 * i + j], b = s->faces[3 * i + (j + 1) % 3],
+                     c = s->faces[3 * i + (j + 2) % 3];
+            auto key = std::make_pair(std::min(a, b), std::max(a, b));
+            auto it = hinge_key.find(key);
+            if (it == hinge_key.end()) {
+                hinge_key[key] = (unsigned)hacc.size();
+                hacc.push_back({a, b, c, 0u, i, 0u, 1u});
+            } else {
+                HingeAcc &h = hacc[it->second];
+                if (h.count == 1) {
+                    h.o1 = c;
+                    h.f1 = i;
+                }
+                ++h.count;
+            }
+        }
+    s->hinge.clear();
+    std::vector<std::vector<unsigned>> hinge_faces;
+    for (auto &h : hacc)
+        if (h.count == 2) {
+            s->hinge.push_back({{h.e0, h.e1, h.o0, h.o1}});
+            hinge_faces.push_back({h.f0, h.f1});
+        }
+    const unsigned ne = (unsigned)s->edge.size(), nh = (unsigned)s->hinge.size();
+
+    // neighbor tables (mesh.rs:172-186)
+    std::vector<std::vector<unsigned>> vf(n), vh(n), ve(n), vr(n);
+    for (unsigned i = 0; i < nf; ++i)
+        for (int k = 0; k < 3; ++k) vf[s->face[i].v[k]].push_back(i);
+    for (unsigned i = 0; i < nh; ++i)
+        for (int k = 0; k < 4; ++k) vh[s->hinge[i].v[k]].push_back(i);
+    for (unsigned i = 0; i < ne; ++i)
+        for (int k = 0; k < 2; ++k) ve[s->edge[i].v[k]].push_back(i);
+    s->nb_vface.from(vf);
+    s->nb_vhinge.from(vh);
+    s->nb_vedge.from(ve);
+    s->nb_vrod.from(vr);
+    s->nb_hface.from(hinge_faces);
+    s->nb_eface.from(edge_faces);
+    s->type_face.assign(nf, 0);
+    s->type_vertex.assign(n, 0);
+    s->type_hinge.assign(nh, 0);
+
+    // pins
+    std::vector<char> fixed_v(n, 0);
+    s->fix.clear();
+    for (size_t i = 0; i < s->pin_index.size(); ++i) {
+        unsigned v = s->pin_index[i];
+        PpfFixPair fp{};
+        for (int d = 0; d < 3; ++d) fp.position.v[d] = s->x[3 * v + d];
+        fp.ghat = 1e-3f;
+        fp.index = v;
+        fp.kinematic = s->pin_kinematic[i] != 0;
+        s->fix.push_back(fp);
+        fixed_v[v] = 1;
+    }
+    s->pull.clear();
+    for (auto &p : s->pulls) {
+        PpfPullPair pp{};
+        for (int d = 0; d < 3; ++d) pp.position.v[d] = s->x[3 * p.first + d];
+        pp.weight = p.second;
+        pp.index = p.first;
+        s->pull.push_back(pp);
+    }
+
+    // face props / params (scene.rs:1655-1840)
+    s->fparam.clear();
+    s->fprop.assign(nf, PpfFaceProp{});
+    std::vector<float> face_area(nf);
+    for (unsigned i = 0; i < nf; ++i) {
+        const PpfShellMaterial &m = s->materials[s->face_material[i]];
+        V3 a = X(s->face[i].v[0]), b = X(s->face[i].v[1]), c = X(s->face[i].v[2]);
+        float area = 0.5f * nrm(crs(sub(b, a), sub(c, a)));
+        face_area[i] = area;
+        PpfFaceParam fp{};
+        fp.model = m.model;
+        float E = m.young_mod, nu = m.poiss_rat;
+        fp.mu = E / (2.0f * (1.0f + nu));
+        fp.lambda = E * nu / ((1.0f + nu) * (1.0f - 2.0f * nu));
+        fp.friction = m.friction;
+        fp.ghat = m.contact_gap;
+        fp.offset = m.contact_offset;
+        fp.bend = m.bend;
+        fp.strainlimit = m.strain_limit;
+        fp.shrink_x = 1.0f;
+        fp.shrink_y = 1.0f;
+        PpfFaceProp pr{};
+        pr.area = area;
+        pr.mass = m.density * area;
+        pr.fixed = fixed_v[s->face[i].v[0]] && fixed_v[s->face[i].v[1]] &&
+                   fixed_v[s->face[i].v[2]];
+        pr.param_index = dedup(s->fparam, fp);
+        s->fprop[i] = pr;
+    }
+
+    // vertex props (builder.rs:560-720) and params (builder.rs:780-870)
+    s->vprop.assign(n, PpfVertexProp{});
+    for (unsigned i = 0; i < n; ++i) s->vprop[i].rest_bend_angle = 3.14159265358979323846f;
+    for (size_t i = 0; i < s->fix.size(); ++i) s->vprop[s->fix[i].index].fix_index = (unsigned)i + 1;
+    for (size_t i = 0; i < s->pull.size(); ++i) s->vprop[s->pull[i].index].pull_index = (unsigned)i + 1;
+    for (unsigned i = 0; i < nf; ++i)
+        for (int k = 0; k < 3; ++k) s->vprop[s->face[i].v[k]].area += s->fprop[i].area / 3.0f;
+    for (unsigned i = 0; i < nf; ++i)
+        for (int k = 0; k < 3; ++k) s->vprop[s->face[i].v[k]].mass += s->fprop[i].mass / 3.0f;
+    s->vparam.clear();
+    for (unsigned j = 0; j < n; ++j) {
+        float gs = 0, os = 0, fs = 0, ws = 0;
+        for (unsigned fi : vf[j]) {
+            const PpfFaceParam &p = s->fparam[s->fprop[fi].param_index];
+            float w = s->fprop[fi].area;
+            gs += w * p.ghat;
+            os += w * p.offset;
+            fs += w * p.friction;
+            ws += w;
+        }
+        if (ws > 0.0f) {
+            PpfVertexParam vp{gs / ws, os / ws, fs / ws};
+            s->vprop[j].param_index = dedup(s->vparam, vp);
+        }
+    }
+
+    // hinge props / params (builder.rs:873-1020)
+    s->hparam.clear();
+    s->hprop.assign(nh, PpfHingeProp{});
+    for (unsigned i = 0; i < nh; ++i) {
+        const PpfVec4u &h = s->hinge[i];
+        float length = nrm(sub(X(h.v[0]), X(h.v[1])));
+        float os = 0, gs = 0, bs = 0, as = 0;
+        bool all_fixed = true;
+        for (unsigned fi : hinge_faces[i]) {
+            const PpfFaceParam &p = s->fparam[s->fprop[fi].param_index];
+            float a = s->fprop[fi].area;
+            all_fixed = all_fixed && s->fprop[fi].fixed;
+            os += a * p.offset;
+            gs += a * p.ghat;
+            bs += a * p.bend;
+            as += a;
+        }
+        PpfHingeParam hp{};
+        hp.bend = all_fixed ? 0.0f : bs / as;
+        hp.ghat = gs / as;
+        hp.offset = os / as;
+        PpfHingeProp pr{};
+        pr.length = length;
+        pr.area = as;
+        pr.rest_angle = 0.0f;
+        pr.uv_edge_sin2 = -1.0f;
+        pr.fixed = fixed_v[h.v[0]] && fixed_v[h.v[1]] && fixed_v[h.v[2]] && fixed_v[h.v[3]];
+        pr.collider = false;
+        pr.param_index = dedup(s->hparam, hp);
+        s->hprop[i] = pr;
+    }
+
+    // face-edge props (main.rs:205-250): zero mass, area-averaged contact
+    s->eparam.clear();
+    s->eprop.assign(ne, PpfEdgeProp{});
+    for (unsigned i = 0; i < ne; ++i) {
+        float gs = 0, os = 0, fs = 0, as = 0;
+        for (unsigned fi : edge_faces[i]) {
+            const PpfFaceParam &p = s->fparam[s->fprop[fi].param_index];
+            float a = face_area[fi];
+            gs += a * p.ghat;
+            os += a * p.offset;
+            fs += a * p.friction;
+            as += a;
+        }
+        PpfEdgeParam ep{};
+        ep.ghat = gs / as;
+        ep.offset = os / as;
+        ep.friction = fs / as;
+        PpfEdgeProp pr{};
+        pr.length = nrm(sub(X(s->edge[i].v[0]), X(s->edge[i].v[1])));
+        pr.initial_length = pr.length;
+        pr.mass = 0.0f;
+        pr.fixed = fixed_v[s->edge[i].v[0]] && fixed_v[s->edge[i].v[1]];
+        pr.param_index = dedup(s->eparam, ep);
+        s->eprop[i] = pr;
+    }
+
+    // inverse rest matrices in the face's tangent frame (builder.rs:157-230)
+    s->inv_rest.resize(nf);
+    for (unsigned i = 0; i < nf; ++i) {
+        V3 x0 = X(s->face[i].v[0]), x1 = X(s->face[i].v[1]), x2 = X(s->face[i].v[2]);
+        V3 d0 = sub(x1, x0), d1 = sub(x2, x0);
+        V3 nn = crs(d0, d1);
+        V3 e2 = crs(nn, d0);
+        e2 = scale(e2, 1.0f / nrm(e2));
+        V3 e1 = scale(d0, 1.0f / nrm(d0));
+        float a = dot(e1, d0), b = dot(e1, d1), c = dot(e2, d0), d = dot(e2, d1);
+        float det = a * d - c * b;
+        if (!(std::fabs(det) > 0.0f)) return 1;
+        PpfMat2x2f inv;
+        // column-major [[d, -b], [-c, a]] / det
+        inv.m[0] = d / det;
+        inv.m[1] = -c / det;
+        inv.m[2] = -b / det;
+        inv.m[3] = a / det;
+        s->inv_rest[i] = inv;
+    }
+
+    // fixed sparsity: diagonal, edge, face and hinge stencils, upper triangle
+    // sorted by column (builder.rs:1244-1340)
+    std::vector<std::vector<unsigned>> rows(n);
+    auto insert = [&](unsigned i, unsigned j) {
+        if (i > j) return;
+        auto &r = rows[i];
+        auto it = std::lower_bound(r.begin(), r.end(), j);
+        if (it == r.end() || *it != j) r.insert(it, j);
+    };
+    for (unsigned i = 0; i < n; ++i) insert(i, i);
+    for (auto &e : s->edge)
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b) insert(e.v[a], e.v[b]);
+    for (auto &f : s->face)
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) insert(f.v[a], f.v[b]);
+    for (auto &h : s->hinge)
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) insert(h.v[a], h.v[b]);
+    s->fixed_table.from(rows);
+    std::vector<std::vector<PpfVec2u>> tr(n);
+    unsigned base = 0;
+    for (unsigned i = 0; i < n; ++i) {
+        for (size_t k = 0; k < rows[i].size(); ++k)
+            if (rows[i][k] != i) tr[rows[i][k]].push_back({{i, base + (unsigned)k}});
+        base += (unsigned)rows[i].size();
+    }
+    s->transpose_data.clear();
+    s->transpose_offset.assign(1, 0u);
+    for (auto &r : tr) {
+        s->transpose_data.insert(s->transpose_data.end(), r.begin(), r.end());
+        s->transpose_offset.push_back((unsigned)s->transpose_data.size());
+    }
+    auto slot_of = [&](unsigned i, unsigned j) -> unsigned {
+        if (i > j) return 0xFFFFFFFFu;
+        auto &r = rows[i];
+        auto it = std::lower_bound(r.begin(), r.end(), j);
+        return s->fixed_table.offset[i] + (unsigned)(it - r.begin());
+    };
+    s->face_slots.clear();
+    for (auto &f : s->face)
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) s->face_slots.push_back(slot_of(f.v[a], f.v[b]));
+    s->hinge_slots.clear();
+    for (auto &h : s->hinge) {
+        unsigned r[4] = {h.v[2], h.v[1], h.v[0], h.v[3]}; // remapped order
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) s->hinge_slots.push_back(slot_of(r[a], r[b]));
+    }
+
+    // assemble the DataSet view
+    PpfDataSet &ds = s->ds;
+    std::memset(&ds, 0, sizeof(ds));
+    set_vec(ds.vertex.prev.data, ds.vertex.prev.size, ds.vertex.prev.allocated, s->prev);
+    set_vec(ds.vertex.curr.data, ds.vertex.curr.size, ds.vertex.curr.allocated, s->curr);
+    set_vec(ds.mesh.mesh.face.data, ds.mesh.mesh.face.size, ds.mesh.mesh.face.allocated, s->face);
+    set_vec(ds.mesh.mesh.hinge.data, ds.mesh.mesh.hinge.size, ds.mesh.mesh.hinge.allocated, s->hinge);
+    set_vec(ds.mesh.mesh.edge.data, ds.mesh.mesh.edge.size, ds.mesh.mesh.edge.allocated, s->edge);
+    s->nb_vface.fill(ds.mesh.neighbor.vertex.face);
+    s->nb_vhinge.fill(ds.mesh.neighbor.vertex.hinge);
+    s->nb_vedge.fill(ds.mesh.neighbor.vertex.edge);
+    s->nb_vrod.fill(ds.mesh.neighbor.vertex.rod);
+    s->nb_hface.fill(ds.mesh.neighbor.hinge.face);
+    s->nb_eface.fill(ds.mesh.neighbor.edge.face);
+    set_vec(ds.mesh.type.face.data, ds.mesh.type.face.size, ds.mesh.type.face.allocated, s->type_face);
+    set_vec(ds.mesh.type.vertex.data, ds.mesh.type.vertex.size, ds.mesh.type.vertex.allocated, s->type_vertex);
+    set_vec(ds.mesh.type.hinge.data, ds.mesh.type.hinge.size, ds.mesh.type.hinge.allocated, s->type_hinge);
+    set_vec(ds.prop.vertex.data, ds.prop.vertex.size, ds.prop.vertex.allocated, s->vprop);
+    set_vec(ds.prop.edge.data, ds.prop.edge.size, ds.prop.edge.allocated, s->eprop);
+    set_vec(ds.prop.face.data, ds.prop.face.size, ds.prop.face.allocated, s->fprop);
+    set_vec(ds.prop.hinge.data, ds.prop.hinge.size, ds.prop.hinge.allocated, s->hprop);
+    set_vec(ds.param_arrays.vertex.data, ds.param_arrays.vertex.size, ds.param_arrays.vertex.allocated, s->vparam);
+    set_vec(ds.param_arrays.edge.data, ds.param_arrays.edge.size, ds.param_arrays.edge.allocated, s->eparam);
+    set_vec(ds.param_arrays.face.data, ds.param_arrays.face.size, ds.param_arrays.face.allocated, s->fparam);
+    set_vec(ds.param_arrays.hinge.data, ds.param_arrays.hinge.size, ds.param_arrays.hinge.allocated, s->hparam);
+    set_vec(ds.inv_rest2x2.data, ds.inv_rest2x2.size, ds.inv_rest2x2.allocated, s->inv_rest);
+    set_vec(ds.constraint.fix.data, ds.constraint.fix.size, ds.constraint.fix.allocated, s->fix);
+    set_vec(ds.constraint.pull.data, ds.constraint.pull.size, ds.constraint.pull.allocated, s->pull);
+    set_vec(ds.constraint.sphere.data, ds.constraint.sphere.size, ds.constraint.sphere.allocated, s->spheres);
+    set_vec(ds.constraint.floor.data, ds.constraint.floor.size, ds.constraint.floor.allocated, s->floors);
+    s->fixed_table.fill(ds.fixed_index_table);
+    ds.transpose_table.data = s->transpose_data.empty() ? nullptr : s->transpose_data.data();
+    ds.transpose_table.offset = s->transpose_offset.data();
+    ds.transpose_table.size = n;
+    ds.transpose_table.nnz = (unsigned)s->transpose_data.size();
+    ds.transpose_table.nnz_allocated = ds.transpose_table.nnz;
+    ds.transpose_table.offset_allocated = n + 1;
+    ds.rod_count = 0;
+    ds.shell_face_count = nf;
+    ds.surface_vert_count = n;
+    set_vec(ds.face_hess_slots.data, ds.face_hess_slots.size, ds.face_hess_slots.allocated, s->face_slots);
+    set_vec(ds.hinge_hess_slots.data, ds.hinge_hess_slots.size, ds.hinge_hess_slots.allocated, s->hinge_slots);
+    s->built = true;
+    return 0;
+}
+
+PpfDataSet *ppf_scene_dataset(PpfScene *s) { return s->built ? &s->ds : nullptr; }
+PpfParamSet *ppf_scene_param(PpfScene *s) { return s->built ? &s->param : nullptr; }
+PpfConstraint *ppf_scene_constraint(PpfScene *s) {
+    return s->built ? &s->ds.constraint : nullptr;
+}
+
+void ppf_scene_set_pin_targets(PpfScene *s, const float *pos, const float *delta) {
+    for (size_t i = 0; i < s->fix.size(); ++i)
+        for (int d = 0; d < 3; ++d) {
+            s->fix[i].position.v[d] = pos[3 * i + d];
+            s->fix[i].step_delta.v[d] = delta ? delta[3 * i + d] : 0.0f;
+        }
+}
+
+} // extern "C"

@@ -5,4 +5,4 @@ include/ppf_gb300.h); this package builds it, binds it with ctypes, and
 generates the seeded synthetic scenes the tests and the benchmark run.
 """
 from . import build  # noqa: F401
-from ._lib import LibraryMissing, oracle, product, reference  # noqa: F401
+from ._lib import LibraryMissing, product  # noqa: F401

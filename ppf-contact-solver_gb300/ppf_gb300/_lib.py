@@ -1,7 +1,7 @@
-"""ctypes bindings of libppf_gb300.so (the product) and of the CPU oracle.
+"""ctypes binding of libppf_gb300.so.
 
-The product library must be present: every GPU entry point here goes through
-it, and a missing library raises instead of falling back to anything else.
+The library must be present: every entry point here goes through it, and a
+missing library raises instead of falling back to anything else.
 """
 from __future__ import annotations
 
@@ -14,8 +14,6 @@ import numpy as np
 from . import build as _build
 
 _PRODUCT = None
-_ORACLE = None
-_REF = None
 
 u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
 f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
@@ -57,31 +55,6 @@ def product() -> C.CDLL:
     return _PRODUCT
 
 
-def oracle() -> C.CDLL:
-    """The CPU oracle (test infrastructure)."""
-    global _ORACLE
-    if _ORACLE is None:
-        path = _build.ORACLE_LIB
-        if not path.exists():
-            _build.build_oracle()
-        lib = C.CDLL(str(path))
-        _declare_oracle(lib)
-        _ORACLE = lib
-    return _ORACLE
-
-
-def reference():
-    """The reference's own element math compiled from its sources, or None
-    where those sources are not available (e.g. on the GPU host)."""
-    global _REF
-    if _REF is None:
-        path = _build.REF_LIB
-        if not path.exists():
-            return None
-        _REF = C.CDLL(str(path))
-    return _REF
-
-
 def _declare_product(lib):
     lib.ppf_lbvh_build_host.restype = C.c_uint
     lib.ppf_lbvh_build_host.argtypes = [
@@ -94,18 +67,10 @@ def _declare_product(lib):
                                           C.c_int, C.c_void_p]
 
 
-def _declare_oracle(lib):
-    lib.oracle_lbvh_build.restype = C.c_uint
-    lib.oracle_lbvh_build.argtypes = [
-        C.c_int, f32p, f32p, C.c_uint, u32p_opt, C.c_uint, f32p, C.c_float,
-        u32p_opt, f32p_opt, u32p_opt]
-    lib.oracle_stable_sort.restype = None
-    lib.oracle_stable_sort.argtypes = [u32p, u32p, C.c_uint, C.c_int]
-
-
-def lbvh(lib, which: str, kind: int, x0, x1, prims, margin, extrapolate=1.0):
-    """Runs one LBVH build through `lib` ('product' or 'oracle' entry point)
-    and returns (root, node[2n-1, 2], box[2n-1, 8], keys[n])."""
+def lbvh(fn, kind: int, x0, x1, prims, margin, extrapolate=1.0):
+    """Runs one LBVH build through `fn`, a C function with the signature of
+    ppf_lbvh_build_host, and returns (root, node[2n-1, 2], box[2n-1, 8],
+    keys[n])."""
     x0 = np.ascontiguousarray(x0, np.float32).reshape(-1)
     x1 = np.ascontiguousarray(x1, np.float32).reshape(-1)
     n_verts = x0.size // 3
@@ -117,7 +82,6 @@ def lbvh(lib, which: str, kind: int, x0, x1, prims, margin, extrapolate=1.0):
     node = np.zeros(2 * nn, np.uint32)
     box = np.zeros(8 * nn, np.float32)
     keys = np.zeros(max(n, 1), np.uint32)
-    fn = lib.ppf_lbvh_build_host if which == "product" else lib.oracle_lbvh_build
     root = fn(kind, x0, x1, n_verts, prims, n, margin, np.float32(extrapolate),
               node, box, keys)
     return root, node.reshape(nn, 2), box.reshape(nn, 8), keys[:n]

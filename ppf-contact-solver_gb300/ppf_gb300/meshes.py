@@ -12,41 +12,32 @@ def grid(nx: int, ny: int, size_x: float = 1.0, size_y: float = 1.0):
     zs = np.linspace(-0.5 * size_y, 0.5 * size_y, ny, dtype=np.float64)
     X, Z = np.meshgrid(xs, zs, indexing="xy")  # [ny, nx]
     v = np.stack([X.ravel(), np.zeros(X.size), Z.ravel()], axis=1).astype(np.float32)
-    faces = []
-    for j in range(ny - 1):
-        for i in range(nx - 1):
-            a = j * nx + i
-            b = a + 1
-            c = a + nx
-            d = c + 1
-            if (i + j) % 2 == 0:
-                faces.append((a, c, b))
-                faces.append((b, c, d))
-            else:
-                faces.append((a, c, d))
-                faces.append((a, d, b))
-    return v, np.asarray(faces, np.uint32)
+    J, I = np.meshgrid(np.arange(ny - 1), np.arange(nx - 1), indexing="ij")
+    a = (J * nx + I).ravel()
+    b, c = a + 1, a + nx
+    d = c + 1
+    even = ((I + J) % 2 == 0).ravel()
+    t0 = np.where(even[:, None], np.stack([a, c, b], 1), np.stack([a, c, d], 1))
+    t1 = np.where(even[:, None], np.stack([b, c, d], 1), np.stack([a, d, b], 1))
+    faces = np.stack([t0, t1], 1).reshape(-1, 3)
+    return v, faces.astype(np.uint32)
 
 
 def tube(n_around: int, n_along: int, radius: float, length: float):
     """Open cylinder along x: n_around x n_along vertices."""
     th = np.linspace(0.0, 2.0 * np.pi, n_around, endpoint=False)
     xs = np.linspace(-0.5 * length, 0.5 * length, n_along)
-    v = np.zeros((n_along * n_around, 3), np.float64)
-    for j, x in enumerate(xs):
-        v[j * n_around:(j + 1) * n_around, 0] = x
-        v[j * n_around:(j + 1) * n_around, 1] = radius * np.cos(th)
-        v[j * n_around:(j + 1) * n_around, 2] = radius * np.sin(th)
-    faces = []
-    for j in range(n_along - 1):
-        for i in range(n_around):
-            a = j * n_around + i
-            b = j * n_around + (i + 1) % n_around
-            c = a + n_around
-            d = b + n_around
-            faces.append((a, c, b))
-            faces.append((b, c, d))
-    return v.astype(np.float32), np.asarray(faces, np.uint32)
+    v = np.zeros((n_along, n_around, 3), np.float64)
+    v[:, :, 0] = xs[:, None]
+    v[:, :, 1] = radius * np.cos(th)[None, :]
+    v[:, :, 2] = radius * np.sin(th)[None, :]
+    v = v.reshape(-1, 3)
+    J, I = np.meshgrid(np.arange(n_along - 1), np.arange(n_around), indexing="ij")
+    a = (J * n_around + I).ravel()
+    b = (J * n_around + (I + 1) % n_around).ravel()
+    c, d = a + n_around, b + n_around
+    faces = np.stack([np.stack([a, c, b], 1), np.stack([b, c, d], 1)], 1).reshape(-1, 3)
+    return v.astype(np.float32), faces.astype(np.uint32)
 
 
 def box(side: float, center=(0.0, 0.0, 0.0)):

@@ -32,21 +32,23 @@ def product_lib():
 
 @pytest.fixture(scope="session")
 def oracle_lib():
-    from ppf_gb300 import _lib, build
+    from oracle import binding
+    from ppf_gb300 import build
 
     build.build_oracle()
-    return _lib.oracle()
+    return binding.oracle()
 
 
 @pytest.fixture(scope="session")
 def ref_lib():
-    from ppf_gb300 import _lib, build
+    from oracle import binding
+    from ppf_gb300 import build
 
     try:
         build.build_reference()
     except Exception:
         pass
-    lib = _lib.reference()
+    lib = binding.reference()
     if lib is None:
         pytest.skip("reference sources not present on this host")
     return lib

@@ -30,5 +30,27 @@ def main():
     print("wrote", len(out), "arrays")
 
 
+
+
+def layout():
+    """Byte layout of the reference's data.hpp, for tests/test_abi_layout.py."""
+    import json
+
+    import abi_fields
+
+    cpp = Path("/root/reference/crates/ppf-cts-solver/src/cpp")
+    shim = [
+        "#include <algorithm>", "#include <cmath>",
+        "using std::max; using std::min; using std::isfinite;",
+        '#include "data.hpp"',
+        'extern "C" { unsigned char g_ppf_fatal_code = 0; char g_ppf_fatal_detail[512]; }',
+        'extern "C" void print_rust(const char *) {}',
+    ]
+    res = abi_fields.measure(shim, "", [str(cpp), "/usr/local/cuda/include"])
+    (Path(__file__).parent / "abi_layout.json").write_text(json.dumps(res, indent=0) + "\n")
+    print("wrote layout of", len(res), "fields")
+
+
 if __name__ == "__main__":
     main()
+    layout()

@@ -59,7 +59,7 @@ def test_oracle_lbvh_invariants(oracle_lib, rng, kind):
     v, f = _cloth(rng, 17, 13)
     n = _count(kind, v, f)
     margin = rng.uniform(1e-4, 1e-3, n).astype(np.float32)
-    root, node, box, keys = _lib.lbvh(oracle_lib, "oracle", kind, v, v,
+    root, node, box, keys = _lib.lbvh(oracle_lib.oracle_lbvh_build, kind, v, v,
                                       _prims(kind, f), margin)
     assert np.all(np.diff(keys.astype(np.int64)) >= 0)
     _check_tree(root, node, box, n)
@@ -110,8 +110,8 @@ def test_lbvh_bit_exact(product_lib, oracle_lib, rng, kind, shape):
     margin = rng.uniform(1e-4, 1e-3, n).astype(np.float32)
     v1 = v + rng.normal(0, 0.01, v.shape).astype(np.float32)
     p = _prims(kind, f)
-    a = _lib.lbvh(product_lib, "product", kind, v, v1, p, margin, 1.25)
-    b = _lib.lbvh(oracle_lib, "oracle", kind, v, v1, p, margin, 1.25)
+    a = _lib.lbvh(product_lib.ppf_lbvh_build_host, kind, v, v1, p, margin, 1.25)
+    b = _lib.lbvh(oracle_lib.oracle_lbvh_build, kind, v, v1, p, margin, 1.25)
     assert a[0] == b[0]
     assert np.array_equal(a[3], b[3]), "Morton codes / sort order differ"
     assert np.array_equal(a[1], b[1]), "node arrays differ"
@@ -126,8 +126,8 @@ def test_lbvh_duplicate_centroids(product_lib, oracle_lib):
     n = 1000
     v = np.zeros((n, 3), np.float32)
     margin = np.full(n, 5e-4, np.float32)
-    a = _lib.lbvh(product_lib, "product", 1, v, v, None, margin)
-    b = _lib.lbvh(oracle_lib, "oracle", 1, v, v, None, margin)
+    a = _lib.lbvh(product_lib.ppf_lbvh_build_host, 1, v, v, None, margin)
+    b = _lib.lbvh(oracle_lib.oracle_lbvh_build, 1, v, v, None, margin)
     assert np.array_equal(a[1], b[1])
     _check_tree(*a[:3], n)
 
@@ -138,7 +138,7 @@ def test_lbvh_large_face_tree(product_lib, oracle_lib, rng):
     v, f = meshes.grid(1024, 1024)
     v = v + rng.normal(0, 1e-3, v.shape).astype(np.float32)
     margin = np.full(len(f), 5e-4, np.float32)
-    a = _lib.lbvh(product_lib, "product", 3, v, v, f, margin)
-    b = _lib.lbvh(oracle_lib, "oracle", 3, v, v, f, margin)
+    a = _lib.lbvh(product_lib.ppf_lbvh_build_host, 3, v, v, f, margin)
+    b = _lib.lbvh(oracle_lib.oracle_lbvh_build, 3, v, v, f, margin)
     assert np.array_equal(a[1], b[1])
     assert np.array_equal(a[2].view(np.uint32), b[2].view(np.uint32))
