@@ -1,0 +1,384 @@
+"""Benchmark of the per-step contact solve on GB300.
+
+One bench "step" is one advance() of the solver: a full time step of the
+Newton loop (LBVH rebuild and refits, contact detection and assembly,
+block-Jacobi PCG, CCD and strain-limit line search) over the stacked-sheets
+workload: 8 cloth sheets of 128 x 128 vertices (131,072 vertices, 254,016
+triangles), seeded rotations and offsets, 2 cm apart above a fixed 0.6 m
+cube, dt = 0.01 s, from t = 0.
+
+Metric: Newton steps/s (Newton iterations completed / device time inside
+advance()), with PCG ms-to-tolerance (relative L1 residual 1e-3) per solve.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+* ours: W untimed steps, then the scene is re-initialized at t = 0 and K
+  steps are timed with CUDA events on the library's stream, the L2 flushed
+  (a 256 MiB write) before each step. `e2e` re-runs the same K steps from
+  t = 0 through the C ABI the reference's driver calls per frame
+  (update_constraint from host memory, advance, fetch to host memory), timed
+  on the host clock. The CPU oracle (an OpenMP restatement of the same step,
+  all host cores) is timed on the first steps of the same run as
+  `cpu_baseline`.
+* reference: the CPU restatement of the reference's step on the host cores,
+  on the same workload and metric; each step is one advance() and the run
+  stops after a bounded time.
+* N > 1 (torchrun): replicas only. Each rank steps its own copy of the
+  scene (seed = rank); value = Newton iterations of all ranks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "ppf-contact-solver_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Newton steps/s (block-Jacobi PCG to rel. residual 1e-3)"
+UNIT = "newton_iters/s"
+WORKLOAD = "stacked_sheets: 8 x 128x128 cloth sheets over a fixed 0.6 m cube"
+L2_FLUSH_BYTES = 256 << 20
+CPU_SAMPLE_SECONDS = 20.0
+REF_BUDGET_SECONDS = 150.0
+
+
+def _env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _bytes_per_iter(fixed_blocks: int, dyn_blocks: int, n: int) -> int:
+    """Algorithmic HBM bytes of one block-Jacobi PCG iteration: every unique
+    upper-triangle block once (36 B value + 4 B column), 4 B of row pointer
+    and 15 fp32 streams of 3 floats per vertex (SpMV: p in, Ap out; update:
+    p, Ap, x, r, P^-1 (3 vectors) in, x, r, z out; direction: z, p in, p
+    out), plus the scalar."""
+    return 40 * fixed_blocks + 40 * dyn_blocks + 184 * n + 4
+
+
+def build_scene(seed: int = 0):
+    from ppf_gb300 import scenes
+
+    return scenes.stacked_sheets(128, 8, seed=seed, dt=0.01)
+
+
+def run_ours(args, rank, local_rank, world):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from ppf_gb300 import abi
+    from ppf_gb300.session import Session
+
+    os.environ.setdefault("PPF_RETURN_ON_FATAL", "1")
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    sc, motion = build_scene(seed=rank)
+    curr0, prev0 = sc.positions()
+    param0 = abi.ParamSet.from_buffer_copy(sc.param.contents)
+
+    def restart():
+        sc.set_positions(curr0, prev0)
+        C.memmove(C.addressof(sc.param.contents), C.addressof(param0), C.sizeof(param0))
+        return Session(sc, motion)
+
+    s = restart()
+    lib = s.lib
+    for _ in range(args.warmup):
+        r = s.step(fetch=False)
+        if not r.success():
+            raise RuntimeError(f"warm-up step failed: {r.as_dict()}")
+
+    # ---- device-timed region -------------------------------------------------
+    s = restart()
+    stream = torch.cuda.ExternalStream(lib.ppf_stream())
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    newton = pcg_iters = 0
+    pcg_ms_all, pcg_iters_all, pcg_bytes, solve_bytes = [], [], 0, []
+    max_contacts = 0
+    sampler = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    launches0 = lib.ppf_kernel_launches()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ev[k][0].record(stream)
+        r = s.step(fetch=False)
+        ev[k][1].record(stream)
+        if not r.success():
+            raise RuntimeError(f"step {k} failed: {r.as_dict()}")
+        st = s.stats()
+        newton += st.newton_iters
+        pcg_iters += st.pcg_iters_total
+        max_contacts = max(max_contacts, st.max_contacts)
+        for i in range(min(st.pcg_solves, abi.STATS_MAX_SOLVES)):
+            b = _bytes_per_iter(st.fixed_blocks, st.dyn_blocks[i], st.vertices)
+            pcg_ms_all.append(st.pcg_ms[i])
+            pcg_iters_all.append(st.pcg_iters[i])
+            pcg_bytes += b * st.pcg_iters[i]
+            solve_bytes.append(b * st.pcg_iters[i])
+    torch.cuda.synchronize()
+    launches = int(lib.ppf_kernel_launches() - launches0)
+    clocks = sampler.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    # the flush runs between the events' predecessor and start: not timed
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        nt = torch.tensor([newton], device="cuda", dtype=torch.float64)
+        dist.all_reduce(nt)
+        newton_all = int(nt.item())
+    else:
+        newton_all = newton
+    value = newton_all / (total_ms / 1e3)
+
+    # ---- end to end through the C ABI, host buffers --------------------------
+    s = restart()
+    n = sc.vertex_count
+    # update_constraint uploads the fix pins (36 B each, PpfFixPair) and the
+    # scene's analytic colliders; fetch reads curr and prev back (12 B each)
+    h2d = sc.n_pins * 36 + sc.n_spheres * 32 + sc.n_floors * 40
+    d2h = 2 * 12 * n
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e2e_newton = 0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        lib.update_constraint(sc.constraint)
+        r = s.step(fetch=True)
+        if not r.success():
+            raise RuntimeError(f"e2e step {k} failed: {r.as_dict()}")
+        e2e_newton += s.stats().newton_iters
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = e2e_newton / e2e_s
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        nt = torch.tensor([e2e_newton], device="cuda", dtype=torch.float64)
+        dist.all_reduce(nt)
+        e2e_value = float(nt.item()) / float(t.item())
+
+    # ---- roofline of the dominant kernel (the persistent PCG) ----------------
+    peak, peak_kind = _peaks()
+    pcg_ms_total = sum(pcg_ms_all)
+    achieved = pcg_bytes / (pcg_ms_total / 1e3) / 1e9 if pcg_ms_total > 0 else 0.0
+    traffic = None
+    tfile = ROOT / "profiles" / "pcg_stacked_sheets_traffic.json"
+    if tfile.exists():
+        traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                "kernel": "k_pcg (persistent block-Jacobi PCG, one launch per solve)",
+                "peak_kind": peak_kind,
+                "bytes_per_launch_mean": (sum(solve_bytes) / len(solve_bytes)
+                                          if solve_bytes else 0)}
+    ms_solve = sorted(pcg_ms_all)
+
+    def pct(a, q):
+        return a[min(len(a) - 1, int(q * len(a)))] if a else None
+
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene generator)",
+        "config": {"workload": WORKLOAD, "vertices": n, "dt": 0.01,
+                   "time_steps": args.steps, "from": "t = 0 after a separate warm-up",
+                   "l2": "256 MiB flush before every timed step",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "pcg": {"solves": len(pcg_ms_all), "ms_to_tol_median": pct(ms_solve, 0.5),
+                "ms_to_tol_p90": pct(ms_solve, 0.9),
+                "iters_median": pct(sorted(pcg_iters_all), 0.5),
+                "iters_total": pcg_iters, "ms_total": round(pcg_ms_total, 3),
+                "share_of_step": round(pcg_ms_total / total_ms, 4) if total_ms else None},
+        "newton_iters": newton_all, "max_contacts": max_contacts,
+        "roofline": roofline,
+        "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "path": "update_constraint + advance + fetch (C ABI, host DataSet)"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(sc, curr0, prev0, param0, CPU_SAMPLE_SECONDS)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def _oracle_run(sc, curr0, prev0, param0, budget_s, max_steps=None, warmup=0):
+    """Steps the CPU oracle from t = 0 until the budget is spent (at least
+    one step); returns (newton_iters, seconds, steps)."""
+    import ctypes as C
+
+    from oracle.binding import OracleSession
+
+    sc.set_positions(curr0, prev0)
+    C.memmove(C.addressof(sc.param.contents), C.addressof(param0), C.sizeof(param0))
+    o = OracleSession(sc)
+    for _ in range(warmup):
+        o.step()
+    newton, secs, steps = 0, 0.0, 0
+    while True:
+        t = time.perf_counter()
+        r = o.step()
+        secs += time.perf_counter() - t
+        if not r.success():
+            raise RuntimeError(f"oracle step failed: {r.as_dict()}")
+        newton += o.stats()["newton_iters"]
+        steps += 1
+        if secs >= budget_s or (max_steps is not None and steps >= max_steps):
+            break
+    return newton, secs, steps
+
+
+def cpu_baseline(sc, curr0, prev0, param0, budget_s):
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    newton, secs, steps = _oracle_run(sc, curr0, prev0, param0, budget_s)
+    return {"value": round(newton / secs, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {steps} time steps of the same workload from t = 0 "
+                      f"({newton} Newton iterations, {secs:.1f} s), OpenMP oracle"}
+
+
+def run_reference(args, rank, local_rank, world):
+    if rank != 0:
+        return
+    from ppf_gb300 import abi
+
+    sc, _ = build_scene(seed=0)
+    curr0, prev0 = sc.positions()
+    param0 = abi.ParamSet.from_buffer_copy(sc.param.contents)
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    newton, secs, steps = _oracle_run(sc, curr0, prev0, param0, REF_BUDGET_SECONDS,
+                                      max_steps=args.steps, warmup=min(args.warmup, 1))
+    value = newton / secs
+    out = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT,
+        "n_gpus": world, "steps": steps, "warmup": min(args.warmup, 1),
+        "ms_per_step": round(1e3 * secs / steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene generator)",
+        "config": {"workload": WORKLOAD, "vertices": sc.vertex_count, "dt": 0.01,
+                   "time_steps": steps, "from": "t = 0"},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads,
+                         "kind": "port",
+                         "sample": f"first {steps} time steps from t = 0 ({newton} Newton "
+                                   f"iterations, {secs:.1f} s); the reference's GPU build "
+                                   "needs CUDA 12.8 and cargo, neither present"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    rank, local_rank, world = _env_rank()
+    if args.impl == "reference":
+        run_reference(args, rank, local_rank, world)
+    else:
+        run_ours(args, rank, local_rank, world)
+
+
+if __name__ == "__main__":
+    main()

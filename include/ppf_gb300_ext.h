@@ -64,8 +64,21 @@ typedef struct {
     float pcg_ms[PPF_STATS_MAX_SOLVES];
     unsigned pcg_iters[PPF_STATS_MAX_SOLVES];
     float toi[PPF_STATS_MAX_SOLVES];
+    /* sizes of the operator each solve ran on: unique upper-triangle blocks
+     * of the fixed pattern (diagonal included), vertices, and the unique
+     * contact blocks outside the pattern per solve */
+    unsigned fixed_blocks;
+    unsigned vertices;
+    unsigned dyn_blocks[PPF_STATS_MAX_SOLVES];
 } PpfStepStats;
 void ppf_step_stats(PpfStepStats *out);
+
+/* The CUDA stream (cudaStream_t, as void*) every kernel of advance() runs
+ * on, so a host can time the step with its own events on that stream. NULL
+ * before initialize(). */
+void *ppf_stream(void);
+/* Number of kernels this library has launched since it was loaded. */
+unsigned long long ppf_kernel_launches(void);
 
 /* ---- stage inspection (parity checks) -------------------------------------
  * Assembles and solves the first Newton system of a step at the current

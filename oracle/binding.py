@@ -60,6 +60,8 @@ def _declare(lib):
     lib.oracle_fetch.restype = None
     lib.oracle_fetch.argtypes = [f32p, f32p_opt]
     lib.oracle_time.restype = C.c_double
+    lib.oracle_check_intersection.restype = C.c_bool
+    lib.oracle_check_intersection.argtypes = [f32p]
     lib.oracle_update_constraint.argtypes = [P]
     lib.oracle_step_stats.argtypes = [C.POINTER(C.c_uint), C.POINTER(C.c_uint),
                                       C.POINTER(C.c_float)]
@@ -102,6 +104,11 @@ class OracleSession:
         prev = np.empty(3 * self.n, np.float32)
         self.lib.oracle_fetch(curr, prev)
         return curr.reshape(-1, 3), prev.reshape(-1, 3)
+
+    def intersection_free(self, x) -> bool:
+        """Independent intersection check of positions x (e.g. the GPU's)."""
+        return bool(self.lib.oracle_check_intersection(
+            np.ascontiguousarray(x, np.float32).reshape(-1)))
 
     def stats(self):
         a, b, c = C.c_uint(), C.c_uint(), C.c_float()

@@ -1191,6 +1191,15 @@ void oracle_fetch(float *curr, float *prev) {
 
 double oracle_time(void) { return g_oracle->prm.time; }
 
+// Intersection check of an arbitrary state of the initialized scene (trees
+// rebuilt at x): true when free of intersections.
+bool oracle_check_intersection(const float *x) {
+    Oracle &o = *g_oracle;
+    std::vector<float> xx(x, x + 3 * (size_t)o.n);
+    o.trees(xx, xx, 1.0f);
+    return o.intersection_free(xx);
+}
+
 void oracle_update_constraint(const PpfConstraint *c) { g_oracle->set_constraint(c); }
 
 void oracle_step_stats(unsigned *newton, unsigned *pcg_iters, float *step_ms) {

@@ -201,8 +201,15 @@ void ppf_step_stats(PpfStepStats *out) {
         out->pcg_ms[i] = s.pcg_ms[i];
         out->pcg_iters[i] = s.pcg_iters[i];
         out->toi[i] = i < s.toi.size() ? s.toi[i] : 0.0f;
+        out->dyn_blocks[i] = i < s.dyn_blocks.size() ? s.dyn_blocks[i] : 0u;
     }
+    out->fixed_blocks = solver_instance().fixed_blocks();
+    out->vertices = solver_instance().vertices();
 }
+
+void *ppf_stream(void) { return (void *)solver_instance().stream(); }
+
+unsigned long long ppf_kernel_launches(void) { return ppf::gpu::g_kernel_launches; }
 
 int ppf_debug_newton_system(float *dx, unsigned *iters, float *resid) {
     try {

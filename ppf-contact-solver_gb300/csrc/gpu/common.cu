@@ -22,6 +22,8 @@ void set_fatal(unsigned char code, const char *detail) {
 
 namespace gpu {
 
+unsigned long long g_kernel_launches = 0;
+
 void check_cuda(cudaError_t err, const char *what, const char *file, int line) {
     if (err == cudaSuccess) return;
     char buf[512];

@@ -30,9 +30,13 @@ enum StatusBits : unsigned {
 };
 
 void check_cuda(cudaError_t err, const char *what, const char *file, int line);
+// Kernels launched by this library since it was loaded (every launch site
+// ends in PPF_LAUNCH_CHECK or counts itself).
+extern unsigned long long g_kernel_launches;
 #define PPF_CUDA(x) ::ppf::gpu::check_cuda((x), #x, __FILE__, __LINE__)
-#define PPF_LAUNCH_CHECK() \
-    ::ppf::gpu::check_cuda(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
+#define PPF_LAUNCH_CHECK()                                                              \
+    (++::ppf::gpu::g_kernel_launches,                                                   \
+     ::ppf::gpu::check_cuda(cudaGetLastError(), "kernel launch", __FILE__, __LINE__))
 
 constexpr unsigned kNumSMs = 152; // GB300: 2 dies x 76 SMs
 

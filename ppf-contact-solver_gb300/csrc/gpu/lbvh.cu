@@ -300,6 +300,7 @@ void lbvh_build(Lbvh &bvh, const PrimSet &ps, const float *x_tree,
         bvh.root = 0;
     } else {
         k_init_bounds<<<1, 32, 0, s>>>(bvh.bounds.data());
+        PPF_LAUNCH_CHECK();
         k_bounds<<<grid, kBlock, 0, s>>>(ps.kind, ps.prims, x_tree, n,
                                          bvh.bounds.data());
         PPF_LAUNCH_CHECK();

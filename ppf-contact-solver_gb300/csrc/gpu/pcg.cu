@@ -368,6 +368,7 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     void *args[] = {(void *)&A, &x, &r, &z, &p, &Ap, &part, &bar, &tol, &max_iter, &res};
     PPF_CUDA(cudaLaunchCooperativeKernel((const void *)k_pcg, dim3(ws.grid), dim3(ws.threads),
                                          args, 0, q));
+    ++g_kernel_launches;
 }
 
 } // namespace gpu

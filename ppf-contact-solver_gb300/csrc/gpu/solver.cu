@@ -575,6 +575,9 @@ void Solver::assemble(float dt) {
             pairs_.cap_ee = (unsigned)ee_buf_.cap;
             PPF_CUDA(cudaMemsetAsync(&st_.data()->n_contact, 0, sizeof(unsigned), q_));
         }
+        if (counts[0] > pairs_.cap_pf || counts[1] > pairs_.cap_pe ||
+            counts[2] > pairs_.cap_pp || counts[3] > pairs_.cap_ee)
+            throw FatalError(4, "contact pair lists still overflow after growing them");
     }
     // contact blocks outside the fixed pattern
     unsigned long long keys = 6ull * counts[0] + 3ull * counts[1] + counts[2] + 6ull * counts[3];
@@ -681,6 +684,7 @@ PpfStepResult Solver::advance() {
         stats_.pcg_ms_total += pcg_ms;
         stats_.pcg_ms.push_back(pcg_ms);
         stats_.pcg_iters.push_back(st.pcg_iter);
+        stats_.dyn_blocks.push_back(st.n_dyn);
         stats_.max_contacts = std::max(stats_.max_contacts, st.n_contact);
         stats_.max_dyn_blocks = std::max(stats_.max_dyn_blocks, st.n_dyn);
         if (st.status & (STATUS_BVH_STACK_OVERFLOW | STATUS_BLOCK_OVERFLOW | STATUS_BAD_SLOT |

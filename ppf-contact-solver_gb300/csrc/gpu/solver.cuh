@@ -23,6 +23,7 @@ struct StepStats {
     std::vector<float> pcg_ms;        // per solve
     std::vector<unsigned> pcg_iters;  // per solve
     std::vector<float> toi;           // per Newton iteration
+    std::vector<unsigned> dyn_blocks; // per solve
 };
 
 class Solver {
@@ -43,6 +44,9 @@ class Solver {
     void set_active(const std::vector<unsigned char> &vert_active);
     unsigned fetch_intersection_records(PpfIntersectionRecord *out, unsigned max_count);
     const StepStats &stats() const { return stats_; }
+    cudaStream_t stream() const { return q_; }
+    unsigned fixed_blocks() const { return nnz_fixed_; }
+    unsigned vertices() const { return n_; }
     // debug views (host copies) for stage parity checks
     void debug_matrix(std::vector<unsigned> &f_off, std::vector<unsigned> &f_col,
                       std::vector<float> &f_val, std::vector<unsigned> &d_off,

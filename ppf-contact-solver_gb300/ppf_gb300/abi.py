@@ -103,6 +103,9 @@ class StepStats(C.Structure):
         ("pcg_ms", C.c_float * STATS_MAX_SOLVES),
         ("pcg_iters", C.c_uint * STATS_MAX_SOLVES),
         ("toi", C.c_float * STATS_MAX_SOLVES),
+        ("fixed_blocks", C.c_uint),
+        ("vertices", C.c_uint),
+        ("dyn_blocks", C.c_uint * STATS_MAX_SOLVES),
     ]
 
 

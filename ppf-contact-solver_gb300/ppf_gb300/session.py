@@ -73,6 +73,10 @@ def _declare(lib):
     lib.ppf_fatal_code.restype = C.c_ubyte
     lib.ppf_fatal_detail.restype = C.c_char_p
     lib.ppf_step_stats.argtypes = [C.POINTER(abi.StepStats)]
+    lib.ppf_stream.restype = C.c_void_p
+    lib.ppf_stream.argtypes = []
+    lib.ppf_kernel_launches.restype = C.c_ulonglong
+    lib.ppf_kernel_launches.argtypes = []
     lib.ppf_debug_newton_system.restype = C.c_int
     lib.ppf_debug_newton_system.argtypes = [_f32, C.POINTER(C.c_uint), C.POINTER(C.c_float)]
     lib.ppf_debug_system_sizes.argtypes = [_u32]
@@ -120,6 +124,8 @@ class Scene:
         _declare(self.lib)
         self.h = C.c_void_p(self.lib.ppf_scene_create())
         self.n_pins = 0
+        self.n_spheres = 0
+        self.n_floors = 0
         self.built = False
 
     def __del__(self):
@@ -154,11 +160,13 @@ class Scene:
         c = np.ascontiguousarray(center, np.float32)
         self.lib.ppf_scene_add_sphere(self.h, c, radius, contact_gap, friction,
                                       int(reverse), int(bowl))
+        self.n_spheres += 1
 
     def add_floor(self, ground, up=(0.0, 1.0, 0.0), contact_gap=1e-3, friction=0.0):
         self.lib.ppf_scene_add_floor(self.h, np.ascontiguousarray(ground, np.float32),
                                      np.ascontiguousarray(up, np.float32), contact_gap,
                                      friction)
+        self.n_floors += 1
 
     @property
     def vertex_count(self) -> int:

@@ -1,0 +1,73 @@
+"""Small seeded scenes for the step-level parity tests.
+
+Each returns (scene, pin_motion) like ppf_gb300.scenes, sized so the CPU
+oracle runs a step in well under a second.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from ppf_gb300 import meshes, scenes
+from ppf_gb300.session import Scene
+
+
+def two_sheets(side: int = 12, gap: float = 6e-4, seed: int = 3):
+    """Two sheets inside each other's contact gap at t = 0, the upper one
+    rotated and moving, the lower one pinned at two corners, over a floor
+    within reach: point-face, point-edge, point-point, edge-edge pairs, a
+    floor constraint and Dirichlet rows in the first Newton system."""
+    rng = np.random.default_rng(seed)
+    mat = scenes.cloth_material()
+    sc = Scene()
+    va, fa = meshes.grid(side, side, 0.4, 0.4)
+    va = va.astype(np.float64)
+    va[:, 1] = 0.5 + rng.uniform(-5e-5, 5e-5, len(va))
+    vb, fb = meshes.grid(side + 1, side - 1, 0.37, 0.41)
+    vb = vb.astype(np.float64)
+    c, s = math.cos(0.37), math.sin(0.37)
+    x, z = vb[:, 0].copy(), vb[:, 2].copy()
+    vb[:, 0] = c * x + s * z + 0.013
+    vb[:, 2] = -s * x + c * z - 0.007
+    vb[:, 1] = 0.5 + gap + rng.uniform(-5e-5, 5e-5, len(vb))
+    a0 = sc.add_shell(va.astype(np.float32), fa, mat)
+    b0 = sc.add_shell(vb.astype(np.float32), fb, mat)
+    # a small triangle just below sheet A, one corner under A's far corner
+    # (a point-point pair: neither projects into the other's interior)
+    corner = va[side * side - 1]
+    tri = np.array([[0.0, 0.0, 0.0], [0.05, 0.0, 0.01], [0.01, 0.0, 0.05]]) + corner
+    tri[:, 1] = corner[1] - gap
+    sc.add_shell(tri.astype(np.float32), np.array([[0, 2, 1]], np.uint32), mat)
+    n = sc.vertex_count
+    vel = np.zeros((n, 3), np.float32)
+    vel[b0:b0 + len(vb)] = (0.2, -0.3, 0.1)
+    sc.set_velocity(vel)
+    sc.pin([a0, a0 + side - 1])
+    sc.add_floor((0.0, 0.5 - 8e-4, 0.0), contact_gap=1e-3, friction=0.5)
+    return sc.build(scenes._param(0.01)), None
+
+
+def sheet_on_sphere(side: int = 20):
+    """cloth_sphere at a reduced size, lowered to just above the sphere."""
+    sc, mot = scenes.cloth_sphere(side)
+    return sc, mot
+
+
+def strain_of(x, rest, faces):
+    """Largest singular value of each face's deformation gradient relative to
+    its rest triangle (the quantity the 1% strain limit bounds)."""
+    x = np.asarray(x, np.float64)
+    rest = np.asarray(rest, np.float64)
+    f = np.asarray(faces, np.int64)
+    r1 = rest[f[:, 1]] - rest[f[:, 0]]
+    r2 = rest[f[:, 2]] - rest[f[:, 0]]
+    e1 = r1 / np.linalg.norm(r1, axis=1, keepdims=True)
+    nrm = np.cross(r1, r2)
+    e2 = np.cross(nrm, r1)
+    e2 /= np.linalg.norm(e2, axis=1, keepdims=True)
+    Dm = np.stack([np.stack([(e1 * r1).sum(1), (e2 * r1).sum(1)], 1),
+                   np.stack([(e1 * r2).sum(1), (e2 * r2).sum(1)], 1)], 2)  # [F,2,2] cols
+    Ds = np.stack([x[f[:, 1]] - x[f[:, 0]], x[f[:, 2]] - x[f[:, 0]]], 2)  # [F,3,2]
+    F = Ds @ np.linalg.inv(Dm)
+    return np.linalg.svd(F, compute_uv=False)[:, 0]

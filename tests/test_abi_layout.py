@@ -34,3 +34,34 @@ def test_library_exports_every_declared_symbol(product_lib):
     assert len(names) > 20
     missing = [n for n in sorted(names) if not hasattr(product_lib, n)]
     assert missing == []
+
+
+def test_ctypes_mirrors_match_headers():
+    """The Python-side ctypes structs have the C headers' byte layout."""
+    import ctypes
+    import subprocess
+    import tempfile
+
+    from ppf_gb300 import abi
+
+    lines = ['#include "ppf_gb300.h"', '#include "ppf_gb300_ext.h"',
+             '#include "ppf_gb300_scene.h"', "#include <cstdio>", "#include <cstddef>",
+             "int main() {"]
+    expect = {}
+    for cname, py in abi.MIRRORS.items():
+        lines.append(f'std::printf("{cname} %zu\\n", sizeof({cname}));')
+        expect[cname] = ctypes.sizeof(py)
+        for fname, _ in py._fields_:
+            key = f"{cname}.{fname}"
+            lines.append(f'std::printf("{key} %zu\\n", offsetof({cname}, {fname}));')
+            expect[key] = getattr(py, fname).offset
+    lines += ["return 0; }"]
+    with tempfile.TemporaryDirectory() as d:
+        src = Path(d) / "m.cpp"
+        exe = Path(d) / "m"
+        src.write_text("\n".join(lines) + "\n")
+        subprocess.run(["g++", "-std=c++17", f"-I{ROOT / 'include'}", str(src), "-o", str(exe)],
+                       check=True, capture_output=True)
+        out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    got = {k: int(v) for k, v in (line.split() for line in out.strip().splitlines())}
+    assert got == expect

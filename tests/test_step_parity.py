@@ -1,0 +1,173 @@
+"""GPU step parity against the CPU oracle, through the C ABI.
+
+* The first Newton system of a step with every contact kind active: the
+  contact pair sets are identical (same element math, same leaf boxes, same
+  rounding: the CUDA build uses -fmad=false, the oracle -ffp-contract=off);
+  the assembled blocks and right-hand side agree to fp32 summation-order
+  error (device atomics add in another order than the oracle's loops); the
+  PCG solution agrees to the solver's own 1e-3 relative-residual tolerance.
+* One full step (Newton loop, CCD line search, strain-limit line search)
+  from an identical state agrees within 1e-5 relative in positions.
+* Trajectories stay intersection-free (checked independently by the oracle)
+  and strain-limited (<= 1% + solver slack) on every frame.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import step_scenes
+from ppf_gb300 import scenes
+from ppf_gb300.session import Session
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def binding(oracle_lib, product_lib):
+    from oracle import binding
+
+    return binding
+
+
+def _sorted_rows(a):
+    a = np.asarray(a)
+    if len(a) == 0:
+        return a
+    order = np.lexsort(a.T[::-1])
+    return a[order]
+
+
+def _dyn_blocks(sysm):
+    rows = []
+    for i in range(len(sysm["d_off"]) - 1):
+        for k in range(sysm["d_off"][i], sysm["d_off"][i + 1]):
+            rows.append((i, int(sysm["d_col"][k]), k))
+    rows.sort()
+    idx = np.array([r[2] for r in rows], np.int64)
+    keys = np.array([(r[0], r[1]) for r in rows], np.int64).reshape(-1, 2)
+    return keys, sysm["d_val"][idx] if len(idx) else np.zeros((0, 9), np.float32)
+
+
+def test_first_newton_system_matches_oracle(binding, product_lib):
+    sc, _ = step_scenes.two_sheets()
+    n = sc.vertex_count
+    orc = binding.OracleSession(sc)
+    st_o, dx_o, it_o, rr_o = orc.newton_system()
+    so = orc.system()
+    Session(sc)  # initialize the product on the same DataSet
+    dx_g = np.empty(3 * n, np.float32)
+    it_g, rr_g = C.c_uint(), C.c_float()
+    st_g = product_lib.ppf_debug_newton_system(dx_g, C.byref(it_g), C.byref(rr_g))
+    sg = binding.product_system(product_lib, n)
+    # pair sets: bit-exact
+    for k in ("pf", "pe", "pp", "ee"):
+        assert len(so[k]) > 0, k
+        assert np.array_equal(_sorted_rows(sg[k]), _sorted_rows(so[k])), k
+    # fixed pattern identical, values to summation-order error
+    assert np.array_equal(sg["f_off"], so["f_off"])
+    assert np.array_equal(sg["f_col"], so["f_col"])
+    scale = np.abs(so["f_val"]).max()
+    assert np.allclose(sg["f_val"], so["f_val"], rtol=1e-5, atol=1e-6 * scale)
+    kg, vg = _dyn_blocks(sg)
+    ko, vo = _dyn_blocks(so)
+    assert np.array_equal(kg, ko)
+    assert np.allclose(vg, vo, rtol=1e-5, atol=1e-6 * scale)
+    assert np.allclose(sg["diag"], so["diag"], rtol=1e-6, atol=1e-6 * scale)
+    fscale = np.abs(so["force"]).max()
+    assert np.allclose(sg["force"], so["force"], rtol=1e-5, atol=1e-6 * fscale)
+    # linear solve: both converged to the 1e-3 relative L1 residual
+    assert st_g == 0 and st_o == 0
+    assert rr_g.value < 1e-3 and rr_o < 1e-3
+    # the GPU's solution solves the oracle's system to the solver tolerance:
+    # true L1 residual (float64) relative to the seeded residual
+    dxg = dx_g.reshape(-1, 3)
+    b = so["force"].astype(np.float64).reshape(-1)
+    r_g = b - _apply(so, dxg)
+    r_o = b - _apply(so, dx_o)
+    assert np.abs(r_g).sum() / np.abs(b).sum() < 2e-3, np.abs(r_g).sum() / np.abs(b).sum()
+    assert np.abs(r_o).sum() / np.abs(b).sum() < 2e-3
+    # and the two iterates differ by what that tolerance allows (the solves
+    # stop at different iterations: the check cadence sees rounding)
+    rel = np.linalg.norm(dxg - dx_o) / np.linalg.norm(dx_o)
+    assert rel < 2e-2, (rel, it_g.value, it_o)
+
+
+def _apply(sysm, v):
+    """y = A v in float64 for the kept system: the fixed upper pattern (with
+    the per-vertex diagonal folded in) and the contact blocks, each applied
+    with its transpose below the diagonal. Blocks are column-major."""
+    v = np.asarray(v, np.float64).reshape(-1, 3)
+    n = len(v)
+    y = np.zeros((n, 3))
+    for off, col, val in ((sysm["f_off"], sysm["f_col"], sysm["f_val"]),
+                          (sysm["d_off"], sysm["d_col"], sysm["d_val"])):
+        rows = np.repeat(np.arange(n), np.diff(off.astype(np.int64)))
+        cols = col.astype(np.int64)
+        B = val.astype(np.float64).reshape(-1, 3, 3).transpose(0, 2, 1)  # row-major
+        np.add.at(y, rows, np.einsum("kij,kj->ki", B, v[cols]))
+        lower = rows != cols
+        np.add.at(y, cols[lower], np.einsum("kji,kj->ki", B[lower], v[rows[lower]]))
+    return y.reshape(-1)
+
+
+def _step_from(sc, curr, prev, t, binding):
+    """One step of product and oracle from the same (curr, prev, time)."""
+    sc.set_positions(curr, prev)
+    sc.param.contents.time = t
+    s = Session(sc)
+    o = binding.OracleSession(sc)
+    rg = s.step()
+    ro = o.step()
+    return rg, ro, s.positions(), o.positions()[0]
+
+
+@pytest.mark.parametrize("warm", [0, 3])
+def test_one_step_from_identical_state(binding, warm):
+    sc, _ = step_scenes.two_sheets()
+    orc = binding.OracleSession(sc)
+    for _ in range(warm):
+        assert orc.step().success()
+    curr, prev = orc.positions()
+    x0 = curr.copy()
+    rg, ro, xg, xo = _step_from(sc, curr, prev, orc.time, binding)
+    assert rg.success() and ro.success(), (rg.as_dict(), ro.as_dict())
+    err = np.abs(xg - xo).max()
+    disp = np.abs(xo - x0).max()
+    assert err <= 1e-5 * np.abs(xo).max(), (err, disp)
+    # relative to the motion of the step the two differ by what the 1e-3
+    # relative PCG residual leaves in each Newton iteration
+    assert err <= 1e-2 * disp, (err, disp)
+
+
+def test_trajectory_cloth_sphere_invariants(binding):
+    sc, _ = scenes.cloth_sphere(24)
+    rest = sc.positions()[0].copy()
+    from ppf_gb300 import meshes
+
+    _, faces = meshes.grid(24, 24)
+    s = Session(sc)
+    checker = binding.OracleSession(sc)
+    for k in range(60):
+        r = s.step()
+        assert r.success(), (k, r.as_dict())
+        x = s.positions()
+        if k % 5 == 4:
+            assert checker.intersection_free(x), k
+            sig = step_scenes.strain_of(x, rest, faces)
+            assert sig.max() <= 1.01 + 1e-3, (k, sig.max())
+    # the cloth fell past the sphere's top without entering it
+    assert x[:, 1].max() < 0.31
+    assert np.linalg.norm(x, axis=1).min() >= 0.3 - 1e-6
+    st = s.stats()
+    assert st.newton_iters >= 2 and st.pcg_iters_total > 0
+
+
+def test_trajectory_matches_oracle_before_contact(binding):
+    sc, _ = scenes.cloth_sphere(16)
+    s = Session(sc)
+    o = binding.OracleSession(sc)
+    for k in range(20):
+        assert s.step().success() and o.step().success()
+    xg, xo = s.positions(), o.positions()[0]
+    assert np.abs(xg - xo).max() <= 1e-5 * np.abs(xo).max()
