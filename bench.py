@@ -176,7 +176,7 @@ def run_ours(args, rank, local_rank, world):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
     newton = pcg_iters = 0
-    pcg_ms_all, pcg_iters_all, pcg_bytes, solve_bytes = [], [], 0, []
+    pcg_ms_all, pcg_iters_all, pcg_bytes, solve_bytes, per_solve = [], [], 0, [], []
     max_contacts = 0
     sampler = ClockSampler(local_rank)
     if dist:
@@ -202,6 +202,8 @@ def run_ours(args, rank, local_rank, world):
             pcg_iters_all.append(st.pcg_iters[i])
             pcg_bytes += b * st.pcg_iters[i]
             solve_bytes.append(b * st.pcg_iters[i])
+            per_solve.append([k, int(st.pcg_iters[i]), round(float(st.pcg_ms[i]), 3),
+                              int(st.dyn_blocks[i])])
     torch.cuda.synchronize()
     launches = int(lib.ppf_kernel_launches() - launches0)
     clocks = sampler.stop()
@@ -280,7 +282,9 @@ def run_ours(args, rank, local_rank, world):
                 "ms_to_tol_p90": pct(ms_solve, 0.9),
                 "iters_median": pct(sorted(pcg_iters_all), 0.5),
                 "iters_total": pcg_iters, "ms_total": round(pcg_ms_total, 3),
-                "share_of_step": round(pcg_ms_total / total_ms, 4) if total_ms else None},
+                "share_of_step": round(pcg_ms_total / total_ms, 4) if total_ms else None,
+                "per_solve": {"fields": ["step", "iters", "ms", "contact_blocks"],
+                              "rows": per_solve[:64]}},
         "newton_iters": newton_all, "max_contacts": max_contacts,
         "roofline": roofline,
         "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": h2d,

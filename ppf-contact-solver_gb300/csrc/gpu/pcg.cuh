@@ -3,33 +3,46 @@
 // Restates crates/ppf-cts-solver/src/cpp/solver/solver.cu:
 //   block-Jacobi inverse (floored eigendecomposition)   357-400
 //   seeded residual r = b - A x0, L1 norm err0          1014-1035
-//   curvature verdict on p^T A p vs 256 eps sum|terms|  66-114
+//   curvature verdict on p^T A p vs 256 eps sum|terms|  66-114, 804-884
 //   recurrence, beta = rz1 / rz0, p = z + beta p        431-571, 1099-1169
 //   convergence err / err0 < tol, checked at iterations 1, 5, 9, ... and at
 //   every iteration once err / err0 < 8 tol             987-988, 1267-1379
 // as ONE persistent cooperative launch per solve: every scalar (alpha, beta,
 // the check schedule, the verdicts) is computed on the device by every block
 // from the same fixed-order reduction, and the host reads the result once.
+//
+// Operator layout (SELL-32): rows are cut into slices of 32; slice s owns
+// slots [off[s], off[s+1]); slot k of lane l holds one 3x3 block of row
+// 32 s + l with its column index. Values are stored entry-major per slot,
+// val[(slot * 9 + e) * 32 + lane] (e = column-major entry of the block), so
+// a warp reads each entry of 32 rows' blocks as one 128-byte line. Both
+// triangles are stored: row i carries A(i, j) for every j, so a row's
+// product needs no atomics and no transposed gathers. Unused slots hold a
+// zero block pointing at the row itself.
 #pragma once
+
+#include <vector>
 
 #include "scene.cuh"
 
 namespace ppf {
 namespace gpu {
 
-// A = fixed (upper + transpose table, diagonal blocks already include the
-// per-vertex diagonal C) + dynamic contact blocks (upper + transpose table).
+constexpr unsigned kSliceRows = 32;
+
+struct SellMatrix {
+    unsigned n_slices;
+    const unsigned *slice_off; // n_slices + 1, in slots
+    const unsigned *col;       // 32 per slot
+    const float *val;          // 9 x 32 per slot
+};
+
+// A = fixed part (elastic + inertia + per-vertex terms, diagonal included)
+// + contact part (blocks outside the fixed pattern).
 struct PcgOperator {
     unsigned n;
-    const unsigned *f_off, *f_col;
-    const float *f_val;
-    const unsigned *f_tr_off;
-    const uint2 *f_tr;
-    const unsigned *d_off, *d_col;
-    const float *d_val;
-    const unsigned *d_tr_off;
-    const uint2 *d_tr;
-    const float *inv_diag; // 9 per row
+    SellMatrix fixed, dyn;
+    const float *inv_diag; // block-Jacobi inverse, (slice * 9 + e) * 32 + lane
 };
 
 struct PcgResult {
@@ -43,7 +56,7 @@ struct PcgResult {
 };
 
 struct PcgWorkspace {
-    DevBuf<float> z, p, Ap;
+    DevBuf<float> z, p0, p1, Ap;
     DevBuf<float> partials;
     DevBuf<unsigned> barrier;
     DevBuf<PcgResult> result;
@@ -51,17 +64,43 @@ struct PcgWorkspace {
     void reserve(unsigned n);
 };
 
-// Diagonal block inverse per row: inv(B(i,i)) with C already folded in.
-void launch_block_jacobi(const PcgOperator &A, const unsigned *diag_slot,
+// ---- SELL layouts ------------------------------------------------------------
+// Fixed part: the slot of every (row, block) is static per scene. `src` maps a
+// (slot, lane) to the upper-triangle block it copies (bit 31: transposed),
+// or 0xffffffff for padding.
+struct SellLayout {
+    DevBuf<unsigned> slice_off, col, src;
+    DevBuf<float> val;
+    unsigned n_slices = 0, slots = 0;
+};
+
+// Host construction of the fixed layout from the upper pattern and its
+// transpose table (row, upper slot) per row.
+void sell_build_fixed(unsigned n, const std::vector<unsigned> &off,
+                      const std::vector<unsigned> &col, const std::vector<unsigned> &tr_off,
+                      const std::vector<uint2> &tr, SellLayout &out);
+// Copies the assembled upper blocks into the fixed layout.
+void sell_pack_fixed(SellLayout &L, const float *upper_val, cudaStream_t q);
+// Contact part, rebuilt per Newton iteration from the deduplicated upper CSR
+// (off, col, val) and its transpose list (tr_off, tr), leaving out the blocks
+// of Dirichlet vertices (dof_mask, zero after elimination). Reads the slot
+// total back to the host (one synchronization) to size the layout.
+void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const float *val,
+                    const unsigned *tr_off, const uint2 *tr, const unsigned *dof_mask,
+                    SellLayout &out, DevBuf<unsigned> &slice_k, DevBuf<unsigned> &scan_tmp,
+                    cudaStream_t q);
+inline SellMatrix sell_view(const SellLayout &L) {
+    return SellMatrix{L.n_slices, L.slice_off.data(), L.col.data(), L.val.data()};
+}
+
+// Diagonal block inverse per row: inv(B(i,i)), written in the slice layout.
+void launch_block_jacobi(unsigned n, const float *upper_val, const unsigned *diag_slot,
                          float *inv_diag, unsigned *d_status, cudaStream_t q);
 
 // Solves A x = b starting from x (b in r on entry; r is overwritten).
 // Writes the result into ws.result (device) and returns immediately.
 void launch_pcg(const PcgOperator &A, float *x, float *r, float tol,
                 unsigned max_iter, PcgWorkspace &ws, cudaStream_t q);
-
-// y = A x (one SpMV, for checks).
-void launch_spmv(const PcgOperator &A, const float *x, float *y, cudaStream_t q);
 
 } // namespace gpu
 } // namespace ppf

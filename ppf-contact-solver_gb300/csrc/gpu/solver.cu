@@ -251,20 +251,7 @@ AssemblyBuffers Solver::abuf() {
 }
 
 PcgOperator Solver::pcg_operator() const {
-    PcgOperator A{};
-    A.n = n_;
-    A.f_off = fixed_off_.data();
-    A.f_col = fixed_col_.data();
-    A.f_val = fixed_val_.data();
-    A.f_tr_off = fixed_tr_off_.data();
-    A.f_tr = fixed_tr_.data();
-    A.d_off = dyn_.off;
-    A.d_col = dyn_.col;
-    A.d_val = dyn_.val;
-    A.d_tr_off = dyn_.tr_off;
-    A.d_tr = dyn_.tr;
-    A.inv_diag = inv_diag_.data();
-    return A;
+    return PcgOperator{n_, sell_view(fixed_sell_), sell_view(dyn_sell_), inv_diag_.data()};
 }
 
 BvhView Solver::view(const Lbvh &b) const {
@@ -336,6 +323,7 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     for (unsigned k = 0; k < toff[n_]; ++k) tr[k] = make_uint2(tt.data[k].v[0], tt.data[k].v[1]);
     upload(fixed_tr_off_, toff);
     upload(fixed_tr_, tr);
+    sell_build_fixed(n_, foff, fcol, toff, tr, fixed_sell_);
     auto slot_of = [&](unsigned i, unsigned j) -> unsigned {
         if (i > j) return kSentinel;
         auto b = fcol.begin() + foff[i], e = fcol.begin() + foff[i + 1];
@@ -391,7 +379,7 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     dx_.reserve(n3);
     r_.reserve(n3);
     diag_.reserve(9 * (size_t)n_);
-    inv_diag_.reserve(9 * (size_t)n_);
+    inv_diag_.reserve(9 * (size_t)fixed_sell_.n_slices * kSliceRows);
     fixed_val_.reserve(9 * (size_t)nnz_fixed_);
     fixed_tmp_.reserve(9 * (size_t)nnz_fixed_);
     st_.reserve(1);
@@ -608,6 +596,12 @@ void Solver::assemble(float dt) {
     k_fold_diag<<<div_up(n_, kB), kB, 0, q_>>>(n_, fixed_diag_.data(), diag_.data(),
                                               fixed_val_.data());
     PPF_LAUNCH_CHECK();
+    // the operator in the PCG's slice layout, and its block-Jacobi inverse
+    sell_pack_fixed(fixed_sell_, fixed_val_.data(), q_);
+    sell_build_dyn(n_, dyn_.off, dyn_.col, dyn_.val, dyn_.tr_off, dyn_.tr, dof_mask_.data(),
+                   dyn_sell_, dyn_slice_k_, dyn_scan_tmp_, q_);
+    launch_block_jacobi(n_, fixed_val_.data(), fixed_diag_.data(), inv_diag_.data(),
+                        &st_.data()->status, q_);
 }
 
 PpfStepResult Solver::advance() {
@@ -648,7 +642,6 @@ PpfStepResult Solver::advance() {
         PPF_CUDA(cudaMemcpyAsync(r_.data(), force_.data(), n3 * sizeof(float),
                                  cudaMemcpyDeviceToDevice, q_));
         PcgOperator A = pcg_operator();
-        launch_block_jacobi(A, fixed_diag_.data(), inv_diag_.data(), &st_.data()->status, q_);
         PPF_CUDA(cudaEventRecord(ev0_, q_));
         launch_pcg(A, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_);
         PPF_CUDA(cudaEventRecord(ev1_, q_));
@@ -880,7 +873,6 @@ int Solver::debug_assemble_solve(std::vector<float> &dx, unsigned &iters, float 
     PPF_CUDA(cudaMemcpyAsync(r_.data(), force_.data(), n3 * sizeof(float),
                              cudaMemcpyDeviceToDevice, q_));
     PcgOperator A = pcg_operator();
-    launch_block_jacobi(A, fixed_diag_.data(), inv_diag_.data(), &st_.data()->status, q_);
     launch_pcg(A, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_);
     PcgResult res;
     PPF_CUDA(cudaMemcpyAsync(&res, pcg_.result.data(), sizeof(PcgResult), cudaMemcpyDeviceToHost, q_));

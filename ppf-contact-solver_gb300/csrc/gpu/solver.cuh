@@ -119,6 +119,8 @@ class Solver {
     DevBuf<float> dval_buf_;
     DevBuf<unsigned> scan_tmp_;
     PcgWorkspace pcg_;
+    SellLayout fixed_sell_, dyn_sell_;
+    DevBuf<unsigned> dyn_slice_k_, dyn_scan_tmp_;
     DevBuf<IterStatus> st_;
     IterStatus *st_host_ = nullptr;
     DevBuf<float> rescale_;
