@@ -254,8 +254,17 @@ void Oracle::compute_target(float dt) {
     }
 }
 
-// Contact pair detection over the trees (contact.cu:1398-1787, stage 0).
+// Query widening of the proximity search: the trees hold tight boxes at x;
+// the guard keeps fp32 rounding of the box corners from dropping a pair at
+// the distance threshold (the distance test alone decides acceptance).
+static float detect_guard(const Vec3 &p) {
+    return 1e-6f * (1.0f + std::fmax(std::fmax(std::fabs(p[0]), std::fabs(p[1])), std::fabs(p[2])));
+}
+
+// Contact pair detection over trees of tight boxes at x
+// (contact.cu:1398-1787, stage 0).
 void Oracle::detect() {
+    trees(x, x, 1.0f);
     pf.clear();
     pe.clear();
     pp.clear();
@@ -265,7 +274,7 @@ void Oracle::detect() {
     for (long long vi = 0; vi < (long long)nsurf; ++vi) {
         unsigned v = (unsigned)vi;
         Vec3 p = X(x, v);
-        float m = margin_v[v];
+        float m = margin_v[v] + detect_guard(p);
         float q[8] = {p[0] - m, p[1] - m, p[2] - m, 1.0f, p[0] + m, p[1] + m, p[2] + m, 0.0f};
         const PpfVertexParam &vp = vparam[vprop[v].param_index];
         query(tf, q, [&](unsigned fi) {
@@ -357,7 +366,7 @@ void Oracle::detect() {
         unsigned ei = (unsigned)eii;
         const unsigned *a = &edge[2 * ei];
         Vec3 pa = X(x, a[0]), pb = X(x, a[1]);
-        float m = margin_e[ei];
+        float m = margin_e[ei] + std::fmax(detect_guard(pa), detect_guard(pb));
         float q[8] = {std::fmin(pa[0], pb[0]) - m, std::fmin(pa[1], pb[1]) - m,
                       std::fmin(pa[2], pb[2]) - m, 1.0f, std::fmax(pa[0], pb[0]) + m,
                       std::fmax(pa[1], pb[1]) + m, std::fmax(pa[2], pb[2]) + m, 0.0f};

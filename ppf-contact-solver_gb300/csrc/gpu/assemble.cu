@@ -199,6 +199,16 @@ __global__ void k_strain_limit(Scene s, StepParams p, AssemblyBuffers b) {
 }
 
 // ---- contact detection (contact.cu:1398-1787, stage 0) ----------------------
+// The trees are refit to tight boxes at the evaluated positions before this
+// runs (the reference queries the swept boxes left by the last line search).
+// A pair passes the distance test only if its tight boxes overlap in exact
+// arithmetic; the query is widened by this guard so fp32 rounding of the box
+// corners cannot drop a pair at the threshold. The accepted set is decided by
+// the distance test alone, as in the reference.
+__device__ __forceinline__ float detect_guard(const Vec3 &p) {
+    return 1e-6f * (1.0f + fmaxf(fmaxf(fabsf(p[0]), fabsf(p[1])), fabsf(p[2])));
+}
+
 __device__ __forceinline__ unsigned push_pair(unsigned *ctr, unsigned cap) {
     unsigned slot = atomicAdd(ctr, 1u);
     return slot < cap ? slot : kSentinel;
@@ -245,8 +255,8 @@ __global__ void k_detect_vertex(Scene s, BvhView fb, BvhView eb, BvhView vb,
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= s.n_surf) return;
     unsigned v = vb.node[t].x - 1u; // Morton order of the vertex tree
-    float m = s.margin_vert[v];
     Vec3 p = X(x, v);
+    float m = s.margin_vert[v] + detect_guard(p);
     float4 qmin = make_float4(p[0] - m, p[1] - m, p[2] - m, 1.0f);
     float4 qmax = make_float4(p[0] + m, p[1] + m, p[2] + m, 0.0f);
     VertexQueryOp op{s, x, v, 0, pl, st, 0u};
@@ -280,8 +290,8 @@ __global__ void k_detect_edge(Scene s, BvhView eb, const float *x, PairLists pl,
     if (t >= s.ne) return;
     unsigned e = eb.node[t].x - 1u;
     const unsigned *ed = s.edge + 2 * e;
-    float m = s.margin_edge[e];
     Vec3 a = X(x, ed[0]), c = X(x, ed[1]);
+    float m = s.margin_edge[e] + fmaxf(detect_guard(a), detect_guard(c));
     float4 qmin = make_float4(fminf(a[0], c[0]) - m, fminf(a[1], c[1]) - m,
                               fminf(a[2], c[2]) - m, 1.0f);
     float4 qmax = make_float4(fmaxf(a[0], c[0]) + m, fmaxf(a[1], c[1]) + m,

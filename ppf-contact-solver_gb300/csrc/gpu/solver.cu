@@ -537,6 +537,8 @@ void Solver::assemble(float dt) {
     launch_strain_limit(s, p, b, q_);
     unsigned counts[4] = {0, 0, 0, 0};
     if (!param->disable_contact) {
+        // tight boxes at the evaluated positions for the proximity queries
+        build_trees(eval_x_.data(), eval_x_.data(), 1.0f, false);
         for (int attempt = 0; attempt < 3; ++attempt) {
             PPF_CUDA(cudaMemsetAsync(st_.data(), 0, 4 * sizeof(unsigned), q_));
             launch_detect(s, view(bvh_face_), view(bvh_edge_), view(bvh_vert_), b, pairs_, q_);
