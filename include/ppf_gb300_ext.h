@@ -48,6 +48,27 @@ int ppf_radix_sort_host(unsigned *keys, unsigned *vals, unsigned n,
 int ppf_radix_sort_device(unsigned *d_keys, unsigned *d_vals, unsigned n,
                           int key_bits, void *stream);
 
+/* The same sort with no allocation at all. It has no counterpart in the
+ * reference. Its scratch (two ping-pong arrays, look-back words, histograms,
+ * counters) lives in static device arrays sized for at most
+ * PPF_NOALLOC_SORT_MAX_PAIRS pairs (about 8.5 MB per device), and neither the
+ * call nor its first use on a device allocates memory. It is for callers that
+ * must not allocate: a per-frame loop where a cudaMalloc / cudaFree would
+ * synchronize the device, or a host whose allocator owns the device memory.
+ *   - n > PPF_NOALLOC_SORT_MAX_PAIRS: returns -2, prints one line to stderr
+ *     and touches nothing.
+ *   - The first call on each device looks up the scratch addresses
+ *     (cudaGetSymbolAddress) with that device current; make it before any
+ *     stream capture begins.
+ *   - Every call resets the histograms, counters and look-back words it uses
+ *     on `stream`; nothing needs zeroing by the caller.
+ *   - There is one scratch set per device: calls that overlap in time (on any
+ *     streams) race on it, so the caller orders them.
+ * Asynchronous on `stream`: the result is ready once the stream is. */
+#define PPF_NOALLOC_SORT_MAX_PAIRS (1u << 20)
+int ppf_radix_sort_device_noalloc(unsigned *d_keys, unsigned *d_vals,
+                                  unsigned n, int key_bits, void *stream);
+
 /* ---- per-step statistics ------------------------------------------------
  * The reference logs these per step through SimpleLog channels (newton_steps,
  * pcg_iter, pcg_linsolve, toi: crates/ppf-cts-solver/src/cpp/main/main.cu:

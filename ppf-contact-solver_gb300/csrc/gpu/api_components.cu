@@ -127,6 +127,24 @@ extern "C" int ppf_radix_sort_host(unsigned *keys, unsigned *vals, unsigned n,
     }
 }
 
+static_assert(ppf::gpu::kNoAllocMaxPairs == PPF_NOALLOC_SORT_MAX_PAIRS,
+              "static sort scratch and the header limit must agree");
+
+extern "C" int ppf_radix_sort_device_noalloc(unsigned *d_keys, unsigned *d_vals,
+                                             unsigned n, int key_bits, void *stream) {
+    try {
+        int rc = radix_sort_pairs_noalloc(d_keys, d_vals, n, key_bits, (cudaStream_t)stream);
+        if (rc == -2)
+            fprintf(stderr,
+                    "[ppf_gb300] ppf_radix_sort_device_noalloc: %u pairs exceed the static "
+                    "scratch capacity of %u pairs; nothing was sorted\n",
+                    n, PPF_NOALLOC_SORT_MAX_PAIRS);
+        return rc;
+    } catch (const FatalError &e) {
+        return report(e);
+    }
+}
+
 extern "C" int ppf_radix_sort_device(unsigned *d_keys, unsigned *d_vals,
                                      unsigned n, int key_bits, void *stream) {
     try {

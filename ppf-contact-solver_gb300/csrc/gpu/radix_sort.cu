@@ -1,4 +1,5 @@
 // radix_sort.cu -- onesweep stable LSD radix sort, 8-bit digits.
+#include "fatal.cuh"
 #include "radix_sort.cuh"
 
 namespace ppf {
@@ -220,6 +221,102 @@ void radix_sort_pairs(unsigned *keys, unsigned *vals, unsigned n, int key_bits,
         PPF_CUDA(cudaMemcpyAsync(vals, src_v, n * sizeof(unsigned),
                                  cudaMemcpyDeviceToDevice, stream));
     }
+}
+
+} // namespace gpu
+} // namespace ppf
+
+// ---- allocation-free variant ------------------------------------------------
+// The same sort with its scratch in file-scope device arrays of a fixed
+// capacity, so a call allocates nothing. One scratch set exists per device:
+// calls that overlap in time on any streams race on it and must be ordered
+// by the caller.
+namespace ppf {
+namespace gpu {
+
+namespace {
+
+constexpr unsigned kNoAllocTiles = (kNoAllocMaxPairs + kSortTile - 1) / kSortTile;
+
+__device__ __align__(256) unsigned g_na_keys[kNoAllocMaxPairs];
+__device__ __align__(256) unsigned g_na_vals[kNoAllocMaxPairs];
+__device__ __align__(256) unsigned g_na_lookback[kNoAllocTiles * kRadix];
+__device__ __align__(256) unsigned g_na_hist[4 * kRadix];
+__device__ __align__(256) unsigned g_na_ctr[4];
+__device__ __align__(256) unsigned g_na_status[1];
+
+struct NoAllocScratch {
+    unsigned *keys = nullptr, *vals = nullptr, *lookback = nullptr;
+    unsigned *hist = nullptr, *ctr = nullptr, *status = nullptr;
+    bool ready = false;
+};
+constexpr int kMaxDevices = 64;
+NoAllocScratch g_na[kMaxDevices];
+
+template <class T> void symbol_address(unsigned **out, const T &sym) {
+    PPF_CUDA(cudaGetSymbolAddress((void **)out, sym));
+}
+
+// Device addresses of the scratch arrays for the current device, looked up
+// once per device.
+const NoAllocScratch &noalloc_scratch() {
+    int dev = 0;
+    PPF_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) throw FatalError(3, "device ordinal out of range");
+    NoAllocScratch &s = g_na[dev];
+    if (!s.ready) {
+        symbol_address(&s.keys, g_na_keys);
+        symbol_address(&s.vals, g_na_vals);
+        symbol_address(&s.lookback, g_na_lookback);
+        symbol_address(&s.hist, g_na_hist);
+        symbol_address(&s.ctr, g_na_ctr);
+        symbol_address(&s.status, g_na_status);
+        s.ready = true;
+    }
+    return s;
+}
+
+} // namespace
+
+int radix_sort_pairs_noalloc(unsigned *keys, unsigned *vals, unsigned n, int key_bits,
+                             cudaStream_t stream) {
+    if (n > kNoAllocMaxPairs) return -2;
+    if (n <= 1 || key_bits <= 0) return 0;
+    const NoAllocScratch &s = noalloc_scratch();
+    int passes = (key_bits + 7) / 8;
+    if (passes > 4) passes = 4;
+    const unsigned tiles = div_up(n, kSortTile);
+    // the histograms, tile counters and status start at zero every call; the
+    // look-back words start at zero every pass
+    PPF_CUDA(cudaMemsetAsync(s.hist, 0, 4 * kRadix * sizeof(unsigned), stream));
+    PPF_CUDA(cudaMemsetAsync(s.ctr, 0, 4 * sizeof(unsigned), stream));
+    PPF_CUDA(cudaMemsetAsync(s.status, 0, sizeof(unsigned), stream));
+    unsigned hgrid = tiles < 4 * kNumSMs ? tiles : 4 * kNumSMs;
+    k_digit_histograms<<<hgrid, 256, 0, stream>>>(keys, n, passes, s.hist);
+    PPF_LAUNCH_CHECK();
+    k_scan_histograms<<<passes, kRadix, 0, stream>>>(s.hist);
+    PPF_LAUNCH_CHECK();
+    unsigned *src_k = keys, *src_v = vals, *dst_k = s.keys, *dst_v = s.vals;
+    for (int p = 0; p < passes; ++p) {
+        PPF_CUDA(cudaMemsetAsync(s.lookback, 0, (size_t)tiles * kRadix * sizeof(unsigned),
+                                 stream));
+        k_onesweep_pass<<<tiles, kSortThreads, 0, stream>>>(src_k, src_v, dst_k, dst_v, n,
+                                                           8 * p, s.hist + p * kRadix,
+                                                           s.lookback, s.ctr + p, s.status);
+        PPF_LAUNCH_CHECK();
+        unsigned *tk = src_k, *tv = src_v;
+        src_k = dst_k;
+        src_v = dst_v;
+        dst_k = tk;
+        dst_v = tv;
+    }
+    if (src_k != keys) {
+        PPF_CUDA(cudaMemcpyAsync(keys, src_k, n * sizeof(unsigned), cudaMemcpyDeviceToDevice,
+                                 stream));
+        PPF_CUDA(cudaMemcpyAsync(vals, src_v, n * sizeof(unsigned), cudaMemcpyDeviceToDevice,
+                                 stream));
+    }
+    return 0;
 }
 
 } // namespace gpu

@@ -34,5 +34,11 @@ void radix_sort_pairs(unsigned *keys, unsigned *vals, unsigned n, int key_bits,
                       RadixSortWorkspace &ws, unsigned *d_status,
                       cudaStream_t stream);
 
+// The same sort with fixed-capacity static device scratch: allocates nothing.
+// Returns -2 (and touches nothing) when n exceeds kNoAllocMaxPairs.
+constexpr unsigned kNoAllocMaxPairs = 1u << 20;
+int radix_sort_pairs_noalloc(unsigned *keys, unsigned *vals, unsigned n, int key_bits,
+                             cudaStream_t stream);
+
 } // namespace gpu
 } // namespace ppf
