@@ -284,21 +284,52 @@ struct EdgeQueryOp {
     }
 };
 
+// One work item per edge piece (edges in the tree's Morton order).
 __global__ void k_detect_edge(Scene s, BvhView eb, const float *x, PairLists pl,
-                              IterStatus *st) {
+                              IterStatus *st, EdgePieces ep) {
+    const unsigned total = ep.off[ep.n];
+    for (unsigned item = blockIdx.x * blockDim.x + threadIdx.x; item < total;
+         item += gridDim.x * blockDim.x) {
+        const unsigned t = piece_slot(ep, item);
+        const unsigned k = item - ep.off[t], K = ep.off[t + 1] - ep.off[t];
+        const unsigned e = eb.node[t].x - 1u;
+        const unsigned *ed = s.edge + 2 * e;
+        Vec3 a = X(x, ed[0]), c = X(x, ed[1]);
+        float m = s.margin_edge[e] + fmaxf(detect_guard(a), detect_guard(c));
+        float4 qmin, qmax;
+        seg_box(piece_point(a, c, k, K), piece_point(a, c, k + 1, K), m, qmin, qmax);
+        EdgeQueryOp op{s, x, e, pl, st, 0u};
+        if (k == 0u) {
+            bvh_query(eb, qmin, qmax, op, &st->status);
+        } else {
+            float4 xmin, xmax;
+            seg_box(piece_point(a, c, k - 1, K), piece_point(a, c, k, K), m, xmin, xmax);
+            bvh_query(eb, qmin, qmax, op, &st->status, &xmin, &xmax);
+        }
+        if (op.found) atomicAdd(&st->n_contact, op.found);
+    }
+}
+
+// Piece counts of every edge (tree order) for a query over positions x, or
+// over the sweep x -> x + t (x1 - x) when x1 is given (t read from t_bits).
+__global__ void k_edge_piece_count(unsigned ne, const uint2 *node, const unsigned *edge,
+                                   const float *x, const float *x1, const unsigned *t_bits,
+                                   float piece_len, unsigned *count) {
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= s.ne) return;
-    unsigned e = eb.node[t].x - 1u;
-    const unsigned *ed = s.edge + 2 * e;
-    Vec3 a = X(x, ed[0]), c = X(x, ed[1]);
-    float m = s.margin_edge[e] + fmaxf(detect_guard(a), detect_guard(c));
-    float4 qmin = make_float4(fminf(a[0], c[0]) - m, fminf(a[1], c[1]) - m,
-                              fminf(a[2], c[2]) - m, 1.0f);
-    float4 qmax = make_float4(fmaxf(a[0], c[0]) + m, fmaxf(a[1], c[1]) + m,
-                              fmaxf(a[2], c[2]) + m, 0.0f);
-    EdgeQueryOp op{s, x, e, pl, st, 0u};
-    bvh_query(eb, qmin, qmax, op, &st->status);
-    if (op.found) atomicAdd(&st->n_contact, op.found);
+    if (t >= ne) return;
+    const unsigned e = node[t].x - 1u;
+    const unsigned *ed = edge + 2 * e;
+    Vec3 a = X(x, ed[0]), b = X(x, ed[1]);
+    float len = (b - a).norm();
+    if (x1) {
+        const float tt = __uint_as_float(*t_bits);
+        Vec3 a1 = vec3(fmaf(tt, x1[3 * ed[0]] - a[0], a[0]), fmaf(tt, x1[3 * ed[0] + 1] - a[1], a[1]),
+                       fmaf(tt, x1[3 * ed[0] + 2] - a[2], a[2]));
+        Vec3 b1 = vec3(fmaf(tt, x1[3 * ed[1]] - b[0], b[0]), fmaf(tt, x1[3 * ed[1] + 1] - b[1], b[1]),
+                       fmaf(tt, x1[3 * ed[1] + 2] - b[2], b[2]));
+        len = fmaxf(len, (b1 - a1).norm());
+    }
+    count[t] = piece_count(len, piece_len);
 }
 
 // ---- dynamic contact blocks: hash dedupe + CSR layout ----------------------
@@ -739,15 +770,28 @@ void launch_strain_limit(const Scene &s, const StepParams &p, const AssemblyBuff
     PPF_LAUNCH_CHECK();
 }
 
+void launch_edge_pieces(const Scene &s, const BvhView &eb, const float *x, const float *x1,
+                        const unsigned *t_bits, float piece_len, PieceBuffers &pb,
+                        cudaStream_t q) {
+    if (!s.ne) return;
+    k_edge_piece_count<<<div_up(s.ne, kB), kB, 0, q>>>(s.ne, eb.node, s.edge, x, x1, t_bits,
+                                                       piece_len, pb.count);
+    PPF_LAUNCH_CHECK();
+    exclusive_scan(pb.count, pb.off, s.ne, pb.scan_tmp, q);
+}
+
+unsigned piece_grid(unsigned ne, unsigned block) { return div_up(ne, block) + 2 * kNumSMs; }
+
 void launch_detect(const Scene &s, const BvhView &fb, const BvhView &eb,
                    const BvhView &vb, const AssemblyBuffers &b, PairLists &pl,
-                   cudaStream_t q) {
+                   const PieceBuffers &pb, cudaStream_t q) {
     if (s.n_surf) {
         k_detect_vertex<<<div_up(s.n_surf, 128u), 128, 0, q>>>(s, fb, eb, vb, b.x, pl, b.st);
         PPF_LAUNCH_CHECK();
     }
     if (s.ne) {
-        k_detect_edge<<<div_up(s.ne, 128u), 128, 0, q>>>(s, eb, b.x, pl, b.st);
+        k_detect_edge<<<piece_grid(s.ne, 128u), 128, 0, q>>>(s, eb, b.x, pl, b.st,
+                                                            EdgePieces{pb.off, s.ne});
         PPF_LAUNCH_CHECK();
     }
 }

@@ -45,9 +45,21 @@ void launch_elastic(const Scene &s, const StepParams &p, const AssemblyBuffers &
                     cudaStream_t q);
 void launch_strain_limit(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
                          cudaStream_t q);
+// Per-edge piece counts for split edge queries (see contact_rules.cuh).
+struct PieceBuffers {
+    unsigned *count;    // E
+    unsigned *off;      // E + 1
+    unsigned *scan_tmp; // scan_tmp_size(E + 1)
+};
+void launch_edge_pieces(const Scene &s, const BvhView &eb, const float *x, const float *x1,
+                        const unsigned *t_bits, float piece_len, PieceBuffers &pb,
+                        cudaStream_t q);
+// Grid of a launch over edge pieces: one thread per edge plus slack for the
+// extra pieces; the kernels loop over any remainder.
+unsigned piece_grid(unsigned ne, unsigned block);
 void launch_detect(const Scene &s, const BvhView &fb, const BvhView &eb,
                    const BvhView &vb, const AssemblyBuffers &b, PairLists &pl,
-                   cudaStream_t q);
+                   const PieceBuffers &pb, cudaStream_t q);
 // Dedupes the contact blocks outside the fixed pattern and lays them out.
 void launch_dyn_build(const Scene &s, const AssemblyBuffers &b, const PairLists &pl,
                       const unsigned counts[4], DynMatrix &dm, unsigned n_dyn_max,

@@ -28,10 +28,13 @@ __device__ __forceinline__ bool box_overlap(const float4 &amin, const float4 &am
            (amin.z <= bmax.z && amax.z >= bmin.z);
 }
 
-// Calls op(prim) for every leaf whose box overlaps the query box.
+// Calls op(prim) for every leaf whose box overlaps the query box. With an
+// exclusion box (xmin, xmax), leaves that also overlap it are skipped: the
+// previous piece of a split query reports those.
 template <class Op>
 __device__ void bvh_query(const BvhView &b, const float4 &qmin, const float4 &qmax,
-                          Op &op, unsigned *status) {
+                          Op &op, unsigned *status, const float4 *xmin = nullptr,
+                          const float4 *xmax = nullptr) {
     if (b.n == 0 || qmin.w == 0.0f) return;
     unsigned stack[kStackDepth];
     int sp = 0;
@@ -42,6 +45,7 @@ __device__ void bvh_query(const BvhView &b, const float4 &qmin, const float4 &qm
         if (!box_overlap(lo, hi, qmin, qmax)) continue;
         uint2 nd = b.node[id];
         if (nd.y == 0u) {
+            if (xmin && box_overlap(lo, hi, *xmin, *xmax)) continue;
             op(nd.x - 1u);
         } else {
             if (sp + 2 > kStackDepth) {
@@ -200,6 +204,55 @@ __device__ __forceinline__ bool accept_edge_edge(const Scene &s, const float *x,
     if (!(e.squared_norm() < sqr(ghat + offset))) return false;
     if (coef) *coef = c;
     return true;
+}
+
+// ---- long edges query in pieces --------------------------------------------
+// An edge much longer than its neighbours (a collider's face diagonal) has a
+// query box covering thousands of leaves, and the one thread walking it
+// holds up the launch. Such an edge is queried as K pieces of at most
+// `piece_len`, one work item each. Pieces cover the segment (consecutive
+// pieces share their split point), so every leaf within the query margin of
+// the edge overlaps some piece box. Split points are monotone in each axis,
+// so the pieces a leaf box overlaps are consecutive: reporting a leaf only
+// from the first of them (the exclusion box is the previous piece) reports
+// it once.
+constexpr unsigned kMaxPieces = 1024;
+
+struct EdgePieces {
+    const unsigned *off; // n + 1: exclusive scan of the piece counts (tree order)
+    unsigned n;          // edges
+};
+
+__device__ __forceinline__ unsigned piece_count(float len, float piece_len) {
+    if (!(piece_len > 0.0f) || !(len > piece_len)) return 1u;
+    float k = ceilf(len / piece_len);
+    return k >= (float)kMaxPieces ? kMaxPieces : (unsigned)k;
+}
+
+// Split point k of K along a -> b, with the end points exact.
+__device__ __forceinline__ Vec3 piece_point(const Vec3 &a, const Vec3 &b, unsigned k,
+                                            unsigned K) {
+    if (k == 0u) return a;
+    if (k >= K) return b;
+    const float u = (float)k / (float)K;
+    return vec3(a[0] + u * (b[0] - a[0]), a[1] + u * (b[1] - a[1]), a[2] + u * (b[2] - a[2]));
+}
+
+// Tree slot of work item `item`: the largest t with off[t] <= item.
+__device__ __forceinline__ unsigned piece_slot(const EdgePieces &ep, unsigned item) {
+    unsigned lo = 0, hi = ep.n;
+    while (hi - lo > 1u) {
+        unsigned mid = (lo + hi) >> 1;
+        if (ep.off[mid] <= item) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void seg_box(const Vec3 &p, const Vec3 &q, float m, float4 &lo,
+                                        float4 &hi) {
+    lo = make_float4(fminf(p[0], q[0]) - m, fminf(p[1], q[1]) - m, fminf(p[2], q[2]) - m, 1.0f);
+    hi = make_float4(fmaxf(p[0], q[0]) + m, fmaxf(p[1], q[1]) + m, fmaxf(p[2], q[2]) + m, 0.0f);
 }
 
 // Slot of block (i, j), i <= j, in the fixed upper pattern, or kSentinel.

@@ -4,6 +4,7 @@
 #include "../physics/accd.cuh"
 #include "../physics/bw.cuh"
 #include "../physics/strainlimit.cuh"
+#include "assemble.cuh"
 #include "linesearch.cuh"
 
 namespace ppf {
@@ -225,27 +226,36 @@ struct EdgeEdgeCcdOp {
     }
 };
 
-__global__ void k_ccd_edge(Scene s, BvhView eb, LineSearchArgs a) {
-    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= s.ne) return;
-    unsigned e = eb.node[t].x - 1u;
-    const unsigned *ed = s.edge + 2 * e;
-    float seed = __uint_as_float(a.st->toi_vf_bits);
-    float m = s.margin_edge[e];
-    Vec3 p0 = X(a.x0, ed[0]), p1 = X(a.x0, ed[1]);
-    Vec3 q0 = sweep_end(a.x0, a.x1, ed[0], seed), q1 = sweep_end(a.x0, a.x1, ed[1], seed);
-    float4 qmin, qmax;
-    qmin.x = fminf(fminf(p0[0], p1[0]) - m, fminf(q0[0], q1[0]) - m);
-    qmin.y = fminf(fminf(p0[1], p1[1]) - m, fminf(q0[1], q1[1]) - m);
-    qmin.z = fminf(fminf(p0[2], p1[2]) - m, fminf(q0[2], q1[2]) - m);
-    qmin.w = 1.0f;
-    qmax.x = fmaxf(fmaxf(p0[0], p1[0]) + m, fmaxf(q0[0], q1[0]) + m);
-    qmax.y = fmaxf(fmaxf(p0[1], p1[1]) + m, fmaxf(q0[1], q1[1]) + m);
-    qmax.z = fmaxf(fmaxf(p0[2], p1[2]) + m, fmaxf(q0[2], q1[2]) + m);
-    qmax.w = 0.0f;
-    EdgeEdgeCcdOp op{s, a, e, seed};
-    bvh_query(eb, qmin, qmax, op, &a.st->status);
-    atomicMin(&a.st->toi_bits, __float_as_uint(op.toi));
+// One work item per edge piece: the piece swept from the previous iterate to
+// the vertex/face seed time. A leaf found by two pieces is tested twice;
+// the result is a minimum, so that changes nothing.
+__global__ void k_ccd_edge(Scene s, BvhView eb, LineSearchArgs a, EdgePieces ep) {
+    const unsigned total = ep.off[ep.n];
+    const float seed = __uint_as_float(a.st->toi_vf_bits);
+    for (unsigned item = blockIdx.x * blockDim.x + threadIdx.x; item < total;
+         item += gridDim.x * blockDim.x) {
+        const unsigned t = piece_slot(ep, item);
+        const unsigned k = item - ep.off[t], K = ep.off[t + 1] - ep.off[t];
+        const unsigned e = eb.node[t].x - 1u;
+        const unsigned *ed = s.edge + 2 * e;
+        float m = s.margin_edge[e];
+        Vec3 a0 = X(a.x0, ed[0]), b0 = X(a.x0, ed[1]);
+        Vec3 a1 = sweep_end(a.x0, a.x1, ed[0], seed), b1 = sweep_end(a.x0, a.x1, ed[1], seed);
+        Vec3 p0 = piece_point(a0, b0, k, K), p1 = piece_point(a0, b0, k + 1, K);
+        Vec3 q0 = piece_point(a1, b1, k, K), q1 = piece_point(a1, b1, k + 1, K);
+        float4 qmin, qmax;
+        qmin.x = fminf(fminf(p0[0], p1[0]) - m, fminf(q0[0], q1[0]) - m);
+        qmin.y = fminf(fminf(p0[1], p1[1]) - m, fminf(q0[1], q1[1]) - m);
+        qmin.z = fminf(fminf(p0[2], p1[2]) - m, fminf(q0[2], q1[2]) - m);
+        qmin.w = 1.0f;
+        qmax.x = fmaxf(fmaxf(p0[0], p1[0]) + m, fmaxf(q0[0], q1[0]) + m);
+        qmax.y = fmaxf(fmaxf(p0[1], p1[1]) + m, fmaxf(q0[1], q1[1]) + m);
+        qmax.z = fmaxf(fmaxf(p0[2], p1[2]) + m, fmaxf(q0[2], q1[2]) + m);
+        qmax.w = 0.0f;
+        EdgeEdgeCcdOp op{s, a, e, seed};
+        bvh_query(eb, qmin, qmax, op, &a.st->status);
+        atomicMin(&a.st->toi_bits, __float_as_uint(op.toi));
+    }
 }
 
 // Analytic colliders alone, for scenes whose mesh contact is switched off
@@ -359,31 +369,51 @@ struct EdgeEdgeIsectOp {
     }
 };
 
+// One work item per edge piece, each leaf reported from its first piece.
+// Piece boxes carry the edge's contact offset plus a rounding guard: every
+// pierced face contains the pierce point, and every edge nearer than the
+// combined offset lies within the edge's offset plus its own leaf margin.
 __global__ void k_isect(Scene s, BvhView fb, BvhView eb, const float *x,
-                        PpfIntersectionRecord *rec, IterStatus *st) {
-    unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= s.ne) return;
-    const unsigned *ed = s.edge + 2 * e;
-    Vec3 a = X(x, ed[0]), b = X(x, ed[1]);
-    float4 qmin = make_float4(fminf(a[0], b[0]), fminf(a[1], b[1]), fminf(a[2], b[2]), 1.0f);
-    float4 qmax = make_float4(fmaxf(a[0], b[0]), fmaxf(a[1], b[1]), fmaxf(a[2], b[2]), 0.0f);
-    FaceEdgeIsectOp op{s, x, e, rec, st};
-    bvh_query(fb, qmin, qmax, op, &st->status);
-    EdgeEdgeIsectOp op2{s, x, e, rec, st};
-    bvh_query(eb, qmin, qmax, op2, &st->status);
+                        PpfIntersectionRecord *rec, IterStatus *st, EdgePieces ep) {
+    const unsigned total = ep.off[ep.n];
+    for (unsigned item = blockIdx.x * blockDim.x + threadIdx.x; item < total;
+         item += gridDim.x * blockDim.x) {
+        const unsigned t = piece_slot(ep, item);
+        const unsigned k = item - ep.off[t], K = ep.off[t + 1] - ep.off[t];
+        const unsigned e = eb.node[t].x - 1u;
+        const unsigned *ed = s.edge + 2 * e;
+        Vec3 a = X(x, ed[0]), b = X(x, ed[1]);
+        const float guard =
+            1e-6f * (1.0f + fmaxf(fmaxf(fmaxf(fabsf(a[0]), fabsf(a[1])), fmaxf(fabsf(a[2]), fabsf(b[0]))),
+                                  fmaxf(fabsf(b[1]), fabsf(b[2]))));
+        const float m = s.eparam[s.eprop[e].param_index].offset + guard;
+        float4 qmin, qmax, xmin, xmax;
+        seg_box(piece_point(a, b, k, K), piece_point(a, b, k + 1, K), m, qmin, qmax);
+        const float4 *xl = nullptr, *xh = nullptr;
+        if (k > 0u) {
+            seg_box(piece_point(a, b, k - 1, K), piece_point(a, b, k, K), m, xmin, xmax);
+            xl = &xmin;
+            xh = &xmax;
+        }
+        FaceEdgeIsectOp op{s, x, e, rec, st};
+        bvh_query(fb, qmin, qmax, op, &st->status, xl, xh);
+        EdgeEdgeIsectOp op2{s, x, e, rec, st};
+        bvh_query(eb, qmin, qmax, op2, &st->status, xl, xh);
+    }
 }
 
 } // namespace
 
 void launch_contact_line_search(const Scene &s, const BvhView &fb, const BvhView &eb,
-                                const BvhView &vb, const LineSearchArgs &a,
-                                cudaStream_t q) {
+                                const BvhView &vb, const LineSearchArgs &a, float piece_len,
+                                PieceBuffers &pb, cudaStream_t q) {
     if (s.n_surf) {
         k_ccd_vertex<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, fb, vb, a);
         PPF_LAUNCH_CHECK();
     }
     if (s.ne) {
-        k_ccd_edge<<<div_up(s.ne, kB), kB, 0, q>>>(s, eb, a);
+        launch_edge_pieces(s, eb, a.x0, a.x1, &a.st->toi_vf_bits, piece_len, pb, q);
+        k_ccd_edge<<<piece_grid(s.ne, kB), kB, 0, q>>>(s, eb, a, EdgePieces{pb.off, s.ne});
         PPF_LAUNCH_CHECK();
     }
     k_fold_vertex_toi<<<1, 1, 0, q>>>(a.st);
@@ -404,9 +434,11 @@ void launch_strain_line_search(const Scene &s, const LineSearchArgs &a, cudaStre
 
 void launch_intersection_check(const Scene &s, const BvhView &fb, const BvhView &eb,
                                const float *x, PpfIntersectionRecord *records, IterStatus *st,
-                               cudaStream_t q) {
+                               float piece_len, PieceBuffers &pb, cudaStream_t q) {
     if (!s.ne) return;
-    k_isect<<<div_up(s.ne, kB), kB, 0, q>>>(s, fb, eb, x, records, st);
+    launch_edge_pieces(s, eb, x, nullptr, nullptr, piece_len, pb, q);
+    k_isect<<<piece_grid(s.ne, kB), kB, 0, q>>>(s, fb, eb, x, records, st,
+                                               EdgePieces{pb.off, s.ne});
     PPF_LAUNCH_CHECK();
 }
 

@@ -1,7 +1,7 @@
 // linesearch.cuh -- feasible step fraction and post-step intersection check.
 #pragma once
 
-#include "contact_rules.cuh"
+#include "assemble.cuh"
 
 namespace ppf {
 namespace gpu {
@@ -21,8 +21,8 @@ struct LineSearchArgs {
 // Results: st->toi_bits (min over every candidate, in units of the sweep),
 // st->overlap, st->pin_infeasible.
 void launch_contact_line_search(const Scene &s, const BvhView &fb, const BvhView &eb,
-                                const BvhView &vb, const LineSearchArgs &a,
-                                cudaStream_t q);
+                                const BvhView &vb, const LineSearchArgs &a, float piece_len,
+                                PieceBuffers &pb, cudaStream_t q);
 
 // The analytic-collider part alone (sphere / floor crossings and infeasible
 // pins), for scenes whose mesh contact is switched off -> st->toi_bits.
@@ -37,7 +37,7 @@ void launch_strain_line_search(const Scene &s, const LineSearchArgs &a, cudaStre
 // PPF_MAX_INTERSECTION_RECORDS), the count to st->n_isect.
 void launch_intersection_check(const Scene &s, const BvhView &fb, const BvhView &eb,
                                const float *x, PpfIntersectionRecord *records, IterStatus *st,
-                               cudaStream_t q);
+                               float piece_len, PieceBuffers &pb, cudaStream_t q);
 
 } // namespace gpu
 } // namespace ppf

@@ -254,6 +254,10 @@ PcgOperator Solver::pcg_operator() const {
     return PcgOperator{n_, sell_view(fixed_sell_), sell_view(dyn_sell_), inv_diag_.data()};
 }
 
+PieceBuffers Solver::pieces() {
+    return PieceBuffers{piece_cnt_.data(), piece_off_.data(), piece_tmp_.data()};
+}
+
 BvhView Solver::view(const Lbvh &b) const {
     return BvhView{b.node.data(), b.bmin.data(), b.bmax.data(), b.root, b.n};
 }
@@ -367,6 +371,26 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     upload(margin_face_, mf);
     upload(margin_edge_, me);
     upload(margin_vert_, mv);
+    // edge queries split into pieces of about twice the median rest length
+    {
+        std::vector<float> len(ne_);
+        const float *x = (const float *)ds->vertex.curr.data;
+        const unsigned *E = (const unsigned *)ds->mesh.mesh.edge.data;
+        for (unsigned i = 0; i < ne_; ++i) {
+            float d0 = x[3 * E[2 * i]] - x[3 * E[2 * i + 1]];
+            float d1 = x[3 * E[2 * i] + 1] - x[3 * E[2 * i + 1] + 1];
+            float d2 = x[3 * E[2 * i] + 2] - x[3 * E[2 * i + 1] + 2];
+            len[i] = std::sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        }
+        piece_len_ = 0.0f;
+        if (ne_) {
+            std::nth_element(len.begin(), len.begin() + ne_ / 2, len.end());
+            piece_len_ = 2.0f * len[ne_ / 2];
+        }
+        piece_cnt_.reserve(ne_ + 1);
+        piece_off_.reserve(ne_ + 1);
+        piece_tmp_.reserve(scan_tmp_size(ne_ + 1));
+    }
     // constraints
     update_constraint(&ds->constraint);
     // state
@@ -492,8 +516,9 @@ void Solver::compute_target(float dt) {
 
 bool Solver::check_intersection(const float *x) {
     PPF_CUDA(cudaMemsetAsync(&st_.data()->n_isect, 0, sizeof(unsigned), q_));
+    PieceBuffers pb = pieces();
     launch_intersection_check(scene(), view(bvh_face_), view(bvh_edge_), x, isect_.data(),
-                              st_.data(), q_);
+                              st_.data(), piece_len_, pb, q_);
     unsigned cnt = 0;
     PPF_CUDA(cudaMemcpyAsync(&cnt, &st_.data()->n_isect, sizeof(unsigned),
                              cudaMemcpyDeviceToHost, q_));
@@ -541,7 +566,10 @@ void Solver::assemble(float dt) {
         build_trees(eval_x_.data(), eval_x_.data(), 1.0f, false);
         for (int attempt = 0; attempt < 3; ++attempt) {
             PPF_CUDA(cudaMemsetAsync(st_.data(), 0, 4 * sizeof(unsigned), q_));
-            launch_detect(s, view(bvh_face_), view(bvh_edge_), view(bvh_vert_), b, pairs_, q_);
+            PieceBuffers pb = pieces();
+            launch_edge_pieces(s, view(bvh_edge_), eval_x_.data(), nullptr, nullptr, piece_len_,
+                               pb, q_);
+            launch_detect(s, view(bvh_face_), view(bvh_edge_), view(bvh_vert_), b, pairs_, pb, q_);
             read_status();
             counts[0] = st_host_->n_pf;
             counts[1] = st_host_->n_pe;
@@ -659,8 +687,9 @@ PpfStepResult Solver::advance() {
                           param->ccd_eps};
         if (!param->disable_contact) {
             build_trees(target_.data(), eval_x_.data(), max_t, false);
+            PieceBuffers pb = pieces();
             launch_contact_line_search(s, view(bvh_face_), view(bvh_edge_), view(bvh_vert_), la,
-                                       q_);
+                                       piece_len_, pb, q_);
         } else {
             launch_constraint_line_search(s, la, q_);
         }
