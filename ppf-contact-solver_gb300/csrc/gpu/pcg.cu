@@ -15,9 +15,12 @@
 // Forming p on the fly removes the third grid barrier a stored p update
 // would need before the next product; p alternates between two buffers so
 // the previous direction stays readable while the new one is written.
-// Values written by other blocks during the launch are read with ld.cg (L2,
-// never a stale L1 line); the operator is read-only inside the launch and
-// goes through the non-coherent path.
+// z, p and A p are kept as one float4 per vertex, so a neighbour gather is a
+// single 16-byte load. Values another block wrote during the launch are read
+// with ld.cg (from L2, never a line an SM's L1 kept from an earlier phase);
+// a vertex's own values, written by the same thread, are read back directly.
+// The operator is read-only inside the launch and goes through the
+// non-coherent path.
 #include "../physics/eig.cuh"
 #include "assemble.cuh"
 #include "pcg.cuh"
@@ -145,23 +148,43 @@ __device__ bool grid_sum2(float &a, float &b, float *part, unsigned *bar, unsign
 __device__ __forceinline__ Vec3 ldcg3(const float *v, unsigned i) {
     return vec3(__ldcg(v + 3 * i), __ldcg(v + 3 * i + 1), __ldcg(v + 3 * i + 2));
 }
+__device__ __forceinline__ Vec3 ld4(const float4 *v, unsigned i) {
+    float4 a = __ldcg(v + i);
+    return vec3(a.x, a.y, a.z);
+}
+__device__ __forceinline__ void st4(float4 *v, unsigned i, const Vec3 &a) {
+    v[i] = make_float4(a[0], a[1], a[2], 0.0f);
+}
 __device__ __forceinline__ void st3(float *v, unsigned i, const Vec3 &a) {
     v[3 * i] = a[0];
     v[3 * i + 1] = a[1];
     v[3 * i + 2] = a[2];
 }
 
-// One slot's block times v(j), v(j) = u(j) + beta w(j) (or u(j)).
-template <bool kCombine>
+// Neighbour value of one slot: v(j) = u(j) + beta w(j) from the float4
+// vectors, or x(j) from the AoS input of the initial product.
+struct GatherCombined {
+    const float4 *u, *w;
+    float beta;
+    __device__ __forceinline__ Vec3 operator()(unsigned j) const {
+        return ld4(u, j) + beta * ld4(w, j);
+    }
+};
+struct GatherPlain {
+    const float *x;
+    __device__ __forceinline__ Vec3 operator()(unsigned j) const { return ldcg3(x, j); }
+};
+
+// One slot's block times its neighbour value.
+template <class G>
 __device__ __forceinline__ void slot_term(const SellMatrix &M, size_t s, unsigned lane,
-                                          unsigned j, const float *u, const float *w,
-                                          float beta, Vec3 &acc, Vec3 &abssum) {
+                                          unsigned j, const G &gather, Vec3 &acc,
+                                          Vec3 &abssum) {
     const float *a = M.val + s * 9 * kSliceRows + lane;
     float m[9];
 #pragma unroll
     for (int e = 0; e < 9; ++e) m[e] = __ldg(a + e * kSliceRows);
-    Vec3 v = ldcg3(u, j);
-    if (kCombine) v = v + beta * ldcg3(w, j);
+    const Vec3 v = gather(j);
     // column-major block: t_r = sum_c m[3 c + r] v_c
     Vec3 t;
     t[0] = m[0] * v[0] + m[3] * v[1] + m[6] * v[2];
@@ -171,15 +194,13 @@ __device__ __forceinline__ void slot_term(const SellMatrix &M, size_t s, unsigne
     abssum += t.cwise_abs();
 }
 
-// Row (32 s + lane) of A v over one SELL matrix, with v(j) = u(j) + beta w(j)
-// formed per column (kCombine false: plain A u). abssum collects the
+// Row (32 s + lane) of A v over one SELL matrix. abssum collects the
 // component-wise |term| of every block product. Slots are taken four at a
 // time (column indices first) so four gathers are in flight per lane; the
 // terms are still added in slot order.
-template <bool kCombine>
+template <class G>
 __device__ __forceinline__ void sell_row(const SellMatrix &M, unsigned slice, unsigned lane,
-                                         const float *u, const float *w, float beta,
-                                         Vec3 &acc, Vec3 &abssum) {
+                                         const G &gather, Vec3 &acc, Vec3 &abssum) {
     const unsigned s0 = __ldg(M.slice_off + slice), s1 = __ldg(M.slice_off + slice + 1);
     unsigned s = s0;
     for (; s + 4 <= s1; s += 4) {
@@ -187,11 +208,11 @@ __device__ __forceinline__ void sell_row(const SellMatrix &M, unsigned slice, un
 #pragma unroll
         for (int q = 0; q < 4; ++q) j[q] = __ldg(M.col + (size_t)(s + q) * kSliceRows + lane);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) slot_term<kCombine>(M, s + q, lane, j[q], u, w, beta, acc, abssum);
+        for (int q = 0; q < 4; ++q) slot_term(M, s + q, lane, j[q], gather, acc, abssum);
     }
     for (; s < s1; ++s) {
         const unsigned j = __ldg(M.col + (size_t)s * kSliceRows + lane);
-        slot_term<kCombine>(M, s, lane, j, u, w, beta, acc, abssum);
+        slot_term(M, s, lane, j, gather, acc, abssum);
     }
 }
 
@@ -205,7 +226,8 @@ __device__ __forceinline__ Mat3 load_inv(const float *inv, unsigned slice, unsig
 
 struct PcgArgs {
     PcgOperator A;
-    float *x, *r, *z, *p0, *p1, *Ap;
+    float *x, *r;
+    float4 *z, *p0, *p1, *Ap;
     float *part; // 2 buffers of 2 floats per block
     unsigned *bar;
     float tol;
@@ -229,14 +251,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
     for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
         const unsigned i = sl * kSliceRows + lane;
         Vec3 acc = Vec3::zero(), ab = Vec3::zero();
-        sell_row<false>(A.fixed, sl, lane, g.x, g.x, 0.0f, acc, ab);
-        sell_row<false>(A.dyn, sl, lane, g.x, g.x, 0.0f, acc, ab);
+        const GatherPlain gx{g.x};
+        sell_row(A.fixed, sl, lane, gx, acc, ab);
+        sell_row(A.dyn, sl, lane, gx, acc, ab);
         if (i < A.n) {
             Vec3 ri = ldcg3(g.r, i) - acc;
             Vec3 zi = load_inv(A.inv_diag, sl, lane) * ri;
             st3(g.r, i, ri);
-            st3(g.z, i, zi);
-            st3(g.p0, i, Vec3::zero());
+            st4(g.z, i, zi);
+            st4(g.p0, i, Vec3::zero());
             a += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
             b += ri.dot(zi);
         }
@@ -255,19 +278,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
         int broke = 0;
         float break_val = 0.0f;
         for (unsigned iter = 1;; ++iter) {
-            const float *p_prev = (iter & 1u) ? g.p0 : g.p1;
-            float *p_new = (iter & 1u) ? g.p1 : g.p0;
+            const float4 *p_prev = (iter & 1u) ? g.p0 : g.p1;
+            float4 *p_new = (iter & 1u) ? g.p1 : g.p0;
             // S: A p_k with p_k = z + beta p_{k-1}
             a = b = 0.0f; // p^T A p, sum |p_i| |terms|
+            const GatherCombined gp{g.z, p_prev, beta};
             for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
                 const unsigned i = sl * kSliceRows + lane;
                 Vec3 acc = Vec3::zero(), ab = Vec3::zero();
-                sell_row<true>(A.fixed, sl, lane, g.z, p_prev, beta, acc, ab);
-                sell_row<true>(A.dyn, sl, lane, g.z, p_prev, beta, acc, ab);
+                sell_row(A.fixed, sl, lane, gp, acc, ab);
+                sell_row(A.dyn, sl, lane, gp, acc, ab);
                 if (i < A.n) {
-                    Vec3 pi = ldcg3(g.z, i) + beta * ldcg3(p_prev, i);
-                    st3(p_new, i, pi);
-                    st3(g.Ap, i, acc);
+                    Vec3 pi = gp(i);
+                    st4(p_new, i, pi);
+                    st4(g.Ap, i, acc);
                     a += pi.dot(acc);
                     b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] + fabsf(pi[2]) * ab[2];
                 }
@@ -289,7 +313,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
                 const unsigned i = sl * kSliceRows + lane;
                 if (i >= A.n) continue;
-                Vec3 pi = ldcg3(p_new, i), api = ldcg3(g.Ap, i);
+                Vec3 pi = ld4(p_new, i), api = ld4(g.Ap, i);
                 Vec3 xi = ldcg3(g.x, i), ri = ldcg3(g.r, i);
                 for (int k = 0; k < 3; ++k) {
                     xi[k] += alpha * pi[k];
@@ -298,7 +322,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
                 Vec3 zi = load_inv(A.inv_diag, sl, lane) * ri;
                 st3(g.x, i, xi);
                 st3(g.r, i, ri);
-                st3(g.z, i, zi);
+                st4(g.z, i, zi);
                 a += ri.dot(zi);
                 b += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
             }
@@ -440,10 +464,10 @@ __global__ void k_dyn_sell_fill(unsigned n, unsigned n_slices, const unsigned *o
 } // namespace
 
 void PcgWorkspace::reserve(unsigned n) {
-    z.reserve(3 * (size_t)n);
-    p0.reserve(3 * (size_t)n);
-    p1.reserve(3 * (size_t)n);
-    Ap.reserve(3 * (size_t)n);
+    z.reserve(n);
+    p0.reserve(n);
+    p1.reserve(n);
+    Ap.reserve(n);
     if (grid == 0) {
         int dev = 0, sms = 0, per_sm = 0;
         PPF_CUDA(cudaGetDevice(&dev));

@@ -56,7 +56,7 @@ struct PcgResult {
 };
 
 struct PcgWorkspace {
-    DevBuf<float> z, p0, p1, Ap;
+    DevBuf<float4> z, p0, p1, Ap; // one float4 per vertex
     DevBuf<float> partials;
     DevBuf<unsigned> barrier;
     DevBuf<PcgResult> result;
