@@ -13,12 +13,12 @@
 //                                                          -> reduce #2
 //
 // Forming p on the fly removes the third grid barrier a stored p update
-// would need before the next product; p alternates between two buffers so
-// the previous direction stays readable while the new one is written.
-// z, p and A p are kept as one float4 per vertex, so a neighbour gather is a
-// single 16-byte load. Values another block wrote during the launch are read
-// with ld.cg (from L2, never a line an SM's L1 kept from an earlier phase);
-// a vertex's own values, written by the same thread, are read back directly.
+// would need before the next product. For that, each vertex's z and p sit
+// in one 32-byte record {z, p} that its owner rewrites at the end of the
+// update phase; a neighbour gather is one 256-bit load of the record (one L2
+// sector), and the owner keeps the p of the current iteration in a separate
+// buffer until then. Values another block wrote during the launch are read
+// with ld.cg (from L2, never a line an SM's L1 kept from an earlier phase).
 // The operator is read-only inside the launch and goes through the
 // non-coherent path.
 #include "../physics/eig.cuh"
@@ -161,13 +161,31 @@ __device__ __forceinline__ void st3(float *v, unsigned i, const Vec3 &a) {
     v[3 * i + 2] = a[2];
 }
 
-// Neighbour value of one slot: v(j) = u(j) + beta w(j) from the float4
-// vectors, or x(j) from the AoS input of the initial product.
+// The {z, p} record of vertex j in one 256-bit load from L2.
+__device__ __forceinline__ void ld_record(const float *R, unsigned j, Vec3 &z, Vec3 &p) {
+    float r[8];
+    asm volatile("ld.global.cg.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]),
+                   "=f"(r[6]), "=f"(r[7])
+                 : "l"(R + 8 * (size_t)j));
+    z = vec3(r[0], r[1], r[2]);
+    p = vec3(r[3], r[4], r[5]);
+}
+__device__ __forceinline__ void st_record(float *R, unsigned i, const Vec3 &z, const Vec3 &p) {
+    float4 *d = reinterpret_cast<float4 *>(R + 8 * (size_t)i);
+    d[0] = make_float4(z[0], z[1], z[2], p[0]);
+    d[1] = make_float4(p[1], p[2], 0.0f, 0.0f);
+}
+
+// Neighbour value of one slot: v(j) = z(j) + beta p(j) from the records, or
+// x(j) from the AoS input of the initial product.
 struct GatherCombined {
-    const float4 *u, *w;
+    const float *R;
     float beta;
     __device__ __forceinline__ Vec3 operator()(unsigned j) const {
-        return ld4(u, j) + beta * ld4(w, j);
+        Vec3 z, p;
+        ld_record(R, j, z, p);
+        return z + beta * p;
     }
 };
 struct GatherPlain {
@@ -194,25 +212,39 @@ __device__ __forceinline__ void slot_term(const SellMatrix &M, size_t s, unsigne
     abssum += t.cwise_abs();
 }
 
-// Row (32 s + lane) of A v over one SELL matrix. abssum collects the
-// component-wise |term| of every block product. Slots are taken four at a
-// time (column indices first) so four gathers are in flight per lane; the
-// terms are still added in slot order.
+// Part of row (32 slice + r) of A v over one SELL matrix: the slots of one
+// parity (`par` 0: even, 1: odd). Two lanes share a row, so a warp holds 16
+// rows and each lane walks half the row; a warp-wide load then touches two
+// 64-byte runs, one per parity. abssum collects the component-wise |term| of
+// every block product. Slots are taken four at a time (column indices first)
+// so four gathers are in flight per lane.
 template <class G>
-__device__ __forceinline__ void sell_row(const SellMatrix &M, unsigned slice, unsigned lane,
-                                         const G &gather, Vec3 &acc, Vec3 &abssum) {
+__device__ __forceinline__ void sell_half_row(const SellMatrix &M, unsigned slice, unsigned r,
+                                              unsigned par, const G &gather, Vec3 &acc,
+                                              Vec3 &abssum) {
     const unsigned s0 = __ldg(M.slice_off + slice), s1 = __ldg(M.slice_off + slice + 1);
-    unsigned s = s0;
-    for (; s + 4 <= s1; s += 4) {
+    unsigned s = s0 + par;
+    for (; s + 6 < s1; s += 8) {
         unsigned j[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) j[q] = __ldg(M.col + (size_t)(s + q) * kSliceRows + lane);
+        for (int q = 0; q < 4; ++q)
+            j[q] = __ldg(M.col + (size_t)(s + 2 * q) * kSliceRows + r);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) slot_term(M, s + q, lane, j[q], gather, acc, abssum);
+        for (int q = 0; q < 4; ++q) slot_term(M, s + 2 * q, r, j[q], gather, acc, abssum);
     }
-    for (; s < s1; ++s) {
-        const unsigned j = __ldg(M.col + (size_t)s * kSliceRows + lane);
-        slot_term(M, s, lane, j, gather, acc, abssum);
+    for (; s < s1; s += 2) {
+        const unsigned j = __ldg(M.col + (size_t)s * kSliceRows + r);
+        slot_term(M, s, r, j, gather, acc, abssum);
+    }
+}
+
+// Row sum of both parities (the two lanes l and l ^ 16 end with the same
+// bits: float addition commutes).
+__device__ __forceinline__ void join_halves(Vec3 &acc, Vec3 &abssum) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], 16);
+        abssum[k] += __shfl_xor_sync(0xffffffffu, abssum[k], 16);
     }
 }
 
@@ -226,14 +258,65 @@ __device__ __forceinline__ Mat3 load_inv(const float *inv, unsigned slice, unsig
 
 struct PcgArgs {
     PcgOperator A;
+    const unsigned *task_start; // grid + 1: each block's range of product tasks
     float *x, *r;
-    float4 *z, *p0, *p1, *Ap;
+    float *R;            // 8 floats per vertex: {z, p} records
+    float4 *p, *Ap, *Ap_ovf;
     float *part; // 2 buffers of 2 floats per block
     unsigned *bar;
     float tol;
     unsigned max_iter;
     PcgResult *res;
 };
+
+// Overflow row k of the contact part: the whole warp strides its entries and
+// folds the partial products in a fixed shuffle order. Result on lane 0.
+template <class G>
+__device__ __forceinline__ void overflow_row(const OverflowRows &O, unsigned k, unsigned lane,
+                                             const G &gather, Vec3 &acc, Vec3 &abssum) {
+    const uint2 rg = __ldg(O.range + k);
+    for (unsigned e = rg.x + lane; e < rg.x + rg.y; e += 32u) {
+        const unsigned j = __ldg(O.col + e);
+        const float *a = O.val + 9 * (size_t)e;
+        float m[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) m[q] = __ldg(a + q);
+        const Vec3 v = gather(j);
+        Vec3 t;
+        t[0] = m[0] * v[0] + m[3] * v[1] + m[6] * v[2];
+        t[1] = m[1] * v[0] + m[4] * v[1] + m[7] * v[2];
+        t[2] = m[2] * v[0] + m[5] * v[1] + m[8] * v[2];
+        acc += t;
+        abssum += t.cwise_abs();
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            acc[c] += __shfl_down_sync(0xffffffffu, acc[c], off);
+            abssum[c] += __shfl_down_sync(0xffffffffu, abssum[c], off);
+        }
+}
+
+// The block's product tasks, handed to its warps one at a time through a
+// shared counter (a block's range holds about 1/grid of the slot work).
+struct BlockTasks {
+    unsigned *next; // shared
+    unsigned end;
+    __device__ __forceinline__ unsigned take(unsigned lane) const {
+        unsigned t = 0;
+        if (lane == 0u) t = atomicAdd(next, 1u);
+        return __shfl_sync(0xffffffffu, t, 0);
+    }
+};
+
+// (A v)(i): the row's slice part plus its overflow part, if any.
+__device__ __forceinline__ Vec3 row_product(const PcgArgs &g, unsigned i) {
+    Vec3 ap = ld4(g.Ap, i);
+    const unsigned k = __ldg(g.A.ovf.index + i);
+    if (k != 0xFFFFFFFFu) ap += ld4(g.Ap_ovf, k);
+    return ap;
+}
 
 __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
     const PcgOperator &A = g.A;
@@ -246,23 +329,46 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
     float *part0 = g.part, *part1 = g.part + 2 * nb;
     float a, b;
 
-    // r = b - A x0, z = P r, p_0 = 0; err0 = |r|_1, rz0 = r^T z
+    // work items of the products: half slices (16 rows, two lanes per row),
+    // then one warp per overflow row of the contact part
+    const unsigned tasks = 2 * n_slices;
+    const unsigned par = lane >> 4;
+
+    __shared__ unsigned s_next;
+    const BlockTasks bt{&s_next, g.task_start[blockIdx.x + 1]};
+    // A x0 (slice part to Ap, overflow part to Ap_ovf) ...
+    if (threadIdx.x == 0) s_next = g.task_start[blockIdx.x];
+    __syncthreads();
+    {
+        const GatherPlain gx{g.x};
+        for (unsigned task = bt.take(lane); task < bt.end; task = bt.take(lane)) {
+            Vec3 acc = Vec3::zero(), ab = Vec3::zero();
+            if (task < tasks) {
+                const unsigned sl = task >> 1, r = (task & 1u) * 16u + (lane & 15u);
+                const unsigned i = sl * kSliceRows + r;
+                sell_half_row(A.fixed, sl, r, par, gx, acc, ab);
+                sell_half_row(A.dyn, sl, r, par, gx, acc, ab);
+                join_halves(acc, ab);
+                if (par == 0u && i < A.n) st4(g.Ap, i, acc);
+            } else {
+                overflow_row(A.ovf, task - tasks, lane, gx, acc, ab);
+                if (lane == 0u) st4(g.Ap_ovf, task - tasks, acc);
+            }
+        }
+    }
+    a = b = 0.0f;
+    if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
+    // ... then r = b - A x0, z = P r, p_0 = 0; err0 = |r|_1, rz0 = r^T z
     a = b = 0.0f;
     for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
         const unsigned i = sl * kSliceRows + lane;
-        Vec3 acc = Vec3::zero(), ab = Vec3::zero();
-        const GatherPlain gx{g.x};
-        sell_row(A.fixed, sl, lane, gx, acc, ab);
-        sell_row(A.dyn, sl, lane, gx, acc, ab);
-        if (i < A.n) {
-            Vec3 ri = ldcg3(g.r, i) - acc;
-            Vec3 zi = load_inv(A.inv_diag, sl, lane) * ri;
-            st3(g.r, i, ri);
-            st4(g.z, i, zi);
-            st4(g.p0, i, Vec3::zero());
-            a += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
-            b += ri.dot(zi);
-        }
+        if (i >= A.n) continue;
+        Vec3 ri = ldcg3(g.r, i) - row_product(g, i);
+        Vec3 zi = load_inv(A.inv_diag, sl, lane) * ri;
+        st3(g.r, i, ri);
+        st_record(g.R, i, zi, Vec3::zero());
+        a += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
+        b += ri.dot(zi);
     }
     if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
     {
@@ -278,22 +384,35 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
         int broke = 0;
         float break_val = 0.0f;
         for (unsigned iter = 1;; ++iter) {
-            const float4 *p_prev = (iter & 1u) ? g.p0 : g.p1;
-            float4 *p_new = (iter & 1u) ? g.p1 : g.p0;
             // S: A p_k with p_k = z + beta p_{k-1}
             a = b = 0.0f; // p^T A p, sum |p_i| |terms|
-            const GatherCombined gp{g.z, p_prev, beta};
-            for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
-                const unsigned i = sl * kSliceRows + lane;
+            const GatherCombined gp{g.R, beta};
+            if (threadIdx.x == 0) s_next = g.task_start[blockIdx.x];
+            __syncthreads();
+            for (unsigned task = bt.take(lane); task < bt.end; task = bt.take(lane)) {
                 Vec3 acc = Vec3::zero(), ab = Vec3::zero();
-                sell_row(A.fixed, sl, lane, gp, acc, ab);
-                sell_row(A.dyn, sl, lane, gp, acc, ab);
-                if (i < A.n) {
-                    Vec3 pi = gp(i);
-                    st4(p_new, i, pi);
-                    st4(g.Ap, i, acc);
-                    a += pi.dot(acc);
-                    b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] + fabsf(pi[2]) * ab[2];
+                if (task < tasks) {
+                    const unsigned sl = task >> 1, r = (task & 1u) * 16u + (lane & 15u);
+                    const unsigned i = sl * kSliceRows + r;
+                    sell_half_row(A.fixed, sl, r, par, gp, acc, ab);
+                    sell_half_row(A.dyn, sl, r, par, gp, acc, ab);
+                    join_halves(acc, ab);
+                    if (par == 0u && i < A.n) {
+                        Vec3 pi = gp(i);
+                        st4(g.p, i, pi);
+                        st4(g.Ap, i, acc);
+                        a += pi.dot(acc);
+                        b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] + fabsf(pi[2]) * ab[2];
+                    }
+                } else {
+                    const unsigned k = task - tasks;
+                    overflow_row(A.ovf, k, lane, gp, acc, ab);
+                    if (lane == 0u) {
+                        const Vec3 pi = gp(__ldg(A.ovf.row + k));
+                        st4(g.Ap_ovf, k, acc);
+                        a += pi.dot(acc);
+                        b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] + fabsf(pi[2]) * ab[2];
+                    }
                 }
             }
             if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
@@ -313,7 +432,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
                 const unsigned i = sl * kSliceRows + lane;
                 if (i >= A.n) continue;
-                Vec3 pi = ld4(p_new, i), api = ld4(g.Ap, i);
+                Vec3 pi = ld4(g.p, i), api = row_product(g, i);
                 Vec3 xi = ldcg3(g.x, i), ri = ldcg3(g.r, i);
                 for (int k = 0; k < 3; ++k) {
                     xi[k] += alpha * pi[k];
@@ -322,7 +441,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
                 Vec3 zi = load_inv(A.inv_diag, sl, lane) * ri;
                 st3(g.x, i, xi);
                 st3(g.r, i, ri);
-                st4(g.z, i, zi);
+                st_record(g.R, i, zi, pi);
                 a += ri.dot(zi);
                 b += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
             }
@@ -406,15 +525,23 @@ __device__ __forceinline__ unsigned dyn_row_count(unsigned i, const unsigned *of
     return c;
 }
 
-__global__ void k_dyn_slice_k(unsigned n, unsigned n_slices, const unsigned *off,
-                              const unsigned *col, const unsigned *tr_off, const uint2 *tr,
-                              const unsigned *mask, unsigned *slice_k) {
+// Per-row block count, slice width (capped) and overflow count per row.
+__global__ void k_dyn_counts(unsigned n, unsigned n_slices, const unsigned *off,
+                             const unsigned *col, const unsigned *tr_off, const uint2 *tr,
+                             const unsigned *mask, unsigned *slice_k, unsigned *row_ovf,
+                             unsigned *row_flag) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned sl = i / kSliceRows;
     if (sl >= n_slices) return;
     unsigned c = i < n ? dyn_row_count(i, off, col, tr_off, tr, mask) : 0u;
-    c = __reduce_max_sync(0xffffffffu, c);
-    if ((i % kSliceRows) == 0) slice_k[sl] = c;
+    unsigned k = __reduce_max_sync(0xffffffffu, c);
+    if (k > kDynSliceCap) k = kDynSliceCap;
+    if ((i % kSliceRows) == 0) slice_k[sl] = k;
+    if (i < n) {
+        unsigned o = c > k ? c - k : 0u;
+        row_ovf[i] = o;
+        row_flag[i] = o ? 1u : 0u;
+    }
 }
 
 __device__ __forceinline__ void put_slot(unsigned *out_col, float *out_val, unsigned s,
@@ -425,15 +552,37 @@ __device__ __forceinline__ void put_slot(unsigned *out_col, float *out_val, unsi
     for (int e = 0; e < 9; ++e) d[e * kSliceRows] = m[e];
 }
 
-__global__ void k_dyn_sell_fill(unsigned n, unsigned n_slices, const unsigned *off,
-                                const unsigned *col, const float *upper, const unsigned *tr_off,
-                                const uint2 *tr, const unsigned *mask,
-                                const unsigned *slice_off, unsigned *out_col, float *out_val) {
+struct DynFillOut {
+    const unsigned *slice_off, *ovf_off, *flag_off;
+    unsigned *col;
+    float *val;
+    unsigned *ovf_row, *ovf_col, *ovf_index;
+    uint2 *ovf_range;
+    float *ovf_val;
+};
+
+// Row entries in order: the first K (the slice width) to the slice slots,
+// the rest to the row's overflow range.
+__global__ void k_dyn_fill(unsigned n, unsigned n_slices, const unsigned *off,
+                           const unsigned *col, const float *upper, const unsigned *tr_off,
+                           const uint2 *tr, const unsigned *mask, DynFillOut o) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned sl = i / kSliceRows, lane = i % kSliceRows;
     if (sl >= n_slices) return;
-    unsigned s = slice_off[sl];
-    const unsigned s1 = slice_off[sl + 1];
+    const unsigned s0 = o.slice_off[sl], K = o.slice_off[sl + 1] - s0;
+    const unsigned obase = i < n ? o.ovf_off[i] : 0u;
+    unsigned k = 0;
+    auto put = [&](unsigned j, const float (&m)[9]) {
+        if (k < K) {
+            put_slot(o.col, o.val, s0 + k, lane, j, m);
+        } else {
+            unsigned e = obase + (k - K);
+            o.ovf_col[e] = j;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) o.ovf_val[9 * (size_t)e + q] = m[q];
+        }
+        ++k;
+    };
     if (i < n && !mask[i]) {
         for (unsigned q = off[i]; q < off[i + 1]; ++q) {
             unsigned j = col[q];
@@ -442,7 +591,7 @@ __global__ void k_dyn_sell_fill(unsigned n, unsigned n_slices, const unsigned *o
             float m[9];
 #pragma unroll
             for (int e = 0; e < 9; ++e) m[e] = b[e];
-            put_slot(out_col, out_val, s++, lane, j, m);
+            put(j, m);
         }
         for (unsigned q = tr_off[i]; q < tr_off[i + 1]; ++q) {
             uint2 rp = tr[q];
@@ -453,20 +602,65 @@ __global__ void k_dyn_sell_fill(unsigned n, unsigned n_slices, const unsigned *o
             for (int r = 0; r < 3; ++r)
 #pragma unroll
                 for (int c = 0; c < 3; ++c) m[3 * c + r] = b[3 * r + c];
-            put_slot(out_col, out_val, s++, lane, rp.x, m);
+            put(rp.x, m);
         }
     }
     const unsigned self = i < n ? i : n - 1;
     const float zero[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (; s < s1; ++s) put_slot(out_col, out_val, s, lane, self, zero);
+    for (unsigned q = k; q < K; ++q) put_slot(o.col, o.val, s0 + q, lane, self, zero);
+    if (i < n) {
+        if (k > K) {
+            unsigned idx = o.flag_off[i];
+            o.ovf_row[idx] = i;
+            o.ovf_range[idx] = make_uint2(obase, k - K);
+            o.ovf_index[i] = idx;
+        } else {
+            o.ovf_index[i] = 0xFFFFFFFFu;
+        }
+    }
+}
+
+// Estimated cost of each product task, in warp slot-steps: a half slice
+// walks half its fixed and contact slots per lane; an overflow row walks its
+// entries 32 at a time. The constant covers the per-task epilogue.
+__global__ void k_task_cost(unsigned n_slices, const unsigned *fixed_off,
+                            const unsigned *dyn_off, unsigned n_ovf, const uint2 *ovf_range,
+                            unsigned *cost) {
+    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned tasks = 2 * n_slices;
+    if (t >= tasks + n_ovf) return;
+    unsigned c;
+    if (t < tasks) {
+        unsigned sl = t >> 1;
+        unsigned k = (fixed_off[sl + 1] - fixed_off[sl]) + (dyn_off[sl + 1] - dyn_off[sl]);
+        c = (k + 1) / 2;
+    } else {
+        c = (ovf_range[t - tasks].y + 31) / 32;
+    }
+    cost[t] = c + 2u;
+}
+
+// Block b takes the tasks whose cost prefix falls in [b W / nb, (b+1) W / nb).
+__global__ void k_task_split(unsigned T, const unsigned *cost_off, unsigned nb,
+                             unsigned *start) {
+    unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > nb) return;
+    const unsigned long long W = cost_off[T];
+    const unsigned long long target = W * b / nb;
+    unsigned lo = 0, hi = T; // first t with cost_off[t] >= target
+    while (lo < hi) {
+        unsigned mid = (lo + hi) >> 1;
+        if ((unsigned long long)cost_off[mid] < target) lo = mid + 1;
+        else hi = mid;
+    }
+    start[b] = (b == nb) ? T : lo;
 }
 
 } // namespace
 
 void PcgWorkspace::reserve(unsigned n) {
-    z.reserve(n);
-    p0.reserve(n);
-    p1.reserve(n);
+    R.reserve(8 * (size_t)n);
+    p.reserve(n);
     Ap.reserve(n);
     if (grid == 0) {
         int dev = 0, sms = 0, per_sm = 0;
@@ -541,29 +735,48 @@ void sell_pack_fixed(SellLayout &L, const float *upper_val, cudaStream_t q) {
 
 void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const float *val,
                     const unsigned *tr_off, const uint2 *tr, const unsigned *dof_mask,
-                    SellLayout &out, DevBuf<unsigned> &slice_k, DevBuf<unsigned> &scan_tmp,
-                    cudaStream_t q) {
+                    DynLayout &D, cudaStream_t q) {
     const unsigned n_slices = (n + kSliceRows - 1) / kSliceRows;
+    SellLayout &out = D.sell;
     out.n_slices = n_slices;
     out.slice_off.reserve(n_slices + 1);
-    slice_k.reserve(n_slices + 1);
-    scan_tmp.reserve(scan_tmp_size(n_slices + 1));
+    D.slice_k.reserve(n_slices + 1);
+    D.row_ovf.reserve(n + 1);
+    D.row_flag.reserve(n + 1);
+    D.ovf_off.reserve(n + 1);
+    D.flag_off.reserve(n + 1);
+    D.ovf_index.reserve(n + 1);
+    D.scan_tmp.reserve(scan_tmp_size(std::max(n, n_slices) + 1));
     const unsigned threads = n_slices * kSliceRows;
-    k_dyn_slice_k<<<div_up(threads, 256u), 256, 0, q>>>(n, n_slices, off, col, tr_off, tr,
-                                                        dof_mask, slice_k.data());
+    k_dyn_counts<<<div_up(threads, 256u), 256, 0, q>>>(n, n_slices, off, col, tr_off, tr,
+                                                       dof_mask, D.slice_k.data(),
+                                                       D.row_ovf.data(), D.row_flag.data());
     PPF_LAUNCH_CHECK();
-    exclusive_scan(slice_k.data(), out.slice_off.data(), n_slices, scan_tmp.data(), q);
-    unsigned slots = 0;
-    PPF_CUDA(cudaMemcpyAsync(&slots, out.slice_off.data() + n_slices, sizeof(unsigned),
+    exclusive_scan(D.slice_k.data(), out.slice_off.data(), n_slices, D.scan_tmp.data(), q);
+    exclusive_scan(D.row_ovf.data(), D.ovf_off.data(), n, D.scan_tmp.data(), q);
+    exclusive_scan(D.row_flag.data(), D.flag_off.data(), n, D.scan_tmp.data(), q);
+    unsigned totals[3] = {0, 0, 0};
+    PPF_CUDA(cudaMemcpyAsync(&totals[0], out.slice_off.data() + n_slices, sizeof(unsigned),
+                             cudaMemcpyDeviceToHost, q));
+    PPF_CUDA(cudaMemcpyAsync(&totals[1], D.ovf_off.data() + n, sizeof(unsigned),
+                             cudaMemcpyDeviceToHost, q));
+    PPF_CUDA(cudaMemcpyAsync(&totals[2], D.flag_off.data() + n, sizeof(unsigned),
                              cudaMemcpyDeviceToHost, q));
     PPF_CUDA(cudaStreamSynchronize(q));
-    out.slots = slots;
-    out.col.reserve((size_t)slots * kSliceRows + 1);
-    out.val.reserve((size_t)slots * kSliceRows * 9 + 1);
-    if (!slots) return;
-    k_dyn_sell_fill<<<div_up(threads, 256u), 256, 0, q>>>(n, n_slices, off, col, val, tr_off,
-                                                          tr, dof_mask, out.slice_off.data(),
-                                                          out.col.data(), out.val.data());
+    out.slots = totals[0];
+    D.ovf_entries = totals[1];
+    D.n_ovf = totals[2];
+    out.col.reserve((size_t)out.slots * kSliceRows + 1);
+    out.val.reserve((size_t)out.slots * kSliceRows * 9 + 1);
+    D.ovf_col.reserve(D.ovf_entries + 1);
+    D.ovf_val.reserve(9 * (size_t)D.ovf_entries + 1);
+    D.ovf_row.reserve(D.n_ovf + 1);
+    D.ovf_range.reserve(D.n_ovf + 1);
+    DynFillOut o{out.slice_off.data(), D.ovf_off.data(), D.flag_off.data(), out.col.data(),
+                 out.val.data(),       D.ovf_row.data(), D.ovf_col.data(),  D.ovf_index.data(),
+                 D.ovf_range.data(),   D.ovf_val.data()};
+    k_dyn_fill<<<div_up(threads, 256u), 256, 0, q>>>(n, n_slices, off, col, val, tr_off, tr,
+                                                     dof_mask, o);
     PPF_LAUNCH_CHECK();
 }
 
@@ -579,13 +792,29 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
                 PcgWorkspace &ws, cudaStream_t q) {
     ws.reserve(A.n);
     PPF_CUDA(cudaMemsetAsync(ws.barrier.data(), 0, 4 * sizeof(unsigned), q));
+    ws.Ap_ovf.reserve(A.ovf.count + 1);
+    // balanced task ranges per block
+    const unsigned T = 2 * A.fixed.n_slices + A.ovf.count;
+    ws.task_cost.reserve(T + 1);
+    ws.task_off.reserve(T + 1);
+    ws.task_start.reserve(ws.grid + 1);
+    ws.scan_tmp.reserve(scan_tmp_size(T + 1));
+    k_task_cost<<<div_up(T, 256u), 256, 0, q>>>(A.fixed.n_slices, A.fixed.slice_off,
+                                                A.dyn.slice_off, A.ovf.count, A.ovf.range,
+                                                ws.task_cost.data());
+    PPF_LAUNCH_CHECK();
+    exclusive_scan(ws.task_cost.data(), ws.task_off.data(), T, ws.scan_tmp.data(), q);
+    k_task_split<<<div_up(ws.grid + 1, 256u), 256, 0, q>>>(T, ws.task_off.data(), ws.grid,
+                                                          ws.task_start.data());
+    PPF_LAUNCH_CHECK();
     PcgArgs g{A,
+              ws.task_start.data(),
               x,
               r,
-              ws.z.data(),
-              ws.p0.data(),
-              ws.p1.data(),
+              ws.R.data(),
+              ws.p.data(),
               ws.Ap.data(),
+              ws.Ap_ovf.data(),
               ws.partials.data(),
               ws.barrier.data(),
               tol,

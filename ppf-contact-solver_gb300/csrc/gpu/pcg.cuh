@@ -37,11 +37,24 @@ struct SellMatrix {
     const float *val;          // 9 x 32 per slot
 };
 
+// Entries of contact rows longer than the contact slices' cap: one row per
+// work item, processed by a whole warp.
+struct OverflowRows {
+    unsigned count;          // rows with overflow
+    const unsigned *row;     // count: vertex of each
+    const uint2 *range;      // count: (first entry, entries)
+    const unsigned *col;     // entries
+    const float *val;        // 9 per entry, column-major block
+    const unsigned *index;   // n: overflow row of each vertex, or 0xffffffff
+};
+
 // A = fixed part (elastic + inertia + per-vertex terms, diagonal included)
-// + contact part (blocks outside the fixed pattern).
+// + contact part (blocks outside the fixed pattern, SELL up to a width cap
+// plus overflow rows).
 struct PcgOperator {
     unsigned n;
     SellMatrix fixed, dyn;
+    OverflowRows ovf;
     const float *inv_diag; // block-Jacobi inverse, (slice * 9 + e) * 32 + lane
 };
 
@@ -56,7 +69,10 @@ struct PcgResult {
 };
 
 struct PcgWorkspace {
-    DevBuf<float4> z, p0, p1, Ap; // one float4 per vertex
+    DevBuf<float> R;               // {z, p} record per vertex (8 floats)
+    DevBuf<float4> p, Ap;          // one float4 per vertex
+    DevBuf<float4> Ap_ovf;         // one per overflow row
+    DevBuf<unsigned> task_cost, task_off, task_start, scan_tmp;
     DevBuf<float> partials;
     DevBuf<unsigned> barrier;
     DevBuf<PcgResult> result;
@@ -74,6 +90,19 @@ struct SellLayout {
     unsigned n_slices = 0, slots = 0;
 };
 
+// Contact slices are at most this many slots wide; longer rows continue in
+// the overflow rows.
+constexpr unsigned kDynSliceCap = 16;
+
+struct DynLayout {
+    SellLayout sell;
+    DevBuf<unsigned> slice_k, row_ovf, row_flag, ovf_off, flag_off, scan_tmp;
+    DevBuf<unsigned> ovf_row, ovf_col, ovf_index;
+    DevBuf<uint2> ovf_range;
+    DevBuf<float> ovf_val;
+    unsigned n_ovf = 0, ovf_entries = 0;
+};
+
 // Host construction of the fixed layout from the upper pattern and its
 // transpose table (row, upper slot) per row.
 void sell_build_fixed(unsigned n, const std::vector<unsigned> &off,
@@ -83,14 +112,17 @@ void sell_build_fixed(unsigned n, const std::vector<unsigned> &off,
 void sell_pack_fixed(SellLayout &L, const float *upper_val, cudaStream_t q);
 // Contact part, rebuilt per Newton iteration from the deduplicated upper CSR
 // (off, col, val) and its transpose list (tr_off, tr), leaving out the blocks
-// of Dirichlet vertices (dof_mask, zero after elimination). Reads the slot
-// total back to the host (one synchronization) to size the layout.
+// of Dirichlet vertices (dof_mask, zero after elimination). Reads three
+// totals back to the host (one synchronization) to size the layout.
 void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const float *val,
                     const unsigned *tr_off, const uint2 *tr, const unsigned *dof_mask,
-                    SellLayout &out, DevBuf<unsigned> &slice_k, DevBuf<unsigned> &scan_tmp,
-                    cudaStream_t q);
+                    DynLayout &out, cudaStream_t q);
 inline SellMatrix sell_view(const SellLayout &L) {
     return SellMatrix{L.n_slices, L.slice_off.data(), L.col.data(), L.val.data()};
+}
+inline OverflowRows overflow_view(const DynLayout &D) {
+    return OverflowRows{D.n_ovf, D.ovf_row.data(), D.ovf_range.data(), D.ovf_col.data(),
+                        D.ovf_val.data(), D.ovf_index.data()};
 }
 
 // Diagonal block inverse per row: inv(B(i,i)), written in the slice layout.

@@ -251,7 +251,8 @@ AssemblyBuffers Solver::abuf() {
 }
 
 PcgOperator Solver::pcg_operator() const {
-    return PcgOperator{n_, sell_view(fixed_sell_), sell_view(dyn_sell_), inv_diag_.data()};
+    return PcgOperator{n_, sell_view(fixed_sell_), sell_view(dyn_layout_.sell),
+                       overflow_view(dyn_layout_), inv_diag_.data()};
 }
 
 PieceBuffers Solver::pieces() {
@@ -629,7 +630,7 @@ void Solver::assemble(float dt) {
     // the operator in the PCG's slice layout, and its block-Jacobi inverse
     sell_pack_fixed(fixed_sell_, fixed_val_.data(), q_);
     sell_build_dyn(n_, dyn_.off, dyn_.col, dyn_.val, dyn_.tr_off, dyn_.tr, dof_mask_.data(),
-                   dyn_sell_, dyn_slice_k_, dyn_scan_tmp_, q_);
+                   dyn_layout_, q_);
     launch_block_jacobi(n_, fixed_val_.data(), fixed_diag_.data(), inv_diag_.data(),
                         &st_.data()->status, q_);
 }

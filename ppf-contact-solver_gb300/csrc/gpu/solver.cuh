@@ -119,11 +119,11 @@ class Solver {
     DevBuf<float> dval_buf_;
     DevBuf<unsigned> scan_tmp_;
     PcgWorkspace pcg_;
-    SellLayout fixed_sell_, dyn_sell_;
+    SellLayout fixed_sell_;
+    DynLayout dyn_layout_;
     DevBuf<unsigned> piece_cnt_, piece_off_, piece_tmp_;
     float piece_len_ = 0.0f;
     PieceBuffers pieces();
-    DevBuf<unsigned> dyn_slice_k_, dyn_scan_tmp_;
     DevBuf<IterStatus> st_;
     IterStatus *st_host_ = nullptr;
     DevBuf<float> rescale_;

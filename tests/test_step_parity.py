@@ -164,10 +164,17 @@ def test_trajectory_cloth_sphere_invariants(binding):
 
 
 def test_trajectory_matches_oracle_before_contact(binding):
+    """20 free-fall steps. Each solve stops at a 1e-3 relative residual, and
+    the device assembly adds with float atomics whose order varies from run
+    to run (as the reference's does), so the stopping iteration, and with it
+    the iterate, moves at that tolerance: the trajectories agree to a small
+    fraction of the 0.2 m fall, not bit for bit."""
     sc, _ = scenes.cloth_sphere(16)
+    x0 = sc.positions()[0].copy()
     s = Session(sc)
     o = binding.OracleSession(sc)
     for k in range(20):
         assert s.step().success() and o.step().success()
     xg, xo = s.positions(), o.positions()[0]
-    assert np.abs(xg - xo).max() <= 1e-5 * np.abs(xo).max()
+    fall = np.abs(xo - x0).max()
+    assert np.abs(xg - xo).max() <= 1e-3 * fall, (np.abs(xg - xo).max(), fall)
