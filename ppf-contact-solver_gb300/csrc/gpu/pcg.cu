@@ -23,6 +23,7 @@
 // non-coherent path.
 #include "../physics/eig.cuh"
 #include "assemble.cuh"
+#include "fatal.cuh"
 #include "pcg.cuh"
 
 #include <algorithm>
@@ -34,6 +35,7 @@ namespace {
 
 constexpr unsigned kThreads = 1024; // one block per SM
 constexpr unsigned kWarps = kThreads / 32;
+static_assert(kWarps == 32, "the block fold reads one partial per lane of warp 0");
 constexpr float kCurvatureSlack = 256.0f;
 constexpr float kFloatEps = 1.19209290e-7f;
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull; // 2 s
@@ -46,103 +48,111 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Grid barrier for a cooperative launch (all blocks co-resident). Waits are
-// bounded in wall time; a timeout latches STATUS_PCG_BREAKDOWN in `abort` so
-// every block leaves the solve instead of waiting again.
-__device__ bool grid_barrier(unsigned *bar, unsigned nblocks, unsigned *abort) {
-    __syncthreads();
-    __shared__ int s_ok;
-    if (threadIdx.x == 0) {
-        volatile unsigned *gen = bar + 1;
-        volatile unsigned *ab = abort;
-        unsigned g = *gen;
-        __threadfence();
-        unsigned arrived = atomicAdd(bar, 1u);
-        int ok = 1;
-        if (arrived == nblocks - 1) {
-            bar[0] = 0u;
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            unsigned long long t0 = global_ns();
-            while (*gen == g) {
-                if (*ab) {
-                    ok = 0;
-                    break;
-                }
-                if (global_ns() - t0 > kBarrierTimeoutNs) {
-                    atomicOr(abort, STATUS_PCG_BREAKDOWN);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        __threadfence();
-        s_ok = ok && (*ab == 0u);
-    }
-    __syncthreads();
-    return s_ok != 0;
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned *p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;"
+                 : "=r"(old)
+                 : "l"(p), "r"(v)
+                 : "memory");
+    return old;
+}
+__device__ __forceinline__ void red_add_release(unsigned *p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(unsigned *p, unsigned v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Block sum of two values (fixed order), result on thread 0.
-__device__ void block_sum2(float &a, float &b) {
-    __shared__ float s[2][kWarps];
-    unsigned lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+// Grid-wide sum of two values for a cooperative launch (all blocks
+// co-resident). Each block folds its threads' values (fixed shuffle order),
+// lane 0 of warp 0 stores the block's partials and arrives at the grid
+// barrier with acquire-release semantics (ordering the partials before the
+// arrival); the last block to arrive resets the counter and releases the
+// generation word, the others wait for it with acquire loads. Warp 0 then
+// folds every block's partials in block order, so every block obtains the
+// same bits. `part` alternates between two buffers from one reduction to the
+// next, so a fast block never overwrites partials still being read.
+//
+// The wait is bounded in wall time: a timeout (or an abort latched by
+// another block) sets STATUS_PCG_BREAKDOWN in `abort`, and every block
+// leaves the solve instead of waiting again.
+__device__ bool grid_sum2(float &a, float &b, float *part, unsigned *bar, unsigned nb,
+                          unsigned *abort) {
+    __shared__ float s_w[2][kWarps];
+    __shared__ float s_res[2];
+    __shared__ int s_ok;
+    const unsigned lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     for (int off = 16; off > 0; off >>= 1) {
         a += __shfl_down_sync(0xffffffffu, a, off);
         b += __shfl_down_sync(0xffffffffu, b, off);
     }
     if (lane == 0) {
-        s[0][w] = a;
-        s[1][w] = b;
+        s_w[0][w] = a;
+        s_w[1][w] = b;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        float x = 0.0f, y = 0.0f;
-        for (unsigned k = 0; k < kWarps; ++k) {
-            x += s[0][k];
-            y += s[1][k];
-        }
-        a = x;
-        b = y;
-    }
-    __syncthreads();
-}
-
-// Grid-wide sum of two values: block partials to `part`, barrier, then every
-// block folds the partials in block order (identical result in every block).
-// The callers alternate `part` between two buffers from one reduction to the
-// next, so a fast block writing the next partials never overwrites ones
-// still being read.
-__device__ bool grid_sum2(float &a, float &b, float *part, unsigned *bar, unsigned nb,
-                          unsigned *abort) {
-    block_sum2(a, b);
-    if (threadIdx.x == 0) {
-        part[2 * blockIdx.x] = a;
-        part[2 * blockIdx.x + 1] = b;
-    }
-    if (!grid_barrier(bar, nb, abort)) return false;
-    __shared__ float s[2];
-    if (threadIdx.x < 32) {
-        float x = 0.0f, y = 0.0f;
-        for (unsigned k = threadIdx.x; k < nb; k += 32) {
-            x += __ldcg(part + 2 * k);
-            y += __ldcg(part + 2 * k + 1);
-        }
+    if (w == 0) {
+        float x = s_w[0][lane], y = s_w[1][lane]; // kWarps == 32
         for (int off = 16; off > 0; off >>= 1) {
             x += __shfl_down_sync(0xffffffffu, x, off);
             y += __shfl_down_sync(0xffffffffu, y, off);
         }
-        if (threadIdx.x == 0) {
-            s[0] = x;
-            s[1] = y;
+        int ok = 1;
+        if (lane == 0) {
+            part[2 * blockIdx.x] = x;
+            part[2 * blockIdx.x + 1] = y;
+            unsigned *count = bar, *gen = bar + 1;
+            const unsigned g0 = ld_relaxed(gen);
+            if (atom_add_acq_rel(count, 1u) == nb - 1) {
+                st_relaxed(count, 0u);
+                red_add_release(gen, 1u);
+            } else {
+                const unsigned long long t0 = global_ns();
+                for (unsigned spin = 0; ld_acquire(gen) == g0; ++spin) {
+                    if ((spin & 63u) == 63u) {
+                        if (ld_relaxed(abort) || global_ns() - t0 > kBarrierTimeoutNs) {
+                            atomicOr(abort, STATUS_PCG_BREAKDOWN);
+                            ok = 0;
+                            break;
+                        }
+                    }
+                }
+            }
+            if (ok && ld_relaxed(abort)) ok = 0;
+        }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        __syncwarp();
+        if (ok) {
+            x = y = 0.0f;
+            for (unsigned k = lane; k < nb; k += 32) {
+                x += __ldcg(part + 2 * k);
+                y += __ldcg(part + 2 * k + 1);
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+                x += __shfl_down_sync(0xffffffffu, x, off);
+                y += __shfl_down_sync(0xffffffffu, y, off);
+            }
+        }
+        if (lane == 0) {
+            s_res[0] = x;
+            s_res[1] = y;
+            s_ok = ok;
         }
     }
     __syncthreads();
-    a = s[0];
-    b = s[1];
-    return true;
+    a = s_res[0];
+    b = s_res[1];
+    return s_ok != 0;
 }
 
 __device__ __forceinline__ Vec3 ldcg3(const float *v, unsigned i) {
@@ -261,7 +271,7 @@ struct PcgArgs {
     const unsigned *task_start; // grid + 1: each block's range of product tasks
     float *x, *r;
     float *R;            // 8 floats per vertex: {z, p} records
-    float4 *p, *Ap, *Ap_ovf;
+    float4 *p, *Ap, *Ap_c, *Ap_ovf;
     float *part; // 2 buffers of 2 floats per block
     unsigned *bar;
     float tol;
@@ -310,12 +320,47 @@ struct BlockTasks {
     }
 };
 
-// (A v)(i): the row's slice part plus its overflow part, if any.
+// (A v)(i): the row's fixed part, plus its contact and overflow parts, if any.
 __device__ __forceinline__ Vec3 row_product(const PcgArgs &g, unsigned i) {
     Vec3 ap = ld4(g.Ap, i);
-    const unsigned k = __ldg(g.A.ovf.index + i);
-    if (k != 0xFFFFFFFFu) ap += ld4(g.Ap_ovf, k);
+    const unsigned c = __ldg(g.A.contact.index + i);
+    if (c != 0xFFFFFFFFu) {
+        ap += ld4(g.Ap_c, c);
+        const unsigned k = __ldg(g.A.ovf.index + i);
+        if (k != 0xFFFFFFFFu) ap += ld4(g.Ap_ovf, k);
+    }
     return ap;
+}
+
+// One product task of warp `lane`s: the fixed part of a half slice, the
+// contact part of a half slice of sorted contact rows, or an overflow row.
+// The epilogue gets (row, A-part, |terms|) on the lanes that own a result.
+template <class G, class E>
+__device__ __forceinline__ void product_task(const PcgArgs &g, unsigned task, unsigned lane,
+                                             const G &gather, E &&epilogue) {
+    const PcgOperator &A = g.A;
+    const unsigned t1 = 2 * A.fixed.n_slices, t2 = t1 + 2 * A.contact.sell.n_slices;
+    const unsigned par = lane >> 4;
+    Vec3 acc = Vec3::zero(), ab = Vec3::zero();
+    if (task < t2) {
+        const bool fixed = task < t1;
+        const unsigned u = fixed ? task : task - t1;
+        const unsigned sl = u >> 1, r = (u & 1u) * 16u + (lane & 15u);
+        const unsigned q = sl * kSliceRows + r;
+        sell_half_row(fixed ? A.fixed : A.contact.sell, sl, r, par, gather, acc, ab);
+        join_halves(acc, ab);
+        if (par == 0u) {
+            if (fixed) {
+                if (q < A.n) epilogue(q, 0u, q, acc, ab);
+            } else if (q < A.contact.rows) {
+                epilogue(__ldg(A.contact.perm + q), 1u, q, acc, ab);
+            }
+        }
+    } else {
+        const unsigned k = task - t2;
+        overflow_row(A.ovf, k, lane, gather, acc, ab);
+        if (lane == 0u) epilogue(__ldg(A.ovf.row + k), 2u, k, acc, ab);
+    }
 }
 
 __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
@@ -331,8 +376,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
 
     // work items of the products: half slices (16 rows, two lanes per row),
     // then one warp per overflow row of the contact part
-    const unsigned tasks = 2 * n_slices;
-    const unsigned par = lane >> 4;
 
     __shared__ unsigned s_next;
     const BlockTasks bt{&s_next, g.task_start[blockIdx.x + 1]};
@@ -341,20 +384,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
     __syncthreads();
     {
         const GatherPlain gx{g.x};
-        for (unsigned task = bt.take(lane); task < bt.end; task = bt.take(lane)) {
-            Vec3 acc = Vec3::zero(), ab = Vec3::zero();
-            if (task < tasks) {
-                const unsigned sl = task >> 1, r = (task & 1u) * 16u + (lane & 15u);
-                const unsigned i = sl * kSliceRows + r;
-                sell_half_row(A.fixed, sl, r, par, gx, acc, ab);
-                sell_half_row(A.dyn, sl, r, par, gx, acc, ab);
-                join_halves(acc, ab);
-                if (par == 0u && i < A.n) st4(g.Ap, i, acc);
-            } else {
-                overflow_row(A.ovf, task - tasks, lane, gx, acc, ab);
-                if (lane == 0u) st4(g.Ap_ovf, task - tasks, acc);
-            }
-        }
+        float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
+        for (unsigned task = bt.take(lane); task < bt.end; task = bt.take(lane))
+            product_task(g, task, lane, gx,
+                         [&](unsigned, unsigned part, unsigned slot, const Vec3 &acc, const Vec3 &) {
+                             st4(dst[part], slot, acc);
+                         });
     }
     a = b = 0.0f;
     if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
@@ -389,32 +424,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             const GatherCombined gp{g.R, beta};
             if (threadIdx.x == 0) s_next = g.task_start[blockIdx.x];
             __syncthreads();
-            for (unsigned task = bt.take(lane); task < bt.end; task = bt.take(lane)) {
-                Vec3 acc = Vec3::zero(), ab = Vec3::zero();
-                if (task < tasks) {
-                    const unsigned sl = task >> 1, r = (task & 1u) * 16u + (lane & 15u);
-                    const unsigned i = sl * kSliceRows + r;
-                    sell_half_row(A.fixed, sl, r, par, gp, acc, ab);
-                    sell_half_row(A.dyn, sl, r, par, gp, acc, ab);
-                    join_halves(acc, ab);
-                    if (par == 0u && i < A.n) {
-                        Vec3 pi = gp(i);
-                        st4(g.p, i, pi);
-                        st4(g.Ap, i, acc);
-                        a += pi.dot(acc);
-                        b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] + fabsf(pi[2]) * ab[2];
-                    }
-                } else {
-                    const unsigned k = task - tasks;
-                    overflow_row(A.ovf, k, lane, gp, acc, ab);
-                    if (lane == 0u) {
-                        const Vec3 pi = gp(__ldg(A.ovf.row + k));
-                        st4(g.Ap_ovf, k, acc);
-                        a += pi.dot(acc);
-                        b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] + fabsf(pi[2]) * ab[2];
-                    }
-                }
-            }
+            float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
+            for (unsigned task = bt.take(lane); task < bt.end; task = bt.take(lane))
+                product_task(g, task, lane, gp,
+                             [&](unsigned row, unsigned part, unsigned slot, const Vec3 &acc,
+                                 const Vec3 &ab) {
+                                 const Vec3 pi = gp(row);
+                                 if (part == 0u) st4(g.p, row, pi);
+                                 st4(dst[part], slot, acc);
+                                 a += pi.dot(acc);
+                                 b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] +
+                                      fabsf(pi[2]) * ab[2];
+                             });
             if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
             const float pAp = a, bound = kCurvatureSlack * kFloatEps * b;
             float alpha;
@@ -525,23 +546,38 @@ __device__ __forceinline__ unsigned dyn_row_count(unsigned i, const unsigned *of
     return c;
 }
 
-// Per-row block count, slice width (capped) and overflow count per row.
-__global__ void k_dyn_counts(unsigned n, unsigned n_slices, const unsigned *off,
-                             const unsigned *col, const unsigned *tr_off, const uint2 *tr,
-                             const unsigned *mask, unsigned *slice_k, unsigned *row_ovf,
-                             unsigned *row_flag) {
+// Per-row contact block count: the sort key (descending count, rows without
+// blocks last), the overflow beyond the slice cap, and the row maps reset.
+__global__ void k_contact_rows(unsigned n, const unsigned *off, const unsigned *col,
+                               const unsigned *tr_off, const uint2 *tr, const unsigned *mask,
+                               unsigned *key, unsigned *perm, unsigned *row_ovf,
+                               unsigned *row_flag, unsigned *index, unsigned *ovf_index,
+                               unsigned *n_rows) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned sl = i / kSliceRows;
-    if (sl >= n_slices) return;
-    unsigned c = i < n ? dyn_row_count(i, off, col, tr_off, tr, mask) : 0u;
-    unsigned k = __reduce_max_sync(0xffffffffu, c);
-    if (k > kDynSliceCap) k = kDynSliceCap;
-    if ((i % kSliceRows) == 0) slice_k[sl] = k;
-    if (i < n) {
-        unsigned o = c > k ? c - k : 0u;
-        row_ovf[i] = o;
-        row_flag[i] = o ? 1u : 0u;
+    if (i >= n) return;
+    const unsigned c = dyn_row_count(i, off, col, tr_off, tr, mask);
+    key[i] = c ? 0xFFFFu - (c < 0xFFFEu ? c : 0xFFFEu) : 0xFFFFu;
+    perm[i] = i;
+    const unsigned o = c > kDynSliceCap ? c - kDynSliceCap : 0u;
+    row_ovf[i] = o;
+    row_flag[i] = o ? 1u : 0u;
+    index[i] = 0xFFFFFFFFu;
+    ovf_index[i] = 0xFFFFFFFFu;
+    if (c) atomicAdd(n_rows, 1u);
+}
+
+// Width of each contact slice: its first (longest) row's count, capped.
+__global__ void k_contact_slice_k(unsigned max_slices, const unsigned *n_rows,
+                                  const unsigned *key, unsigned *slice_k) {
+    unsigned sl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sl >= max_slices) return;
+    const unsigned m = *n_rows;
+    unsigned k = 0;
+    if (sl * kSliceRows < m) {
+        unsigned c = 0xFFFFu - key[sl * kSliceRows];
+        k = c < kDynSliceCap ? c : kDynSliceCap;
     }
+    slice_k[sl] = k;
 }
 
 __device__ __forceinline__ void put_slot(unsigned *out_col, float *out_val, unsigned s,
@@ -553,89 +589,91 @@ __device__ __forceinline__ void put_slot(unsigned *out_col, float *out_val, unsi
 }
 
 struct DynFillOut {
-    const unsigned *slice_off, *ovf_off, *flag_off;
+    const unsigned *slice_off, *ovf_off, *flag_off, *perm, *n_rows;
     unsigned *col;
     float *val;
-    unsigned *ovf_row, *ovf_col, *ovf_index;
+    unsigned *index, *ovf_row, *ovf_col, *ovf_index;
     uint2 *ovf_range;
     float *ovf_val;
 };
 
-// Row entries in order: the first K (the slice width) to the slice slots,
-// the rest to the row's overflow range.
-__global__ void k_dyn_fill(unsigned n, unsigned n_slices, const unsigned *off,
-                           const unsigned *col, const float *upper, const unsigned *tr_off,
-                           const uint2 *tr, const unsigned *mask, DynFillOut o) {
-    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned sl = i / kSliceRows, lane = i % kSliceRows;
-    if (sl >= n_slices) return;
+// Sorted position q: the row's entries in order, the first K (the slice
+// width) to the slice slots, the rest to the row's overflow range.
+__global__ void k_contact_fill(unsigned max_slices, const unsigned *off, const unsigned *col,
+                               const float *upper, const unsigned *tr_off, const uint2 *tr,
+                               const unsigned *mask, DynFillOut o) {
+    unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned sl = q / kSliceRows, lane = q % kSliceRows;
+    const unsigned m = *o.n_rows;
+    if (sl >= max_slices || sl * kSliceRows >= m) return;
     const unsigned s0 = o.slice_off[sl], K = o.slice_off[sl + 1] - s0;
-    const unsigned obase = i < n ? o.ovf_off[i] : 0u;
+    const bool real = q < m;
+    const unsigned i = real ? o.perm[q] : o.perm[m - 1];
+    const unsigned obase = real ? o.ovf_off[i] : 0u;
     unsigned k = 0;
-    auto put = [&](unsigned j, const float (&m)[9]) {
+    auto put = [&](unsigned j, const float (&mm)[9]) {
         if (k < K) {
-            put_slot(o.col, o.val, s0 + k, lane, j, m);
+            put_slot(o.col, o.val, s0 + k, lane, j, mm);
         } else {
             unsigned e = obase + (k - K);
             o.ovf_col[e] = j;
 #pragma unroll
-            for (int q = 0; q < 9; ++q) o.ovf_val[9 * (size_t)e + q] = m[q];
+            for (int t = 0; t < 9; ++t) o.ovf_val[9 * (size_t)e + t] = mm[t];
         }
         ++k;
     };
-    if (i < n && !mask[i]) {
-        for (unsigned q = off[i]; q < off[i + 1]; ++q) {
-            unsigned j = col[q];
+    if (real) {
+        for (unsigned p = off[i]; p < off[i + 1]; ++p) {
+            unsigned j = col[p];
             if (mask[j]) continue;
-            const float *b = upper + 9 * (size_t)q;
-            float m[9];
+            const float *b = upper + 9 * (size_t)p;
+            float mm[9];
 #pragma unroll
-            for (int e = 0; e < 9; ++e) m[e] = b[e];
-            put(j, m);
+            for (int e = 0; e < 9; ++e) mm[e] = b[e];
+            put(j, mm);
         }
-        for (unsigned q = tr_off[i]; q < tr_off[i + 1]; ++q) {
-            uint2 rp = tr[q];
+        for (unsigned p = tr_off[i]; p < tr_off[i + 1]; ++p) {
+            uint2 rp = tr[p];
             if (mask[rp.x]) continue;
             const float *b = upper + 9 * (size_t)rp.y;
-            float m[9];
+            float mm[9];
 #pragma unroll
             for (int r = 0; r < 3; ++r)
 #pragma unroll
-                for (int c = 0; c < 3; ++c) m[3 * c + r] = b[3 * r + c];
-            put(rp.x, m);
+                for (int c = 0; c < 3; ++c) mm[3 * c + r] = b[3 * r + c];
+            put(rp.x, mm);
         }
+        o.index[i] = q;
     }
-    const unsigned self = i < n ? i : n - 1;
     const float zero[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (unsigned q = k; q < K; ++q) put_slot(o.col, o.val, s0 + q, lane, self, zero);
-    if (i < n) {
-        if (k > K) {
-            unsigned idx = o.flag_off[i];
-            o.ovf_row[idx] = i;
-            o.ovf_range[idx] = make_uint2(obase, k - K);
-            o.ovf_index[i] = idx;
-        } else {
-            o.ovf_index[i] = 0xFFFFFFFFu;
-        }
+    for (unsigned t = k; t < K; ++t) put_slot(o.col, o.val, s0 + t, lane, i, zero);
+    if (real && k > K) {
+        unsigned idx = o.flag_off[i];
+        o.ovf_row[idx] = i;
+        o.ovf_range[idx] = make_uint2(obase, k - K);
+        o.ovf_index[i] = idx;
     }
 }
 
 // Estimated cost of each product task, in warp slot-steps: a half slice
-// walks half its fixed and contact slots per lane; an overflow row walks its
-// entries 32 at a time. The constant covers the per-task epilogue.
-__global__ void k_task_cost(unsigned n_slices, const unsigned *fixed_off,
-                            const unsigned *dyn_off, unsigned n_ovf, const uint2 *ovf_range,
-                            unsigned *cost) {
+// walks half its slots per lane; an overflow row walks its entries 32 at a
+// time. The constant covers the per-task epilogue. Task order: fixed half
+// slices, contact half slices, overflow rows.
+__global__ void k_task_cost(unsigned n_slices, const unsigned *fixed_off, unsigned c_slices,
+                            const unsigned *contact_off, unsigned n_ovf,
+                            const uint2 *ovf_range, unsigned *cost) {
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned tasks = 2 * n_slices;
-    if (t >= tasks + n_ovf) return;
+    const unsigned t1 = 2 * n_slices, t2 = t1 + 2 * c_slices;
+    if (t >= t2 + n_ovf) return;
     unsigned c;
-    if (t < tasks) {
+    if (t < t1) {
         unsigned sl = t >> 1;
-        unsigned k = (fixed_off[sl + 1] - fixed_off[sl]) + (dyn_off[sl + 1] - dyn_off[sl]);
-        c = (k + 1) / 2;
+        c = (fixed_off[sl + 1] - fixed_off[sl] + 1) / 2;
+    } else if (t < t2) {
+        unsigned sl = (t - t1) >> 1;
+        c = (contact_off[sl + 1] - contact_off[sl] + 1) / 2;
     } else {
-        c = (ovf_range[t - tasks].y + 31) / 32;
+        c = (ovf_range[t - t2].y + 31) / 32;
     }
     cost[t] = c + 2u;
 }
@@ -736,47 +774,64 @@ void sell_pack_fixed(SellLayout &L, const float *upper_val, cudaStream_t q) {
 void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const float *val,
                     const unsigned *tr_off, const uint2 *tr, const unsigned *dof_mask,
                     DynLayout &D, cudaStream_t q) {
-    const unsigned n_slices = (n + kSliceRows - 1) / kSliceRows;
+    const unsigned max_slices = (n + kSliceRows - 1) / kSliceRows;
     SellLayout &out = D.sell;
-    out.n_slices = n_slices;
-    out.slice_off.reserve(n_slices + 1);
-    D.slice_k.reserve(n_slices + 1);
+    out.slice_off.reserve(max_slices + 1);
+    D.key.reserve(n + 1);
+    D.perm.reserve(n + 1);
+    D.index.reserve(n + 1);
+    D.slice_k.reserve(max_slices + 1);
     D.row_ovf.reserve(n + 1);
     D.row_flag.reserve(n + 1);
     D.ovf_off.reserve(n + 1);
     D.flag_off.reserve(n + 1);
     D.ovf_index.reserve(n + 1);
-    D.scan_tmp.reserve(scan_tmp_size(std::max(n, n_slices) + 1));
-    const unsigned threads = n_slices * kSliceRows;
-    k_dyn_counts<<<div_up(threads, 256u), 256, 0, q>>>(n, n_slices, off, col, tr_off, tr,
-                                                       dof_mask, D.slice_k.data(),
-                                                       D.row_ovf.data(), D.row_flag.data());
+    D.counters.reserve(4);
+    D.scan_tmp.reserve(scan_tmp_size(n + 1));
+    PPF_CUDA(cudaMemsetAsync(D.counters.data(), 0, 4 * sizeof(unsigned), q));
+    k_contact_rows<<<div_up(n, 256u), 256, 0, q>>>(n, off, col, tr_off, tr, dof_mask,
+                                                   D.key.data(), D.perm.data(),
+                                                   D.row_ovf.data(), D.row_flag.data(),
+                                                   D.index.data(), D.ovf_index.data(),
+                                                   D.counters.data());
     PPF_LAUNCH_CHECK();
-    exclusive_scan(D.slice_k.data(), out.slice_off.data(), n_slices, D.scan_tmp.data(), q);
+    // stable: rows of equal count keep their index order
+    radix_sort_pairs(D.key.data(), D.perm.data(), n, 16, D.sort_ws, D.counters.data() + 1, q);
+    k_contact_slice_k<<<div_up(max_slices, 256u), 256, 0, q>>>(max_slices, D.counters.data(),
+                                                               D.key.data(), D.slice_k.data());
+    PPF_LAUNCH_CHECK();
+    exclusive_scan(D.slice_k.data(), out.slice_off.data(), max_slices, D.scan_tmp.data(), q);
     exclusive_scan(D.row_ovf.data(), D.ovf_off.data(), n, D.scan_tmp.data(), q);
     exclusive_scan(D.row_flag.data(), D.flag_off.data(), n, D.scan_tmp.data(), q);
-    unsigned totals[3] = {0, 0, 0};
-    PPF_CUDA(cudaMemcpyAsync(&totals[0], out.slice_off.data() + n_slices, sizeof(unsigned),
+    unsigned totals[5] = {0, 0, 0, 0, 0};
+    PPF_CUDA(cudaMemcpyAsync(&totals[0], D.counters.data(), 2 * sizeof(unsigned),
                              cudaMemcpyDeviceToHost, q));
-    PPF_CUDA(cudaMemcpyAsync(&totals[1], D.ovf_off.data() + n, sizeof(unsigned),
+    PPF_CUDA(cudaMemcpyAsync(&totals[2], out.slice_off.data() + max_slices, sizeof(unsigned),
                              cudaMemcpyDeviceToHost, q));
-    PPF_CUDA(cudaMemcpyAsync(&totals[2], D.flag_off.data() + n, sizeof(unsigned),
+    PPF_CUDA(cudaMemcpyAsync(&totals[3], D.ovf_off.data() + n, sizeof(unsigned),
+                             cudaMemcpyDeviceToHost, q));
+    PPF_CUDA(cudaMemcpyAsync(&totals[4], D.flag_off.data() + n, sizeof(unsigned),
                              cudaMemcpyDeviceToHost, q));
     PPF_CUDA(cudaStreamSynchronize(q));
-    out.slots = totals[0];
-    D.ovf_entries = totals[1];
-    D.n_ovf = totals[2];
+    if (totals[1]) throw FatalError(4, "contact-row sort look-back timed out");
+    D.rows = totals[0];
+    out.n_slices = (D.rows + kSliceRows - 1) / kSliceRows;
+    out.slots = totals[2];
+    D.ovf_entries = totals[3];
+    D.n_ovf = totals[4];
     out.col.reserve((size_t)out.slots * kSliceRows + 1);
     out.val.reserve((size_t)out.slots * kSliceRows * 9 + 1);
     D.ovf_col.reserve(D.ovf_entries + 1);
     D.ovf_val.reserve(9 * (size_t)D.ovf_entries + 1);
     D.ovf_row.reserve(D.n_ovf + 1);
     D.ovf_range.reserve(D.n_ovf + 1);
-    DynFillOut o{out.slice_off.data(), D.ovf_off.data(), D.flag_off.data(), out.col.data(),
-                 out.val.data(),       D.ovf_row.data(), D.ovf_col.data(),  D.ovf_index.data(),
-                 D.ovf_range.data(),   D.ovf_val.data()};
-    k_dyn_fill<<<div_up(threads, 256u), 256, 0, q>>>(n, n_slices, off, col, val, tr_off, tr,
-                                                     dof_mask, o);
+    if (!D.rows) return;
+    DynFillOut o{out.slice_off.data(), D.ovf_off.data(), D.flag_off.data(), D.perm.data(),
+                 D.counters.data(),    out.col.data(),   out.val.data(),    D.index.data(),
+                 D.ovf_row.data(),     D.ovf_col.data(), D.ovf_index.data(), D.ovf_range.data(),
+                 D.ovf_val.data()};
+    k_contact_fill<<<div_up(out.n_slices * kSliceRows, 256u), 256, 0, q>>>(
+        out.n_slices, off, col, val, tr_off, tr, dof_mask, o);
     PPF_LAUNCH_CHECK();
 }
 
@@ -793,15 +848,16 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     ws.reserve(A.n);
     PPF_CUDA(cudaMemsetAsync(ws.barrier.data(), 0, 4 * sizeof(unsigned), q));
     ws.Ap_ovf.reserve(A.ovf.count + 1);
+    ws.Ap_c.reserve(A.contact.rows + 1);
     // balanced task ranges per block
-    const unsigned T = 2 * A.fixed.n_slices + A.ovf.count;
+    const unsigned T = 2 * A.fixed.n_slices + 2 * A.contact.sell.n_slices + A.ovf.count;
     ws.task_cost.reserve(T + 1);
     ws.task_off.reserve(T + 1);
     ws.task_start.reserve(ws.grid + 1);
     ws.scan_tmp.reserve(scan_tmp_size(T + 1));
     k_task_cost<<<div_up(T, 256u), 256, 0, q>>>(A.fixed.n_slices, A.fixed.slice_off,
-                                                A.dyn.slice_off, A.ovf.count, A.ovf.range,
-                                                ws.task_cost.data());
+                                                A.contact.sell.n_slices, A.contact.sell.slice_off,
+                                                A.ovf.count, A.ovf.range, ws.task_cost.data());
     PPF_LAUNCH_CHECK();
     exclusive_scan(ws.task_cost.data(), ws.task_off.data(), T, ws.scan_tmp.data(), q);
     k_task_split<<<div_up(ws.grid + 1, 256u), 256, 0, q>>>(T, ws.task_off.data(), ws.grid,
@@ -814,6 +870,7 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
               ws.R.data(),
               ws.p.data(),
               ws.Ap.data(),
+              ws.Ap_c.data(),
               ws.Ap_ovf.data(),
               ws.partials.data(),
               ws.barrier.data(),

@@ -23,6 +23,7 @@
 
 #include <vector>
 
+#include "radix_sort.cuh"
 #include "scene.cuh"
 
 namespace ppf {
@@ -48,12 +49,23 @@ struct OverflowRows {
     const unsigned *index;   // n: overflow row of each vertex, or 0xffffffff
 };
 
+// Contact part: only the rows that have contact blocks, in a stable order of
+// decreasing block count, cut into SELL-32 slices over that order (lane l of
+// slice s is row perm[32 s + l]), so rows of like length share a slice.
+struct ContactRows {
+    unsigned rows;          // rows with contact blocks
+    SellMatrix sell;        // n_slices = ceil(rows / 32)
+    const unsigned *perm;   // sorted position -> row
+    const unsigned *index;  // n: row -> sorted position, or 0xffffffff
+};
+
 // A = fixed part (elastic + inertia + per-vertex terms, diagonal included)
-// + contact part (blocks outside the fixed pattern, SELL up to a width cap
-// plus overflow rows).
+// + contact part (blocks outside the fixed pattern: sorted contact rows up to
+// a width cap, plus overflow rows).
 struct PcgOperator {
     unsigned n;
-    SellMatrix fixed, dyn;
+    SellMatrix fixed;
+    ContactRows contact;
     OverflowRows ovf;
     const float *inv_diag; // block-Jacobi inverse, (slice * 9 + e) * 32 + lane
 };
@@ -72,6 +84,7 @@ struct PcgWorkspace {
     DevBuf<float> R;               // {z, p} record per vertex (8 floats)
     DevBuf<float4> p, Ap;          // one float4 per vertex
     DevBuf<float4> Ap_ovf;         // one per overflow row
+    DevBuf<float4> Ap_c;           // one per contact row (sorted position)
     DevBuf<unsigned> task_cost, task_off, task_start, scan_tmp;
     DevBuf<float> partials;
     DevBuf<unsigned> barrier;
@@ -92,15 +105,17 @@ struct SellLayout {
 
 // Contact slices are at most this many slots wide; longer rows continue in
 // the overflow rows.
-constexpr unsigned kDynSliceCap = 16;
+constexpr unsigned kDynSliceCap = 32;
 
 struct DynLayout {
-    SellLayout sell;
-    DevBuf<unsigned> slice_k, row_ovf, row_flag, ovf_off, flag_off, scan_tmp;
+    SellLayout sell; // over the sorted contact rows
+    DevBuf<unsigned> key, perm, index, slice_k, row_ovf, row_flag, ovf_off, flag_off;
+    DevBuf<unsigned> scan_tmp, counters;
     DevBuf<unsigned> ovf_row, ovf_col, ovf_index;
     DevBuf<uint2> ovf_range;
     DevBuf<float> ovf_val;
-    unsigned n_ovf = 0, ovf_entries = 0;
+    RadixSortWorkspace sort_ws;
+    unsigned rows = 0, n_ovf = 0, ovf_entries = 0;
 };
 
 // Host construction of the fixed layout from the upper pattern and its
@@ -112,13 +127,17 @@ void sell_build_fixed(unsigned n, const std::vector<unsigned> &off,
 void sell_pack_fixed(SellLayout &L, const float *upper_val, cudaStream_t q);
 // Contact part, rebuilt per Newton iteration from the deduplicated upper CSR
 // (off, col, val) and its transpose list (tr_off, tr), leaving out the blocks
-// of Dirichlet vertices (dof_mask, zero after elimination). Reads three
-// totals back to the host (one synchronization) to size the layout.
+// of Dirichlet vertices (dof_mask, zero after elimination). Rows are sorted
+// by block count with the stable radix sort; four totals are read back to
+// the host (one synchronization) to size the layout.
 void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const float *val,
                     const unsigned *tr_off, const uint2 *tr, const unsigned *dof_mask,
                     DynLayout &out, cudaStream_t q);
 inline SellMatrix sell_view(const SellLayout &L) {
     return SellMatrix{L.n_slices, L.slice_off.data(), L.col.data(), L.val.data()};
+}
+inline ContactRows contact_view(const DynLayout &D) {
+    return ContactRows{D.rows, sell_view(D.sell), D.perm.data(), D.index.data()};
 }
 inline OverflowRows overflow_view(const DynLayout &D) {
     return OverflowRows{D.n_ovf, D.ovf_row.data(), D.ovf_range.data(), D.ovf_col.data(),

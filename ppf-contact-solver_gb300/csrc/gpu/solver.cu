@@ -251,7 +251,7 @@ AssemblyBuffers Solver::abuf() {
 }
 
 PcgOperator Solver::pcg_operator() const {
-    return PcgOperator{n_, sell_view(fixed_sell_), sell_view(dyn_layout_.sell),
+    return PcgOperator{n_, sell_view(fixed_sell_), contact_view(dyn_layout_),
                        overflow_view(dyn_layout_), inv_diag_.data()};
 }
 
