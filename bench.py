@@ -131,6 +131,19 @@ def _bytes_per_iter(fixed_blocks: int, dyn_blocks: int, n: int) -> int:
     return 40 * fixed_blocks + 40 * dyn_blocks + 184 * n + 4
 
 
+def aggregate(dist, device, seconds_or_ms: float, newton: int):
+    """Whole-job numbers of a replicas run: the slowest rank's time and the
+    Newton iterations of all ranks (one scene per rank, no data-path
+    collective)."""
+    import torch
+
+    t = torch.tensor([seconds_or_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = torch.tensor([float(newton)], dtype=torch.float64, device=device)
+    dist.all_reduce(n)
+    return float(t.item()), int(n.item())
+
+
 def build_scene(seed: int = 0):
     from ppf_gb300 import scenes
 
@@ -211,12 +224,7 @@ def run_ours(args, rank, local_rank, world):
     total_ms = sum(step_ms)
     # the flush runs between the events' predecessor and start: not timed
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        nt = torch.tensor([newton], device="cuda", dtype=torch.float64)
-        dist.all_reduce(nt)
-        newton_all = int(nt.item())
+        total_ms, newton_all = aggregate(dist, "cuda", total_ms, newton)
     else:
         newton_all = newton
     value = newton_all / (total_ms / 1e3)
@@ -243,11 +251,8 @@ def run_ours(args, rank, local_rank, world):
     e2e_s = time.perf_counter() - t0
     e2e_value = e2e_newton / e2e_s
     if dist:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        nt = torch.tensor([e2e_newton], device="cuda", dtype=torch.float64)
-        dist.all_reduce(nt)
-        e2e_value = float(nt.item()) / float(t.item())
+        e2e_s, e2e_all = aggregate(dist, "cuda", e2e_s, e2e_newton)
+        e2e_value = e2e_all / e2e_s
 
     # ---- roofline of the dominant kernel (the persistent PCG) ----------------
     peak, peak_kind = _peaks()
@@ -255,8 +260,12 @@ def run_ours(args, rank, local_rank, world):
     achieved = pcg_bytes / (pcg_ms_total / 1e3) / 1e9 if pcg_ms_total > 0 else 0.0
     traffic = None
     tfile = ROOT / "profiles" / "pcg_stacked_sheets_traffic.json"
-    if tfile.exists():
-        traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
+    if tfile.exists() and pcg_iters_all:
+        # DRAM bytes per iteration from one ncu capture of a launch of this
+        # workload, scaled to the mean iterations per launch of this run
+        per_iter = json.loads(tfile.read_text()).get("dram_bytes_per_iteration")
+        if per_iter:
+            traffic = int(per_iter * (sum(pcg_iters_all) / len(pcg_iters_all)))
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                 "kernel": "k_pcg (persistent block-Jacobi PCG, one launch per solve)",
