@@ -45,6 +45,40 @@ def reference():
     return _REF
 
 
+_REF_PIPE = None
+
+
+def reference_pipeline():
+    """The reference's own assembly, contact detection, line searches and
+    intersection check compiled from its sources with host shims
+    (oracle/ref_pipeline.cpp), or None where those sources are not available."""
+    global _REF_PIPE
+    if _REF_PIPE is None:
+        path = Path(_build.REF_PIPE_LIB)
+        if not path.exists():
+            return None
+        lib = C.CDLL(str(path))
+        P = C.c_void_p
+        lib.refpipe_init.restype = C.c_bool
+        lib.refpipe_init.argtypes = [P, C.POINTER(abi.ParamSet)]
+        lib.refpipe_state.restype = None
+        lib.refpipe_state.argtypes = [f32p, f32p, C.POINTER(abi.ParamSet)]
+        lib.refpipe_assemble.restype = C.c_uint
+        lib.refpipe_assemble.argtypes = [f32p, f32p, C.c_float]
+        lib.refpipe_blocks.restype = C.c_uint
+        lib.refpipe_blocks.argtypes = [u32p_opt, u32p_opt, f32p_opt]
+        lib.refpipe_force.restype = None
+        lib.refpipe_force.argtypes = [f32p]
+        lib.refpipe_line_search.restype = C.c_float
+        lib.refpipe_line_search.argtypes = [f32p, f32p, C.POINTER(C.c_uint), C.POINTER(C.c_int)]
+        lib.refpipe_strain_line_search.restype = C.c_float
+        lib.refpipe_strain_line_search.argtypes = [f32p, f32p]
+        lib.refpipe_check_intersection.restype = C.c_bool
+        lib.refpipe_check_intersection.argtypes = [f32p]
+        _REF_PIPE = lib
+    return _REF_PIPE
+
+
 def _declare(lib):
     P = C.c_void_p
     lib.oracle_lbvh_build.restype = C.c_uint
@@ -68,6 +102,14 @@ def _declare(lib):
     lib.oracle_newton_system.restype = C.c_int
     lib.oracle_newton_system.argtypes = [f32p, C.POINTER(C.c_uint), C.POINTER(C.c_float)]
     lib.oracle_system_sizes.argtypes = [u32p]
+    lib.oracle_assemble_first.restype = C.c_float
+    lib.oracle_assemble_first.argtypes = [C.c_int, f32p_opt]
+    lib.oracle_param.restype = None
+    lib.oracle_param.argtypes = [C.POINTER(abi.ParamSet)]
+    lib.oracle_line_search_at.restype = C.c_float
+    lib.oracle_line_search_at.argtypes = [f32p, f32p, C.POINTER(C.c_uint), C.POINTER(C.c_int)]
+    lib.oracle_strain_line_search_at.restype = C.c_float
+    lib.oracle_strain_line_search_at.argtypes = [f32p, f32p]
     lib.oracle_system.argtypes = [u32p_opt, u32p_opt, f32p_opt, u32p_opt, u32p_opt, f32p_opt,
                                   f32p_opt, f32p_opt, u32p_opt, u32p_opt, u32p_opt, u32p_opt]
 

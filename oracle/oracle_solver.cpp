@@ -82,6 +82,7 @@ struct Oracle {
     Tree tf, te, tv;
     StepStatsO stats;
     unsigned last_pcg_iters = 0;
+    bool dirichlet = true; // eliminate fix pins after assembly (main.cu:954-1049)
     float last_pcg_resid = 0.0f;
 
     Vec3 X(const std::vector<float> &v, unsigned i) const {
@@ -155,6 +156,7 @@ struct Oracle {
                   const std::vector<std::vector<std::pair<unsigned, const Mat3 *>>> &dy_rows,
                   Vec3 &abssum) const;
     float line_search(unsigned &pin_bad, bool &overlap);
+    float strain_line_search() const;
     bool intersection_free(const std::vector<float> &xx);
     PpfStepResult advance();
     void set_constraint(const PpfConstraint *c);
@@ -710,7 +712,7 @@ void Oracle::assemble(float dt) {
         }
     }
     // Dirichlet elimination
-    if (!fix.empty()) {
+    if (dirichlet && !fix.empty()) {
         auto mask = [&](unsigned v) { return vprop[v].fix_index > 0 && vprop[v].pdrd_body_index == 0; };
         auto presc = [&](unsigned v) { return X(x, v) - X(target, v); };
         auto lift = [&](unsigned row, const Mat3 &blk, const Vec3 &pv, bool tr) {
@@ -867,6 +869,26 @@ int Oracle::solve(unsigned &iters, float &resid) {
             next_check = iter + stride;
         }
     }
+}
+
+// Strain-limit line search of the shells from target to x
+// (strainlimiting/strainlimiting.cu:247-305): the largest t <= T along it.
+float Oracle::strain_line_search() const {
+    const float T = prm.line_search_max_t;
+    float sl = T;
+    for (unsigned i = 0; i < nf; ++i) {
+        const PpfFaceProp &pr = fprop[i];
+        const PpfFaceParam &fp = fparam[pr.param_index];
+        if (pr.fixed || pr.rest_excluded || !(fp.strainlimit > 0.0f)) continue;
+        float limit = strain::effective_limit(fp.strainlimit, fp.shrink_x, fp.shrink_y);
+        const unsigned *f = &face[3 * i];
+        Mat2 inv;
+        for (int k = 0; k < 4; ++k) inv.m[k] = inv_rest[4 * i + k];
+        Mat3x2 F0 = bw::deformation_grad(X(target, f[0]), X(target, f[1]), X(target, f[2]), inv);
+        Mat3x2 F1 = bw::deformation_grad(X(x, f[0]), X(x, f[1]), X(x, f[2]), inv);
+        sl = std::fmin(sl, strain::line_search(F0, F1, limit, T));
+    }
+    return sl;
 }
 
 float Oracle::line_search(unsigned &pin_bad, bool &overlap) {
@@ -1136,20 +1158,7 @@ PpfStepResult Oracle::advance() {
             res.contact_separated = false;
             return res;
         }
-        float sl = T;
-        for (unsigned i = 0; i < nf; ++i) {
-            const PpfFaceProp &pr = fprop[i];
-            const PpfFaceParam &fp = fparam[pr.param_index];
-            if (pr.fixed || pr.rest_excluded || !(fp.strainlimit > 0.0f)) continue;
-            float limit = strain::effective_limit(fp.strainlimit, fp.shrink_x, fp.shrink_y);
-            const unsigned *f = &face[3 * i];
-            Mat2 inv;
-            for (int k = 0; k < 4; ++k) inv.m[k] = inv_rest[4 * i + k];
-            Mat3x2 F0 = bw::deformation_grad(X(target, f[0]), X(target, f[1]), X(target, f[2]), inv);
-            Mat3x2 F1 = bw::deformation_grad(X(x, f[0]), X(x, f[1]), X(x, f[2]), inv);
-            sl = std::fmin(sl, strain::line_search(F0, F1, limit, T));
-        }
-        toi = std::fmin(toi, sl / T);
+        toi = std::fmin(toi, strain_line_search() / T);
         if (toi <= 1.19209290e-7f) {
             res.ccd_success = false;
             return res;
@@ -1283,6 +1292,43 @@ void oracle_system(unsigned *f_off, unsigned *f_col, float *f_val, unsigned *d_o
     put3(pe, o.pe);
     put3(pp, o.pp);
     put2(ee, o.ee);
+}
+
+// The first Newton system of the step at the current state, assembled and
+// kept without solving; `dirichlet` = 0 keeps the fix-pin rows as assembled.
+// Writes the step's target and returns dt.
+float oracle_assemble_first(int dirichlet, float *target_out) {
+    Oracle &o = *g_oracle;
+    float dt = o.prm.dt * o.prm.playback;
+    o.compute_target(dt);
+    o.x = o.curr;
+    o.dirichlet = dirichlet != 0;
+    o.assemble(dt);
+    o.dirichlet = true;
+    if (target_out) std::memcpy(target_out, o.target.data(), o.target.size() * sizeof(float));
+    return dt;
+}
+
+void oracle_param(PpfParamSet *out) { *out = g_oracle->prm; }
+
+// Contact line search and strain-limit line search from x0 to x1 (trees
+// swept over x0 -> x0 + T (x1 - x0)), as one Newton iteration runs them.
+float oracle_line_search_at(const float *x0, const float *x1, unsigned *pin_bad, int *overlap) {
+    Oracle &o = *g_oracle;
+    o.target.assign(x0, x0 + 3 * (size_t)o.n);
+    o.x.assign(x1, x1 + 3 * (size_t)o.n);
+    o.trees(o.target, o.x, o.prm.line_search_max_t);
+    bool ov = false;
+    float toi = o.line_search(*pin_bad, ov);
+    *overlap = ov ? 1 : 0;
+    return toi;
+}
+
+float oracle_strain_line_search_at(const float *x0, const float *x1) {
+    Oracle &o = *g_oracle;
+    o.target.assign(x0, x0 + 3 * (size_t)o.n);
+    o.x.assign(x1, x1 + 3 * (size_t)o.n);
+    return o.strain_line_search();
 }
 
 } // extern "C"

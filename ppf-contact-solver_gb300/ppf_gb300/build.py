@@ -29,6 +29,7 @@ PRODUCT_LIB = LIBDIR / "libppf_gb300.so"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "liboracle_ppf.so"
 REF_LIB = ORACLE_DIR / "_ref" / "libppfref.so"
+REF_PIPE_LIB = ORACLE_DIR / "_ref" / "libppfref_pipe.so"
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 CXX = os.environ.get("CXX", "g++")
