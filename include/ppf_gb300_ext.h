@@ -91,8 +91,33 @@ typedef struct {
     unsigned fixed_blocks;
     unsigned vertices;
     unsigned dyn_blocks[PPF_STATS_MAX_SOLVES];
+    /* the preconditioner of the step's solves (PPF_PRECOND_*), how many of
+     * its solves fell back to block-Jacobi, and the iterations the factored
+     * preconditioner ran (included in pcg_iters_total and pcg_iters) */
+    unsigned precond_kind;
+    unsigned fallbacks;
+    unsigned factor_iters_total;
 } PpfStepStats;
 void ppf_step_stats(PpfStepStats *out);
+
+/* ---- preconditioner --------------------------------------------------------
+ * The reference's PCG uses block-Jacobi (solver/solver.cu:357-400), the
+ * default here. The factored kinds use P = G^T G + eps D^{-1} with G block
+ * lower-triangular on the operator's own pattern (D: the diagonal blocks):
+ *   PPF_PRECOND_FIRST_ORDER  G from the block-Jacobi-normalised operator,
+ *                            G = I - param * (strict lower part); param 0.5
+ *   PPF_PRECOND_LEARNED      G emitted by the message-passing network whose
+ *                            weights ppf_set_learned_weights loaded
+ * A factored solve runs to the same relative residual with at most as many
+ * iterations as the last block-Jacobi solve took; when it stalls or reaches
+ * that count, the Newton iteration solves again with block-Jacobi from the
+ * same start (the first solve of a session is block-Jacobi, which sets the
+ * count). Returns 0, or -1 for an unknown kind or a learned kind without
+ * weights. */
+#define PPF_PRECOND_BLOCK_JACOBI 0
+#define PPF_PRECOND_FIRST_ORDER 1
+#define PPF_PRECOND_LEARNED 2
+int ppf_set_preconditioner(int kind, float param);
 
 /* The CUDA stream (cudaStream_t, as void*) every kernel of advance() runs
  * on, so a host can time the step with its own events on that stream. NULL

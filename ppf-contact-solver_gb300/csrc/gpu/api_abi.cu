@@ -205,6 +205,13 @@ void ppf_step_stats(PpfStepStats *out) {
     }
     out->fixed_blocks = solver_instance().fixed_blocks();
     out->vertices = solver_instance().vertices();
+    out->precond_kind = (unsigned)solver_instance().preconditioner();
+    out->fallbacks = s.fallbacks;
+    out->factor_iters_total = s.factor_iters_total;
+}
+
+int ppf_set_preconditioner(int kind, float param) {
+    return solver_instance().set_preconditioner(kind, param) ? 0 : -1;
 }
 
 void *ppf_stream(void) { return (void *)solver_instance().stream(); }

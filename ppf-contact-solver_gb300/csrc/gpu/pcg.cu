@@ -202,12 +202,29 @@ struct GatherPlain {
     const float *x;
     __device__ __forceinline__ Vec3 operator()(unsigned j) const { return ldcg3(x, j); }
 };
+struct GatherY {
+    const float4 *Y;
+    __device__ __forceinline__ Vec3 operator()(unsigned j) const { return ld4(Y, j); }
+};
 
-// One slot's block times its neighbour value.
-template <class G>
+// Which slots a product takes: all of them, only those below the diagonal
+// of their row (column < row), or only those above it (column > row).
+enum SlotMask : int { kAllSlots = 0, kBelow = 1, kAbove = 2 };
+
+template <int MASK>
+__device__ __forceinline__ bool takes(unsigned j, unsigned row) {
+    if (MASK == kBelow) return j < row;
+    if (MASK == kAbove) return j > row;
+    return true;
+}
+
+// One slot's block times its neighbour value. `row` is the slot's row
+// (0xffffffff for a lane without one, which a masked product then skips).
+template <int MASK, class G>
 __device__ __forceinline__ void slot_term(const SellMatrix &M, size_t s, unsigned lane,
-                                          unsigned j, const G &gather, Vec3 &acc,
+                                          unsigned j, unsigned row, const G &gather, Vec3 &acc,
                                           Vec3 &abssum) {
+    if (MASK != kAllSlots && (row == 0xFFFFFFFFu || !takes<MASK>(j, row))) return;
     const float *a = M.val + s * 9 * kSliceRows + lane;
     float m[9];
 #pragma unroll
@@ -228,11 +245,16 @@ __device__ __forceinline__ void slot_term(const SellMatrix &M, size_t s, unsigne
 // 64-byte runs, one per parity. abssum collects the component-wise |term| of
 // every block product. Slots are taken four at a time (column indices first)
 // so four gathers are in flight per lane.
-template <class G>
+template <int MASK, class G>
 __device__ __forceinline__ void sell_half_row(const SellMatrix &M, unsigned slice, unsigned r,
-                                              unsigned par, const G &gather, Vec3 &acc,
-                                              Vec3 &abssum) {
-    const unsigned s0 = __ldg(M.slice_off + slice), s1 = __ldg(M.slice_off + slice + 1);
+                                              unsigned par, unsigned row, const G &gather,
+                                              Vec3 &acc, Vec3 &abssum) {
+    unsigned s0 = __ldg(M.slice_off + slice), s1 = __ldg(M.slice_off + slice + 1);
+    if (MASK != kAllSlots && M.slice_mid) {
+        const unsigned mid = __ldg(M.slice_mid + slice);
+        if (MASK == kBelow) s1 = mid;
+        else s0 = mid;
+    }
     unsigned s = s0 + par;
     for (; s + 6 < s1; s += 8) {
         unsigned j[4];
@@ -240,11 +262,12 @@ __device__ __forceinline__ void sell_half_row(const SellMatrix &M, unsigned slic
         for (int q = 0; q < 4; ++q)
             j[q] = __ldg(M.col + (size_t)(s + 2 * q) * kSliceRows + r);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) slot_term(M, s + 2 * q, r, j[q], gather, acc, abssum);
+        for (int q = 0; q < 4; ++q)
+            slot_term<MASK>(M, s + 2 * q, r, j[q], row, gather, acc, abssum);
     }
     for (; s < s1; s += 2) {
         const unsigned j = __ldg(M.col + (size_t)s * kSliceRows + r);
-        slot_term(M, s, r, j, gather, acc, abssum);
+        slot_term<MASK>(M, s, r, j, row, gather, acc, abssum);
     }
 }
 
@@ -268,26 +291,35 @@ __device__ __forceinline__ Mat3 load_inv(const float *inv, unsigned slice, unsig
 
 struct PcgArgs {
     PcgOperator A;
-    const unsigned *task_start; // grid + 1: each block's range of product tasks
+    const unsigned *task_start; // grid + 1: each block's static range of product
+                                // tasks; task_start[grid] starts the common pool
+    unsigned n_tasks;
+    unsigned *dyn_ctr;          // one zeroed counter per product phase
+    unsigned n_ctr;
     float *x, *r;
     float *R;            // 8 floats per vertex: {z, p} records
     float4 *p, *Ap, *Ap_c, *Ap_ovf;
+    float4 *Y;   // G r of the factored preconditioner
     float *part; // 2 buffers of 2 floats per block
     unsigned *bar;
     float tol;
     unsigned max_iter;
     PcgResult *res;
+    const unsigned *run_if; // null, or the solve runs only when *run_if != 0
 };
 
 // Overflow row k of the contact part: the whole warp strides its entries and
 // folds the partial products in a fixed shuffle order. Result on lane 0.
-template <class G>
-__device__ __forceinline__ void overflow_row(const OverflowRows &O, unsigned k, unsigned lane,
-                                             const G &gather, Vec3 &acc, Vec3 &abssum) {
+template <int MASK, class G>
+__device__ __forceinline__ void overflow_row(const OverflowRows &O, const float *vals,
+                                             unsigned k, unsigned lane, const G &gather,
+                                             Vec3 &acc, Vec3 &abssum) {
     const uint2 rg = __ldg(O.range + k);
+    const unsigned row = MASK == kAllSlots ? 0u : __ldg(O.row + k);
     for (unsigned e = rg.x + lane; e < rg.x + rg.y; e += 32u) {
         const unsigned j = __ldg(O.col + e);
-        const float *a = O.val + 9 * (size_t)e;
+        if (!takes<MASK>(j, row)) continue;
+        const float *a = vals + 9 * (size_t)e;
         float m[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) m[q] = __ldg(a + q);
@@ -308,14 +340,43 @@ __device__ __forceinline__ void overflow_row(const OverflowRows &O, unsigned k, 
         }
 }
 
-// The block's product tasks, handed to its warps one at a time through a
-// shared counter (a block's range holds about 1/grid of the slot work).
+constexpr unsigned kNoTask = 0xFFFFFFFFu;
+// Share of the product work (in sixteenths of its cost) split statically
+// among the blocks; the rest, the last tasks in order (contact rows and
+// overflow rows), goes to whichever warps finish first.
+constexpr unsigned kStaticSixteenths = 12;
+
+// The product tasks of one phase: first the block's static range, handed to
+// its warps one at a time through a shared counter, then tasks of the common
+// pool [dyn0, total) through the phase's global counter. Each product phase
+// of a solve has its own counter (zeroed before the launch).
 struct BlockTasks {
-    unsigned *next; // shared
-    unsigned end;
+    unsigned *next;       // shared
+    unsigned begin, end;  // this block's static range
+    unsigned dyn0, total; // the common pool
+    unsigned *ctrs;       // one per phase
+    unsigned n_ctrs;
+    unsigned phase = 0;
+    unsigned *ctr = nullptr;
+    // Starts a product phase (every thread of the block calls it).
+    __device__ __forceinline__ void start() {
+        ctr = phase < n_ctrs ? ctrs + phase : nullptr;
+        ++phase;
+        if (threadIdx.x == 0) *next = begin;
+        __syncthreads();
+    }
     __device__ __forceinline__ unsigned take(unsigned lane) const {
         unsigned t = 0;
-        if (lane == 0u) t = atomicAdd(next, 1u);
+        if (lane == 0u) {
+            t = atomicAdd(next, 1u);
+            if (t >= end) {
+                t = kNoTask;
+                if (ctr) {
+                    const unsigned d = atomicAdd(ctr, 1u);
+                    if (d < total - dyn0) t = dyn0 + d;
+                }
+            }
+        }
         return __shfl_sync(0xffffffffu, t, 0);
     }
 };
@@ -335,9 +396,12 @@ __device__ __forceinline__ Vec3 row_product(const PcgArgs &g, unsigned i) {
 // One product task of warp `lane`s: the fixed part of a half slice, the
 // contact part of a half slice of sorted contact rows, or an overflow row.
 // The epilogue gets (row, A-part, |terms|) on the lanes that own a result.
-template <class G, class E>
-__device__ __forceinline__ void product_task(const PcgArgs &g, unsigned task, unsigned lane,
-                                             const G &gather, E &&epilogue) {
+// `vals` are the value arrays the slots are read from: the operator's own
+// (fixed, contact, overflow) or a factor's parallel ones.
+template <int MASK, class G, class E>
+__device__ __forceinline__ void product_task(const PcgArgs &g, const float *const vals[3],
+                                             unsigned task, unsigned lane, const G &gather,
+                                             E &&epilogue) {
     const PcgOperator &A = g.A;
     const unsigned t1 = 2 * A.fixed.n_slices, t2 = t1 + 2 * A.contact.sell.n_slices;
     const unsigned par = lane >> 4;
@@ -347,7 +411,14 @@ __device__ __forceinline__ void product_task(const PcgArgs &g, unsigned task, un
         const unsigned u = fixed ? task : task - t1;
         const unsigned sl = u >> 1, r = (u & 1u) * 16u + (lane & 15u);
         const unsigned q = sl * kSliceRows + r;
-        sell_half_row(fixed ? A.fixed : A.contact.sell, sl, r, par, gather, acc, ab);
+        SellMatrix M = fixed ? A.fixed : A.contact.sell;
+        M.val = vals[fixed ? 0 : 1];
+        unsigned row = 0xFFFFFFFFu;
+        if (MASK != kAllSlots) {
+            if (fixed) row = q < A.n ? q : 0xFFFFFFFFu;
+            else row = q < A.contact.rows ? __ldg(A.contact.perm + q) : 0xFFFFFFFFu;
+        }
+        sell_half_row<MASK>(M, sl, r, par, row, gather, acc, ab);
         join_halves(acc, ab);
         if (par == 0u) {
             if (fixed) {
@@ -358,12 +429,14 @@ __device__ __forceinline__ void product_task(const PcgArgs &g, unsigned task, un
         }
     } else {
         const unsigned k = task - t2;
-        overflow_row(A.ovf, k, lane, gather, acc, ab);
+        overflow_row<MASK>(A.ovf, vals[2], k, lane, gather, acc, ab);
         if (lane == 0u) epilogue(__ldg(A.ovf.row + k), 2u, k, acc, ab);
     }
 }
 
 __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
+    // a conditional solve that is not needed leaves everything as it is
+    if (g.run_if && *g.run_if == 0u) return;
     const PcgOperator &A = g.A;
     const unsigned nb = gridDim.x;
     const unsigned lane = threadIdx.x & 31u;
@@ -378,15 +451,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
     // then one warp per overflow row of the contact part
 
     __shared__ unsigned s_next;
-    const BlockTasks bt{&s_next, g.task_start[blockIdx.x + 1]};
+    BlockTasks bt{&s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
+                  g.task_start[gridDim.x], g.n_tasks, g.dyn_ctr, g.n_ctr};
     // A x0 (slice part to Ap, overflow part to Ap_ovf) ...
-    if (threadIdx.x == 0) s_next = g.task_start[blockIdx.x];
-    __syncthreads();
+    bt.start();
     {
         const GatherPlain gx{g.x};
         float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
-        for (unsigned task = bt.take(lane); task < bt.end; task = bt.take(lane))
-            product_task(g, task, lane, gx,
+        const float *const vals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
+        for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
+            product_task<kAllSlots>(g, vals, task, lane, gx,
                          [&](unsigned, unsigned part, unsigned slot, const Vec3 &acc, const Vec3 &) {
                              st4(dst[part], slot, acc);
                          });
@@ -422,11 +496,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             // S: A p_k with p_k = z + beta p_{k-1}
             a = b = 0.0f; // p^T A p, sum |p_i| |terms|
             const GatherCombined gp{g.R, beta};
-            if (threadIdx.x == 0) s_next = g.task_start[blockIdx.x];
-            __syncthreads();
+            bt.start();
             float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
-            for (unsigned task = bt.take(lane); task < bt.end; task = bt.take(lane))
-                product_task(g, task, lane, gp,
+            const float *const vals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
+            for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
+                product_task<kAllSlots>(g, vals, task, lane, gp,
                              [&](unsigned row, unsigned part, unsigned slot, const Vec3 &acc,
                                  const Vec3 &ab) {
                                  const Vec3 pi = gp(row);
@@ -468,6 +542,195 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             }
             if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
             const float rz_new = a, err_now = b;
+            beta = rz_new / rz0;
+            rz0 = rz_new;
+            const bool at_cap = iter >= g.max_iter;
+            if (iter == next_check || at_cap) {
+                const float reresid = err_now / err0;
+                PcgResult out{iter, reresid, -1, broke, err0, break_val, 0u};
+                if (reresid < g.tol) out.state = 0;
+                else if (broke == 3) out.state = 1;
+                else if (broke == 1) out.state = 2;
+                else if (!isfinite(reresid) || at_cap) out.state = 2;
+                if (out.state >= 0) {
+                    if (blockIdx.x == 0 && threadIdx.x == 0) *g.res = out;
+                    return;
+                }
+                if (reresid < 8.0f * g.tol) stride = 1;
+                next_check = iter + stride;
+            }
+        }
+    }
+aborted:
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        *g.res = PcgResult{0u, 0.0f, 2, 0, 0.0f, 0.0f, STATUS_PCG_BREAKDOWN};
+}
+
+// z = P r with P = G^T G + eps D^{-1}, after r is final grid-wide and the
+// records hold z = 0 and Y = 0 (the caller's update phase wrote them):
+//   Z1: y = G r      (slots below the diagonal plus the diagonal blocks)
+//   Z2: z = G^T y + eps D^{-1} r  (slots above the diagonal plus the
+//       transposed diagonal blocks), added into the records' z
+// Each row's parts (fixed, contact, overflow) are added with atomics; r^T z
+// is linear in them, so its partial sums need no complete z. Returns false
+// when the grid barrier aborted; rz gets the grid-wide r^T z.
+__device__ bool apply_factor(const PcgArgs &g, BlockTasks &bt, unsigned lane, float *part_a,
+                             float *part_b, unsigned *abort, float &rz) {
+    const PcgOperator &A = g.A;
+    const unsigned nb = gridDim.x;
+    const float *const vals[3] = {A.factor.fixed, A.factor.contact, A.factor.ovf};
+    bt.start();
+    {
+        const GatherPlain gr{g.r};
+        for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
+            product_task<kBelow>(g, vals, task, lane, gr,
+                                 [&](unsigned row, unsigned part, unsigned, Vec3 acc, const Vec3 &) {
+                                     if (part == 0u)
+                                         acc += load_mat3(A.factor.diag + 9 * (size_t)row) *
+                                                ldcg3(g.r, row);
+                                     float *y = reinterpret_cast<float *>(g.Y + row);
+                                     atomicAdd(y, acc[0]);
+                                     atomicAdd(y + 1, acc[1]);
+                                     atomicAdd(y + 2, acc[2]);
+                                 });
+    }
+    float a = 0.0f, b = 0.0f;
+    if (!grid_sum2(a, b, part_a, g.bar, nb, abort)) return false;
+    bt.start();
+    a = 0.0f;
+    {
+        const GatherY gy{g.Y};
+        for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
+            product_task<kAbove>(g, vals, task, lane, gy,
+                                 [&](unsigned row, unsigned part, unsigned, Vec3 acc, const Vec3 &) {
+                                     const Vec3 ri = ldcg3(g.r, row);
+                                     if (part == 0u) {
+                                         acc += load_mat3(A.factor.diag + 9 * (size_t)row)
+                                                    .transpose() *
+                                                gy(row);
+                                         acc += A.factor.eps *
+                                                (load_inv(A.inv_diag, row / kSliceRows,
+                                                          row % kSliceRows) *
+                                                 ri);
+                                     }
+                                     float *z = g.R + 8 * (size_t)row;
+                                     atomicAdd(z, acc[0]);
+                                     atomicAdd(z + 1, acc[1]);
+                                     atomicAdd(z + 2, acc[2]);
+                                     a += ri.dot(acc);
+                                 });
+    }
+    b = 0.0f;
+    if (!grid_sum2(a, b, part_b, g.bar, nb, abort)) return false;
+    rz = a;
+    return true;
+}
+
+// PCG with the factored preconditioner: the recurrence, verdicts and checks
+// of k_pcg, with z = P r computed by apply_factor after each update (two
+// more grid barriers per iteration).
+__global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
+    const PcgOperator &A = g.A;
+    const unsigned nb = gridDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned n_slices = A.fixed.n_slices;
+    unsigned *abort = g.bar + 2;
+    float *part0 = g.part, *part1 = g.part + 2 * nb;
+    float a, b;
+
+    __shared__ unsigned s_next;
+    BlockTasks bt{&s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
+                  g.task_start[gridDim.x], g.n_tasks, g.dyn_ctr, g.n_ctr};
+    const float *const avals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
+    // A x0
+    bt.start();
+    {
+        const GatherPlain gx{g.x};
+        float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
+        for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
+            product_task<kAllSlots>(g, avals, task, lane, gx,
+                                    [&](unsigned, unsigned part, unsigned slot, const Vec3 &acc,
+                                        const Vec3 &) { st4(dst[part], slot, acc); });
+    }
+    a = b = 0.0f;
+    if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
+    // r = b - A x0, err0 = |r|_1; records {0, 0}, Y = 0
+    a = b = 0.0f;
+    for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
+        const unsigned i = sl * kSliceRows + lane;
+        if (i >= A.n) continue;
+        Vec3 ri = ldcg3(g.r, i) - row_product(g, i);
+        st3(g.r, i, ri);
+        st_record(g.R, i, Vec3::zero(), Vec3::zero());
+        st4(g.Y, i, Vec3::zero());
+        a += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
+    }
+    if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+    {
+        const float err0 = a;
+        if (err0 == 0.0f) {
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+                *g.res = PcgResult{1u, 0.0f, 0, 0, 0.0f, 0.0f, 0u};
+            return;
+        }
+        float rz0;
+        if (!apply_factor(g, bt, lane, part1, part0, abort, rz0)) goto aborted;
+        float beta = 0.0f;
+        unsigned stride = 4, next_check = 1;
+        int broke = 0;
+        float break_val = 0.0f;
+        for (unsigned iter = 1;; ++iter) {
+            // S: A p_k with p_k = z + beta p_{k-1}
+            a = b = 0.0f;
+            const GatherCombined gp{g.R, beta};
+            bt.start();
+            float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
+            for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
+                product_task<kAllSlots>(g, avals, task, lane, gp,
+                                        [&](unsigned row, unsigned part, unsigned slot,
+                                            const Vec3 &acc, const Vec3 &ab) {
+                                            const Vec3 pi = gp(row);
+                                            if (part == 0u) st4(g.p, row, pi);
+                                            st4(dst[part], slot, acc);
+                                            a += pi.dot(acc);
+                                            b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] +
+                                                 fabsf(pi[2]) * ab[2];
+                                        });
+            if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
+            const float pAp = a, bound = kCurvatureSlack * kFloatEps * b;
+            float alpha;
+            if (pAp > bound) {
+                alpha = rz0 / pAp;
+            } else {
+                alpha = 0.0f;
+                if (!broke) {
+                    broke = (pAp < -bound || pAp != pAp) ? 1 : 3;
+                    break_val = pAp;
+                }
+            }
+            // U: x += alpha p, r -= alpha A p; records {0, p}, Y = 0; |r|_1
+            a = b = 0.0f;
+            for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
+                const unsigned i = sl * kSliceRows + lane;
+                if (i >= A.n) continue;
+                Vec3 pi = ld4(g.p, i), api = row_product(g, i);
+                Vec3 xi = ldcg3(g.x, i), ri = ldcg3(g.r, i);
+                for (int k = 0; k < 3; ++k) {
+                    xi[k] += alpha * pi[k];
+                    ri[k] = ri[k] - alpha * api[k];
+                }
+                st3(g.x, i, xi);
+                st3(g.r, i, ri);
+                st_record(g.R, i, Vec3::zero(), pi);
+                st4(g.Y, i, Vec3::zero());
+                b += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
+            }
+            if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+            const float err_now = b;
+            float rz_new;
+            if (!apply_factor(g, bt, lane, part1, part0, abort, rz_new)) goto aborted;
             beta = rz_new / rz0;
             rz0 = rz_new;
             const bool at_cap = iter >= g.max_iter;
@@ -678,12 +941,14 @@ __global__ void k_task_cost(unsigned n_slices, const unsigned *fixed_off, unsign
     cost[t] = c + 2u;
 }
 
-// Block b takes the tasks whose cost prefix falls in [b W / nb, (b+1) W / nb).
+// Block b takes the tasks whose cost prefix falls in [b Ws / nb,
+// (b+1) Ws / nb), Ws the static share of the total cost W; start[nb] is the
+// first task of the common pool.
 __global__ void k_task_split(unsigned T, const unsigned *cost_off, unsigned nb,
                              unsigned *start) {
     unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b > nb) return;
-    const unsigned long long W = cost_off[T];
+    const unsigned long long W = (unsigned long long)cost_off[T] * kStaticSixteenths / 16u;
     const unsigned long long target = W * b / nb;
     unsigned lo = 0, hi = T; // first t with cost_off[t] >= target
     while (lo < hi) {
@@ -691,7 +956,7 @@ __global__ void k_task_split(unsigned T, const unsigned *cost_off, unsigned nb,
         if ((unsigned long long)cost_off[mid] < target) lo = mid + 1;
         else hi = mid;
     }
-    start[b] = (b == nb) ? T : lo;
+    start[b] = lo;
 }
 
 } // namespace
@@ -700,6 +965,7 @@ void PcgWorkspace::reserve(unsigned n) {
     R.reserve(8 * (size_t)n);
     p.reserve(n);
     Ap.reserve(n);
+    Y.reserve(n);
     if (grid == 0) {
         int dev = 0, sms = 0, per_sm = 0;
         PPF_CUDA(cudaGetDevice(&dev));
@@ -719,15 +985,17 @@ void sell_build_fixed(unsigned n, const std::vector<unsigned> &off,
                       const std::vector<unsigned> &col, const std::vector<unsigned> &tr_off,
                       const std::vector<uint2> &tr, SellLayout &out) {
     const unsigned n_slices = (n + kSliceRows - 1) / kSliceRows;
-    std::vector<unsigned> slice_off(n_slices + 1, 0u);
+    std::vector<unsigned> slice_off(n_slices + 1, 0u), slice_mid(n_slices, 0u);
     for (unsigned sl = 0; sl < n_slices; ++sl) {
-        unsigned k = 0;
+        unsigned kl = 0, ku = 0;
         for (unsigned l = 0; l < kSliceRows; ++l) {
             unsigned i = sl * kSliceRows + l;
             if (i >= n) break;
-            k = std::max(k, (off[i + 1] - off[i]) + (tr_off[i + 1] - tr_off[i]));
+            kl = std::max(kl, tr_off[i + 1] - tr_off[i]);
+            ku = std::max(ku, off[i + 1] - off[i]);
         }
-        slice_off[sl + 1] = slice_off[sl] + k;
+        slice_mid[sl] = slice_off[sl] + kl;
+        slice_off[sl + 1] = slice_mid[sl] + ku;
     }
     const unsigned slots = slice_off[n_slices];
     std::vector<unsigned> c((size_t)slots * kSliceRows), src((size_t)slots * kSliceRows);
@@ -735,22 +1003,26 @@ void sell_build_fixed(unsigned n, const std::vector<unsigned> &off,
         for (unsigned l = 0; l < kSliceRows; ++l) {
             unsigned i = sl * kSliceRows + l;
             unsigned self = i < n ? i : n - 1;
-            unsigned k = 0;
-            auto put = [&](unsigned j, unsigned s) {
-                size_t e = (size_t)(slice_off[sl] + k) * kSliceRows + l;
+            auto put = [&](unsigned slot, unsigned j, unsigned s) {
+                size_t e = (size_t)slot * kSliceRows + l;
                 c[e] = j;
                 src[e] = s;
-                ++k;
             };
-            if (i < n) {
-                for (unsigned q = off[i]; q < off[i + 1]; ++q) put(col[q], q);
+            unsigned k = slice_off[sl];
+            if (i < n)
                 for (unsigned q = tr_off[i]; q < tr_off[i + 1]; ++q)
-                    put(tr[q].x, tr[q].y | kTransposed);
-            }
-            while (slice_off[sl] + k < slice_off[sl + 1]) put(self, kPad);
+                    put(k++, tr[q].x, tr[q].y | kTransposed);
+            while (k < slice_mid[sl]) put(k++, self, kPad);
+            if (i < n)
+                for (unsigned q = off[i]; q < off[i + 1]; ++q) put(k++, col[q], q);
+            while (k < slice_off[sl + 1]) put(k++, self, kPad);
         }
     out.n_slices = n_slices;
     out.slots = slots;
+    out.slice_mid.reserve(n_slices + 1);
+    if (n_slices)
+        PPF_CUDA(cudaMemcpy(out.slice_mid.data(), slice_mid.data(), n_slices * 4,
+                            cudaMemcpyHostToDevice));
     out.slice_off.reserve(n_slices + 1);
     out.col.reserve((size_t)slots * kSliceRows + 1);
     out.src.reserve((size_t)slots * kSliceRows + 1);
@@ -844,7 +1116,7 @@ void launch_block_jacobi(unsigned n, const float *upper_val, const unsigned *dia
 }
 
 void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned max_iter,
-                PcgWorkspace &ws, cudaStream_t q) {
+                PcgWorkspace &ws, cudaStream_t q, const unsigned *run_if) {
     ws.reserve(A.n);
     PPF_CUDA(cudaMemsetAsync(ws.barrier.data(), 0, 4 * sizeof(unsigned), q));
     ws.Ap_ovf.reserve(A.ovf.count + 1);
@@ -863,8 +1135,16 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     k_task_split<<<div_up(ws.grid + 1, 256u), 256, 0, q>>>(T, ws.task_off.data(), ws.grid,
                                                           ws.task_start.data());
     PPF_LAUNCH_CHECK();
+    // one counter per product phase: the initial product, then one (block-
+    // Jacobi) or three (factored) per iteration, plus the factored start
+    const unsigned n_ctr = 3 * max_iter + 8;
+    ws.dyn_ctr.reserve(n_ctr);
+    PPF_CUDA(cudaMemsetAsync(ws.dyn_ctr.data(), 0, n_ctr * sizeof(unsigned), q));
     PcgArgs g{A,
               ws.task_start.data(),
+              T,
+              ws.dyn_ctr.data(),
+              n_ctr,
               x,
               r,
               ws.R.data(),
@@ -872,14 +1152,16 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
               ws.Ap.data(),
               ws.Ap_c.data(),
               ws.Ap_ovf.data(),
+              ws.Y.data(),
               ws.partials.data(),
               ws.barrier.data(),
               tol,
               max_iter,
-              ws.result.data()};
+              ws.result.data(),
+              run_if};
     void *args[] = {(void *)&g};
-    PPF_CUDA(cudaLaunchCooperativeKernel((const void *)k_pcg, dim3(ws.grid), dim3(ws.threads),
-                                         args, 0, q));
+    const void *kernel = A.factor.diag ? (const void *)k_pcg_factor : (const void *)k_pcg;
+    PPF_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(ws.grid), dim3(ws.threads), args, 0, q));
     ++g_kernel_launches;
 }
 

@@ -36,6 +36,10 @@ struct SellMatrix {
     const unsigned *slice_off; // n_slices + 1, in slots
     const unsigned *col;       // 32 per slot
     const float *val;          // 9 x 32 per slot
+    // null, or per slice the first slot of its upper segment: each row's
+    // blocks left of the diagonal sit in [slice_off, slice_mid), the
+    // diagonal block and those right of it in [slice_mid, slice_off + 1)
+    const unsigned *slice_mid;
 };
 
 // Entries of contact rows longer than the contact slices' cap: one row per
@@ -59,6 +63,21 @@ struct ContactRows {
     const unsigned *index;  // n: row -> sorted position, or 0xffffffff
 };
 
+// Factored preconditioner P = G^T G + eps D^{-1} (D^{-1}: the block-Jacobi
+// inverse), G block lower-triangular on the operator's own pattern. Its
+// values sit in arrays parallel to the operator's value arrays: the slot of
+// row a, column b holds G(a, b) when b < a and G(b, a)^T when b > a, so
+// y = G r walks the slots below the diagonal and z = G^T y the slots above
+// it. The diagonal blocks G(a, a) are kept apart, 9 floats per vertex
+// (column-major). Slots touching a Dirichlet vertex hold zero blocks.
+struct PcgFactor {
+    const float *fixed;   // as SellMatrix::val of the fixed part
+    const float *contact; // as the contact part's SellMatrix::val
+    const float *ovf;     // as OverflowRows::val
+    const float *diag;    // 9 per vertex; null: block-Jacobi only
+    float eps;
+};
+
 // A = fixed part (elastic + inertia + per-vertex terms, diagonal included)
 // + contact part (blocks outside the fixed pattern: sorted contact rows up to
 // a width cap, plus overflow rows).
@@ -68,6 +87,7 @@ struct PcgOperator {
     ContactRows contact;
     OverflowRows ovf;
     const float *inv_diag; // block-Jacobi inverse, (slice * 9 + e) * 32 + lane
+    PcgFactor factor;      // factor.diag == null: P = block-Jacobi
 };
 
 struct PcgResult {
@@ -85,7 +105,8 @@ struct PcgWorkspace {
     DevBuf<float4> p, Ap;          // one float4 per vertex
     DevBuf<float4> Ap_ovf;         // one per overflow row
     DevBuf<float4> Ap_c;           // one per contact row (sorted position)
-    DevBuf<unsigned> task_cost, task_off, task_start, scan_tmp;
+    DevBuf<float4> Y;              // G r of the factored preconditioner
+    DevBuf<unsigned> task_cost, task_off, task_start, scan_tmp, dyn_ctr;
     DevBuf<float> partials;
     DevBuf<unsigned> barrier;
     DevBuf<PcgResult> result;
@@ -98,7 +119,7 @@ struct PcgWorkspace {
 // (slot, lane) to the upper-triangle block it copies (bit 31: transposed),
 // or 0xffffffff for padding.
 struct SellLayout {
-    DevBuf<unsigned> slice_off, col, src;
+    DevBuf<unsigned> slice_off, slice_mid, col, src;
     DevBuf<float> val;
     unsigned n_slices = 0, slots = 0;
 };
@@ -119,7 +140,9 @@ struct DynLayout {
 };
 
 // Host construction of the fixed layout from the upper pattern and its
-// transpose table (row, upper slot) per row.
+// transpose table (row, upper slot) per row, in two segments per slice: the
+// blocks left of the diagonal (transposed), then the diagonal and the blocks
+// right of it, so a triangular product walks one segment only.
 void sell_build_fixed(unsigned n, const std::vector<unsigned> &off,
                       const std::vector<unsigned> &col, const std::vector<unsigned> &tr_off,
                       const std::vector<uint2> &tr, SellLayout &out);
@@ -134,7 +157,8 @@ void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const 
                     const unsigned *tr_off, const uint2 *tr, const unsigned *dof_mask,
                     DynLayout &out, cudaStream_t q);
 inline SellMatrix sell_view(const SellLayout &L) {
-    return SellMatrix{L.n_slices, L.slice_off.data(), L.col.data(), L.val.data()};
+    return SellMatrix{L.n_slices, L.slice_off.data(), L.col.data(), L.val.data(),
+                      L.slice_mid.data()};
 }
 inline ContactRows contact_view(const DynLayout &D) {
     return ContactRows{D.rows, sell_view(D.sell), D.perm.data(), D.index.data()};
@@ -150,8 +174,11 @@ void launch_block_jacobi(unsigned n, const float *upper_val, const unsigned *dia
 
 // Solves A x = b starting from x (b in r on entry; r is overwritten).
 // Writes the result into ws.result (device) and returns immediately.
+// With run_if set, the solve runs only when *run_if is nonzero on the device
+// when it starts (otherwise x, r and the result stay as they are).
 void launch_pcg(const PcgOperator &A, float *x, float *r, float tol,
-                unsigned max_iter, PcgWorkspace &ws, cudaStream_t q);
+                unsigned max_iter, PcgWorkspace &ws, cudaStream_t q,
+                const unsigned *run_if = nullptr);
 
 } // namespace gpu
 } // namespace ppf

@@ -1,0 +1,193 @@
+// precond.cu -- factor arrays of the PCG's factored preconditioner.
+#include "../physics/linalg.cuh"
+#include "fatal.cuh"
+#include "precond.cuh"
+
+namespace ppf {
+namespace gpu {
+
+namespace {
+
+constexpr unsigned kT = 256;
+
+__device__ __forceinline__ Mat3 ld_mat3(const float *p) {
+    Mat3 m;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) m.m[e] = __ldg(p + e);
+    return m;
+}
+__device__ __forceinline__ void st_mat3(float *p, const Mat3 &m) {
+#pragma unroll
+    for (int e = 0; e < 9; ++e) p[e] = m.m[e];
+}
+
+// Lower Cholesky factor L of a symmetric 3x3 block and its inverse.
+__device__ bool chol_inv3(const Mat3 &a, Mat3 &inv) {
+    const float l00 = sqrtf(a(0, 0));
+    const float l10 = a(1, 0) / l00, l20 = a(2, 0) / l00;
+    const float d1 = a(1, 1) - l10 * l10;
+    const float l11 = sqrtf(d1);
+    const float l21 = (a(2, 1) - l20 * l10) / l11;
+    const float d2 = a(2, 2) - l20 * l20 - l21 * l21;
+    const float l22 = sqrtf(d2);
+    if (!(a(0, 0) > 0.0f && d1 > 0.0f && d2 > 0.0f) || !isfinite(l22)) return false;
+    const float i00 = 1.0f / l00, i11 = 1.0f / l11, i22 = 1.0f / l22;
+    const float i10 = -l10 * i00 * i11;
+    const float i21 = -l21 * i11 * i22;
+    const float i20 = -(l20 * i00 + l21 * i10) * i22;
+    inv = Mat3::zero();
+    inv(0, 0) = i00;
+    inv(1, 0) = i10;
+    inv(1, 1) = i11;
+    inv(2, 0) = i20;
+    inv(2, 1) = i21;
+    inv(2, 2) = i22;
+    return true;
+}
+
+__global__ void k_chol_inv(unsigned n, const float *upper_val, const unsigned *diag_slot,
+                           float *cinv, unsigned *status) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Mat3 a = ld_mat3(upper_val + 9 * (size_t)__ldg(diag_slot + i));
+    Mat3 c;
+    if (!chol_inv3(a, c)) {
+        atomicOr(status, STATUS_PRECOND_NONSPD);
+        c = Mat3::zero();
+        for (int k = 0; k < 3; ++k) c(k, k) = 1.0f / sqrtf(fmaxf(fabsf(a(k, k)), 1e-30f));
+    }
+    st_mat3(cinv + 9 * (size_t)i, c);
+}
+
+// Ĝ of the first-order rule.
+struct FirstOrderHead {
+    float alpha;
+    __device__ __forceinline__ Mat3 edge(unsigned, unsigned, const Mat3 &ah) const {
+        return (-alpha) * ah;
+    }
+    __device__ __forceinline__ Mat3 diag(unsigned) const { return Mat3::identity(); }
+};
+
+// The factor value of one slot of row a holding the operator block B =
+// A(a, b): G(a, b) for b < a, G(b, a)^T for b > a, zero on the diagonal, for
+// padding and for Dirichlet vertices.
+template <class Head>
+__device__ __forceinline__ Mat3 slot_value(unsigned a, unsigned b, const Mat3 &B,
+                                           const Mat3 &Ca, const unsigned *dof_mask,
+                                           const float *cinv, const Head &head) {
+    if (b == a || __ldg(dof_mask + b) != 0u) return Mat3::zero();
+    const bool lower = b < a;
+    const Mat3 Cb = ld_mat3(cinv + 9 * (size_t)b);
+    const unsigned hi = lower ? a : b, lo = lower ? b : a;
+    const Mat3 Ahl = lower ? B : B.transpose();
+    const Mat3 &Chi = lower ? Ca : Cb;
+    const Mat3 &Clo = lower ? Cb : Ca;
+    const Mat3 ah = (Chi * Ahl) * Clo.transpose();
+    const Mat3 G = head.edge(hi, lo, ah) * Clo;
+    return lower ? G : G.transpose();
+}
+
+// One thread per (slice, lane) of a SELL part: every slot of its row.
+template <class Head>
+__global__ void k_factor_sell(SellMatrix M, unsigned rows, const unsigned *perm,
+                              const unsigned *dof_mask, const float *cinv, Head head,
+                              float *out) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned sl = t / kSliceRows, lane = t % kSliceRows;
+    if (sl >= M.n_slices) return;
+    const bool real = t < rows;
+    const unsigned a = real ? (perm ? __ldg(perm + t) : t) : 0u;
+    const bool live = real && __ldg(dof_mask + a) == 0u;
+    const Mat3 Ca = live ? ld_mat3(cinv + 9 * (size_t)a) : Mat3::zero();
+    const unsigned s0 = __ldg(M.slice_off + sl), s1 = __ldg(M.slice_off + sl + 1);
+    for (unsigned s = s0; s < s1; ++s) {
+        const size_t base = (size_t)s * 9 * kSliceRows + lane;
+        Mat3 v = Mat3::zero();
+        if (live) {
+            const unsigned b = __ldg(M.col + (size_t)s * kSliceRows + lane);
+            Mat3 B;
+#pragma unroll
+            for (int e = 0; e < 9; ++e) B.m[e] = __ldg(M.val + base + e * kSliceRows);
+            v = slot_value(a, b, B, Ca, dof_mask, cinv, head);
+        }
+#pragma unroll
+        for (int e = 0; e < 9; ++e) out[base + e * kSliceRows] = v.m[e];
+    }
+}
+
+// One warp per overflow row: every entry of it.
+template <class Head>
+__global__ void k_factor_ovf(OverflowRows O, const unsigned *dof_mask, const float *cinv,
+                             Head head, float *out) {
+    const unsigned k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (k >= O.count) return;
+    const unsigned a = __ldg(O.row + k);
+    const bool live = __ldg(dof_mask + a) == 0u;
+    const Mat3 Ca = live ? ld_mat3(cinv + 9 * (size_t)a) : Mat3::zero();
+    const uint2 rg = __ldg(O.range + k);
+    for (unsigned e = rg.x + lane; e < rg.x + rg.y; e += 32u) {
+        Mat3 v = Mat3::zero();
+        if (live) v = slot_value(a, __ldg(O.col + e), ld_mat3(O.val + 9 * (size_t)e), Ca,
+                                 dof_mask, cinv, head);
+        st_mat3(out + 9 * (size_t)e, v);
+    }
+}
+
+template <class Head>
+__global__ void k_factor_diag(unsigned n, const unsigned *dof_mask, const float *cinv, Head head,
+                              float *diag) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Mat3 C = ld_mat3(cinv + 9 * (size_t)i);
+    const Mat3 g = __ldg(dof_mask + i) ? C : head.diag(i) * C;
+    st_mat3(diag + 9 * (size_t)i, g);
+}
+
+template <class Head>
+void launch_factor(const PcgOperator &A, const unsigned *dof_mask, const Head &head,
+                   FactorBuffers &F, cudaStream_t q) {
+    const float *cinv = F.cinv.data();
+    if (A.fixed.n_slices) {
+        k_factor_sell<<<div_up(A.fixed.n_slices * kSliceRows, kT), kT, 0, q>>>(
+            A.fixed, A.n, nullptr, dof_mask, cinv, head, F.fixed.data());
+        PPF_LAUNCH_CHECK();
+    }
+    if (A.contact.sell.n_slices) {
+        k_factor_sell<<<div_up(A.contact.sell.n_slices * kSliceRows, kT), kT, 0, q>>>(
+            A.contact.sell, A.contact.rows, A.contact.perm, dof_mask, cinv, head,
+            F.contact.data());
+        PPF_LAUNCH_CHECK();
+    }
+    if (A.ovf.count) {
+        k_factor_ovf<<<div_up(A.ovf.count * 32u, kT), kT, 0, q>>>(A.ovf, dof_mask, cinv, head,
+                                                                  F.ovf.data());
+        PPF_LAUNCH_CHECK();
+    }
+    k_factor_diag<<<div_up(A.n, kT), kT, 0, q>>>(A.n, dof_mask, cinv, head, F.diag.data());
+    PPF_LAUNCH_CHECK();
+}
+
+} // namespace
+
+void launch_chol_inv(unsigned n, const float *upper_val, const unsigned *diag_slot, float *cinv,
+                     unsigned *d_status, cudaStream_t q) {
+    k_chol_inv<<<div_up(n, kT), kT, 0, q>>>(n, upper_val, diag_slot, cinv, d_status);
+    PPF_LAUNCH_CHECK();
+}
+
+void reserve_factor(const PcgOperator &A, unsigned fixed_slots, unsigned contact_slots,
+                    unsigned ovf_entries, FactorBuffers &F) {
+    F.fixed.reserve(9 * (size_t)kSliceRows * fixed_slots + 1);
+    F.contact.reserve(9 * (size_t)kSliceRows * contact_slots + 1);
+    F.ovf.reserve(9 * (size_t)ovf_entries + 1);
+    F.diag.reserve(9 * (size_t)A.n);
+    F.cinv.reserve(9 * (size_t)A.n);
+}
+
+void launch_factor_first_order(const PcgOperator &A, const unsigned *dof_mask, float alpha,
+                               FactorBuffers &F, cudaStream_t q) {
+    launch_factor(A, dof_mask, FirstOrderHead{alpha}, F, q);
+}
+
+} // namespace gpu
+} // namespace ppf

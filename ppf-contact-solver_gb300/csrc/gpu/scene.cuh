@@ -110,6 +110,8 @@ struct IterStatus {
     float pcg_resid;
     int pcg_state;                     // 0 converged, 1 truncated, 2 failed
     float pcg_err0;
+    unsigned factor_iter;              // iterations of the factored solve
+    unsigned fallback;                 // 1: it fell back to block-Jacobi
 };
 
 } // namespace gpu

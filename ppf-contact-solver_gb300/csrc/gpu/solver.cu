@@ -122,6 +122,25 @@ __global__ void k_init_ls(IterStatus *st, float max_t, PcgResult *res) {
     st->status |= res->status;
 }
 
+// After a factored solve: when it did not converge (stalled, broke down or
+// reached the block-Jacobi count), restore the solve's start (r = b,
+// dx = dx0) and flag the block-Jacobi solve that follows to run.
+__global__ void k_factor_verdict(unsigned n3, const PcgResult *res, const float *b,
+                                 const float *dx0, float *r, float *dx, unsigned *run_plain,
+                                 IterStatus *st) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool redo = res->state != 0;
+    if (i == 0) {
+        *run_plain = redo ? 1u : 0u;
+        st->factor_iter = res->iter;
+        st->fallback = redo ? 1u : 0u;
+    }
+    if (redo && i < n3) {
+        r[i] = b[i];
+        dx[i] = dx0[i];
+    }
+}
+
 __global__ void k_override_velocity(const unsigned *idx, unsigned count, const float *curr,
                                     float *prev, float vx, float vy, float vz) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -251,8 +270,32 @@ AssemblyBuffers Solver::abuf() {
 }
 
 PcgOperator Solver::pcg_operator() const {
-    return PcgOperator{n_, sell_view(fixed_sell_), contact_view(dyn_layout_),
-                       overflow_view(dyn_layout_), inv_diag_.data()};
+    return PcgOperator{n_,
+                       sell_view(fixed_sell_),
+                       contact_view(dyn_layout_),
+                       overflow_view(dyn_layout_),
+                       inv_diag_.data(),
+                       factor_active_ ? factor_.view(factor_eps_) : PcgFactor{}};
+}
+
+bool Solver::set_preconditioner(int kind, float param) {
+    if (kind < 0 || kind > 2 || (kind == 2 && !learned_ready_)) return false;
+    precond_kind_ = kind;
+    if (kind == 1) precond_param_ = param > 0.0f ? param : 0.5f;
+    plain_iters_ = 0;
+    return true;
+}
+
+// The factor of the assembled operator (after the block-Jacobi inverse).
+void Solver::build_factor() {
+    const PcgOperator A = PcgOperator{n_, sell_view(fixed_sell_), contact_view(dyn_layout_),
+                                      overflow_view(dyn_layout_), inv_diag_.data(),
+                                      PcgFactor{}};
+    reserve_factor(A, fixed_sell_.slots, dyn_layout_.sell.slots, dyn_layout_.ovf_entries,
+                   factor_);
+    launch_chol_inv(n_, fixed_val_.data(), fixed_diag_.data(), factor_.cinv.data(),
+                    &st_.data()->status, q_);
+    launch_factor_first_order(A, dof_mask_.data(), precond_param_, factor_, q_);
 }
 
 PieceBuffers Solver::pieces() {
@@ -277,6 +320,7 @@ void Solver::upload_props() {
 bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     host = ds;
     param = prm;
+    plain_iters_ = 0; // a new scene's first solve is block-Jacobi again
     n_ = ds->vertex.curr.size;
     n_surf_ = ds->surface_vert_count;
     nf_ = ds->mesh.mesh.face.size;
@@ -633,6 +677,10 @@ void Solver::assemble(float dt) {
                    dyn_layout_, q_);
     launch_block_jacobi(n_, fixed_val_.data(), fixed_diag_.data(), inv_diag_.data(),
                         &st_.data()->status, q_);
+    // the factored preconditioner once a block-Jacobi solve has set the
+    // iteration count it must stay within
+    factor_active_ = precond_kind_ != 0 && (plain_iters_ != 0 || force_factor_);
+    if (factor_active_) build_factor();
 }
 
 PpfStepResult Solver::advance() {
@@ -674,7 +722,26 @@ PpfStepResult Solver::advance() {
                                  cudaMemcpyDeviceToDevice, q_));
         PcgOperator A = pcg_operator();
         PPF_CUDA(cudaEventRecord(ev0_, q_));
-        launch_pcg(A, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_);
+        if (factor_active_) {
+            // factored solve within the block-Jacobi count, then block-Jacobi
+            // from the same start if it stalled or reached that count
+            dx0_.reserve(n3);
+            run_plain_.reserve(1);
+            PPF_CUDA(cudaMemcpyAsync(dx0_.data(), dx_.data(), n3 * sizeof(float),
+                                     cudaMemcpyDeviceToDevice, q_));
+            launch_pcg(A, dx_.data(), r_.data(), param->cg_tol,
+                       std::min(plain_iters_, param->cg_max_iter), pcg_, q_);
+            k_factor_verdict<<<div_up(n3, (size_t)kB), kB, 0, q_>>>(
+                (unsigned)n3, pcg_.result.data(), force_.data(), dx0_.data(), r_.data(),
+                dx_.data(), run_plain_.data(), st_.data());
+            PPF_LAUNCH_CHECK();
+            PcgOperator J = A;
+            J.factor = PcgFactor{};
+            launch_pcg(J, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_,
+                       run_plain_.data());
+        } else {
+            launch_pcg(A, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_);
+        }
         PPF_CUDA(cudaEventRecord(ev1_, q_));
         // rescaled Newton step, swept boxes, line search
         k_max_dx<<<div_up(n_, kB), kB, 0, q_>>>(n_, dx_.data(), st_.data());
@@ -705,10 +772,21 @@ PpfStepResult Solver::advance() {
         PPF_CUDA(cudaEventElapsedTime(&pcg_ms, ev0_, ev1_));
         stats_.newton_iters++;
         stats_.pcg_solves++;
-        stats_.pcg_iters_total += st.pcg_iter;
+        unsigned iters = st.pcg_iter;
+        if (factor_active_) {
+            stats_.factor_iters_total += st.factor_iter;
+            if (st.fallback) {
+                stats_.fallbacks++;
+                plain_iters_ = std::max(st.pcg_iter, 1u);
+                iters += st.factor_iter;
+            }
+        } else if (precond_kind_ != 0) {
+            plain_iters_ = std::max(st.pcg_iter, 1u);
+        }
+        stats_.pcg_iters_total += iters;
         stats_.pcg_ms_total += pcg_ms;
         stats_.pcg_ms.push_back(pcg_ms);
-        stats_.pcg_iters.push_back(st.pcg_iter);
+        stats_.pcg_iters.push_back(iters);
         stats_.dyn_blocks.push_back(st.n_dyn);
         stats_.max_contacts = std::max(stats_.max_contacts, st.n_contact);
         stats_.max_dyn_blocks = std::max(stats_.max_dyn_blocks, st.n_dyn);
@@ -901,7 +979,9 @@ int Solver::debug_assemble_solve(std::vector<float> &dx, unsigned &iters, float 
     compute_target(dt);
     PPF_CUDA(cudaMemcpyAsync(eval_x_.data(), curr_.data(), n3 * sizeof(float),
                              cudaMemcpyDeviceToDevice, q_));
+    force_factor_ = true; // with a factored kind set, solve with it alone
     assemble(dt);
+    force_factor_ = false;
     PPF_CUDA(cudaMemcpyAsync(r_.data(), force_.data(), n3 * sizeof(float),
                              cudaMemcpyDeviceToDevice, q_));
     PcgOperator A = pcg_operator();

@@ -7,6 +7,7 @@
 #include "lbvh.cuh"
 #include "linesearch.cuh"
 #include "pcg.cuh"
+#include "precond.cuh"
 
 namespace ppf {
 namespace gpu {
@@ -24,6 +25,8 @@ struct StepStats {
     std::vector<unsigned> pcg_iters;  // per solve
     std::vector<float> toi;           // per Newton iteration
     std::vector<unsigned> dyn_blocks; // per solve
+    unsigned fallbacks = 0;           // factored solves redone with block-Jacobi
+    unsigned factor_iters_total = 0;  // iterations of the factored solves
 };
 
 class Solver {
@@ -47,6 +50,9 @@ class Solver {
     cudaStream_t stream() const { return q_; }
     unsigned fixed_blocks() const { return nnz_fixed_; }
     unsigned vertices() const { return n_; }
+    // PPF_PRECOND_* of ppf_gb300_ext.h; false for an unknown kind
+    bool set_preconditioner(int kind, float param);
+    int preconditioner() const { return precond_kind_; }
     // debug views (host copies) for stage parity checks
     void debug_matrix(std::vector<unsigned> &f_off, std::vector<unsigned> &f_col,
                       std::vector<float> &f_val, std::vector<unsigned> &d_off,
@@ -119,6 +125,18 @@ class Solver {
     DevBuf<float> dval_buf_;
     DevBuf<unsigned> scan_tmp_;
     PcgWorkspace pcg_;
+    // factored preconditioner (block-Jacobi stays the fallback)
+    int precond_kind_ = 0;
+    float precond_param_ = 0.5f;
+    float factor_eps_ = 1e-3f;
+    unsigned plain_iters_ = 0; // iterations of the last block-Jacobi solve
+    bool factor_active_ = false;
+    bool learned_ready_ = false; // network weights loaded
+    bool force_factor_ = false;  // the debug solve uses the factor directly
+    FactorBuffers factor_;
+    DevBuf<float> dx0_;
+    DevBuf<unsigned> run_plain_;
+    void build_factor();
     SellLayout fixed_sell_;
     DynLayout dyn_layout_;
     DevBuf<unsigned> piece_cnt_, piece_off_, piece_tmp_;

@@ -13,6 +13,7 @@ import ctypes as C
 STATS_MAX_SOLVES = 256
 
 BARRIER_CUBIC, BARRIER_QUAD, BARRIER_LOG = 0, 1, 2
+PRECOND_BLOCK_JACOBI, PRECOND_FIRST_ORDER, PRECOND_LEARNED = 0, 1, 2
 FRICTION_MIN, FRICTION_MAX, FRICTION_MEAN = 0, 1, 2
 MODEL_ARAP, MODEL_STVK, MODEL_BARAFF_WITKIN, MODEL_SNHK = 0, 1, 2, 3
 
@@ -106,6 +107,9 @@ class StepStats(C.Structure):
         ("fixed_blocks", C.c_uint),
         ("vertices", C.c_uint),
         ("dyn_blocks", C.c_uint * STATS_MAX_SOLVES),
+        ("precond_kind", C.c_uint),
+        ("fallbacks", C.c_uint),
+        ("factor_iters_total", C.c_uint),
     ]
 
 

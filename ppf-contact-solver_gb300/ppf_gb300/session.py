@@ -56,6 +56,8 @@ def _declare(lib):
     lib.ppf_scene_vertex_count.argtypes = [P]
     lib.ppf_scene_positions.argtypes = [P, C.c_void_p, C.c_void_p]
     lib.ppf_scene_set_positions.argtypes = [P, C.c_void_p, C.c_void_p]
+    lib.ppf_set_preconditioner.restype = C.c_int
+    lib.ppf_set_preconditioner.argtypes = [C.c_int, C.c_float]
     # reference entry points (include/ppf_gb300.h)
     lib.initialize.restype = C.c_bool
     lib.initialize.argtypes = [P, C.POINTER(abi.ParamSet)]
@@ -279,6 +281,13 @@ class Session:
         s = abi.StepStats()
         self.lib.ppf_step_stats(C.byref(s))
         return s
+
+    def set_preconditioner(self, kind: int, param: float = 0.0) -> None:
+        """abi.PRECOND_BLOCK_JACOBI (the reference's), PRECOND_FIRST_ORDER
+        (param: the factor's coupling weight, 0.5 by default) or
+        PRECOND_LEARNED (after the network's weights are loaded)."""
+        if self.lib.ppf_set_preconditioner(int(kind), float(param)) != 0:
+            raise ValueError(f"preconditioner kind {kind} is not available")
 
     def intersection_records(self, max_count: int = 256):
         buf = (abi.IntersectionRecord * max_count)()
