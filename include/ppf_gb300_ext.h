@@ -118,6 +118,19 @@ void ppf_step_stats(PpfStepStats *out);
 #define PPF_PRECOND_FIRST_ORDER 1
 #define PPF_PRECOND_LEARNED 2
 int ppf_set_preconditioner(int kind, float param);
+/* Reported by PpfStepStats.precond_kind when the scene's ParamSet asks for the
+ * reference's aggregate additive-Schwarz preconditioner (precond == 1,
+ * schwarz/schwarz.hpp:38-86). */
+#define PPF_PRECOND_SCHWARZ 3
+
+/* The Schwarz aggregation on the host (schwarz/schwarz.cu:551-645): the graph
+ * as a both-triangle CSR (n + 1 offsets, columns, one weight per entry: the
+ * Frobenius norm of the block), aggregates of at most kmax matrix-connected
+ * vertices grown greedily by the heaviest coupling, seeds in decreasing order
+ * of summed coupling. Writes the aggregate of each vertex to agg (n) and
+ * returns the number of aggregates. */
+unsigned ppf_schwarz_aggregate(unsigned n, const unsigned *off, const unsigned *col,
+                               const float *wgt, unsigned kmax, unsigned *agg);
 
 /* The CUDA stream (cudaStream_t, as void*) every kernel of advance() runs
  * on, so a host can time the step with its own events on that stream. NULL

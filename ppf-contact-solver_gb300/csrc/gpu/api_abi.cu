@@ -3,6 +3,7 @@
 // stage-inspection extensions of include/ppf_gb300_ext.h.
 #include "../../../include/ppf_gb300_ext.h"
 #include "fatal.cuh"
+#include "schwarz.cuh"
 #include "solver.cuh"
 
 #include <cstdlib>
@@ -208,6 +209,15 @@ void ppf_step_stats(PpfStepStats *out) {
     out->precond_kind = (unsigned)solver_instance().preconditioner();
     out->fallbacks = s.fallbacks;
     out->factor_iters_total = s.factor_iters_total;
+}
+
+unsigned ppf_schwarz_aggregate(unsigned n, const unsigned *off, const unsigned *col,
+                               const float *wgt, unsigned kmax, unsigned *agg) {
+    std::vector<unsigned> o(off, off + n + 1), c(col, col + off[n]), a;
+    std::vector<float> w(wgt, wgt + off[n]);
+    const unsigned n_agg = ppf::gpu::schwarz_aggregate(n, o, c, w, kmax, a);
+    std::copy(a.begin(), a.end(), agg);
+    return n_agg;
 }
 
 int ppf_set_preconditioner(int kind, float param) {

@@ -755,6 +755,198 @@ aborted:
         *g.res = PcgResult{0u, 0.0f, 2, 0, 0.0f, 0.0f, STATUS_PCG_BREAKDOWN};
 }
 
+constexpr unsigned kSchwarzDim = 3 * kSchwarzMaxMembers;
+// floats of a warp's shared region: r, y, z, p of the aggregate and its
+// staged packed factor (rounded up to 16 bytes)
+constexpr unsigned kSchwarzTri = (kSchwarzDim * (kSchwarzDim + 1) / 2 + 3) & ~3u;
+constexpr unsigned kSchwarzWarpFloats = 4 * kSchwarzDim + kSchwarzTri;
+
+// One Schwarz aggregate, by one warp: the update of its member rows
+// (`init`: r = r - A x0 and p = 0; otherwise x += alpha p, r -= alpha A p),
+// then z = G^T (G r) on the aggregate, and the members' {z, p} records.
+// Adds r^T z to `a` and |r|_1 to `b`. `seg` is the warp's shared region
+// (kSchwarzWarpFloats, 16-byte aligned); the packed factor is staged there
+// with 16-byte loads and both triangular products read it from there.
+__device__ __forceinline__ void schwarz_segment(const PcgArgs &g, unsigned ag, unsigned lane,
+                                                bool init, float alpha, float *seg, float &a,
+                                                float &b) {
+    const SchwarzView &S = g.A.schwarz;
+    constexpr unsigned D = kSchwarzDim;
+    float *sr = seg, *sy = seg + D, *sz = seg + 2 * D, *sp = seg + 3 * D;
+    float *sG = seg + 4 * D;
+    const unsigned base = __ldg(S.agg_off + ag), m = __ldg(S.agg_off + ag + 1) - base;
+    const unsigned d = 3u * m;
+    for (unsigned k = lane; k < m; k += 32u) {
+        const unsigned i = __ldg(S.members + base + k);
+        Vec3 ri = ldcg3(g.r, i), pi = Vec3::zero();
+        const Vec3 api = row_product(g, i);
+        if (init) {
+            ri = ri - api;
+        } else {
+            pi = ld4(g.p, i);
+            Vec3 xi = ldcg3(g.x, i);
+            for (int c = 0; c < 3; ++c) {
+                xi[c] += alpha * pi[c];
+                ri[c] = ri[c] - alpha * api[c];
+            }
+            st3(g.x, i, xi);
+        }
+        st3(g.r, i, ri);
+        for (int c = 0; c < 3; ++c) {
+            sr[3 * k + c] = ri[c];
+            sp[3 * k + c] = pi[c];
+        }
+        b += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
+    }
+    {
+        const float4 *G4 = reinterpret_cast<const float4 *>(S.ainv + __ldg(S.ainv_off + ag));
+        float4 *s4 = reinterpret_cast<float4 *>(sG);
+        const unsigned n4 = (d * (d + 1u) / 2u + 3u) / 4u;
+        for (unsigned e = lane; e < n4; e += 32u) s4[e] = __ldg(G4 + e);
+    }
+    __syncwarp();
+    for (unsigned p = lane; p < d; p += 32u) { // y = G r
+        const float *row = sG + p * (p + 1u) / 2u;
+        float acc = 0.0f;
+        for (unsigned q = 0; q <= p; ++q) acc += row[q] * sr[q];
+        sy[p] = acc;
+    }
+    __syncwarp();
+    for (unsigned p = lane; p < d; p += 32u) { // z = G^T y
+        float acc = 0.0f;
+        for (unsigned q = p; q < d; ++q) acc += sG[q * (q + 1u) / 2u + p] * sy[q];
+        sz[p] = acc;
+    }
+    __syncwarp();
+    for (unsigned k = lane; k < m; k += 32u) {
+        const unsigned i = __ldg(S.members + base + k);
+        const Vec3 zi = vec3(sz[3 * k], sz[3 * k + 1], sz[3 * k + 2]);
+        const Vec3 ri = vec3(sr[3 * k], sr[3 * k + 1], sr[3 * k + 2]);
+        st_record(g.R, i, zi, vec3(sp[3 * k], sp[3 * k + 1], sp[3 * k + 2]));
+        a += ri.dot(zi);
+    }
+    __syncwarp();
+}
+
+// PCG with the aggregate-Schwarz preconditioner: the recurrence, verdicts and
+// checks of k_pcg, with the update phase walking aggregates instead of
+// slices. A non-positive (or non-finite) r^T z ends the solve as failed with
+// break cause 2, the reference's cue to solve again with block-Jacobi
+// (solver/solver.cu:1627-1676).
+__global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
+    const PcgOperator &A = g.A;
+    const unsigned nb = gridDim.x;
+    const unsigned lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned n_agg = A.schwarz.n_agg;
+    unsigned *abort = g.bar + 2;
+    float *part0 = g.part, *part1 = g.part + 2 * nb;
+    float a, b;
+    extern __shared__ float4 s_dyn4[];
+    float *seg = reinterpret_cast<float *>(s_dyn4) + (size_t)wib * kSchwarzWarpFloats;
+
+    __shared__ unsigned s_next;
+    BlockTasks bt{&s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
+                  g.task_start[gridDim.x], g.n_tasks, g.dyn_ctr, g.n_ctr};
+    const float *const avals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
+    bt.start();
+    {
+        const GatherPlain gx{g.x};
+        float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
+        for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
+            product_task<kAllSlots>(g, avals, task, lane, gx,
+                                    [&](unsigned, unsigned part, unsigned slot, const Vec3 &acc,
+                                        const Vec3 &) { st4(dst[part], slot, acc); });
+    }
+    a = b = 0.0f;
+    if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
+    // r = b - A x0, z = P r, p_0 = 0; rz0, err0
+    a = b = 0.0f;
+    for (unsigned ag = warp; ag < n_agg; ag += nwarps)
+        schwarz_segment(g, ag, lane, true, 0.0f, seg, a, b);
+    if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+    {
+        const float err0 = b;
+        float rz0 = a;
+        if (err0 == 0.0f) {
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+                *g.res = PcgResult{1u, 0.0f, 0, 0, 0.0f, 0.0f, 0u};
+            return;
+        }
+        if (!(rz0 > 0.0f)) {
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+                *g.res = PcgResult{1u, 1.0f, 2, 2, err0, rz0, 0u};
+            return;
+        }
+        float beta = 0.0f;
+        unsigned stride = 4, next_check = 1;
+        int broke = 0;
+        float break_val = 0.0f;
+        for (unsigned iter = 1;; ++iter) {
+            // S: A p_k with p_k = z + beta p_{k-1}
+            a = b = 0.0f;
+            const GatherCombined gp{g.R, beta};
+            bt.start();
+            float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
+            for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
+                product_task<kAllSlots>(g, avals, task, lane, gp,
+                                        [&](unsigned row, unsigned part, unsigned slot,
+                                            const Vec3 &acc, const Vec3 &ab) {
+                                            const Vec3 pi = gp(row);
+                                            if (part == 0u) st4(g.p, row, pi);
+                                            st4(dst[part], slot, acc);
+                                            a += pi.dot(acc);
+                                            b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] +
+                                                 fabsf(pi[2]) * ab[2];
+                                        });
+            if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
+            const float pAp = a, bound = kCurvatureSlack * kFloatEps * b;
+            float alpha;
+            if (pAp > bound) {
+                alpha = rz0 / pAp;
+            } else {
+                alpha = 0.0f;
+                if (!broke) {
+                    broke = (pAp < -bound || pAp != pAp) ? 1 : 3;
+                    break_val = pAp;
+                }
+            }
+            // U: per aggregate, x += alpha p, r -= alpha A p, z = P r
+            a = b = 0.0f;
+            for (unsigned ag = warp; ag < n_agg; ag += nwarps)
+                schwarz_segment(g, ag, lane, false, alpha, seg, a, b);
+            if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+            const float rz_new = a, err_now = b;
+            const bool rz_bad = !(rz_new > 0.0f);
+            beta = rz_new / rz0;
+            rz0 = rz_new;
+            const bool at_cap = iter >= g.max_iter;
+            if (iter == next_check || at_cap || rz_bad) {
+                const float reresid = err_now / err0;
+                PcgResult out{iter, reresid, -1, broke, err0, break_val, 0u};
+                if (reresid < g.tol) out.state = 0;
+                else if (rz_bad) {
+                    out.state = 2;
+                    out.break_cause = 2;
+                    out.break_val = rz_new;
+                } else if (broke == 3) out.state = 1;
+                else if (broke == 1) out.state = 2;
+                else if (!isfinite(reresid) || at_cap) out.state = 2;
+                if (out.state >= 0) {
+                    if (blockIdx.x == 0 && threadIdx.x == 0) *g.res = out;
+                    return;
+                }
+                if (reresid < 8.0f * g.tol) stride = 1;
+                next_check = iter + stride;
+            }
+        }
+    }
+aborted:
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        *g.res = PcgResult{0u, 0.0f, 2, 0, 0.0f, 0.0f, STATUS_PCG_BREAKDOWN};
+}
+
 __global__ void k_block_jacobi(unsigned n, const float *upper_val, const unsigned *diag_slot,
                                float *inv, unsigned *status) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1160,8 +1352,22 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
               ws.result.data(),
               run_if};
     void *args[] = {(void *)&g};
-    const void *kernel = A.factor.diag ? (const void *)k_pcg_factor : (const void *)k_pcg;
-    PPF_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(ws.grid), dim3(ws.threads), args, 0, q));
+    const void *kernel = A.schwarz.n_agg ? (const void *)k_pcg_schwarz
+                         : A.factor.diag ? (const void *)k_pcg_factor
+                                         : (const void *)k_pcg;
+    size_t dyn_smem = 0;
+    if (A.schwarz.n_agg) {
+        dyn_smem = (size_t)kWarps * kSchwarzWarpFloats * sizeof(float);
+        static bool attr_set = false;
+        if (!attr_set) {
+            PPF_CUDA(cudaFuncSetAttribute((const void *)k_pcg_schwarz,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)dyn_smem));
+            attr_set = true;
+        }
+    }
+    PPF_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(ws.grid), dim3(ws.threads), args, dyn_smem,
+                                         q));
     ++g_kernel_launches;
 }
 

@@ -78,6 +78,17 @@ struct PcgFactor {
     float eps;
 };
 
+constexpr unsigned kSchwarzMaxMembers = 16; // vertices per Schwarz aggregate
+
+// Aggregate additive-Schwarz preconditioner (schwarz.cuh); n_agg == 0 when
+// unused. Aggregate g holds members[agg_off[g] .. agg_off[g+1]) and its
+// factor G = L^{-1} packed row-major lower-triangular at ainv + ainv_off[g].
+struct SchwarzView {
+    unsigned n_agg;
+    const unsigned *agg_off, *members, *ainv_off;
+    const float *ainv;
+};
+
 // A = fixed part (elastic + inertia + per-vertex terms, diagonal included)
 // + contact part (blocks outside the fixed pattern: sorted contact rows up to
 // a width cap, plus overflow rows).
@@ -88,6 +99,7 @@ struct PcgOperator {
     OverflowRows ovf;
     const float *inv_diag; // block-Jacobi inverse, (slice * 9 + e) * 32 + lane
     PcgFactor factor;      // factor.diag == null: P = block-Jacobi
+    SchwarzView schwarz;   // n_agg > 0: P = aggregate Schwarz (factor unused)
 };
 
 struct PcgResult {

@@ -124,12 +124,13 @@ __global__ void k_init_ls(IterStatus *st, float max_t, PcgResult *res) {
 
 // After a factored solve: when it did not converge (stalled, broke down or
 // reached the block-Jacobi count), restore the solve's start (r = b,
-// dx = dx0) and flag the block-Jacobi solve that follows to run.
-__global__ void k_factor_verdict(unsigned n3, const PcgResult *res, const float *b,
-                                 const float *dx0, float *r, float *dx, unsigned *run_plain,
-                                 IterStatus *st) {
+// dx = dx0) and flag the block-Jacobi solve that follows to run. After a
+// Schwarz solve (any_failure 0) only a non-positive r^T z does that.
+__global__ void k_factor_verdict(unsigned n3, const PcgResult *res, int any_failure,
+                                 const float *b, const float *dx0, float *r, float *dx,
+                                 unsigned *run_plain, IterStatus *st) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool redo = res->state != 0;
+    const bool redo = any_failure ? res->state != 0 : (res->state == 2 && res->break_cause == 2);
     if (i == 0) {
         *run_plain = redo ? 1u : 0u;
         st->factor_iter = res->iter;
@@ -275,7 +276,8 @@ PcgOperator Solver::pcg_operator() const {
                        contact_view(dyn_layout_),
                        overflow_view(dyn_layout_),
                        inv_diag_.data(),
-                       factor_active_ ? factor_.view(factor_eps_) : PcgFactor{}};
+                       factor_active_ ? factor_.view(factor_eps_) : PcgFactor{},
+                       schwarz_active_ ? schwarz_.view() : SchwarzView{}};
 }
 
 bool Solver::set_preconditioner(int kind, float param) {
@@ -321,6 +323,7 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     host = ds;
     param = prm;
     plain_iters_ = 0; // a new scene's first solve is block-Jacobi again
+    schwarz_.ready = false;
     n_ = ds->vertex.curr.size;
     n_surf_ = ds->surface_vert_count;
     nf_ = ds->mesh.mesh.face.size;
@@ -681,6 +684,14 @@ void Solver::assemble(float dt) {
     // iteration count it must stay within
     factor_active_ = precond_kind_ != 0 && (plain_iters_ != 0 || force_factor_);
     if (factor_active_) build_factor();
+    // the reference's aggregate Schwarz when the scene asks for it
+    schwarz_active_ = precond_kind_ == 0 && param->precond == 1;
+    if (schwarz_active_) {
+        PcgOperator A{n_, sell_view(fixed_sell_), contact_view(dyn_layout_),
+                      overflow_view(dyn_layout_), inv_diag_.data(), PcgFactor{}, SchwarzView{}};
+        if (!schwarz_.ready || schwarz_.n != n_) schwarz_setup(A, schwarz_, q_);
+        launch_schwarz_factor(A, schwarz_, &st_.data()->status, q_);
+    }
 }
 
 PpfStepResult Solver::advance() {
@@ -722,19 +733,24 @@ PpfStepResult Solver::advance() {
                                  cudaMemcpyDeviceToDevice, q_));
         PcgOperator A = pcg_operator();
         PPF_CUDA(cudaEventRecord(ev0_, q_));
-        if (factor_active_) {
+        if (factor_active_ || schwarz_active_) {
             // factored solve within the block-Jacobi count, then block-Jacobi
-            // from the same start if it stalled or reached that count
+            // from the same start if it stalled or reached that count; a
+            // Schwarz solve goes back to block-Jacobi only when r^T z <= 0
+            // (solver/solver.cu:1627-1676)
             dx0_.reserve(n3);
             run_plain_.reserve(1);
             PPF_CUDA(cudaMemcpyAsync(dx0_.data(), dx_.data(), n3 * sizeof(float),
                                      cudaMemcpyDeviceToDevice, q_));
             launch_pcg(A, dx_.data(), r_.data(), param->cg_tol,
-                       std::min(plain_iters_, param->cg_max_iter), pcg_, q_);
+                       factor_active_ ? std::min(plain_iters_, param->cg_max_iter)
+                                      : param->cg_max_iter,
+                       pcg_, q_);
             k_factor_verdict<<<div_up(n3, (size_t)kB), kB, 0, q_>>>(
-                (unsigned)n3, pcg_.result.data(), force_.data(), dx0_.data(), r_.data(),
-                dx_.data(), run_plain_.data(), st_.data());
+                (unsigned)n3, pcg_.result.data(), factor_active_ ? 1 : 0, force_.data(),
+                dx0_.data(), r_.data(), dx_.data(), run_plain_.data(), st_.data());
             PPF_LAUNCH_CHECK();
+            A.schwarz = SchwarzView{};
             PcgOperator J = A;
             J.factor = PcgFactor{};
             launch_pcg(J, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_,
@@ -773,7 +789,12 @@ PpfStepResult Solver::advance() {
         stats_.newton_iters++;
         stats_.pcg_solves++;
         unsigned iters = st.pcg_iter;
-        if (factor_active_) {
+        if (schwarz_active_) {
+            if (st.fallback) {
+                stats_.fallbacks++;
+                iters += st.factor_iter;
+            }
+        } else if (factor_active_) {
             stats_.factor_iters_total += st.factor_iter;
             if (st.fallback) {
                 stats_.fallbacks++;

@@ -8,6 +8,7 @@
 #include "linesearch.cuh"
 #include "pcg.cuh"
 #include "precond.cuh"
+#include "schwarz.cuh"
 
 namespace ppf {
 namespace gpu {
@@ -52,7 +53,8 @@ class Solver {
     unsigned vertices() const { return n_; }
     // PPF_PRECOND_* of ppf_gb300_ext.h; false for an unknown kind
     bool set_preconditioner(int kind, float param);
-    int preconditioner() const { return precond_kind_; }
+    // the kind of the last solve: PPF_PRECOND_* (3: aggregate Schwarz)
+    int preconditioner() const { return schwarz_active_ ? 3 : precond_kind_; }
     // debug views (host copies) for stage parity checks
     void debug_matrix(std::vector<unsigned> &f_off, std::vector<unsigned> &f_col,
                       std::vector<float> &f_val, std::vector<unsigned> &d_off,
@@ -134,6 +136,9 @@ class Solver {
     bool learned_ready_ = false; // network weights loaded
     bool force_factor_ = false;  // the debug solve uses the factor directly
     FactorBuffers factor_;
+    // aggregate Schwarz (ParamSet::precond == 1), aggregated once per scene
+    bool schwarz_active_ = false;
+    SchwarzLayout schwarz_;
     DevBuf<float> dx0_;
     DevBuf<unsigned> run_plain_;
     void build_factor();
