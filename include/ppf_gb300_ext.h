@@ -97,6 +97,13 @@ typedef struct {
     unsigned precond_kind;
     unsigned fallbacks;
     unsigned factor_iters_total;
+    /* the last solve's verdict: state (0 converged, 1 truncated, 2 failed),
+     * break cause (0 none, 1 negative curvature, 2 r^T z <= 0, 3 curvature
+     * within round-off), relative residual at return, the offending value */
+    int last_pcg_state;
+    int last_break_cause;
+    float last_pcg_resid;
+    float last_break_val;
 } PpfStepStats;
 void ppf_step_stats(PpfStepStats *out);
 

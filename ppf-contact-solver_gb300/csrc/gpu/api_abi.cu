@@ -209,6 +209,10 @@ void ppf_step_stats(PpfStepStats *out) {
     out->precond_kind = (unsigned)solver_instance().preconditioner();
     out->fallbacks = s.fallbacks;
     out->factor_iters_total = s.factor_iters_total;
+    out->last_pcg_state = s.last_state;
+    out->last_break_cause = s.last_break_cause;
+    out->last_pcg_resid = s.last_resid;
+    out->last_break_val = s.last_break_val;
 }
 
 unsigned ppf_schwarz_aggregate(unsigned n, const unsigned *off, const unsigned *col,

@@ -110,6 +110,9 @@ struct IterStatus {
     float pcg_resid;
     int pcg_state;                     // 0 converged, 1 truncated, 2 failed
     float pcg_err0;
+    int pcg_break_cause;               // 0 none, 1 negative curvature, 2 r^T z <= 0,
+                                       // 3 unresolvable curvature
+    float pcg_break_val;
     unsigned factor_iter;              // iterations of the factored solve
     unsigned fallback;                 // 1: it fell back to block-Jacobi
 };

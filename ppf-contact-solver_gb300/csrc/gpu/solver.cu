@@ -119,6 +119,8 @@ __global__ void k_init_ls(IterStatus *st, float max_t, PcgResult *res) {
     st->pcg_resid = res->resid;
     st->pcg_state = res->state;
     st->pcg_err0 = res->err0;
+    st->pcg_break_cause = res->break_cause;
+    st->pcg_break_val = res->break_val;
     st->status |= res->status;
 }
 
@@ -805,6 +807,10 @@ PpfStepResult Solver::advance() {
             plain_iters_ = std::max(st.pcg_iter, 1u);
         }
         stats_.pcg_iters_total += iters;
+        stats_.last_state = st.pcg_state;
+        stats_.last_break_cause = st.pcg_break_cause;
+        stats_.last_resid = st.pcg_resid;
+        stats_.last_break_val = st.pcg_break_val;
         stats_.pcg_ms_total += pcg_ms;
         stats_.pcg_ms.push_back(pcg_ms);
         stats_.pcg_iters.push_back(iters);

@@ -28,6 +28,9 @@ struct StepStats {
     std::vector<unsigned> dyn_blocks; // per solve
     unsigned fallbacks = 0;           // factored solves redone with block-Jacobi
     unsigned factor_iters_total = 0;  // iterations of the factored solves
+    // the last solve's verdict
+    int last_state = 0, last_break_cause = 0;
+    float last_resid = 0.0f, last_break_val = 0.0f;
 };
 
 class Solver {

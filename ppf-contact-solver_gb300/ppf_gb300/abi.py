@@ -110,6 +110,10 @@ class StepStats(C.Structure):
         ("precond_kind", C.c_uint),
         ("fallbacks", C.c_uint),
         ("factor_iters_total", C.c_uint),
+        ("last_pcg_state", C.c_int),
+        ("last_break_cause", C.c_int),
+        ("last_pcg_resid", C.c_float),
+        ("last_break_val", C.c_float),
     ]
 
 
