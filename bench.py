@@ -44,7 +44,8 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Newton steps/s (block-Jacobi PCG to rel. residual 1e-3)"
 UNIT = "newton_iters/s"
-WORKLOAD = "stacked_sheets: 8 x 128x128 cloth sheets over a fixed 0.6 m cube"
+WORKLOAD = ("stacked_sheets: 8 x 128x128 cloth sheets over a 0.6 m cube that is a static "
+            "collision mesh")
 L2_FLUSH_BYTES = 256 << 20
 CPU_SAMPLE_SECONDS = 20.0
 REF_BUDGET_SECONDS = 150.0

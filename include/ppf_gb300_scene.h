@@ -63,6 +63,12 @@ void ppf_scene_pull(PpfScene *scene, const unsigned *indices, unsigned count,
 void ppf_scene_add_sphere(PpfScene *scene, const float *center, float radius,
                           float contact_gap, float friction, int reverse,
                           int bowl);
+/* A static collision mesh (Constraint::mesh, builder.rs:1823-1935): nv
+ * vertices and nf triangles, with its contact gap, offset and friction. Its
+ * edges are extracted at build; meshes added in turn are concatenated. */
+void ppf_scene_add_collision_mesh(PpfScene *scene, const float *vertices, unsigned nv,
+                                  const unsigned *faces, unsigned nf, float contact_gap,
+                                  float contact_offset, float friction);
 void ppf_scene_add_floor(PpfScene *scene, const float *ground, const float *up,
                          float contact_gap, float friction);
 

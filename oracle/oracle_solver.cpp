@@ -80,6 +80,18 @@ struct Oracle {
     std::unordered_map<unsigned long long, Mat3> dyn;
     std::vector<Pair> pf, pe, pp, ee;
     Tree tf, te, tv;
+    // static collision mesh (Constraint::mesh) and its trees, built once
+    unsigned ncv = 0, ncf = 0, nce = 0;
+    std::vector<float> cm_x;
+    std::vector<unsigned> cm_face, cm_edge;
+    std::vector<PpfVertexProp> cm_vprop;
+    std::vector<PpfFaceProp> cm_fprop;
+    std::vector<PpfEdgeProp> cm_eprop;
+    std::vector<PpfVertexParam> cm_vparam;
+    std::vector<PpfFaceParam> cm_fparam;
+    std::vector<PpfEdgeParam> cm_eparam;
+    std::vector<float> cm_margin_f, cm_margin_e;
+    Tree tcf, tce;
     StepStatsO stats;
     unsigned last_pcg_iters = 0;
     bool dirichlet = true; // eliminate fix pins after assembly (main.cu:954-1049)
@@ -87,6 +99,11 @@ struct Oracle {
 
     Vec3 X(const std::vector<float> &v, unsigned i) const {
         return vec3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+    }
+    Vec3 CX(unsigned i) const { return X(cm_x, i); }
+    static void point_box(const Vec3 &p, float m, float q[8]) {
+        q[0] = p[0] - m; q[1] = p[1] - m; q[2] = p[2] - m; q[3] = 1.0f;
+        q[4] = p[0] + m; q[5] = p[1] + m; q[6] = p[2] + m; q[7] = 0.0f;
     }
     unsigned slot(unsigned i, unsigned j) const {
         auto b = fcol.begin() + foff[i], e = fcol.begin() + foff[i + 1];
@@ -118,8 +135,8 @@ struct Oracle {
         if (!count) return;
         t.node.assign(2 * (2 * count - 1), 0u);
         t.box.assign(8 * (2 * count - 1), 0.0f);
-        t.root = oracle_lbvh_build(kind, x0.data(), x1.data(), n, prims, count, margin, e,
-                                   t.node.data(), t.box.data(), nullptr);
+        t.root = oracle_lbvh_build(kind, x0.data(), x1.data(), (unsigned)(x0.size() / 3), prims,
+                                   count, margin, e, t.node.data(), t.box.data(), nullptr);
     }
     template <class Op>
     void query(const Tree &t, const float q[8], Op &&op) const {
@@ -210,6 +227,35 @@ bool Oracle::init(const PpfDataSet *ds, const PpfParamSet *p) {
     for (unsigned i = 0; i < n; ++i) {
         const PpfVertexParam &q = vparam[vprop[i].param_index];
         margin_v[i] = 0.5f * q.ghat + q.offset;
+    }
+    {
+        const PpfCollisionMesh &cm = ds->constraint.mesh;
+        ncv = cm.vertex.size;
+        ncf = cm.face.size;
+        nce = cm.edge.size;
+        const float *cx = (const float *)cm.vertex.data;
+        cm_x.assign(cx, cx + 3 * (size_t)ncv);
+        cm_face.assign((const unsigned *)cm.face.data, (const unsigned *)cm.face.data + 3 * (size_t)ncf);
+        cm_edge.assign((const unsigned *)cm.edge.data, (const unsigned *)cm.edge.data + 2 * (size_t)nce);
+        cm_vprop.assign(cm.prop.vertex.data, cm.prop.vertex.data + cm.prop.vertex.size);
+        cm_fprop.assign(cm.prop.face.data, cm.prop.face.data + cm.prop.face.size);
+        cm_eprop.assign(cm.prop.edge.data, cm.prop.edge.data + cm.prop.edge.size);
+        cm_vparam.assign(cm.param_arrays.vertex.data, cm.param_arrays.vertex.data + cm.param_arrays.vertex.size);
+        cm_fparam.assign(cm.param_arrays.face.data, cm.param_arrays.face.data + cm.param_arrays.face.size);
+        cm_eparam.assign(cm.param_arrays.edge.data, cm.param_arrays.edge.data + cm.param_arrays.edge.size);
+        cm_margin_f.resize(ncf);
+        cm_margin_e.resize(nce);
+        for (unsigned i = 0; i < ncf; ++i) {
+            const PpfFaceParam &q = cm_fparam[cm_fprop[i].param_index];
+            cm_margin_f[i] = 0.5f * q.ghat + q.offset;
+        }
+        for (unsigned i = 0; i < nce; ++i) {
+            const PpfEdgeParam &q = cm_eparam[cm_eprop[i].param_index];
+            cm_margin_e[i] = 0.5f * q.ghat + q.offset;
+        }
+        // lbvh/lbvh.cu:1100-1118: static trees over the mesh as it is
+        build(tcf, 3, ncf, cm_face.data(), cm_margin_f.data(), cm_x, cm_x, 1.0f);
+        build(tce, 2, nce, cm_edge.data(), cm_margin_e.data(), cm_x, cm_x, 1.0f);
     }
     const float *c = (const float *)ds->vertex.curr.data;
     const float *pv = (const float *)ds->vertex.prev.data;
@@ -711,6 +757,100 @@ void Oracle::assemble(float dt) {
             add_block(i, i, H);
         }
     }
+    // static collision mesh (contact/contact.cu:1834-1947; element math at
+    // 899-1152): free vertices against its faces, its vertices against the
+    // free faces, free edges against its edges; every block lands in the
+    // fixed pattern
+    if (!prm.disable_contact && ncv) {
+        for (unsigned i = 0; i < nsurf; ++i) {
+            const PpfVertexProp &vp = vprop[i];
+            const PpfVertexParam &vq = vparam[vp.param_index];
+            float q[8];
+            point_box(X(x, i), 0.5f * vq.ghat + vq.offset, q);
+            const Mat3 local = fixed_block(ftmp, i, i);
+            query(tcf, q, [&](unsigned fi) {
+                if (!(vp.fix_index == 0 && vp.mass > 0.0f)) return;
+                const unsigned *cf = &cm_face[3 * fi];
+                const PpfFaceParam &fq = cm_fparam[cm_fprop[fi].param_index];
+                Vec3 f;
+                Mat3 H;
+                if (contact::mesh_vertex_face(
+                        X(x, i), X(curr, i), vp.mass, local, CX(cf[0]), CX(cf[1]), CX(cf[2]),
+                        vq.offset + fq.offset, 0.5f * (vq.ghat + fq.ghat),
+                        contact::combine_friction(vq.friction, fq.friction, prm.friction_mode),
+                        prm.friction_eps, f, H)) {
+                    for (int d = 0; d < 3; ++d) force[3 * i + d] += f[d];
+                    add_block(i, i, H);
+                }
+            });
+        }
+        for (unsigned v = 0; v < ncv; ++v) {
+            const PpfVertexParam &cq = cm_vparam[cm_vprop[v].param_index];
+            float q[8];
+            point_box(CX(v), 0.5f * cq.ghat + cq.offset, q);
+            query(tf, q, [&](unsigned fi) {
+                const PpfFaceProp &fp = fprop[fi];
+                if (fp.fixed || !(fp.mass > 0.0f)) return;
+                const unsigned *fc = &face[3 * fi];
+                const PpfFaceParam &fq = fparam[fp.param_index];
+                Vec3 t[3], s[3];
+                float m[3];
+                Mat9 local;
+                for (int a = 0; a < 3; ++a) {
+                    t[a] = X(x, fc[a]);
+                    s[a] = X(curr, fc[a]);
+                    m[a] = vprop[fc[a]].mass;
+                    for (int b = 0; b < 3; ++b)
+                        local.set_block<3, 3>(3 * a, 3 * b, fixed_block(ftmp, fc[a], fc[b]));
+                }
+                Mat<3, 3> ff;
+                Mat9 HH;
+                if (contact::mesh_face_vertex(
+                        CX(v), t, s, m, local, fq.offset + cq.offset, 0.5f * (fq.ghat + cq.ghat),
+                        contact::combine_friction(fq.friction, cq.friction, prm.friction_mode),
+                        prm.friction_eps, ff, HH)) {
+                    for (int a = 0; a < 3; ++a)
+                        for (int d = 0; d < 3; ++d) force[3 * fc[a] + d] += ff(d, a);
+                    for (int a = 0; a < 3; ++a)
+                        for (int b = 0; b < 3; ++b)
+                            if (fc[a] <= fc[b]) add_block(fc[a], fc[b], HH.block<3, 3>(3 * a, 3 * b));
+                }
+            });
+        }
+        for (unsigned ei = 0; ei < ne; ++ei) {
+            const PpfEdgeProp &ep = eprop[ei];
+            const PpfEdgeParam &eq = eparam[ep.param_index];
+            const unsigned *ed = &edge[2 * ei];
+            const Vec3 a = X(x, ed[0]), b = X(x, ed[1]);
+            const float m = 0.5f * eq.ghat + eq.offset;
+            float q[8] = {std::fmin(a[0], b[0]) - m, std::fmin(a[1], b[1]) - m, std::fmin(a[2], b[2]) - m,
+                          1.0f, std::fmax(a[0], b[0]) + m, std::fmax(a[1], b[1]) + m,
+                          std::fmax(a[2], b[2]) + m, 0.0f};
+            Mat6 local;
+            for (int u = 0; u < 2; ++u)
+                for (int w = 0; w < 2; ++w)
+                    local.set_block<3, 3>(3 * u, 3 * w, fixed_block(ftmp, ed[u], ed[w]));
+            query(tce, q, [&](unsigned ce) {
+                if (ep.fixed || !(ep.mass > 0.0f)) return;
+                const unsigned *cedge = &cm_edge[2 * ce];
+                const PpfEdgeParam &cq = cm_eparam[cm_eprop[ce].param_index];
+                Mat<3, 2> ff;
+                Mat6 HH;
+                if (contact::mesh_edge_edge(
+                        a, b, X(curr, ed[0]), X(curr, ed[1]), CX(cedge[0]), CX(cedge[1]),
+                        vprop[ed[0]].mass, vprop[ed[1]].mass, local, eq.offset + cq.offset,
+                        0.5f * (eq.ghat + cq.ghat),
+                        contact::combine_friction(eq.friction, cq.friction, prm.friction_mode),
+                        prm.friction_eps, ff, HH)) {
+                    for (int u = 0; u < 2; ++u)
+                        for (int d = 0; d < 3; ++d) force[3 * ed[u] + d] += ff(d, u);
+                    for (int u = 0; u < 2; ++u)
+                        for (int w = 0; w < 2; ++w)
+                            if (ed[u] <= ed[w]) add_block(ed[u], ed[w], HH.block<3, 3>(3 * u, 3 * w));
+                }
+            });
+        }
+    }
     // Dirichlet elimination
     if (dirichlet && !fix.empty()) {
         auto mask = [&](unsigned v) { return vprop[v].fix_index > 0 && vprop[v].pdrd_body_index == 0; };
@@ -985,14 +1125,61 @@ float Oracle::line_search(unsigned &pin_bad, bool &overlap) {
                     if (r == 0.0f) ov[v] = 1;
                 }
             });
+            // against the static collision mesh's faces (contact.cu:2596-2626)
+            if (vp.fix_index == 0 && vp.mass > 0.0f)
+                query(tcf, q, [&](unsigned fi) {
+                    const unsigned *cf = &cm_face[3 * fi];
+                    const PpfFaceParam &fp = cm_fparam[cm_fprop[fi].param_index];
+                    accd::CcdFlag flag;
+                    float r = accd::point_triangle(X(x0, v), X(x, v), CX(cf[0]), CX(cf[1]), CX(cf[2]),
+                                                   CX(cf[0]), CX(cf[1]), CX(cf[2]), pv.offset + fp.offset,
+                                                   0.5f * (pv.ghat + fp.ghat), T, prm.ccd_eps, &flag);
+                    if (r < T) {
+                        toi = std::fmin(toi, r);
+                        if (r == 0.0f) ov[v] = 1;
+                    }
+                });
         }
         vtoi[v] = toi;
+    }
+    // the collision mesh's vertices against the free faces (contact.cu:2628-2655)
+    std::vector<float> ctoi(ncv, T);
+    std::vector<char> cov(ncv, 0);
+    if (!prm.disable_contact) {
+#pragma omp parallel for schedule(dynamic, 64)
+        for (long long cvi = 0; cvi < (long long)ncv; ++cvi) {
+            const unsigned cv = (unsigned)cvi;
+            const PpfVertexParam &cq = cm_vparam[cm_vprop[cv].param_index];
+            const Vec3 y = CX(cv);
+            float q[8];
+            point_box(y, 0.5f * cq.ghat + cq.offset, q);
+            float toi = T;
+            query(tf, q, [&](unsigned fi) {
+                const PpfFaceProp &fp = fprop[fi];
+                if (fp.fixed || !(fp.mass > 0.0f)) return;
+                const unsigned *f = &face[3 * fi];
+                const PpfFaceParam &fq = fparam[fp.param_index];
+                accd::CcdFlag flag;
+                float r = accd::point_triangle(y, y, X(x0, f[0]), X(x0, f[1]), X(x0, f[2]), X(x, f[0]),
+                                               X(x, f[1]), X(x, f[2]), fq.offset + cq.offset,
+                                               0.5f * (fq.ghat + cq.ghat), T, prm.ccd_eps, &flag);
+                if (r < T) {
+                    toi = std::fmin(toi, r);
+                    if (r == 0.0f) cov[cv] = 1;
+                }
+            });
+            ctoi[cv] = toi;
+        }
     }
     float seed = T;
     for (unsigned v = 0; v < nsurf; ++v) {
         seed = std::fmin(seed, vtoi[v]);
         pin_bad = std::min(pin_bad, bad[v]);
         if (ov[v]) overlap = true;
+    }
+    for (unsigned cv = 0; cv < ncv; ++cv) {
+        seed = std::fmin(seed, ctoi[cv]);
+        if (cov[cv]) overlap = true;
     }
     std::vector<float> te_(ne, T);
     std::vector<char> ove(ne, 0);
@@ -1044,6 +1231,21 @@ float Oracle::line_search(unsigned &pin_bad, bool &overlap) {
                     if (r == 0.0f) ove[e] = 1;
                 }
             });
+            // against the static collision mesh's edges (contact.cu:2697-2732)
+            if (!eprop[e].fixed && eprop[e].mass > 0.0f)
+                query(tce, q, [&](unsigned ce) {
+                    const unsigned *c = &cm_edge[2 * ce];
+                    const PpfEdgeParam &pa = eparam[eprop[e].param_index];
+                    const PpfEdgeParam &pb = cm_eparam[cm_eprop[ce].param_index];
+                    accd::CcdFlag flag;
+                    float r = accd::edge_edge(X(x0, ed[0]), X(x0, ed[1]), CX(c[0]), CX(c[1]), X(x, ed[0]),
+                                              X(x, ed[1]), CX(c[0]), CX(c[1]), pa.offset + pb.offset,
+                                              0.5f * (pa.ghat + pb.ghat), T, prm.ccd_eps, &flag);
+                    if (r < T) {
+                        toi = std::fmin(toi, r);
+                        if (r == 0.0f) ove[e] = 1;
+                    }
+                });
             te_[e] = toi;
         }
     }
@@ -1074,6 +1276,12 @@ bool Oracle::intersection_free(const std::vector<float> &xx) {
                 if (ed[0] == f[k] || ed[1] == f[k]) return;
             if (contact::edge_triangle_intersect(a, b, X(xx, f[0]), X(xx, f[1]), X(xx, f[2]))) ok = false;
         });
+        // against the static collision mesh's faces (contact.cu:3114-3122)
+        if (eprop[e].mass > 0.0f)
+            query(tcf, q, [&](unsigned fi) {
+                const unsigned *f = &cm_face[3 * fi];
+                if (contact::edge_triangle_intersect(a, b, CX(f[0]), CX(f[1]), CX(f[2]))) ok = false;
+            });
         query(te, q, [&](unsigned o) {
             if (!(o < e)) return;
             const unsigned *e1 = &edge[2 * o];

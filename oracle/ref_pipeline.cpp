@@ -249,8 +249,8 @@ namespace {
 // by median splits. Which valid tree the query walks does not change what it
 // finds, so the reference's own LBVH builder (device code) is not needed.
 struct HostTrees {
-    std::vector<Vec2u> node[3];
-    std::vector<AABB> box[3];
+    std::vector<Vec2u> node[5]; // faces, edges, vertices, collision faces, collision edges
+    std::vector<AABB> box[5];
 };
 
 AABB join_box(const AABB &a, const AABB &b) {
@@ -412,6 +412,31 @@ struct RefPipe {
         install_tree(bvh_storage::get_bvh().vertex, contact::get_vertex_aabb(), trees.node[2],
                      trees.box[2], leaf);
     }
+
+    // The static collision mesh's trees (lbvh/lbvh.cu:1100-1118: boxes of the
+    // mesh as it is, widened by its parameters' 0.5 ghat + offset).
+    void build_collision_trees() {
+        const CollisionMesh &cm = data.constraint.mesh;
+        const Vec3f *v = cm.vertex.data;
+        std::vector<AABB> leaf(cm.face.size);
+        for (unsigned i = 0; i < cm.face.size; ++i) {
+            const Vec3u f = cm.face[i];
+            Vec3f y[3] = {v[f[0]], v[f[1]], v[f[2]]};
+            const FaceParam &fp = cm.param_arrays.face[cm.prop.face[i].param_index];
+            leaf[i] = leaf_box(y, y, 3, 1.0f, 0.5f * fp.ghat + fp.offset);
+        }
+        install_tree(bvh_storage::get_collision_mesh_bvh().face,
+                     contact::get_collision_mesh_face_aabb(), trees.node[3], trees.box[3], leaf);
+        leaf.resize(cm.edge.size);
+        for (unsigned i = 0; i < cm.edge.size; ++i) {
+            const Vec2u g = cm.edge[i];
+            Vec3f y[2] = {v[g[0]], v[g[1]]};
+            const EdgeParam &ep = cm.param_arrays.edge[cm.prop.edge[i].param_index];
+            leaf[i] = leaf_box(y, y, 2, 1.0f, 0.5f * ep.ghat + ep.offset);
+        }
+        install_tree(bvh_storage::get_collision_mesh_bvh().edge,
+                     contact::get_collision_mesh_edge_aabb(), trees.node[4], trees.box[4], leaf);
+    }
 };
 
 RefPipe *g_pipe = nullptr;
@@ -440,6 +465,7 @@ bool refpipe_init(const DataSet *ds, const ParamSet *param) {
     p.fixed = FixedCSRMat::alloc(p.data.fixed_index_table, p.data.transpose_table);
     p.tmp_fixed = FixedCSRMat::alloc(p.data.fixed_index_table, p.data.transpose_table);
     contact::initialize(p.data, p.prm);
+    p.build_collision_trees();
     return true;
 }
 

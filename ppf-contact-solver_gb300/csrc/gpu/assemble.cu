@@ -617,6 +617,171 @@ __global__ void k_vertex_constraints(Scene s, StepParams p, AssemblyBuffers b) {
     atomicAdd(&b.st->n_contact, nc);
 }
 
+// ---- static collision mesh (contact/contact.cu:1834-1947) -------------------
+// Push-model contacts against a mesh without degrees of freedom (element math
+// in contact_local.cuh). Every block they touch is in the fixed pattern: a
+// vertex's diagonal, a face's and an edge's own blocks.
+
+// A free vertex against the collision faces.
+struct MeshFaceOp {
+    const Scene &s;
+    const StepParams &p;
+    const AssemblyBuffers &b;
+    unsigned v;
+    Mat3 local;
+    Vec3 f;
+    Mat3 H;
+    unsigned n;
+    __device__ void operator()(unsigned fi) {
+        const PpfVertexProp &vp = s.vprop[v];
+        const unsigned *cf = s.cm_face + 3 * fi;
+        const PpfVertexParam &vq = s.vparam[vp.param_index];
+        const PpfFaceParam &fq = s.cm_fparam[s.cm_fprop[fi].param_index];
+        Vec3 fo;
+        Mat3 Ho;
+        if (contact::mesh_vertex_face(X(b.x, v), X(b.x0, v), vp.mass, local, X(s.cm_x, cf[0]),
+                                      X(s.cm_x, cf[1]), X(s.cm_x, cf[2]), vq.offset + fq.offset,
+                                      0.5f * (vq.ghat + fq.ghat),
+                                      contact::combine_friction(vq.friction, fq.friction,
+                                                                p.friction_mode),
+                                      p.friction_eps, fo, Ho)) {
+            f += fo;
+            H += Ho;
+            ++n;
+        }
+    }
+};
+
+__global__ void k_mesh_vertex_face(Scene s, StepParams p, AssemblyBuffers b) {
+    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= s.n_surf) return;
+    const PpfVertexProp &vp = s.vprop[v];
+    if (!(vp.fix_index == 0 && vp.mass > 0.0f)) return;
+    const PpfVertexParam &vq = s.vparam[vp.param_index];
+    const Vec3 x = X(b.x, v);
+    const float m = 0.5f * vq.ghat + vq.offset + detect_guard(x);
+    const float4 qmin = make_float4(x[0] - m, x[1] - m, x[2] - m, 1.0f);
+    const float4 qmax = make_float4(x[0] + m, x[1] + m, x[2] + m, 0.0f);
+    MeshFaceOp op{s, p, b, v, load_block(b.fixed_tmp + 9 * (size_t)s.fixed_diag[v]),
+                  Vec3::zero(), Mat3::zero(), 0u};
+    bvh_query(s.cm_face_bvh, qmin, qmax, op, &b.st->status);
+    if (!op.n) return;
+    atomic_add3(b.force + 3 * v, op.f);
+    atomic_add_block(b.fixed_val + 9 * (size_t)s.fixed_diag[v], op.H);
+    atomicAdd(&b.st->n_contact, op.n);
+}
+
+// A collision vertex against the free faces.
+struct MeshVertexOp {
+    const Scene &s;
+    const StepParams &p;
+    const AssemblyBuffers &b;
+    unsigned cv;
+    unsigned n;
+    __device__ void operator()(unsigned fi) {
+        const PpfFaceProp &fp = s.fprop[fi];
+        if (fp.fixed || !(fp.mass > 0.0f)) return;
+        const unsigned *fc = s.face + 3 * fi;
+        const PpfFaceParam &fq = s.fparam[fp.param_index];
+        const PpfVertexParam &cq = s.cm_vparam[s.cm_vprop[cv].param_index];
+        Vec3 t[3], sx[3];
+        float m[3];
+        Mat9 local;
+        for (int a = 0; a < 3; ++a) {
+            t[a] = X(b.x, fc[a]);
+            sx[a] = X(b.x0, fc[a]);
+            m[a] = s.vprop[fc[a]].mass;
+            for (int c = 0; c < 3; ++c)
+                local.set_block<3, 3>(3 * a, 3 * c, fixed_block(s, b.fixed_tmp, fc[a], fc[c]));
+        }
+        Mat<3, 3> ff;
+        Mat9 HH;
+        if (!contact::mesh_face_vertex(X(s.cm_x, cv), t, sx, m, local, fq.offset + cq.offset,
+                                       0.5f * (fq.ghat + cq.ghat),
+                                       contact::combine_friction(fq.friction, cq.friction,
+                                                                 p.friction_mode),
+                                       p.friction_eps, ff, HH))
+            return;
+        for (int a = 0; a < 3; ++a) atomic_add3(b.force + 3 * fc[a], ff.col(a));
+        const unsigned *slot = s.face_slot + 9 * fi;
+        for (int a = 0; a < 3; ++a)
+            for (int c = 0; c < 3; ++c) {
+                const unsigned sl = slot[3 * a + c];
+                if (sl != kSentinel)
+                    atomic_add_block(b.fixed_val + 9 * (size_t)sl, HH.block<3, 3>(3 * a, 3 * c));
+            }
+        ++n;
+    }
+};
+
+__global__ void k_mesh_face_vertex(Scene s, StepParams p, AssemblyBuffers b, BvhView fb) {
+    unsigned cv = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cv >= s.ncv) return;
+    const PpfVertexParam &cq = s.cm_vparam[s.cm_vprop[cv].param_index];
+    const Vec3 y = X(s.cm_x, cv);
+    const float m = 0.5f * cq.ghat + cq.offset + detect_guard(y);
+    const float4 qmin = make_float4(y[0] - m, y[1] - m, y[2] - m, 1.0f);
+    const float4 qmax = make_float4(y[0] + m, y[1] + m, y[2] + m, 0.0f);
+    MeshVertexOp op{s, p, b, cv, 0u};
+    bvh_query(fb, qmin, qmax, op, &b.st->status);
+    if (op.n) atomicAdd(&b.st->n_contact, op.n);
+}
+
+// A free edge of positive mass against the collision edges (a shell's edges
+// carry no mass, so for cloth this finds nothing, as in the reference).
+struct MeshEdgeOp {
+    const Scene &s;
+    const StepParams &p;
+    const AssemblyBuffers &b;
+    unsigned e;
+    unsigned n;
+    __device__ void operator()(unsigned ce) {
+        const unsigned *ed = s.edge + 2 * e, *c = s.cm_edge + 2 * ce;
+        const PpfEdgeParam &eq = s.eparam[s.eprop[e].param_index];
+        const PpfEdgeParam &cq = s.cm_eparam[s.cm_eprop[ce].param_index];
+        Mat6 local;
+        for (int u = 0; u < 2; ++u)
+            for (int w = 0; w < 2; ++w)
+                local.set_block<3, 3>(3 * u, 3 * w, fixed_block(s, b.fixed_tmp, ed[u], ed[w]));
+        Mat<3, 2> ff;
+        Mat6 HH;
+        if (!contact::mesh_edge_edge(X(b.x, ed[0]), X(b.x, ed[1]), X(b.x0, ed[0]), X(b.x0, ed[1]),
+                                     X(s.cm_x, c[0]), X(s.cm_x, c[1]), s.vprop[ed[0]].mass,
+                                     s.vprop[ed[1]].mass, local, eq.offset + cq.offset,
+                                     0.5f * (eq.ghat + cq.ghat),
+                                     contact::combine_friction(eq.friction, cq.friction,
+                                                               p.friction_mode),
+                                     p.friction_eps, ff, HH))
+            return;
+        for (int u = 0; u < 2; ++u) atomic_add3(b.force + 3 * ed[u], ff.col(u));
+        for (int u = 0; u < 2; ++u)
+            for (int w = 0; w < 2; ++w)
+                if (ed[u] <= ed[w]) {
+                    const unsigned sl = fixed_slot(s, ed[u], ed[w]);
+                    if (sl != kSentinel)
+                        atomic_add_block(b.fixed_val + 9 * (size_t)sl,
+                                         HH.block<3, 3>(3 * u, 3 * w));
+                }
+        ++n;
+    }
+};
+
+__global__ void k_mesh_edge_edge(Scene s, StepParams p, AssemblyBuffers b) {
+    unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= s.ne) return;
+    const PpfEdgeProp &ep = s.eprop[e];
+    if (ep.fixed || !(ep.mass > 0.0f)) return;
+    const unsigned *ed = s.edge + 2 * e;
+    const PpfEdgeParam &eq = s.eparam[ep.param_index];
+    float4 qmin, qmax;
+    const Vec3 a = X(b.x, ed[0]), c = X(b.x, ed[1]);
+    seg_box(a, c, 0.5f * eq.ghat + eq.offset + fmaxf(detect_guard(a), detect_guard(c)), qmin,
+            qmax);
+    MeshEdgeOp op{s, p, b, e, 0u};
+    bvh_query(s.cm_edge_bvh, qmin, qmax, op, &b.st->status);
+    if (op.n) atomicAdd(&b.st->n_contact, op.n);
+}
+
 // ---- Dirichlet elimination of pinned vertices (main.cu:954-1049) -------------
 __device__ __forceinline__ void lift_sub(float *force, unsigned row, const Mat3 &blk,
                                          const Vec3 &pv, bool transposed) {
@@ -845,6 +1010,21 @@ void launch_vertex_constraints(const Scene &s, const StepParams &p,
     if (!s.n_surf || (s.nsphere == 0 && s.nfloor == 0)) return;
     k_vertex_constraints<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, p, b);
     PPF_LAUNCH_CHECK();
+}
+
+void launch_collision_mesh(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+                           const BvhView &fb, cudaStream_t q) {
+    if (!s.ncv) return;
+    if (s.ncf && s.n_surf) {
+        k_mesh_vertex_face<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, p, b);
+        PPF_LAUNCH_CHECK();
+    }
+    k_mesh_face_vertex<<<div_up(s.ncv, kB), kB, 0, q>>>(s, p, b, fb);
+    PPF_LAUNCH_CHECK();
+    if (s.nce && s.ne) {
+        k_mesh_edge_edge<<<div_up(s.ne, kB), kB, 0, q>>>(s, p, b);
+        PPF_LAUNCH_CHECK();
+    }
 }
 
 void launch_dirichlet(const Scene &s, const AssemblyBuffers &b, const DynMatrix &dm,

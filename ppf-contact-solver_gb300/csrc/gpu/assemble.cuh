@@ -69,6 +69,10 @@ void launch_contact_assemble(const Scene &s, const StepParams &p,
                              const unsigned counts[4], DynMatrix &dm, cudaStream_t q);
 void launch_vertex_constraints(const Scene &s, const StepParams &p,
                                const AssemblyBuffers &b, cudaStream_t q);
+// Contacts against the static collision mesh (contact/contact.cu:1834-1947);
+// fb is the free faces' tree of this Newton iteration.
+void launch_collision_mesh(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+                           const BvhView &fb, cudaStream_t q);
 void launch_dirichlet(const Scene &s, const AssemblyBuffers &b, const DynMatrix &dm,
                       float *dx, cudaStream_t q);
 // Exclusive scan of n u32 into out (n + 1 entries, out[n] = total).

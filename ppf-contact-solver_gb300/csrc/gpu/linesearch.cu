@@ -156,6 +156,98 @@ struct PointPointCcdOp {
     }
 };
 
+// ---- static collision mesh (contact/contact.cu:1956-2094, 2596-2732) --------
+// A free vertex's sweep against the collision faces.
+struct MeshPointFaceCcdOp {
+    const Scene &s;
+    const LineSearchArgs &a;
+    unsigned v;
+    float toi;
+    __device__ void operator()(unsigned fi) {
+        const unsigned *cf = s.cm_face + 3 * fi;
+        const PpfVertexParam &vq = s.vparam[s.vprop[v].param_index];
+        const PpfFaceParam &fq = s.cm_fparam[s.cm_fprop[fi].param_index];
+        const Vec3 t0 = X(s.cm_x, cf[0]), t1 = X(s.cm_x, cf[1]), t2 = X(s.cm_x, cf[2]);
+        accd::CcdFlag fl;
+        float r = accd::point_triangle(X(a.x0, v), X(a.x1, v), t0, t1, t2, t0, t1, t2,
+                                       vq.offset + fq.offset, 0.5f * (vq.ghat + fq.ghat), a.max_t,
+                                       a.ccd_eps, &fl);
+        if (r < a.max_t) {
+            toi = fminf(toi, r);
+            if (r == 0.0f) {
+                record_overlap(a.st, fl, v, cf[0], 3u);
+                if (!fl.overlap) atomicOr(&a.st->overlap, 1u);
+            }
+        }
+    }
+};
+
+// A collision vertex against the free faces' sweeps.
+struct MeshVertexCcdOp {
+    const Scene &s;
+    const LineSearchArgs &a;
+    unsigned cv;
+    float toi;
+    __device__ void operator()(unsigned fi) {
+        const PpfFaceProp &fp = s.fprop[fi];
+        if (fp.fixed || !(fp.mass > 0.0f)) return;
+        const unsigned *f = s.face + 3 * fi;
+        const PpfFaceParam &fq = s.fparam[fp.param_index];
+        const PpfVertexParam &cq = s.cm_vparam[s.cm_vprop[cv].param_index];
+        const Vec3 y = X(s.cm_x, cv);
+        accd::CcdFlag fl;
+        float r = accd::point_triangle(y, y, X(a.x0, f[0]), X(a.x0, f[1]), X(a.x0, f[2]),
+                                       X(a.x1, f[0]), X(a.x1, f[1]), X(a.x1, f[2]),
+                                       fq.offset + cq.offset, 0.5f * (fq.ghat + cq.ghat), a.max_t,
+                                       a.ccd_eps, &fl);
+        if (r < a.max_t) {
+            toi = fminf(toi, r);
+            if (r == 0.0f) {
+                record_overlap(a.st, fl, f[0], cv, 4u);
+                if (!fl.overlap) atomicOr(&a.st->overlap, 1u);
+            }
+        }
+    }
+};
+
+// A free edge of positive mass against the collision edges.
+struct MeshEdgeCcdOp {
+    const Scene &s;
+    const LineSearchArgs &a;
+    unsigned e;
+    float toi;
+    __device__ void operator()(unsigned ce) {
+        const unsigned *ed = s.edge + 2 * e, *c = s.cm_edge + 2 * ce;
+        const PpfEdgeParam &pa = s.eparam[s.eprop[e].param_index];
+        const PpfEdgeParam &pb = s.cm_eparam[s.cm_eprop[ce].param_index];
+        const Vec3 q0 = X(s.cm_x, c[0]), q1 = X(s.cm_x, c[1]);
+        accd::CcdFlag fl;
+        float r = accd::edge_edge(X(a.x0, ed[0]), X(a.x0, ed[1]), q0, q1, X(a.x1, ed[0]),
+                                  X(a.x1, ed[1]), q0, q1, pa.offset + pb.offset,
+                                  0.5f * (pa.ghat + pb.ghat), a.max_t, a.ccd_eps, &fl);
+        if (r < a.max_t) {
+            toi = fminf(toi, r);
+            if (r == 0.0f) {
+                record_overlap(a.st, fl, ed[0], c[0], 5u);
+                if (!fl.overlap) atomicOr(&a.st->overlap, 1u);
+            }
+        }
+    }
+};
+
+__global__ void k_ccd_mesh_vertex(Scene s, BvhView fb, LineSearchArgs a) {
+    unsigned cv = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cv >= s.ncv) return;
+    const PpfVertexParam &cq = s.cm_vparam[s.cm_vprop[cv].param_index];
+    const Vec3 y = X(s.cm_x, cv);
+    const float m = 0.5f * cq.ghat + cq.offset;
+    const float4 qmin = make_float4(y[0] - m, y[1] - m, y[2] - m, 1.0f);
+    const float4 qmax = make_float4(y[0] + m, y[1] + m, y[2] + m, 0.0f);
+    MeshVertexCcdOp op{s, a, cv, a.max_t};
+    bvh_query(fb, qmin, qmax, op, &a.st->status);
+    atomicMin(&a.st->toi_vf_bits, __float_as_uint(op.toi));
+}
+
 __global__ void k_ccd_vertex(Scene s, BvhView fb, BvhView vb, LineSearchArgs a) {
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= s.n_surf) return;
@@ -172,6 +264,12 @@ __global__ void k_ccd_vertex(Scene s, BvhView fb, BvhView vb, LineSearchArgs a) 
     PointPointCcdOp pp{s, a, v, a.max_t};
     bvh_query(vb, qmin, qmax, pp, &a.st->status);
     toi = fminf(toi, fminf(pf.toi, pp.toi));
+    const PpfVertexProp &vp = s.vprop[v];
+    if (s.ncf && vp.fix_index == 0 && vp.mass > 0.0f) {
+        MeshPointFaceCcdOp mf{s, a, v, a.max_t};
+        bvh_query(s.cm_face_bvh, qmin, qmax, mf, &a.st->status);
+        toi = fminf(toi, mf.toi);
+    }
     atomicMin(&a.st->toi_vf_bits, __float_as_uint(toi));
 }
 
@@ -254,6 +352,11 @@ __global__ void k_ccd_edge(Scene s, BvhView eb, LineSearchArgs a, EdgePieces ep)
         qmax.w = 0.0f;
         EdgeEdgeCcdOp op{s, a, e, seed};
         bvh_query(eb, qmin, qmax, op, &a.st->status);
+        if (s.nce && !s.eprop[e].fixed && s.eprop[e].mass > 0.0f) {
+            MeshEdgeCcdOp me{s, a, e, op.toi};
+            bvh_query(s.cm_edge_bvh, qmin, qmax, me, &a.st->status);
+            op.toi = me.toi;
+        }
         atomicMin(&a.st->toi_bits, __float_as_uint(op.toi));
     }
 }
@@ -373,6 +476,35 @@ struct EdgeEdgeIsectOp {
 // Piece boxes carry the edge's contact offset plus a rounding guard: every
 // pierced face contains the pierce point, and every edge nearer than the
 // combined offset lies within the edge's offset plus its own leaf margin.
+// A free edge of positive mass piercing a collision face
+// (contact/contact.cu:2955-2987, 3114-3122).
+struct MeshFaceEdgeIsectOp {
+    const Scene &s;
+    const float *x;
+    unsigned e;
+    PpfIntersectionRecord *records;
+    IterStatus *st;
+    __device__ void operator()(unsigned fi) {
+        const unsigned *f = s.cm_face + 3 * fi;
+        const unsigned *ed = s.edge + 2 * e;
+        const Vec3 t0 = X(s.cm_x, f[0]), t1 = X(s.cm_x, f[1]), t2 = X(s.cm_x, f[2]);
+        const Vec3 y0 = X(x, ed[0]), y1 = X(x, ed[1]);
+        if (!contact::edge_triangle_intersect(y0, y1, t0, t1, t2)) return;
+        unsigned slot = atomicAdd(&st->n_isect, 1u);
+        if (slot < PPF_MAX_INTERSECTION_RECORDS) {
+            PpfIntersectionRecord &r = records[slot];
+            r.type = 2;
+            r.elem0 = fi;
+            r.elem1 = e;
+            r.num_verts0 = 3;
+            r.num_verts1 = 2;
+            const Vec3 vs[5] = {t0, t1, t2, y0, y1};
+            for (int k = 0; k < 5; ++k)
+                for (int d = 0; d < 3; ++d) r.positions[3 * k + d] = vs[k][d];
+        }
+    }
+};
+
 __global__ void k_isect(Scene s, BvhView fb, BvhView eb, const float *x,
                         PpfIntersectionRecord *rec, IterStatus *st, EdgePieces ep) {
     const unsigned total = ep.off[ep.n];
@@ -399,6 +531,10 @@ __global__ void k_isect(Scene s, BvhView fb, BvhView eb, const float *x,
         bvh_query(fb, qmin, qmax, op, &st->status, xl, xh);
         EdgeEdgeIsectOp op2{s, x, e, rec, st};
         bvh_query(eb, qmin, qmax, op2, &st->status, xl, xh);
+        if (s.ncf && s.eprop[e].mass > 0.0f) {
+            MeshFaceEdgeIsectOp op3{s, x, e, rec, st};
+            bvh_query(s.cm_face_bvh, qmin, qmax, op3, &st->status, xl, xh);
+        }
     }
 }
 
@@ -409,6 +545,10 @@ void launch_contact_line_search(const Scene &s, const BvhView &fb, const BvhView
                                 PieceBuffers &pb, cudaStream_t q) {
     if (s.n_surf) {
         k_ccd_vertex<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, fb, vb, a);
+        PPF_LAUNCH_CHECK();
+    }
+    if (s.ncv) { // before the edge seed is read
+        k_ccd_mesh_vertex<<<div_up(s.ncv, kB), kB, 0, q>>>(s, fb, a);
         PPF_LAUNCH_CHECK();
     }
     if (s.ne) {

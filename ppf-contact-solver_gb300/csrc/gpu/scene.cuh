@@ -77,6 +77,17 @@ struct Scene {
     const float *margin_face, *margin_edge, *margin_vert;
     // collision-window activity (null when every element is active)
     const unsigned char *vert_active, *edge_active;
+    // static collision mesh (Constraint::mesh) and its trees (built once)
+    unsigned ncv, ncf, nce;
+    const float *cm_x;
+    const unsigned *cm_face, *cm_edge;
+    const PpfVertexProp *cm_vprop;
+    const PpfFaceProp *cm_fprop;
+    const PpfEdgeProp *cm_eprop;
+    const PpfVertexParam *cm_vparam;
+    const PpfFaceParam *cm_fparam;
+    const PpfEdgeParam *cm_eparam;
+    BvhView cm_face_bvh, cm_edge_bvh;
 };
 
 struct StepParams {

@@ -232,7 +232,56 @@ Scene Solver::scene() const {
     s.margin_vert = margin_vert_.data();
     s.vert_active = use_active_ ? vert_active_.data() : nullptr;
     s.edge_active = use_active_ ? edge_active_.data() : nullptr;
+    s.ncv = ncv_;
+    s.ncf = ncf_;
+    s.nce = nce_;
+    s.cm_x = cm_x_.data();
+    s.cm_face = cm_face_.data();
+    s.cm_edge = cm_edge_.data();
+    s.cm_vprop = cm_vprop_.data();
+    s.cm_fprop = cm_fprop_.data();
+    s.cm_eprop = cm_eprop_.data();
+    s.cm_vparam = cm_vparam_.data();
+    s.cm_fparam = cm_fparam_.data();
+    s.cm_eparam = cm_eparam_.data();
+    s.cm_face_bvh = view(cm_bvh_face_);
+    s.cm_edge_bvh = view(cm_bvh_edge_);
     return s;
+}
+
+// The collision mesh as the DataSet gives it, and its face and edge trees
+// over the mesh as it is (lbvh/lbvh.cu:1100-1118), built once.
+void Solver::upload_collision_mesh(const PpfCollisionMesh &cm) {
+    ncv_ = cm.vertex.size;
+    ncf_ = cm.face.size;
+    nce_ = cm.edge.size;
+    if (!ncv_) return;
+    upload(cm_x_, (const float *)cm.vertex.data, 3 * (size_t)ncv_);
+    upload(cm_face_, (const unsigned *)cm.face.data, 3 * (size_t)ncf_);
+    upload(cm_edge_, (const unsigned *)cm.edge.data, 2 * (size_t)nce_);
+    upload(cm_vprop_, cm.prop.vertex.data, cm.prop.vertex.size);
+    upload(cm_fprop_, cm.prop.face.data, cm.prop.face.size);
+    upload(cm_eprop_, cm.prop.edge.data, cm.prop.edge.size);
+    upload(cm_vparam_, cm.param_arrays.vertex.data, cm.param_arrays.vertex.size);
+    upload(cm_fparam_, cm.param_arrays.face.data, cm.param_arrays.face.size);
+    upload(cm_eparam_, cm.param_arrays.edge.data, cm.param_arrays.edge.size);
+    std::vector<float> mf(ncf_), me(nce_);
+    for (unsigned i = 0; i < ncf_; ++i) {
+        const PpfFaceParam &p = cm.param_arrays.face.data[cm.prop.face.data[i].param_index];
+        mf[i] = 0.5f * p.ghat + p.offset;
+    }
+    for (unsigned i = 0; i < nce_; ++i) {
+        const PpfEdgeParam &p = cm.param_arrays.edge.data[cm.prop.edge.data[i].param_index];
+        me[i] = 0.5f * p.ghat + p.offset;
+    }
+    upload(cm_margin_f_, mf);
+    upload(cm_margin_e_, me);
+    unsigned *status = &st_.data()->status;
+    const float *x = cm_x_.data();
+    PrimSet pf{PRIM_FACE, ncf_, cm_face_.data(), cm_margin_f_.data(), nullptr};
+    PrimSet pe{PRIM_EDGE, nce_, cm_edge_.data(), cm_margin_e_.data(), nullptr};
+    if (ncf_) lbvh_build(cm_bvh_face_, pf, x, x, x, 1.0f, sort_ws_, status, q_);
+    if (nce_) lbvh_build(cm_bvh_edge_, pe, x, x, x, 1.0f, sort_ws_, status, q_);
 }
 
 StepParams Solver::step_params(float dt) const {
@@ -478,6 +527,7 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     dcnt2_buf_.reserve(n_ + 1);
     scan_tmp_.reserve(scan_tmp_size(n_ + 1));
     pcg_.reserve(n_);
+    upload_collision_mesh(ds->constraint.mesh);
     initialized_ = true;
     // initial trees and intersection check on prev and curr (main.cu:196-262)
     if (!param->disable_contact) {
@@ -672,6 +722,7 @@ void Solver::assemble(float dt) {
     PPF_CUDA(cudaMemsetAsync(dval_buf_.data(), 0, 9 * (size_t)dcap * sizeof(float), q_));
     launch_contact_assemble(s, p, b, pairs_, counts, dyn_, q_);
     launch_vertex_constraints(s, p, b, q_);
+    if (!param->disable_contact) launch_collision_mesh(s, p, b, view(bvh_face_), q_);
     launch_dirichlet(s, b, dyn_, dx_.data(), q_);
     k_fold_diag<<<div_up(n_, kB), kB, 0, q_>>>(n_, fixed_diag_.data(), diag_.data(),
                                               fixed_val_.data());

@@ -139,6 +139,18 @@ class Solver {
     bool learned_ready_ = false; // network weights loaded
     bool force_factor_ = false;  // the debug solve uses the factor directly
     FactorBuffers factor_;
+    // static collision mesh
+    unsigned ncv_ = 0, ncf_ = 0, nce_ = 0;
+    DevBuf<float> cm_x_, cm_margin_f_, cm_margin_e_;
+    DevBuf<unsigned> cm_face_, cm_edge_;
+    DevBuf<PpfVertexProp> cm_vprop_;
+    DevBuf<PpfFaceProp> cm_fprop_;
+    DevBuf<PpfEdgeProp> cm_eprop_;
+    DevBuf<PpfVertexParam> cm_vparam_;
+    DevBuf<PpfFaceParam> cm_fparam_;
+    DevBuf<PpfEdgeParam> cm_eparam_;
+    Lbvh cm_bvh_face_, cm_bvh_edge_;
+    void upload_collision_mesh(const PpfCollisionMesh &cm);
     // aggregate Schwarz (ParamSet::precond == 1), aggregated once per scene
     bool schwarz_active_ = false;
     SchwarzLayout schwarz_;

@@ -80,6 +80,11 @@ struct PpfScene {
     std::vector<std::pair<unsigned, float>> pulls;
     std::vector<PpfSphere> spheres;
     std::vector<PpfFloor> floors;
+    // static collision mesh (Constraint::mesh): triangles and one contact
+    // parameter set per added mesh
+    std::vector<float> cm_x;
+    std::vector<unsigned> cm_faces, cm_face_param;
+    std::vector<PpfVertexParam> cm_params;
 
     // outputs
     std::vector<PpfVec3f> curr, prev;
@@ -103,6 +108,15 @@ struct PpfScene {
     std::vector<PpfVec2u> transpose_data;
     std::vector<unsigned> transpose_offset;
     std::vector<unsigned> face_slots, hinge_slots;
+    std::vector<PpfVec3f> cm_vertex;
+    std::vector<PpfVec3u> cm_face;
+    std::vector<PpfVec2u> cm_edge;
+    std::vector<PpfVertexProp> cm_vprop;
+    std::vector<PpfEdgeProp> cm_eprop;
+    std::vector<PpfFaceProp> cm_fprop;
+    std::vector<PpfVertexParam> cm_vparam;
+    std::vector<PpfEdgeParam> cm_eparam;
+    std::vector<PpfFaceParam> cm_fparam;
     PpfDataSet ds;
     PpfParamSet param;
     bool built = false;
@@ -200,6 +214,16 @@ void ppf_scene_add_sphere(PpfScene *s, const float *c, float r, float gap,
     sp.reverse = reverse != 0;
     sp.kinematic = false;
     s->spheres.push_back(sp);
+}
+
+void ppf_scene_add_collision_mesh(PpfScene *s, const float *v, unsigned nv, const unsigned *f,
+                                  unsigned nf, float gap, float offset, float friction) {
+    const unsigned base = (unsigned)s->cm_x.size() / 3;
+    const unsigned param = (unsigned)s->cm_params.size();
+    s->cm_x.insert(s->cm_x.end(), v, v + 3 * (size_t)nv);
+    for (unsigned i = 0; i < 3 * nf; ++i) s->cm_faces.push_back(base + f[i]);
+    s->cm_face_param.insert(s->cm_face_param.end(), nf, param);
+    s->cm_params.push_back(PpfVertexParam{gap, offset, friction});
 }
 
 void ppf_scene_add_floor(PpfScene *s, const float *g, const float *up, float gap,
@@ -542,6 +566,68 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     set_vec(ds.constraint.pull.data, ds.constraint.pull.size, ds.constraint.pull.allocated, s->pull);
     set_vec(ds.constraint.sphere.data, ds.constraint.sphere.size, ds.constraint.sphere.allocated, s->spheres);
     set_vec(ds.constraint.floor.data, ds.constraint.floor.size, ds.constraint.floor.allocated, s->floors);
+    // collision mesh (builder.rs:1823-1935): vertices, faces, the edges in
+    // first-seen order; every element takes its mesh's contact parameters
+    // (one set per mesh: the reference's area-weighted averages of equal
+    // values), props carry no mass
+    {
+        const unsigned ncv = (unsigned)s->cm_x.size() / 3, ncf = (unsigned)s->cm_faces.size() / 3;
+        s->cm_vertex.resize(ncv);
+        for (unsigned i = 0; i < ncv; ++i)
+            s->cm_vertex[i] = {{s->cm_x[3 * i], s->cm_x[3 * i + 1], s->cm_x[3 * i + 2]}};
+        s->cm_face.resize(ncf);
+        s->cm_edge.clear();
+        s->cm_fprop.assign(ncf, PpfFaceProp{});
+        s->cm_fparam.clear();
+        s->cm_eprop.clear();
+        s->cm_eparam.clear();
+        s->cm_vparam = s->cm_params;
+        s->cm_vprop.assign(ncv, PpfVertexProp{});
+        std::map<std::pair<unsigned, unsigned>, unsigned> cm_edge_id;
+        for (const PpfVertexParam &p : s->cm_params) {
+            PpfFaceParam fp{};
+            fp.model = PPF_MODEL_BARAFF_WITKIN;
+            fp.ghat = p.ghat;
+            fp.offset = p.offset;
+            fp.friction = p.friction;
+            s->cm_fparam.push_back(fp);
+            PpfEdgeParam ep{};
+            ep.ghat = p.ghat;
+            ep.offset = p.offset;
+            ep.friction = p.friction;
+            s->cm_eparam.push_back(ep);
+        }
+        for (unsigned i = 0; i < ncf; ++i) {
+            const unsigned *t = &s->cm_faces[3 * i];
+            const unsigned param = s->cm_face_param[i];
+            s->cm_face[i] = {{t[0], t[1], t[2]}};
+            s->cm_fprop[i].param_index = param;
+            for (int k = 0; k < 3; ++k) {
+                s->cm_vprop[t[k]].param_index = param;
+                s->cm_vprop[t[k]].rest_bend_angle = 3.14159265358979f;
+                const unsigned a = std::min(t[k], t[(k + 1) % 3]), b = std::max(t[k], t[(k + 1) % 3]);
+                if (cm_edge_id.emplace(std::make_pair(a, b), (unsigned)s->cm_edge.size()).second) {
+                    s->cm_edge.push_back({{a, b}});
+                    PpfEdgeProp ep{};
+                    ep.param_index = param;
+                    s->cm_eprop.push_back(ep);
+                }
+            }
+        }
+        PpfCollisionMesh &cm = ds.constraint.mesh;
+        set_vec(cm.vertex.data, cm.vertex.size, cm.vertex.allocated, s->cm_vertex);
+        set_vec(cm.face.data, cm.face.size, cm.face.allocated, s->cm_face);
+        set_vec(cm.edge.data, cm.edge.size, cm.edge.allocated, s->cm_edge);
+        set_vec(cm.prop.vertex.data, cm.prop.vertex.size, cm.prop.vertex.allocated, s->cm_vprop);
+        set_vec(cm.prop.face.data, cm.prop.face.size, cm.prop.face.allocated, s->cm_fprop);
+        set_vec(cm.prop.edge.data, cm.prop.edge.size, cm.prop.edge.allocated, s->cm_eprop);
+        set_vec(cm.param_arrays.vertex.data, cm.param_arrays.vertex.size,
+                cm.param_arrays.vertex.allocated, s->cm_vparam);
+        set_vec(cm.param_arrays.face.data, cm.param_arrays.face.size,
+                cm.param_arrays.face.allocated, s->cm_fparam);
+        set_vec(cm.param_arrays.edge.data, cm.param_arrays.edge.size,
+                cm.param_arrays.edge.allocated, s->cm_eparam);
+    }
     s->fixed_table.fill(ds.fixed_index_table);
     ds.transpose_table.data = s->transpose_data.empty() ? nullptr : s->transpose_data.data();
     ds.transpose_table.offset = s->transpose_offset.data();

@@ -212,5 +212,104 @@ PPF_HD bool shared_edges_within_offset(const Vec3 &s, const Vec3 &a, const Vec3 
     return fminf(d0, d1) < offset * offset;
 }
 
+// ---- static collision mesh (contact/contact.cu:899-1152) --------------------
+// The push model of the analytic colliders, against the triangles and edges
+// of a mesh without degrees of freedom. `local` is the elastic-only block(s)
+// of the fixed Hessian the stiffness is read from.
+
+// A free vertex at p (start of step x_start) against the static triangle
+// (t0, t1, t2) (contact.cu:899-962). Force and Hessian of the vertex.
+PPF_HD unsigned mesh_vertex_face(const Vec3 &p, const Vec3 &x_start, float mass,
+                                 const Mat3 &local, const Vec3 &t0w, const Vec3 &t1w,
+                                 const Vec3 &t2w, float offset, float ghat, float mu,
+                                 float friction_eps, Vec3 &f, Mat3 &H) {
+    const Vec3 q = x_start - p;
+    const Vec3 t0 = t0w - p, t1 = t1w - p, t2 = t2w - p;
+    const Vec3 c = dist::point_triangle_coeff_unclassified(Vec3::zero(), t0, t1, t2);
+    const Vec3 y = c[0] * t0 + c[1] * t1 + c[2] * t2;
+    const Vec3 e = -y;
+    if (!(e.squared_norm() < sqr(offset + ghat))) return 0u;
+    const Vec3 normal = e.normalized();
+    const Vec3 proj_x = y + (offset + ghat) * normal;
+    const float gap_squared = sqr(e.norm() - offset);
+    const float stiff_k = normal.dot(local * normal) + mass / gap_squared;
+    f = stiff_k * push::gradient(-proj_x, normal, ghat);
+    H = stiff_k * push::hessian(-proj_x, normal, ghat);
+    Friction fr(f, -q, normal, mu, friction_eps);
+    f += fr.gradient();
+    H += fr.hessian();
+    return 1u;
+}
+
+// A static vertex y against the free triangle with vertices at t (start of
+// step s) (contact.cu:964-1057): local is the 9x9 elastic block of the
+// triangle, mass the triangle vertices' masses. Writes the 3 force columns
+// and the 9x9 Hessian over the triangle's vertices.
+PPF_HD unsigned mesh_face_vertex(const Vec3 &y, const Vec3 (&t)[3], const Vec3 (&s)[3],
+                                 const float (&mass)[3], const Mat9 &local, float offset,
+                                 float ghat, float mu, float friction_eps, Mat<3, 3> &ff,
+                                 Mat9 &HH) {
+    const Vec3 t0 = t[0] - y, t1 = t[1] - y, t2 = t[2] - y;
+    const Vec3 s0 = s[0] - y, s1 = s[1] - y, s2 = s[2] - y;
+    const Vec3 c = dist::point_triangle_coeff_unclassified(Vec3::zero(), t0, t1, t2);
+    const Vec3 p = c[0] * t0 + c[1] * t1 + c[2] * t2;
+    const Vec3 q = c[0] * s0 + c[1] * s1 + c[2] * s2;
+    const Vec3 &e = p;
+    if (!(e.squared_norm() < sqr(offset + ghat))) return 0u;
+    const Vec3 normal = e.normalized();
+    const float gap_squared = sqr(e.norm() - offset);
+    Mat9 lh = local;
+    for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k) lh(3 * i + k, 3 * i + k) += mass[i] / gap_squared;
+    Vec9 ne;
+    for (int j = 0; j < 9; ++j) ne[j] = c[j / 3] * normal[j % 3];
+    const float stiff_k = (lh * ne).dot(ne) / ne.squared_norm();
+    const Vec3 proj_x = (offset + ghat) * normal;
+    Vec3 f = stiff_k * push::gradient(p - proj_x, normal, ghat);
+    Mat3 H = stiff_k * push::hessian(p - proj_x, normal, ghat);
+    Friction fr(f, p - q, normal, mu, friction_eps);
+    f += fr.gradient();
+    H += fr.hessian();
+    for (int i = 0; i < 3; ++i) ff.set_col(i, c[i] * f);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) HH.template set_block<3, 3>(3 * i, 3 * j, (c[i] * c[j]) * H);
+    return 1u;
+}
+
+// A free edge (p0, p1; start of step b0, b1) against the static edge (q0, q1)
+// (contact.cu:1059-1152): local is the edge's 6x6 elastic block. Writes the
+// 2 force columns and the 6x6 Hessian over the edge's vertices.
+PPF_HD unsigned mesh_edge_edge(const Vec3 &p0, const Vec3 &p1, const Vec3 &b0, const Vec3 &b1,
+                               const Vec3 &q0, const Vec3 &q1, float m0, float m1,
+                               const Mat6 &local, float offset, float ghat, float mu,
+                               float friction_eps, Mat<3, 2> &ff, Mat6 &HH) {
+    const Vec4 c = dist::edge_edge_coeff(p0, p1, q0, q1);
+    const Vec3 x = c[0] * p0 + c[1] * p1;
+    const Vec3 y = c[2] * q0 + c[3] * q1;
+    const Vec3 z = c[0] * b0 + c[1] * b1;
+    const Vec3 e = x - y;
+    if (!(e.squared_norm() < sqr(offset + ghat))) return 0u;
+    const Vec3 normal = e.normalized();
+    const Vec3 proj_x = (offset + ghat) * normal;
+    Vec6 ne;
+    for (int j = 0; j < 6; ++j) ne[j] = c[j / 3] * normal[j % 3];
+    const float gap_squared = sqr(e.norm() - offset);
+    Mat6 lh = local;
+    for (int k = 0; k < 3; ++k) {
+        lh(k, k) += m0 / gap_squared;
+        lh(3 + k, 3 + k) += m1 / gap_squared;
+    }
+    const float stiff_k = (lh * ne).dot(ne) / ne.squared_norm();
+    Vec3 f = stiff_k * push::gradient(e - proj_x, normal, ghat);
+    Mat3 H = stiff_k * push::hessian(e - proj_x, normal, ghat);
+    Friction fr(f, x - z, normal, mu, friction_eps);
+    f += fr.gradient();
+    H += fr.hessian();
+    for (int i = 0; i < 2; ++i) ff.set_col(i, c[i] * f);
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) HH.template set_block<3, 3>(3 * i, 3 * j, (c[i] * c[j]) * H);
+    return 1u;
+}
+
 } // namespace contact
 } // namespace ppf

@@ -64,11 +64,13 @@ def _rot_y(v, angle):
 
 
 def stacked_sheets(side: int = 128, sheets: int = 8, seed: int = 0, dt: float = 0.01,
-                   cube: float = 0.6, gap: float = 0.02):
+                   cube: float = 0.6, gap: float = 0.02, collider: str = "mesh"):
     """`sheets` cloth sheets of side x side vertices (1 m), each rotated by a
     seeded uniform angle about the vertical, shifted by seeded uniform
     horizontal offsets in +-0.1 m, stacked `gap` apart above a fixed cube of
-    side `cube` whose top face is at y = cube."""
+    side `cube` whose top face is at y = cube. The cube is a static collision
+    mesh (`collider="mesh"`, the reference's representation) or a fully
+    pinned shell (`collider="pinned"`)."""
     rng = np.random.default_rng(seed)
     sc = Scene()
     mat = cloth_material()
@@ -80,8 +82,11 @@ def stacked_sheets(side: int = 128, sheets: int = 8, seed: int = 0, dt: float = 
         v[:, 1] = cube + gap * (k + 1)
         sc.add_shell(v.astype(np.float32), f, mat)
     cv, cf = meshes.box(cube, center=(0.0, 0.5 * cube, 0.0))
-    base = sc.add_shell(cv, cf, mat)
-    sc.pin(np.arange(base, base + cv.shape[0]))
+    if collider == "mesh":
+        sc.add_collision_mesh(cv, cf, contact_gap=mat.contact_gap, friction=mat.friction)
+    else:
+        base = sc.add_shell(cv, cf, mat)
+        sc.pin(np.arange(base, base + cv.shape[0]))
     return sc.build(_param(dt)), None
 
 

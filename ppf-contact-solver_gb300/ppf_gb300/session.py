@@ -43,6 +43,8 @@ def _declare(lib):
     lib.ppf_scene_add_sphere.argtypes = [P, _f32, C.c_float, C.c_float, C.c_float,
                                          C.c_int, C.c_int]
     lib.ppf_scene_add_floor.argtypes = [P, _f32, _f32, C.c_float, C.c_float]
+    lib.ppf_scene_add_collision_mesh.argtypes = [P, _f32, C.c_uint, _u32, C.c_uint, C.c_float,
+                                                 C.c_float, C.c_float]
     lib.ppf_scene_build.restype = C.c_int
     lib.ppf_scene_build.argtypes = [P, C.POINTER(abi.ParamSet)]
     lib.ppf_scene_dataset.restype = P
@@ -128,6 +130,7 @@ class Scene:
         self.n_pins = 0
         self.n_spheres = 0
         self.n_floors = 0
+        self.n_collision_vertices = 0
         self.built = False
 
     def __del__(self):
@@ -169,6 +172,16 @@ class Scene:
                                      np.ascontiguousarray(up, np.float32), contact_gap,
                                      friction)
         self.n_floors += 1
+
+    def add_collision_mesh(self, vertices, faces, contact_gap=1e-3, contact_offset=0.0,
+                           friction=0.0):
+        """A static triangle mesh that the cloth collides with but that has no
+        degrees of freedom (the reference's Constraint::mesh)."""
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1)
+        f = np.ascontiguousarray(faces, np.uint32).reshape(-1)
+        self.lib.ppf_scene_add_collision_mesh(self.h, v, v.size // 3, f, f.size // 3,
+                                              contact_gap, contact_offset, friction)
+        self.n_collision_vertices += v.size // 3
 
     @property
     def vertex_count(self) -> int:

@@ -48,6 +48,27 @@ def two_sheets(side: int = 12, gap: float = 6e-4, seed: int = 3):
     return sc.build(scenes._param(0.01)), None
 
 
+def cloth_on_box(side: int = 12, gap: float = 6e-4):
+    """A sheet resting inside the contact gap of a static collision box's top
+    face, rotated about the vertical and overhanging one top corner, so the
+    first Newton system holds every collision-mesh contact: cloth vertices
+    against the top face, the box corner against cloth faces and the box's top
+    edges against cloth edges."""
+    mat = scenes.cloth_material()
+    sc = Scene()
+    v, f = meshes.grid(side, side, 0.3, 0.3)
+    v = v.astype(np.float64)
+    c, s = math.cos(0.31), math.sin(0.31)
+    x, z = v[:, 0].copy(), v[:, 2].copy()
+    v[:, 0] = c * x + s * z + 0.04
+    v[:, 2] = -s * x + c * z + 0.05
+    v[:, 1] = 0.2 + gap
+    sc.add_shell(v.astype(np.float32), f, mat)
+    bv, bf = meshes.box(0.2, center=(0.0, 0.1, 0.0))
+    sc.add_collision_mesh(bv, bf, contact_gap=1e-3, friction=0.5)
+    return sc.build(scenes._param(0.01)), None
+
+
 def sheet_on_sphere(side: int = 20):
     """cloth_sphere at a reduced size, lowered to just above the sphere."""
     sc, mot = scenes.cloth_sphere(side)

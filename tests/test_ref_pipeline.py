@@ -124,3 +124,34 @@ def test_oracle_matches_frozen_reference(scene):
     _check_line_searches(o, curr, dx, ref_of)
     for name, x in rpc.intersection_cases(curr).items():
         assert o.intersection_free(x) == bool(g[f"isect_{name}"]), name
+
+
+def test_collision_mesh_matches_reference(oracle_lib, product_lib, ref_pipe):
+    """A sheet inside the contact gap of a static collision box: the first
+    Newton systems of 4 steps (cloth vertices against the box's faces, the
+    box's corner against cloth faces) and the line searches of the sheet
+    pushed into the box, against the reference's own collision-mesh code."""
+    from oracle.binding import OracleSession
+
+    sc, _ = step_scenes.cloth_on_box()
+    o = OracleSession(sc)
+    assert ref_pipe.refpipe_init(sc.dataset, C.byref(o.param))
+    for _ in range(4):
+        curr, prev, prm, target, dt, ok, ob, of = rpc.oracle_first_system(o)
+        rk, rb, rf, count = rpc.reference_first_system(ref_pipe, curr, prev, prm, target, dt)
+        rpc.compare_systems(o.n, (rk, rb, rf), (ok, ob, of))
+        assert count > 40
+        assert o.step().success()
+    x0 = o.positions()[0].reshape(-1).copy()
+    ref_pipe.refpipe_state(x0, o.positions()[1].reshape(-1).copy(),
+                           C.byref(rpc.oracle_param(o)))
+    for dy in (-3e-3, -3e-2):
+        x1 = x0.reshape(-1, 3).copy()
+        x1[:, 1] += dy
+        x1 = x1.reshape(-1).astype(np.float32)
+        pa, oa, pb, ob2 = C.c_uint(), C.c_int(), C.c_uint(), C.c_int()
+        t_ref = ref_pipe.refpipe_line_search(x0, x1, C.byref(pa), C.byref(oa))
+        t_orc = o.lib.oracle_line_search_at(x0, x1, C.byref(pb), C.byref(ob2))
+        assert np.float32(t_ref) == np.float32(t_orc) and t_orc < 1.0, (dy, t_ref, t_orc)
+        assert (pa.value, oa.value) == (pb.value, ob2.value)
+    assert ref_pipe.refpipe_check_intersection(x0) and o.intersection_free(x0)
