@@ -342,8 +342,8 @@ __device__ __forceinline__ void overflow_row(const OverflowRows &O, const float 
 
 constexpr unsigned kNoTask = 0xFFFFFFFFu;
 // Share of the product work (in sixteenths of its cost) split statically
-// among the blocks; the rest, the last tasks in order (contact rows and
-// overflow rows), goes to whichever warps finish first.
+// among the blocks; the rest, the last tasks in order (fixed half slices,
+// short and even), goes to whichever warps finish first.
 constexpr unsigned kStaticSixteenths = 12;
 
 // The product tasks of one phase: first the block's static range, handed to
@@ -403,12 +403,15 @@ __device__ __forceinline__ void product_task(const PcgArgs &g, const float *cons
                                              unsigned task, unsigned lane, const G &gather,
                                              E &&epilogue) {
     const PcgOperator &A = g.A;
-    const unsigned t1 = 2 * A.fixed.n_slices, t2 = t1 + 2 * A.contact.sell.n_slices;
+    // task order: overflow rows, contact half slices, fixed half slices (the
+    // long and uneven items first, so the common pool at the end of the
+    // order holds short, even ones)
+    const unsigned t1 = A.ovf.count, t2 = t1 + 2 * A.contact.sell.n_slices;
     const unsigned par = lane >> 4;
     Vec3 acc = Vec3::zero(), ab = Vec3::zero();
-    if (task < t2) {
-        const bool fixed = task < t1;
-        const unsigned u = fixed ? task : task - t1;
+    if (task >= t1) {
+        const bool fixed = task >= t2;
+        const unsigned u = fixed ? task - t2 : task - t1;
         const unsigned sl = u >> 1, r = (u & 1u) * 16u + (lane & 15u);
         const unsigned q = sl * kSliceRows + r;
         SellMatrix M = fixed ? A.fixed : A.contact.sell;
@@ -428,7 +431,7 @@ __device__ __forceinline__ void product_task(const PcgArgs &g, const float *cons
             }
         }
     } else {
-        const unsigned k = task - t2;
+        const unsigned k = task;
         overflow_row<MASK>(A.ovf, vals[2], k, lane, gather, acc, ab);
         if (lane == 0u) epilogue(__ldg(A.ovf.row + k), 2u, k, acc, ab);
     }
@@ -1118,17 +1121,17 @@ __global__ void k_task_cost(unsigned n_slices, const unsigned *fixed_off, unsign
                             const unsigned *contact_off, unsigned n_ovf,
                             const uint2 *ovf_range, unsigned *cost) {
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned t1 = 2 * n_slices, t2 = t1 + 2 * c_slices;
-    if (t >= t2 + n_ovf) return;
+    const unsigned t1 = n_ovf, t2 = t1 + 2 * c_slices;
+    if (t >= t2 + 2 * n_slices) return;
     unsigned c;
     if (t < t1) {
-        unsigned sl = t >> 1;
-        c = (fixed_off[sl + 1] - fixed_off[sl] + 1) / 2;
+        c = (ovf_range[t].y + 31) / 32;
     } else if (t < t2) {
         unsigned sl = (t - t1) >> 1;
         c = (contact_off[sl + 1] - contact_off[sl] + 1) / 2;
     } else {
-        c = (ovf_range[t - t2].y + 31) / 32;
+        unsigned sl = (t - t2) >> 1;
+        c = (fixed_off[sl + 1] - fixed_off[sl] + 1) / 2;
     }
     cost[t] = c + 2u;
 }
