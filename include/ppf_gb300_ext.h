@@ -125,6 +125,53 @@ void ppf_step_stats(PpfStepStats *out);
 #define PPF_PRECOND_FIRST_ORDER 1
 #define PPF_PRECOND_LEARNED 2
 int ppf_set_preconditioner(int kind, float param);
+/* ---- learned preconditioner -------------------------------------------------
+ * The reference has no learned preconditioner; these entry points have no
+ * counterpart in it. A message-passing network (hidden width 32, bf16 weights,
+ * fp32 accumulation) over the Newton system's own sparsity emits the factor G
+ * of PPF_PRECOND_LEARNED: in the block-Jacobi-normalised operator
+ * Â = C^-1 A C^-T (A(i,i) = C(i) C(i)^T), G(i,i) = d_i C(i)^-1 and
+ * G(hi,lo) = -alpha_e Â(hi,lo) C(lo)^-1 per matrix edge. The weights are one
+ * flat bf16 blob of PPF_LEARNED_WEIGHTS values (row-major [out][in] layers:
+ * W0 32x16, W1..W3 32x80, Wh 80x48, Wf 32x16, wo 48).
+ *
+ * Loads the weights (host memory, bf16 bit patterns). Returns 0, or -1 when
+ * count != PPF_LEARNED_WEIGHTS. */
+#define PPF_LEARNED_WEIGHTS 12592
+int ppf_set_learned_weights(const unsigned short *bf16, unsigned count);
+
+/* Training on the device. A sample is one Newton system as the solver dumps
+ * it (ppf_debug_system after ppf_debug_newton_system): the fixed pattern's
+ * upper CSR (n + 1 offsets, columns, 9 column-major floats per block, the
+ * diagonal blocks included), the contact blocks' upper CSR (offsets may be
+ * NULL for none), the Dirichlet mask and the vertex masses
+ * (ppf_debug_vertex_info). It is copied to the device and kept. Returns the
+ * sample's index, or -1 for an invalid system. */
+int ppf_learned_add_sample(unsigned n, const unsigned *f_off, const unsigned *f_col,
+                           const float *f_val, const unsigned *c_off,
+                           const unsigned *c_col, const float *c_val,
+                           const unsigned *dof_mask, const float *mass);
+void ppf_learned_clear_samples(void);
+/* n, edges (upper entries of both parts: the length of h_alpha below) and
+ * free vertices of a sample; -1 for an unknown index. */
+int ppf_learned_sample_info(int sample, unsigned *n, unsigned *edges,
+                            unsigned *n_free);
+/* The network on a sample with device weights (16-byte aligned): alpha per
+ * upper entry (fixed entries first, then contact ones; 0 where the entry is
+ * diagonal or touches a Dirichlet vertex) and the head output q per vertex
+ * (d = exp(clamp(q, -4, 4))), into host arrays (either may be NULL). */
+int ppf_learned_forward(int sample, const void *d_weights, float *h_alpha,
+                        float *h_q);
+/* Kaporin's condition number of M = Ĝ Â Ĝ^T as the training loss,
+ *   L = ln(tr(M) / N) - (1/N) ln det(Ĝ)^2,  N = 3 (free vertices),
+ * with tr(M) estimated by n_probes probe vectors (d_probes: n_probes x n x 3
+ * floats, +-1, on the device), and its gradient with respect to the weights
+ * (d_grad: PPF_LEARNED_WEIGHTS floats on the device, overwritten). Runs on
+ * `stream` and waits for it; writes the loss to *h_loss. Returns 0 or -1. */
+int ppf_learned_loss_grad(int sample, const void *d_weights, const float *d_probes,
+                          unsigned n_probes, float *d_grad, float *h_loss,
+                          void *stream);
+
 /* Reported by PpfStepStats.precond_kind when the scene's ParamSet asks for the
  * reference's aggregate additive-Schwarz preconditioner (precond == 1,
  * schwarz/schwarz.hpp:38-86). */
@@ -160,6 +207,11 @@ void ppf_debug_system_sizes(unsigned *sizes);
  * columns, values), the per-vertex diagonal (9n), the right-hand side (3n)
  * and the pair lists (pf: 2 u32, pe / pp: 3 u32 with the multiplicity and the
  * friction flag in bit 31, ee: 2 u32 per pair). Any pointer may be NULL. */
+/* The vertex masses (n floats) and Dirichlet mask (n u32, nonzero = pinned)
+ * of the initialized scene, and the diagonal blocks G(i,i) (9n floats,
+ * column-major) of the last factor a factored preconditioner built. */
+void ppf_debug_vertex_info(float *mass, unsigned *dof_mask);
+void ppf_debug_factor_diag(float *out);
 void ppf_debug_system(unsigned *f_off, unsigned *f_col, float *f_val,
                       unsigned *d_off, unsigned *d_col, float *d_val,
                       float *diag, float *force, unsigned *pf, unsigned *pe,

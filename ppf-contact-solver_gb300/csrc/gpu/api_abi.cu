@@ -3,6 +3,7 @@
 // stage-inspection extensions of include/ppf_gb300_ext.h.
 #include "../../../include/ppf_gb300_ext.h"
 #include "fatal.cuh"
+#include "learned.cuh"
 #include "schwarz.cuh"
 #include "solver.cuh"
 
@@ -274,6 +275,86 @@ void ppf_debug_system(unsigned *f_off, unsigned *f_col, float *f_val, unsigned *
     cp(pe, g_dbg.pe);
     cp(pp, g_dbg.pp);
     cp(ee, g_dbg.ee);
+}
+
+void ppf_debug_vertex_info(float *mass, unsigned *dof_mask) {
+    try {
+        std::vector<float> m;
+        std::vector<unsigned> d;
+        solver_instance().debug_vertex_info(m, d);
+        if (mass) std::memcpy(mass, m.data(), m.size() * sizeof(float));
+        if (dof_mask) std::memcpy(dof_mask, d.data(), d.size() * sizeof(unsigned));
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+void ppf_debug_factor_diag(float *out) {
+    try {
+        std::vector<float> d;
+        solver_instance().debug_factor_diag(d);
+        std::memcpy(out, d.data(), d.size() * sizeof(float));
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+int ppf_set_learned_weights(const unsigned short *bf16, unsigned count) {
+    try {
+        return solver_instance().set_learned_weights(bf16, count) ? 0 : -1;
+    } catch (const FatalError &e) {
+        fatal(e);
+        return -1;
+    }
+}
+
+int ppf_learned_add_sample(unsigned n, const unsigned *f_off, const unsigned *f_col,
+                           const float *f_val, const unsigned *c_off, const unsigned *c_col,
+                           const float *c_val, const unsigned *dof_mask, const float *mass) {
+    try {
+        return ppf::gpu::learned_add_sample(n, f_off, f_col, f_val, c_off, c_col, c_val,
+                                            dof_mask, mass);
+    } catch (const FatalError &e) {
+        fatal(e);
+        return -1;
+    }
+}
+
+void ppf_learned_clear_samples(void) {
+    try {
+        ppf::gpu::learned_clear_samples();
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+int ppf_learned_sample_info(int sample, unsigned *n, unsigned *edges, unsigned *n_free) {
+    return ppf::gpu::learned_sample_info(sample, n, edges, n_free);
+}
+
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+int ppf_learned_forward(int sample, const void *d_weights, float *h_alpha, float *h_q) {
+    if (!aligned16(d_weights)) return -1;
+    try {
+        return ppf::gpu::learned_forward(sample, (const ppf::gpu::bf16_t *)d_weights, h_alpha,
+                                         h_q);
+    } catch (const FatalError &e) {
+        fatal(e);
+        return -1;
+    }
+}
+
+int ppf_learned_loss_grad(int sample, const void *d_weights, const float *d_probes,
+                          unsigned n_probes, float *d_grad, float *h_loss, void *stream) {
+    if (!aligned16(d_weights)) return -1;
+    try {
+        return ppf::gpu::learned_loss_grad(sample, (const ppf::gpu::bf16_t *)d_weights, d_probes,
+                                           n_probes, d_grad, h_loss, (cudaStream_t)stream);
+    } catch (const FatalError &e) {
+        fatal(e);
+        return -1;
+    }
 }
 
 } // extern "C"

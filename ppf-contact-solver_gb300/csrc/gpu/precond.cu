@@ -68,6 +68,19 @@ struct FirstOrderHead {
     __device__ __forceinline__ Mat3 diag(unsigned) const { return Mat3::identity(); }
 };
 
+// Ĝ emitted by the learned network (learned.cuh): the edge head evaluated on
+// the slot's own Â(hi, lo), the vertex scale d_i from the head's output Y.
+struct LearnedHead {
+    const float *Y;
+    const bf16_t *w;
+    __device__ __forceinline__ Mat3 edge(unsigned hi, unsigned lo, const Mat3 &ah) const {
+        return (-learned_alpha_of(learned_edge_o(Y, w, hi, lo, ah))) * ah;
+    }
+    __device__ __forceinline__ Mat3 diag(unsigned i) const {
+        return learned_diag_scale(Y, i) * Mat3::identity();
+    }
+};
+
 // The factor value of one slot of row a holding the operator block B =
 // A(a, b): G(a, b) for b < a, G(b, a)^T for b > a, zero on the diagonal, for
 // padding and for Dirichlet vertices.
@@ -187,6 +200,11 @@ void reserve_factor(const PcgOperator &A, unsigned fixed_slots, unsigned contact
 void launch_factor_first_order(const PcgOperator &A, const unsigned *dof_mask, float alpha,
                                FactorBuffers &F, cudaStream_t q) {
     launch_factor(A, dof_mask, FirstOrderHead{alpha}, F, q);
+}
+
+void launch_factor_learned(const PcgOperator &A, const unsigned *dof_mask, const float *Y,
+                           const bf16_t *w, FactorBuffers &F, cudaStream_t q) {
+    launch_factor(A, dof_mask, LearnedHead{Y, w}, F, q);
 }
 
 } // namespace gpu

@@ -13,6 +13,7 @@
 // blocks are exact transposes), so y = G r and z = G^T y use the same G.
 #pragma once
 
+#include "learned.cuh"
 #include "pcg.cuh"
 #include "scene.cuh"
 
@@ -38,6 +39,11 @@ void launch_chol_inv(unsigned n, const float *upper_val, const unsigned *diag_sl
 // cloth systems. Sizes the factor's arrays to the operator.
 void launch_factor_first_order(const PcgOperator &A, const unsigned *dof_mask, float alpha,
                                FactorBuffers &F, cudaStream_t q);
+
+// The learned factor: Ĝ from the network's head output Y (n x 80) and its
+// bf16 weights w (learned.cuh), on the same slots as the first-order one.
+void launch_factor_learned(const PcgOperator &A, const unsigned *dof_mask, const float *Y,
+                           const bf16_t *w, FactorBuffers &F, cudaStream_t q);
 
 // Sizes F's value arrays to A's (fixed slots, contact slots, overflow
 // entries, vertices).

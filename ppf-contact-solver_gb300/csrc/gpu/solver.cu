@@ -348,7 +348,32 @@ void Solver::build_factor() {
                    factor_);
     launch_chol_inv(n_, fixed_val_.data(), fixed_diag_.data(), factor_.cinv.data(),
                     &st_.data()->status, q_);
-    launch_factor_first_order(A, dof_mask_.data(), precond_param_, factor_, q_);
+    if (precond_kind_ == 2) {
+        LearnedGraph g;
+        g.n = n_;
+        g.fixed = LearnedPart{fixed_off_.data(), fixed_col_.data(), fixed_val_.data(),
+                              fixed_tr_off_.data(), fixed_tr_.data(), nnz_fixed_};
+        // the contact part's edge numbering is only used by the trainer
+        g.contact = LearnedPart{dyn_.off, dyn_.col, dyn_.val, dyn_.tr_off, dyn_.tr, 0u};
+        g.diag_slot = fixed_diag_.data();
+        g.dof_mask = dof_mask_.data();
+        g.mass = mass_.data();
+        g.cinv = factor_.cinv.data();
+        learned_forward_nodes(g, learned_w_.data(), learned_nodes_, q_);
+        launch_factor_learned(A, dof_mask_.data(), learned_nodes_.Y.data(), learned_w_.data(),
+                              factor_, q_);
+    } else {
+        launch_factor_first_order(A, dof_mask_.data(), precond_param_, factor_, q_);
+    }
+}
+
+bool Solver::set_learned_weights(const unsigned short *w, unsigned count) {
+    if (!w || count != learned::kWeights) return false;
+    learned_w_.reserve(count);
+    PPF_CUDA(cudaMemcpy(learned_w_.data(), w, count * sizeof(unsigned short),
+                        cudaMemcpyHostToDevice));
+    learned_ready_ = true;
+    return true;
 }
 
 PieceBuffers Solver::pieces() {
@@ -368,6 +393,9 @@ void Solver::upload_props() {
     for (unsigned i = 0; i < n_; ++i)
         mask[i] = (h_vprop_[i].fix_index > 0 && h_vprop_[i].pdrd_body_index == 0) ? 1u : 0u;
     upload(dof_mask_, mask);
+    std::vector<float> mass(n_);
+    for (unsigned i = 0; i < n_; ++i) mass[i] = h_vprop_[i].mass;
+    upload(mass_, mass);
 }
 
 bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
@@ -1030,6 +1058,23 @@ void Solver::debug_matrix(std::vector<unsigned> &f_off, std::vector<unsigned> &f
     PPF_CUDA(cudaMemcpy(diag.data(), diag_.data(), diag.size() * 4, cudaMemcpyDeviceToHost));
     force.resize(3 * (size_t)n_);
     PPF_CUDA(cudaMemcpy(force.data(), force_.data(), force.size() * 4, cudaMemcpyDeviceToHost));
+}
+
+void Solver::debug_vertex_info(std::vector<float> &mass, std::vector<unsigned> &dof) {
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    mass.resize(n_);
+    dof.resize(n_);
+    PPF_CUDA(cudaMemcpy(mass.data(), mass_.data(), n_ * sizeof(float), cudaMemcpyDeviceToHost));
+    PPF_CUDA(cudaMemcpy(dof.data(), dof_mask_.data(), n_ * sizeof(unsigned),
+                        cudaMemcpyDeviceToHost));
+}
+
+void Solver::debug_factor_diag(std::vector<float> &diag) {
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    diag.assign(9 * (size_t)n_, 0.0f);
+    if (factor_.diag.cap >= diag.size())
+        PPF_CUDA(cudaMemcpy(diag.data(), factor_.diag.data(), diag.size() * sizeof(float),
+                            cudaMemcpyDeviceToHost));
 }
 
 void Solver::debug_pairs(std::vector<unsigned> &pf, std::vector<unsigned> &pe,

@@ -56,6 +56,9 @@ class Solver {
     unsigned vertices() const { return n_; }
     // PPF_PRECOND_* of ppf_gb300_ext.h; false for an unknown kind
     bool set_preconditioner(int kind, float param);
+    // bf16 weight blob of the learned preconditioner (learned.cuh); false
+    // when count is not the network's size
+    bool set_learned_weights(const unsigned short *w, unsigned count);
     // the kind of the last solve: PPF_PRECOND_* (3: aggregate Schwarz)
     int preconditioner() const { return schwarz_active_ ? 3 : precond_kind_; }
     // debug views (host copies) for stage parity checks
@@ -63,6 +66,9 @@ class Solver {
                       std::vector<float> &f_val, std::vector<unsigned> &d_off,
                       std::vector<unsigned> &d_col, std::vector<float> &d_val,
                       std::vector<float> &diag, std::vector<float> &force);
+    // per-vertex mass and Dirichlet mask; G(i, i) of the last factor built
+    void debug_vertex_info(std::vector<float> &mass, std::vector<unsigned> &dof);
+    void debug_factor_diag(std::vector<float> &diag);
     void debug_pairs(std::vector<unsigned> &pf, std::vector<unsigned> &pe,
                      std::vector<unsigned> &pp, std::vector<unsigned> &ee);
     // one assembly + solve at the current positions, without line search
@@ -139,6 +145,9 @@ class Solver {
     bool learned_ready_ = false; // network weights loaded
     bool force_factor_ = false;  // the debug solve uses the factor directly
     FactorBuffers factor_;
+    DevBuf<bf16_t> learned_w_;
+    LearnedNodes learned_nodes_;
+    DevBuf<float> mass_;
     // static collision mesh
     unsigned ncv_ = 0, ncf_ = 0, nce_ = 0;
     DevBuf<float> cm_x_, cm_margin_f_, cm_margin_e_;

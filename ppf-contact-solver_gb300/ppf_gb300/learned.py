@@ -1,0 +1,310 @@
+"""The learned PCG preconditioner: Newton-system capture, training and weights.
+
+The network (csrc/gpu/learned.cuh) emits the factor G of
+P = G^T G + eps D^{-1} on the Newton system's own sparsity. Its forward and
+backward passes are the library's own kernels, reached through
+ppf_learned_loss_grad; PyTorch only holds the device buffers and runs Adam on
+the fp32 master copy of the weights, whose bf16 rounding is what the kernels
+read. Training data are the Newton systems the solver itself assembles
+(ppf_debug_newton_system), and the loss is Kaporin's condition number of
+Ĝ Â Ĝ^T, estimated with random +-1 probes.
+
+The reference has no learned preconditioner: its PCG uses block-Jacobi
+(crates/ppf-cts-solver/src/cpp/solver/solver.cu:357-400), which stays the
+fallback of every learned solve.
+
+Usage (on a GPU):
+    python -m ppf_gb300.learned train --out weights.npz
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import abi, scenes
+from ._lib import f32p, f32p_opt, product, u32p, u32p_opt
+from .session import Session
+
+N_WEIGHTS = 12592
+OFF_W0, OFF_W1, OFF_WH, OFF_WF, OFF_WO = 0, 512, 8192, 12032, 12544
+WEIGHTS_FILE = Path(__file__).resolve().parent / "weights" / "learned_precond.npz"
+
+_declared = set()
+
+
+def _declare(lib):
+    if id(lib) in _declared:
+        return
+    P = C.c_void_p
+    lib.ppf_set_learned_weights.restype = C.c_int
+    lib.ppf_set_learned_weights.argtypes = [np.ctypeslib.ndpointer(np.uint16, flags="C"), C.c_uint]
+    lib.ppf_learned_add_sample.restype = C.c_int
+    lib.ppf_learned_add_sample.argtypes = [C.c_uint, u32p, u32p, f32p, u32p_opt, u32p_opt,
+                                           f32p_opt, u32p, f32p]
+    lib.ppf_learned_clear_samples.restype = None
+    lib.ppf_learned_clear_samples.argtypes = []
+    lib.ppf_learned_sample_info.restype = C.c_int
+    lib.ppf_learned_sample_info.argtypes = [C.c_int, C.POINTER(C.c_uint), C.POINTER(C.c_uint),
+                                            C.POINTER(C.c_uint)]
+    lib.ppf_learned_forward.restype = C.c_int
+    lib.ppf_learned_forward.argtypes = [C.c_int, P, f32p_opt, f32p_opt]
+    lib.ppf_learned_loss_grad.restype = C.c_int
+    lib.ppf_learned_loss_grad.argtypes = [C.c_int, P, P, C.c_uint, P, C.POINTER(C.c_float), P]
+    lib.ppf_debug_vertex_info.restype = None
+    lib.ppf_debug_vertex_info.argtypes = [f32p_opt, u32p_opt]
+    lib.ppf_debug_factor_diag.restype = None
+    lib.ppf_debug_factor_diag.argtypes = [f32p]
+    lib.ppf_debug_system.restype = None
+    lib.ppf_debug_system.argtypes = [u32p_opt, u32p_opt, f32p_opt, u32p_opt, u32p_opt, f32p_opt,
+                                     f32p_opt, f32p_opt, u32p_opt, u32p_opt, u32p_opt, u32p_opt]
+    lib.ppf_debug_system_sizes.argtypes = [u32p]
+    _declared.add(id(lib))
+
+
+def lib():
+    L = product()
+    _declare(L)
+    return L
+
+
+# ---- weights ----------------------------------------------------------------------------
+
+
+def init_weights(seed: int = 0) -> np.ndarray:
+    """Initial fp32 weights: uniform +-1/sqrt(fan in) per layer over the used
+    inputs, a head scaled by 0.1, and the edge output biased so that alpha
+    starts at 1/2 (the first-order factor) and d at 1."""
+    rng = np.random.default_rng(seed)
+    w = np.zeros(N_WEIGHTS, np.float32)
+
+    def fill(off, rows, cols, used_rows, used_cols, scale=1.0):
+        m = w[off:off + rows * cols].reshape(rows, cols)
+        m[:used_rows, :used_cols] = scale * rng.uniform(-1, 1, (used_rows, used_cols)) / np.sqrt(used_cols)
+
+    fill(OFF_W0, 32, 16, 32, 16)
+    for l in range(3):
+        fill(OFF_W1 + l * 32 * 80, 32, 80, 32, 65)
+    fill(OFF_WH, 80, 48, 65, 33, 0.1)
+    fill(OFF_WF, 32, 16, 32, 11)
+    w[OFF_WO:OFF_WO + 32] = 0.1 * rng.uniform(-1, 1, 32) / np.sqrt(32)
+    w[OFF_WO + 32] = np.log(1.0 / 3.0)  # 2 sigmoid(ln 1/3) = 1/2
+    return w
+
+
+def to_bf16_bits(w) -> np.ndarray:
+    """fp32 -> bf16 bit patterns, rounding to nearest even."""
+    u = np.ascontiguousarray(w, np.float32).view(np.uint32).astype(np.uint64)
+    return (((u + 0x7FFF + ((u >> 16) & 1)) >> 16) & 0xFFFF).astype(np.uint16)
+
+
+def load_weights(path=None) -> np.ndarray:
+    """fp32 master weights of a trained network (the packaged ones by default)."""
+    with np.load(Path(path) if path else WEIGHTS_FILE) as z:
+        w = np.asarray(z["w"], np.float32)
+    if w.size != N_WEIGHTS:
+        raise ValueError(f"weights have {w.size} values, the network needs {N_WEIGHTS}")
+    return w
+
+
+def use_weights(w=None) -> None:
+    """Loads weights into the solver (the packaged trained ones by default), so
+    Session.set_preconditioner(abi.PRECOND_LEARNED) becomes available."""
+    bits = to_bf16_bits(load_weights() if w is None else w)
+    if lib().ppf_set_learned_weights(bits, bits.size) != 0:
+        raise ValueError("the library rejected the weights")
+
+
+# ---- Newton systems as samples -------------------------------------------------------------
+
+
+def capture_system(n: int) -> dict:
+    """The Newton system of the current state of the live session, assembled
+    by the solver itself: its fixed pattern, contact blocks, right-hand side,
+    masses, Dirichlet mask, and the block-Jacobi iteration count."""
+    L = lib()
+    dx = np.empty(3 * n, np.float32)
+    it, rr = C.c_uint(), C.c_float()
+    L.ppf_debug_newton_system(dx, C.byref(it), C.byref(rr))
+    sizes = np.zeros(6, np.uint32)
+    L.ppf_debug_system_sizes(sizes)
+    nf, nd = int(sizes[0]), int(sizes[1])
+    s = {
+        "f_off": np.zeros(n + 1, np.uint32), "f_col": np.zeros(max(nf, 1), np.uint32),
+        "f_val": np.zeros(9 * max(nf, 1), np.float32),
+        "d_off": np.zeros(n + 1, np.uint32), "d_col": np.zeros(max(nd, 1), np.uint32),
+        "d_val": np.zeros(9 * max(nd, 1), np.float32), "force": np.zeros(3 * n, np.float32),
+    }
+    L.ppf_debug_system(s["f_off"], s["f_col"], s["f_val"], s["d_off"], s["d_col"], s["d_val"],
+                       None, s["force"], None, None, None, None)
+    s["f_col"], s["f_val"] = s["f_col"][:nf], s["f_val"][:9 * nf]
+    s["d_col"], s["d_val"] = s["d_col"][:nd], s["d_val"][:9 * nd]
+    s["mass"] = np.zeros(n, np.float32)
+    s["dof"] = np.zeros(n, np.uint32)
+    L.ppf_debug_vertex_info(s["mass"], s["dof"])
+    s["n"] = n
+    s["bj_iters"] = int(it.value)
+    return s
+
+
+def collect(scene, steps: int, every: int = 3, start: int = 1, pin_motion=None):
+    """Steps a scene with block-Jacobi and yields the Newton system captured at
+    the start of every `every`-th step from `start` on."""
+    sess = Session(scene, pin_motion=pin_motion)
+    sess.set_preconditioner(abi.PRECOND_BLOCK_JACOBI)
+    n = scene.vertex_count
+    for k in range(steps):
+        if k >= start and (k - start) % every == 0:
+            yield capture_system(n)
+        r = sess.step()
+        if not r.success():
+            break
+
+
+def add_sample(s: dict) -> int:
+    d_off = s["d_off"] if s["d_off"][-1] else None
+    idx = lib().ppf_learned_add_sample(
+        int(s["n"]), s["f_off"], s["f_col"], s["f_val"], d_off,
+        s["d_col"] if d_off is not None else None, s["d_val"] if d_off is not None else None,
+        s["dof"], s["mass"])
+    if idx < 0:
+        raise ValueError("the library rejected the sample")
+    return idx
+
+
+# ---- training -------------------------------------------------------------------------------
+
+
+class Trainer:
+    """Adam on the fp32 master weights; loss and gradient from the library's
+    kernels on the samples kept on the device."""
+
+    def __init__(self, ids, sizes, seed: int = 0, lr: float = 3e-3, probes: int = 8, w0=None):
+        import torch
+
+        self.torch = torch
+        self.dev = torch.device("cuda")
+        self.ids = list(ids)
+        self.n = [int(x) for x in sizes]
+        self.param = torch.nn.Parameter(torch.tensor(
+            init_weights(seed) if w0 is None else np.asarray(w0, np.float32), device=self.dev))
+        self.opt = torch.optim.Adam([self.param], lr=lr)
+        self.probes = probes
+        self.gen = torch.Generator(device=self.dev)
+        self.gen.manual_seed(seed)
+
+    def loss_grad(self, k: int, w_bf16=None):
+        """(loss, fp32 gradient tensor) of sample k at the current weights."""
+        torch = self.torch
+        wb = (self.param.detach().to(torch.bfloat16) if w_bf16 is None else w_bf16).contiguous()
+        pr = torch.randint(0, 2, (self.probes, self.n[k], 3), generator=self.gen,
+                           device=self.dev, dtype=torch.int32).to(torch.float32) * 2 - 1
+        grad = torch.empty(N_WEIGHTS, dtype=torch.float32, device=self.dev)
+        loss = C.c_float()
+        rc = lib().ppf_learned_loss_grad(self.ids[k], wb.data_ptr(), pr.data_ptr(), self.probes,
+                                         grad.data_ptr(), C.byref(loss),
+                                         torch.cuda.current_stream().cuda_stream)
+        if rc != 0:
+            raise RuntimeError("ppf_learned_loss_grad failed")
+        return float(loss.value), grad
+
+    def step(self, k: int) -> float:
+        loss, grad = self.loss_grad(k)
+        self.opt.zero_grad()
+        self.param.grad = grad
+        self.opt.step()
+        return loss
+
+    def weights(self) -> np.ndarray:
+        return self.param.detach().cpu().numpy().astype(np.float32)
+
+
+def sample_loss(ids, w, probes: int = 16, seed: int = 1) -> list:
+    """Mean Kaporin loss of weights w on already added samples."""
+    import torch
+
+    dev = torch.device("cuda")
+    wb = torch.tensor(w, device=dev).to(torch.bfloat16).contiguous()
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    out = []
+    grad = torch.empty(N_WEIGHTS, dtype=torch.float32, device=dev)
+    for k in ids:
+        n = C.c_uint()
+        lib().ppf_learned_sample_info(k, C.byref(n), None, None)
+        pr = torch.randint(0, 2, (probes, n.value, 3), generator=gen, device=dev,
+                           dtype=torch.int32).to(torch.float32) * 2 - 1
+        loss = C.c_float()
+        lib().ppf_learned_loss_grad(k, wb.data_ptr(), pr.data_ptr(), probes, grad.data_ptr(),
+                                    C.byref(loss), torch.cuda.current_stream().cuda_stream)
+        out.append(float(loss.value))
+    return out
+
+
+def default_training_scenes():
+    """Stacked cloth sheets (8 sheets of 128 x 128 over a cube) under seeded
+    rotations and offsets, and a twisted tube, as (name, scene, pin_motion,
+    steps, every)."""
+    out = []
+    for seed in (1, 2, 3):
+        sc, _ = scenes.stacked_sheets(side=128, sheets=8, seed=seed)
+        out.append((f"stacked_sheets_128x8_seed{seed}", sc, None, 90, 3))
+    sc, motion = scenes.twisted_tube(around=128, along=256)
+    out.append(("twisted_tube_128x256", sc, motion, 45, 3))
+    return out
+
+
+def train_main(argv=None):
+    ap = argparse.ArgumentParser(description="train the learned PCG preconditioner on a GPU")
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--iters", type=int, default=2000)
+    ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--probes", type=int, default=8)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--log", default=None)
+    a = ap.parse_args(argv)
+    t0 = time.time()
+    lib().ppf_learned_clear_samples()
+    ids, sizes, names = [], [], []
+    for name, sc, motion, steps, every in default_training_scenes():
+        k0 = len(ids)
+        for s in collect(sc, steps, every=every, pin_motion=motion):
+            ids.append(add_sample(s))
+            sizes.append(int(s["n"]))
+            names.append(name)
+        print(f"{name}: {len(ids) - k0} systems ({time.time() - t0:.0f} s)", flush=True)
+        del sc
+    rng = np.random.default_rng(a.seed)
+    held = set(rng.choice(len(ids), size=max(1, len(ids) // 10), replace=False).tolist())
+    train = [i for i in range(len(ids)) if i not in held]
+    test_ids = [ids[i] for i in sorted(held)]
+    tr = Trainer([ids[i] for i in train], [sizes[i] for i in train], seed=a.seed, lr=a.lr,
+                 probes=a.probes)
+    before = float(np.mean(sample_loss(test_ids, tr.weights())))
+    losses = []
+    for it in range(a.iters):
+        losses.append(tr.step(int(rng.integers(len(train)))))
+        if it % 200 == 0:
+            print(f"iter {it}: loss {np.mean(losses[-200:]):.4f} ({time.time() - t0:.0f} s)",
+                  flush=True)
+    after = float(np.mean(sample_loss(test_ids, tr.weights())))
+    meta = {"systems": len(ids), "train": len(train), "held_out": len(test_ids),
+            "iters": a.iters, "lr": a.lr, "probes": a.probes,
+            "held_out_loss_init": before, "held_out_loss_trained": after,
+            "scenes": sorted(set(names)), "seconds": time.time() - t0}
+    print(json.dumps(meta), flush=True)
+    Path(a.out).parent.mkdir(parents=True, exist_ok=True)
+    np.savez(a.out, w=tr.weights(), meta=json.dumps(meta))
+    lib().ppf_learned_clear_samples()
+
+
+if __name__ == "__main__":
+    import sys
+
+    if len(sys.argv) < 2 or sys.argv[1] != "train":
+        raise SystemExit("usage: python -m ppf_gb300.learned train --out FILE [--iters N]")
+    train_main(sys.argv[2:])
