@@ -44,8 +44,13 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Newton steps/s (block-Jacobi PCG to rel. residual 1e-3)"
 UNIT = "newton_iters/s"
-WORKLOAD = ("stacked_sheets: 8 x 128x128 cloth sheets over a 0.6 m cube that is a static "
-            "collision mesh")
+WORKLOADS = {
+    "stacked_sheets": ("stacked_sheets: 8 x 128x128 cloth sheets over a 0.6 m cube that is a "
+                       "static collision mesh"),
+    "sphere_field": ("sphere_field: one 1024x1024 cloth (1,048,576 vertices) dropped over 50 "
+                     "fixed spheres of seeded radii 0.02-0.1 m"),
+}
+WORKLOAD = WORKLOADS["stacked_sheets"]
 L2_FLUSH_BYTES = 256 << 20
 CPU_SAMPLE_SECONDS = 20.0
 REF_BUDGET_SECONDS = 150.0
@@ -145,9 +150,11 @@ def aggregate(dist, device, seconds_or_ms: float, newton: int):
     return float(t.item()), int(n.item())
 
 
-def build_scene(seed: int = 0):
+def build_scene(seed: int = 0, workload: str = "stacked_sheets"):
     from ppf_gb300 import scenes
 
+    if workload == "sphere_field":
+        return scenes.sphere_field(1024, 50, seed=seed, dt=0.01)
     return scenes.stacked_sheets(128, 8, seed=seed, dt=0.01)
 
 
@@ -167,7 +174,7 @@ def run_ours(args, rank, local_rank, world):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    sc, motion = build_scene(seed=rank)
+    sc, motion = build_scene(seed=rank, workload=args.workload)
     curr0, prev0 = sc.positions()
     param0 = abi.ParamSet.from_buffer_copy(sc.param.contents)
 
@@ -261,7 +268,7 @@ def run_ours(args, rank, local_rank, world):
     achieved = pcg_bytes / (pcg_ms_total / 1e3) / 1e9 if pcg_ms_total > 0 else 0.0
     traffic = None
     tfile = ROOT / "profiles" / "pcg_stacked_sheets_traffic.json"
-    if tfile.exists() and pcg_iters_all:
+    if tfile.exists() and pcg_iters_all and args.workload == "stacked_sheets":
         # DRAM bytes per iteration from one ncu capture of a launch of this
         # workload, scaled to the mean iterations per launch of this run
         per_iter = json.loads(tfile.read_text()).get("dram_bytes_per_iteration")
@@ -284,7 +291,7 @@ def run_ours(args, rank, local_rank, world):
         "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded scene generator)",
-        "config": {"workload": WORKLOAD, "vertices": n, "dt": 0.01,
+        "config": {"workload": WORKLOADS[args.workload], "vertices": n, "dt": 0.01,
                    "time_steps": args.steps, "from": "t = 0 after a separate warm-up",
                    "l2": "256 MiB flush before every timed step",
                    "parallelism": "replicas" if world > 1 else "single"},
@@ -451,6 +458,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precond-steps", type=int, default=24,
                     help="time steps of the preconditioner comparison (0: skip)")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="stacked_sheets",
+                    help="stacked_sheets (the headline) or sphere_field (one 1M-vertex cloth)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -302,9 +302,68 @@ def train_main(argv=None):
     lib().ppf_learned_clear_samples()
 
 
+def bench_main(argv=None):
+    """Times the network on one Newton system of a stacked-sheets scene: the
+    inference pass (features, layers, edge head on every upper entry) and one
+    training step (forward, Kaporin loss, backward), with CUDA events; prints
+    one JSON line."""
+    import torch
+
+    ap = argparse.ArgumentParser(description="time the learned preconditioner's kernels")
+    ap.add_argument("--side", type=int, default=128)
+    ap.add_argument("--sheets", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=15, help="time steps before the capture")
+    ap.add_argument("--iters", type=int, default=50)
+    ap.add_argument("--probes", type=int, default=8)
+    a = ap.parse_args(argv)
+    sc, _ = scenes.stacked_sheets(side=a.side, sheets=a.sheets, seed=1)
+    s = next(iter(collect(sc, a.steps + 1, every=a.steps + 1, start=a.steps)))
+    L = lib()
+    L.ppf_learned_clear_samples()
+    k = add_sample(s)
+    n, E = C.c_uint(), C.c_uint()
+    L.ppf_learned_sample_info(k, C.byref(n), C.byref(E), None)
+    w = load_weights() if WEIGHTS_FILE.exists() else init_weights(0)
+    tr = Trainer([k], [n.value], probes=a.probes, w0=w)
+    wb = torch.tensor(w, device="cuda").to(torch.bfloat16).contiguous()
+    alpha = np.zeros(E.value, np.float32)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(a.iters):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / a.iters
+
+    fwd_ms = timed(lambda: L.ppf_learned_forward(k, wb.data_ptr(), None, None))
+    step_ms = timed(lambda: tr.loss_grad(0, wb))
+    L.ppf_learned_forward(k, wb.data_ptr(), alpha, None)
+    nn = n.value
+    # dense-layer flops per forward pass: 2 x rows x in x out
+    flops = 2 * nn * (16 * 32 + 3 * 80 * 32 + 48 * 80)
+    out = {"workload": f"stacked sheets {a.sheets} x {a.side}^2, Newton system after {a.steps} steps",
+           "vertices": nn, "upper_entries": E.value,
+           "live_edges": int((alpha != 0).sum()),
+           "contact_blocks": int(s["d_off"][-1]),
+           "inference_ms": round(fwd_ms, 4), "train_step_ms": round(step_ms, 4),
+           "probes": a.probes, "dense_layer_gflop_per_forward": round(flops / 1e9, 3),
+           "note": "inference_ms: features, the four layers and the edge head on every "
+                   "upper entry, one device synchronization per call; the solver runs the "
+                   "same kernels when it builds the learned factor"}
+    print(json.dumps(out), flush=True)
+    L.ppf_learned_clear_samples()
+
+
 if __name__ == "__main__":
     import sys
 
-    if len(sys.argv) < 2 or sys.argv[1] != "train":
-        raise SystemExit("usage: python -m ppf_gb300.learned train --out FILE [--iters N]")
-    train_main(sys.argv[2:])
+    cmds = {"train": train_main, "bench": bench_main}
+    if len(sys.argv) < 2 or sys.argv[1] not in cmds:
+        raise SystemExit("usage: python -m ppf_gb300.learned train --out FILE [--iters N]\n"
+                         "       python -m ppf_gb300.learned bench [--side N] [--iters N]")
+    cmds[sys.argv[1]](sys.argv[2:])
