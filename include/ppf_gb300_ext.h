@@ -172,6 +172,14 @@ int ppf_learned_loss_grad(int sample, const void *d_weights, const float *d_prob
                           unsigned n_probes, float *d_grad, float *h_loss,
                           void *stream);
 
+/* The network's forward layers run on the tensor cores either as tcgen05
+ * tiles (M = 128, accumulator in tensor memory; tc = 1) or as mma.sync tiles
+ * (tc = 0); tc = -1 only reads the setting. Returns the previous setting.
+ * ppf_learned_tc_status is nonzero once a tcgen05 tile gave up waiting for its
+ * accumulator (bounded wait; its outputs are then not written). */
+int ppf_learned_tensor_path(int tc);
+unsigned ppf_learned_tc_status(void);
+
 /* Reported by PpfStepStats.precond_kind when the scene's ParamSet asks for the
  * reference's aggregate additive-Schwarz preconditioner (precond == 1,
  * schwarz/schwarz.hpp:38-86). */

@@ -328,6 +328,17 @@ void ppf_learned_clear_samples(void) {
     }
 }
 
+int ppf_learned_tensor_path(int tc) { return ppf::gpu::learned_tensor_path(tc); }
+
+unsigned ppf_learned_tc_status(void) {
+    try {
+        return ppf::gpu::learned_tc_status();
+    } catch (const FatalError &e) {
+        fatal(e);
+        return ~0u;
+    }
+}
+
 int ppf_learned_sample_info(int sample, unsigned *n, unsigned *edges, unsigned *n_free) {
     return ppf::gpu::learned_sample_info(sample, n, edges, n_free);
 }

@@ -203,6 +203,152 @@ __global__ void __launch_bounds__(128) k_gemm_rows(unsigned R, const bf16_t *__r
     }
 }
 
+// ---- the same row-tile product on the 5th-generation tensor cores ----------------
+// One CTA of 4 warps per 128-row tile: both operands are staged by the CTA's
+// threads into shared memory in the no-swizzle K-major canonical layout
+// (8 rows x 16 B core matrices; A: core matrix (row group g, K chunk c) at
+// c * 2048 + g * 128 bytes, B: at c * N * 16 + g * 128), one elected thread
+// issues K / 16 tcgen05.mma (kind::f16, bf16 inputs, M = 128, fp32
+// accumulator of N columns in tensor memory) and commits them to an
+// mbarrier; each warp then reads its 32 accumulator lanes (rows) back with
+// tcgen05.ld for the epilogue. The mbarrier wait is bounded: on timeout the
+// kernel latches STATUS_TC_TIMEOUT, waits (bounded again) and frees its
+// tensor memory.
+constexpr unsigned kTcRows = 128;
+__device__ unsigned g_tc_status;
+
+__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t phase, unsigned limit) {
+    uint32_t done = 0;
+    for (unsigned it = 0; it < limit && !done; ++it)
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+    return done != 0;
+}
+
+template <int N> constexpr uint32_t tc_cols() { return N <= 32 ? 32u : N <= 64 ? 64u : 128u; }
+
+template <int K, int N>
+__global__ void __launch_bounds__(128) k_gemm_rows_tc(unsigned R, const bf16_t *__restrict__ A,
+                                                      const bf16_t *__restrict__ B, float *Cf,
+                                                      bf16_t *Cb) {
+    static_assert(K % 16 == 0 && N % 16 == 0 && N >= 16 && N <= 256, "tcgen05 tile shape");
+    constexpr uint32_t kCols = tc_cols<N>();
+    __shared__ __align__(128) uint8_t sA[kTcRows * K * 2];
+    __shared__ __align__(128) uint8_t sB[N * K * 2];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    const unsigned r0 = blockIdx.x * kTcRows;
+    (void)lane;
+    const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(&mbar);
+    if (warp == 0) {
+        const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(slot),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar_a) : "memory");
+    constexpr int KV = K / 8; // 16-byte chunks per row
+    for (int t = tid; t < N * KV; t += 128) {
+        const int n = t / KV, c = t % KV;
+        *reinterpret_cast<uint4 *>(sB + c * N * 16 + n * 16) =
+            __ldg(reinterpret_cast<const uint4 *>(B + (size_t)n * K + c * 8));
+    }
+    for (int t = tid; t < (int)kTcRows * KV; t += 128) {
+        const int r = t / KV, c = t % KV;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (r0 + r < R) v = __ldg(reinterpret_cast<const uint4 *>(A + (size_t)(r0 + r) * K + c * 8));
+        *reinterpret_cast<uint4 *>(sA + c * 2048 + r * 16) = v;
+    }
+    // generic-proxy smem writes -> visible to the tensor core's async proxy
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    if (tid == 0) {
+        const uint32_t a0 = (uint32_t)__cvta_generic_to_shared(sA);
+        const uint32_t b0 = (uint32_t)__cvta_generic_to_shared(sB);
+        const uint32_t idesc = (1u << 4)           // accumulator f32
+                               | (1u << 7)         // A bf16
+                               | (1u << 10)        // B bf16
+                               | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+#pragma unroll
+        for (int s = 0; s < K / 16; ++s) {
+            const uint64_t ad = tc_smem_desc(a0 + s * 2 * 2048, 2048, 128);
+            const uint64_t bd = tc_smem_desc(b0 + s * 2 * N * 16, N * 16, 128);
+            const uint32_t acc = s > 0 ? 1u : 0u;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                : "memory");
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                mbar_a)
+            : "memory");
+    }
+    const bool ok = __syncthreads_and(tc_wait(mbar_a, 0u, 1u << 22)) != 0;
+    if (!ok) {
+        if (tid == 0) atomicOr(&g_tc_status, 1u);
+        tc_wait(mbar_a, 0u, 1u << 22);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (ok) {
+        const unsigned row = r0 + warp * 32 + lane;
+#pragma unroll
+        for (int c = 0; c < N / 16; ++c) {
+            uint32_t v[16];
+            const uint32_t taddr = tmem + ((warp * 32u) << 16) + (uint32_t)(c * 16);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
+                "%12,%13,%14,%15}, [%16];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                  "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                  "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (row < R) {
+                if (Cb) {
+#pragma unroll
+                    for (int j = 0; j < 16; j += 2) {
+                        __nv_bfloat162 p;
+                        p.x = __float2bfloat16_rn(fmaxf(__uint_as_float(v[j]), 0.0f));
+                        p.y = __float2bfloat16_rn(fmaxf(__uint_as_float(v[j + 1]), 0.0f));
+                        *reinterpret_cast<__nv_bfloat162 *>(Cb + (size_t)row * N + c * 16 + j) = p;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; j += 4)
+                        *reinterpret_cast<float4 *>(Cf + (size_t)row * N + c * 16 + j) =
+                            make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]),
+                                        __uint_as_float(v[j + 2]), __uint_as_float(v[j + 3]));
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
+                     "r"(kCols)
+                     : "memory");
+}
+
+bool g_use_tc = false; // forward row products on tcgen05 (else mma.sync)
+
 constexpr unsigned kReduceRows = 1024; // rows per block in reduce mode
 constexpr int kChunk = 32;             // rows staged per step
 
@@ -281,6 +427,20 @@ void gemm_rows(unsigned R, const bf16_t *A, const bf16_t *B, float *Cf, bf16_t *
     PPF_LAUNCH_CHECK();
 }
 
+// The forward layers' products: tcgen05 tiles (N a multiple of 16), or the
+// mma.sync tiles when the tensor path is switched off.
+template <int K, int N>
+void gemm_fwd(unsigned R, const bf16_t *A, const bf16_t *B, float *Cf, bf16_t *Cb,
+              cudaStream_t q) {
+    if (!R) return;
+    if (g_use_tc) {
+        k_gemm_rows_tc<K, N><<<div_up(R, kTcRows), 128, 0, q>>>(R, A, B, Cf, Cb);
+        PPF_LAUNCH_CHECK();
+    } else {
+        gemm_rows<K, N>(R, A, B, Cf, Cb, q);
+    }
+}
+
 template <int M, int N>
 void gemm_reduce(unsigned R, const bf16_t *A, const bf16_t *B, float *C, cudaStream_t q) {
     if (!R) return;
@@ -306,19 +466,19 @@ void learned_forward_nodes(const LearnedGraph &g, const bf16_t *w, LearnedNodes 
     k_node_inputs<<<div_up(n, kT), kT, 0, q>>>(g, b.X0.data(), b.deg.data());
     PPF_LAUNCH_CHECK();
     bf16_t *H = b.H.data();
-    gemm_rows<kIn0, 32>(n, b.X0.data(), w + kOffW0, nullptr, H, q);
+    gemm_fwd<kIn0, 32>(n, b.X0.data(), w + kOffW0, nullptr, H, q);
     for (int l = 0; l < 3; ++l) {
         bf16_t *X = b.X.data() + (size_t)l * n * kInL;
         k_aggregate<true><<<div_up(32u * n, kT), kT, 0, q>>>(g, H + (size_t)l * n * 32,
                                                              b.deg.data(), X);
         PPF_LAUNCH_CHECK();
-        gemm_rows<kInL, 32>(n, X, w + kOffW1 + l * 32 * kInL, nullptr,
-                            H + (size_t)(l + 1) * n * 32, q);
+        gemm_fwd<kInL, 32>(n, X, w + kOffW1 + l * 32 * kInL, nullptr,
+                           H + (size_t)(l + 1) * n * 32, q);
     }
     k_aggregate<false><<<div_up(32u * n, kT), kT, 0, q>>>(g, H + (size_t)3 * n * 32,
                                                           b.deg.data(), b.Xh.data());
     PPF_LAUNCH_CHECK();
-    gemm_rows<kInH, kOutH>(n, b.Xh.data(), w + kOffWh, b.Y.data(), nullptr, q);
+    gemm_fwd<kInH, kOutH>(n, b.Xh.data(), w + kOffWh, b.Y.data(), nullptr, q);
 }
 
 // ---- training ------------------------------------------------------------------------------
@@ -751,6 +911,18 @@ void learned_clear_samples() {
         delete S;
     }
     g_samples.clear();
+}
+
+int learned_tensor_path(int tc) {
+    const int prev = g_use_tc ? 1 : 0;
+    if (tc >= 0) g_use_tc = tc != 0;
+    return prev;
+}
+
+unsigned learned_tc_status() {
+    unsigned v = 0;
+    PPF_CUDA(cudaMemcpyFromSymbol(&v, g_tc_status, sizeof(v)));
+    return v;
 }
 
 int learned_sample_info(int s, unsigned *n, unsigned *edges, unsigned *n_free) {

@@ -141,6 +141,11 @@ int learned_add_sample(unsigned n, const unsigned *f_off, const unsigned *f_col,
                        const float *f_val, const unsigned *c_off, const unsigned *c_col,
                        const float *c_val, const unsigned *dof_mask, const float *mass);
 void learned_clear_samples();
+// Selects the forward layers' tensor-core path (1: tcgen05, 0: mma.sync; -1
+// only reads it); returns the previous one.
+int learned_tensor_path(int tc);
+// Nonzero once a tcgen05 tile gave up waiting for its accumulator.
+unsigned learned_tc_status();
 int learned_sample_info(int s, unsigned *n, unsigned *edges, unsigned *n_free);
 int learned_forward(int s, const bf16_t *d_w, float *h_alpha, float *h_d);
 int learned_loss_grad(int s, const bf16_t *d_w, const float *d_probes, unsigned n_probes,

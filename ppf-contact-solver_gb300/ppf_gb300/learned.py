@@ -55,6 +55,10 @@ def _declare(lib):
     lib.ppf_learned_forward.argtypes = [C.c_int, P, f32p_opt, f32p_opt]
     lib.ppf_learned_loss_grad.restype = C.c_int
     lib.ppf_learned_loss_grad.argtypes = [C.c_int, P, P, C.c_uint, P, C.POINTER(C.c_float), P]
+    lib.ppf_learned_tensor_path.restype = C.c_int
+    lib.ppf_learned_tensor_path.argtypes = [C.c_int]
+    lib.ppf_learned_tc_status.restype = C.c_uint
+    lib.ppf_learned_tc_status.argtypes = []
     lib.ppf_debug_vertex_info.restype = None
     lib.ppf_debug_vertex_info.argtypes = [f32p_opt, u32p_opt]
     lib.ppf_debug_factor_diag.restype = None
@@ -212,8 +216,11 @@ class Trainer:
             raise RuntimeError("ppf_learned_loss_grad failed")
         return float(loss.value), grad
 
-    def step(self, k: int) -> float:
+    def step(self, k: int, lr: float = None) -> float:
         loss, grad = self.loss_grad(k)
+        if lr is not None:
+            for group in self.opt.param_groups:
+                group["lr"] = lr
         self.opt.zero_grad()
         self.param.grad = grad
         self.opt.step()
@@ -247,22 +254,64 @@ def sample_loss(ids, w, probes: int = 16, seed: int = 1) -> list:
 
 def default_training_scenes():
     """Stacked cloth sheets (8 sheets of 128 x 128 over a cube) under seeded
-    rotations and offsets, and a twisted tube, as (name, scene, pin_motion,
-    steps, every)."""
+    rotations and offsets, a twisted tube, and cloth dropped over fields of
+    spheres, as (name, scene, pin_motion, steps, every)."""
     out = []
     for seed in (1, 2, 3):
         sc, _ = scenes.stacked_sheets(side=128, sheets=8, seed=seed)
         out.append((f"stacked_sheets_128x8_seed{seed}", sc, None, 90, 3))
     sc, motion = scenes.twisted_tube(around=128, along=256)
     out.append(("twisted_tube_128x256", sc, motion, 45, 3))
+    for seed in (1, 2):
+        sc, _ = scenes.sphere_field(side=256, spheres=12, seed=seed)
+        out.append((f"sphere_field_256_seed{seed}", sc, None, 60, 3))
+    return out
+
+
+def held_out_scenes():
+    """Scenes of none of the training seeds, for comparing preconditioners."""
+    return {
+        "stacked_sheets_64x8_seed11": lambda: scenes.stacked_sheets(side=64, sheets=8, seed=11),
+        "sphere_field_256_seed7": lambda: scenes.sphere_field(side=256, spheres=12, seed=7),
+    }
+
+
+def compare(scene_fn, steps: int, weights=None) -> dict:
+    """PCG iterations, solves, block-Jacobi fallbacks and PCG ms of the same
+    steps solved with block-Jacobi, the first-order factor and the learned
+    factor (weights: fp32 master weights, the packaged ones by default)."""
+    use_weights(weights)
+    out = {}
+    for name, kind in (("block_jacobi", abi.PRECOND_BLOCK_JACOBI),
+                       ("first_order", abi.PRECOND_FIRST_ORDER),
+                       ("learned", abi.PRECOND_LEARNED)):
+        sc, motion = scene_fn()
+        sess = Session(sc, pin_motion=motion)
+        sess.set_preconditioner(kind)
+        it = solves = fb = 0
+        ms = 0.0
+        for _ in range(steps):
+            if not sess.step(fetch=False).success():
+                break
+            st = sess.stats()
+            it += st.pcg_iters_total
+            solves += st.pcg_solves
+            fb += st.fallbacks
+            ms += st.pcg_ms_total
+        sess.set_preconditioner(abi.PRECOND_BLOCK_JACOBI)
+        out[name] = {"pcg_iters": it, "solves": solves, "fallbacks": fb,
+                     "pcg_ms": round(ms, 2)}
+        del sess, sc
     return out
 
 
 def train_main(argv=None):
     ap = argparse.ArgumentParser(description="train the learned PCG preconditioner on a GPU")
     ap.add_argument("--out", required=True)
-    ap.add_argument("--iters", type=int, default=2000)
+    ap.add_argument("--iters", type=int, default=6000)
     ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--lr-final", type=float, default=1e-4,
+                    help="cosine decay of the learning rate down to this value")
     ap.add_argument("--probes", type=int, default=8)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--log", default=None)
@@ -287,13 +336,14 @@ def train_main(argv=None):
     before = float(np.mean(sample_loss(test_ids, tr.weights())))
     losses = []
     for it in range(a.iters):
-        losses.append(tr.step(int(rng.integers(len(train)))))
+        lr = a.lr_final + 0.5 * (a.lr - a.lr_final) * (1 + np.cos(np.pi * it / max(1, a.iters)))
+        losses.append(tr.step(int(rng.integers(len(train))), lr=lr))
         if it % 200 == 0:
             print(f"iter {it}: loss {np.mean(losses[-200:]):.4f} ({time.time() - t0:.0f} s)",
                   flush=True)
     after = float(np.mean(sample_loss(test_ids, tr.weights())))
     meta = {"systems": len(ids), "train": len(train), "held_out": len(test_ids),
-            "iters": a.iters, "lr": a.lr, "probes": a.probes,
+            "iters": a.iters, "lr": a.lr, "lr_final": a.lr_final, "probes": a.probes,
             "held_out_loss_init": before, "held_out_loss_trained": after,
             "scenes": sorted(set(names)), "seconds": time.time() - t0}
     print(json.dumps(meta), flush=True)
@@ -315,7 +365,11 @@ def bench_main(argv=None):
     ap.add_argument("--steps", type=int, default=15, help="time steps before the capture")
     ap.add_argument("--iters", type=int, default=50)
     ap.add_argument("--probes", type=int, default=8)
+    ap.add_argument("--tensor-path", choices=["tc", "sync"], default=None,
+                    help="forward layers as tcgen05 or mma.sync tiles (default: the library's)")
     a = ap.parse_args(argv)
+    if a.tensor_path:
+        lib().ppf_learned_tensor_path(1 if a.tensor_path == "tc" else 0)
     sc, _ = scenes.stacked_sheets(side=a.side, sheets=a.sheets, seed=1)
     s = next(iter(collect(sc, a.steps + 1, every=a.steps + 1, start=a.steps)))
     L = lib()
@@ -352,6 +406,8 @@ def bench_main(argv=None):
            "contact_blocks": int(s["d_off"][-1]),
            "inference_ms": round(fwd_ms, 4), "train_step_ms": round(step_ms, 4),
            "probes": a.probes, "dense_layer_gflop_per_forward": round(flops / 1e9, 3),
+           "tensor_path": "tcgen05" if L.ppf_learned_tensor_path(-1) else "mma.sync",
+           "tc_status": int(L.ppf_learned_tc_status()),
            "note": "inference_ms: features, the four layers and the edge head on every "
                    "upper entry, one device synchronization per call; the solver runs the "
                    "same kernels when it builds the learned factor"}
@@ -362,8 +418,19 @@ def bench_main(argv=None):
 if __name__ == "__main__":
     import sys
 
-    cmds = {"train": train_main, "bench": bench_main}
+    def eval_main(argv):
+        ap = argparse.ArgumentParser(description="compare preconditioners on held-out scenes")
+        ap.add_argument("--weights", default=None)
+        ap.add_argument("--steps", type=int, default=30)
+        a = ap.parse_args(argv)
+        w = load_weights(a.weights)
+        for name, fn in held_out_scenes().items():
+            print(json.dumps({"scene": name, "steps": a.steps, **compare(fn, a.steps, w)}),
+                  flush=True)
+
+    cmds = {"train": train_main, "bench": bench_main, "eval": eval_main}
     if len(sys.argv) < 2 or sys.argv[1] not in cmds:
         raise SystemExit("usage: python -m ppf_gb300.learned train --out FILE [--iters N]\n"
-                         "       python -m ppf_gb300.learned bench [--side N] [--iters N]")
+                         "       python -m ppf_gb300.learned bench [--side N] [--iters N]\n"
+                         "       python -m ppf_gb300.learned eval [--weights FILE]")
     cmds[sys.argv[1]](sys.argv[2:])

@@ -116,6 +116,41 @@ def test_gpu_forward_matches_oracle(product_lib, torch_cuda):
 
 
 @pytest.mark.gpu
+def test_tcgen05_layers_match_mma_sync(product_lib, torch_cuda):
+    """The forward layers as tcgen05 tiles (tensor memory accumulators) give
+    the mma.sync tiles' results: the same bf16 products summed in fp32 in
+    another order, over several 128-row tiles and a partial one."""
+    from ppf_gb300 import learned as PL
+
+    torch = torch_cuda
+    L = PL.lib()
+    L.ppf_learned_clear_samples()
+    s = learned_cases.synthetic(n=1000, seed=8)
+    g = learned_cases.graph(s)
+    k = _add(product_lib, s)
+    w = _weights(5)
+    wb = torch.tensor(w, device="cuda").to(torch.bfloat16).contiguous()
+    E = len(g.lo)
+    out = {}
+    prev = L.ppf_learned_tensor_path(-1)
+    try:
+        for tc in (0, 1):
+            L.ppf_learned_tensor_path(tc)
+            a = np.zeros(E, np.float32)
+            q = np.zeros(g.n, np.float32)
+            assert L.ppf_learned_forward(k, wb.data_ptr(), a, q) == 0
+            out[tc] = (a, q)
+    finally:
+        L.ppf_learned_tensor_path(prev)
+    assert L.ppf_learned_tc_status() == 0
+    (a0, q0), (a1, q1) = out[0], out[1]
+    assert np.abs(q1 - q0).max() <= 5e-3 * max(1.0, np.abs(q0).max()), np.abs(q1 - q0).max()
+    assert np.abs(a1 - a0).max() < 5e-3
+    f = OL.forward(g, w)
+    assert np.abs(q1 - f["q"])[g.free].max() <= 2e-2 * max(1.0, np.abs(f["q"]).max())
+
+
+@pytest.mark.gpu
 def test_gpu_gradient_matches_oracle(product_lib, torch_cuda):
     from ppf_gb300 import learned as PL
 
