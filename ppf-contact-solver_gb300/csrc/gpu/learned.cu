@@ -1,16 +1,19 @@
 // learned.cu -- the learned preconditioner's network: inference and training
 // kernels (layout and formulas in learned.cuh).
 //
-// Dense layers run on the tensor cores as bf16 x bf16 -> fp32
-// mma.sync.m16n8k16 over row tiles staged in shared memory:
-//   rows mode    C[R x N] = A[R x K] B[N x K]^T  (forward layers, input grads)
-//   reduce mode  C[M x N] += A[R x M]^T B[R x N] (weight grads, split over
-//                row ranges, one fp32 atomic add per output per block)
+// Dense layers run on the tensor cores as bf16 x bf16 -> fp32 products:
+//   rows mode    C[R x N] = A[R x K] B[N x K]^T: the forward layers as
+//                tcgen05.mma tiles (k_gemm_rows_tc), the input gradients as
+//                mma.sync.m16n8k16 tiles (k_gemm_rows)
+//   reduce mode  C[M x N] += A[R x M]^T B[R x N] (weight grads, mma.sync,
+//                split over row ranges, one fp32 atomic add per output per
+//                block)
 // Graph work (features, neighbour means, edge head, probes) is scalar fp32 in
 // a fixed order per vertex: each vertex walks its neighbours as fixed upper
 // entries, fixed transposed entries, contact upper entries, contact
 // transposed entries, skipping Dirichlet vertices, so every sum has one
 // order and the forward pass is deterministic.
+#include <algorithm>
 #include <vector>
 
 #include "fatal.cuh"
@@ -204,17 +207,20 @@ __global__ void __launch_bounds__(128) k_gemm_rows(unsigned R, const bf16_t *__r
 }
 
 // ---- the same row-tile product on the 5th-generation tensor cores ----------------
-// One CTA of 4 warps per 128-row tile: both operands are staged by the CTA's
-// threads into shared memory in the no-swizzle K-major canonical layout
-// (8 rows x 16 B core matrices; A: core matrix (row group g, K chunk c) at
-// c * 2048 + g * 128 bytes, B: at c * N * 16 + g * 128), one elected thread
+// Persistent CTAs of 4 warps walk 128-row tiles. Operands sit in shared memory
+// in the no-swizzle K-major canonical layout (8 rows x 16 B core matrices;
+// A: core matrix (row group g, K chunk c) at c * 2048 + g * 128 bytes, B: at
+// c * N * 16 + g * 128). B (the weights) is staged once per CTA; A tiles are
+// double-buffered and fetched with cp.async, so the next tile's rows stream
+// in while the current tile's epilogue runs. Per tile one elected thread
 // issues K / 16 tcgen05.mma (kind::f16, bf16 inputs, M = 128, fp32
-// accumulator of N columns in tensor memory) and commits them to an
-// mbarrier; each warp then reads its 32 accumulator lanes (rows) back with
-// tcgen05.ld for the epilogue. The mbarrier wait is bounded: on timeout the
-// kernel latches STATUS_TC_TIMEOUT, waits (bounded again) and frees its
-// tensor memory.
+// accumulator of N columns in tensor memory, allocated once per CTA) and
+// commits them to an mbarrier; each warp reads its 32 accumulator lanes
+// (rows) back with tcgen05.ld for the epilogue. The mbarrier waits are
+// bounded: on timeout the kernel latches g_tc_status, waits (bounded again),
+// frees its tensor memory and returns.
 constexpr unsigned kTcRows = 128;
+constexpr unsigned kTcCtasPerSm = 4;
 __device__ unsigned g_tc_status;
 
 __device__ __forceinline__ uint64_t tc_smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -236,20 +242,42 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t phase, unsigned 
 
 template <int N> constexpr uint32_t tc_cols() { return N <= 32 ? 32u : N <= 64 ? 64u : 128u; }
 
+// 16-byte asynchronous copy global -> shared; src_bytes 0 writes zeros.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src),
+                 "r"(src_bytes)
+                 : "memory");
+}
+
+template <int K>
+__device__ __forceinline__ void tc_fetch_tile(uint32_t sa, const bf16_t *A, unsigned R,
+                                              unsigned r0) {
+    constexpr int KV = K / 8;
+    for (int t = threadIdx.x; t < (int)kTcRows * KV; t += 128) {
+        const int r = t / KV, c = t % KV;
+        const bool in = r0 + r < R;
+        const bf16_t *src = in ? A + (size_t)(r0 + r) * K + c * 8 : A;
+        cp_async16(sa + c * 2048 + r * 16, src, in ? 16u : 0u);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
 template <int K, int N>
 __global__ void __launch_bounds__(128) k_gemm_rows_tc(unsigned R, const bf16_t *__restrict__ A,
                                                       const bf16_t *__restrict__ B, float *Cf,
                                                       bf16_t *Cb) {
     static_assert(K % 16 == 0 && N % 16 == 0 && N >= 16 && N <= 256, "tcgen05 tile shape");
     constexpr uint32_t kCols = tc_cols<N>();
-    __shared__ __align__(128) uint8_t sA[kTcRows * K * 2];
-    __shared__ __align__(128) uint8_t sB[N * K * 2];
+    extern __shared__ __align__(128) uint8_t tc_smem[];
+    uint8_t *sB = tc_smem;                          // N * K * 2
+    uint8_t *sA = tc_smem + ((N * K * 2 + 127) / 128) * 128; // 2 x kTcRows * K * 2
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
-    const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
-    const unsigned r0 = blockIdx.x * kTcRows;
-    (void)lane;
+    const unsigned tid = threadIdx.x, warp = tid >> 5;
+    const unsigned tiles = (R + kTcRows - 1) / kTcRows;
     const uint32_t mbar_a = (uint32_t)__cvta_generic_to_shared(&mbar);
+    const uint32_t sa0 = (uint32_t)__cvta_generic_to_shared(sA);
+    const uint32_t sb0 = (uint32_t)__cvta_generic_to_shared(sB);
     if (warp == 0) {
         const uint32_t slot = (uint32_t)__cvta_generic_to_shared(&tmem_slot);
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(slot),
@@ -259,55 +287,58 @@ __global__ void __launch_bounds__(128) k_gemm_rows_tc(unsigned R, const bf16_t *
     }
     if (tid == 0)
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar_a) : "memory");
-    constexpr int KV = K / 8; // 16-byte chunks per row
+    constexpr int KV = K / 8;
     for (int t = tid; t < N * KV; t += 128) {
         const int n = t / KV, c = t % KV;
         *reinterpret_cast<uint4 *>(sB + c * N * 16 + n * 16) =
             __ldg(reinterpret_cast<const uint4 *>(B + (size_t)n * K + c * 8));
     }
-    for (int t = tid; t < (int)kTcRows * KV; t += 128) {
-        const int r = t / KV, c = t % KV;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (r0 + r < R) v = __ldg(reinterpret_cast<const uint4 *>(A + (size_t)(r0 + r) * K + c * 8));
-        *reinterpret_cast<uint4 *>(sA + c * 2048 + r * 16) = v;
-    }
-    // generic-proxy smem writes -> visible to the tensor core's async proxy
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    if (blockIdx.x < tiles) tc_fetch_tile<K>(sa0, A, R, blockIdx.x * kTcRows);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = tmem_slot;
-    if (tid == 0) {
-        const uint32_t a0 = (uint32_t)__cvta_generic_to_shared(sA);
-        const uint32_t b0 = (uint32_t)__cvta_generic_to_shared(sB);
-        const uint32_t idesc = (1u << 4)           // accumulator f32
-                               | (1u << 7)         // A bf16
-                               | (1u << 10)        // B bf16
-                               | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+    const uint32_t idesc = (1u << 4)      // accumulator f32
+                           | (1u << 7)    // A bf16
+                           | (1u << 10)   // B bf16
+                           | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+    bool ok = true;
+    unsigned i = 0;
+    for (unsigned tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x, ++i) {
+        const uint32_t sa = sa0 + (i & 1u) * (kTcRows * K * 2);
+        // this tile's rows have landed (this thread's copies), and every
+        // thread's copies are visible to the tensor core's async proxy
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        if (tid == 0) {
 #pragma unroll
-        for (int s = 0; s < K / 16; ++s) {
-            const uint64_t ad = tc_smem_desc(a0 + s * 2 * 2048, 2048, 128);
-            const uint64_t bd = tc_smem_desc(b0 + s * 2 * N * 16, N * 16, 128);
-            const uint32_t acc = s > 0 ? 1u : 0u;
+            for (int s = 0; s < K / 16; ++s) {
+                const uint64_t ad = tc_smem_desc(sa + s * 2 * 2048, 2048, 128);
+                const uint64_t bd = tc_smem_desc(sb0 + s * 2 * N * 16, N * 16, 128);
+                const uint32_t acc = s > 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
             asm volatile(
-                "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                    mbar_a)
                 : "memory");
         }
-        asm volatile(
-            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                mbar_a)
-            : "memory");
-    }
-    const bool ok = __syncthreads_and(tc_wait(mbar_a, 0u, 1u << 22)) != 0;
-    if (!ok) {
-        if (tid == 0) atomicOr(&g_tc_status, 1u);
-        tc_wait(mbar_a, 0u, 1u << 22);
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (ok) {
-        const unsigned row = r0 + warp * 32 + lane;
+        // the next tile streams into the other buffer (its last reader, the
+        // previous tile's MMAs, completed before that tile's epilogue)
+        const unsigned next = tile + gridDim.x;
+        if (next < tiles)
+            tc_fetch_tile<K>(sa0 + ((i + 1) & 1u) * (kTcRows * K * 2), A, R, next * kTcRows);
+        ok = __syncthreads_and(tc_wait(mbar_a, i & 1u, 1u << 22)) != 0;
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const unsigned row = tile * kTcRows + warp * 32 + (tid & 31u);
 #pragma unroll
         for (int c = 0; c < N / 16; ++c) {
             uint32_t v[16];
@@ -322,13 +353,17 @@ __global__ void __launch_bounds__(128) k_gemm_rows_tc(unsigned R, const bf16_t *
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             if (row < R) {
                 if (Cb) {
+                    uint32_t pk[8];
 #pragma unroll
-                    for (int j = 0; j < 16; j += 2) {
+                    for (int j = 0; j < 8; ++j) {
                         __nv_bfloat162 p;
-                        p.x = __float2bfloat16_rn(fmaxf(__uint_as_float(v[j]), 0.0f));
-                        p.y = __float2bfloat16_rn(fmaxf(__uint_as_float(v[j + 1]), 0.0f));
-                        *reinterpret_cast<__nv_bfloat162 *>(Cb + (size_t)row * N + c * 16 + j) = p;
+                        p.x = __float2bfloat16_rn(fmaxf(__uint_as_float(v[2 * j]), 0.0f));
+                        p.y = __float2bfloat16_rn(fmaxf(__uint_as_float(v[2 * j + 1]), 0.0f));
+                        pk[j] = *reinterpret_cast<uint32_t *>(&p);
                     }
+                    uint4 *dst = reinterpret_cast<uint4 *>(Cb + (size_t)row * N + c * 16);
+                    dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
                 } else {
 #pragma unroll
                     for (int j = 0; j < 16; j += 4)
@@ -339,6 +374,11 @@ __global__ void __launch_bounds__(128) k_gemm_rows_tc(unsigned R, const bf16_t *
             }
         }
     }
+    if (!ok) {
+        if (tid == 0) atomicOr(&g_tc_status, 1u);
+        tc_wait(mbar_a, (i & 1u), 1u << 22);
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -347,7 +387,11 @@ __global__ void __launch_bounds__(128) k_gemm_rows_tc(unsigned R, const bf16_t *
                      : "memory");
 }
 
-bool g_use_tc = false; // forward row products on tcgen05 (else mma.sync)
+template <int K, int N> constexpr size_t tc_smem_bytes() {
+    return ((size_t)(N * K * 2 + 127) / 128) * 128 + 2 * (size_t)kTcRows * K * 2;
+}
+
+bool g_use_tc = true; // forward row products on tcgen05 (else mma.sync)
 
 constexpr unsigned kReduceRows = 1024; // rows per block in reduce mode
 constexpr int kChunk = 32;             // rows staged per step
@@ -434,7 +478,16 @@ void gemm_fwd(unsigned R, const bf16_t *A, const bf16_t *B, float *Cf, bf16_t *C
               cudaStream_t q) {
     if (!R) return;
     if (g_use_tc) {
-        k_gemm_rows_tc<K, N><<<div_up(R, kTcRows), 128, 0, q>>>(R, A, B, Cf, Cb);
+        constexpr size_t smem = tc_smem_bytes<K, N>();
+        static bool configured = false;
+        if (!configured) {
+            PPF_CUDA(cudaFuncSetAttribute(k_gemm_rows_tc<K, N>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+            configured = true;
+        }
+        const unsigned grid = std::min(div_up(R, kTcRows), kNumSMs * kTcCtasPerSm);
+        k_gemm_rows_tc<K, N><<<grid, 128, smem, q>>>(R, A, B, Cf, Cb);
         PPF_LAUNCH_CHECK();
     } else {
         gemm_rows<K, N>(R, A, B, Cf, Cb, q);

@@ -12,8 +12,9 @@
 // fallback of every factored solve.
 //
 // Network (hidden width 32, bf16 weights, fp32 accumulation on the tensor
-// cores through mma.sync m16n8k16; every layer input carries a constant-1
-// column holding the bias):
+// cores: the forward layers as tcgen05.mma tiles with tensor-memory
+// accumulators, the backward products as mma.sync m16n8k16 tiles; every
+// layer input carries a constant-1 column holding the bias):
 //   X0 = [node features, 1]                    n x 16  (k_node_inputs)
 //   H0 = bf16(relu(X0 W0^T))                   n x 32
 //   Xl = [H, bf16(mean_nbr H), 1, 0..]          n x 80  (k_aggregate)

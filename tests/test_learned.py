@@ -148,6 +148,26 @@ def test_tcgen05_layers_match_mma_sync(product_lib, torch_cuda):
     assert np.abs(a1 - a0).max() < 5e-3
     f = OL.forward(g, w)
     assert np.abs(q1 - f["q"])[g.free].max() <= 2e-2 * max(1.0, np.abs(f["q"]).max())
+    # more 128-row tiles than resident CTAs: each CTA walks several tiles
+    # through its double-buffered operand tiles
+    L.ppf_learned_clear_samples()
+    big = learned_cases.synthetic(n=50000, seed=9)
+    k = _add(product_lib, big)
+    E = int(big["f_off"][-1]) + int(big["d_off"][-1])
+    try:
+        for tc in (0, 1):
+            L.ppf_learned_tensor_path(tc)
+            a = np.zeros(E, np.float32)
+            q = np.zeros(big["n"], np.float32)
+            assert L.ppf_learned_forward(k, wb.data_ptr(), a, q) == 0
+            out[tc] = (a, q)
+    finally:
+        L.ppf_learned_tensor_path(prev)
+    assert L.ppf_learned_tc_status() == 0
+    (a0, q0), (a1, q1) = out[0], out[1]
+    assert np.abs(q1 - q0).max() <= 5e-3 * max(1.0, np.abs(q0).max()), np.abs(q1 - q0).max()
+    assert np.abs(a1 - a0).max() < 5e-3
+    L.ppf_learned_clear_samples()
 
 
 @pytest.mark.gpu
