@@ -49,6 +49,8 @@ WORKLOADS = {
                        "static collision mesh"),
     "sphere_field": ("sphere_field: one 1024x1024 cloth (1,048,576 vertices) dropped over 50 "
                      "fixed spheres of seeded radii 0.02-0.1 m"),
+    "sphere_field_512": ("sphere_field_512: the same drop with a 512x512 cloth (262,144 "
+                         "vertices), the small case for DRAM counters"),
 }
 WORKLOAD = WORKLOADS["stacked_sheets"]
 L2_FLUSH_BYTES = 256 << 20
@@ -155,6 +157,8 @@ def build_scene(seed: int = 0, workload: str = "stacked_sheets"):
 
     if workload == "sphere_field":
         return scenes.sphere_field(1024, 50, seed=seed, dt=0.01)
+    if workload == "sphere_field_512":
+        return scenes.sphere_field(512, 50, seed=seed, dt=0.01)
     return scenes.stacked_sheets(128, 8, seed=seed, dt=0.01)
 
 
@@ -267,13 +271,18 @@ def run_ours(args, rank, local_rank, world):
     pcg_ms_total = sum(pcg_ms_all)
     achieved = pcg_bytes / (pcg_ms_total / 1e3) / 1e9 if pcg_ms_total > 0 else 0.0
     traffic = None
-    tfile = ROOT / "profiles" / "pcg_stacked_sheets_traffic.json"
-    if tfile.exists() and pcg_iters_all and args.workload == "stacked_sheets":
-        # DRAM bytes per iteration from one ncu capture of a launch of this
-        # workload, scaled to the mean iterations per launch of this run
-        per_iter = json.loads(tfile.read_text()).get("dram_bytes_per_iteration")
+    tname = ("pcg_stacked_sheets_traffic.json" if args.workload == "stacked_sheets"
+             else "pcg_sphere_field_traffic.json")
+    tfile = ROOT / "profiles" / tname
+    if tfile.exists() and pcg_iters_all:
+        # DRAM bytes per iteration from one ncu capture of this workload (the
+        # sphere fields: of the 512 x 512 drop, scaled by vertices), times the
+        # mean iterations per launch of this run
+        t = json.loads(tfile.read_text())
+        per_iter = t.get("dram_bytes_per_iteration")
         if per_iter:
-            traffic = int(per_iter * (sum(pcg_iters_all) / len(pcg_iters_all)))
+            scale = n / t["vertices"] if "vertices" in t else 1.0
+            traffic = int(per_iter * scale * (sum(pcg_iters_all) / len(pcg_iters_all)))
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                 "kernel": "k_pcg (persistent block-Jacobi PCG, one launch per solve)",
