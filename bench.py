@@ -334,8 +334,9 @@ def run_ours(args, rank, local_rank, world):
 def compare_preconditioners(restart, sc, lib, stream, steps):
     """The same first `steps` time steps from t = 0 with each preconditioner:
     block-Jacobi (the reference's default and the headline's), the
-    reference's aggregate additive Schwarz (ParamSet precond = 1) and the
-    first-order factored preconditioner. Each solve runs to the same 1e-3
+    reference's aggregate additive Schwarz (ParamSet precond = 1), the
+    first-order and FSAI factored preconditioners and, when the package holds
+    trained weights, the learned one. Each solve runs to the same 1e-3
     relative residual. Device time per step from CUDA events on the
     library's stream."""
     import torch
@@ -346,7 +347,8 @@ def compare_preconditioners(restart, sc, lib, stream, steps):
 
     kinds = [("block_jacobi", 0, abi.PRECOND_BLOCK_JACOBI),
              ("schwarz", 1, abi.PRECOND_BLOCK_JACOBI),
-             ("first_order_factor", 0, abi.PRECOND_FIRST_ORDER)]
+             ("first_order_factor", 0, abi.PRECOND_FIRST_ORDER),
+             ("fsai", 0, abi.PRECOND_FSAI)]
     out = {"steps": steps, "from": "t = 0", "tolerance": "1e-3 relative L1 residual"}
     if learned.WEIGHTS_FILE.exists():
         learned.use_weights()

@@ -115,7 +115,11 @@ void ppf_step_stats(PpfStepStats *out);
  *                            G = I - param * (strict lower part); param 0.5
  *   PPF_PRECOND_LEARNED      G emitted by the message-passing network whose
  *                            weights ppf_set_learned_weights loaded
- * A factored solve runs to the same relative residual with at most as many
+ *   PPF_PRECOND_FSAI         the factorised sparse approximate inverse
+ *                            (Kolotilina-Yeremin) on each row's strongest 15
+ *                            lower neighbours: (G A G^T)(i, i) = I and
+ *                            (G A)(i, j) = 0 on the row's pattern
+ * These kinds have no counterpart in the reference. A factored solve runs to the same relative residual with at most as many
  * iterations as the last block-Jacobi solve took; when it stalls or reaches
  * that count, the Newton iteration solves again with block-Jacobi from the
  * same start (the first solve of a session is block-Jacobi, which sets the
@@ -124,6 +128,7 @@ void ppf_step_stats(PpfStepStats *out);
 #define PPF_PRECOND_BLOCK_JACOBI 0
 #define PPF_PRECOND_FIRST_ORDER 1
 #define PPF_PRECOND_LEARNED 2
+#define PPF_PRECOND_FSAI 4
 int ppf_set_preconditioner(int kind, float param);
 /* ---- learned preconditioner -------------------------------------------------
  * The reference has no learned preconditioner; these entry points have no

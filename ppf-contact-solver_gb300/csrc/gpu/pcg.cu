@@ -1053,6 +1053,9 @@ struct DynFillOut {
     unsigned *index, *ovf_row, *ovf_col, *ovf_index;
     uint2 *ovf_range;
     float *ovf_val;
+    // the contact block each slot / overflow entry copies (bit 31:
+    // transposed), or kPad
+    unsigned *src, *ovf_src;
 };
 
 // Sorted position q: the row's entries in order, the first K (the slice
@@ -1069,12 +1072,14 @@ __global__ void k_contact_fill(unsigned max_slices, const unsigned *off, const u
     const unsigned i = real ? o.perm[q] : o.perm[m - 1];
     const unsigned obase = real ? o.ovf_off[i] : 0u;
     unsigned k = 0;
-    auto put = [&](unsigned j, const float (&mm)[9]) {
+    auto put = [&](unsigned j, const float (&mm)[9], unsigned src) {
         if (k < K) {
             put_slot(o.col, o.val, s0 + k, lane, j, mm);
+            o.src[(size_t)(s0 + k) * kSliceRows + lane] = src;
         } else {
             unsigned e = obase + (k - K);
             o.ovf_col[e] = j;
+            o.ovf_src[e] = src;
 #pragma unroll
             for (int t = 0; t < 9; ++t) o.ovf_val[9 * (size_t)e + t] = mm[t];
         }
@@ -1088,7 +1093,7 @@ __global__ void k_contact_fill(unsigned max_slices, const unsigned *off, const u
             float mm[9];
 #pragma unroll
             for (int e = 0; e < 9; ++e) mm[e] = b[e];
-            put(j, mm);
+            put(j, mm, p);
         }
         for (unsigned p = tr_off[i]; p < tr_off[i + 1]; ++p) {
             uint2 rp = tr[p];
@@ -1099,12 +1104,15 @@ __global__ void k_contact_fill(unsigned max_slices, const unsigned *off, const u
             for (int r = 0; r < 3; ++r)
 #pragma unroll
                 for (int c = 0; c < 3; ++c) mm[3 * c + r] = b[3 * r + c];
-            put(rp.x, mm);
+            put(rp.x, mm, rp.y | kTransposed);
         }
         o.index[i] = q;
     }
     const float zero[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (unsigned t = k; t < K; ++t) put_slot(o.col, o.val, s0 + t, lane, i, zero);
+    for (unsigned t = k; t < K; ++t) {
+        put_slot(o.col, o.val, s0 + t, lane, i, zero);
+        o.src[(size_t)(s0 + t) * kSliceRows + lane] = kPad;
+    }
     if (real && k > K) {
         unsigned idx = o.flag_off[i];
         o.ovf_row[idx] = i;
@@ -1288,6 +1296,8 @@ void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const 
     D.n_ovf = totals[4];
     out.col.reserve((size_t)out.slots * kSliceRows + 1);
     out.val.reserve((size_t)out.slots * kSliceRows * 9 + 1);
+    out.src.reserve((size_t)out.slots * kSliceRows + 1);
+    D.ovf_src.reserve(D.ovf_entries + 1);
     D.ovf_col.reserve(D.ovf_entries + 1);
     D.ovf_val.reserve(9 * (size_t)D.ovf_entries + 1);
     D.ovf_row.reserve(D.n_ovf + 1);
@@ -1296,7 +1306,7 @@ void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const 
     DynFillOut o{out.slice_off.data(), D.ovf_off.data(), D.flag_off.data(), D.perm.data(),
                  D.counters.data(),    out.col.data(),   out.val.data(),    D.index.data(),
                  D.ovf_row.data(),     D.ovf_col.data(), D.ovf_index.data(), D.ovf_range.data(),
-                 D.ovf_val.data()};
+                 D.ovf_val.data(),     out.src.data(),   D.ovf_src.data()};
     k_contact_fill<<<div_up(out.n_slices * kSliceRows, 256u), 256, 0, q>>>(
         out.n_slices, off, col, val, tr_off, tr, dof_mask, o);
     PPF_LAUNCH_CHECK();

@@ -136,6 +136,12 @@ struct SellLayout {
     unsigned n_slices = 0, slots = 0;
 };
 
+// Slot source maps (SellLayout::src, DynLayout::ovf_src): the upper block a
+// slot copies, with this bit set when the slot holds its transpose (the slot
+// lies in the block's column row), or kSlotPad for padding.
+constexpr unsigned kSlotTransposed = 0x80000000u;
+constexpr unsigned kSlotPad = 0xFFFFFFFFu;
+
 // Contact slices are at most this many slots wide; longer rows continue in
 // the overflow rows.
 constexpr unsigned kDynSliceCap = 32;
@@ -144,7 +150,7 @@ struct DynLayout {
     SellLayout sell; // over the sorted contact rows
     DevBuf<unsigned> key, perm, index, slice_k, row_ovf, row_flag, ovf_off, flag_off;
     DevBuf<unsigned> scan_tmp, counters;
-    DevBuf<unsigned> ovf_row, ovf_col, ovf_index;
+    DevBuf<unsigned> ovf_row, ovf_col, ovf_index, ovf_src;
     DevBuf<uint2> ovf_range;
     DevBuf<float> ovf_val;
     RadixSortWorkspace sort_ws;

@@ -21,30 +21,6 @@ __device__ __forceinline__ void st_mat3(float *p, const Mat3 &m) {
     for (int e = 0; e < 9; ++e) p[e] = m.m[e];
 }
 
-// Lower Cholesky factor L of a symmetric 3x3 block and its inverse.
-__device__ bool chol_inv3(const Mat3 &a, Mat3 &inv) {
-    const float l00 = sqrtf(a(0, 0));
-    const float l10 = a(1, 0) / l00, l20 = a(2, 0) / l00;
-    const float d1 = a(1, 1) - l10 * l10;
-    const float l11 = sqrtf(d1);
-    const float l21 = (a(2, 1) - l20 * l10) / l11;
-    const float d2 = a(2, 2) - l20 * l20 - l21 * l21;
-    const float l22 = sqrtf(d2);
-    if (!(a(0, 0) > 0.0f && d1 > 0.0f && d2 > 0.0f) || !isfinite(l22)) return false;
-    const float i00 = 1.0f / l00, i11 = 1.0f / l11, i22 = 1.0f / l22;
-    const float i10 = -l10 * i00 * i11;
-    const float i21 = -l21 * i11 * i22;
-    const float i20 = -(l20 * i00 + l21 * i10) * i22;
-    inv = Mat3::zero();
-    inv(0, 0) = i00;
-    inv(1, 0) = i10;
-    inv(1, 1) = i11;
-    inv(2, 0) = i20;
-    inv(2, 1) = i21;
-    inv(2, 2) = i22;
-    return true;
-}
-
 __global__ void k_chol_inv(unsigned n, const float *upper_val, const unsigned *diag_slot,
                            float *cinv, unsigned *status) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -20,9 +20,36 @@
 namespace ppf {
 namespace gpu {
 
-// Parallel value arrays of a factor (PcgFactor) plus the per-vertex C^{-1}.
+// Lower Cholesky factor L of a symmetric 3x3 block: inv = L^{-1}; false when
+// a pivot is not positive.
+__device__ __forceinline__ bool chol_inv3(const Mat3 &a, Mat3 &inv) {
+    const float l00 = sqrtf(a(0, 0));
+    const float l10 = a(1, 0) / l00, l20 = a(2, 0) / l00;
+    const float d1 = a(1, 1) - l10 * l10;
+    const float l11 = sqrtf(d1);
+    const float l21 = (a(2, 1) - l20 * l10) / l11;
+    const float d2 = a(2, 2) - l20 * l20 - l21 * l21;
+    const float l22 = sqrtf(d2);
+    if (!(a(0, 0) > 0.0f && d1 > 0.0f && d2 > 0.0f) || !isfinite(l22)) return false;
+    const float i00 = 1.0f / l00, i11 = 1.0f / l11, i22 = 1.0f / l22;
+    const float i10 = -l10 * i00 * i11;
+    const float i21 = -l21 * i11 * i22;
+    const float i20 = -(l20 * i00 + l21 * i10) * i22;
+    inv = Mat3::zero();
+    inv(0, 0) = i00;
+    inv(1, 0) = i10;
+    inv(1, 1) = i11;
+    inv(2, 0) = i20;
+    inv(2, 1) = i21;
+    inv(2, 2) = i22;
+    return true;
+}
+
+// Parallel value arrays of a factor (PcgFactor) plus the per-vertex C^{-1};
+// edge_f / edge_d: per upper entry of the fixed / contact CSR, G(hi, lo)
+// (FSAI only).
 struct FactorBuffers {
-    DevBuf<float> fixed, contact, ovf, diag, cinv;
+    DevBuf<float> fixed, contact, ovf, diag, cinv, edge_f, edge_d;
     PcgFactor view(float eps) const {
         return PcgFactor{fixed.data(), contact.data(), ovf.data(), diag.data(), eps};
     }

@@ -4,6 +4,7 @@
 // the iteration's status block after the line search).
 #include "fatal.cuh"
 #include "solver.cuh"
+#include "fsai.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -332,7 +333,7 @@ PcgOperator Solver::pcg_operator() const {
 }
 
 bool Solver::set_preconditioner(int kind, float param) {
-    if (kind < 0 || kind > 2 || (kind == 2 && !learned_ready_)) return false;
+    if (kind < 0 || kind > 4 || kind == 3 || (kind == 2 && !learned_ready_)) return false;
     precond_kind_ = kind;
     if (kind == 1) precond_param_ = param > 0.0f ? param : 0.5f;
     plain_iters_ = 0;
@@ -348,7 +349,24 @@ void Solver::build_factor() {
                    factor_);
     launch_chol_inv(n_, fixed_val_.data(), fixed_diag_.data(), factor_.cinv.data(),
                     &st_.data()->status, q_);
-    if (precond_kind_ == 2) {
+    if (precond_kind_ == 4) {
+        FsaiSystem S{n_,
+                     fixed_off_.data(),
+                     fixed_col_.data(),
+                     fixed_val_.data(),
+                     fixed_tr_off_.data(),
+                     fixed_tr_.data(),
+                     dyn_.off,
+                     dyn_.col,
+                     dyn_.val,
+                     dyn_.tr_off,
+                     dyn_.tr,
+                     fixed_diag_.data(),
+                     dof_mask_.data()};
+        launch_factor_fsai(A, S, nnz_fixed_, dyn_.cap, fixed_sell_.src.data(),
+                           dyn_layout_.sell.src.data(), dyn_layout_.ovf_src.data(), factor_,
+                           &st_.data()->status, q_);
+    } else if (precond_kind_ == 2) {
         LearnedGraph g;
         g.n = n_;
         g.fixed = LearnedPart{fixed_off_.data(), fixed_col_.data(), fixed_val_.data(),

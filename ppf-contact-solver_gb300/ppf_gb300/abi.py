@@ -14,6 +14,7 @@ STATS_MAX_SOLVES = 256
 
 BARRIER_CUBIC, BARRIER_QUAD, BARRIER_LOG = 0, 1, 2
 PRECOND_BLOCK_JACOBI, PRECOND_FIRST_ORDER, PRECOND_LEARNED = 0, 1, 2
+PRECOND_FSAI = 4
 FRICTION_MIN, FRICTION_MAX, FRICTION_MEAN = 0, 1, 2
 MODEL_ARAP, MODEL_STVK, MODEL_BARAFF_WITKIN, MODEL_SNHK = 0, 1, 2, 3
 

@@ -284,7 +284,8 @@ def compare(scene_fn, steps: int, weights=None) -> dict:
     out = {}
     for name, kind in (("block_jacobi", abi.PRECOND_BLOCK_JACOBI),
                        ("first_order", abi.PRECOND_FIRST_ORDER),
-                       ("learned", abi.PRECOND_LEARNED)):
+                       ("learned", abi.PRECOND_LEARNED),
+                       ("fsai", abi.PRECOND_FSAI)):
         sc, motion = scene_fn()
         sess = Session(sc, pin_motion=motion)
         sess.set_preconditioner(kind)

@@ -21,7 +21,9 @@ def _csr(n, pairs):
     return np.array(off, np.uint32), np.array(col, np.uint32)
 
 
-def synthetic(n=40, seed=0, dirichlet=(3, 17)):
+def synthetic(n=40, seed=0, dirichlet=(3, 17), hub=0):
+    """hub > 0: the last vertex also gets contact couplings to the first `hub`
+    vertices (a row with more lower neighbours than a factor keeps)."""
     rng = np.random.default_rng(seed)
     fixed = [(i, i) for i in range(n)] + [(i, i + 1) for i in range(n - 1)]
     fixed += [(int(a), int(b)) for a, b in rng.integers(0, n, (n, 2)) if a != b]
@@ -29,6 +31,7 @@ def synthetic(n=40, seed=0, dirichlet=(3, 17)):
     fset = {(min(a, b), max(a, b)) for a, b in fixed}
     contact = [(int(a), int(b)) for a, b in rng.integers(0, n, (n // 2, 2))
                if a != b and (min(a, b), max(a, b)) not in fset]
+    contact += [(j, n - 1) for j in range(hub) if (j, n - 1) not in fset]
     c_off, c_col = _csr(n, contact)
     dof = np.zeros(n, np.uint32)
     dof[list(dirichlet)] = 1
