@@ -120,6 +120,31 @@ def test_lbvh_bit_exact(product_lib, oracle_lib, rng, kind, shape):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("kind", [1, 2, 3])
+def test_lbvh_single_primitive(product_lib, oracle_lib, kind):
+    """One primitive: the tree is that leaf alone (root 0), its box the swept
+    primitive's, as the oracle has it."""
+    v = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]], np.float32)
+    v1 = v + np.float32(0.01)
+    prims = {1: None, 2: np.array([[0, 1]], np.uint32), 3: np.array([[0, 1, 2]], np.uint32)}[kind]
+    x0 = v[:1] if kind == 1 else v
+    x1 = v1[:1] if kind == 1 else v1
+    margin = np.full(1, 5e-4, np.float32)
+    a = _lib.lbvh(product_lib.ppf_lbvh_build_host, kind, x0, x1, prims, margin, 1.0)
+    b = _lib.lbvh(oracle_lib.oracle_lbvh_build, kind, x0, x1, prims, margin, 1.0)
+    assert a[0] == b[0] == 0
+    assert np.array_equal(a[1], b[1])
+    assert np.array_equal(a[2].view(np.uint32), b[2].view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_radix_sort_empty_input(product_lib):
+    keys = np.zeros(0, np.uint32)
+    vals = np.zeros(0, np.uint32)
+    assert product_lib.ppf_radix_sort_host(keys, vals, 0, 30) == 0
+
+
+@pytest.mark.gpu
 def test_lbvh_duplicate_centroids(product_lib, oracle_lib):
     """All primitives at one point: every Morton code ties, so the topology is
     decided by the index tie-break alone."""
