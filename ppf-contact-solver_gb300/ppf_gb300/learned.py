@@ -28,7 +28,7 @@ import numpy as np
 
 from . import abi, scenes
 from ._lib import f32p, f32p_opt, product, u32p, u32p_opt
-from .session import Session
+from .session import Session, SolverError
 
 N_WEIGHTS = 12592
 OFF_W0, OFF_W1, OFF_WH, OFF_WF, OFF_WO = 0, 512, 8192, 12032, 12544
@@ -164,7 +164,10 @@ def collect(scene, steps: int, every: int = 3, start: int = 1, pin_motion=None):
     for k in range(steps):
         if k >= start and (k - start) % every == 0:
             yield capture_system(n)
-        r = sess.step()
+        try:
+            r = sess.step()
+        except SolverError:
+            break
         if not r.success():
             break
 
@@ -252,19 +255,36 @@ def sample_loss(ids, w, probes: int = 16, seed: int = 1) -> list:
     return out
 
 
-def default_training_scenes():
-    """Stacked cloth sheets (8 sheets of 128 x 128 over a cube) under seeded
-    rotations and offsets, a twisted tube, and cloth dropped over fields of
-    spheres, as (name, scene, pin_motion, steps, every)."""
-    out = []
-    for seed in (1, 2, 3):
-        sc, _ = scenes.stacked_sheets(side=128, sheets=8, seed=seed)
-        out.append((f"stacked_sheets_128x8_seed{seed}", sc, None, 90, 3))
-    sc, motion = scenes.twisted_tube(around=128, along=256)
-    out.append(("twisted_tube_128x256", sc, motion, 45, 3))
-    for seed in (1, 2):
-        sc, _ = scenes.sphere_field(side=256, spheres=12, seed=seed)
-        out.append((f"sphere_field_256_seed{seed}", sc, None, 60, 3))
+def training_scenes(preset: str = "small"):
+    """The scenes the training systems come from, as (name, factory, steps,
+    every); factory() returns (scene, pin_motion).
+
+    small: stacked cloth sheets (8 sheets of 128 x 128 over a cube) at seeds
+    1-3, a 128 x 256 twisted tube, and 256^2 cloth over 12 spheres at seeds
+    1-2 (145 systems).
+    full: the 131,072-vertex stacked sheets at seeds 1-26 (seeded rotations
+    and offsets), every second step of 90, 256 x 512 twisted tubes whose end
+    rings turn at a seeded rate in [1.5, 2.5] rad/s (seeds 1-16, the first 45
+    steps), and the two sphere fields: about 2,000 systems."""
+    if preset == "small":
+        out = [(f"stacked_sheets_128x8_seed{k}",
+                (lambda k=k: scenes.stacked_sheets(side=128, sheets=8, seed=k)), 90, 3)
+               for k in (1, 2, 3)]
+        out.append(("twisted_tube_128x256", lambda: scenes.twisted_tube(around=128, along=256),
+                    45, 3))
+    else:
+        out = [(f"stacked_sheets_128x8_seed{k}",
+                (lambda k=k: scenes.stacked_sheets(side=128, sheets=8, seed=k)), 90, 2)
+               for k in range(1, 27)]
+        rng = np.random.default_rng(2024)
+        for k in range(1, 17):
+            omega = float(rng.uniform(1.5, 2.5))
+            out.append((f"twisted_tube_256x512_seed{k}",
+                        (lambda om=omega: scenes.twisted_tube(around=256, along=512, omega=om)),
+                        45, 1))
+    out += [(f"sphere_field_256_seed{k}",
+             (lambda k=k: scenes.sphere_field(side=256, spheres=12, seed=k)), 60, 3)
+            for k in (1, 2)]
     return out
 
 
@@ -315,18 +335,29 @@ def train_main(argv=None):
                     help="cosine decay of the learning rate down to this value")
     ap.add_argument("--probes", type=int, default=8)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--log", default=None)
+    ap.add_argument("--preset", choices=["small", "full"], default="small")
+    ap.add_argument("--systems", type=int, default=2000, help="stop collecting at this many")
+    ap.add_argument("--min-free-gb", type=float, default=24.0,
+                    help="stop collecting when less device memory than this is free")
     a = ap.parse_args(argv)
+    import torch
+
     t0 = time.time()
     lib().ppf_learned_clear_samples()
     ids, sizes, names = [], [], []
-    for name, sc, motion, steps, every in default_training_scenes():
+    for name, factory, steps, every in training_scenes(a.preset):
+        if len(ids) >= a.systems or torch.cuda.mem_get_info()[0] < a.min_free_gb * 2**30:
+            break
+        sc, motion = factory()
         k0 = len(ids)
         for s in collect(sc, steps, every=every, pin_motion=motion):
             ids.append(add_sample(s))
             sizes.append(int(s["n"]))
             names.append(name)
-        print(f"{name}: {len(ids) - k0} systems ({time.time() - t0:.0f} s)", flush=True)
+            if len(ids) >= a.systems or torch.cuda.mem_get_info()[0] < a.min_free_gb * 2**30:
+                break
+        print(f"{name}: {len(ids) - k0} systems ({time.time() - t0:.0f} s, "
+              f"{torch.cuda.mem_get_info()[0] / 2**30:.0f} GB free)", flush=True)
         del sc
     rng = np.random.default_rng(a.seed)
     held = set(rng.choice(len(ids), size=max(1, len(ids) // 10), replace=False).tolist())
@@ -345,7 +376,7 @@ def train_main(argv=None):
     after = float(np.mean(sample_loss(test_ids, tr.weights())))
     meta = {"systems": len(ids), "train": len(train), "held_out": len(test_ids),
             "iters": a.iters, "lr": a.lr, "lr_final": a.lr_final, "probes": a.probes,
-            "held_out_loss_init": before, "held_out_loss_trained": after,
+            "preset": a.preset, "held_out_loss_init": before, "held_out_loss_trained": after,
             "scenes": sorted(set(names)), "seconds": time.time() - t0}
     print(json.dumps(meta), flush=True)
     Path(a.out).parent.mkdir(parents=True, exist_ok=True)
