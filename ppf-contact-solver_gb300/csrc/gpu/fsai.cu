@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(32 * kFsaiWarps)
 // other holds its transpose. Diagonal, padding and Dirichlet slots hold zero.
 __global__ void k_fsai_fill_sell(SellMatrix M, unsigned rows, const unsigned *perm,
                                  const unsigned *src, const float *edge, const unsigned *dof,
-                                 float *out) {
+                                 bf16_t *out) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned sl = t / kSliceRows, lane = t % kSliceRows;
     if (sl >= M.n_slices) return;
@@ -277,15 +277,15 @@ __global__ void k_fsai_fill_sell(SellMatrix M, unsigned rows, const unsigned *pe
             v = ld9(edge + 9 * (size_t)(sv & ~kSlotTransposed));
             if (!(sv & kSlotTransposed)) v = v.transpose();
         }
-        float *d = out + (size_t)s * 9 * kSliceRows + lane;
+        bf16_t *d = out + (size_t)s * 9 * kSliceRows + lane;
 #pragma unroll
-        for (int e = 0; e < 9; ++e) d[e * kSliceRows] = v.m[e];
+        for (int e = 0; e < 9; ++e) d[e * kSliceRows] = __float2bfloat16_rn(v.m[e]);
     }
 }
 
 // One warp per overflow row: its entries, as k_fsai_fill_sell.
 __global__ void k_fsai_fill_ovf(OverflowRows O, const unsigned *src, const float *edge,
-                                const unsigned *dof, float *out) {
+                                const unsigned *dof, bf16_t *out) {
     const unsigned k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
     if (k >= O.count) return;
     const unsigned a = __ldg(O.row + k);
@@ -298,7 +298,8 @@ __global__ void k_fsai_fill_ovf(OverflowRows O, const unsigned *src, const float
             v = ld9(edge + 9 * (size_t)(sv & ~kSlotTransposed));
             if (!(sv & kSlotTransposed)) v = v.transpose();
         }
-        st9(out + 9 * (size_t)e, v);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) out[9 * (size_t)e + q] = __float2bfloat16_rn(v.m[q]);
     }
 }
 

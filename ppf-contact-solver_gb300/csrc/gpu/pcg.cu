@@ -207,6 +207,12 @@ struct GatherY {
     __device__ __forceinline__ Vec3 operator()(unsigned j) const { return ld4(Y, j); }
 };
 
+// A stored value: the operator's are fp32, a factor's bf16.
+__device__ __forceinline__ float ld_val(const float *p) { return __ldg(p); }
+__device__ __forceinline__ float ld_val(const bf16_t *p) {
+    return __bfloat162float(__ushort_as_bfloat16(__ldg(reinterpret_cast<const unsigned short *>(p))));
+}
+
 // Which slots a product takes: all of them, only those below the diagonal
 // of their row (column < row), or only those above it (column > row).
 enum SlotMask : int { kAllSlots = 0, kBelow = 1, kAbove = 2 };
@@ -220,15 +226,15 @@ __device__ __forceinline__ bool takes(unsigned j, unsigned row) {
 
 // One slot's block times its neighbour value. `row` is the slot's row
 // (0xffffffff for a lane without one, which a masked product then skips).
-template <int MASK, class G>
-__device__ __forceinline__ void slot_term(const SellMatrix &M, size_t s, unsigned lane,
-                                          unsigned j, unsigned row, const G &gather, Vec3 &acc,
+template <int MASK, class V, class G>
+__device__ __forceinline__ void slot_term(const V *val, size_t s, unsigned lane, unsigned j,
+                                          unsigned row, const G &gather, Vec3 &acc,
                                           Vec3 &abssum) {
     if (MASK != kAllSlots && (row == 0xFFFFFFFFu || !takes<MASK>(j, row))) return;
-    const float *a = M.val + s * 9 * kSliceRows + lane;
+    const V *a = val + s * 9 * kSliceRows + lane;
     float m[9];
 #pragma unroll
-    for (int e = 0; e < 9; ++e) m[e] = __ldg(a + e * kSliceRows);
+    for (int e = 0; e < 9; ++e) m[e] = ld_val(a + e * kSliceRows);
     const Vec3 v = gather(j);
     // column-major block: t_r = sum_c m[3 c + r] v_c
     Vec3 t;
@@ -245,8 +251,9 @@ __device__ __forceinline__ void slot_term(const SellMatrix &M, size_t s, unsigne
 // 64-byte runs, one per parity. abssum collects the component-wise |term| of
 // every block product. Slots are taken four at a time (column indices first)
 // so four gathers are in flight per lane.
-template <int MASK, class G>
-__device__ __forceinline__ void sell_half_row(const SellMatrix &M, unsigned slice, unsigned r,
+template <int MASK, class V, class G>
+__device__ __forceinline__ void sell_half_row(const SellMatrix &M, const V *val, unsigned slice,
+                                              unsigned r,
                                               unsigned par, unsigned row, const G &gather,
                                               Vec3 &acc, Vec3 &abssum) {
     unsigned s0 = __ldg(M.slice_off + slice), s1 = __ldg(M.slice_off + slice + 1);
@@ -263,11 +270,11 @@ __device__ __forceinline__ void sell_half_row(const SellMatrix &M, unsigned slic
             j[q] = __ldg(M.col + (size_t)(s + 2 * q) * kSliceRows + r);
 #pragma unroll
         for (int q = 0; q < 4; ++q)
-            slot_term<MASK>(M, s + 2 * q, r, j[q], row, gather, acc, abssum);
+            slot_term<MASK>(val, s + 2 * q, r, j[q], row, gather, acc, abssum);
     }
     for (; s < s1; s += 2) {
         const unsigned j = __ldg(M.col + (size_t)s * kSliceRows + r);
-        slot_term<MASK>(M, s, r, j, row, gather, acc, abssum);
+        slot_term<MASK>(val, s, r, j, row, gather, acc, abssum);
     }
 }
 
@@ -310,8 +317,8 @@ struct PcgArgs {
 
 // Overflow row k of the contact part: the whole warp strides its entries and
 // folds the partial products in a fixed shuffle order. Result on lane 0.
-template <int MASK, class G>
-__device__ __forceinline__ void overflow_row(const OverflowRows &O, const float *vals,
+template <int MASK, class V, class G>
+__device__ __forceinline__ void overflow_row(const OverflowRows &O, const V *vals,
                                              unsigned k, unsigned lane, const G &gather,
                                              Vec3 &acc, Vec3 &abssum) {
     const uint2 rg = __ldg(O.range + k);
@@ -319,10 +326,10 @@ __device__ __forceinline__ void overflow_row(const OverflowRows &O, const float 
     for (unsigned e = rg.x + lane; e < rg.x + rg.y; e += 32u) {
         const unsigned j = __ldg(O.col + e);
         if (!takes<MASK>(j, row)) continue;
-        const float *a = vals + 9 * (size_t)e;
+        const V *a = vals + 9 * (size_t)e;
         float m[9];
 #pragma unroll
-        for (int q = 0; q < 9; ++q) m[q] = __ldg(a + q);
+        for (int q = 0; q < 9; ++q) m[q] = ld_val(a + q);
         const Vec3 v = gather(j);
         Vec3 t;
         t[0] = m[0] * v[0] + m[3] * v[1] + m[6] * v[2];
@@ -398,8 +405,8 @@ __device__ __forceinline__ Vec3 row_product(const PcgArgs &g, unsigned i) {
 // The epilogue gets (row, A-part, |terms|) on the lanes that own a result.
 // `vals` are the value arrays the slots are read from: the operator's own
 // (fixed, contact, overflow) or a factor's parallel ones.
-template <int MASK, class G, class E>
-__device__ __forceinline__ void product_task(const PcgArgs &g, const float *const vals[3],
+template <int MASK, class V, class G, class E>
+__device__ __forceinline__ void product_task(const PcgArgs &g, const V *const vals[3],
                                              unsigned task, unsigned lane, const G &gather,
                                              E &&epilogue) {
     const PcgOperator &A = g.A;
@@ -414,14 +421,14 @@ __device__ __forceinline__ void product_task(const PcgArgs &g, const float *cons
         const unsigned u = fixed ? task - t2 : task - t1;
         const unsigned sl = u >> 1, r = (u & 1u) * 16u + (lane & 15u);
         const unsigned q = sl * kSliceRows + r;
-        SellMatrix M = fixed ? A.fixed : A.contact.sell;
-        M.val = vals[fixed ? 0 : 1];
+        const SellMatrix &M = fixed ? A.fixed : A.contact.sell;
+        const V *val = vals[fixed ? 0 : 1];
         unsigned row = 0xFFFFFFFFu;
         if (MASK != kAllSlots) {
             if (fixed) row = q < A.n ? q : 0xFFFFFFFFu;
             else row = q < A.contact.rows ? __ldg(A.contact.perm + q) : 0xFFFFFFFFu;
         }
-        sell_half_row<MASK>(M, sl, r, par, row, gather, acc, ab);
+        sell_half_row<MASK>(M, val, sl, r, par, row, gather, acc, ab);
         join_halves(acc, ab);
         if (par == 0u) {
             if (fixed) {
@@ -569,19 +576,19 @@ aborted:
         *g.res = PcgResult{0u, 0.0f, 2, 0, 0.0f, 0.0f, STATUS_PCG_BREAKDOWN};
 }
 
-// z = P r with P = G^T G + eps D^{-1}, after r is final grid-wide and the
-// records hold z = 0 and Y = 0 (the caller's update phase wrote them):
-//   Z1: y = G r      (slots below the diagonal plus the diagonal blocks)
-//   Z2: z = G^T y + eps D^{-1} r  (slots above the diagonal plus the
-//       transposed diagonal blocks), added into the records' z
+// The factored preconditioner's two products (P = G^T G + eps D^{-1}):
+//   factor_y: y = G r (slots below the diagonal plus the diagonal blocks) into
+//             Y, which the caller zeroed; then a grid barrier
+//   factor_z: z = G^T y + eps D^{-1} r (slots above the diagonal plus the
+//             transposed diagonal blocks), added into the records' z, which
+//             the caller zeroed; then the grid-wide r^T z
 // Each row's parts (fixed, contact, overflow) are added with atomics; r^T z
-// is linear in them, so its partial sums need no complete z. Returns false
-// when the grid barrier aborted; rz gets the grid-wide r^T z.
-__device__ bool apply_factor(const PcgArgs &g, BlockTasks &bt, unsigned lane, float *part_a,
-                             float *part_b, unsigned *abort, float &rz) {
+// is linear in them, so its partial sums need no complete z. Both return
+// false when the grid barrier aborted.
+__device__ bool factor_y(const PcgArgs &g, BlockTasks &bt, unsigned lane, float *part,
+                         unsigned *abort) {
     const PcgOperator &A = g.A;
-    const unsigned nb = gridDim.x;
-    const float *const vals[3] = {A.factor.fixed, A.factor.contact, A.factor.ovf};
+    const bf16_t *const vals[3] = {A.factor.fixed, A.factor.contact, A.factor.ovf};
     bt.start();
     {
         const GatherPlain gr{g.r};
@@ -598,9 +605,15 @@ __device__ bool apply_factor(const PcgArgs &g, BlockTasks &bt, unsigned lane, fl
                                  });
     }
     float a = 0.0f, b = 0.0f;
-    if (!grid_sum2(a, b, part_a, g.bar, nb, abort)) return false;
+    return grid_sum2(a, b, part, g.bar, gridDim.x, abort);
+}
+
+__device__ bool factor_z(const PcgArgs &g, BlockTasks &bt, unsigned lane, float *part,
+                         unsigned *abort, float &rz) {
+    const PcgOperator &A = g.A;
+    const bf16_t *const vals[3] = {A.factor.fixed, A.factor.contact, A.factor.ovf};
     bt.start();
-    a = 0.0f;
+    float a = 0.0f;
     {
         const GatherY gy{g.Y};
         for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
@@ -623,15 +636,49 @@ __device__ bool apply_factor(const PcgArgs &g, BlockTasks &bt, unsigned lane, fl
                                      a += ri.dot(acc);
                                  });
     }
-    b = 0.0f;
-    if (!grid_sum2(a, b, part_b, g.bar, nb, abort)) return false;
+    float b = 0.0f;
+    if (!grid_sum2(a, b, part, g.bar, gridDim.x, abort)) return false;
     rz = a;
     return true;
 }
 
+// (A v)(j) of every column a product gathers: the sum of the row's parts
+// that the product phase stored (complete after its grid barrier).
+struct GatherAp {
+    const PcgArgs *g;
+    __device__ __forceinline__ Vec3 operator()(unsigned j) const { return row_product(*g, j); }
+};
+
+// Y -= alpha G (A p): the update of y = G r that follows r -= alpha A p, run
+// inside the update phase (A p is complete after the product phase's
+// barrier), so y needs no barrier of its own. No barrier here.
+__device__ void factor_y_update(const PcgArgs &g, BlockTasks &bt, unsigned lane, float alpha) {
+    const PcgOperator &A = g.A;
+    const bf16_t *const vals[3] = {A.factor.fixed, A.factor.contact, A.factor.ovf};
+    bt.start();
+    const GatherAp gap{&g};
+    for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
+        product_task<kBelow>(g, vals, task, lane, gap,
+                             [&](unsigned row, unsigned part, unsigned, Vec3 acc, const Vec3 &) {
+                                 if (part == 0u)
+                                     acc += load_mat3(A.factor.diag + 9 * (size_t)row) *
+                                            row_product(g, row);
+                                 float *y = reinterpret_cast<float *>(g.Y + row);
+                                 atomicAdd(y, -alpha * acc[0]);
+                                 atomicAdd(y + 1, -alpha * acc[1]);
+                                 atomicAdd(y + 2, -alpha * acc[2]);
+                             });
+}
+
+// y = G r is recomputed from r every this many iterations (otherwise it
+// follows r's recurrence), which bounds the rounding the recurrence gathers.
+constexpr unsigned kYRefresh = 16;
+
 // PCG with the factored preconditioner: the recurrence, verdicts and checks
-// of k_pcg, with z = P r computed by apply_factor after each update (two
-// more grid barriers per iteration).
+// of k_pcg, with z = P r after each update: y = G r follows r's recurrence
+// inside the update phase (recomputed from r every kYRefresh iterations),
+// then z = G^T y + eps D^{-1} r, so an iteration takes three grid barriers
+// (four on a refresh).
 __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
     const PcgOperator &A = g.A;
     const unsigned nb = gridDim.x;
@@ -679,7 +726,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
             return;
         }
         float rz0;
-        if (!apply_factor(g, bt, lane, part1, part0, abort, rz0)) goto aborted;
+        if (!factor_y(g, bt, lane, part1, abort)) goto aborted;
+        if (!factor_z(g, bt, lane, part0, abort, rz0)) goto aborted;
         float beta = 0.0f;
         unsigned stride = 4, next_check = 1;
         int broke = 0;
@@ -713,7 +761,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
                     break_val = pAp;
                 }
             }
-            // U: x += alpha p, r -= alpha A p; records {0, p}, Y = 0; |r|_1
+            // U: x += alpha p, r -= alpha A p; records {0, p}; |r|_1; and
+            // y -= alpha G A p, or, every kYRefresh iterations, Y = 0 for
+            // y = G r from scratch after the barrier
+            const bool refresh = iter % kYRefresh == 0;
             a = b = 0.0f;
             for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
                 const unsigned i = sl * kSliceRows + lane;
@@ -727,13 +778,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
                 st3(g.x, i, xi);
                 st3(g.r, i, ri);
                 st_record(g.R, i, Vec3::zero(), pi);
-                st4(g.Y, i, Vec3::zero());
+                if (refresh) st4(g.Y, i, Vec3::zero());
                 b += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
             }
+            if (!refresh) factor_y_update(g, bt, lane, alpha);
             if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
             const float err_now = b;
             float rz_new;
-            if (!apply_factor(g, bt, lane, part1, part0, abort, rz_new)) goto aborted;
+            if (refresh && !factor_y(g, bt, lane, part1, abort)) goto aborted;
+            if (!factor_z(g, bt, lane, part0, abort, rz_new)) goto aborted;
             beta = rz_new / rz0;
             rz0 = rz_new;
             const bool at_cap = iter >= g.max_iter;

@@ -23,6 +23,8 @@
 
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "radix_sort.cuh"
 #include "scene.cuh"
 
@@ -63,17 +65,21 @@ struct ContactRows {
     const unsigned *index;  // n: row -> sorted position, or 0xffffffff
 };
 
+typedef __nv_bfloat16 bf16_t;
+
 // Factored preconditioner P = G^T G + eps D^{-1} (D^{-1}: the block-Jacobi
 // inverse), G block lower-triangular on the operator's own pattern. Its
-// values sit in arrays parallel to the operator's value arrays: the slot of
+// slot values are bf16 (both slots of an edge round the same value, so P
+// stays symmetric positive definite) in arrays parallel to the operator's
+// value arrays: the slot of
 // row a, column b holds G(a, b) when b < a and G(b, a)^T when b > a, so
 // y = G r walks the slots below the diagonal and z = G^T y the slots above
 // it. The diagonal blocks G(a, a) are kept apart, 9 floats per vertex
 // (column-major). Slots touching a Dirichlet vertex hold zero blocks.
 struct PcgFactor {
-    const float *fixed;   // as SellMatrix::val of the fixed part
-    const float *contact; // as the contact part's SellMatrix::val
-    const float *ovf;     // as OverflowRows::val
+    const bf16_t *fixed;   // as SellMatrix::val of the fixed part
+    const bf16_t *contact; // as the contact part's SellMatrix::val
+    const bf16_t *ovf;     // as OverflowRows::val
     const float *diag;    // 9 per vertex; null: block-Jacobi only
     float eps;
 };

@@ -80,7 +80,7 @@ __device__ __forceinline__ Mat3 slot_value(unsigned a, unsigned b, const Mat3 &B
 template <class Head>
 __global__ void k_factor_sell(SellMatrix M, unsigned rows, const unsigned *perm,
                               const unsigned *dof_mask, const float *cinv, Head head,
-                              float *out) {
+                              bf16_t *out) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned sl = t / kSliceRows, lane = t % kSliceRows;
     if (sl >= M.n_slices) return;
@@ -100,14 +100,14 @@ __global__ void k_factor_sell(SellMatrix M, unsigned rows, const unsigned *perm,
             v = slot_value(a, b, B, Ca, dof_mask, cinv, head);
         }
 #pragma unroll
-        for (int e = 0; e < 9; ++e) out[base + e * kSliceRows] = v.m[e];
+        for (int e = 0; e < 9; ++e) out[base + e * kSliceRows] = __float2bfloat16_rn(v.m[e]);
     }
 }
 
 // One warp per overflow row: every entry of it.
 template <class Head>
 __global__ void k_factor_ovf(OverflowRows O, const unsigned *dof_mask, const float *cinv,
-                             Head head, float *out) {
+                             Head head, bf16_t *out) {
     const unsigned k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
     if (k >= O.count) return;
     const unsigned a = __ldg(O.row + k);
@@ -118,7 +118,8 @@ __global__ void k_factor_ovf(OverflowRows O, const unsigned *dof_mask, const flo
         Mat3 v = Mat3::zero();
         if (live) v = slot_value(a, __ldg(O.col + e), ld_mat3(O.val + 9 * (size_t)e), Ca,
                                  dof_mask, cinv, head);
-        st_mat3(out + 9 * (size_t)e, v);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) out[9 * (size_t)e + q] = __float2bfloat16_rn(v.m[q]);
     }
 }
 

@@ -49,7 +49,8 @@ __device__ __forceinline__ bool chol_inv3(const Mat3 &a, Mat3 &inv) {
 // edge_f / edge_d: per upper entry of the fixed / contact CSR, G(hi, lo)
 // (FSAI only).
 struct FactorBuffers {
-    DevBuf<float> fixed, contact, ovf, diag, cinv, edge_f, edge_d;
+    DevBuf<bf16_t> fixed, contact, ovf;
+    DevBuf<float> diag, cinv, edge_f, edge_d;
     PcgFactor view(float eps) const {
         return PcgFactor{fixed.data(), contact.data(), ovf.data(), diag.data(), eps};
     }

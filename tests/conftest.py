@@ -57,3 +57,17 @@ def ref_lib():
 @pytest.fixture
 def rng():
     return np.random.default_rng(1234)
+
+
+@pytest.fixture(autouse=True)
+def _block_jacobi_after_each_test(request):
+    """The library keeps its preconditioner choice across sessions (it is a
+    process-wide setting, like the rest of its state): put block-Jacobi, the
+    reference's, back after every GPU test, so no test inherits another's."""
+    yield
+    if request.node.get_closest_marker("gpu") is None:
+        return
+    from ppf_gb300 import _lib
+
+    if _lib._PRODUCT is not None:
+        _lib._PRODUCT.ppf_set_preconditioner(0, 0.0)
