@@ -190,6 +190,30 @@ unsigned ppf_learned_tc_status(void);
  * schwarz/schwarz.hpp:38-86). */
 #define PPF_PRECOND_SCHWARZ 3
 
+/* ---- batched PCG ------------------------------------------------------------
+ * Many independent Newton systems (one per scene of a batch of uneven scenes)
+ * solved by the reference's block-Jacobi PCG (solver/solver.cu:357-400,
+ * 431-571, 1002-1278; x0 = 0, relative L1 residual tol, the same check
+ * schedule and curvature verdict) in ONE launch: one 1024-thread CTA per
+ * system with block barriers only, so each system stops on its own iteration
+ * count. No counterpart in the reference, which solves one scene per process.
+ *   row_off   n_sys + 1 vertex-row offsets: system s owns rows
+ *             [row_off[s], row_off[s+1])
+ *   off, col, val   both-triangle block rows over all rows (off: rows + 1;
+ *             col: the global row of each block's column, inside the same
+ *             system; val: 9 column-major floats per block)
+ *   rhs       3 floats per row
+ *   one_by_one  nonzero: one launch per system instead (for comparison)
+ * Host memory in and out (any output may be NULL): x (3 per row), the
+ * iterations, relative residual and state (0 converged, 1 truncated, 2
+ * failed) per system, and the device time of the launch(es) in ms.
+ * Returns 0, or -1 for an invalid batch. */
+int ppf_batch_pcg(unsigned n_sys, const unsigned *row_off, const unsigned *off,
+                  const unsigned *col, const float *val, const float *rhs,
+                  float tol, unsigned max_iter, int one_by_one, float *x_out,
+                  unsigned *iters_out, float *resid_out, int *state_out,
+                  float *ms_out);
+
 /* The Schwarz aggregation on the host (schwarz/schwarz.cu:551-645): the graph
  * as a both-triangle CSR (n + 1 offsets, columns, one weight per entry: the
  * Frobenius norm of the block), aggregates of at most kmax matrix-connected

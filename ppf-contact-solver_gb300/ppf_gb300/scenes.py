@@ -140,6 +140,40 @@ def sphere_field(side: int = 1024, spheres: int = 50, seed: int = 0, dt: float =
     return sc.build(_param(dt)), None
 
 
+def cloth_drop(side: int, height: float, collider: str, size: float, dt: float = 0.01):
+    """One 1 m square sheet of side x side vertices whose lowest point starts
+    `height` above a fixed collider whose top is at y = 0: a sphere of radius
+    `size` (the reference's analytic sphere) or a cube of side `size` (a static
+    collision mesh). One scene of the batch of uneven drops."""
+    v, f = meshes.grid(side, side, 1.0, 1.0)
+    v[:, 1] = height
+    sc = Scene()
+    sc.add_shell(v, f, cloth_material())
+    if collider == "sphere":
+        sc.add_sphere((0.0, -size, 0.0), size, contact_gap=1e-3, friction=0.5)
+    else:
+        cv, cf = meshes.box(size, center=(0.0, -0.5 * size, 0.0))
+        sc.add_collision_mesh(cv, cf, contact_gap=1e-3, friction=0.5)
+    return sc.build(_param(dt)), None
+
+
+def uneven_drops(count: int = 256, seed: int = 0):
+    """The batch of uneven scenes: per scene a sheet side drawn log-uniformly
+    from 16 to 96 vertices, a drop height uniform in [0.2, 1.0] m, and a
+    collider drawn from a sphere of radius U(0.1, 0.4) m or a cube of side
+    U(0.2, 0.6) m (seeded). Returns the parameters, not built scenes."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        side = int(round(math.exp(rng.uniform(math.log(16), math.log(96)))))
+        height = float(rng.uniform(0.2, 1.0))
+        if rng.random() < 0.5:
+            out.append((side, height, "sphere", float(rng.uniform(0.1, 0.4))))
+        else:
+            out.append((side, height, "box", float(rng.uniform(0.2, 0.6))))
+    return out
+
+
 WORKLOADS = {
     "cloth_sphere": cloth_sphere,
     "stacked_sheets": stacked_sheets,

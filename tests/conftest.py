@@ -67,7 +67,9 @@ def _block_jacobi_after_each_test(request):
     yield
     if request.node.get_closest_marker("gpu") is None:
         return
+    import ctypes
+
     from ppf_gb300 import _lib
 
     if _lib._PRODUCT is not None:
-        _lib._PRODUCT.ppf_set_preconditioner(0, 0.0)
+        _lib._PRODUCT.ppf_set_preconditioner(ctypes.c_int(0), ctypes.c_float(0.0))

@@ -1,0 +1,137 @@
+"""Batched PCG over many independent systems (ppf_batch_pcg).
+
+CPU: the packed both-triangle layout is the system's operator.
+GPU: one launch over many systems gives each system the bits it gets alone;
+every system is solved to the tolerance, in the iterations a float64
+restatement of the same PCG takes; captured uneven drops all converge.
+"""
+import numpy as np
+import pytest
+
+import learned_cases
+from oracle import fsai as OF
+
+
+def _dense_from_packed(packed, s):
+    row_off, off, col, val, _ = packed
+    lo, hi = int(row_off[s]), int(row_off[s + 1])
+    n = hi - lo
+    A = np.zeros((3 * n, 3 * n))
+    for i in range(lo, hi):
+        for k in range(int(off[i]), int(off[i + 1])):
+            j = int(col[k]) - lo
+            A[3 * (i - lo):3 * (i - lo) + 3, 3 * j:3 * j + 3] = \
+                val[9 * k:9 * k + 9].reshape(3, 3).T
+    return A
+
+
+def _samples(seeds, n=300):
+    out = []
+    for k in seeds:
+        s = learned_cases.synthetic(n=n, seed=k)
+        A = OF.dense_operator(learned_cases.graph(s))
+        free = np.repeat(s["dof"] == 0, 3)
+        b = np.random.default_rng(k).normal(size=3 * n) * free
+        s["force"] = b.astype(np.float32)
+        s["A"] = A
+        out.append(s)
+    return out
+
+
+def _pcg_iters(A, b, tol=1e-3, maxit=10000):
+    """The PCG of the kernel in float64: x0 = 0, block-Jacobi, relative L1
+    residual checked at iterations 1, 5, 9, ... and every iteration once
+    below 8 tol."""
+    n = len(b) // 3
+    Pinv = np.zeros_like(A)
+    for i in range(n):
+        Pinv[3 * i:3 * i + 3, 3 * i:3 * i + 3] = np.linalg.inv(A[3 * i:3 * i + 3, 3 * i:3 * i + 3])
+    x = np.zeros_like(b)
+    r = b.copy()
+    z = Pinv @ r
+    p = z.copy()
+    rz = r @ z
+    err0 = np.abs(r).sum()
+    stride, nxt = 4, 1
+    for it in range(1, maxit + 1):
+        Ap = A @ p
+        a = rz / (p @ Ap)
+        x += a * p
+        r -= a * Ap
+        z = Pinv @ r
+        rz1 = r @ z
+        if it == nxt:
+            rr = np.abs(r).sum() / err0
+            if rr < tol:
+                return it
+            if rr < 8 * tol:
+                stride = 1
+            nxt = it + stride
+        p = z + rz1 / rz * p
+        rz = rz1
+    return maxit
+
+
+def test_packed_rows_are_the_operator():
+    from ppf_gb300 import batch
+
+    samples = _samples([1, 2, 3], n=60)
+    packed = batch.pack(samples)
+    assert packed[0].tolist() == [0, 60, 120, 180]
+    for s, smp in enumerate(samples):
+        np.testing.assert_allclose(_dense_from_packed(packed, s), smp["A"], rtol=0, atol=1e-6)
+        np.testing.assert_array_equal(packed[4][3 * 60 * s:3 * 60 * (s + 1)], smp["force"])
+
+
+@pytest.mark.gpu
+def test_batch_equals_one_launch_per_system(product_lib):
+    from ppf_gb300 import batch
+
+    samples = _samples(range(10, 16))
+    packed = batch.pack(samples)
+    a = batch.solve(packed)
+    b = batch.solve(packed, one_by_one=True)
+    assert np.array_equal(a["x"], b["x"])
+    assert np.array_equal(a["iters"], b["iters"])
+    # a system alone in its own batch
+    one = batch.solve(batch.pack(samples[2:3]))
+    assert np.array_equal(one["x"], a["x"][600:900]) and one["iters"][0] == a["iters"][2]
+
+
+@pytest.mark.gpu
+def test_batch_solves_every_system(product_lib):
+    from ppf_gb300 import batch
+
+    samples = _samples(range(20, 26))
+    packed = batch.pack(samples)
+    out = batch.solve(packed)
+    assert np.all(out["state"] == 0)
+    for s, smp in enumerate(samples):
+        x = out["x"][300 * s:300 * (s + 1)].reshape(-1).astype(np.float64)
+        b = smp["force"].astype(np.float64)
+        res = np.abs(b - smp["A"] @ x).sum() / np.abs(b).sum()
+        assert res < 2e-3, (s, res)
+        it = _pcg_iters(smp["A"], b)
+        assert abs(int(out["iters"][s]) - it) <= 4, (s, out["iters"][s], it)
+
+
+@pytest.mark.gpu
+def test_batch_of_captured_uneven_drops(product_lib):
+    """Newton systems the solver assembles for a few uneven drops (sphere and
+    box colliders, sides 16-40), solved in one launch."""
+    from ppf_gb300 import batch
+
+    params = [(16, 0.2, "sphere", 0.2), (24, 0.3, "box", 0.4), (40, 0.25, "sphere", 0.35),
+              (20, 0.2, "box", 0.3)]
+    samples = [batch.capture_drop(p) for p in params]
+    packed = batch.pack(samples)
+    out = batch.solve(packed)
+    assert np.all(out["state"] == 0), out["state"]
+    base = 0
+    for s, smp in enumerate(samples):
+        n = int(smp["n"])
+        x = out["x"][base:base + n].reshape(-1).astype(np.float64)
+        A = _dense_from_packed(packed, s)
+        b = smp["force"].astype(np.float64).reshape(-1)
+        assert np.abs(b - A @ x).sum() / np.abs(b).sum() < 2e-3
+        base += n
