@@ -11,6 +11,8 @@
 // converges on its own schedule and hundreds of uneven systems share one
 // launch. Rows are strided over the CTA's threads; sums fold in a fixed
 // order, so a system's result does not depend on the others in the launch.
+#include <algorithm>
+#include <numeric>
 #include <vector>
 
 #include "../../../include/ppf_gb300_ext.h"
@@ -18,9 +20,13 @@
 #include "common.cuh"
 #include "fatal.cuh"
 
+#include <cooperative_groups.h>
+
 namespace ppf {
 namespace gpu {
 namespace {
+
+namespace cg = cooperative_groups;
 
 constexpr unsigned kBT = 1024;
 constexpr float kSlack = 256.0f;
@@ -28,6 +34,7 @@ constexpr float kEps = 1.19209290e-7f;
 
 struct BatchArgs {
     unsigned base;             // first system of this launch
+    const unsigned *order;     // null, or the system of each CTA (largest first)
     const unsigned *row_off;   // systems + 1: vertex rows of each system
     const unsigned *off;       // rows + 1: both-triangle block rows
     const unsigned *col;       // global row of each block's column
@@ -57,35 +64,83 @@ __device__ __forceinline__ Mat3 ldm(const float *p) {
     return m;
 }
 
-// Block-wide sums of (a, b): every thread gets the same bits (warp sums,
-// then the 32 warp sums added in warp order by every thread).
-__device__ __forceinline__ float2 block_sum2(float a, float b, float2 *sh) {
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_xor_sync(0xffffffffu, a, o);
-        b += __shfl_xor_sync(0xffffffffu, b, o);
+// The team that solves one system: one CTA (kCluster false; block barriers)
+// or a thread-block cluster (kCluster true; cluster barriers and the CTAs'
+// partial sums read through distributed shared memory). Rows are strided
+// over the team's threads. Sums fold in a fixed order, so every thread of
+// the team gets the same bits.
+template <bool kCluster> struct Team {
+    unsigned rank = 0, size = 1;
+    __device__ Team() {
+        if (kCluster) {
+            cg::cluster_group cl = cg::this_cluster();
+            rank = cl.block_rank();
+            size = cl.num_blocks();
+        }
     }
-    if ((threadIdx.x & 31u) == 0) sh[threadIdx.x >> 5] = make_float2(a, b);
-    __syncthreads();
-    float2 t = make_float2(0.0f, 0.0f);
-    for (unsigned w = 0; w < kBT / 32; ++w) {
-        t.x += sh[w].x;
-        t.y += sh[w].y;
+    __device__ __forceinline__ void sync() const {
+        if (kCluster) cg::this_cluster().sync();
+        else __syncthreads();
     }
-    __syncthreads();
-    return t;
-}
+    __device__ __forceinline__ unsigned first(unsigned lo) const {
+        return lo + rank * kBT + threadIdx.x;
+    }
+    __device__ __forceinline__ unsigned stride() const { return size * kBT; }
+    // a vector entry another thread of the team may have written: through L2
+    // when that thread can sit on another SM
+    __device__ __forceinline__ Vec3 ld_shared_vec(const float *v, unsigned i) const {
+        if (kCluster) return vec3(__ldcg(v + 3 * i), __ldcg(v + 3 * i + 1), __ldcg(v + 3 * i + 2));
+        return vec3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+    }
+    // team-wide (a, b); `part` is a double-buffered per-CTA slot, `k` the
+    // buffer (alternating between calls, so one barrier per sum suffices)
+    __device__ float2 sum2(float a, float b, float2 *sh, float2 *part, unsigned k) const {
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+        if ((threadIdx.x & 31u) == 0) sh[threadIdx.x >> 5] = make_float2(a, b);
+        __syncthreads();
+        float2 t = make_float2(0.0f, 0.0f);
+        for (unsigned w = 0; w < kBT / 32; ++w) {
+            t.x += sh[w].x;
+            t.y += sh[w].y;
+        }
+        if (!kCluster) {
+            __syncthreads();
+            return t;
+        }
+        if (threadIdx.x == 0) part[k] = t;
+        cg::cluster_group cl = cg::this_cluster();
+        cl.sync();
+        float2 u = make_float2(0.0f, 0.0f);
+        for (unsigned r = 0; r < size; ++r) {
+            const float2 v = *cl.map_shared_rank(part + k, r);
+            u.x += v.x;
+            u.y += v.y;
+        }
+        return u;
+    }
+};
 
+// One system per team: team t (CTA, or cluster of CTAs) takes system
+// order[t] (base + t without an order).
+template <bool kCluster>
 __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
     __shared__ float2 sh[kBT / 32];
-    const unsigned s = g.base + blockIdx.x;
+    __shared__ float2 part[2];
+    const Team<kCluster> team;
+    const unsigned t_idx = blockIdx.x / team.size;
+    const unsigned s = g.order ? __ldg(g.order + t_idx) : g.base + t_idx;
     const unsigned lo = __ldg(g.row_off + s), hi = __ldg(g.row_off + s + 1);
-    const unsigned tid = threadIdx.x;
+    const unsigned i0 = team.first(lo), di = team.stride();
+    unsigned k = 0;
     // x0 = 0, r = b, block-Jacobi inverse, z = P r, p = z
     float a = 0.0f, e = 0.0f;
-    for (unsigned i = lo + tid; i < hi; i += kBT) {
+    for (unsigned i = i0; i < hi; i += di) {
         Mat3 d = Mat3::identity();
-        for (unsigned k = __ldg(g.off + i), k1 = __ldg(g.off + i + 1); k < k1; ++k)
-            if (__ldg(g.col + k) == i) d = ldm(g.val + 9 * (size_t)k);
+        for (unsigned q = __ldg(g.off + i), q1 = __ldg(g.off + i + 1); q < q1; ++q)
+            if (__ldg(g.col + q) == i) d = ldm(g.val + 9 * (size_t)q);
         Mat3 P;
         if (!eig::invert_spd(d, P)) P = Mat3::identity();
 #pragma unroll
@@ -99,15 +154,17 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
         a += bi.dot(zi);
         e += fabsf(bi[0]) + fabsf(bi[1]) + fabsf(bi[2]);
     }
-    float2 t = block_sum2(a, e, sh);
+    float2 t = team.sum2(a, e, sh, part, k);
+    k ^= 1u;
     float rz = t.x;
     const float err0 = t.y;
     if (err0 == 0.0f) {
-        if (tid == 0) {
+        if (team.rank == 0 && threadIdx.x == 0) {
             g.iters[s] = 0;
             g.resid[s] = 0.0f;
             g.state[s] = 0;
         }
+        team.sync(); // no CTA leaves while another may still read its partials
         return;
     }
     unsigned stride = 4, next_check = 1;
@@ -115,11 +172,11 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
     for (unsigned iter = 1;; ++iter) {
         // A p, p^T A p and its round-off scale
         a = e = 0.0f;
-        for (unsigned i = lo + tid; i < hi; i += kBT) {
+        for (unsigned i = i0; i < hi; i += di) {
             Vec3 acc = Vec3::zero(), ab = Vec3::zero();
-            for (unsigned k = __ldg(g.off + i), k1 = __ldg(g.off + i + 1); k < k1; ++k) {
-                const float *m = g.val + 9 * (size_t)k;
-                const Vec3 v = ld3(g.p, __ldg(g.col + k));
+            for (unsigned q = __ldg(g.off + i), q1 = __ldg(g.off + i + 1); q < q1; ++q) {
+                const float *m = g.val + 9 * (size_t)q;
+                const Vec3 v = team.ld_shared_vec(g.p, __ldg(g.col + q));
                 Vec3 term;
                 term[0] = __ldg(m + 0) * v[0] + __ldg(m + 3) * v[1] + __ldg(m + 6) * v[2];
                 term[1] = __ldg(m + 1) * v[0] + __ldg(m + 4) * v[1] + __ldg(m + 7) * v[2];
@@ -132,7 +189,8 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
             a += pi.dot(acc);
             e += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] + fabsf(pi[2]) * ab[2];
         }
-        t = block_sum2(a, e, sh);
+        t = team.sum2(a, e, sh, part, k);
+        k ^= 1u;
         const float pAp = t.x, bound = kSlack * kEps * t.y;
         float alpha = 0.0f;
         if (pAp > bound) {
@@ -140,9 +198,9 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
         } else if (!broke) {
             broke = (pAp < -bound || pAp != pAp) ? 1 : 3;
         }
-        // x += alpha p, r -= alpha A p, z = P r
+        // x += alpha p, r -= alpha A p, z = P r (rows of this thread only)
         a = e = 0.0f;
-        for (unsigned i = lo + tid; i < hi; i += kBT) {
+        for (unsigned i = i0; i < hi; i += di) {
             Vec3 xi = ld3(g.x, i), ri = ld3(g.r, i);
             const Vec3 pi = ld3(g.p, i), api = ld3(g.Ap, i);
             for (int c = 0; c < 3; ++c) {
@@ -159,7 +217,8 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
             a += ri.dot(zi);
             e += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
         }
-        t = block_sum2(a, e, sh);
+        t = team.sum2(a, e, sh, part, k);
+        k ^= 1u;
         const float rz_new = t.x, err_now = t.y;
         const float beta = rz_new / rz;
         rz = rz_new;
@@ -172,22 +231,23 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
             else if (broke == 1) st = 2;
             else if (!isfinite(reresid) || at_cap) st = 2;
             if (st >= 0) {
-                if (tid == 0) {
+                if (team.rank == 0 && threadIdx.x == 0) {
                     g.iters[s] = iter;
                     g.resid[s] = reresid;
                     g.state[s] = st;
                 }
+                team.sync();
                 return;
             }
             if (reresid < 8.0f * g.tol) stride = 1;
             next_check = iter + stride;
         }
-        // p = z + beta p
-        for (unsigned i = lo + tid; i < hi; i += kBT) {
+        // p = z + beta p, then the whole team sees the new p
+        for (unsigned i = i0; i < hi; i += di) {
             const Vec3 zi = ld3(g.z, i), pi = ld3(g.p, i);
             st3v(g.p, i, zi + beta * pi);
         }
-        __syncthreads();
+        team.sync();
     }
 }
 
@@ -199,6 +259,32 @@ template <class T> struct Dev {
     }
     ~Dev() { cudaFree(d); }
 };
+
+constexpr unsigned kClusterCtas = 8;     // CTAs of a large system's cluster
+constexpr unsigned kLargeRows = 2 * kBT; // systems above this many rows take a cluster
+
+void launch_single(const BatchArgs &g, unsigned systems, cudaStream_t q) {
+    if (!systems) return;
+    k_batch_pcg<false><<<systems, kBT, 0, q>>>(g);
+    PPF_LAUNCH_CHECK();
+}
+
+void launch_clusters(const BatchArgs &g, unsigned systems, cudaStream_t q) {
+    if (!systems) return;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(systems * kClusterCtas);
+    cfg.blockDim = dim3(kBT);
+    cfg.stream = q;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PPF_CUDA(cudaLaunchKernelEx(&cfg, k_batch_pcg<true>, g));
+    ++g_kernel_launches;
+}
 
 } // namespace
 } // namespace gpu
@@ -223,28 +309,56 @@ extern "C" int ppf_batch_pcg(unsigned n_sys, const unsigned *row_off, const unsi
         Dev<unsigned> it(n_sys);
         Dev<float> res(n_sys);
         Dev<int> st(n_sys);
-        BatchArgs g{0u,   d_row.d, d_off.d, d_col.d, d_val.d, d_b.d, x.d, r.d,   z.d,  p.d,
-                    Ap.d, inv.d,   tol,     max_iter, it.d,   res.d, st.d};
-        cudaEvent_t e0, e1;
+        // small systems take one CTA each, large ones a cluster of CTAs; each
+        // class largest first (by blocks), so the long solves start first
+        std::vector<unsigned> small, large;
+        for (unsigned s = 0; s < n_sys; ++s)
+            (row_off[s + 1] - row_off[s] > kLargeRows ? large : small).push_back(s);
+        auto by_size = [&](unsigned a, unsigned b) {
+            return off[row_off[a + 1]] - off[row_off[a]] > off[row_off[b + 1]] - off[row_off[b]];
+        };
+        std::stable_sort(small.begin(), small.end(), by_size);
+        std::stable_sort(large.begin(), large.end(), by_size);
+        std::vector<unsigned> order(small);
+        order.insert(order.end(), large.begin(), large.end());
+        Dev<unsigned> d_order(n_sys, order.data());
+        BatchArgs g{0u,   nullptr, d_row.d, d_off.d, d_col.d, d_val.d, d_b.d, x.d, r.d,  z.d,
+                    p.d,  Ap.d,    inv.d,   tol,     max_iter, it.d,   res.d, st.d};
+        cudaStream_t qs, ql;
+        PPF_CUDA(cudaStreamCreateWithFlags(&qs, cudaStreamNonBlocking));
+        PPF_CUDA(cudaStreamCreateWithFlags(&ql, cudaStreamNonBlocking));
+        cudaEvent_t e0, e1, es, el;
         PPF_CUDA(cudaEventCreate(&e0));
         PPF_CUDA(cudaEventCreate(&e1));
-        PPF_CUDA(cudaEventRecord(e0, 0));
+        PPF_CUDA(cudaEventCreateWithFlags(&es, cudaEventDisableTiming));
+        PPF_CUDA(cudaEventCreateWithFlags(&el, cudaEventDisableTiming));
+        PPF_CUDA(cudaDeviceSynchronize());
+        PPF_CUDA(cudaEventRecord(e0, qs));
+        PPF_CUDA(cudaStreamWaitEvent(ql, e0, 0));
         if (one_by_one) {
-            for (unsigned s = 0; s < n_sys; ++s) {
-                g.base = s;
-                k_batch_pcg<<<1, kBT>>>(g);
-                PPF_LAUNCH_CHECK();
+            // one launch per system, each with its own team kind
+            for (unsigned k = 0; k < n_sys; ++k) {
+                BatchArgs h = g;
+                h.order = d_order.d + k;
+                if (k < small.size()) launch_single(h, 1, qs);
+                else launch_clusters(h, 1, qs);
             }
         } else {
-            k_batch_pcg<<<n_sys, kBT>>>(g);
-            PPF_LAUNCH_CHECK();
+            BatchArgs hs = g, hl = g;
+            hs.order = d_order.d;
+            hl.order = d_order.d + small.size();
+            launch_clusters(hl, (unsigned)large.size(), ql);
+            launch_single(hs, (unsigned)small.size(), qs);
         }
-        PPF_CUDA(cudaEventRecord(e1, 0));
+        PPF_CUDA(cudaEventRecord(el, ql));
+        PPF_CUDA(cudaStreamWaitEvent(qs, el, 0));
+        PPF_CUDA(cudaEventRecord(e1, qs));
         PPF_CUDA(cudaEventSynchronize(e1));
         float ms = 0.0f;
         PPF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        for (cudaEvent_t ev : {e0, e1, es, el}) cudaEventDestroy(ev);
+        cudaStreamDestroy(qs);
+        cudaStreamDestroy(ql);
         if (ms_out) *ms_out = ms;
         if (x_out)
             PPF_CUDA(cudaMemcpy(x_out, x.d, 3 * (size_t)rows * sizeof(float),

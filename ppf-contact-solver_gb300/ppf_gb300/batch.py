@@ -137,6 +137,11 @@ def bench_main(argv=None):
     single = min((solve(packed, one_by_one=True) for _ in range(a.reps)), key=lambda r: r["ms"])
     same = bool(np.array_equal(batched["x"], single["x"]) and
                 np.array_equal(batched["iters"], single["iters"]))
+    # the largest system alone: the floor of a batch whose systems each run
+    # on one CTA
+    big = int(np.argmax([int(packed[1][packed[0][k + 1]] - packed[1][packed[0][k]])
+                         for k in range(a.count)]))
+    alone = min(solve(pack(samples[big:big + 1]))["ms"] for _ in range(a.reps))
     it = np.sort(batched["iters"])
     verts = [int(s["n"]) for s in samples]
     out = {
@@ -147,6 +152,9 @@ def bench_main(argv=None):
         "vertices_min_max": [min(verts), max(verts)], "blocks": int(packed[1][-1]),
         "batched_ms": round(batched["ms"], 3), "one_launch_per_system_ms": round(single["ms"], 3),
         "speedup": round(single["ms"] / batched["ms"], 2),
+        "largest_system_alone_ms": round(alone, 3),
+        "largest_system": {"vertices": int(samples[big]["n"]),
+                           "pcg_iters": int(batched["iters"][big])},
         "systems_per_s": round(a.count / (batched["ms"] / 1e3), 1),
         "pcg_iters_median": int(it[len(it) // 2]), "pcg_iters_p90": int(it[int(0.9 * len(it))]),
         "pcg_iters_max": int(it[-1]), "converged": int((batched["state"] == 0).sum()),

@@ -99,6 +99,28 @@ def test_batch_equals_one_launch_per_system(product_lib):
 
 
 @pytest.mark.gpu
+def test_cluster_teams_for_large_systems(product_lib):
+    """Systems above 2,048 vertices run on clusters of CTAs (partial sums
+    through distributed shared memory): a batch mixing them with small ones
+    gives every system the bits it gets alone, and solves it."""
+    from ppf_gb300 import batch
+
+    samples = _samples([31], n=300) + _samples([32], n=3000) + _samples([33], n=5000)
+    packed = batch.pack(samples)
+    a = batch.solve(packed)
+    b = batch.solve(packed, one_by_one=True)
+    assert np.array_equal(a["x"], b["x"]) and np.array_equal(a["iters"], b["iters"])
+    assert np.all(a["state"] == 0)
+    base = 0
+    for s, smp in enumerate(samples):
+        n = int(smp["n"])
+        x = a["x"][base:base + n].reshape(-1).astype(np.float64)
+        bb = smp["force"].astype(np.float64)
+        assert np.abs(bb - smp["A"] @ x).sum() / np.abs(bb).sum() < 2e-3
+        base += n
+
+
+@pytest.mark.gpu
 def test_batch_solves_every_system(product_lib):
     from ppf_gb300 import batch
 
