@@ -204,15 +204,36 @@ unsigned ppf_learned_tc_status(void);
  *             system; val: 9 column-major floats per block)
  *   rhs       3 floats per row
  *   one_by_one  nonzero: one launch per system instead (for comparison)
+ * A system's team is one CTA or a thread-block cluster of 2 to 16 CTAs,
+ * chosen by its size bucket (ppf_batch_team_ctas); systems of one team size
+ * share one launch, the launches run on concurrent streams.
  * Host memory in and out (any output may be NULL): x (3 per row), the
  * iterations, relative residual and state (0 converged, 1 truncated, 2
  * failed) per system, and the device time of the launch(es) in ms.
- * Returns 0, or -1 for an invalid batch. */
+ * Returns 0, or -1 for an invalid batch (a column outside its system's rows
+ * included). */
 int ppf_batch_pcg(unsigned n_sys, const unsigned *row_off, const unsigned *off,
                   const unsigned *col, const float *val, const float *rhs,
                   float tol, unsigned max_iter, int one_by_one, float *x_out,
                   unsigned *iters_out, float *resid_out, int *state_out,
                   float *ms_out);
+/* The team size (CTAs; 1, 2, 4, 8 or 16) of each of the 5 system-size
+ * buckets: at most 1024, 2048, 4096, 8192 rows, and more. set = 0 reads the
+ * table into table[5], set != 0 replaces it (-1 for a size not listed).
+ * Defaults: 1, 1, 8, 8, 8. */
+int ppf_batch_team_ctas(unsigned *table, int set);
+/* The autotuner of the batched PCG: for every size bucket present in the
+ * batch (layout as ppf_batch_pcg), solves all of the bucket's systems in one
+ * launch with teams of 1, 2, 4, 8 and 16 CTAs (sizes that would leave half
+ * the team idle on the bucket's largest system, and cluster sizes the device
+ * cannot schedule, are skipped), three times each, and keeps the fastest in
+ * the table that ppf_batch_pcg uses. Writes
+ * the table to table_out[5] and the best time of each (bucket, size) to
+ * ms_out[5 * 5] (-1 where not tried; both may be NULL). Returns 0 or -1. */
+int ppf_batch_autotune(unsigned n_sys, const unsigned *row_off, const unsigned *off,
+                       const unsigned *col, const float *val, const float *rhs,
+                       float tol, unsigned max_iter, unsigned *table_out,
+                       float *ms_out);
 
 /* The Schwarz aggregation on the host (schwarz/schwarz.cu:551-645): the graph
  * as a both-triangle CSR (n + 1 offsets, columns, one weight per entry: the

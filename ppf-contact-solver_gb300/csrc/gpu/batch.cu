@@ -260,115 +260,252 @@ template <class T> struct Dev {
     ~Dev() { cudaFree(d); }
 };
 
-constexpr unsigned kClusterCtas = 8;     // CTAs of a large system's cluster
-constexpr unsigned kLargeRows = 2 * kBT; // systems above this many rows take a cluster
+// Team size (CTAs) per system-size bucket: rows <= 1024, <= 2048, <= 4096,
+// <= 8192, more. Defaults: one CTA up to 2,048 rows, clusters of 8 above;
+// ppf_batch_autotune replaces them with measured choices.
+constexpr unsigned kBuckets = 5;
+unsigned g_team_ctas[kBuckets] = {1, 1, 8, 8, 8};
 
-void launch_single(const BatchArgs &g, unsigned systems, cudaStream_t q) {
-    if (!systems) return;
-    k_batch_pcg<false><<<systems, kBT, 0, q>>>(g);
-    PPF_LAUNCH_CHECK();
+unsigned bucket_of(unsigned rows) {
+    unsigned b = 0;
+    for (unsigned lim = kBT; b + 1 < kBuckets && rows > lim; lim *= 2) ++b;
+    return b;
 }
 
-void launch_clusters(const BatchArgs &g, unsigned systems, cudaStream_t q) {
-    if (!systems) return;
+// One launch of `systems` teams of `ctas` CTAs (ctas == 1: plain CTAs, else
+// thread-block clusters). Returns the launch's error instead of throwing, so
+// a cluster size the device cannot schedule is just a failed candidate.
+cudaError_t launch_teams(const BatchArgs &g, unsigned systems, unsigned ctas, cudaStream_t q) {
+    if (!systems) return cudaSuccess;
+    if (ctas == 1) {
+        k_batch_pcg<false><<<systems, kBT, 0, q>>>(g);
+        ++g_kernel_launches;
+        return cudaGetLastError();
+    }
+    static bool non_portable = false;
+    if (ctas > 8 && !non_portable) {
+        cudaError_t e = cudaFuncSetAttribute(k_batch_pcg<true>,
+                                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+        non_portable = true;
+    }
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(systems * kClusterCtas);
+    cfg.gridDim = dim3(systems * ctas);
     cfg.blockDim = dim3(kBT);
     cfg.stream = q;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.x = ctas;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    PPF_CUDA(cudaLaunchKernelEx(&cfg, k_batch_pcg<true>, g));
     ++g_kernel_launches;
+    return cudaLaunchKernelEx(&cfg, k_batch_pcg<true>, g);
+}
+
+// A batch uploaded to the device, with its work buffers.
+struct DeviceBatch {
+    unsigned n_sys, rows, blocks;
+    Dev<unsigned> row, off, col, it;
+    Dev<float> val, b, x, r, z, p, Ap, inv, res;
+    Dev<int> st;
+    DeviceBatch(unsigned n, const unsigned *row_off, const unsigned *h_off,
+                const unsigned *h_col, const float *h_val, const float *rhs)
+        : n_sys(n), rows(row_off[n]), blocks(h_off[row_off[n]]), row(n + 1, row_off),
+          off(rows + 1, h_off), col(blocks, h_col), it(n), val(9 * (size_t)blocks, h_val),
+          b(3 * (size_t)rows, rhs), x(3 * (size_t)rows), r(3 * (size_t)rows),
+          z(3 * (size_t)rows), p(3 * (size_t)rows), Ap(3 * (size_t)rows),
+          inv(9 * (size_t)rows), res(n), st(n) {}
+    BatchArgs args(float tol, unsigned max_iter) const {
+        return BatchArgs{0u,  nullptr, row.d, off.d, col.d,    val.d, b.d,   x.d, r.d,
+                         z.d, p.d,     Ap.d,  inv.d, tol, max_iter, it.d, res.d, st.d};
+    }
+};
+
+// Runs the systems of `order` (device array: group after group, each group
+// largest first) as consecutive groups of (count, team CTAs), one stream per
+// group, or one launch per system; returns the device time in ms.
+float run_groups(const BatchArgs &g0, const unsigned *d_order,
+                 const std::vector<std::pair<unsigned, unsigned>> &groups, bool one_by_one) {
+    std::vector<cudaStream_t> qs(groups.size() + 1);
+    for (auto &q : qs) PPF_CUDA(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+    cudaEvent_t e0, e1;
+    PPF_CUDA(cudaEventCreate(&e0));
+    PPF_CUDA(cudaEventCreate(&e1));
+    std::vector<cudaEvent_t> done(groups.size());
+    for (auto &e : done) PPF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PPF_CUDA(cudaDeviceSynchronize());
+    PPF_CUDA(cudaEventRecord(e0, qs[0]));
+    unsigned first = 0;
+    cudaError_t err = cudaSuccess;
+    for (size_t k = 0; k < groups.size(); ++k) {
+        cudaStream_t q = one_by_one ? qs[0] : qs[k + 1];
+        if (!one_by_one) PPF_CUDA(cudaStreamWaitEvent(q, e0, 0));
+        BatchArgs g = g0;
+        if (one_by_one) {
+            for (unsigned j = 0; j < groups[k].first && err == cudaSuccess; ++j) {
+                g.order = d_order + first + j;
+                err = launch_teams(g, 1, groups[k].second, q);
+            }
+        } else {
+            g.order = d_order + first;
+            err = launch_teams(g, groups[k].first, groups[k].second, q);
+        }
+        first += groups[k].first;
+        PPF_CUDA(cudaEventRecord(done[k], q));
+        PPF_CUDA(cudaStreamWaitEvent(qs[0], done[k], 0));
+    }
+    PPF_CUDA(cudaEventRecord(e1, qs[0]));
+    PPF_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    PPF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (auto &e : done) cudaEventDestroy(e);
+    for (auto &q : qs) cudaStreamDestroy(q);
+    if (err != cudaSuccess) return -1.0f;
+    return ms;
 }
 
 } // namespace
 } // namespace gpu
 } // namespace ppf
 
+namespace {
+using namespace ppf::gpu;
+
+bool valid_batch(unsigned n_sys, const unsigned *row_off, const unsigned *off,
+                 const unsigned *col, const float *val, const float *rhs) {
+    if (!n_sys || !row_off || !off || !col || !val || !rhs) return false;
+    for (unsigned s = 0; s < n_sys; ++s)
+        if (row_off[s + 1] < row_off[s]) return false;
+    const unsigned rows = row_off[n_sys];
+    for (unsigned s = 0; s < n_sys; ++s)
+        for (unsigned i = row_off[s]; i < row_off[s + 1]; ++i) {
+            if (off[i + 1] < off[i]) return false;
+            for (unsigned k = off[i]; k < off[i + 1]; ++k)
+                if (col[k] < row_off[s] || col[k] >= row_off[s + 1] || col[k] >= rows)
+                    return false;
+        }
+    return true;
+}
+
+// Systems grouped by the team size of their bucket, each group largest
+// first (by blocks): the order and the (count, CTAs) of each group.
+void group_systems(unsigned n_sys, const unsigned *row_off, const unsigned *off,
+                   std::vector<unsigned> &order,
+                   std::vector<std::pair<unsigned, unsigned>> &groups) {
+    order.clear();
+    groups.clear();
+    const unsigned sizes[] = {1, 2, 4, 8, 16};
+    for (unsigned c : sizes) {
+        std::vector<unsigned> g;
+        for (unsigned s = 0; s < n_sys; ++s)
+            if (g_team_ctas[bucket_of(row_off[s + 1] - row_off[s])] == c) g.push_back(s);
+        if (g.empty()) continue;
+        std::stable_sort(g.begin(), g.end(), [&](unsigned a, unsigned b) {
+            return off[row_off[a + 1]] - off[row_off[a]] > off[row_off[b + 1]] - off[row_off[b]];
+        });
+        order.insert(order.end(), g.begin(), g.end());
+        groups.emplace_back((unsigned)g.size(), c);
+    }
+}
+} // namespace
+
 extern "C" int ppf_batch_pcg(unsigned n_sys, const unsigned *row_off, const unsigned *off,
                              const unsigned *col, const float *val, const float *rhs, float tol,
                              unsigned max_iter, int one_by_one, float *x_out,
                              unsigned *iters_out, float *resid_out, int *state_out,
                              float *ms_out) {
-    using namespace ppf::gpu;
     try {
-        if (!n_sys || !row_off || !off || !col || !val || !rhs) return -1;
-        const unsigned rows = row_off[n_sys];
-        const unsigned blocks = off[rows];
-        for (unsigned k = 0; k < blocks; ++k)
-            if (col[k] >= rows) return -1;
-        Dev<unsigned> d_row(n_sys + 1, row_off), d_off(rows + 1, off), d_col(blocks, col);
-        Dev<float> d_val(9 * (size_t)blocks, val), d_b(3 * (size_t)rows, rhs);
-        Dev<float> x(3 * (size_t)rows), r(3 * (size_t)rows), z(3 * (size_t)rows),
-            p(3 * (size_t)rows), Ap(3 * (size_t)rows), inv(9 * (size_t)rows);
-        Dev<unsigned> it(n_sys);
-        Dev<float> res(n_sys);
-        Dev<int> st(n_sys);
-        // small systems take one CTA each, large ones a cluster of CTAs; each
-        // class largest first (by blocks), so the long solves start first
-        std::vector<unsigned> small, large;
-        for (unsigned s = 0; s < n_sys; ++s)
-            (row_off[s + 1] - row_off[s] > kLargeRows ? large : small).push_back(s);
-        auto by_size = [&](unsigned a, unsigned b) {
-            return off[row_off[a + 1]] - off[row_off[a]] > off[row_off[b + 1]] - off[row_off[b]];
-        };
-        std::stable_sort(small.begin(), small.end(), by_size);
-        std::stable_sort(large.begin(), large.end(), by_size);
-        std::vector<unsigned> order(small);
-        order.insert(order.end(), large.begin(), large.end());
+        if (!valid_batch(n_sys, row_off, off, col, val, rhs)) return -1;
+        DeviceBatch B(n_sys, row_off, off, col, val, rhs);
+        std::vector<unsigned> order;
+        std::vector<std::pair<unsigned, unsigned>> groups;
+        group_systems(n_sys, row_off, off, order, groups);
         Dev<unsigned> d_order(n_sys, order.data());
-        BatchArgs g{0u,   nullptr, d_row.d, d_off.d, d_col.d, d_val.d, d_b.d, x.d, r.d,  z.d,
-                    p.d,  Ap.d,    inv.d,   tol,     max_iter, it.d,   res.d, st.d};
-        cudaStream_t qs, ql;
-        PPF_CUDA(cudaStreamCreateWithFlags(&qs, cudaStreamNonBlocking));
-        PPF_CUDA(cudaStreamCreateWithFlags(&ql, cudaStreamNonBlocking));
-        cudaEvent_t e0, e1, es, el;
-        PPF_CUDA(cudaEventCreate(&e0));
-        PPF_CUDA(cudaEventCreate(&e1));
-        PPF_CUDA(cudaEventCreateWithFlags(&es, cudaEventDisableTiming));
-        PPF_CUDA(cudaEventCreateWithFlags(&el, cudaEventDisableTiming));
-        PPF_CUDA(cudaDeviceSynchronize());
-        PPF_CUDA(cudaEventRecord(e0, qs));
-        PPF_CUDA(cudaStreamWaitEvent(ql, e0, 0));
-        if (one_by_one) {
-            // one launch per system, each with its own team kind
-            for (unsigned k = 0; k < n_sys; ++k) {
-                BatchArgs h = g;
-                h.order = d_order.d + k;
-                if (k < small.size()) launch_single(h, 1, qs);
-                else launch_clusters(h, 1, qs);
-            }
-        } else {
-            BatchArgs hs = g, hl = g;
-            hs.order = d_order.d;
-            hl.order = d_order.d + small.size();
-            launch_clusters(hl, (unsigned)large.size(), ql);
-            launch_single(hs, (unsigned)small.size(), qs);
-        }
-        PPF_CUDA(cudaEventRecord(el, ql));
-        PPF_CUDA(cudaStreamWaitEvent(qs, el, 0));
-        PPF_CUDA(cudaEventRecord(e1, qs));
-        PPF_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.0f;
-        PPF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        for (cudaEvent_t ev : {e0, e1, es, el}) cudaEventDestroy(ev);
-        cudaStreamDestroy(qs);
-        cudaStreamDestroy(ql);
+        const float ms = run_groups(B.args(tol, max_iter), d_order.d, groups, one_by_one != 0);
+        if (ms < 0.0f) return -1;
         if (ms_out) *ms_out = ms;
+        const unsigned rows = B.rows;
         if (x_out)
-            PPF_CUDA(cudaMemcpy(x_out, x.d, 3 * (size_t)rows * sizeof(float),
+            PPF_CUDA(cudaMemcpy(x_out, B.x.d, 3 * (size_t)rows * sizeof(float),
                                 cudaMemcpyDeviceToHost));
         if (iters_out)
-            PPF_CUDA(cudaMemcpy(iters_out, it.d, n_sys * sizeof(unsigned), cudaMemcpyDeviceToHost));
+            PPF_CUDA(cudaMemcpy(iters_out, B.it.d, n_sys * sizeof(unsigned), cudaMemcpyDeviceToHost));
         if (resid_out)
-            PPF_CUDA(cudaMemcpy(resid_out, res.d, n_sys * sizeof(float), cudaMemcpyDeviceToHost));
+            PPF_CUDA(cudaMemcpy(resid_out, B.res.d, n_sys * sizeof(float), cudaMemcpyDeviceToHost));
         if (state_out)
-            PPF_CUDA(cudaMemcpy(state_out, st.d, n_sys * sizeof(int), cudaMemcpyDeviceToHost));
+            PPF_CUDA(cudaMemcpy(state_out, B.st.d, n_sys * sizeof(int), cudaMemcpyDeviceToHost));
+        return 0;
+    } catch (const ppf::FatalError &) {
+        return -1;
+    }
+}
+
+extern "C" int ppf_batch_team_ctas(unsigned *table, int set) {
+    if (!table) return -1;
+    if (set) {
+        for (unsigned b = 0; b < kBuckets; ++b)
+            if (table[b] != 1 && table[b] != 2 && table[b] != 4 && table[b] != 8 &&
+                table[b] != 16)
+                return -1;
+        for (unsigned b = 0; b < kBuckets; ++b) g_team_ctas[b] = table[b];
+    } else {
+        for (unsigned b = 0; b < kBuckets; ++b) table[b] = g_team_ctas[b];
+    }
+    return 0;
+}
+
+extern "C" int ppf_batch_autotune(unsigned n_sys, const unsigned *row_off, const unsigned *off,
+                                  const unsigned *col, const float *val, const float *rhs,
+                                  float tol, unsigned max_iter, unsigned *table_out,
+                                  float *ms_out) {
+    try {
+        if (!valid_batch(n_sys, row_off, off, col, val, rhs)) return -1;
+        DeviceBatch B(n_sys, row_off, off, col, val, rhs);
+        const BatchArgs g = B.args(tol, max_iter);
+        for (unsigned b = 0; b < kBuckets; ++b) {
+            // all of the bucket's systems, largest first, in one launch per
+            // candidate: the team size that solves the bucket's population
+            // fastest (throughput, as the systems share the GPU in a batch)
+            std::vector<unsigned> members;
+            unsigned largest_rows = 0;
+            for (unsigned s = 0; s < n_sys; ++s)
+                if (bucket_of(row_off[s + 1] - row_off[s]) == b) {
+                    members.push_back(s);
+                    largest_rows = std::max(largest_rows, row_off[s + 1] - row_off[s]);
+                }
+            if (members.empty()) continue;
+            std::stable_sort(members.begin(), members.end(), [&](unsigned a, unsigned c) {
+                return off[row_off[a + 1]] - off[row_off[a]] > off[row_off[c + 1]] - off[row_off[c]];
+            });
+            Dev<unsigned> d_order(members.size(), members.data());
+            const unsigned count = (unsigned)members.size();
+            unsigned pick = g_team_ctas[b];
+            float pick_ms = -1.0f;
+            for (unsigned c : {1u, 2u, 4u, 8u, 16u}) {
+                if (c > 1 && (c / 2) * kBT >= largest_rows) break; // half the team would idle
+                float t = -1.0f;
+                for (int rep = 0; rep < 3; ++rep) {
+                    const float m = run_groups(g, d_order.d, {{count, c}}, false);
+                    if (m < 0.0f) {
+                        t = -1.0f;
+                        break;
+                    }
+                    t = t < 0.0f ? m : std::min(t, m);
+                }
+                if (ms_out) ms_out[b * 5 + (c == 1 ? 0 : c == 2 ? 1 : c == 4 ? 2 : c == 8 ? 3 : 4)] = t;
+                if (t >= 0.0f && (pick_ms < 0.0f || t < pick_ms)) {
+                    pick = c;
+                    pick_ms = t;
+                }
+            }
+            g_team_ctas[b] = pick;
+        }
+        if (table_out)
+            for (unsigned b = 0; b < kBuckets; ++b) table_out[b] = g_team_ctas[b];
         return 0;
     } catch (const ppf::FatalError &) {
         return -1;

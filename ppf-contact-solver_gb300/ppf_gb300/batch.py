@@ -35,7 +35,40 @@ def _declare(lib):
                                   C.c_int, f32p_opt, np.ctypeslib.ndpointer(np.uint32, flags="C"),
                                   f32p_opt, np.ctypeslib.ndpointer(np.int32, flags="C"),
                                   C.POINTER(C.c_float)]
+    lib.ppf_batch_team_ctas.restype = C.c_int
+    lib.ppf_batch_team_ctas.argtypes = [u32p, C.c_int]
+    lib.ppf_batch_autotune.restype = C.c_int
+    lib.ppf_batch_autotune.argtypes = [C.c_uint, u32p, u32p, u32p, f32p, f32p, C.c_float,
+                                       C.c_uint, u32p, f32p]
     _declared.add(id(lib))
+
+
+BUCKETS = ("<=1024 rows", "<=2048", "<=4096", "<=8192", ">8192")
+TEAM_SIZES = (1, 2, 4, 8, 16)
+
+
+def team_ctas(table=None):
+    """The team size per size bucket (reads it; with `table`, sets it)."""
+    lib = product()
+    _declare(lib)
+    t = np.zeros(5, np.uint32) if table is None else np.ascontiguousarray(table, np.uint32)
+    if lib.ppf_batch_team_ctas(t, 0 if table is None else 1) != 0:
+        raise ValueError("invalid team sizes")
+    return t
+
+
+def autotune(packed, tol: float = 1e-3, max_iter: int = 10000):
+    """Measures each team size on all of the batch's systems of a size bucket
+    at once and keeps the fastest per bucket; returns (table, ms[5, 5])."""
+    lib = product()
+    _declare(lib)
+    row_off, off, col, val, rhs = packed
+    table = np.zeros(5, np.uint32)
+    ms = np.full(25, -1.0, np.float32)
+    if lib.ppf_batch_autotune(len(row_off) - 1, row_off, off, col, val, rhs, tol, max_iter,
+                              table, ms) != 0:
+        raise ValueError("the library rejected the batch")
+    return table, ms.reshape(5, 5)
 
 
 def full_rows(sample: dict):
@@ -132,7 +165,10 @@ def bench_main(argv=None):
     samples = [capture_drop(p) for p in params]
     capture_s = time.time() - t0
     packed = pack(samples)
+    default_table = team_ctas()
     solve(packed)  # warm-up
+    default_ms = min(solve(packed)["ms"] for _ in range(a.reps))
+    table, tune_ms = autotune(packed)
     batched = min((solve(packed) for _ in range(a.reps)), key=lambda r: r["ms"])
     single = min((solve(packed, one_by_one=True) for _ in range(a.reps)), key=lambda r: r["ms"])
     same = bool(np.array_equal(batched["x"], single["x"]) and
@@ -151,6 +187,11 @@ def bench_main(argv=None):
         "systems": a.count, "vertices_total": int(sum(verts)),
         "vertices_min_max": [min(verts), max(verts)], "blocks": int(packed[1][-1]),
         "batched_ms": round(batched["ms"], 3), "one_launch_per_system_ms": round(single["ms"], 3),
+        "team_ctas_default": [int(v) for v in default_table], "batched_ms_default_teams":
+            round(default_ms, 3), "team_ctas_autotuned": [int(v) for v in table],
+        "autotune_ms": {BUCKETS[b]: {str(TEAM_SIZES[c]): round(float(tune_ms[b, c]), 3)
+                                     for c in range(5) if tune_ms[b, c] >= 0}
+                        for b in range(5) if (tune_ms[b] >= 0).any()},
         "speedup": round(single["ms"] / batched["ms"], 2),
         "largest_system_alone_ms": round(alone, 3),
         "largest_system": {"vertices": int(samples[big]["n"]),

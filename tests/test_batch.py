@@ -121,6 +121,30 @@ def test_cluster_teams_for_large_systems(product_lib):
 
 
 @pytest.mark.gpu
+def test_autotuned_team_sizes(product_lib):
+    """The autotuner picks a measured team size per size bucket, and a batch
+    solved with any table gives every system the bits it gets alone."""
+    from ppf_gb300 import batch
+
+    samples = _samples([41], n=300) + _samples([42], n=1500) + _samples([43], n=3000)
+    packed = batch.pack(samples)
+    default = batch.team_ctas()
+    try:
+        table, ms = batch.autotune(packed)
+        for b in (0, 1, 2):  # the buckets present
+            tried = ms[b][ms[b] >= 0]
+            assert tried.size >= 1 and table[b] in batch.TEAM_SIZES
+            assert ms[b][batch.TEAM_SIZES.index(int(table[b]))] == tried.min()
+        for t in (table, np.array([1, 1, 1, 1, 1]), np.array([2, 4, 4, 8, 8])):
+            batch.team_ctas(t)
+            a = batch.solve(packed)
+            b = batch.solve(packed, one_by_one=True)
+            assert np.array_equal(a["x"], b["x"]) and np.all(a["state"] == 0)
+    finally:
+        batch.team_ctas(default)
+
+
+@pytest.mark.gpu
 def test_batch_solves_every_system(product_lib):
     from ppf_gb300 import batch
 
