@@ -23,6 +23,10 @@ advance()), with PCG ms-to-tolerance (relative L1 residual 1e-3) per solve.
 * reference: the CPU restatement of the reference's step on the host cores,
   on the same workload and metric; each step is one advance() and the run
   stops after a bounded time.
+* batched_pcg: the batched-scenes workload, 256 uneven cloth drops (sides
+  16-96, sphere or box colliders). Their Newton systems are solved in one
+  launch per autotuned team size, against one launch per system
+  (ppf_gb300.batch).
 * N > 1 (torchrun): replicas only. Each rank steps its own copy of the
   scene (seed = rank); value = Newton iterations of all ranks / max time.
 """
@@ -322,6 +326,13 @@ def run_ours(args, rank, local_rank, world):
     if rank == 0 and args.precond_steps > 0:
         out["preconditioners"] = compare_preconditioners(restart, sc, lib, stream,
                                                          args.precond_steps)
+    if rank == 0 and args.batch_count > 0:
+        # the batched-scenes workload: many uneven drops' Newton systems
+        # solved in one launch per team size (autotuned), against one launch
+        # per system; outside the timed region of the headline
+        from ppf_gb300 import batch
+
+        out["batched_pcg"] = batch.run_bench(args.batch_count, seed=0, reps=3)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(sc, curr0, prev0, param0, CPU_SAMPLE_SECONDS)
     if dist:
@@ -469,6 +480,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precond-steps", type=int, default=24,
                     help="time steps of the preconditioner comparison (0: skip)")
+    ap.add_argument("--batch-count", type=int, default=256,
+                    help="uneven drops of the batched-PCG comparison (0: skip)")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="stacked_sheets",
                     help="stacked_sheets (the headline) or sphere_field (one 1M-vertex cloth)")
     args = ap.parse_args()

@@ -154,12 +154,11 @@ def capture_drop(params, extra_steps: int = 3) -> dict:
     return out
 
 
-def bench_main(argv=None):
-    ap = argparse.ArgumentParser(description="batched PCG over uneven cloth drops")
-    ap.add_argument("--count", type=int, default=256)
-    ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--reps", type=int, default=3)
-    a = ap.parse_args(argv)
+def run_bench(count: int = 256, seed: int = 0, reps: int = 3) -> dict:
+    """Captures the uneven drops' Newton systems, autotunes the team sizes
+    and times the batch against one launch per system; returns the figures.
+    Leaves the library's team-size table as it found it."""
+    a = argparse.Namespace(count=count, seed=seed, reps=reps)
     t0 = time.time()
     params = scenes.uneven_drops(a.count, a.seed)
     samples = [capture_drop(p) for p in params]
@@ -201,7 +200,17 @@ def bench_main(argv=None):
         "pcg_iters_max": int(it[-1]), "converged": int((batched["state"] == 0).sum()),
         "batched_equals_one_by_one": same, "capture_s": round(capture_s, 1),
     }
-    print(json.dumps(out), flush=True)
+    team_ctas(default_table)
+    return out
+
+
+def bench_main(argv=None):
+    ap = argparse.ArgumentParser(description="batched PCG over uneven cloth drops")
+    ap.add_argument("--count", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--reps", type=int, default=3)
+    a = ap.parse_args(argv)
+    print(json.dumps(run_bench(a.count, a.seed, a.reps)), flush=True)
 
 
 if __name__ == "__main__":
