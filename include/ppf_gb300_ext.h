@@ -203,6 +203,10 @@ unsigned ppf_learned_tc_status(void);
  *             col: the global row of each block's column, inside the same
  *             system; val: 9 column-major floats per block)
  *   rhs       3 floats per row
+ *   precond   PPF_PRECOND_BLOCK_JACOBI (the reference's), or PPF_PRECOND_FSAI:
+ *             each system's FSAI factor (each row's 15 strongest lower
+ *             couplings; rows sorted by column required), built on the device
+ *             in the timed region, applied as P = G^T G + 1e-3 D^{-1}
  *   one_by_one  nonzero: one launch per system instead (for comparison)
  * A system's team is one CTA or a thread-block cluster of 2 to 16 CTAs,
  * chosen by its size bucket (ppf_batch_team_ctas); systems of one team size
@@ -214,7 +218,8 @@ unsigned ppf_learned_tc_status(void);
  * included). */
 int ppf_batch_pcg(unsigned n_sys, const unsigned *row_off, const unsigned *off,
                   const unsigned *col, const float *val, const float *rhs,
-                  float tol, unsigned max_iter, int one_by_one, float *x_out,
+                  float tol, unsigned max_iter, int precond, int one_by_one,
+                  float *x_out,
                   unsigned *iters_out, float *resid_out, int *state_out,
                   float *ms_out);
 /* The team size (CTAs; 1, 2, 4, 8 or 16) of each of the 5 system-size

@@ -19,6 +19,7 @@
 #include "../physics/eig.cuh"
 #include "common.cuh"
 #include "fatal.cuh"
+#include "precond.cuh"
 
 #include <cooperative_groups.h>
 
@@ -42,6 +43,11 @@ struct BatchArgs {
     const float *b;            // 3 per row
     float *x, *r, *z, *p, *Ap; // 3 per row
     float *inv;                // 9 per row: inverse of the diagonal block
+    // FSAI factor (null: block-Jacobi): per block slot G(i, j) for j < i and
+    // G(j, i)^T for j > i, per row G(i, i); y: 3 per row
+    const float *gval, *gdiag;
+    float *y;
+    float eps;
     float tol;
     unsigned max_iter;
     unsigned *iters;
@@ -123,6 +129,45 @@ template <bool kCluster> struct Team {
     }
 };
 
+// z = P r with the FSAI factor, P = G^T G + eps D^{-1} (the factored
+// preconditioner of pcg.cuh, on the batch's full rows): y = G r from the
+// slots left of the diagonal, a team barrier, z = G^T y from the slots right
+// of it. Writes z (and p = z when set_p) of this thread's rows; returns their
+// part of r^T z. Starts with a team barrier (every r final).
+template <bool kCluster>
+__device__ float factor_apply(const BatchArgs &g, const Team<kCluster> &team, unsigned i0,
+                              unsigned di, unsigned hi, bool set_p) {
+    team.sync();
+    for (unsigned i = i0; i < hi; i += di) {
+        Vec3 yi = ldm(g.gdiag + 9 * (size_t)i) * ld3(g.r, i);
+        for (unsigned q = __ldg(g.off + i), q1 = __ldg(g.off + i + 1); q < q1; ++q) {
+            const unsigned j = __ldg(g.col + q);
+            if (j >= i) break; // columns sorted: the lower slots come first
+            yi += ldm(g.gval + 9 * (size_t)q) * team.ld_shared_vec(g.r, j);
+        }
+        st3v(g.y, i, yi);
+    }
+    team.sync();
+    float a = 0.0f;
+    for (unsigned i = i0; i < hi; i += di) {
+        const Vec3 ri = ld3(g.r, i);
+        Mat3 P;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) P.m[q] = g.inv[9 * (size_t)i + q];
+        Vec3 zi = ldm(g.gdiag + 9 * (size_t)i).transpose() * ld3(g.y, i);
+        for (unsigned q = __ldg(g.off + i), q1 = __ldg(g.off + i + 1); q < q1; ++q) {
+            const unsigned j = __ldg(g.col + q);
+            if (j <= i) continue;
+            zi += ldm(g.gval + 9 * (size_t)q) * team.ld_shared_vec(g.y, j);
+        }
+        zi += g.eps * (P * ri);
+        st3v(g.z, i, zi);
+        if (set_p) st3v(g.p, i, zi);
+        a += ri.dot(zi);
+    }
+    return a;
+}
+
 // One system per team: team t (CTA, or cluster of CTAs) takes system
 // order[t] (base + t without an order).
 template <bool kCluster>
@@ -146,14 +191,17 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
 #pragma unroll
         for (int q = 0; q < 9; ++q) g.inv[9 * (size_t)i + q] = P.m[q];
         const Vec3 bi = vec3(__ldg(g.b + 3 * i), __ldg(g.b + 3 * i + 1), __ldg(g.b + 3 * i + 2));
-        const Vec3 zi = P * bi;
         st3v(g.x, i, Vec3::zero());
         st3v(g.r, i, bi);
-        st3v(g.z, i, zi);
-        st3v(g.p, i, zi);
-        a += bi.dot(zi);
+        if (!g.gval) {
+            const Vec3 zi = P * bi;
+            st3v(g.z, i, zi);
+            st3v(g.p, i, zi);
+            a += bi.dot(zi);
+        }
         e += fabsf(bi[0]) + fabsf(bi[1]) + fabsf(bi[2]);
     }
+    if (g.gval) a = factor_apply(g, team, i0, di, hi, true);
     float2 t = team.sum2(a, e, sh, part, k);
     k ^= 1u;
     float rz = t.x;
@@ -207,16 +255,19 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
                 xi[c] += alpha * pi[c];
                 ri[c] = ri[c] - alpha * api[c];
             }
-            Mat3 P;
-#pragma unroll
-            for (int q = 0; q < 9; ++q) P.m[q] = g.inv[9 * (size_t)i + q];
-            const Vec3 zi = P * ri;
             st3v(g.x, i, xi);
             st3v(g.r, i, ri);
-            st3v(g.z, i, zi);
-            a += ri.dot(zi);
+            if (!g.gval) {
+                Mat3 P;
+#pragma unroll
+                for (int q = 0; q < 9; ++q) P.m[q] = g.inv[9 * (size_t)i + q];
+                const Vec3 zi = P * ri;
+                st3v(g.z, i, zi);
+                a += ri.dot(zi);
+            }
             e += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
         }
+        if (g.gval) a = factor_apply(g, team, i0, di, hi, false);
         t = team.sum2(a, e, sh, part, k);
         k ^= 1u;
         const float rz_new = t.x, err_now = t.y;
@@ -248,6 +299,211 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
             st3v(g.p, i, zi + beta * pi);
         }
         team.sync();
+    }
+}
+
+// ---- FSAI factor of every system (fsai.cuh restated on the batch's full rows) ----
+constexpr int kBfMax = 15;                // kept lower neighbours per row
+constexpr int kBfDim = 3 * (kBfMax + 1);  // 48
+constexpr unsigned kBfWarps = 4;
+
+// The slot of column c in row r (rows sorted by column), or ~0u.
+__device__ __forceinline__ unsigned find_slot(const unsigned *off, const unsigned *col,
+                                              unsigned r, unsigned c) {
+    unsigned lo = __ldg(off + r), hi = __ldg(off + r + 1);
+    while (lo < hi) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (__ldg(col + mid) < c) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < __ldg(off + r + 1) && __ldg(col + lo) == c) ? lo : ~0u;
+}
+
+// C(i)^{-1} of every row's diagonal block (identity fallback).
+__global__ void k_batch_cinv(unsigned rows, const unsigned *off, const unsigned *col,
+                             const float *val, float *cinv) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows) return;
+    const unsigned k = find_slot(off, col, i, i);
+    Mat3 c = Mat3::identity();
+    if (k != ~0u && !chol_inv3(ldm(val + 9 * (size_t)k), c)) c = Mat3::identity();
+#pragma unroll
+    for (int e = 0; e < 9; ++e) cinv[9 * (size_t)i + e] = c.m[e];
+}
+
+struct BfShared {
+    float M[kBfDim][kBfDim + 1];
+    float Y[kBfDim][3];
+    unsigned J[kBfMax], K[kBfMax];
+};
+
+// One warp per row i: G(i, j) of its (at most 15 strongest) lower
+// neighbours into their slots of row i, G(i, i) into gdiag.
+__global__ void __launch_bounds__(32 * kBfWarps)
+    k_batch_fsai(unsigned rows, const unsigned *off, const unsigned *col, const float *val,
+                 const float *cinv, float *gval, float *gdiag) {
+    __shared__ BfShared sh[kBfWarps];
+    const unsigned lane = threadIdx.x & 31u, wi = threadIdx.x >> 5;
+    const unsigned i = blockIdx.x * kBfWarps + wi;
+    if (i >= rows) return;
+    BfShared &W = sh[wi];
+    const Mat3 Ci = ldm(cinv + 9 * (size_t)i);
+    const unsigned k0 = __ldg(off + i);
+    unsigned nl = 0; // lower slots come first (columns sorted)
+    while (k0 + nl < __ldg(off + i + 1) && __ldg(col + k0 + nl) < i) ++nl;
+    auto norm_of = [&](unsigned t) {
+        const unsigned j = __ldg(col + k0 + t);
+        const Mat3 ah = (Ci * ldm(val + 9 * (size_t)(k0 + t))) * ldm(cinv + 9 * (size_t)j).transpose();
+        float acc = 0.0f;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) acc = acc + ah.m[e] * ah.m[e];
+        return sqrtf(acc);
+    };
+    // kept: all lower slots, or the 15 strongest (ties: the earlier slot)
+    unsigned m = 0;
+    if (lane == 0) {
+        if (nl <= (unsigned)kBfMax) {
+            for (unsigned t = 0; t < nl; ++t) {
+                W.J[m] = __ldg(col + k0 + t);
+                W.K[m] = k0 + t;
+                ++m;
+            }
+        } else {
+            // selection by repeated maxima over the (few) lower slots
+            unsigned taken[4] = {0u, 0u, 0u, 0u}; // up to 128 lower slots considered
+            const unsigned cap = nl < 128u ? nl : 128u;
+            for (int round = 0; round < kBfMax; ++round) {
+                float best = -1.0f;
+                unsigned bt = ~0u;
+                for (unsigned t = 0; t < cap; ++t) {
+                    if (taken[t >> 5] & (1u << (t & 31u))) continue;
+                    const float v = norm_of(t);
+                    if (v > best) {
+                        best = v;
+                        bt = t;
+                    }
+                }
+                if (bt == ~0u) break;
+                taken[bt >> 5] |= 1u << (bt & 31u);
+            }
+            for (unsigned t = 0; t < cap; ++t)
+                if (taken[t >> 5] & (1u << (t & 31u))) {
+                    W.J[m] = __ldg(col + k0 + t);
+                    W.K[m] = k0 + t;
+                    ++m;
+                }
+        }
+    }
+    m = __shfl_sync(0xffffffffu, m, 0);
+    __syncwarp();
+    const unsigned d = 3 * (m + 1);
+    const unsigned pairs = (m + 1) * (m + 2) / 2;
+    for (unsigned q = lane; q < pairs; q += 32) {
+        unsigned a = 0, rem = q;
+        while (rem >= m + 1 - a) {
+            rem -= m + 1 - a;
+            ++a;
+        }
+        const unsigned b = a + rem;
+        const unsigned va = a < m ? W.J[a] : i, vb = b < m ? W.J[b] : i;
+        const Mat3 Ca = ldm(cinv + 9 * (size_t)va), Cb = ldm(cinv + 9 * (size_t)vb);
+        Mat3 blk = Mat3::zero();
+        const unsigned kk = find_slot(off, col, va, vb); // A(va, vb) in row va
+        if (kk != ~0u) blk = (Ca * ldm(val + 9 * (size_t)kk)) * Cb.transpose();
+#pragma unroll
+        for (int x = 0; x < 3; ++x)
+#pragma unroll
+            for (int y = 0; y < 3; ++y) {
+                W.M[3 * a + x][3 * b + y] = blk(x, y);
+                W.M[3 * b + y][3 * a + x] = blk(x, y);
+            }
+    }
+    bool ok = true;
+    for (unsigned k = 0; k < d; ++k) {
+        __syncwarp();
+        const float piv = W.M[k][k];
+        if (!(piv > 0.0f) || !isfinite(piv)) {
+            ok = false;
+            break;
+        }
+        const float lkk = sqrtf(piv);
+        __syncwarp();
+        if (lane == 0) W.M[k][k] = lkk;
+        for (unsigned r = k + 1 + lane; r < d; r += 32) W.M[r][k] = W.M[r][k] / lkk;
+        __syncwarp();
+        for (unsigned r = k + 1 + lane; r < d; r += 32) {
+            const float lrk = W.M[r][k];
+            for (unsigned c = k + 1; c <= r; ++c) W.M[r][c] = W.M[r][c] - lrk * W.M[c][k];
+        }
+    }
+    __syncwarp();
+    Mat3 Gii = Mat3::identity();
+    if (ok) {
+        for (unsigned r = lane; r < d; r += 32)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) W.Y[r][c] = 0.0f;
+        __syncwarp();
+        if (lane < 3) {
+            const unsigned c = lane, b0 = 3 * m;
+            for (unsigned x = 0; x < 3; ++x) {
+                float v = x == c ? 1.0f : 0.0f;
+                for (unsigned y = 0; y < x; ++y) v = v - W.M[b0 + x][b0 + y] * W.Y[b0 + y][c];
+                W.Y[b0 + x][c] = v / W.M[b0 + x][b0 + x];
+            }
+        }
+        for (int k = (int)d - 1; k >= 0; --k) {
+            __syncwarp();
+            if (lane < 3) W.Y[k][lane] = W.Y[k][lane] / W.M[k][k];
+            __syncwarp();
+            for (int r = (int)lane; r < k; r += 32)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) W.Y[r][c] = W.Y[r][c] - W.M[k][r] * W.Y[k][c];
+        }
+        __syncwarp();
+        Mat3 Yii;
+#pragma unroll
+        for (int x = 0; x < 3; ++x)
+#pragma unroll
+            for (int y = 0; y < 3; ++y)
+                Yii(x, y) = 0.5f * (W.Y[3 * m + x][y] + W.Y[3 * m + y][x]);
+        Mat3 L3inv;
+        ok = chol_inv3(Yii, L3inv);
+        if (ok) {
+            Gii = L3inv * Yii;
+            for (unsigned a = lane; a < m; a += 32) {
+                Mat3 Yat;
+#pragma unroll
+                for (int x = 0; x < 3; ++x)
+#pragma unroll
+                    for (int y = 0; y < 3; ++y) Yat(x, y) = W.Y[3 * a + y][x];
+                const Mat3 G = (L3inv * Yat) * ldm(cinv + 9 * (size_t)W.J[a]);
+#pragma unroll
+                for (int e = 0; e < 9; ++e) gval[9 * (size_t)W.K[a] + e] = G.m[e];
+            }
+        }
+    }
+    if (!ok) Gii = Mat3::identity();
+    if (lane == 0) {
+        const Mat3 g = Gii * Ci;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) gdiag[9 * (size_t)i + e] = g.m[e];
+    }
+}
+
+// Upper slots (a, b > a) take the transpose of the edge's value, stored in
+// row b's slot for column a.
+__global__ void k_batch_fsai_mirror(unsigned rows, const unsigned *off, const unsigned *col,
+                                    float *gval) {
+    const unsigned a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= rows) return;
+    for (unsigned k = __ldg(off + a), k1 = __ldg(off + a + 1); k < k1; ++k) {
+        const unsigned b = __ldg(col + k);
+        if (b <= a) continue;
+        const unsigned kk = find_slot(off, col, b, a);
+        Mat3 g = Mat3::zero();
+        if (kk != ~0u) g = ldm(gval + 9 * (size_t)kk).transpose();
+#pragma unroll
+        for (int e = 0; e < 9; ++e) gval[9 * (size_t)k + e] = g.m[e];
     }
 }
 
@@ -318,8 +574,24 @@ struct DeviceBatch {
           z(3 * (size_t)rows), p(3 * (size_t)rows), Ap(3 * (size_t)rows),
           inv(9 * (size_t)rows), res(n), st(n) {}
     BatchArgs args(float tol, unsigned max_iter) const {
-        return BatchArgs{0u,  nullptr, row.d, off.d, col.d,    val.d, b.d,   x.d, r.d,
-                         z.d, p.d,     Ap.d,  inv.d, tol, max_iter, it.d, res.d, st.d};
+        BatchArgs g{};
+        g.row_off = row.d;
+        g.off = off.d;
+        g.col = col.d;
+        g.val = val.d;
+        g.b = b.d;
+        g.x = x.d;
+        g.r = r.d;
+        g.z = z.d;
+        g.p = p.d;
+        g.Ap = Ap.d;
+        g.inv = inv.d;
+        g.tol = tol;
+        g.max_iter = max_iter;
+        g.iters = it.d;
+        g.resid = res.d;
+        g.state = st.d;
+        return g;
     }
 };
 
@@ -415,19 +687,51 @@ void group_systems(unsigned n_sys, const unsigned *row_off, const unsigned *off,
 
 extern "C" int ppf_batch_pcg(unsigned n_sys, const unsigned *row_off, const unsigned *off,
                              const unsigned *col, const float *val, const float *rhs, float tol,
-                             unsigned max_iter, int one_by_one, float *x_out,
+                             unsigned max_iter, int precond, int one_by_one, float *x_out,
                              unsigned *iters_out, float *resid_out, int *state_out,
                              float *ms_out) {
     try {
         if (!valid_batch(n_sys, row_off, off, col, val, rhs)) return -1;
+        if (precond != PPF_PRECOND_BLOCK_JACOBI && precond != PPF_PRECOND_FSAI) return -1;
         DeviceBatch B(n_sys, row_off, off, col, val, rhs);
         std::vector<unsigned> order;
         std::vector<std::pair<unsigned, unsigned>> groups;
         group_systems(n_sys, row_off, off, order, groups);
         Dev<unsigned> d_order(n_sys, order.data());
-        const float ms = run_groups(B.args(tol, max_iter), d_order.d, groups, one_by_one != 0);
+        BatchArgs g = B.args(tol, max_iter);
+        // the FSAI factor of every system, timed with the solve
+        const bool fsai = precond == PPF_PRECOND_FSAI;
+        Dev<float> cinv(fsai ? 9 * (size_t)B.rows : 1), gval(fsai ? 9 * (size_t)B.blocks : 1),
+            gdiag(fsai ? 9 * (size_t)B.rows : 1), yv(fsai ? 3 * (size_t)B.rows : 1);
+        float build_ms = 0.0f;
+        if (fsai) {
+            cudaEvent_t b0, b1;
+            PPF_CUDA(cudaEventCreate(&b0));
+            PPF_CUDA(cudaEventCreate(&b1));
+            PPF_CUDA(cudaDeviceSynchronize());
+            PPF_CUDA(cudaEventRecord(b0, 0));
+            PPF_CUDA(cudaMemsetAsync(gval.d, 0, 9 * (size_t)B.blocks * sizeof(float), 0));
+            k_batch_cinv<<<div_up(B.rows, 256u), 256>>>(B.rows, B.off.d, B.col.d, B.val.d, cinv.d);
+            PPF_LAUNCH_CHECK();
+            k_batch_fsai<<<div_up(B.rows, kBfWarps), 32 * kBfWarps>>>(B.rows, B.off.d, B.col.d,
+                                                                      B.val.d, cinv.d, gval.d,
+                                                                      gdiag.d);
+            PPF_LAUNCH_CHECK();
+            k_batch_fsai_mirror<<<div_up(B.rows, 256u), 256>>>(B.rows, B.off.d, B.col.d, gval.d);
+            PPF_LAUNCH_CHECK();
+            PPF_CUDA(cudaEventRecord(b1, 0));
+            PPF_CUDA(cudaEventSynchronize(b1));
+            PPF_CUDA(cudaEventElapsedTime(&build_ms, b0, b1));
+            cudaEventDestroy(b0);
+            cudaEventDestroy(b1);
+            g.gval = gval.d;
+            g.gdiag = gdiag.d;
+            g.y = yv.d;
+            g.eps = 1e-3f;
+        }
+        const float ms = run_groups(g, d_order.d, groups, one_by_one != 0);
         if (ms < 0.0f) return -1;
-        if (ms_out) *ms_out = ms;
+        if (ms_out) *ms_out = ms + build_ms;
         const unsigned rows = B.rows;
         if (x_out)
             PPF_CUDA(cudaMemcpy(x_out, B.x.d, 3 * (size_t)rows * sizeof(float),

@@ -32,7 +32,7 @@ def _declare(lib):
         return
     lib.ppf_batch_pcg.restype = C.c_int
     lib.ppf_batch_pcg.argtypes = [C.c_uint, u32p, u32p, u32p, f32p, f32p, C.c_float, C.c_uint,
-                                  C.c_int, f32p_opt, np.ctypeslib.ndpointer(np.uint32, flags="C"),
+                                  C.c_int, C.c_int, f32p_opt, np.ctypeslib.ndpointer(np.uint32, flags="C"),
                                   f32p_opt, np.ctypeslib.ndpointer(np.int32, flags="C"),
                                   C.POINTER(C.c_float)]
     lib.ppf_batch_team_ctas.restype = C.c_int
@@ -117,9 +117,11 @@ def pack(samples):
             np.concatenate(vals).astype(np.float32), np.concatenate(rhs).astype(np.float32))
 
 
-def solve(packed, tol: float = 1e-3, max_iter: int = 10000, one_by_one: bool = False) -> dict:
-    """Solves every packed system; returns x (rows x 3), and per system the
-    iterations, relative L1 residual and state, and the device time."""
+def solve(packed, tol: float = 1e-3, max_iter: int = 10000, one_by_one: bool = False,
+          precond: int = abi.PRECOND_BLOCK_JACOBI) -> dict:
+    """Solves every packed system (block-Jacobi, or abi.PRECOND_FSAI); returns
+    x (rows x 3), and per system the iterations, relative L1 residual and
+    state, and the device time (the FSAI factor build included)."""
     lib = product()
     _declare(lib)
     row_off, off, col, val, rhs = packed
@@ -130,8 +132,8 @@ def solve(packed, tol: float = 1e-3, max_iter: int = 10000, one_by_one: bool = F
     res = np.zeros(ns, np.float32)
     st = np.zeros(ns, np.int32)
     ms = C.c_float()
-    rc = lib.ppf_batch_pcg(ns, row_off, off, col, val, rhs, tol, max_iter, int(one_by_one), x,
-                           it, res, st, C.byref(ms))
+    rc = lib.ppf_batch_pcg(ns, row_off, off, col, val, rhs, tol, max_iter, int(precond),
+                           int(one_by_one), x, it, res, st, C.byref(ms))
     if rc != 0:
         raise ValueError("the library rejected the batch")
     return {"x": x.reshape(-1, 3), "iters": it, "resid": res, "state": st, "ms": ms.value}
@@ -172,6 +174,9 @@ def run_bench(count: int = 256, seed: int = 0, reps: int = 3) -> dict:
     single = min((solve(packed, one_by_one=True) for _ in range(a.reps)), key=lambda r: r["ms"])
     same = bool(np.array_equal(batched["x"], single["x"]) and
                 np.array_equal(batched["iters"], single["iters"]))
+    fsai = min((solve(packed, precond=abi.PRECOND_FSAI) for _ in range(a.reps)),
+               key=lambda r: r["ms"])
+    fit = np.sort(fsai["iters"])
     # the largest system alone: the floor of a batch whose systems each run
     # on one CTA
     big = int(np.argmax([int(packed[1][packed[0][k + 1]] - packed[1][packed[0][k]])
@@ -199,6 +204,11 @@ def run_bench(count: int = 256, seed: int = 0, reps: int = 3) -> dict:
         "pcg_iters_median": int(it[len(it) // 2]), "pcg_iters_p90": int(it[int(0.9 * len(it))]),
         "pcg_iters_max": int(it[-1]), "converged": int((batched["state"] == 0).sum()),
         "batched_equals_one_by_one": same, "capture_s": round(capture_s, 1),
+        "fsai": {"batched_ms": round(fsai["ms"], 3),
+                 "speedup_over_block_jacobi": round(batched["ms"] / fsai["ms"], 2),
+                 "pcg_iters_median": int(fit[len(fit) // 2]),
+                 "pcg_iters_p90": int(fit[int(0.9 * len(fit))]),
+                 "converged": int((fsai["state"] == 0).sum())},
     }
     team_ctas(default_table)
     return out
