@@ -44,8 +44,10 @@ struct BatchArgs {
     float *x, *r, *z, *p, *Ap; // 3 per row
     float *inv;                // 9 per row: inverse of the diagonal block
     // FSAI factor (null: block-Jacobi): per block slot G(i, j) for j < i and
-    // G(j, i)^T for j > i, per row G(i, i); y: 3 per row
-    const float *gval, *gdiag;
+    // G(j, i)^T for j > i (bf16, 9 per slot, column-major), per row G(i, i)
+    // (fp32); y: 3 per row
+    const bf16_t *gval;
+    const float *gdiag;
     float *y;
     float eps;
     float tol;
@@ -67,6 +69,12 @@ __device__ __forceinline__ Mat3 ldm(const float *p) {
     Mat3 m;
 #pragma unroll
     for (int e = 0; e < 9; ++e) m.m[e] = __ldg(p + e);
+    return m;
+}
+__device__ __forceinline__ Mat3 ldm(const bf16_t *p) {
+    Mat3 m;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) m.m[e] = __bfloat162float(__ldg(p + e));
     return m;
 }
 
@@ -129,25 +137,44 @@ template <bool kCluster> struct Team {
     }
 };
 
-// z = P r with the FSAI factor, P = G^T G + eps D^{-1} (the factored
-// preconditioner of pcg.cuh, on the batch's full rows): y = G r from the
-// slots left of the diagonal, a team barrier, z = G^T y from the slots right
-// of it. Writes z (and p = z when set_p) of this thread's rows; returns their
-// part of r^T z. Starts with a team barrier (every r final).
+// The FSAI preconditioner P = G^T G + eps D^{-1} (the factored preconditioner
+// of pcg.cuh, on the batch's full rows) in two passes with a team barrier
+// between them: y = G r over the slots left of the diagonal (factor_y), then
+// z = G^T y + eps D^{-1} r over the slots right of it (factor_z). Between
+// exact passes the update phase carries y by y -= alpha G A p, which needs
+// no barrier of its own (A p is final team-wide once p^T A p is summed); the
+// exact pass runs every kYRefresh iterations to bound the drift.
+constexpr unsigned kYRefresh = 16;
+
+// acc + the sum over row i's slots left of the diagonal (they come first:
+// columns sorted) of G(i, j) v_j; the next slot's column loads one slot
+// ahead.
 template <bool kCluster>
-__device__ float factor_apply(const BatchArgs &g, const Team<kCluster> &team, unsigned i0,
-                              unsigned di, unsigned hi, bool set_p) {
-    team.sync();
-    for (unsigned i = i0; i < hi; i += di) {
-        Vec3 yi = ldm(g.gdiag + 9 * (size_t)i) * ld3(g.r, i);
-        for (unsigned q = __ldg(g.off + i), q1 = __ldg(g.off + i + 1); q < q1; ++q) {
-            const unsigned j = __ldg(g.col + q);
-            if (j >= i) break; // columns sorted: the lower slots come first
-            yi += ldm(g.gval + 9 * (size_t)q) * team.ld_shared_vec(g.r, j);
-        }
-        st3v(g.y, i, yi);
+__device__ __forceinline__ Vec3 lower_product(const BatchArgs &g, const Team<kCluster> &team,
+                                              unsigned i, const float *v, Vec3 acc) {
+    const unsigned q0 = __ldg(g.off + i), q1 = __ldg(g.off + i + 1);
+    unsigned j = q0 < q1 ? __ldg(g.col + q0) : i;
+    for (unsigned q = q0; q < q1 && j < i; ++q) {
+        const unsigned jn = q + 1 < q1 ? __ldg(g.col + q + 1) : i;
+        acc += ldm(g.gval + 9 * (size_t)q) * team.ld_shared_vec(v, j);
+        j = jn;
     }
-    team.sync();
+    return acc;
+}
+
+// y = G r of this thread's rows (every r final).
+template <bool kCluster>
+__device__ void factor_y(const BatchArgs &g, const Team<kCluster> &team, unsigned i0, unsigned di,
+                         unsigned hi) {
+    for (unsigned i = i0; i < hi; i += di)
+        st3v(g.y, i, lower_product(g, team, i, g.r, ldm(g.gdiag + 9 * (size_t)i) * ld3(g.r, i)));
+}
+
+// z = G^T y + eps D^{-1} r of this thread's rows (every y final); writes
+// p = z too when set_p; returns their part of r^T z.
+template <bool kCluster>
+__device__ float factor_z(const BatchArgs &g, const Team<kCluster> &team, unsigned i0, unsigned di,
+                          unsigned hi, bool set_p) {
     float a = 0.0f;
     for (unsigned i = i0; i < hi; i += di) {
         const Vec3 ri = ld3(g.r, i);
@@ -155,10 +182,12 @@ __device__ float factor_apply(const BatchArgs &g, const Team<kCluster> &team, un
 #pragma unroll
         for (int q = 0; q < 9; ++q) P.m[q] = g.inv[9 * (size_t)i + q];
         Vec3 zi = ldm(g.gdiag + 9 * (size_t)i).transpose() * ld3(g.y, i);
-        for (unsigned q = __ldg(g.off + i), q1 = __ldg(g.off + i + 1); q < q1; ++q) {
-            const unsigned j = __ldg(g.col + q);
-            if (j <= i) continue;
-            zi += ldm(g.gval + 9 * (size_t)q) * team.ld_shared_vec(g.y, j);
+        const unsigned q0 = __ldg(g.off + i), q1 = __ldg(g.off + i + 1);
+        unsigned j = q0 < q1 ? __ldg(g.col + q0) : 0u;
+        for (unsigned q = q0; q < q1; ++q) {
+            const unsigned jn = q + 1 < q1 ? __ldg(g.col + q + 1) : 0u;
+            if (j > i) zi += ldm(g.gval + 9 * (size_t)q) * team.ld_shared_vec(g.y, j);
+            j = jn;
         }
         zi += g.eps * (P * ri);
         st3v(g.z, i, zi);
@@ -201,7 +230,12 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
         }
         e += fabsf(bi[0]) + fabsf(bi[1]) + fabsf(bi[2]);
     }
-    if (g.gval) a = factor_apply(g, team, i0, di, hi, true);
+    if (g.gval) {
+        team.sync();
+        factor_y(g, team, i0, di, hi);
+        team.sync();
+        a = factor_z(g, team, i0, di, hi, true);
+    }
     float2 t = team.sum2(a, e, sh, part, k);
     k ^= 1u;
     float rz = t.x;
@@ -246,7 +280,9 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
         } else if (!broke) {
             broke = (pAp < -bound || pAp != pAp) ? 1 : 3;
         }
-        // x += alpha p, r -= alpha A p, z = P r (rows of this thread only)
+        // x += alpha p, r -= alpha A p, z = P r (rows of this thread only);
+        // with the FSAI factor y -= alpha G A p, or the exact y below
+        const bool exact_y = iter % kYRefresh == 0;
         a = e = 0.0f;
         for (unsigned i = i0; i < hi; i += di) {
             Vec3 xi = ld3(g.x, i), ri = ld3(g.r, i);
@@ -264,10 +300,20 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
                 const Vec3 zi = P * ri;
                 st3v(g.z, i, zi);
                 a += ri.dot(zi);
+            } else if (!exact_y) {
+                const Vec3 gap = lower_product(g, team, i, g.Ap, ldm(g.gdiag + 9 * (size_t)i) * api);
+                st3v(g.y, i, ld3(g.y, i) - alpha * gap);
             }
             e += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
         }
-        if (g.gval) a = factor_apply(g, team, i0, di, hi, false);
+        if (g.gval) {
+            team.sync();
+            if (exact_y) {
+                factor_y(g, team, i0, di, hi);
+                team.sync();
+            }
+            a = factor_z(g, team, i0, di, hi, false);
+        }
         t = team.sum2(a, e, sh, part, k);
         k ^= 1u;
         const float rz_new = t.x, err_now = t.y;
@@ -341,7 +387,7 @@ struct BfShared {
 // neighbours into their slots of row i, G(i, i) into gdiag.
 __global__ void __launch_bounds__(32 * kBfWarps)
     k_batch_fsai(unsigned rows, const unsigned *off, const unsigned *col, const float *val,
-                 const float *cinv, float *gval, float *gdiag) {
+                 const float *cinv, bf16_t *gval, float *gdiag) {
     __shared__ BfShared sh[kBfWarps];
     const unsigned lane = threadIdx.x & 31u, wi = threadIdx.x >> 5;
     const unsigned i = blockIdx.x * kBfWarps + wi;
@@ -478,7 +524,7 @@ __global__ void __launch_bounds__(32 * kBfWarps)
                     for (int y = 0; y < 3; ++y) Yat(x, y) = W.Y[3 * a + y][x];
                 const Mat3 G = (L3inv * Yat) * ldm(cinv + 9 * (size_t)W.J[a]);
 #pragma unroll
-                for (int e = 0; e < 9; ++e) gval[9 * (size_t)W.K[a] + e] = G.m[e];
+                for (int e = 0; e < 9; ++e) gval[9 * (size_t)W.K[a] + e] = __float2bfloat16_rn(G.m[e]);
             }
         }
     }
@@ -493,17 +539,20 @@ __global__ void __launch_bounds__(32 * kBfWarps)
 // Upper slots (a, b > a) take the transpose of the edge's value, stored in
 // row b's slot for column a.
 __global__ void k_batch_fsai_mirror(unsigned rows, const unsigned *off, const unsigned *col,
-                                    float *gval) {
+                                    bf16_t *gval) {
     const unsigned a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= rows) return;
     for (unsigned k = __ldg(off + a), k1 = __ldg(off + a + 1); k < k1; ++k) {
         const unsigned b = __ldg(col + k);
         if (b <= a) continue;
         const unsigned kk = find_slot(off, col, b, a);
-        Mat3 g = Mat3::zero();
-        if (kk != ~0u) g = ldm(gval + 9 * (size_t)kk).transpose();
+        // the transpose of the edge's bf16 value, bit for bit
 #pragma unroll
-        for (int e = 0; e < 9; ++e) gval[9 * (size_t)k + e] = g.m[e];
+        for (int x = 0; x < 3; ++x)
+#pragma unroll
+            for (int y = 0; y < 3; ++y)
+                gval[9 * (size_t)k + 3 * x + y] =
+                    kk != ~0u ? gval[9 * (size_t)kk + 3 * y + x] : __float2bfloat16_rn(0.0f);
     }
 }
 
@@ -701,8 +750,9 @@ extern "C" int ppf_batch_pcg(unsigned n_sys, const unsigned *row_off, const unsi
         BatchArgs g = B.args(tol, max_iter);
         // the FSAI factor of every system, timed with the solve
         const bool fsai = precond == PPF_PRECOND_FSAI;
-        Dev<float> cinv(fsai ? 9 * (size_t)B.rows : 1), gval(fsai ? 9 * (size_t)B.blocks : 1),
-            gdiag(fsai ? 9 * (size_t)B.rows : 1), yv(fsai ? 3 * (size_t)B.rows : 1);
+        Dev<float> cinv(fsai ? 9 * (size_t)B.rows : 1), gdiag(fsai ? 9 * (size_t)B.rows : 1),
+            yv(fsai ? 3 * (size_t)B.rows : 1);
+        Dev<bf16_t> gval(fsai ? 9 * (size_t)B.blocks : 1);
         float build_ms = 0.0f;
         if (fsai) {
             cudaEvent_t b0, b1;
@@ -710,7 +760,7 @@ extern "C" int ppf_batch_pcg(unsigned n_sys, const unsigned *row_off, const unsi
             PPF_CUDA(cudaEventCreate(&b1));
             PPF_CUDA(cudaDeviceSynchronize());
             PPF_CUDA(cudaEventRecord(b0, 0));
-            PPF_CUDA(cudaMemsetAsync(gval.d, 0, 9 * (size_t)B.blocks * sizeof(float), 0));
+            PPF_CUDA(cudaMemsetAsync(gval.d, 0, 9 * (size_t)B.blocks * sizeof(bf16_t), 0));
             k_batch_cinv<<<div_up(B.rows, 256u), 256>>>(B.rows, B.off.d, B.col.d, B.val.d, cinv.d);
             PPF_LAUNCH_CHECK();
             k_batch_fsai<<<div_up(B.rows, kBfWarps), 32 * kBfWarps>>>(B.rows, B.off.d, B.col.d,
