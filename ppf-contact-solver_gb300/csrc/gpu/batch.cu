@@ -40,11 +40,18 @@ struct BatchArgs {
     const unsigned *off;       // rows + 1: both-triangle block rows
     const unsigned *col;       // global row of each block's column
     const float *val;          // 9 per block, column-major
+    // the same blocks sliced for the products (SELL-32): each system's rows
+    // in slices of 32 from its first row, block k of row i at rbase[i] +
+    // 32 k; entry e of the 32 blocks at 32 m .. 32 m + 31 at 32 (9 m + e) ..
+    // 32 (9 m + e) + 31, so a warp's 32 rows read each entry coalesced
+    const unsigned *rbase;     // rows: SELL position of the row's first block
+    const unsigned *scol;      // SELL: global row of each block's column
+    const float *sval;         // SELL: 9 per block, entry-interleaved
     const float *b;            // 3 per row
     float *x, *r, *z, *p, *Ap; // 3 per row
     float *inv;                // 9 per row: inverse of the diagonal block
     // FSAI factor (null: block-Jacobi): per block slot G(i, j) for j < i and
-    // G(j, i)^T for j > i (bf16, 9 per slot, column-major), per row G(i, i)
+    // G(j, i)^T for j > i (bf16, SELL positions as sval), per row G(i, i)
     // (fp32); y: 3 per row
     const bf16_t *gval;
     const float *gdiag;
@@ -71,10 +78,20 @@ __device__ __forceinline__ Mat3 ldm(const float *p) {
     for (int e = 0; e < 9; ++e) m.m[e] = __ldg(p + e);
     return m;
 }
-__device__ __forceinline__ Mat3 ldm(const bf16_t *p) {
+// block q of a SELL-32 value array (entry-interleaved in groups of 32)
+__device__ __forceinline__ size_t sell_at(unsigned q, int e) {
+    return ((size_t)(q >> 5) * 9 + e) * 32 + (q & 31u);
+}
+__device__ __forceinline__ Mat3 ldm_sell(const float *v, unsigned q) {
     Mat3 m;
 #pragma unroll
-    for (int e = 0; e < 9; ++e) m.m[e] = __bfloat162float(__ldg(p + e));
+    for (int e = 0; e < 9; ++e) m.m[e] = __ldg(v + sell_at(q, e));
+    return m;
+}
+__device__ __forceinline__ Mat3 ldm_sell(const bf16_t *v, unsigned q) {
+    Mat3 m;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) m.m[e] = __bfloat162float(__ldg(v + sell_at(q, e)));
     return m;
 }
 
@@ -152,11 +169,12 @@ constexpr unsigned kYRefresh = 16;
 template <bool kCluster>
 __device__ __forceinline__ Vec3 lower_product(const BatchArgs &g, const Team<kCluster> &team,
                                               unsigned i, const float *v, Vec3 acc) {
-    const unsigned q0 = __ldg(g.off + i), q1 = __ldg(g.off + i + 1);
-    unsigned j = q0 < q1 ? __ldg(g.col + q0) : i;
-    for (unsigned q = q0; q < q1 && j < i; ++q) {
-        const unsigned jn = q + 1 < q1 ? __ldg(g.col + q + 1) : i;
-        acc += ldm(g.gval + 9 * (size_t)q) * team.ld_shared_vec(v, j);
+    const unsigned len = __ldg(g.off + i + 1) - __ldg(g.off + i), q0 = __ldg(g.rbase + i);
+    unsigned j = len ? __ldg(g.scol + q0) : i;
+    for (unsigned k = 0; k < len && j < i; ++k) {
+        const unsigned q = q0 + 32u * k;
+        const unsigned jn = k + 1 < len ? __ldg(g.scol + q + 32u) : i;
+        acc += ldm_sell(g.gval, q) * team.ld_shared_vec(v, j);
         j = jn;
     }
     return acc;
@@ -182,11 +200,12 @@ __device__ float factor_z(const BatchArgs &g, const Team<kCluster> &team, unsign
 #pragma unroll
         for (int q = 0; q < 9; ++q) P.m[q] = g.inv[9 * (size_t)i + q];
         Vec3 zi = ldm(g.gdiag + 9 * (size_t)i).transpose() * ld3(g.y, i);
-        const unsigned q0 = __ldg(g.off + i), q1 = __ldg(g.off + i + 1);
-        unsigned j = q0 < q1 ? __ldg(g.col + q0) : 0u;
-        for (unsigned q = q0; q < q1; ++q) {
-            const unsigned jn = q + 1 < q1 ? __ldg(g.col + q + 1) : 0u;
-            if (j > i) zi += ldm(g.gval + 9 * (size_t)q) * team.ld_shared_vec(g.y, j);
+        const unsigned len = __ldg(g.off + i + 1) - __ldg(g.off + i), q0 = __ldg(g.rbase + i);
+        unsigned j = len ? __ldg(g.scol + q0) : 0u;
+        for (unsigned k = 0; k < len; ++k) {
+            const unsigned q = q0 + 32u * k;
+            const unsigned jn = k + 1 < len ? __ldg(g.scol + q + 32u) : 0u;
+            if (j > i) zi += ldm_sell(g.gval, q) * team.ld_shared_vec(g.y, j);
             j = jn;
         }
         zi += g.eps * (P * ri);
@@ -256,13 +275,15 @@ __global__ void __launch_bounds__(kBT) k_batch_pcg(BatchArgs g) {
         a = e = 0.0f;
         for (unsigned i = i0; i < hi; i += di) {
             Vec3 acc = Vec3::zero(), ab = Vec3::zero();
-            for (unsigned q = __ldg(g.off + i), q1 = __ldg(g.off + i + 1); q < q1; ++q) {
-                const float *m = g.val + 9 * (size_t)q;
-                const Vec3 v = team.ld_shared_vec(g.p, __ldg(g.col + q));
+            const unsigned len = __ldg(g.off + i + 1) - __ldg(g.off + i), q0 = __ldg(g.rbase + i);
+            for (unsigned k = 0; k < len; ++k) {
+                const unsigned q = q0 + 32u * k;
+                const float *m = g.sval + sell_at(q, 0); // entry e at m + 32 e
+                const Vec3 v = team.ld_shared_vec(g.p, __ldg(g.scol + q));
                 Vec3 term;
-                term[0] = __ldg(m + 0) * v[0] + __ldg(m + 3) * v[1] + __ldg(m + 6) * v[2];
-                term[1] = __ldg(m + 1) * v[0] + __ldg(m + 4) * v[1] + __ldg(m + 7) * v[2];
-                term[2] = __ldg(m + 2) * v[0] + __ldg(m + 5) * v[1] + __ldg(m + 8) * v[2];
+                term[0] = __ldg(m + 0) * v[0] + __ldg(m + 96) * v[1] + __ldg(m + 192) * v[2];
+                term[1] = __ldg(m + 32) * v[0] + __ldg(m + 128) * v[1] + __ldg(m + 224) * v[2];
+                term[2] = __ldg(m + 64) * v[0] + __ldg(m + 160) * v[1] + __ldg(m + 256) * v[2];
                 acc += term;
                 ab += term.cwise_abs();
             }
@@ -556,6 +577,46 @@ __global__ void k_batch_fsai_mirror(unsigned rows, const unsigned *off, const un
     }
 }
 
+// Row i's blocks (CSR slots off[i] ..) to their SELL positions rbase[i] +
+// 32 k: columns, and 9 values per block (fp32 operator or bf16 factor).
+__global__ void k_batch_sell_cols(unsigned rows, const unsigned *off, const unsigned *rbase,
+                                  const unsigned *col, unsigned *scol) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows) return;
+    const unsigned q0 = __ldg(off + i), len = __ldg(off + i + 1) - q0, b = __ldg(rbase + i);
+    for (unsigned k = 0; k < len; ++k) scol[b + 32u * k] = __ldg(col + q0 + k);
+}
+template <class T>
+__global__ void k_batch_sell_vals(unsigned rows, const unsigned *off, const unsigned *rbase,
+                                  const T *val, T *sval) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows) return;
+    const unsigned q0 = __ldg(off + i), len = __ldg(off + i + 1) - q0, b = __ldg(rbase + i);
+    for (unsigned k = 0; k < len; ++k)
+#pragma unroll
+        for (int e = 0; e < 9; ++e) sval[sell_at(b + 32u * k, e)] = val[9 * (size_t)(q0 + k) + e];
+}
+
+// SELL-32 positions of a batch: each system's rows in slices of 32 from its
+// first row, a slice as wide as its longest row. Fills rbase (rows) and
+// returns the slices' total blocks.
+size_t sell_layout(unsigned n, const unsigned *row_off, const unsigned *off,
+                   std::vector<unsigned> &rbase) {
+    rbase.assign(row_off[n], 0u);
+    size_t base = 0;
+    for (unsigned s = 0; s < n; ++s)
+        for (unsigned lo = row_off[s]; lo < row_off[s + 1]; lo += 32) {
+            const unsigned hi = std::min(lo + 32u, row_off[s + 1]);
+            unsigned w = 0;
+            for (unsigned i = lo; i < hi; ++i) w = std::max(w, off[i + 1] - off[i]);
+            for (unsigned i = lo; i < hi; ++i) rbase[i] = (unsigned)std::min<size_t>(base + (i - lo), ~0u);
+            base += 32 * (size_t)w;
+        }
+    return base;
+}
+// SELL positions must fit the kernels' 32-bit block index
+constexpr size_t kSellMaxBlocks = 0xFFFFFFFFull - 64;
+
 template <class T> struct Dev {
     T *d = nullptr;
     explicit Dev(size_t n, const T *h = nullptr) {
@@ -612,22 +673,37 @@ cudaError_t launch_teams(const BatchArgs &g, unsigned systems, unsigned ctas, cu
 // A batch uploaded to the device, with its work buffers.
 struct DeviceBatch {
     unsigned n_sys, rows, blocks;
-    Dev<unsigned> row, off, col, it;
-    Dev<float> val, b, x, r, z, p, Ap, inv, res;
+    size_t sell_blocks;
+    Dev<unsigned> row, off, col, it, rbase, scol;
+    Dev<float> val, sval, b, x, r, z, p, Ap, inv, res;
     Dev<int> st;
+    // rbase: sell_layout's positions (sell_blocks in all)
     DeviceBatch(unsigned n, const unsigned *row_off, const unsigned *h_off,
-                const unsigned *h_col, const float *h_val, const float *rhs)
-        : n_sys(n), rows(row_off[n]), blocks(h_off[row_off[n]]), row(n + 1, row_off),
-          off(rows + 1, h_off), col(blocks, h_col), it(n), val(9 * (size_t)blocks, h_val),
-          b(3 * (size_t)rows, rhs), x(3 * (size_t)rows), r(3 * (size_t)rows),
+                const unsigned *h_col, const float *h_val, const float *rhs,
+                const std::vector<unsigned> &h_rbase, size_t sell)
+        : n_sys(n), rows(row_off[n]), blocks(h_off[row_off[n]]), sell_blocks(sell),
+          row(n + 1, row_off), off(rows + 1, h_off), col(blocks, h_col), it(n),
+          rbase(rows, h_rbase.data()), scol(sell), val(9 * (size_t)blocks, h_val),
+          sval(9 * sell), b(3 * (size_t)rows, rhs), x(3 * (size_t)rows), r(3 * (size_t)rows),
           z(3 * (size_t)rows), p(3 * (size_t)rows), Ap(3 * (size_t)rows),
           inv(9 * (size_t)rows), res(n), st(n) {}
+    // the operator's SELL copy (on stream 0)
+    void slice() const {
+        if (!rows) return;
+        k_batch_sell_cols<<<div_up(rows, 256u), 256>>>(rows, off.d, rbase.d, col.d, scol.d);
+        PPF_LAUNCH_CHECK();
+        k_batch_sell_vals<float><<<div_up(rows, 256u), 256>>>(rows, off.d, rbase.d, val.d, sval.d);
+        PPF_LAUNCH_CHECK();
+    }
     BatchArgs args(float tol, unsigned max_iter) const {
         BatchArgs g{};
         g.row_off = row.d;
         g.off = off.d;
         g.col = col.d;
         g.val = val.d;
+        g.rbase = rbase.d;
+        g.scol = scol.d;
+        g.sval = sval.d;
         g.b = b.d;
         g.x = x.d;
         g.r = r.d;
@@ -742,42 +818,54 @@ extern "C" int ppf_batch_pcg(unsigned n_sys, const unsigned *row_off, const unsi
     try {
         if (!valid_batch(n_sys, row_off, off, col, val, rhs)) return -1;
         if (precond != PPF_PRECOND_BLOCK_JACOBI && precond != PPF_PRECOND_FSAI) return -1;
-        DeviceBatch B(n_sys, row_off, off, col, val, rhs);
+        std::vector<unsigned> rbase;
+        const size_t sell = sell_layout(n_sys, row_off, off, rbase);
+        if (sell > kSellMaxBlocks) return -1;
+        DeviceBatch B(n_sys, row_off, off, col, val, rhs, rbase, sell);
         std::vector<unsigned> order;
         std::vector<std::pair<unsigned, unsigned>> groups;
         group_systems(n_sys, row_off, off, order, groups);
         Dev<unsigned> d_order(n_sys, order.data());
         BatchArgs g = B.args(tol, max_iter);
-        // the FSAI factor of every system, timed with the solve
         const bool fsai = precond == PPF_PRECOND_FSAI;
         Dev<float> cinv(fsai ? 9 * (size_t)B.rows : 1), gdiag(fsai ? 9 * (size_t)B.rows : 1),
             yv(fsai ? 3 * (size_t)B.rows : 1);
         Dev<bf16_t> gval(fsai ? 9 * (size_t)B.blocks : 1);
+        Dev<bf16_t> gsell(fsai ? 9 * B.sell_blocks : 1);
+        // the SELL copies (and the FSAI factor), timed with the solve
         float build_ms = 0.0f;
-        if (fsai) {
+        {
             cudaEvent_t b0, b1;
             PPF_CUDA(cudaEventCreate(&b0));
             PPF_CUDA(cudaEventCreate(&b1));
             PPF_CUDA(cudaDeviceSynchronize());
             PPF_CUDA(cudaEventRecord(b0, 0));
-            PPF_CUDA(cudaMemsetAsync(gval.d, 0, 9 * (size_t)B.blocks * sizeof(bf16_t), 0));
-            k_batch_cinv<<<div_up(B.rows, 256u), 256>>>(B.rows, B.off.d, B.col.d, B.val.d, cinv.d);
-            PPF_LAUNCH_CHECK();
-            k_batch_fsai<<<div_up(B.rows, kBfWarps), 32 * kBfWarps>>>(B.rows, B.off.d, B.col.d,
-                                                                      B.val.d, cinv.d, gval.d,
-                                                                      gdiag.d);
-            PPF_LAUNCH_CHECK();
-            k_batch_fsai_mirror<<<div_up(B.rows, 256u), 256>>>(B.rows, B.off.d, B.col.d, gval.d);
-            PPF_LAUNCH_CHECK();
+            B.slice();
+            if (fsai) {
+                PPF_CUDA(cudaMemsetAsync(gval.d, 0, 9 * (size_t)B.blocks * sizeof(bf16_t), 0));
+                k_batch_cinv<<<div_up(B.rows, 256u), 256>>>(B.rows, B.off.d, B.col.d, B.val.d,
+                                                            cinv.d);
+                PPF_LAUNCH_CHECK();
+                k_batch_fsai<<<div_up(B.rows, kBfWarps), 32 * kBfWarps>>>(
+                    B.rows, B.off.d, B.col.d, B.val.d, cinv.d, gval.d, gdiag.d);
+                PPF_LAUNCH_CHECK();
+                k_batch_fsai_mirror<<<div_up(B.rows, 256u), 256>>>(B.rows, B.off.d, B.col.d,
+                                                                    gval.d);
+                PPF_LAUNCH_CHECK();
+                k_batch_sell_vals<bf16_t><<<div_up(B.rows, 256u), 256>>>(B.rows, B.off.d,
+                                                                         B.rbase.d, gval.d,
+                                                                         gsell.d);
+                PPF_LAUNCH_CHECK();
+                g.gval = gsell.d;
+                g.gdiag = gdiag.d;
+                g.y = yv.d;
+                g.eps = 1e-3f;
+            }
             PPF_CUDA(cudaEventRecord(b1, 0));
             PPF_CUDA(cudaEventSynchronize(b1));
             PPF_CUDA(cudaEventElapsedTime(&build_ms, b0, b1));
             cudaEventDestroy(b0);
             cudaEventDestroy(b1);
-            g.gval = gval.d;
-            g.gdiag = gdiag.d;
-            g.y = yv.d;
-            g.eps = 1e-3f;
         }
         const float ms = run_groups(g, d_order.d, groups, one_by_one != 0);
         if (ms < 0.0f) return -1;
@@ -818,7 +906,11 @@ extern "C" int ppf_batch_autotune(unsigned n_sys, const unsigned *row_off, const
                                   float *ms_out) {
     try {
         if (!valid_batch(n_sys, row_off, off, col, val, rhs)) return -1;
-        DeviceBatch B(n_sys, row_off, off, col, val, rhs);
+        std::vector<unsigned> rbase;
+        const size_t sell = sell_layout(n_sys, row_off, off, rbase);
+        if (sell > kSellMaxBlocks) return -1;
+        DeviceBatch B(n_sys, row_off, off, col, val, rhs, rbase, sell);
+        B.slice();
         const BatchArgs g = B.args(tol, max_iter);
         for (unsigned b = 0; b < kBuckets; ++b) {
             // all of the bucket's systems, largest first, in one launch per
