@@ -2,7 +2,8 @@
 
 A batch of uneven scenes (the reference runs one scene per process) gives
 many small Newton systems at a time. ppf_batch_pcg solves all of them with the
-reference's block-Jacobi PCG in one launch, one CTA per system, each to its
+reference's block-Jacobi PCG (or each system's FSAI factor) in one launch per
+team size, one team (a CTA or a thread-block cluster) per system, each to its
 own tolerance and iteration count. This module packs the systems the solver
 itself assembles (ppf_debug_newton_system) into that launch's layout and
 drives it.
@@ -71,6 +72,47 @@ def autotune(packed, tol: float = 1e-3, max_iter: int = 10000):
     return table, ms.reshape(5, 5)
 
 
+def refine(packed, table, ms, tol: float = 1e-3, max_iter: int = 10000, reps: int = 3,
+           rounds: int = 2, margin: float = 0.01):
+    """Whole-batch refinement of a per-bucket table (autotune's).
+
+    autotune times each bucket's systems alone. In a batch all buckets share
+    the GPU, and a smaller team in one bucket can leave room for the others.
+    Coordinate descent: each present bucket in turn tries the team sizes
+    autotune could run (ms >= 0), timing the whole batch (best of `reps`),
+    and keeps a change that saves more than `margin`; at most `rounds`
+    sweeps. Sets the library's table to the result and returns
+    (table, batch ms)."""
+    ms = np.asarray(ms).reshape(5, 5)
+
+    def cost(t):
+        team_ctas(t)
+        return min(solve(packed, tol, max_iter)["ms"] for _ in range(reps))
+
+    best_t = [int(v) for v in table]
+    best = cost(best_t)
+    seen = {tuple(best_t): best}
+    for _ in range(rounds):
+        improved = False
+        for b in range(5):
+            if not (ms[b] >= 0).any():
+                continue  # no system in this bucket
+            for c, size in enumerate(TEAM_SIZES):
+                if ms[b, c] < 0 or size == best_t[b]:
+                    continue
+                t = list(best_t)
+                t[b] = size
+                if tuple(t) in seen:
+                    continue
+                m = seen[tuple(t)] = cost(t)
+                if m < best * (1.0 - margin):
+                    best, best_t, improved = m, t, True
+        if not improved:
+            break
+    team_ctas(best_t)
+    return np.array(best_t, np.uint32), best
+
+
 def full_rows(sample: dict):
     """Both-triangle block rows (off, col, val) of a captured Newton system:
     every upper block (r, c) of the fixed pattern and the contact blocks, and
@@ -121,7 +163,8 @@ def solve(packed, tol: float = 1e-3, max_iter: int = 10000, one_by_one: bool = F
           precond: int = abi.PRECOND_BLOCK_JACOBI) -> dict:
     """Solves every packed system (block-Jacobi, or abi.PRECOND_FSAI); returns
     x (rows x 3), and per system the iterations, relative L1 residual and
-    state, and the device time (the FSAI factor build included)."""
+    state, and the device time (the operator's SELL-32 copy and the FSAI
+    factor build included)."""
     lib = product()
     _declare(lib)
     row_off, off, col, val, rhs = packed
@@ -158,7 +201,8 @@ def capture_drop(params, extra_steps: int = 3) -> dict:
 
 def run_bench(count: int = 256, seed: int = 0, reps: int = 3) -> dict:
     """Captures the uneven drops' Newton systems, autotunes the team sizes
-    and times the batch against one launch per system; returns the figures.
+    (per bucket, then refined on the whole batch) and times the batch
+    against one launch per system; returns the figures.
     Leaves the library's team-size table as it found it."""
     a = argparse.Namespace(count=count, seed=seed, reps=reps)
     t0 = time.time()
@@ -169,7 +213,8 @@ def run_bench(count: int = 256, seed: int = 0, reps: int = 3) -> dict:
     default_table = team_ctas()
     solve(packed)  # warm-up
     default_ms = min(solve(packed)["ms"] for _ in range(a.reps))
-    table, tune_ms = autotune(packed)
+    bucket_table, tune_ms = autotune(packed)
+    table, _ = refine(packed, bucket_table, tune_ms)
     batched = min((solve(packed) for _ in range(a.reps)), key=lambda r: r["ms"])
     single = min((solve(packed, one_by_one=True) for _ in range(a.reps)), key=lambda r: r["ms"])
     same = bool(np.array_equal(batched["x"], single["x"]) and
@@ -192,7 +237,8 @@ def run_bench(count: int = 256, seed: int = 0, reps: int = 3) -> dict:
         "vertices_min_max": [min(verts), max(verts)], "blocks": int(packed[1][-1]),
         "batched_ms": round(batched["ms"], 3), "one_launch_per_system_ms": round(single["ms"], 3),
         "team_ctas_default": [int(v) for v in default_table], "batched_ms_default_teams":
-            round(default_ms, 3), "team_ctas_autotuned": [int(v) for v in table],
+            round(default_ms, 3), "team_ctas_per_bucket": [int(v) for v in bucket_table],
+        "team_ctas_autotuned": [int(v) for v in table],
         "autotune_ms": {BUCKETS[b]: {str(TEAM_SIZES[c]): round(float(tune_ms[b, c]), 3)
                                      for c in range(5) if tune_ms[b, c] >= 0}
                         for b in range(5) if (tune_ms[b] >= 0).any()},

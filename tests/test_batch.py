@@ -83,6 +83,44 @@ def test_packed_rows_are_the_operator():
         np.testing.assert_array_equal(packed[4][3 * 60 * s:3 * 60 * (s + 1)], smp["force"])
 
 
+def test_refine_keeps_the_fastest_whole_batch_table(monkeypatch):
+    """The whole-batch refinement (CPU, with the library calls replaced by a
+    cost model): it moves one bucket at a time to a faster team size, tries
+    only the sizes the per-bucket tuner could run, ignores changes within the
+    noise margin, and leaves the library's table at its answer."""
+    from ppf_gb300 import batch
+
+    state = {"table": [1, 1, 1, 1, 1], "calls": 0}
+
+    def fake_team_ctas(table=None):
+        if table is not None:
+            state["table"] = [int(v) for v in table]
+        return np.array(state["table"], np.uint32)
+
+    def fake_solve(packed, tol=1e-3, max_iter=10000, **kw):
+        t = state["table"]
+        state["calls"] += 1
+        # bucket 3 is best at 4 CTAs, bucket 4 at 16, bucket 1 indifferent
+        # within 0.5 %; bucket 0 and 2 fixed by the tuner's ms
+        ms = 30.0 + 3.0 * abs(t[3] - 4) / 4 + (0.0 if t[4] == 16 else 5.0)
+        ms += 0.1 if t[1] == 1 else 0.0
+        return {"ms": ms}
+
+    monkeypatch.setattr(batch, "team_ctas", fake_team_ctas)
+    monkeypatch.setattr(batch, "solve", fake_solve)
+    ms = np.full((5, 5), -1.0)
+    ms[0, 0] = 1.0
+    ms[1, :2] = [2.0, 1.5]
+    ms[3, :4] = [9.0, 5.0, 3.0, 2.0]
+    ms[4, :] = [9.0, 6.0, 4.0, 3.0, 2.0]
+    table, best = batch.refine(None, [1, 2, 1, 8, 16], ms, reps=1)
+    assert table.tolist() == [1, 2, 1, 4, 16] and best == 30.0
+    assert state["table"] == [1, 2, 1, 4, 16]
+    # a start away from the optimum in two buckets
+    table, best = batch.refine(None, [1, 2, 1, 1, 2], ms, reps=1)
+    assert table.tolist() == [1, 2, 1, 4, 16] and best == 30.0
+
+
 @pytest.mark.gpu
 def test_batch_equals_one_launch_per_system(product_lib):
     from ppf_gb300 import batch
