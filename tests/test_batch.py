@@ -83,6 +83,33 @@ def test_packed_rows_are_the_operator():
         np.testing.assert_array_equal(packed[4][3 * 60 * s:3 * 60 * (s + 1)], smp["force"])
 
 
+def test_batch_rejects_invalid_input(product_lib):
+    """The batch entry points check their input on the host before any device
+    work (so this runs without a GPU): a column that points into another
+    system, decreasing row offsets, an unknown preconditioner and a team size
+    that is not 1, 2, 4, 8 or 16 are refused, and a refused table leaves the
+    library's table as it was."""
+    from ppf_gb300 import abi, batch
+
+    packed = batch.pack(_samples([1, 2], n=40))
+    row_off, off, col, val, rhs = packed
+    bad_col = col.copy()
+    bad_col[0] = 50  # row 0 is system 0's; row 50 is system 1's
+    with pytest.raises(ValueError):
+        batch.solve((row_off, off, bad_col, val, rhs))
+    bad_rows = row_off.copy()
+    bad_rows[1] = 90  # past the end of the next system
+    with pytest.raises(ValueError):
+        batch.solve((bad_rows, off, col, val, rhs))
+    with pytest.raises(ValueError):
+        batch.solve(packed, precond=3)
+    assert abi.PRECOND_FSAI != 3
+    before = batch.team_ctas().tolist()
+    with pytest.raises(ValueError):
+        batch.team_ctas([1, 3, 1, 1, 1])
+    assert batch.team_ctas().tolist() == before
+
+
 def test_refine_keeps_the_fastest_whole_batch_table(monkeypatch):
     """The whole-batch refinement (CPU, with the library calls replaced by a
     cost model): it moves one bucket at a time to a faster team size, tries
