@@ -360,21 +360,29 @@ bool initialize(PpfDataSet *dataset, PpfParamSet *param);
  * BVH rebuild, inertial target, Newton loop (assembly, block-Jacobi PCG,
  * additive-CCD line search, strain-limit line search), commit. */
 void advance(PpfStepResult *result);
-/* main.cu:1926-1937.  Device -> host copy of vertex.curr/prev (and the per
- * object contact statistics when present). */
+/* main.cu:1926-1937.  Device -> host copy of vertex.curr/prev. The optional
+ * per-object contact statistics (statistics_contact_count) are not counted
+ * by this library; a host array given for them is left as it is. */
 void fetch(void);
-/* main.cu:1939-1948 */
+/* main.cu:1939-1948.  Device -> host copy of the rest-shape inverses
+ * (inv_rest2x2; update_rest_shape is what changes them on the device). */
 void fetch_inv_rest(void);
-/* main.cu:1950-1968 */
+/* main.cu:1950-1968.  Device -> host copy of the hinge and vertex props,
+ * which carry the rest angles. Nothing on the device changes them in this
+ * library (bend plasticity is not built), so the copy returns what the host
+ * last uploaded. */
 void fetch_rest_angles(void);
-/* main.cu:1970-1977.  Size of the carried dynamic contact pattern. */
+/* main.cu:1970-1977.  Size of the carried dynamic contact pattern: the
+ * last assembly's, or the one update_dyn restored since. */
 void fetch_dyn_counts(unsigned *n_value, unsigned *n_offset);
 /* main.cu:1979-1982.  Carried dynamic contact pattern (row offsets and
  * column indices of the upper-triangle contact blocks outside the fixed
  * pattern); value may be NULL. */
 void fetch_dyn(unsigned *index, PpfMat3x3f *value, unsigned *offset);
 /* main.cu:1984-1986.  Restores a carried pattern (checkpoint resume). The
- * pattern only seeds capacity; it never changes values. */
+ * pattern only seeds capacity; it never changes values. It reserves the
+ * contact-block buffers for its count and is what fetch_dyn_counts /
+ * fetch_dyn report until the next assembly. */
 void update_dyn(unsigned *index, unsigned *offset);
 /* main.cu:1988-2077 */
 void update_constraint(const PpfConstraint *constraint);
@@ -402,7 +410,9 @@ unsigned fetch_intersection_records(PpfIntersectionRecord *out,
 /* main.cu:1662-1668 */
 unsigned char ppf_fatal_code(void);
 const char *ppf_fatal_detail(void);
-/* main.cu:1680-1682 */
+/* main.cu:1680-1682.  Creates data_dir and appends per-step logs there in
+ * SimpleLog's format: advance.out ("time msec") and advance.<channel>.out
+ * for the channels iter, toi, num_contact, newton_steps and final_dt. */
 void set_log_path(const char *data_dir);
 
 /* Fatal codes (crates/ppf-cts-solver/src/cpp/main/fatal.hpp:48-55). */

@@ -44,30 +44,56 @@ int ppf_radix_sort_host(unsigned *keys, unsigned *vals, unsigned n,
                         int key_bits);
 
 /* Same sort on device memory, asynchronous on `stream`; scratch is allocated
- * by the library on first use and kept. */
+ * by the library on first use and kept. Returns 0, or -1 on a CUDA error at
+ * launch. The sort's own status (a look-back wait that ran out, which leaves
+ * the pairs unsorted) is reset at the start of every call and read with
+ * ppf_radix_sort_device_status. */
 int ppf_radix_sort_device(unsigned *d_keys, unsigned *d_vals, unsigned n,
                           int key_bits, void *stream);
 
+/* Status bits of the last ppf_radix_sort_device call ordered before this one
+ * on `stream`. Waits for the stream, then returns 0 (sorted) or a set of
+ * device status bits (1: a look-back wait ran out; the pairs are not
+ * sorted), or -1 on a CUDA error. */
+int ppf_radix_sort_device_status(void *stream);
+
 /* The same sort with no allocation at all. It has no counterpart in the
  * reference. Its scratch (two ping-pong arrays, look-back words, histograms,
- * counters) lives in static device arrays sized for at most
- * PPF_NOALLOC_SORT_MAX_PAIRS pairs (about 8.5 MB per device), and neither the
- * call nor its first use on a device allocates memory. It is for callers that
- * must not allocate: a per-frame loop where a cudaMalloc / cudaFree would
- * synchronize the device, or a host whose allocator owns the device memory.
+ * counters, a status word) lives in static device arrays sized for at most
+ * PPF_NOALLOC_SORT_MAX_PAIRS pairs (about 8.5 MB per device). It is for
+ * callers that must not allocate: a per-frame loop where a cudaMalloc /
+ * cudaFree would synchronize the device, or a host whose allocator owns the
+ * device memory.
+ *   - The static scratch is reserved when the library's device code is
+ *     loaded on a device. Under lazy module loading (CUDA_MODULE_LOADING=LAZY,
+ *     the CUDA 12+ default) that happens at the first call on each device,
+ *     which can fail when the host's pool already owns the device memory. A
+ *     caller that must not allocate later makes one warm-up call at its own
+ *     initialisation, for example with n = 0: that call performs the set-up
+ *     below and sorts nothing.
  *   - n > PPF_NOALLOC_SORT_MAX_PAIRS: returns -2, prints one line to stderr
  *     and touches nothing.
  *   - The first call on each device looks up the scratch addresses
  *     (cudaGetSymbolAddress) with that device current; make it before any
- *     stream capture begins.
- *   - Every call resets the histograms, counters and look-back words it uses
- *     on `stream`; nothing needs zeroing by the caller.
+ *     stream capture begins. Concurrent first calls from several host
+ *     threads are safe (the set-up runs once per device).
+ *   - Every call resets the status word, histograms, counters and look-back
+ *     words it uses on `stream`; nothing needs zeroing by the caller.
  *   - There is one scratch set per device: calls that overlap in time (on any
  *     streams) race on it, so the caller orders them.
- * Asynchronous on `stream`: the result is ready once the stream is. */
+ * Asynchronous on `stream`: the result is ready once the stream is. A
+ * look-back wait that runs out leaves the pairs unsorted and is reported by
+ * ppf_radix_sort_noalloc_status, not by this return code. */
 #define PPF_NOALLOC_SORT_MAX_PAIRS (1u << 20)
 int ppf_radix_sort_device_noalloc(unsigned *d_keys, unsigned *d_vals,
                                   unsigned n, int key_bits, void *stream);
+
+/* Status bits of the last ppf_radix_sort_device_noalloc call ordered before
+ * this one on `stream` (the current device's static status word). Waits for
+ * the stream, then returns 0 (sorted), 1 (a look-back wait ran out: the pairs
+ * are not sorted), or -1 on a CUDA error. Allocates nothing. The next sort
+ * on the device resets the word, so read it before the next call. */
+int ppf_radix_sort_noalloc_status(void *stream);
 
 /* ---- per-step statistics ------------------------------------------------
  * The reference logs these per step through SimpleLog channels (newton_steps,

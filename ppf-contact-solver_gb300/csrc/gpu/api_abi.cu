@@ -7,8 +7,12 @@
 #include "schwarz.cuh"
 #include "solver.cuh"
 
+#include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
+#include <sys/stat.h>
 #include <vector>
 
 using ppf::FatalError;
@@ -44,6 +48,38 @@ struct Windows {
 } g_win;
 constexpr unsigned kMaxCollisionWindows = 8; // main.cu:45
 
+// Per-step log files in the directory set_log_path names, in the format of
+// the reference's SimpleLog (simplelog/SimpleLog.cpp:86-120): `advance.out`
+// holds "time msec" per step, and `advance.<channel>.out` one "time value"
+// line per value marked in the step (integers as %d, others as %e), with
+// time the simulation time at the start of the step (main.cu:329).
+struct StepLog {
+    std::string dir;
+    void line(const char *channel, double t, double v) const {
+        std::string path = dir + "/advance" + (channel[0] ? "." : "") + channel + ".out";
+        FILE *fp = std::fopen(path.c_str(), "a");
+        if (!fp) return;
+        if (std::fmod(v, 1.0) == 0.0 && std::fabs(v) < 2e9)
+            std::fprintf(fp, "%f %d\n", t, (int)v);
+        else
+            std::fprintf(fp, "%f %e\n", t, v);
+        std::fclose(fp);
+    }
+    void step(double t, const ppf::gpu::StepStats &s, double final_dt) const {
+        if (dir.empty()) return;
+        FILE *fp = std::fopen((dir + "/advance.out").c_str(), "a");
+        if (fp) {
+            std::fprintf(fp, "%f %lu\n", t, (unsigned long)s.step_ms);
+            std::fclose(fp);
+        }
+        for (size_t k = 0; k < s.pcg_iters.size(); ++k) line("iter", t, s.pcg_iters[k]);
+        for (size_t k = 0; k < s.toi.size(); ++k) line("toi", t, s.toi[k]);
+        line("num_contact", t, s.max_contacts);
+        line("newton_steps", t, s.newton_iters);
+        line("final_dt", t, final_dt);
+    }
+} g_log;
+
 } // namespace
 
 extern "C" {
@@ -63,7 +99,10 @@ bool initialize(PpfDataSet *dataset, PpfParamSet *param) {
 
 void advance(PpfStepResult *result) {
     try {
+        const double t0 = solver_instance().param ? solver_instance().param->time : 0.0;
         *result = solver_instance().advance();
+        if (!g_log.dir.empty())
+            g_log.step(t0, solver_instance().stats(), solver_instance().param->prev_dt);
     } catch (const FatalError &e) {
         fatal(e);
         std::memset(result, 0, sizeof(*result));
@@ -78,9 +117,21 @@ void fetch(void) {
     }
 }
 
-void fetch_inv_rest(void) {}
+void fetch_inv_rest(void) {
+    try {
+        solver_instance().fetch_inv_rest();
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
 
-void fetch_rest_angles(void) {}
+void fetch_rest_angles(void) {
+    try {
+        solver_instance().fetch_rest_angles();
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
 
 void fetch_dyn_counts(unsigned *n_value, unsigned *n_offset) {
     try {
@@ -99,11 +150,11 @@ void fetch_dyn(unsigned *index, PpfMat3x3f *value, unsigned *offset) {
 }
 
 void update_dyn(unsigned *index, unsigned *offset) {
-    // The carried pattern only seeds capacity in the reference; here the
-    // contact blocks are re-derived every Newton iteration, so there is
-    // nothing to restore.
-    (void)index;
-    (void)offset;
+    try {
+        solver_instance().update_dyn(index, offset);
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
 }
 
 void update_constraint(const PpfConstraint *constraint) {
@@ -185,7 +236,10 @@ unsigned fetch_intersection_records(PpfIntersectionRecord *out, unsigned max_cou
 
 unsigned char ppf_fatal_code(void) { return g_ppf_fatal_code; }
 const char *ppf_fatal_detail(void) { return g_ppf_fatal_detail; }
-void set_log_path(const char *data_dir) { (void)data_dir; }
+void set_log_path(const char *data_dir) {
+    g_log.dir = data_dir ? data_dir : "";
+    if (!g_log.dir.empty()) mkdir(g_log.dir.c_str(), 0775);
+}
 
 // ---- extensions -------------------------------------------------------------
 void ppf_step_stats(PpfStepStats *out) {

@@ -145,15 +145,42 @@ extern "C" int ppf_radix_sort_device_noalloc(unsigned *d_keys, unsigned *d_vals,
     }
 }
 
+namespace {
+// Status word of the allocating device-memory sort: reset on the caller's
+// stream at the start of every call, read by ppf_radix_sort_device_status.
+StatusWord *g_sort_status = nullptr;
+RadixSortWorkspace g_sort_ws;
+} // namespace
+
 extern "C" int ppf_radix_sort_device(unsigned *d_keys, unsigned *d_vals,
                                      unsigned n, int key_bits, void *stream) {
     try {
-        static RadixSortWorkspace ws;
-        static StatusWord *status = nullptr;
-        if (!status) status = new StatusWord();
-        radix_sort_pairs(d_keys, d_vals, n, key_bits, ws, status->d,
+        if (!g_sort_status) g_sort_status = new StatusWord();
+        PPF_CUDA(cudaMemsetAsync(g_sort_status->d, 0, sizeof(unsigned), (cudaStream_t)stream));
+        radix_sort_pairs(d_keys, d_vals, n, key_bits, g_sort_ws, g_sort_status->d,
                          (cudaStream_t)stream);
         return 0;
+    } catch (const FatalError &e) {
+        return report(e);
+    }
+}
+
+extern "C" int ppf_radix_sort_device_status(void *stream) {
+    try {
+        if (!g_sort_status) return 0;
+        unsigned h = 0;
+        PPF_CUDA(cudaMemcpyAsync(&h, g_sort_status->d, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                 (cudaStream_t)stream));
+        PPF_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+        return (int)h;
+    } catch (const FatalError &e) {
+        return report(e);
+    }
+}
+
+extern "C" int ppf_radix_sort_noalloc_status(void *stream) {
+    try {
+        return (int)radix_sort_noalloc_status((cudaStream_t)stream);
     } catch (const FatalError &e) {
         return report(e);
     }

@@ -2,6 +2,8 @@
 #include "fatal.cuh"
 #include "radix_sort.cuh"
 
+#include <mutex>
+
 namespace ppf {
 namespace gpu {
 
@@ -248,32 +250,34 @@ __device__ __align__(256) unsigned g_na_status[1];
 struct NoAllocScratch {
     unsigned *keys = nullptr, *vals = nullptr, *lookback = nullptr;
     unsigned *hist = nullptr, *ctr = nullptr, *status = nullptr;
-    bool ready = false;
 };
 constexpr int kMaxDevices = 64;
 NoAllocScratch g_na[kMaxDevices];
+std::once_flag g_na_once[kMaxDevices];
 
 template <class T> void symbol_address(unsigned **out, const T &sym) {
     PPF_CUDA(cudaGetSymbolAddress((void **)out, sym));
 }
 
 // Device addresses of the scratch arrays for the current device, looked up
-// once per device.
+// once per device under a once-flag, so two host threads making their first
+// call on one device do not race. A lookup that throws leaves the flag unset
+// and the next call tries again.
 const NoAllocScratch &noalloc_scratch() {
     int dev = 0;
     PPF_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) throw FatalError(3, "device ordinal out of range");
-    NoAllocScratch &s = g_na[dev];
-    if (!s.ready) {
+    std::call_once(g_na_once[dev], [dev] {
+        NoAllocScratch s;
         symbol_address(&s.keys, g_na_keys);
         symbol_address(&s.vals, g_na_vals);
         symbol_address(&s.lookback, g_na_lookback);
         symbol_address(&s.hist, g_na_hist);
         symbol_address(&s.ctr, g_na_ctr);
         symbol_address(&s.status, g_na_status);
-        s.ready = true;
-    }
-    return s;
+        g_na[dev] = s;
+    });
+    return g_na[dev];
 }
 
 } // namespace
@@ -281,16 +285,17 @@ const NoAllocScratch &noalloc_scratch() {
 int radix_sort_pairs_noalloc(unsigned *keys, unsigned *vals, unsigned n, int key_bits,
                              cudaStream_t stream) {
     if (n > kNoAllocMaxPairs) return -2;
-    if (n <= 1 || key_bits <= 0) return 0;
+    // set-up first, so that a call with n = 0 performs it (a warm-up call)
     const NoAllocScratch &s = noalloc_scratch();
+    PPF_CUDA(cudaMemsetAsync(s.status, 0, sizeof(unsigned), stream));
+    if (n <= 1 || key_bits <= 0) return 0;
     int passes = (key_bits + 7) / 8;
     if (passes > 4) passes = 4;
     const unsigned tiles = div_up(n, kSortTile);
-    // the histograms, tile counters and status start at zero every call; the
-    // look-back words start at zero every pass
+    // the histograms and tile counters start at zero every call (the status
+    // word was cleared above); the look-back words start at zero every pass
     PPF_CUDA(cudaMemsetAsync(s.hist, 0, 4 * kRadix * sizeof(unsigned), stream));
     PPF_CUDA(cudaMemsetAsync(s.ctr, 0, 4 * sizeof(unsigned), stream));
-    PPF_CUDA(cudaMemsetAsync(s.status, 0, sizeof(unsigned), stream));
     unsigned hgrid = tiles < 4 * kNumSMs ? tiles : 4 * kNumSMs;
     k_digit_histograms<<<hgrid, 256, 0, stream>>>(keys, n, passes, s.hist);
     PPF_LAUNCH_CHECK();
@@ -317,6 +322,14 @@ int radix_sort_pairs_noalloc(unsigned *keys, unsigned *vals, unsigned n, int key
                                  stream));
     }
     return 0;
+}
+
+unsigned radix_sort_noalloc_status(cudaStream_t stream) {
+    const NoAllocScratch &s = noalloc_scratch();
+    unsigned h = 0;
+    PPF_CUDA(cudaMemcpyAsync(&h, s.status, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+    PPF_CUDA(cudaStreamSynchronize(stream));
+    return h;
 }
 
 } // namespace gpu

@@ -39,6 +39,9 @@ void radix_sort_pairs(unsigned *keys, unsigned *vals, unsigned n, int key_bits,
 constexpr unsigned kNoAllocMaxPairs = 1u << 20;
 int radix_sort_pairs_noalloc(unsigned *keys, unsigned *vals, unsigned n, int key_bits,
                              cudaStream_t stream);
+// Status bits of the last allocation-free sort ordered before this call on
+// `stream` (waits for the stream): 0, or STATUS_SORT_LOOKBACK_TIMEOUT.
+unsigned radix_sort_noalloc_status(cudaStream_t stream);
 
 } // namespace gpu
 } // namespace ppf

@@ -575,6 +575,7 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     pcg_.reserve(n_);
     upload_collision_mesh(ds->constraint.mesh);
     initialized_ = true;
+    carried_ = false;
     // initial trees and intersection check on prev and curr (main.cu:196-262)
     if (!param->disable_contact) {
         build_trees(curr_.data(), curr_.data(), 1.0f, true);
@@ -765,6 +766,7 @@ void Solver::assemble(float dt) {
     dyn_.cap = dcap;
     PPF_CUDA(cudaMemsetAsync(&st_.data()->n_dyn, 0, sizeof(unsigned), q_));
     launch_dyn_build(s, b, pairs_, counts, dyn_, dcap, scan_tmp_.data(), q_);
+    carried_ = false;
     PPF_CUDA(cudaMemsetAsync(dval_buf_.data(), 0, 9 * (size_t)dcap * sizeof(float), q_));
     launch_contact_assemble(s, p, b, pairs_, counts, dyn_, q_);
     launch_vertex_constraints(s, p, b, q_);
@@ -980,12 +982,67 @@ void Solver::fetch() {
 
 void Solver::fetch_dyn_counts(unsigned *n_value, unsigned *n_offset) {
     *n_offset = n_ + 1;
+    if (carried_) {
+        *n_value = carried_off_[n_];
+        return;
+    }
     unsigned v = 0;
+    PPF_CUDA(cudaStreamSynchronize(q_));
     if (dyn_.off) PPF_CUDA(cudaMemcpy(&v, dyn_.off + n_, sizeof(unsigned), cudaMemcpyDeviceToHost));
     *n_value = v;
 }
 
+// The reference restores its carried contact pattern from a saved state
+// (main.cu:1985-1987, csrmat.cu:146-153). That pattern seeds the capacity of
+// the next assembly and never changes its values. Here the contact blocks are
+// re-derived every Newton iteration, so the restored pattern reserves the
+// contact-block buffers for its count and is what fetch_dyn reports until an
+// assembly replaces it: a state saved, restored and saved again writes the
+// same pattern.
+void Solver::update_dyn(const unsigned *index, const unsigned *offset) {
+    if (!initialized_ || !offset) return;
+    carried_off_.assign(offset, offset + n_ + 1);
+    for (unsigned i = 0; i < n_; ++i)
+        if (carried_off_[i + 1] < carried_off_[i])
+            throw FatalError(4, "update_dyn: row offsets decrease");
+    const unsigned nnz = carried_off_[n_];
+    carried_col_.assign(index, index + nnz);
+    for (unsigned c : carried_col_)
+        if (c >= n_) throw FatalError(4, "update_dyn: column index out of range");
+    carried_ = true;
+    const unsigned cap = std::max(nnz, 16u);
+    dcol_buf_.reserve(cap);
+    dtr_buf_.reserve(cap);
+    dval_buf_.reserve(9 * (size_t)cap);
+}
+
+void Solver::fetch_inv_rest() {
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    const size_t n = host->inv_rest2x2.size;
+    if (n && inv_rest_.data())
+        PPF_CUDA(cudaMemcpy(host->inv_rest2x2.data, inv_rest_.data(), n * sizeof(PpfMat2x2f),
+                            cudaMemcpyDeviceToHost));
+}
+
+void Solver::fetch_rest_angles() {
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    if (nh_ && host->prop.hinge.size)
+        PPF_CUDA(cudaMemcpy(host->prop.hinge.data, hprop_.data(), nh_ * sizeof(PpfHingeProp),
+                            cudaMemcpyDeviceToHost));
+    if (n_ && host->prop.vertex.size)
+        PPF_CUDA(cudaMemcpy(host->prop.vertex.data, vprop_.data(), n_ * sizeof(PpfVertexProp),
+                            cudaMemcpyDeviceToHost));
+}
+
 void Solver::fetch_dyn(unsigned *index, PpfMat3x3f *value, unsigned *offset) {
+    if (carried_) {
+        std::memcpy(offset, carried_off_.data(), (n_ + 1) * sizeof(unsigned));
+        if (!carried_col_.empty())
+            std::memcpy(index, carried_col_.data(), carried_col_.size() * sizeof(unsigned));
+        if (value) std::memset(value, 0, carried_col_.size() * sizeof(PpfMat3x3f));
+        return;
+    }
+    PPF_CUDA(cudaStreamSynchronize(q_));
     std::vector<unsigned> off(n_ + 1, 0u);
     if (dyn_.off)
         PPF_CUDA(cudaMemcpy(off.data(), dyn_.off, (n_ + 1) * sizeof(unsigned), cudaMemcpyDeviceToHost));

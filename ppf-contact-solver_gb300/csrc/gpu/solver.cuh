@@ -42,6 +42,9 @@ class Solver {
     void update_rest_shape(const PpfRestShapeUpdate *u);
     void fetch_dyn_counts(unsigned *n_value, unsigned *n_offset);
     void fetch_dyn(unsigned *index, PpfMat3x3f *value, unsigned *offset);
+    void update_dyn(const unsigned *index, const unsigned *offset);
+    void fetch_inv_rest();
+    void fetch_rest_angles();
     void override_velocity(const unsigned *idx, unsigned count, float vx, float vy,
                            float vz, float dt);
     void override_angular_velocity(const unsigned *idx, unsigned count, float wx,
@@ -135,6 +138,10 @@ class Solver {
     DevBuf<uint2> dtr_buf_;
     DevBuf<float> dval_buf_;
     DevBuf<unsigned> scan_tmp_;
+    // contact pattern restored by update_dyn (a resumed run's carried
+    // pattern): reported by fetch_dyn until the next assembly replaces it
+    std::vector<unsigned> carried_off_, carried_col_;
+    bool carried_ = false;
     PcgWorkspace pcg_;
     // factored preconditioner (block-Jacobi stays the fallback)
     int precond_kind_ = 0;

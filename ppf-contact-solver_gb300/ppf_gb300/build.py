@@ -125,10 +125,17 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
+def reference_root() -> Path:
+    """The reference checkout: $PPF_REF_ROOT, else a ``reference`` directory
+    beside this repository's root."""
+    env = os.environ.get("PPF_REF_ROOT")
+    return Path(env) if env else ROOT.parent / "reference"
+
+
 def build_reference(force: bool = False) -> Path | None:
     """Compile the reference's header-only element math where its sources are
     present (oracle/Makefile); returns None when they are not."""
-    ref_root = Path(os.environ.get("PPF_REF_ROOT", "/root/reference"))
+    ref_root = reference_root()
     if not (ref_root / "crates/ppf-cts-solver/src/cpp/data.hpp").exists():
         return None
     if shutil.which("make") is None:

@@ -38,7 +38,7 @@ def layout():
 
     import abi_fields
 
-    cpp = Path("/root/reference/crates/ppf-cts-solver/src/cpp")
+    cpp = build.reference_root() / "crates/ppf-cts-solver/src/cpp"
     shim = [
         "#include <algorithm>", "#include <cmath>",
         "using std::max; using std::min; using std::isfinite;",
