@@ -248,23 +248,37 @@ def run_ours(args, rank, local_rank, world):
     # ---- end to end through the C ABI, host buffers --------------------------
     s = restart()
     n = sc.vertex_count
-    # update_constraint uploads the fix pins (36 B each, PpfFixPair) and the
-    # scene's analytic colliders; fetch reads curr and prev back (12 B each)
-    h2d = sc.n_pins * 36 + sc.n_spheres * 32 + sc.n_floors * 40
-    d2h = 2 * 12 * n
+    # the bytes update_constraint, advance and fetch copy between host and
+    # device, counted by the library itself (ppf_transfer_bytes)
+    lib.ppf_transfer_bytes.argtypes = [C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]
+    lib.ppf_transfer_bytes.restype = None
+    h0, d0 = C.c_ulonglong(), C.c_ulonglong()
+    h1, d1 = C.c_ulonglong(), C.c_ulonglong()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     e2e_newton = 0
+    first_step_x = None   # the GPU's positions after the first timed step
+    contact_state = None  # the state after the first step with self-contact
+    lib.ppf_transfer_bytes(C.byref(h0), C.byref(d0))
     t0 = time.perf_counter()
     for k in range(args.steps):
         lib.update_constraint(sc.constraint)
         r = s.step(fetch=True)
         if not r.success():
             raise RuntimeError(f"e2e step {k} failed: {r.as_dict()}")
-        e2e_newton += s.stats().newton_iters
+        st = s.stats()
+        e2e_newton += st.newton_iters
+        if k == 0:
+            first_step_x = sc.positions()[0]
+        if contact_state is None and st.max_dyn_blocks > 0:
+            contact_state = (k, *sc.positions(),
+                             abi.ParamSet.from_buffer_copy(sc.param.contents))
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    lib.ppf_transfer_bytes(C.byref(h1), C.byref(d1))
+    h2d = (h1.value - h0.value) // args.steps
+    d2h = (d1.value - d0.value) // args.steps
     e2e_value = e2e_newton / e2e_s
     if dist:
         e2e_s, e2e_all = aggregate(dist, "cuda", e2e_s, e2e_newton)
@@ -316,9 +330,15 @@ def run_ours(args, rank, local_rank, world):
                 "per_solve": {"fields": ["step", "iters", "ms", "contact_blocks"],
                               "rows": per_solve[:64]}},
         "newton_iters": newton_all, "max_contacts": max_contacts,
+        "contact": {"solves": len(per_solve),
+                    "solves_with_contact_blocks": sum(1 for r in per_solve if r[3] > 0),
+                    "contact_blocks_max": max((r[3] for r in per_solve), default=0),
+                    "max_active_contacts": max_contacts},
         "roofline": roofline,
         "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
+                "bytes": "counted by the library at its host<->device copies "
+                         "(ppf_transfer_bytes), mean per timed step",
                 "path": "update_constraint + advance + fetch (C ABI, host DataSet)"},
         "gpu_launches": launches,
         "clocks": clocks,
@@ -334,7 +354,9 @@ def run_ours(args, rank, local_rank, world):
 
         out["batched_pcg"] = batch.run_bench(args.batch_count, seed=0, reps=3)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(sc, curr0, prev0, param0, CPU_SAMPLE_SECONDS)
+        out["cpu_baseline"], first_o = cpu_baseline(sc, curr0, prev0, param0,
+                                                    CPU_SAMPLE_SECONDS)
+        out["parity"] = parity_check(sc, lib, first_step_x, first_o, contact_state)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -406,9 +428,66 @@ def compare_preconditioners(restart, sc, lib, stream, steps):
     return out
 
 
-def _oracle_run(sc, curr0, prev0, param0, budget_s, max_steps=None, warmup=0):
+def parity_check(sc, lib, first_gpu, first_oracle, contact_state):
+    """The oracle as checker of this run, outside every timed region.
+
+    * first timed step: the oracle's first step of the CPU-baseline sample
+      starts from the same state as the GPU's first timed step (t = 0); the
+      positions after it must agree within 1e-5 relative.
+    * first self-contact Newton system: the GPU state after the first timed
+      step that assembled contact blocks is loaded into both the library and
+      the oracle, each assembles and solves its first Newton system, and the
+      pair sets are compared with the pairs within 1e-6 * ghat of the gap
+      threshold listed (oracle/parity.py)."""
+    import ctypes as C
+
+    import numpy as np
+
+    from oracle import binding, parity
+    from ppf_gb300.session import Session
+
+    out = {}
+    if first_gpu is not None and first_oracle is not None:
+        err = float(np.abs(first_gpu - first_oracle).max()) / float(np.abs(first_oracle).max())
+        out["first_timed_step"] = {"rel_err": err, "tol": 1e-5, "pass": err <= 1e-5}
+    if contact_state is None:
+        out["first_contact_system"] = "no self-contact within the timed steps"
+        return out
+    k, curr, prev, prm = contact_state
+    sc.set_positions(curr, prev)
+    C.memmove(C.addressof(sc.param.contents), C.addressof(prm), C.sizeof(prm))
+    Session(sc)
+    n = sc.vertex_count
+    dx = np.empty(3 * n, np.float32)
+    it, rr = C.c_uint(), C.c_float()
+    st_g = lib.ppf_debug_newton_system(dx, C.byref(it), C.byref(rr))
+    sg = binding.product_system(lib, n)
+    o = binding.OracleSession(sc)
+    st_o, _, _, _ = o.newton_system()
+    so = o.system()
+    res = parity.compare_systems(sg, so, curr, sc.array("face"), sc.array("edge"), 1e-3)
+    b = so["force"].astype(np.float64).reshape(-1)
+    rel = float(np.abs(b - parity.apply_system(so, dx)).sum() / np.abs(b).sum())
+    pairs = res["pairs"]
+    out["first_contact_system"] = {
+        "state": f"after timed step {k}", "pairs": pairs["pairs"],
+        "listed_within_1e-6_ghat": pairs["listed"],
+        "pair_sets_equal_outside_listed": pairs["equal_outside_listed"],
+        "contact_blocks": res["contact_blocks"],
+        "fixed_blocks_max_rel_err": res.get("fixed_max_err"),
+        "contact_blocks_max_rel_err": res.get("contact_max_err"),
+        "force_max_rel_err": res["force_max_err"],
+        "gpu_solution_true_rel_residual": rel, "pcg_states": [int(st_g), int(st_o)],
+        "pass": bool(pairs["equal_outside_listed"] and res["fixed_max_err"] <= 1e-5
+                     and res["force_max_err"] <= 1e-5 and rel < 2e-3)}
+    return out
+
+
+def _oracle_run(sc, curr0, prev0, param0, budget_s, max_steps=None, warmup=0,
+                keep_first=False):
     """Steps the CPU oracle from t = 0 until the budget is spent (at least
-    one step); returns (newton_iters, seconds, steps)."""
+    one step); returns (newton_iters, seconds, steps) and, with keep_first,
+    the positions after the first step."""
     import ctypes as C
 
     from oracle.binding import OracleSession
@@ -419,6 +498,7 @@ def _oracle_run(sc, curr0, prev0, param0, budget_s, max_steps=None, warmup=0):
     for _ in range(warmup):
         o.step()
     newton, secs, steps = 0, 0.0, 0
+    first = None
     while True:
         t = time.perf_counter()
         r = o.step()
@@ -427,17 +507,22 @@ def _oracle_run(sc, curr0, prev0, param0, budget_s, max_steps=None, warmup=0):
             raise RuntimeError(f"oracle step failed: {r.as_dict()}")
         newton += o.stats()["newton_iters"]
         steps += 1
+        if keep_first and steps == 1:
+            first = o.positions()[0]
         if secs >= budget_s or (max_steps is not None and steps >= max_steps):
             break
+    if keep_first:
+        return newton, secs, steps, first
     return newton, secs, steps
 
 
 def cpu_baseline(sc, curr0, prev0, param0, budget_s):
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    newton, secs, steps = _oracle_run(sc, curr0, prev0, param0, budget_s)
-    return {"value": round(newton / secs, 3), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {steps} time steps of the same workload from t = 0 "
-                      f"({newton} Newton iterations, {secs:.1f} s), OpenMP oracle"}
+    newton, secs, steps, first = _oracle_run(sc, curr0, prev0, param0, budget_s,
+                                             keep_first=True)
+    return ({"value": round(newton / secs, 3), "unit": UNIT, "cores": threads, "kind": "port",
+             "sample": f"first {steps} time steps of the same workload from t = 0 "
+                       f"({newton} Newton iterations, {secs:.1f} s), OpenMP oracle"}, first)
 
 
 def run_reference(args, rank, local_rank, world):

@@ -281,6 +281,12 @@ unsigned ppf_schwarz_aggregate(unsigned n, const unsigned *off, const unsigned *
 void *ppf_stream(void);
 /* Number of kernels this library has launched since it was loaded. */
 unsigned long long ppf_kernel_launches(void);
+/* Bytes copied host -> device and device -> host by the library since it was
+ * loaded, counted at the copies of the per-step path: update_constraint's
+ * uploads, the status and count reads inside advance(), intersection
+ * records and fetch(). No counterpart in the reference. Either pointer may
+ * be NULL. */
+void ppf_transfer_bytes(unsigned long long *h2d, unsigned long long *d2h);
 
 /* ---- stage inspection (parity checks) -------------------------------------
  * Assembles and solves the first Newton system of a step at the current

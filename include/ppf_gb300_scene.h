@@ -20,6 +20,8 @@
 
 #include "ppf_gb300.h"
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -90,6 +92,17 @@ unsigned ppf_scene_vertex_count(PpfScene *scene);
 void ppf_scene_positions(PpfScene *scene, float *curr, float *prev);
 void ppf_scene_set_positions(PpfScene *scene, const float *curr,
                              const float *prev);
+/* Byte size of one named array of the built scene, copied into `out` when it
+ * is not NULL (0 for an unknown name or an unbuilt scene). It has no
+ * counterpart in the reference: it exposes what the builder computed so a
+ * host can check it. Names: face, edge, hinge (u32 per corner);
+ * inv_rest2x2 (4 f32 per face, column-major); fixed_offset, fixed_index
+ * (the upper-triangle fixed pattern, u32); transpose_offset, transpose (u32
+ * (row, slot) pairs per lower entry); face_slots (9 u32 per face),
+ * hinge_slots (16 u32 per hinge); edge_face_offset, edge_face (u32); and f32
+ * per element: vertex_mass, vertex_area, face_area, face_mass, edge_length,
+ * hinge_length, hinge_area, face_mu, face_lambda, hinge_bend. */
+size_t ppf_scene_array(PpfScene *scene, const char *name, void *out);
 
 #ifdef __cplusplus
 }

@@ -96,6 +96,8 @@ def _declare(lib):
     lib.oracle_time.restype = C.c_double
     lib.oracle_check_intersection.restype = C.c_bool
     lib.oracle_check_intersection.argtypes = [f32p]
+    lib.oracle_intersection_records.restype = C.c_uint
+    lib.oracle_intersection_records.argtypes = [f32p, u32p, C.c_uint]
     lib.oracle_update_constraint.argtypes = [P]
     lib.oracle_step_stats.argtypes = [C.POINTER(C.c_uint), C.POINTER(C.c_uint),
                                       C.POINTER(C.c_float)]
@@ -151,6 +153,15 @@ class OracleSession:
         """Independent intersection check of positions x (e.g. the GPU's)."""
         return bool(self.lib.oracle_check_intersection(
             np.ascontiguousarray(x, np.float32).reshape(-1)))
+
+    def intersection_records(self, x, max_count: int = 4096):
+        """Every intersecting pair of positions x as an array of (type, elem0,
+        elem1) rows, in the reference's record types (0 face-edge, 1
+        edge-edge, 2 collision face-edge)."""
+        out = np.zeros(3 * max_count, np.uint32)
+        n = self.lib.oracle_intersection_records(
+            np.ascontiguousarray(x, np.float32).reshape(-1), out, max_count)
+        return out[:3 * min(n, max_count)].reshape(-1, 3), int(n)
 
     def stats(self):
         a, b, c = C.c_uint(), C.c_uint(), C.c_float()

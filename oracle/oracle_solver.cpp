@@ -27,6 +27,7 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -175,6 +176,8 @@ struct Oracle {
     float line_search(unsigned &pin_bad, bool &overlap);
     float strain_line_search() const;
     bool intersection_free(const std::vector<float> &xx);
+    void intersections(const std::vector<float> &xx, std::vector<std::array<unsigned, 3>> &out,
+                       bool first_only);
     PpfStepResult advance();
     void set_constraint(const PpfConstraint *c);
 };
@@ -1258,10 +1261,14 @@ float Oracle::line_search(unsigned &pin_bad, bool &overlap) {
 }
 
 // Post-step intersection check over the current face / edge trees
-// (contact/contact.cu:3056-3175, testers at 2762-2960).
-bool Oracle::intersection_free(const std::vector<float> &xx) {
-    bool ok = true;
-    for (unsigned e = 0; e < ne && ok; ++e) {
+// (contact/contact.cu:3056-3175, testers at 2762-2960). Every intersecting
+// pair goes to `out` as (type, elem0, elem1) with the reference's record
+// types: 0 face-edge (face, edge), 1 edge-edge (edge, earlier edge),
+// 2 collision face-edge (collision face, edge). With first_only the walk
+// stops after the edge that produced the first record.
+void Oracle::intersections(const std::vector<float> &xx,
+                           std::vector<std::array<unsigned, 3>> &out, bool first_only) {
+    for (unsigned e = 0; e < ne && !(first_only && !out.empty()); ++e) {
         const unsigned *ed = &edge[2 * e];
         Vec3 a = X(xx, ed[0]), b = X(xx, ed[1]);
         float q[8] = {std::fmin(a[0], b[0]), std::fmin(a[1], b[1]), std::fmin(a[2], b[2]), 1.0f,
@@ -1274,13 +1281,15 @@ bool Oracle::intersection_free(const std::vector<float> &xx) {
             if (!either || !nonzero || bc) return;
             for (int k = 0; k < 3; ++k)
                 if (ed[0] == f[k] || ed[1] == f[k]) return;
-            if (contact::edge_triangle_intersect(a, b, X(xx, f[0]), X(xx, f[1]), X(xx, f[2]))) ok = false;
+            if (contact::edge_triangle_intersect(a, b, X(xx, f[0]), X(xx, f[1]), X(xx, f[2])))
+                out.push_back({0u, fi, e});
         });
         // against the static collision mesh's faces (contact.cu:3114-3122)
         if (eprop[e].mass > 0.0f)
             query(tcf, q, [&](unsigned fi) {
                 const unsigned *f = &cm_face[3 * fi];
-                if (contact::edge_triangle_intersect(a, b, CX(f[0]), CX(f[1]), CX(f[2]))) ok = false;
+                if (contact::edge_triangle_intersect(a, b, CX(f[0]), CX(f[1]), CX(f[2])))
+                    out.push_back({2u, fi, e});
             });
         query(te, q, [&](unsigned o) {
             if (!(o < e)) return;
@@ -1303,10 +1312,15 @@ bool Oracle::intersection_free(const std::vector<float> &xx) {
                                                                   X(xx, e1[1 - j]), off);
                 }
             }
-            if (hit) ok = false;
+            if (hit) out.push_back({1u, e, o});
         });
     }
-    return ok;
+}
+
+bool Oracle::intersection_free(const std::vector<float> &xx) {
+    std::vector<std::array<unsigned, 3>> hits;
+    intersections(xx, hits, true);
+    return hits.empty();
 }
 
 PpfStepResult Oracle::advance() {
@@ -1424,6 +1438,20 @@ bool oracle_check_intersection(const float *x) {
     std::vector<float> xx(x, x + 3 * (size_t)o.n);
     o.trees(xx, xx, 1.0f);
     return o.intersection_free(xx);
+}
+
+// Every intersecting pair of an arbitrary state (trees rebuilt at x), as
+// (type, elem0, elem1) triples in `out` (3 * max_count); returns the count,
+// which may exceed max_count.
+unsigned oracle_intersection_records(const float *x, unsigned *out, unsigned max_count) {
+    Oracle &o = *g_oracle;
+    std::vector<float> xx(x, x + 3 * (size_t)o.n);
+    o.trees(xx, xx, 1.0f);
+    std::vector<std::array<unsigned, 3>> hits;
+    o.intersections(xx, hits, false);
+    for (size_t k = 0; k < hits.size() && k < max_count; ++k)
+        for (int d = 0; d < 3; ++d) out[3 * k + d] = hits[k][d];
+    return (unsigned)hits.size();
 }
 
 void oracle_update_constraint(const PpfConstraint *c) { g_oracle->set_constraint(c); }

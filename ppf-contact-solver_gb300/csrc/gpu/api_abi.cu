@@ -86,6 +86,9 @@ extern "C" {
 
 bool initialize(PpfDataSet *dataset, PpfParamSet *param) {
     try {
+        // a new session starts without the previous one's fatal report (a
+        // host that gets failures back may initialize again in one process)
+        ppf::set_fatal(0, "");
         int count = 0;
         if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
             throw FatalError(PPF_FATAL_CUDA_DRIVER, "no CUDA device is visible to this process");
@@ -286,6 +289,10 @@ int ppf_set_preconditioner(int kind, float param) {
 void *ppf_stream(void) { return (void *)solver_instance().stream(); }
 
 unsigned long long ppf_kernel_launches(void) { return ppf::gpu::g_kernel_launches; }
+void ppf_transfer_bytes(unsigned long long *h2d, unsigned long long *d2h) {
+    if (h2d) *h2d = ppf::gpu::g_h2d_bytes;
+    if (d2h) *d2h = ppf::gpu::g_d2h_bytes;
+}
 
 int ppf_debug_newton_system(float *dx, unsigned *iters, float *resid) {
     try {

@@ -23,6 +23,7 @@ void set_fatal(unsigned char code, const char *detail) {
 namespace gpu {
 
 unsigned long long g_kernel_launches = 0;
+unsigned long long g_h2d_bytes = 0, g_d2h_bytes = 0;
 
 void check_cuda(cudaError_t err, const char *what, const char *file, int line) {
     if (err == cudaSuccess) return;

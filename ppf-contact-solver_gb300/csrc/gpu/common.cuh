@@ -33,6 +33,10 @@ void check_cuda(cudaError_t err, const char *what, const char *file, int line);
 // Kernels launched by this library since it was loaded (every launch site
 // ends in PPF_LAUNCH_CHECK or counts itself).
 extern unsigned long long g_kernel_launches;
+// Bytes the library has copied host -> device and device -> host since it was
+// loaded, counted at the copies of the per-step path (uploads, status reads,
+// contact-layout totals, intersection records, fetch).
+extern unsigned long long g_h2d_bytes, g_d2h_bytes;
 #define PPF_CUDA(x) ::ppf::gpu::check_cuda((x), #x, __FILE__, __LINE__)
 #define PPF_LAUNCH_CHECK()                                                              \
     (++::ppf::gpu::g_kernel_launches,                                                   \

@@ -1341,6 +1341,7 @@ void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const 
     PPF_CUDA(cudaMemcpyAsync(&totals[4], D.flag_off.data() + n, sizeof(unsigned),
                              cudaMemcpyDeviceToHost, q));
     PPF_CUDA(cudaStreamSynchronize(q));
+    g_d2h_bytes += sizeof(totals);
     if (totals[1]) throw FatalError(4, "contact-row sort look-back timed out");
     D.rows = totals[0];
     out.n_slices = (D.rows + kSliceRows - 1) / kSliceRows;

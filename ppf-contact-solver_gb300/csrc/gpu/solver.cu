@@ -20,6 +20,7 @@ constexpr unsigned kB = 256;
 template <class T> void upload(DevBuf<T> &d, const T *h, size_t n) {
     d.reserve(n ? n : 1);
     if (n) PPF_CUDA(cudaMemcpy(d.data(), h, n * sizeof(T), cudaMemcpyHostToDevice));
+    g_h2d_bytes += n * sizeof(T);
 }
 template <class T> void upload(DevBuf<T> &d, const std::vector<T> &h) {
     upload(d, h.data(), h.size());
@@ -624,9 +625,11 @@ void Solver::update_constraint(const PpfConstraint *c) {
 }
 
 void Solver::update_rest_shape(const PpfRestShapeUpdate *u) {
-    if (u->inv_rest2x2.size)
+    if (u->inv_rest2x2.size) {
         PPF_CUDA(cudaMemcpy(inv_rest_.data(), u->inv_rest2x2.data,
                             u->inv_rest2x2.size * sizeof(PpfMat2x2f), cudaMemcpyHostToDevice));
+        g_h2d_bytes += u->inv_rest2x2.size * sizeof(PpfMat2x2f);
+    }
     if (u->exclude_face.size) {
         for (unsigned i = 0; i < u->exclude_face.size && i < nf_; ++i)
             h_fprop_[i].rest_excluded = u->exclude_face.data[i] != 0;
@@ -675,6 +678,7 @@ bool Solver::check_intersection(const float *x) {
     if (isect_count_)
         PPF_CUDA(cudaMemcpy(isect_host_.data(), isect_.data(),
                             isect_count_ * sizeof(PpfIntersectionRecord), cudaMemcpyDeviceToHost));
+    g_d2h_bytes += sizeof(unsigned) + isect_count_ * sizeof(PpfIntersectionRecord);
     return cnt == 0;
 }
 
@@ -687,6 +691,7 @@ unsigned Solver::fetch_intersection_records(PpfIntersectionRecord *out, unsigned
 void Solver::read_status() {
     PPF_CUDA(cudaMemcpyAsync(st_host_, st_.data(), sizeof(IterStatus), cudaMemcpyDeviceToHost, q_));
     PPF_CUDA(cudaStreamSynchronize(q_));
+    g_d2h_bytes += sizeof(IterStatus);
 }
 
 // Assembly of the Newton system at eval_x (main.cu:713-1049).
@@ -884,6 +889,7 @@ PpfStepResult Solver::advance() {
                                  cudaMemcpyDeviceToHost, q_));
         PPF_CUDA(cudaMemcpyAsync(&rescale, rescale_.data(), sizeof(float), cudaMemcpyDeviceToHost, q_));
         PPF_CUDA(cudaStreamSynchronize(q_));
+        g_d2h_bytes += sizeof(IterStatus) + sizeof(float);
         const IterStatus st = *st_host_;
         float pcg_ms = 0.0f;
         PPF_CUDA(cudaEventElapsedTime(&pcg_ms, ev0_, ev1_));
@@ -978,6 +984,7 @@ void Solver::fetch() {
                         cudaMemcpyDeviceToHost));
     PPF_CUDA(cudaMemcpy(host->vertex.prev.data, prev_.data(), 3 * (size_t)n_ * sizeof(float),
                         cudaMemcpyDeviceToHost));
+    g_d2h_bytes += 2 * 3 * (size_t)n_ * sizeof(float);
 }
 
 void Solver::fetch_dyn_counts(unsigned *n_value, unsigned *n_offset) {

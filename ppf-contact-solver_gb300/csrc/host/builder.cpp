@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <string>
 #include <unordered_map>
 #include <vector>
 
@@ -648,6 +649,53 @@ PpfDataSet *ppf_scene_dataset(PpfScene *s) { return s->built ? &s->ds : nullptr;
 PpfParamSet *ppf_scene_param(PpfScene *s) { return s->built ? &s->param : nullptr; }
 PpfConstraint *ppf_scene_constraint(PpfScene *s) {
     return s->built ? &s->ds.constraint : nullptr;
+}
+
+// Byte size of a named array of the built scene, copied to `out` when it is
+// not NULL; 0 for an unknown name or an unbuilt scene.
+size_t ppf_scene_array(PpfScene *s, const char *name, void *out) {
+    if (!s->built || !name) return 0;
+    std::vector<float> tmp;
+    const void *src = nullptr;
+    size_t bytes = 0;
+    auto take = [&](const auto &v) {
+        src = v.data();
+        bytes = v.size() * sizeof(v[0]);
+    };
+    auto per = [&](const auto &props, auto get) {
+        tmp.resize(props.size());
+        for (size_t i = 0; i < props.size(); ++i) tmp[i] = get(props[i]);
+        take(tmp);
+    };
+    const std::string n(name);
+    if (n == "face") take(s->face);
+    else if (n == "edge") take(s->edge);
+    else if (n == "hinge") take(s->hinge);
+    else if (n == "inv_rest2x2") take(s->inv_rest);
+    else if (n == "fixed_offset") take(s->fixed_table.offset);
+    else if (n == "fixed_index") take(s->fixed_table.data);
+    else if (n == "transpose_offset") take(s->transpose_offset);
+    else if (n == "transpose") take(s->transpose_data);
+    else if (n == "face_slots") take(s->face_slots);
+    else if (n == "hinge_slots") take(s->hinge_slots);
+    else if (n == "edge_face_offset") take(s->nb_eface.offset);
+    else if (n == "edge_face") take(s->nb_eface.data);
+    else if (n == "vertex_mass") per(s->vprop, [](const PpfVertexProp &p) { return p.mass; });
+    else if (n == "vertex_area") per(s->vprop, [](const PpfVertexProp &p) { return p.area; });
+    else if (n == "face_area") per(s->fprop, [](const PpfFaceProp &p) { return p.area; });
+    else if (n == "face_mass") per(s->fprop, [](const PpfFaceProp &p) { return p.mass; });
+    else if (n == "edge_length") per(s->eprop, [](const PpfEdgeProp &p) { return p.length; });
+    else if (n == "hinge_length") per(s->hprop, [](const PpfHingeProp &p) { return p.length; });
+    else if (n == "hinge_area") per(s->hprop, [](const PpfHingeProp &p) { return p.area; });
+    else if (n == "face_mu")
+        per(s->fprop, [&](const PpfFaceProp &p) { return s->fparam[p.param_index].mu; });
+    else if (n == "face_lambda")
+        per(s->fprop, [&](const PpfFaceProp &p) { return s->fparam[p.param_index].lambda; });
+    else if (n == "hinge_bend")
+        per(s->hprop, [&](const PpfHingeProp &p) { return s->hparam[p.param_index].bend; });
+    else return 0;
+    if (out && bytes) std::memcpy(out, src, bytes);
+    return bytes;
 }
 
 void ppf_scene_set_pin_targets(PpfScene *s, const float *pos, const float *delta) {

@@ -58,6 +58,8 @@ def _declare(lib):
     lib.ppf_scene_vertex_count.argtypes = [P]
     lib.ppf_scene_positions.argtypes = [P, C.c_void_p, C.c_void_p]
     lib.ppf_scene_set_positions.argtypes = [P, C.c_void_p, C.c_void_p]
+    lib.ppf_scene_array.restype = C.c_size_t
+    lib.ppf_scene_array.argtypes = [P, C.c_char_p, C.c_void_p]
     lib.ppf_set_preconditioner.restype = C.c_int
     lib.ppf_set_preconditioner.argtypes = [C.c_int, C.c_float]
     # reference entry points (include/ppf_gb300.h)
@@ -228,6 +230,26 @@ class Scene:
                 keep.append(a)
                 args.append(a.ctypes.data_as(C.c_void_p))
         self.lib.ppf_scene_set_positions(self.h, *args)
+
+    _ARRAY_DTYPES = {"inv_rest2x2": np.float32, "vertex_mass": np.float32,
+                     "vertex_area": np.float32, "face_area": np.float32,
+                     "face_mass": np.float32, "edge_length": np.float32,
+                     "hinge_length": np.float32, "hinge_area": np.float32,
+                     "face_mu": np.float32, "face_lambda": np.float32,
+                     "hinge_bend": np.float32}
+
+    def array(self, name: str) -> np.ndarray:
+        """A named array of the built DataSet (ppf_scene_array): topology
+        (face, edge, hinge), inv_rest2x2, the fixed pattern and its transpose
+        and slot tables, or a per-element float (vertex_mass, face_area, ...)."""
+        dtype = self._ARRAY_DTYPES.get(name, np.uint32)
+        nbytes = int(self.lib.ppf_scene_array(self.h, name.encode(), None))
+        if nbytes == 0 and name not in ("hinge", "transpose"):
+            raise KeyError(name)
+        out = np.empty(nbytes // np.dtype(dtype).itemsize, dtype)
+        if nbytes:
+            self.lib.ppf_scene_array(self.h, name.encode(), out.ctypes.data_as(C.c_void_p))
+        return out
 
     def set_pin_targets(self, position, step_delta=None):
         pos = np.ascontiguousarray(position, np.float32).reshape(-1)

@@ -54,6 +54,20 @@ def ref_lib():
     return lib
 
 
+@pytest.fixture(scope="session")
+def ref_pipeline_or_none():
+    """The reference's own pipeline compiled as host code, or None where its
+    sources are absent (the frozen fixtures stand in there)."""
+    from oracle import binding
+    from ppf_gb300 import build
+
+    try:
+        build.build_reference()
+    except Exception:
+        pass
+    return binding.reference_pipeline()
+
+
 @pytest.fixture
 def rng():
     return np.random.default_rng(1234)

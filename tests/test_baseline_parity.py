@@ -1,0 +1,167 @@
+"""GPU parity against the CPU oracle at the benchmark configurations' own
+sizes, through the C ABI.
+
+* The 64 x 64 cloth on the r = 0.3 sphere, 60 steps (the small plain
+  configuration): at every step both the GPU and the oracle advance from the
+  GPU's state (lockstep), and the positions must agree within 1e-5 relative
+  to the coordinate scale, the benchmark spec's one-step bar. Every frame is
+  intersection-free by the oracle's own check and strain-limited; Newton
+  iteration counts match and PCG iteration counts agree within what the 1e-3
+  relative residual lets the stopping iteration move.
+* The 8 x 128^2 stacked sheets (131,072 vertices) at their first Newton
+  system with self-contact: pair sets identical except pairs listed within
+  1e-6 * ghat of the gap threshold (listed, and their count printed), the
+  fixed and contact blocks and the right-hand side within fp32
+  summation-order error, and the GPU's solution solving the oracle's system
+  to the solver's tolerance.
+* The intersection check on an intersecting state: the GPU's records are the
+  oracle's enumeration, and the verdict is the reference's.
+"""
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import step_scenes
+from oracle import parity
+from ppf_gb300 import scenes
+from ppf_gb300.session import Session
+
+pytestmark = pytest.mark.gpu
+
+GHAT = 1e-3
+
+
+@pytest.fixture(scope="module")
+def binding(oracle_lib, product_lib):
+    from oracle import binding
+
+    return binding
+
+
+def test_cloth_sphere_64_lockstep_60_steps(binding):
+    sc, _ = scenes.cloth_sphere(64)
+    rest = sc.positions()[0].copy()
+    faces = sc.array("face").reshape(-1, 3)
+    s = Session(sc)
+    worst = 0.0
+    newton_g = newton_o = pcg_g = pcg_o = 0
+    for k in range(60):
+        # the oracle starts from the GPU's state: the scene's host arrays hold
+        # what the last fetch wrote, and the ParamSet carries the GPU's time
+        o = binding.OracleSession(sc)
+        rg = s.step()
+        ro = o.step()
+        assert rg.success() and ro.success(), (k, rg.as_dict(), ro.as_dict())
+        xg = s.positions()
+        xo = o.positions()[0]
+        err = float(np.abs(xg - xo).max()) / float(np.abs(xo).max())
+        worst = max(worst, err)
+        assert err <= 1e-5, (k, err)
+        sg, so = s.stats(), o.stats()
+        assert sg.newton_iters == so["newton_iters"], (k, sg.newton_iters, so)
+        newton_g += sg.newton_iters
+        newton_o += so["newton_iters"]
+        pcg_g += sg.pcg_iters_total
+        pcg_o += so["pcg_iters_total"]
+        # the step's solves stop at checks 4 iterations apart, and the
+        # residual's round-off moves the stopping check by one at most
+        assert abs(sg.pcg_iters_total - so["pcg_iters_total"]) <= 4 * sg.pcg_solves + 0.05 * \
+            so["pcg_iters_total"], (k, sg.pcg_iters_total, so)
+        assert o.intersection_free(xg), k
+        sig = step_scenes.strain_of(xg, rest, faces)
+        assert sig.max() <= 1.01 + 1e-3, (k, sig.max())
+    print(f"cloth_sphere 64: worst one-step error {worst:.2e} relative; Newton {newton_g} vs "
+          f"{newton_o}; PCG {pcg_g} vs {pcg_o}")
+    assert abs(pcg_g - pcg_o) <= 0.05 * pcg_o + 8
+    # the cloth draped over the sphere without entering it
+    assert np.linalg.norm(xg, axis=1).min() >= 0.3 - 1e-6
+    assert xg[:, 1].max() < 0.35
+
+
+def _first_self_contact_state(s, max_steps=40):
+    for k in range(max_steps):
+        r = s.step()
+        assert r.success(), (k, r.as_dict())
+        if s.stats().max_dyn_blocks > 0:
+            return k
+    raise AssertionError("no self-contact within the first steps")
+
+
+def test_stacked_sheets_first_contact_system(binding, product_lib):
+    sc, _ = scenes.stacked_sheets(128, 8, seed=0, dt=0.01)
+    n = sc.vertex_count
+    s = Session(sc)
+    step = _first_self_contact_state(s)
+    x = sc.positions()[0]
+    # GPU: the first Newton system of the next step at this state
+    dx_g = np.empty(3 * n, np.float32)
+    it_g, rr_g = C.c_uint(), C.c_float()
+    st_g = product_lib.ppf_debug_newton_system(dx_g, C.byref(it_g), C.byref(rr_g))
+    sg = binding.product_system(product_lib, n)
+    # oracle: the same system from the same state
+    o = binding.OracleSession(sc)
+    st_o, dx_o, it_o, rr_o = o.newton_system()
+    so = o.system()
+    res = parity.compare_systems(sg, so, x, sc.array("face"), sc.array("edge"), GHAT)
+    pairs = res["pairs"]
+    print(f"stacked sheets, state after step {step}: {pairs['pairs']} pairs, "
+          f"{pairs['listed']} listed within {pairs['band']}, "
+          f"{res['contact_blocks']} contact blocks; per kind {pairs['kinds']}")
+    assert pairs["pairs"] > 0
+    assert pairs["equal_outside_listed"], pairs
+    assert res["fixed_pattern_equal"]
+    assert res["fixed_max_err"] <= 1e-5, res
+    if pairs["listed"] == 0:
+        assert res["contact_pattern_equal"], res
+        assert res["contact_max_err"] <= 1e-5, res
+    assert res["force_max_err"] <= 1e-5, res
+    assert res["diag_max_err"] <= 1e-5, res
+    assert st_g == 0 and st_o == 0
+    assert rr_g.value < 1e-3 and rr_o < 1e-3
+    b = so["force"].astype(np.float64).reshape(-1)
+    r_g = b - parity.apply_system(so, dx_g)
+    rel = np.abs(r_g).sum() / np.abs(b).sum()
+    assert rel < 2e-3, rel
+
+
+def test_intersection_check_reports_a_tilted_sheet(binding, product_lib, ref_pipeline_or_none):
+    """Sheet B tilted through sheet A: initialize() must refuse the state
+    (the reference's INIT_INTERSECTION), and the GPU check's records must be
+    the oracle's complete enumeration of intersecting pairs."""
+    import ref_pipeline_cases as rpc
+    from ppf_gb300 import abi
+
+    sc, _ = step_scenes.two_sheets()
+    curr = sc.positions()[0].reshape(-1).copy()
+    tilt = rpc.intersection_cases(curr)["tilted"].reshape(-1, 3)
+    sc.set_positions(tilt, tilt)
+    lib = product_lib
+    ok = lib.initialize(sc.dataset, sc.param)
+    assert not ok
+    assert int(lib.ppf_fatal_code()) == 1  # INIT_INTERSECTION
+    buf = (abi.IntersectionRecord * 256)()
+    cnt = lib.fetch_intersection_records(buf, 256)
+    assert 0 < cnt < 256
+    got = sorted((r.type, r.elem0, r.elem1) for r in buf[:cnt])
+    # the oracle's enumeration on the same state (its trees are built at x)
+    sc.set_positions(curr.reshape(-1, 3), curr.reshape(-1, 3))
+    o = binding.OracleSession(sc)
+    rec, total = o.intersection_records(tilt)
+    assert total == cnt
+    assert got == sorted(map(tuple, rec.tolist()))
+    assert not o.intersection_free(tilt)
+    # the records carry the intersecting elements' positions
+    for r in buf[:cnt]:
+        pos = np.array(r.positions[:3 * (r.num_verts0 + r.num_verts1)]).reshape(-1, 3)
+        assert np.all(np.isfinite(pos))
+    if ref_pipeline_or_none is not None:
+        assert ref_pipeline_or_none.refpipe_init(sc.dataset, C.byref(o.param))
+        assert not ref_pipeline_or_none.refpipe_check_intersection(tilt.reshape(-1))
+    else:
+        g = np.load(Path(__file__).parent / "golden" / "ref_pipeline.npz")
+        assert not bool(g["isect_tilted"])
+    # the library is usable again: a separated state initializes
+    s = Session(sc)
+    assert s.step().success()
