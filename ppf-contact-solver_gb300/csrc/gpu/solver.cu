@@ -602,7 +602,20 @@ void Solver::update_constraint(const PpfConstraint *c) {
     upload(sphere_, c->sphere.data, nsphere_);
     upload(floor_, c->floor.data, nfloor_);
     if (h_vprop_.empty()) return;
-    // rebuild fix/pull indices and element `fixed` flags (main.cu:2012-2077)
+    // rebuild fix/pull indices and element `fixed` flags (main.cu:2012-2077).
+    // The reference re-uploads every prop array on each call; when the pinned
+    // and pulled vertices and their order are those of the last call, the
+    // props it would upload are the ones already on the device, so only the
+    // constraint arrays above are copied.
+    {
+        bool same = true;
+        std::vector<unsigned> fix_of(n_, 0u), pull_of(n_, 0u);
+        for (unsigned i = 0; i < nfix_; ++i) fix_of[c->fix.data[i].index] = i + 1;
+        for (unsigned i = 0; i < npull_; ++i) pull_of[c->pull.data[i].index] = i + 1;
+        for (unsigned v = 0; v < n_ && same; ++v)
+            same = h_vprop_[v].fix_index == fix_of[v] && h_vprop_[v].pull_index == pull_of[v];
+        if (same) return;
+    }
     for (auto &v : h_vprop_) v.fix_index = v.pull_index = 0;
     for (unsigned i = 0; i < nfix_; ++i) h_vprop_[c->fix.data[i].index].fix_index = i + 1;
     for (unsigned i = 0; i < npull_; ++i) h_vprop_[c->pull.data[i].index].pull_index = i + 1;
