@@ -93,7 +93,7 @@ void ppf_scene_positions(PpfScene *scene, float *curr, float *prev);
 void ppf_scene_set_positions(PpfScene *scene, const float *curr,
                              const float *prev);
 /* Byte size of one named array of the built scene, copied into `out` when it
- * is not NULL (0 for an unknown name or an unbuilt scene). It has no
+ * is not NULL ((size_t)-1 for an unknown name or an unbuilt scene). It has no
  * counterpart in the reference: it exposes what the builder computed so a
  * host can check it. Names: face, edge, hinge (u32 per corner);
  * inv_rest2x2 (4 f32 per face, column-major); fixed_offset, fixed_index

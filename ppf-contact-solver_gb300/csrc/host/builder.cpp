@@ -65,7 +65,7 @@ V3 crs(V3 a, V3 b) {
 }
 float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 float nrm(V3 a) { return std::sqrt(dot(a, a)); }
-V3 scale(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+V3 unscale(V3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
 
 } // namespace
 
@@ -472,9 +472,11 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
         V3 x0 = X(s->face[i].v[0]), x1 = X(s->face[i].v[1]), x2 = X(s->face[i].v[2]);
         V3 d0 = sub(x1, x0), d1 = sub(x2, x0);
         V3 nn = crs(d0, d1);
+        // normalize divides by the norm (nalgebra's normalize), which rounds
+        // differently from multiplying by its reciprocal
         V3 e2 = crs(nn, d0);
-        e2 = scale(e2, 1.0f / nrm(e2));
-        V3 e1 = scale(d0, 1.0f / nrm(d0));
+        e2 = unscale(e2, nrm(e2));
+        V3 e1 = unscale(d0, nrm(d0));
         float a = dot(e1, d0), b = dot(e1, d1), c = dot(e2, d0), d = dot(e2, d1);
         float det = a * d - c * b;
         if (!(std::fabs(det) > 0.0f)) return 1;
@@ -652,9 +654,9 @@ PpfConstraint *ppf_scene_constraint(PpfScene *s) {
 }
 
 // Byte size of a named array of the built scene, copied to `out` when it is
-// not NULL; 0 for an unknown name or an unbuilt scene.
+// not NULL; (size_t)-1 for an unknown name or an unbuilt scene.
 size_t ppf_scene_array(PpfScene *s, const char *name, void *out) {
-    if (!s->built || !name) return 0;
+    if (!s->built || !name) return (size_t)-1;
     std::vector<float> tmp;
     const void *src = nullptr;
     size_t bytes = 0;
@@ -693,7 +695,7 @@ size_t ppf_scene_array(PpfScene *s, const char *name, void *out) {
         per(s->fprop, [&](const PpfFaceProp &p) { return s->fparam[p.param_index].lambda; });
     else if (n == "hinge_bend")
         per(s->hprop, [&](const PpfHingeProp &p) { return s->hparam[p.param_index].bend; });
-    else return 0;
+    else return (size_t)-1;
     if (out && bytes) std::memcpy(out, src, bytes);
     return bytes;
 }

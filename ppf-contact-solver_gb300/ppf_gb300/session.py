@@ -244,7 +244,7 @@ class Scene:
         and slot tables, or a per-element float (vertex_mass, face_area, ...)."""
         dtype = self._ARRAY_DTYPES.get(name, np.uint32)
         nbytes = int(self.lib.ppf_scene_array(self.h, name.encode(), None))
-        if nbytes == 0 and name not in ("hinge", "transpose"):
+        if nbytes == C.c_size_t(-1).value:
             raise KeyError(name)
         out = np.empty(nbytes // np.dtype(dtype).itemsize, dtype)
         if nbytes:
