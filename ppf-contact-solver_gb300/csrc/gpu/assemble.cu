@@ -210,8 +210,7 @@ __device__ __forceinline__ float detect_guard(const Vec3 &p) {
 }
 
 __device__ __forceinline__ unsigned push_pair(unsigned *ctr, unsigned cap) {
-    unsigned slot = atomicAdd(ctr, 1u);
-    return slot < cap ? slot : kSentinel;
+    return push_slot(ctr, cap);
 }
 
 struct VertexQueryOp {
@@ -250,21 +249,26 @@ struct VertexQueryOp {
     }
 };
 
+// One lane per surface vertex, in the vertex tree's Morton order, so a warp's
+// queries are neighbours in space; all lanes of a warp query together.
 __global__ void k_detect_vertex(Scene s, BvhView fb, BvhView eb, BvhView vb,
                                 const float *x, PairLists pl, IterStatus *st) {
-    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= s.n_surf) return;
-    unsigned v = vb.node[t].x - 1u; // Morton order of the vertex tree
-    Vec3 p = X(x, v);
-    float m = s.margin_vert[v] + detect_guard(p);
-    float4 qmin = make_float4(p[0] - m, p[1] - m, p[2] - m, 1.0f);
-    float4 qmax = make_float4(p[0] + m, p[1] + m, p[2] + m, 0.0f);
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = t < s.n_surf;
+    const unsigned v = act ? vb.node[t].x - 1u : 0u;
+    float4 qmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qmax = qmin;
+    if (act) {
+        Vec3 p = X(x, v);
+        float m = s.margin_vert[v] + detect_guard(p);
+        qmin = make_float4(p[0] - m, p[1] - m, p[2] - m, 1.0f);
+        qmax = make_float4(p[0] + m, p[1] + m, p[2] + m, 0.0f);
+    }
     VertexQueryOp op{s, x, v, 0, pl, st, 0u};
-    bvh_query(fb, qmin, qmax, op, &st->status);
+    warp_query(fb, act, qmin, qmax, op, &st->status);
     op.kind = 1;
-    bvh_query(eb, qmin, qmax, op, &st->status);
+    warp_query(eb, act, qmin, qmax, op, &st->status);
     op.kind = 2;
-    bvh_query(vb, qmin, qmax, op, &st->status);
+    warp_query(vb, act, qmin, qmax, op, &st->status);
     if (op.found) atomicAdd(&st->n_contact, op.found);
 }
 
@@ -285,27 +289,35 @@ struct EdgeQueryOp {
 };
 
 // One work item per edge piece (edges in the tree's Morton order).
+// Work items (edge pieces in the tree's Morton order) are taken a warp at a
+// time; a piece after the first excludes the leaves its predecessor reports.
 __global__ void k_detect_edge(Scene s, BvhView eb, const float *x, PairLists pl,
                               IterStatus *st, EdgePieces ep) {
     const unsigned total = ep.off[ep.n];
-    for (unsigned item = blockIdx.x * blockDim.x + threadIdx.x; item < total;
-         item += gridDim.x * blockDim.x) {
-        const unsigned t = piece_slot(ep, item);
-        const unsigned k = item - ep.off[t], K = ep.off[t + 1] - ep.off[t];
-        const unsigned e = eb.node[t].x - 1u;
-        const unsigned *ed = s.edge + 2 * e;
-        Vec3 a = X(x, ed[0]), c = X(x, ed[1]);
-        float m = s.margin_edge[e] + fmaxf(detect_guard(a), detect_guard(c));
-        float4 qmin, qmax;
-        seg_box(piece_point(a, c, k, K), piece_point(a, c, k + 1, K), m, qmin, qmax);
-        EdgeQueryOp op{s, x, e, pl, st, 0u};
-        if (k == 0u) {
-            bvh_query(eb, qmin, qmax, op, &st->status);
-        } else {
-            float4 xmin, xmax;
-            seg_box(piece_point(a, c, k - 1, K), piece_point(a, c, k, K), m, xmin, xmax);
-            bvh_query(eb, qmin, qmax, op, &st->status, &xmin, &xmax);
+    for (WarpItems w; w.base < total; w.base += w.stride) {
+        const unsigned item = w.base + w.lane;
+        const bool act = item < total;
+        unsigned e = 0u;
+        float4 qmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qmax = qmin;
+        float4 xmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), xmax = xmin;
+        bool excl = false;
+        if (act) {
+            const unsigned t = piece_slot(ep, item);
+            const unsigned k = item - ep.off[t], K = ep.off[t + 1] - ep.off[t];
+            e = eb.node[t].x - 1u;
+            const unsigned *ed = s.edge + 2 * e;
+            Vec3 a = X(x, ed[0]), c = X(x, ed[1]);
+            float m = s.margin_edge[e] + fmaxf(detect_guard(a), detect_guard(c));
+            seg_box(piece_point(a, c, k, K), piece_point(a, c, k + 1, K), m, qmin, qmax);
+            if (k > 0u) {
+                seg_box(piece_point(a, c, k - 1, K), piece_point(a, c, k, K), m, xmin, xmax);
+                excl = true;
+            }
         }
+        EdgeQueryOp op{s, x, e, pl, st, 0u};
+        // a lane without an exclusion box gets one that overlaps nothing
+        if (!excl) xmin.w = 0.0f;
+        warp_query(eb, act, qmin, qmax, op, &st->status, &xmin, &xmax);
         if (op.found) atomicAdd(&st->n_contact, op.found);
     }
 }
@@ -653,18 +665,21 @@ struct MeshFaceOp {
 };
 
 __global__ void k_mesh_vertex_face(Scene s, StepParams p, AssemblyBuffers b) {
-    unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= s.n_surf) return;
-    const PpfVertexProp &vp = s.vprop[v];
-    if (!(vp.fix_index == 0 && vp.mass > 0.0f)) return;
-    const PpfVertexParam &vq = s.vparam[vp.param_index];
-    const Vec3 x = X(b.x, v);
-    const float m = 0.5f * vq.ghat + vq.offset + detect_guard(x);
-    const float4 qmin = make_float4(x[0] - m, x[1] - m, x[2] - m, 1.0f);
-    const float4 qmax = make_float4(x[0] + m, x[1] + m, x[2] + m, 0.0f);
-    MeshFaceOp op{s, p, b, v, load_block(b.fixed_tmp + 9 * (size_t)s.fixed_diag[v]),
-                  Vec3::zero(), Mat3::zero(), 0u};
-    bvh_query(s.cm_face_bvh, qmin, qmax, op, &b.st->status);
+    const unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    bool act = v < s.n_surf;
+    if (act) act = s.vprop[v].fix_index == 0 && s.vprop[v].mass > 0.0f;
+    float4 qmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qmax = qmin;
+    Mat3 local = Mat3::zero();
+    if (act) {
+        const PpfVertexParam &vq = s.vparam[s.vprop[v].param_index];
+        const Vec3 x = X(b.x, v);
+        const float m = 0.5f * vq.ghat + vq.offset + detect_guard(x);
+        qmin = make_float4(x[0] - m, x[1] - m, x[2] - m, 1.0f);
+        qmax = make_float4(x[0] + m, x[1] + m, x[2] + m, 0.0f);
+        local = load_block(b.fixed_tmp + 9 * (size_t)s.fixed_diag[v]);
+    }
+    MeshFaceOp op{s, p, b, act ? v : 0u, local, Vec3::zero(), Mat3::zero(), 0u};
+    warp_query(s.cm_face_bvh, act, qmin, qmax, op, &b.st->status);
     if (!op.n) return;
     atomic_add3(b.force + 3 * v, op.f);
     atomic_add_block(b.fixed_val + 9 * (size_t)s.fixed_diag[v], op.H);
@@ -715,15 +730,18 @@ struct MeshVertexOp {
 };
 
 __global__ void k_mesh_face_vertex(Scene s, StepParams p, AssemblyBuffers b, BvhView fb) {
-    unsigned cv = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cv >= s.ncv) return;
-    const PpfVertexParam &cq = s.cm_vparam[s.cm_vprop[cv].param_index];
-    const Vec3 y = X(s.cm_x, cv);
-    const float m = 0.5f * cq.ghat + cq.offset + detect_guard(y);
-    const float4 qmin = make_float4(y[0] - m, y[1] - m, y[2] - m, 1.0f);
-    const float4 qmax = make_float4(y[0] + m, y[1] + m, y[2] + m, 0.0f);
-    MeshVertexOp op{s, p, b, cv, 0u};
-    bvh_query(fb, qmin, qmax, op, &b.st->status);
+    const unsigned cv = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = cv < s.ncv;
+    float4 qmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qmax = qmin;
+    if (act) {
+        const PpfVertexParam &cq = s.cm_vparam[s.cm_vprop[cv].param_index];
+        const Vec3 y = X(s.cm_x, cv);
+        const float m = 0.5f * cq.ghat + cq.offset + detect_guard(y);
+        qmin = make_float4(y[0] - m, y[1] - m, y[2] - m, 1.0f);
+        qmax = make_float4(y[0] + m, y[1] + m, y[2] + m, 0.0f);
+    }
+    MeshVertexOp op{s, p, b, act ? cv : 0u, 0u};
+    warp_query(fb, act, qmin, qmax, op, &b.st->status);
     if (op.n) atomicAdd(&b.st->n_contact, op.n);
 }
 
@@ -767,18 +785,19 @@ struct MeshEdgeOp {
 };
 
 __global__ void k_mesh_edge_edge(Scene s, StepParams p, AssemblyBuffers b) {
-    unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= s.ne) return;
-    const PpfEdgeProp &ep = s.eprop[e];
-    if (ep.fixed || !(ep.mass > 0.0f)) return;
-    const unsigned *ed = s.edge + 2 * e;
-    const PpfEdgeParam &eq = s.eparam[ep.param_index];
-    float4 qmin, qmax;
-    const Vec3 a = X(b.x, ed[0]), c = X(b.x, ed[1]);
-    seg_box(a, c, 0.5f * eq.ghat + eq.offset + fmaxf(detect_guard(a), detect_guard(c)), qmin,
-            qmax);
-    MeshEdgeOp op{s, p, b, e, 0u};
-    bvh_query(s.cm_edge_bvh, qmin, qmax, op, &b.st->status);
+    const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+    bool act = e < s.ne;
+    if (act) act = !s.eprop[e].fixed && s.eprop[e].mass > 0.0f;
+    float4 qmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qmax = qmin;
+    if (act) {
+        const unsigned *ed = s.edge + 2 * e;
+        const PpfEdgeParam &eq = s.eparam[s.eprop[e].param_index];
+        const Vec3 a = X(b.x, ed[0]), c = X(b.x, ed[1]);
+        seg_box(a, c, 0.5f * eq.ghat + eq.offset + fmaxf(detect_guard(a), detect_guard(c)),
+                qmin, qmax);
+    }
+    MeshEdgeOp op{s, p, b, act ? e : 0u, 0u};
+    warp_query(s.cm_edge_bvh, act, qmin, qmax, op, &b.st->status);
     if (op.n) atomicAdd(&b.st->n_contact, op.n);
 }
 

@@ -8,18 +8,18 @@
 //   point-edge   627-731  (interior closest point, face-neighbor count)
 //   point-face   733-808  (interior closest point)
 //   edge-edge    810-887  (edge < query edge, no shared vertex, interior)
-// and the traversal of contact/aabb.hpp:78-107 (push left then right), with a
-// bounded stack that latches STATUS_BVH_STACK_OVERFLOW instead of asserting.
+// and the traversal of contact/aabb.hpp:78-107, restated stackless (escape
+// links) with warp-synchronous leaf tests; a bounded walk latches
+// STATUS_BVH_STACK_OVERFLOW instead of asserting.
 #pragma once
 
 #include "../physics/contact_local.cuh"
 #include "../physics/distance.cuh"
+#include "lbvh.cuh"
 #include "scene.cuh"
 
 namespace ppf {
 namespace gpu {
-
-constexpr int kStackDepth = 96;
 
 __device__ __forceinline__ bool box_overlap(const float4 &amin, const float4 &amax,
                                             const float4 &bmin, const float4 &bmax) {
@@ -28,35 +28,79 @@ __device__ __forceinline__ bool box_overlap(const float4 &amin, const float4 &am
            (amin.z <= bmax.z && amax.z >= bmin.z);
 }
 
-// Calls op(prim) for every leaf whose box overlaps the query box. With an
-// exclusion box (xmin, xmax), leaves that also overlap it are skipped: the
-// previous piece of a split query reports those.
+// Stackless traversal with warp-synchronous leaf tests. Every lane of the
+// warp calls this together (a lane without a query passes active = false).
+// Each lane walks the tree depth-first through the traversal links (left
+// child on a box hit, escape node otherwise: no stack, no local memory)
+// until it reaches its next overlapping leaf; then every lane that holds a
+// leaf runs op(prim) in the same pass, so the narrow-phase test, the heavy
+// part, executes once for the warp instead of once per diverged lane. The
+// rounds repeat until no lane finds a leaf. With an exclusion box (xmin,
+// xmax), leaves that also overlap it are skipped: the previous piece of a
+// split query reports those. A walk longer than the tree allows latches
+// STATUS_BVH_STACK_OVERFLOW (a corrupted tree) and ends.
 template <class Op>
-__device__ void bvh_query(const BvhView &b, const float4 &qmin, const float4 &qmax,
-                          Op &op, unsigned *status, const float4 *xmin = nullptr,
-                          const float4 *xmax = nullptr) {
-    if (b.n == 0 || qmin.w == 0.0f) return;
-    unsigned stack[kStackDepth];
-    int sp = 0;
-    stack[sp++] = b.root;
-    while (sp) {
-        unsigned id = stack[--sp];
-        float4 lo = b.bmin[id], hi = b.bmax[id];
-        if (!box_overlap(lo, hi, qmin, qmax)) continue;
-        uint2 nd = b.node[id];
-        if (nd.y == 0u) {
-            if (xmin && box_overlap(lo, hi, *xmin, *xmax)) continue;
-            op(nd.x - 1u);
-        } else {
-            if (sp + 2 > kStackDepth) {
+__device__ void warp_query(const BvhView &b, bool active, const float4 &qmin,
+                           const float4 &qmax, Op &op, unsigned *status,
+                           const float4 *xmin = nullptr, const float4 *xmax = nullptr) {
+    unsigned cur = (active && b.n != 0u && qmin.w != 0.0f) ? b.root : kLinkEnd;
+    const unsigned bound = 4u * b.n + 64u;
+    unsigned steps = 0;
+    while (true) {
+        unsigned cand = kLinkEnd;
+        while (cur != kLinkEnd) {
+            const float4 lo = b.bmin[cur], hi = b.bmax[cur];
+            const uint2 ln = b.link[cur];
+            if (++steps > bound) {
                 atomicOr(status, STATUS_BVH_STACK_OVERFLOW);
-                return;
+                cur = kLinkEnd;
+                break;
             }
-            stack[sp++] = nd.x - 1u;
-            stack[sp++] = nd.y - 1u;
+            if (box_overlap(lo, hi, qmin, qmax)) {
+                if (!(ln.x & kLinkLeaf)) {
+                    cur = ln.x;
+                    continue;
+                }
+                cur = ln.y;
+                if (!xmin || !box_overlap(lo, hi, *xmin, *xmax)) {
+                    cand = ln.x & ~kLinkLeaf;
+                    break;
+                }
+            } else {
+                cur = ln.y;
+            }
         }
+        if (!__any_sync(0xffffffffu, cand != kLinkEnd)) break;
+        if (cand != kLinkEnd) op(cand);
     }
 }
+
+// Warp-aggregated slot reservation: the lanes that reach this call together
+// take consecutive slots with one atomic add on the counter. Returns
+// kSentinel past the capacity (the counter still counts, so the host sees
+// the size a list needs).
+__device__ __forceinline__ unsigned push_slot(unsigned *ctr, unsigned cap) {
+    const unsigned mask = __activemask();
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned leader = __ffs(mask) - 1u;
+    unsigned base = 0u;
+    if (lane == leader) base = atomicAdd(ctr, (unsigned)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    const unsigned slot = base + (unsigned)__popc(mask & ((1u << lane) - 1u));
+    return slot < cap ? slot : kSentinel;
+}
+
+// Work items of a grid-stride loop taken a warp at a time, so that all 32
+// lanes stay together for warp_query: item = base + lane, valid when below
+// the total; `base` is the same on every lane of the warp.
+struct WarpItems {
+    unsigned base, stride, lane;
+    __device__ __forceinline__ WarpItems() {
+        lane = threadIdx.x & 31u;
+        base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u;
+        stride = ((gridDim.x * blockDim.x) >> 5) * 32u;
+    }
+};
 
 __device__ __forceinline__ Vec3 X(const float *x, unsigned i) {
     return vec3(x[3 * i], x[3 * i + 1], x[3 * i + 2]);

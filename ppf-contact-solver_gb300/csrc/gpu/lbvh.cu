@@ -255,9 +255,37 @@ __global__ void k_leaf_refit(PrimKind kind, const unsigned *prims,
 }
 
 __global__ void k_single_leaf(PrimKind kind, const unsigned *prims, uint2 *node,
-                              unsigned *parent) {
+                              unsigned *parent, uint2 *link) {
     node[0] = make_uint2(1u, 0u);
     parent[0] = 0u;
+    link[0] = make_uint2(0u | kLinkLeaf, kLinkEnd);
+}
+
+// Traversal links of every node: its left child (or primitive, for a leaf)
+// and its escape node, the right sibling of the nearest ancestor-or-self that
+// is a left child (kLinkEnd when there is none). A stackless depth-first walk
+// goes to the left child on a box hit and to the escape node otherwise.
+__global__ void k_links(unsigned n, const uint2 *node, const unsigned *parent, unsigned root,
+                        uint2 *link, unsigned *status) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * n - 1) return;
+    const uint2 nd = node[t];
+    const unsigned first = nd.y == 0u ? ((nd.x - 1u) | kLinkLeaf) : nd.x - 1u;
+    unsigned esc = kLinkEnd, cur = t;
+    for (unsigned guard = 0; cur != root; ++guard) {
+        const unsigned p = parent[cur];
+        const uint2 pn = node[p];
+        if (pn.x - 1u == cur) {
+            esc = pn.y - 1u;
+            break;
+        }
+        cur = p;
+        if (guard > 2 * n + 64u) {
+            atomicOr(status, STATUS_REFIT_CYCLE);
+            break;
+        }
+    }
+    link[t] = make_uint2(first, esc);
 }
 
 } // namespace
@@ -265,6 +293,7 @@ __global__ void k_single_leaf(PrimKind kind, const unsigned *prims, uint2 *node,
 void Lbvh::reserve(unsigned count) {
     unsigned nn = count == 0 ? 1 : 2 * count - 1;
     node.reserve(nn);
+    link.reserve(nn);
     parent.reserve(nn);
     bmin.reserve(nn);
     bmax.reserve(nn);
@@ -276,6 +305,7 @@ void Lbvh::reserve(unsigned count) {
 
 void Lbvh::release() {
     node.release();
+    link.release();
     parent.release();
     bmin.release();
     bmax.release();
@@ -295,7 +325,7 @@ void lbvh_build(Lbvh &bvh, const PrimSet &ps, const float *x_tree,
     unsigned grid = div_up(n, kBlock);
     if (n == 1) {
         k_single_leaf<<<1, 1, 0, s>>>(ps.kind, ps.prims, bvh.node.data(),
-                                      bvh.parent.data());
+                                      bvh.parent.data(), bvh.link.data());
         PPF_LAUNCH_CHECK();
         bvh.root = 0;
     } else {
@@ -315,6 +345,10 @@ void lbvh_build(Lbvh &bvh, const PrimSet &ps, const float *x_tree,
                                          bvh.visit.data());
         PPF_LAUNCH_CHECK();
         bvh.root = n;
+        k_links<<<div_up(2 * n - 1, kBlock), kBlock, 0, s>>>(n, bvh.node.data(),
+                                                             bvh.parent.data(), bvh.root,
+                                                             bvh.link.data(), d_status);
+        PPF_LAUNCH_CHECK();
     }
     lbvh_refit(bvh, ps, x0, x1, extrapolate, d_status, s);
 }

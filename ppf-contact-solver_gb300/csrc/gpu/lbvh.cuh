@@ -17,10 +17,18 @@ namespace gpu {
 
 enum PrimKind : int { PRIM_VERTEX = 1, PRIM_EDGE = 2, PRIM_FACE = 3 };
 
+constexpr unsigned kLinkLeaf = 0x80000000u;
+constexpr unsigned kLinkEnd = 0xFFFFFFFFu;
+
 struct Lbvh {
     unsigned n = 0;            // primitives
     unsigned root = 0;         // node index of the root
     DevBuf<uint2> node;        // 2n-1
+    // 2n-1 traversal links: x = left child of an internal node, or the
+    // primitive | kLinkLeaf for a leaf; y = escape node (the node a
+    // depth-first walk visits after this node's subtree), kLinkEnd after the
+    // last one
+    DevBuf<uint2> link;
     DevBuf<unsigned> parent;   // 2n-1 (root is its own parent)
     DevBuf<float4> bmin;       // 2n-1, w = 1 if active else 0
     DevBuf<float4> bmax;       // 2n-1

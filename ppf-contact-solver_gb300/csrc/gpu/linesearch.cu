@@ -235,42 +235,61 @@ struct MeshEdgeCcdOp {
     }
 };
 
-__global__ void k_ccd_mesh_vertex(Scene s, BvhView fb, LineSearchArgs a) {
-    unsigned cv = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cv >= s.ncv) return;
-    const PpfVertexParam &cq = s.cm_vparam[s.cm_vprop[cv].param_index];
-    const Vec3 y = X(s.cm_x, cv);
-    const float m = 0.5f * cq.ghat + cq.offset;
-    const float4 qmin = make_float4(y[0] - m, y[1] - m, y[2] - m, 1.0f);
-    const float4 qmax = make_float4(y[0] + m, y[1] + m, y[2] + m, 0.0f);
-    MeshVertexCcdOp op{s, a, cv, a.max_t};
-    bvh_query(fb, qmin, qmax, op, &a.st->status);
-    atomicMin(&a.st->toi_vf_bits, __float_as_uint(op.toi));
+// The warp's minimum of a per-lane time of impact, taken into `bits` with one
+// atomic by lane 0 (every lane of the warp calls this).
+__device__ __forceinline__ void warp_min_toi(unsigned *bits, float toi) {
+    for (int off = 16; off > 0; off >>= 1)
+        toi = fminf(toi, __shfl_xor_sync(0xffffffffu, toi, off));
+    if ((threadIdx.x & 31u) == 0u) atomicMin(bits, __float_as_uint(toi));
 }
 
+__global__ void k_ccd_mesh_vertex(Scene s, BvhView fb, LineSearchArgs a) {
+    const unsigned cv = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = cv < s.ncv;
+    float4 qmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qmax = qmin;
+    if (act) {
+        const PpfVertexParam &cq = s.cm_vparam[s.cm_vprop[cv].param_index];
+        const Vec3 y = X(s.cm_x, cv);
+        const float m = 0.5f * cq.ghat + cq.offset;
+        qmin = make_float4(y[0] - m, y[1] - m, y[2] - m, 1.0f);
+        qmax = make_float4(y[0] + m, y[1] + m, y[2] + m, 0.0f);
+    }
+    MeshVertexCcdOp op{s, a, act ? cv : 0u, a.max_t};
+    warp_query(fb, act, qmin, qmax, op, &a.st->status);
+    warp_min_toi(&a.st->toi_vf_bits, op.toi);
+}
+
+// One lane per surface vertex in the vertex tree's Morton order; the warp's
+// lanes walk the face, vertex and collision-face trees together.
 __global__ void k_ccd_vertex(Scene s, BvhView fb, BvhView vb, LineSearchArgs a) {
-    unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= s.n_surf) return;
-    unsigned v = vb.node[t].x - 1u;
-    float toi = vertex_constraint_toi(s, a, v);
-    float m = s.margin_vert[v];
-    Vec3 p0 = X(a.x0, v), p1 = sweep_end(a.x0, a.x1, v, a.max_t);
-    float4 qmin = make_float4(fminf(p0[0], p1[0]) - m, fminf(p0[1], p1[1]) - m,
-                              fminf(p0[2], p1[2]) - m, 1.0f);
-    float4 qmax = make_float4(fmaxf(p0[0], p1[0]) + m, fmaxf(p0[1], p1[1]) + m,
-                              fmaxf(p0[2], p1[2]) + m, 0.0f);
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = t < s.n_surf;
+    const unsigned v = act ? vb.node[t].x - 1u : 0u;
+    float toi = a.max_t;
+    float4 qmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qmax = qmin;
+    bool mesh = false;
+    if (act) {
+        toi = vertex_constraint_toi(s, a, v);
+        float m = s.margin_vert[v];
+        Vec3 p0 = X(a.x0, v), p1 = sweep_end(a.x0, a.x1, v, a.max_t);
+        qmin = make_float4(fminf(p0[0], p1[0]) - m, fminf(p0[1], p1[1]) - m,
+                           fminf(p0[2], p1[2]) - m, 1.0f);
+        qmax = make_float4(fmaxf(p0[0], p1[0]) + m, fmaxf(p0[1], p1[1]) + m,
+                           fmaxf(p0[2], p1[2]) + m, 0.0f);
+        const PpfVertexProp &vp = s.vprop[v];
+        mesh = s.ncf && vp.fix_index == 0 && vp.mass > 0.0f;
+    }
     PointFaceCcdOp pf{s, a, v, a.max_t};
-    bvh_query(fb, qmin, qmax, pf, &a.st->status);
+    warp_query(fb, act, qmin, qmax, pf, &a.st->status);
     PointPointCcdOp pp{s, a, v, a.max_t};
-    bvh_query(vb, qmin, qmax, pp, &a.st->status);
+    warp_query(vb, act, qmin, qmax, pp, &a.st->status);
     toi = fminf(toi, fminf(pf.toi, pp.toi));
-    const PpfVertexProp &vp = s.vprop[v];
-    if (s.ncf && vp.fix_index == 0 && vp.mass > 0.0f) {
+    if (s.ncf) {
         MeshPointFaceCcdOp mf{s, a, v, a.max_t};
-        bvh_query(s.cm_face_bvh, qmin, qmax, mf, &a.st->status);
+        warp_query(s.cm_face_bvh, mesh, qmin, qmax, mf, &a.st->status);
         toi = fminf(toi, mf.toi);
     }
-    atomicMin(&a.st->toi_vf_bits, __float_as_uint(toi));
+    warp_min_toi(&a.st->toi_vf_bits, toi);
 }
 
 struct EdgeEdgeCcdOp {
@@ -330,34 +349,40 @@ struct EdgeEdgeCcdOp {
 __global__ void k_ccd_edge(Scene s, BvhView eb, LineSearchArgs a, EdgePieces ep) {
     const unsigned total = ep.off[ep.n];
     const float seed = __uint_as_float(a.st->toi_vf_bits);
-    for (unsigned item = blockIdx.x * blockDim.x + threadIdx.x; item < total;
-         item += gridDim.x * blockDim.x) {
-        const unsigned t = piece_slot(ep, item);
-        const unsigned k = item - ep.off[t], K = ep.off[t + 1] - ep.off[t];
-        const unsigned e = eb.node[t].x - 1u;
-        const unsigned *ed = s.edge + 2 * e;
-        float m = s.margin_edge[e];
-        Vec3 a0 = X(a.x0, ed[0]), b0 = X(a.x0, ed[1]);
-        Vec3 a1 = sweep_end(a.x0, a.x1, ed[0], seed), b1 = sweep_end(a.x0, a.x1, ed[1], seed);
-        Vec3 p0 = piece_point(a0, b0, k, K), p1 = piece_point(a0, b0, k + 1, K);
-        Vec3 q0 = piece_point(a1, b1, k, K), q1 = piece_point(a1, b1, k + 1, K);
-        float4 qmin, qmax;
-        qmin.x = fminf(fminf(p0[0], p1[0]) - m, fminf(q0[0], q1[0]) - m);
-        qmin.y = fminf(fminf(p0[1], p1[1]) - m, fminf(q0[1], q1[1]) - m);
-        qmin.z = fminf(fminf(p0[2], p1[2]) - m, fminf(q0[2], q1[2]) - m);
-        qmin.w = 1.0f;
-        qmax.x = fmaxf(fmaxf(p0[0], p1[0]) + m, fmaxf(q0[0], q1[0]) + m);
-        qmax.y = fmaxf(fmaxf(p0[1], p1[1]) + m, fmaxf(q0[1], q1[1]) + m);
-        qmax.z = fmaxf(fmaxf(p0[2], p1[2]) + m, fmaxf(q0[2], q1[2]) + m);
-        qmax.w = 0.0f;
+    for (WarpItems w; w.base < total; w.base += w.stride) {
+        const unsigned item = w.base + w.lane;
+        const bool act = item < total;
+        unsigned e = 0u;
+        bool mesh = false;
+        float4 qmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qmax = qmin;
+        if (act) {
+            const unsigned t = piece_slot(ep, item);
+            const unsigned k = item - ep.off[t], K = ep.off[t + 1] - ep.off[t];
+            e = eb.node[t].x - 1u;
+            const unsigned *ed = s.edge + 2 * e;
+            float m = s.margin_edge[e];
+            Vec3 a0 = X(a.x0, ed[0]), b0 = X(a.x0, ed[1]);
+            Vec3 a1 = sweep_end(a.x0, a.x1, ed[0], seed), b1 = sweep_end(a.x0, a.x1, ed[1], seed);
+            Vec3 p0 = piece_point(a0, b0, k, K), p1 = piece_point(a0, b0, k + 1, K);
+            Vec3 q0 = piece_point(a1, b1, k, K), q1 = piece_point(a1, b1, k + 1, K);
+            qmin.x = fminf(fminf(p0[0], p1[0]) - m, fminf(q0[0], q1[0]) - m);
+            qmin.y = fminf(fminf(p0[1], p1[1]) - m, fminf(q0[1], q1[1]) - m);
+            qmin.z = fminf(fminf(p0[2], p1[2]) - m, fminf(q0[2], q1[2]) - m);
+            qmin.w = 1.0f;
+            qmax.x = fmaxf(fmaxf(p0[0], p1[0]) + m, fmaxf(q0[0], q1[0]) + m);
+            qmax.y = fmaxf(fmaxf(p0[1], p1[1]) + m, fmaxf(q0[1], q1[1]) + m);
+            qmax.z = fmaxf(fmaxf(p0[2], p1[2]) + m, fmaxf(q0[2], q1[2]) + m);
+            qmax.w = 0.0f;
+            mesh = s.nce && !s.eprop[e].fixed && s.eprop[e].mass > 0.0f;
+        }
         EdgeEdgeCcdOp op{s, a, e, seed};
-        bvh_query(eb, qmin, qmax, op, &a.st->status);
-        if (s.nce && !s.eprop[e].fixed && s.eprop[e].mass > 0.0f) {
+        warp_query(eb, act, qmin, qmax, op, &a.st->status);
+        if (s.nce) {
             MeshEdgeCcdOp me{s, a, e, op.toi};
-            bvh_query(s.cm_edge_bvh, qmin, qmax, me, &a.st->status);
+            warp_query(s.cm_edge_bvh, mesh, qmin, qmax, me, &a.st->status);
             op.toi = me.toi;
         }
-        atomicMin(&a.st->toi_bits, __float_as_uint(op.toi));
+        warp_min_toi(&a.st->toi_bits, op.toi);
     }
 }
 
@@ -508,32 +533,38 @@ struct MeshFaceEdgeIsectOp {
 __global__ void k_isect(Scene s, BvhView fb, BvhView eb, const float *x,
                         PpfIntersectionRecord *rec, IterStatus *st, EdgePieces ep) {
     const unsigned total = ep.off[ep.n];
-    for (unsigned item = blockIdx.x * blockDim.x + threadIdx.x; item < total;
-         item += gridDim.x * blockDim.x) {
-        const unsigned t = piece_slot(ep, item);
-        const unsigned k = item - ep.off[t], K = ep.off[t + 1] - ep.off[t];
-        const unsigned e = eb.node[t].x - 1u;
-        const unsigned *ed = s.edge + 2 * e;
-        Vec3 a = X(x, ed[0]), b = X(x, ed[1]);
-        const float guard =
-            1e-6f * (1.0f + fmaxf(fmaxf(fmaxf(fabsf(a[0]), fabsf(a[1])), fmaxf(fabsf(a[2]), fabsf(b[0]))),
-                                  fmaxf(fabsf(b[1]), fabsf(b[2]))));
-        const float m = s.eparam[s.eprop[e].param_index].offset + guard;
-        float4 qmin, qmax, xmin, xmax;
-        seg_box(piece_point(a, b, k, K), piece_point(a, b, k + 1, K), m, qmin, qmax);
-        const float4 *xl = nullptr, *xh = nullptr;
-        if (k > 0u) {
-            seg_box(piece_point(a, b, k - 1, K), piece_point(a, b, k, K), m, xmin, xmax);
-            xl = &xmin;
-            xh = &xmax;
+    for (WarpItems w; w.base < total; w.base += w.stride) {
+        const unsigned item = w.base + w.lane;
+        const bool act = item < total;
+        unsigned e = 0u;
+        bool mesh = false;
+        float4 qmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qmax = qmin;
+        float4 xmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), xmax = xmin;
+        if (act) {
+            const unsigned t = piece_slot(ep, item);
+            const unsigned k = item - ep.off[t], K = ep.off[t + 1] - ep.off[t];
+            e = eb.node[t].x - 1u;
+            const unsigned *ed = s.edge + 2 * e;
+            Vec3 a = X(x, ed[0]), b = X(x, ed[1]);
+            const float guard =
+                1e-6f * (1.0f + fmaxf(fmaxf(fmaxf(fabsf(a[0]), fabsf(a[1])),
+                                            fmaxf(fabsf(a[2]), fabsf(b[0]))),
+                                      fmaxf(fabsf(b[1]), fabsf(b[2]))));
+            const float m = s.eparam[s.eprop[e].param_index].offset + guard;
+            seg_box(piece_point(a, b, k, K), piece_point(a, b, k + 1, K), m, qmin, qmax);
+            // a piece after the first excludes what its predecessor reports;
+            // the first piece's exclusion box (w = 0) overlaps nothing
+            if (k > 0u)
+                seg_box(piece_point(a, b, k - 1, K), piece_point(a, b, k, K), m, xmin, xmax);
+            mesh = s.ncf && s.eprop[e].mass > 0.0f;
         }
         FaceEdgeIsectOp op{s, x, e, rec, st};
-        bvh_query(fb, qmin, qmax, op, &st->status, xl, xh);
+        warp_query(fb, act, qmin, qmax, op, &st->status, &xmin, &xmax);
         EdgeEdgeIsectOp op2{s, x, e, rec, st};
-        bvh_query(eb, qmin, qmax, op2, &st->status, xl, xh);
-        if (s.ncf && s.eprop[e].mass > 0.0f) {
+        warp_query(eb, act, qmin, qmax, op2, &st->status, &xmin, &xmax);
+        if (s.ncf) {
             MeshFaceEdgeIsectOp op3{s, x, e, rec, st};
-            bvh_query(s.cm_face_bvh, qmin, qmax, op3, &st->status, xl, xh);
+            warp_query(s.cm_face_bvh, mesh, qmin, qmax, op3, &st->status, &xmin, &xmax);
         }
     }
 }

@@ -31,6 +31,7 @@ struct BvhView {
     const float4 *bmax;
     unsigned root;
     unsigned n;
+    const uint2 *link; // traversal links (Lbvh::link)
 };
 
 struct CsrView {

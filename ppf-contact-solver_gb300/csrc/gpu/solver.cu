@@ -400,7 +400,7 @@ PieceBuffers Solver::pieces() {
 }
 
 BvhView Solver::view(const Lbvh &b) const {
-    return BvhView{b.node.data(), b.bmin.data(), b.bmax.data(), b.root, b.n};
+    return BvhView{b.node.data(), b.bmin.data(), b.bmax.data(), b.root, b.n, b.link.data()};
 }
 
 void Solver::upload_props() {
