@@ -53,6 +53,15 @@ void ppf_scene_default_param(PpfParamSet *out);
 unsigned ppf_scene_add_shell(PpfScene *scene, const float *vertices,
                              unsigned n_vertices, const unsigned *faces,
                              unsigned n_faces, const PpfShellMaterial *mat);
+/* A shell whose faces carry their own materials (the reference scene's
+ * per-face tri-* parameter arrays, scene.rs:1660-1830): face i uses
+ * materials[face_material[i]]. Vertices are appended as by
+ * ppf_scene_add_shell; returns the index of the first, or 0xffffffff when a
+ * face names a material past n_materials. */
+unsigned ppf_scene_add_shell_faces(PpfScene *scene, const float *vertices, unsigned nv,
+                                   const unsigned *faces, unsigned nf,
+                                   const unsigned *face_material,
+                                   const PpfShellMaterial *materials, unsigned n_materials);
 /* Initial velocity of every vertex (3 floats each); prev = curr - v dt. */
 void ppf_scene_set_velocity(PpfScene *scene, const float *velocity);
 /* Fix pins at the vertices' current positions. kinematic != 0 marks pins

@@ -221,6 +221,8 @@ struct VertexQueryOp {
     PairLists &pl;
     IterStatus *st;
     unsigned found;
+    // a point-point pair is kept from its higher-index vertex
+    __device__ bool pre(unsigned prim) const { return kind != 2 || prim < v; }
     __device__ void operator()(unsigned prim) {
         if (kind == 0) {
             if (accept_point_face(s, x, v, prim)) {
@@ -279,6 +281,8 @@ struct EdgeQueryOp {
     PairLists &pl;
     IterStatus *st;
     unsigned found;
+    // accept_edge_edge keeps the pair with the query edge first
+    __device__ bool pre(unsigned other) const { return e < other; }
     __device__ void operator()(unsigned other) {
         if (accept_edge_edge(s, x, e, other)) {
             unsigned k = push_pair(&st->n_ee, pl.cap_ee);

@@ -13,6 +13,8 @@
 // STATUS_BVH_STACK_OVERFLOW instead of asserting.
 #pragma once
 
+#include <utility>
+
 #include "../physics/contact_local.cuh"
 #include "../physics/distance.cuh"
 #include "lbvh.cuh"
@@ -39,6 +41,16 @@ __device__ __forceinline__ bool box_overlap(const float4 &amin, const float4 &am
 // xmax), leaves that also overlap it are skipped: the previous piece of a
 // split query reports those. A walk longer than the tree allows latches
 // STATUS_BVH_STACK_OVERFLOW (a corrupted tree) and ends.
+// An op may define `bool pre(unsigned prim) const`, a cheap test (an index
+// order, say) that the walk applies to a leaf before handing it over, so a
+// leaf the narrow phase would reject at once costs no round of the warp.
+template <class T> struct HasPre {
+    template <class U>
+    static auto test(int) -> decltype(std::declval<const U &>().pre(0u), char());
+    template <class> static long test(...);
+    static constexpr bool value = sizeof(test<T>(0)) == sizeof(char);
+};
+
 template <class Op>
 __device__ void warp_query(const BvhView &b, bool active, const float4 &qmin,
                            const float4 &qmax, Op &op, unsigned *status,
@@ -62,8 +74,11 @@ __device__ void warp_query(const BvhView &b, bool active, const float4 &qmin,
                     continue;
                 }
                 cur = ln.y;
-                if (!xmin || !box_overlap(lo, hi, *xmin, *xmax)) {
-                    cand = ln.x & ~kLinkLeaf;
+                const unsigned prim = ln.x & ~kLinkLeaf;
+                bool take = !xmin || !box_overlap(lo, hi, *xmin, *xmax);
+                if constexpr (HasPre<Op>::value) take = take && op.pre(prim);
+                if (take) {
+                    cand = prim;
                     break;
                 }
             } else {

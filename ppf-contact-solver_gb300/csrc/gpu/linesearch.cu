@@ -136,6 +136,7 @@ struct PointPointCcdOp {
     const LineSearchArgs &a;
     unsigned v;
     float toi;
+    __device__ bool pre(unsigned w) const { return w < v; }
     __device__ void operator()(unsigned w) {
         bool either_dyn = s.vprop[v].fix_index == 0 || s.vprop[w].fix_index == 0;
         bool both_collider = s.vprop[v].collider && s.vprop[w].collider;
@@ -297,6 +298,7 @@ struct EdgeEdgeCcdOp {
     const LineSearchArgs &a;
     unsigned e;
     float toi;
+    __device__ bool pre(unsigned o) const { return e < o; }
     __device__ void operator()(unsigned o) {
         const unsigned *e0 = s.edge + 2 * e;
         const unsigned *e1 = s.edge + 2 * o;
@@ -457,6 +459,7 @@ struct EdgeEdgeIsectOp {
     unsigned e;
     PpfIntersectionRecord *records;
     IterStatus *st;
+    __device__ bool pre(unsigned o) const { return o < e; }
     __device__ void operator()(unsigned o) {
         if (!(o < e)) return;
         const unsigned *e0 = s.edge + 2 * e;

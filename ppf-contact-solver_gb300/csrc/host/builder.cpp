@@ -188,6 +188,23 @@ unsigned ppf_scene_add_shell(PpfScene *s, const float *v, unsigned nv,
     return base;
 }
 
+unsigned ppf_scene_add_shell_faces(PpfScene *s, const float *v, unsigned nv, const unsigned *f,
+                                   unsigned nf, const unsigned *face_material,
+                                   const PpfShellMaterial *materials, unsigned n_materials) {
+    if (n_materials == 0) return 0xFFFFFFFFu;
+    for (unsigned i = 0; i < nf; ++i)
+        if (face_material[i] >= n_materials) return 0xFFFFFFFFu;
+    unsigned base = (unsigned)s->x.size() / 3;
+    s->x.insert(s->x.end(), v, v + 3 * (size_t)nv);
+    s->vel.insert(s->vel.end(), 3 * (size_t)nv, 0.0f);
+    unsigned m0 = (unsigned)s->materials.size();
+    s->materials.insert(s->materials.end(), materials, materials + n_materials);
+    for (unsigned i = 0; i < 3 * nf; ++i) s->faces.push_back(base + f[i]);
+    for (unsigned i = 0; i < nf; ++i) s->face_material.push_back(m0 + face_material[i]);
+    s->built = false;
+    return base;
+}
+
 void ppf_scene_set_velocity(PpfScene *s, const float *velocity) {
     std::memcpy(s->vel.data(), velocity, s->vel.size() * sizeof(float));
 }

@@ -103,6 +103,24 @@ def build_product(force: bool = False, verbose: bool = False) -> Path:
     return PRODUCT_LIB
 
 
+DRIVER = PKG / "bin" / "ppf-contact-solver"
+
+
+def build_driver(force: bool = False) -> Path:
+    """Compile the solver executable (csrc/driver/main.cpp) against the
+    product library, with an rpath to it."""
+    srcs = _sources([CSRC / "driver"], {".cpp"})
+    deps = srcs + _sources([INCLUDE], {".h"}) + [PRODUCT_LIB]
+    if not force and DRIVER.exists() and DRIVER.stat().st_mtime > _newest(deps):
+        return DRIVER
+    DRIVER.parent.mkdir(parents=True, exist_ok=True)
+    tmp = DRIVER.with_suffix(".tmp")
+    _run([CXX, "-std=c++17", "-O2", "-I", str(INCLUDE), *map(str, srcs), "-o", str(tmp),
+          "-L", str(LIBDIR), "-lppf_gb300", "-Wl,-rpath,$ORIGIN/../lib"])
+    os.replace(tmp, DRIVER)
+    return DRIVER
+
+
 def build_oracle(force: bool = False) -> Path:
     """Compile the CPU oracle (oracle/*.cpp) into oracle/liboracle_ppf.so."""
     srcs = sorted(ORACLE_DIR.glob("oracle_*.cpp"))
@@ -155,6 +173,7 @@ def build_all(force: bool = False) -> None:
         f1.result()
         f2.result()
         f3.result()
+    build_driver(force)
 
 
 if __name__ == "__main__":
