@@ -96,6 +96,9 @@ def _declare(lib):
     lib.oracle_time.restype = C.c_double
     lib.oracle_check_intersection.restype = C.c_bool
     lib.oracle_check_intersection.argtypes = [f32p]
+    lib.oracle_ls_trace.restype = C.c_bool
+    lib.oracle_ls_trace.argtypes = [C.c_uint, f32p, f32p, C.POINTER(C.c_float),
+                                    C.POINTER(C.c_float)]
     lib.oracle_intersection_records.restype = C.c_uint
     lib.oracle_intersection_records.argtypes = [f32p, u32p, C.c_uint]
     lib.oracle_update_constraint.argtypes = [P]
@@ -162,6 +165,16 @@ class OracleSession:
         n = self.lib.oracle_intersection_records(
             np.ascontiguousarray(x, np.float32).reshape(-1), out, max_count)
         return out[:3 * min(n, max_count)].reshape(-1, 3), int(n)
+
+    def ls_trace(self, k: int = 0):
+        """Line-search inputs of the k-th newest Newton iteration: (x0, x1,
+        contact toi, raw strain-limit toi), or None."""
+        x0 = np.empty(3 * self.n, np.float32)
+        x1 = np.empty(3 * self.n, np.float32)
+        tc, ts = C.c_float(), C.c_float()
+        if not self.lib.oracle_ls_trace(k, x0, x1, C.byref(tc), C.byref(ts)):
+            return None
+        return x0, x1, tc.value, ts.value
 
     def stats(self):
         a, b, c = C.c_uint(), C.c_uint(), C.c_float()

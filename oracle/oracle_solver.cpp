@@ -94,6 +94,14 @@ struct Oracle {
     std::vector<float> cm_margin_f, cm_margin_e;
     Tree tcf, tce;
     StepStatsO stats;
+    // the line-search inputs of the last Newton iterations (x0: the previous
+    // iterate, x1: the candidate) with their contact and strain-limit times,
+    // newest last, for reproducing a failing step
+    struct LsTrace {
+        std::vector<float> x0, x1;
+        float toi_contact, toi_strain;
+    };
+    std::vector<LsTrace> ls_trace;
     unsigned last_pcg_iters = 0;
     bool dirichlet = true; // eliminate fix pins after assembly (main.cu:954-1049)
     float last_pcg_resid = 0.0f;
@@ -1380,7 +1388,12 @@ PpfStepResult Oracle::advance() {
             res.contact_separated = false;
             return res;
         }
-        toi = std::fmin(toi, strain_line_search() / T);
+        {
+            const float sl = strain_line_search();
+            if (ls_trace.size() >= 8) ls_trace.erase(ls_trace.begin());
+            ls_trace.push_back(LsTrace{target, x, toi, sl});
+            toi = std::fmin(toi, sl / T);
+        }
         if (toi <= 1.19209290e-7f) {
             res.ccd_success = false;
             return res;
@@ -1455,6 +1468,20 @@ unsigned oracle_intersection_records(const float *x, unsigned *out, unsigned max
 }
 
 void oracle_update_constraint(const PpfConstraint *c) { g_oracle->set_constraint(c); }
+
+// Line-search record k of the last (up to 8) Newton iterations, 0 the
+// newest: x0 (previous iterate), x1 (candidate), and the contact and raw
+// strain-limit times of impact. Returns false past the records kept.
+bool oracle_ls_trace(unsigned k, float *x0, float *x1, float *toi_contact, float *toi_strain) {
+    const auto &t = g_oracle->ls_trace;
+    if (k >= t.size()) return false;
+    const auto &r = t[t.size() - 1 - k];
+    std::memcpy(x0, r.x0.data(), r.x0.size() * sizeof(float));
+    std::memcpy(x1, r.x1.data(), r.x1.size() * sizeof(float));
+    *toi_contact = r.toi_contact;
+    *toi_strain = r.toi_strain;
+    return true;
+}
 
 void oracle_step_stats(unsigned *newton, unsigned *pcg_iters, float *step_ms) {
     *newton = g_oracle->stats.newton;

@@ -155,3 +155,52 @@ def test_collision_mesh_matches_reference(oracle_lib, product_lib, ref_pipe):
         assert np.float32(t_ref) == np.float32(t_orc) and t_orc < 1.0, (dy, t_ref, t_orc)
         assert (pa.value, oa.value) == (pb.value, ob2.value)
     assert ref_pipe.refpipe_check_intersection(x0) and o.intersection_free(x0)
+
+
+def test_twisted_tube_failure_is_the_reference_algorithm(oracle_lib, product_lib, ref_pipe):
+    """A 32 x 64 twisted tube (both end rings pinned and turned at 2 rad/s)
+    fails around step 65 with a non-finite Newton system, on the oracle as
+    on the GPU. This pins that failure to the reference's own code: on the
+    line-search inputs of the failing step's last Newton iterations (each
+    admitting only a tiny step, the tube twisted against its 1% strain
+    limit) the reference's strainlimiting::line_search returns the oracle's
+    time of impact bit for bit, and the reference's own assembly at the
+    iterate those steps reach holds non-finite blocks and forces (a face on
+    the strain limit: the barrier's 1 / gap^2 stiffness)."""
+    from oracle.binding import OracleSession
+    from ppf_gb300 import abi, scenes
+
+    sc, motion = scenes.twisted_tube(32, 64)
+    o = OracleSession(sc, motion)
+    failed = None
+    for k in range(90):
+        r = o.step()
+        if not r.success():
+            failed = (k, r.as_dict())
+            break
+    assert failed is not None and not failed[1]["pcg_success"], failed
+    assert ref_pipe.refpipe_init(sc.dataset, C.byref(o.param))
+    T = np.float32(o.param.line_search_max_t)
+    records = [o.ls_trace(j) for j in range(8)]
+    records = [r for r in records if r is not None]
+    assert len(records) == 8
+    for x0, x1, tc, ts in records:
+        tref = ref_pipe.refpipe_strain_line_search(x0, x1)
+        assert np.float32(np.float32(ts) / T) == np.float32(tref), (ts, tref)
+        assert ts / T < 1e-3  # the strain limit admits a tiny step only
+    # the iterate the newest record leads to, and the reference's system there
+    x0, x1, tc, ts = records[0]
+    toi = np.float32(min(tc, np.float32(ts) / T))
+    ev = (x0 + (toi * (x1 - x0)).astype(np.float32)).astype(np.float32)
+    curr, prev = o.positions()
+    prm = abi.ParamSet.from_buffer_copy(o.param)
+    prm.time = o.time
+    ref_pipe.refpipe_state(curr.reshape(-1), prev.reshape(-1), C.byref(prm))
+    ref_pipe.refpipe_assemble(ev, ev, np.float32(prm.dt))
+    nb = ref_pipe.refpipe_blocks(None, None, None)
+    rows, cols = np.zeros(nb, np.uint32), np.zeros(nb, np.uint32)
+    blocks = np.zeros(9 * nb, np.float32)
+    ref_pipe.refpipe_blocks(rows, cols, blocks)
+    force = np.zeros(ev.size, np.float32)
+    ref_pipe.refpipe_force(force)
+    assert (~np.isfinite(blocks)).sum() > 0 and (~np.isfinite(force)).sum() > 0
