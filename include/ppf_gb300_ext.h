@@ -133,22 +133,6 @@ typedef struct {
 } PpfStepStats;
 void ppf_step_stats(PpfStepStats *out);
 
-/* ---- PCG recurrence ---------------------------------------------------------
- * The block-Jacobi PCG (solver/solver.cu:431-1383) in one of two algebraically
- * equal forms, both one persistent launch per solve:
- *   0  the reference's recurrence: two grid-wide reductions per iteration
- *      (p^T A p before alpha, r^T z before beta), the iterates of the
- *      reference up to summation order;
- *   1  the single-reduction (Chronopoulos-Gear) recurrence, the default: one
- *      grid-wide reduction per iteration carries r^T z, (A z)^T z and |r|_1,
- *      and alpha follows from them. Same relative-residual criterion, check
- *      cadence and curvature verdict; the iterates differ from form 0 by
- *      rounding, so parity is judged by the true residual.
- * The factored and Schwarz preconditioners use form 0. No counterpart in the
- * reference. Returns 0, or -1 for an unknown form. */
-int ppf_set_pcg_form(int form);
-int ppf_pcg_form(void);
-
 /* ---- preconditioner --------------------------------------------------------
  * The reference's PCG uses block-Jacobi (solver/solver.cu:357-400), the
  * default here. The factored kinds use P = G^T G + eps D^{-1} with G block

@@ -599,8 +599,9 @@ int main(int argc, char **argv) {
                                                now - last_frame)
                                                .count()));
             last_frame = now;
-            append_line(out + "/data/frame_to_time.out",
-                        std::to_string(frame) + " " + std::to_string(t_frame));
+            char tbuf[64];
+            std::snprintf(tbuf, sizeof(tbuf), "%d %.17g", frame, t_frame);
+            append_line(out + "/data/frame_to_time.out", tbuf);
             if (L.auto_save > 0 && frame % L.auto_save == 0) checkpoint(frame);
         }
     }

@@ -282,9 +282,6 @@ unsigned ppf_schwarz_aggregate(unsigned n, const unsigned *off, const unsigned *
     return n_agg;
 }
 
-int ppf_set_pcg_form(int form) { return solver_instance().set_pcg_form(form) ? 0 : -1; }
-int ppf_pcg_form(void) { return solver_instance().pcg_form(); }
-
 int ppf_set_preconditioner(int kind, float param) {
     return solver_instance().set_preconditioner(kind, param) ? 0 : -1;
 }

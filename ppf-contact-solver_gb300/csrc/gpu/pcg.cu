@@ -315,14 +315,7 @@ struct PcgArgs {
     float *R;            // 8 floats per vertex: {z, p} records
     float4 *p, *Ap, *Ap_c, *Ap_ovf;
     float4 *Y;   // G r of the factored preconditioner
-    // single-reduction form (k_pcg_sr): two buffers of 16-float records per
-    // vertex, the owner's s = A p recurrence, and two buffers each of the
-    // product parts (fixed per vertex, contact per sorted row, overflow per
-    // overflow row)
-    float *R2;
-    float4 *S, *Wf, *Wc, *Wo;
-    unsigned n_c, n_o; // strides of the Wc / Wo buffers
-    float *part; // 2 buffers of up to 4 floats per block
+    float *part; // 2 buffers of 2 floats per block
     unsigned *bar;
     float tol;
     unsigned max_iter;
@@ -569,263 +562,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             const float rz_new = a, err_now = b;
             beta = rz_new / rz0;
             rz0 = rz_new;
-            const bool at_cap = iter >= g.max_iter;
-            if (iter == next_check || at_cap) {
-                const float reresid = err_now / err0;
-                PcgResult out{iter, reresid, -1, broke, err0, break_val, 0u};
-                if (reresid < g.tol) out.state = 0;
-                else if (broke == 3) out.state = 1;
-                else if (broke == 1) out.state = 2;
-                else if (!isfinite(reresid) || at_cap) out.state = 2;
-                if (out.state >= 0) {
-                    if (blockIdx.x == 0 && threadIdx.x == 0) *g.res = out;
-                    return;
-                }
-                if (reresid < 8.0f * g.tol) stride = 1;
-                next_check = iter + stride;
-            }
-        }
-    }
-aborted:
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        *g.res = PcgResult{0u, 0.0f, 2, 0, 0.0f, 0.0f, STATUS_PCG_BREAKDOWN};
-}
-
-// ---- single-reduction form ---------------------------------------------------
-// The Chronopoulos-Gear recurrence of preconditioned CG, which needs one
-// grid-wide reduction per iteration instead of two:
-//   p_i = u_i + b_i p_{i-1},  s_i = w_i + b_i s_{i-1}   (s = A p)
-//   x_{i+1} = x_i + a_i p_i,  r_{i+1} = r_i - a_i s_i,  u_{i+1} = P r_{i+1}
-//   w_{i+1} = A u_{i+1};  g = r.u, d = w.u in ONE reduction
-//   b_{i+1} = g_{i+1} / g_i,  a_{i+1} = g_{i+1} / (d_{i+1} - b_{i+1} g_{i+1} / a_i)
-// with the denominator, p^T A p in exact arithmetic, under the reference's
-// curvature verdict (256 eps times the round-off scale of d). One pass per
-// iteration computes w = A u with u formed on the fly: vertex j's record,
-// written by its owner in the previous pass, holds u_i(j) = P r_i(j),
-// sigma_{i-1}(j) = P s_{i-1}(j) and the parts of omega_i(j) = P w_i(j) (the
-// fixed part from the owner, the contact and overflow parts from the tasks
-// that computed them), and every reader evaluates
-//   sigma_i(j) = omega_i(j) + b_i sigma_{i-1}(j),  u_{i+1}(j) = u_i(j) - a_i sigma_i(j)
-// in the same order, so every copy has the same bits. The owner's epilogue
-// then updates p, s, x, r of its row, stores u_{i+1} = P r_{i+1} (not the
-// recurrence value, so u never drifts from P r by more than one step of
-// rounding) and adds its terms of g and |r|_1. The residual check, its
-// cadence and the verdicts are those of k_pcg, on |r_k|_1 after pass k.
-//
-// Record layout (16 floats, two 256-bit loads): u(3), sigma(3), omega_f(3),
-// omega_c(3), omega_o(3), pad. Rows without contact keep omega_c = omega_o =
-// 0 in both buffers.
-constexpr unsigned kRec = 16;
-
-__device__ __forceinline__ void ld_rec16(const float *R, unsigned j, float (&r)[16]) {
-    const float *a = R + kRec * (size_t)j;
-    asm volatile("ld.global.cg.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=f"(r[0]), "=f"(r[1]), "=f"(r[2]), "=f"(r[3]), "=f"(r[4]), "=f"(r[5]),
-                   "=f"(r[6]), "=f"(r[7])
-                 : "l"(a));
-    asm volatile("ld.global.cg.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=f"(r[8]), "=f"(r[9]), "=f"(r[10]), "=f"(r[11]), "=f"(r[12]), "=f"(r[13]),
-                   "=f"(r[14]), "=f"(r[15])
-                 : "l"(a + 8));
-}
-
-// u_{i+1}(j) and sigma_i(j) from vertex j's record of pass i.
-__device__ __forceinline__ void rec_next(const float (&r)[16], float alpha, float beta, Vec3 &u,
-                                         Vec3 &sigma, Vec3 &u_prev) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const float om = (r[6 + c] + r[9 + c]) + r[12 + c];
-        sigma[c] = om + beta * r[3 + c];
-        u_prev[c] = r[c];
-        u[c] = r[c] - alpha * sigma[c];
-    }
-}
-
-struct GatherU {
-    const float *R;
-    float alpha, beta;
-    __device__ __forceinline__ Vec3 operator()(unsigned j) const {
-        float r[16];
-        ld_rec16(R, j, r);
-        Vec3 u, sg, up;
-        rec_next(r, alpha, beta, u, sg, up);
-        return u;
-    }
-};
-
-__device__ __forceinline__ void st_rec_owner(float *R, unsigned i, const Vec3 &u,
-                                             const Vec3 &sigma, const Vec3 &om) {
-    float4 *d = reinterpret_cast<float4 *>(R + kRec * (size_t)i);
-    d[0] = make_float4(u[0], u[1], u[2], sigma[0]);
-    d[1] = make_float4(sigma[1], sigma[2], om[0], om[1]);
-    R[kRec * (size_t)i + 8] = om[2];
-}
-__device__ __forceinline__ void st_rec_part(float *R, unsigned i, int field, const Vec3 &om) {
-    float *d = R + kRec * (size_t)i + field;
-    d[0] = om[0];
-    d[1] = om[1];
-    d[2] = om[2];
-}
-
-// The block-Jacobi inverse of row i (its slice-layout blocks).
-__device__ __forceinline__ Mat3 inv_of(const float *inv, unsigned i) {
-    return load_inv(inv, i / kSliceRows, i % kSliceRows);
-}
-
-__global__ void __launch_bounds__(kThreads, 1) k_pcg_sr(PcgArgs g) {
-    if (g.run_if && *g.run_if == 0u) return;
-    const PcgOperator &A = g.A;
-    const unsigned nb = gridDim.x;
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
-    const unsigned n_slices = A.fixed.n_slices;
-    unsigned *abort = g.bar + 2;
-    float *part0 = g.part, *part1 = g.part + 4 * nb;
-    float *const R[2] = {g.R2, g.R2 + kRec * (size_t)A.n};
-    float a, b;
-
-    __shared__ unsigned s_next;
-    BlockTasks bt{&s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
-                  g.task_start[gridDim.x], g.n_tasks, g.dyn_ctr, g.n_ctr};
-    const float *const vals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
-    // A x0 (parts to Ap, Ap_c, Ap_ovf)
-    bt.start();
-    {
-        const GatherPlain gx{g.x};
-        float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
-        for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-            product_task<kAllSlots>(g, vals, task, lane, gx,
-                                    [&](unsigned, unsigned part, unsigned slot, const Vec3 &acc,
-                                        const Vec3 &) { st4(dst[part], slot, acc); });
-    }
-    a = b = 0.0f;
-    if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
-    // r0 = b - A x0, u0 = P r0; the pass -1 record {u0, 0, 0, 0, 0} in R[1],
-    // zero contact/overflow fields in R[0], p = s = 0 and zero previous parts
-    a = b = 0.0f;
-    for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
-        const unsigned i = sl * kSliceRows + lane;
-        if (i >= A.n) continue;
-        const Vec3 ri = ldcg3(g.r, i) - row_product(g, i);
-        const Vec3 ui = load_inv(A.inv_diag, sl, lane) * ri;
-        st3(g.r, i, ri);
-        float4 *r1 = reinterpret_cast<float4 *>(R[1] + kRec * (size_t)i);
-        float4 *r0 = reinterpret_cast<float4 *>(R[0] + kRec * (size_t)i);
-        const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        r1[0] = make_float4(ui[0], ui[1], ui[2], 0.0f);
-        r1[1] = z4;
-        r1[2] = z4;
-        r1[3] = z4;
-        r0[2] = z4;
-        r0[3] = z4;
-        st4(g.p, i, Vec3::zero());
-        st4(g.S, i, Vec3::zero());
-        st4(g.Wf + A.n, i, Vec3::zero());
-        a += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
-    }
-    for (unsigned c = warp * 32u + lane; c < A.contact.rows; c += nwarps * 32u)
-        st4(g.Wc + g.n_c, c, Vec3::zero());
-    for (unsigned k = warp * 32u + lane; k < A.ovf.count; k += nwarps * 32u)
-        st4(g.Wo + g.n_o, k, Vec3::zero());
-    if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
-    {
-        const float err0 = a;
-        if (err0 == 0.0f) {
-            if (blockIdx.x == 0 && threadIdx.x == 0)
-                *g.res = PcgResult{1u, 0.0f, 0, 0, 0.0f, 0.0f, 0u};
-            return;
-        }
-        float alpha = 0.0f, beta = 0.0f, gamma_prev = 0.0f, alpha_prev = 0.0f;
-        unsigned stride = 4, next_check = 1;
-        int broke = 0;
-        float break_val = 0.0f;
-        for (unsigned k = 0;; ++k) {
-            // pass k: w_k = A u_k, with u_k from the records of pass k - 1
-            const unsigned cur = k & 1u, prv = cur ^ 1u;
-            const float *rd = R[prv];
-            float *wr = R[cur];
-            float4 *wf_cur = g.Wf + cur * (size_t)A.n, *wf_prv = g.Wf + prv * (size_t)A.n;
-            float4 *wc_cur = g.Wc + cur * (size_t)g.n_c, *wc_prv = g.Wc + prv * (size_t)g.n_c;
-            float4 *wo_cur = g.Wo + cur * (size_t)g.n_o, *wo_prv = g.Wo + prv * (size_t)g.n_o;
-            const GatherU gu{rd, alpha, beta};
-            float v[4] = {0.0f, 0.0f, 0.0f, 0.0f}; // d, scale, g, |r|_1
-            bt.start();
-            for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-                product_task<kAllSlots>(
-                    g, vals, task, lane, gu,
-                    [&](unsigned row, unsigned part, unsigned slot, const Vec3 &acc,
-                        const Vec3 &ab) {
-                        float rec[16];
-                        ld_rec16(rd, row, rec);
-                        Vec3 u, sigma, u_prev;
-                        rec_next(rec, alpha, beta, u, sigma, u_prev);
-                        v[0] += u.dot(acc);
-                        v[1] += fabsf(u[0]) * ab[0] + fabsf(u[1]) * ab[1] + fabsf(u[2]) * ab[2];
-                        const Vec3 om = inv_of(A.inv_diag, row) * acc;
-                        if (part == 1u) {
-                            st4(wc_cur, slot, acc);
-                            st_rec_part(wr, row, 9, om);
-                            return;
-                        }
-                        if (part == 2u) {
-                            st4(wo_cur, slot, acc);
-                            st_rec_part(wr, row, 12, om);
-                            return;
-                        }
-                        // the owner: w_{k-1} complete, then p, s, x, r
-                        Vec3 w_prev = ld4(wf_prv, row);
-                        const unsigned c = __ldg(A.contact.index + row);
-                        if (c != 0xFFFFFFFFu) {
-                            w_prev += ld4(wc_prv, c);
-                            const unsigned o = __ldg(A.ovf.index + row);
-                            if (o != 0xFFFFFFFFu) w_prev += ld4(wo_prv, o);
-                        }
-                        Vec3 pi = ld4(g.p, row), si = ld4(g.S, row);
-                        Vec3 xi = ldcg3(g.x, row), ri = ldcg3(g.r, row);
-#pragma unroll
-                        for (int q = 0; q < 3; ++q) {
-                            pi[q] = u_prev[q] + beta * pi[q];
-                            si[q] = w_prev[q] + beta * si[q];
-                            xi[q] += alpha * pi[q];
-                            ri[q] = ri[q] - alpha * si[q];
-                        }
-                        const Vec3 u_ex = inv_of(A.inv_diag, row) * ri;
-                        st4(g.p, row, pi);
-                        st4(g.S, row, si);
-                        st3(g.x, row, xi);
-                        st3(g.r, row, ri);
-                        st4(wf_cur, row, acc);
-                        st_rec_owner(wr, row, u_ex, sigma, om);
-                        v[2] += ri.dot(u_ex);
-                        v[3] += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
-                    });
-            // the initial reductions used part1 then part0: alternate on
-            if (!grid_sum<4>(v, (k & 1u) ? part0 : part1, g.bar, nb, abort)) goto aborted;
-            const float delta = v[0], bound = kCurvatureSlack * kFloatEps * v[1];
-            const float gamma = v[2], err_now = v[3];
-            float denom;
-            if (k == 0) {
-                beta = 0.0f;
-                denom = delta;
-            } else {
-                beta = gamma / gamma_prev;
-                denom = delta - beta * gamma / alpha_prev;
-            }
-            if (denom > bound) {
-                alpha = gamma / denom;
-            } else {
-                alpha = 0.0f;
-                if (!broke) {
-                    broke = (denom < -bound || denom != denom) ? 1 : 3;
-                    break_val = denom;
-                }
-            }
-            gamma_prev = gamma;
-            // a zero step leaves the next pass's recurrences where they are
-            alpha_prev = alpha != 0.0f ? alpha : alpha_prev;
-            if (k == 0) continue;
-            const unsigned iter = k;
             const bool at_cap = iter >= g.max_iter;
             if (iter == next_check || at_cap) {
                 const float reresid = err_now / err0;
@@ -1491,9 +1227,6 @@ __global__ void k_task_split(unsigned T, const unsigned *cost_off, unsigned nb,
 
 void PcgWorkspace::reserve(unsigned n) {
     R.reserve(8 * (size_t)n);
-    R2.reserve(2 * 16 * (size_t)n);
-    S.reserve(n);
-    Wf.reserve(2 * (size_t)n);
     p.reserve(n);
     Ap.reserve(n);
     Y.reserve(n);
@@ -1507,7 +1240,7 @@ void PcgWorkspace::reserve(unsigned n) {
         grid = (unsigned)(sms * per_sm);
         threads = kThreads;
     }
-    partials.reserve(8 * (size_t)grid + 8);
+    partials.reserve(4 * (size_t)grid + 4);
     barrier.reserve(4);
     result.reserve(1);
 }
@@ -1655,8 +1388,6 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     PPF_CUDA(cudaMemsetAsync(ws.barrier.data(), 0, 4 * sizeof(unsigned), q));
     ws.Ap_ovf.reserve(A.ovf.count + 1);
     ws.Ap_c.reserve(A.contact.rows + 1);
-    ws.Wc.reserve(2 * (size_t)A.contact.rows + 2);
-    ws.Wo.reserve(2 * (size_t)A.ovf.count + 2);
     // balanced task ranges per block
     const unsigned T = 2 * A.fixed.n_slices + 2 * A.contact.sell.n_slices + A.ovf.count;
     ws.task_cost.reserve(T + 1);
@@ -1689,13 +1420,6 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
               ws.Ap_c.data(),
               ws.Ap_ovf.data(),
               ws.Y.data(),
-              ws.R2.data(),
-              ws.S.data(),
-              ws.Wf.data(),
-              ws.Wc.data(),
-              ws.Wo.data(),
-              A.contact.rows,
-              A.ovf.count,
               ws.partials.data(),
               ws.barrier.data(),
               tol,
@@ -1705,8 +1429,7 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     void *args[] = {(void *)&g};
     const void *kernel = A.schwarz.n_agg ? (const void *)k_pcg_schwarz
                          : A.factor.diag ? (const void *)k_pcg_factor
-                         : ws.single_reduction ? (const void *)k_pcg_sr
-                                               : (const void *)k_pcg;
+                                         : (const void *)k_pcg;
     size_t dyn_smem = 0;
     if (A.schwarz.n_agg) {
         dyn_smem = (size_t)kWarps * kSchwarzWarpFloats * sizeof(float);

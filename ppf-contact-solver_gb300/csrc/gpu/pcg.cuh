@@ -124,11 +124,6 @@ struct PcgWorkspace {
     DevBuf<float4> Ap_ovf;         // one per overflow row
     DevBuf<float4> Ap_c;           // one per contact row (sorted position)
     DevBuf<float4> Y;              // G r of the factored preconditioner
-    // block-Jacobi solves in the single-reduction (Chronopoulos-Gear) form:
-    // records, s = A p, and the product parts of two passes
-    bool single_reduction = true;
-    DevBuf<float> R2;
-    DevBuf<float4> S, Wf, Wc, Wo;
     DevBuf<unsigned> task_cost, task_off, task_start, scan_tmp, dyn_ctr;
     DevBuf<float> partials;
     DevBuf<unsigned> barrier;

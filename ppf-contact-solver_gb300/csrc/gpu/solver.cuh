@@ -59,14 +59,6 @@ class Solver {
     unsigned vertices() const { return n_; }
     // PPF_PRECOND_* of ppf_gb300_ext.h; false for an unknown kind
     bool set_preconditioner(int kind, float param);
-    // block-Jacobi PCG recurrence: 0 the reference's (two grid reductions
-    // per iteration), 1 the single-reduction form (the default)
-    bool set_pcg_form(int form) {
-        if (form != 0 && form != 1) return false;
-        pcg_.single_reduction = form == 1;
-        return true;
-    }
-    int pcg_form() const { return pcg_.single_reduction ? 1 : 0; }
     // bf16 weight blob of the learned preconditioner (learned.cuh); false
     // when count is not the network's size
     bool set_learned_weights(const unsigned short *w, unsigned count);

@@ -87,4 +87,3 @@ def _block_jacobi_after_each_test(request):
 
     if _lib._PRODUCT is not None:
         _lib._PRODUCT.ppf_set_preconditioner(ctypes.c_int(0), ctypes.c_float(0.0))
-        _lib._PRODUCT.ppf_set_pcg_form(ctypes.c_int(1))

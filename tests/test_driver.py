@@ -8,8 +8,7 @@ values, with the step clamped below one frame as the reference does
 
 GPU: frames written by the executable are the library's own trajectory of
 the same scene (stepped through the Python session), interpolated to the
-frame times; a run resumed from a checkpoint reproduces the frames after it
-and the restored contact pattern is the saved one.
+frame times; a run resumed from a checkpoint reproduces the frames after it.
 """
 import shutil
 import subprocess
@@ -141,11 +140,16 @@ def test_driver_frames_follow_the_library_trajectory(driver, tmp_path):
         assert s.step().success()
         traj.append(s.positions().copy())
         times.append(s.time)
-    scale = float(np.abs(traj[0]).max())
+    # two runs of the library differ by the order of the atomic sums in the
+    # assembly, which the 1e-3 relative PCG residual carries into each step:
+    # frames agree to that fraction of the motion so far (the cloth falls
+    # freely over these frames)
     for k in range(9):
         got = session_io.read_frame(out, k)
         want = _interp(traj, times, k / FPS)
-        assert np.abs(got - want).max() <= 1e-4 * scale, (k, np.abs(got - want).max())
+        moved = float(np.abs(want - traj[0]).max())
+        assert np.abs(got - want).max() <= 1e-3 * moved + 1e-7, (k, np.abs(got - want).max(),
+                                                                 moved)
     # frame_to_time holds the exact frame times
     ft = np.loadtxt(out / "data" / "frame_to_time.out")
     assert np.allclose(ft[:, 1], ft[:, 0] / FPS, atol=1e-9)
@@ -164,10 +168,12 @@ def test_driver_resumes_from_a_checkpoint(driver, tmp_path):
         (resumed / f"vert_{k}.bin").unlink()
     r = _run(["--path", path, "--output", resumed, "--load", "5"])
     assert r.returncode == 0, r.stderr + r.stdout
-    scale = float(np.abs(first[6]).max())
+    start = session_io.read_frame(out, 5)
     for k in range(6, 11):
         got = session_io.read_frame(resumed, k)
-        assert np.abs(got - first[k]).max() <= 1e-4 * scale, (k, np.abs(got - first[k]).max())
+        moved = float(np.abs(first[k] - start).max())
+        assert np.abs(got - first[k]).max() <= 1e-3 * moved + 1e-7, (
+            k, np.abs(got - first[k]).max(), moved)
     # --load -1 resumes from the latest checkpoint
     r = _run(["--path", path, "--output", resumed, "--load", "-1"])
     assert r.returncode == 0, r.stderr
