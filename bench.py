@@ -55,6 +55,8 @@ WORKLOADS = {
                      "fixed spheres of seeded radii 0.02-0.1 m"),
     "sphere_field_512": ("sphere_field_512: the same drop with a 512x512 cloth (262,144 "
                          "vertices), the small case for DRAM counters"),
+    "twisted_tube": ("twisted_tube: a 256 x 512 tube (131,072 vertices), both end rings pinned "
+                     "and turned at +-2 rad/s"),
 }
 WORKLOAD = WORKLOADS["stacked_sheets"]
 L2_FLUSH_BYTES = 256 << 20
@@ -163,6 +165,8 @@ def build_scene(seed: int = 0, workload: str = "stacked_sheets"):
         return scenes.sphere_field(1024, 50, seed=seed, dt=0.01)
     if workload == "sphere_field_512":
         return scenes.sphere_field(512, 50, seed=seed, dt=0.01)
+    if workload == "twisted_tube":
+        return scenes.twisted_tube(256, 512)
     return scenes.stacked_sheets(128, 8, seed=seed, dt=0.01)
 
 

@@ -279,8 +279,16 @@ unsigned ppf_schwarz_aggregate(unsigned n, const unsigned *off, const unsigned *
  * on, so a host can time the step with its own events on that stream. NULL
  * before initialize(). */
 void *ppf_stream(void);
-/* Number of kernels this library has launched since it was loaded. */
+/* Number of kernels this library has launched since it was loaded (the
+ * kernels of a replayed CUDA graph count each time). */
 unsigned long long ppf_kernel_launches(void);
+/* Replays of the CUDA graph that holds a Newton iteration's line-search stage
+ * (the rescaled step, the swept-box refits, the contact and strain-limit line
+ * searches and the status copy): one per Newton iteration. The graph is
+ * captured at the first iteration after initialize, update_constraint or a
+ * change of the active collision windows. No counterpart in the reference
+ * (which captures its PCG iteration, solver/solver.cu:1195-1244). */
+unsigned long long ppf_graph_launches(void);
 /* Bytes copied host -> device and device -> host by the library since it was
  * loaded, counted at the copies of the per-step path: update_constraint's
  * uploads, the status and count reads inside advance(), intersection

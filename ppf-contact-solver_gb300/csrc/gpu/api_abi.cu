@@ -289,6 +289,7 @@ int ppf_set_preconditioner(int kind, float param) {
 void *ppf_stream(void) { return (void *)solver_instance().stream(); }
 
 unsigned long long ppf_kernel_launches(void) { return ppf::gpu::g_kernel_launches; }
+unsigned long long ppf_graph_launches(void) { return solver_instance().ls_replays_; }
 void ppf_transfer_bytes(unsigned long long *h2d, unsigned long long *d2h) {
     if (h2d) *h2d = ppf::gpu::g_h2d_bytes;
     if (d2h) *d2h = ppf::gpu::g_d2h_bytes;

@@ -127,6 +127,7 @@ struct IterStatus {
     float pcg_break_val;
     unsigned factor_iter;              // iterations of the factored solve
     unsigned fallback;                 // 1: it fell back to block-Jacobi
+    float rescale;                     // min(1, max_dx / |dx|_max) of the step
 };
 
 } // namespace gpu

@@ -85,11 +85,11 @@ __global__ void k_max_dx(unsigned n, const float *dx, IterStatus *st) {
 
 // target <- eval_x; eval_x -= min(1, max_dx / |dx|_max) dx (main.cu:1142-1188)
 __global__ void k_apply_dx(unsigned n, float *x, float *target, const float *dx,
-                           const IterStatus *st, float max_dx_param, float *rescale_out) {
+                           IterStatus *st, float max_dx_param) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     float mdx = __uint_as_float(st->max_dx_bits);
     float rescale = fminf(1.0f, max_dx_param / mdx);
-    if (i == 0) *rescale_out = rescale;
+    if (i == 0) st->rescale = rescale;
     if (i >= n) return;
     for (int d = 0; d < 3; ++d) {
         float v = x[3 * i + d];
@@ -553,7 +553,6 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     fixed_val_.reserve(9 * (size_t)nnz_fixed_);
     fixed_tmp_.reserve(9 * (size_t)nnz_fixed_);
     st_.reserve(1);
-    rescale_.reserve(1);
     isect_.reserve(PPF_MAX_INTERSECTION_RECORDS);
     if (!st_host_) PPF_CUDA(cudaMallocHost(&st_host_, sizeof(IterStatus)));
     // pair lists and contact-block buffers start at a size proportional to the
@@ -577,6 +576,7 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     upload_collision_mesh(ds->constraint.mesh);
     initialized_ = true;
     carried_ = false;
+    ++scene_version_;
     // initial trees and intersection check on prev and curr (main.cu:196-262)
     if (!param->disable_contact) {
         build_trees(curr_.data(), curr_.data(), 1.0f, true);
@@ -593,6 +593,7 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
 }
 
 void Solver::update_constraint(const PpfConstraint *c) {
+    ++scene_version_;
     nfix_ = c->fix.size;
     npull_ = c->pull.size;
     nsphere_ = c->sphere.size;
@@ -813,6 +814,72 @@ void Solver::assemble(float dt) {
     }
 }
 
+// The line-search stage of a Newton iteration (main.cu:1142-1354): the
+// rescaled step, the swept-box refits, contact (or analytic-collider) and
+// strain-limit line searches, and the status block's copy to pinned host
+// memory. Its launches depend only on the scene's buffers and constants, so
+// the sequence is captured once as a CUDA graph and replayed every
+// iteration; the capture is redone when the scene changes (scene_version_).
+void Solver::enqueue_line_search() {
+    const Scene s = scene();
+    const float max_t = param->line_search_max_t;
+    k_max_dx<<<div_up(n_, kB), kB, 0, q_>>>(n_, dx_.data(), st_.data());
+    PPF_LAUNCH_CHECK();
+    k_apply_dx<<<div_up(n_, kB), kB, 0, q_>>>(n_, eval_x_.data(), target_.data(), dx_.data(),
+                                               st_.data(), param->max_dx);
+    PPF_LAUNCH_CHECK();
+    k_init_ls<<<1, 1, 0, q_>>>(st_.data(), max_t, pcg_.result.data());
+    PPF_LAUNCH_CHECK();
+    LineSearchArgs la{target_.data(), eval_x_.data(), curr_.data(), st_.data(), max_t,
+                      param->ccd_eps};
+    if (!param->disable_contact) {
+        build_trees(target_.data(), eval_x_.data(), max_t, false);
+        PieceBuffers pb = pieces();
+        launch_contact_line_search(s, view(bvh_face_), view(bvh_edge_), view(bvh_vert_), la,
+                                   piece_len_, pb, q_);
+    } else {
+        launch_constraint_line_search(s, la, q_);
+    }
+    launch_strain_line_search(s, la, q_);
+    PPF_CUDA(cudaMemcpyAsync(st_host_, st_.data(), sizeof(IterStatus), cudaMemcpyDeviceToHost,
+                             q_));
+}
+
+void Solver::line_search_stage() {
+    const unsigned long long key = scene_version_ * 4ull + (param->disable_contact ? 1u : 0u) +
+                                   (use_active_ ? 2u : 0u);
+    if (!ls_graph_ || ls_key_ != key || ls_max_t_ != param->line_search_max_t ||
+        ls_max_dx_ != param->max_dx || ls_ccd_eps_ != param->ccd_eps) {
+        if (ls_graph_) {
+            PPF_CUDA(cudaGraphExecDestroy(ls_graph_));
+            ls_graph_ = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        const unsigned long long l0 = g_kernel_launches;
+        PPF_CUDA(cudaStreamBeginCapture(q_, cudaStreamCaptureModeThreadLocal));
+        try {
+            enqueue_line_search();
+        } catch (...) {
+            cudaGraph_t aborted = nullptr;
+            cudaStreamEndCapture(q_, &aborted);
+            if (aborted) cudaGraphDestroy(aborted);
+            throw;
+        }
+        PPF_CUDA(cudaStreamEndCapture(q_, &graph));
+        ls_launches_ = (unsigned)(g_kernel_launches - l0);
+        g_kernel_launches = l0;
+        PPF_CUDA(cudaGraphInstantiate(&ls_graph_, graph, 0ull));
+        PPF_CUDA(cudaGraphDestroy(graph));
+        ls_key_ = key;
+        ls_max_t_ = param->line_search_max_t;
+        ls_max_dx_ = param->max_dx;
+        ls_ccd_eps_ = param->ccd_eps;
+    }
+    PPF_CUDA(cudaGraphLaunch(ls_graph_, q_));
+    g_kernel_launches += ls_launches_;
+    ++ls_replays_;
+}
+
 PpfStepResult Solver::advance() {
     PpfStepResult result{};
     result.ccd_success = result.pcg_success = result.intersection_free = true;
@@ -878,31 +945,13 @@ PpfStepResult Solver::advance() {
             launch_pcg(A, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_);
         }
         PPF_CUDA(cudaEventRecord(ev1_, q_));
-        // rescaled Newton step, swept boxes, line search
-        k_max_dx<<<div_up(n_, kB), kB, 0, q_>>>(n_, dx_.data(), st_.data());
-        PPF_LAUNCH_CHECK();
-        k_apply_dx<<<div_up(n_, kB), kB, 0, q_>>>(n_, eval_x_.data(), target_.data(), dx_.data(),
-                                                   st_.data(), param->max_dx, rescale_.data());
-        PPF_LAUNCH_CHECK();
-        k_init_ls<<<1, 1, 0, q_>>>(st_.data(), max_t, pcg_.result.data());
-        PPF_LAUNCH_CHECK();
-        LineSearchArgs la{target_.data(), eval_x_.data(), curr_.data(), st_.data(), max_t,
-                          param->ccd_eps};
-        if (!param->disable_contact) {
-            build_trees(target_.data(), eval_x_.data(), max_t, false);
-            PieceBuffers pb = pieces();
-            launch_contact_line_search(s, view(bvh_face_), view(bvh_edge_), view(bvh_vert_), la,
-                                       piece_len_, pb, q_);
-        } else {
-            launch_constraint_line_search(s, la, q_);
-        }
-        launch_strain_line_search(s, la, q_);
-        float rescale = 1.0f;
-        PPF_CUDA(cudaMemcpyAsync(st_host_, st_.data(), sizeof(IterStatus),
-                                 cudaMemcpyDeviceToHost, q_));
-        PPF_CUDA(cudaMemcpyAsync(&rescale, rescale_.data(), sizeof(float), cudaMemcpyDeviceToHost, q_));
+        // rescaled Newton step, swept boxes, line search, status to the host:
+        // a fixed sequence of launches over this scene's buffers, replayed as
+        // one CUDA graph
+        line_search_stage();
         PPF_CUDA(cudaStreamSynchronize(q_));
-        g_d2h_bytes += sizeof(IterStatus) + sizeof(float);
+        g_d2h_bytes += sizeof(IterStatus);
+        const float rescale = st_host_->rescale;
         const IterStatus st = *st_host_;
         float pcg_ms = 0.0f;
         PPF_CUDA(cudaEventElapsedTime(&pcg_ms, ev0_, ev1_));
@@ -1128,6 +1177,7 @@ void Solver::set_active(const std::vector<unsigned char> &va) {
     upload(face_active_, fa);
     upload(edge_active_, ea);
     use_active_ = true;
+    ++scene_version_;
 }
 
 void Solver::debug_matrix(std::vector<unsigned> &f_off, std::vector<unsigned> &f_col,

@@ -92,6 +92,8 @@ class Solver {
     void compute_target(float dt);
     void assemble(float dt);
     bool check_intersection(const float *x);
+    void enqueue_line_search();
+    void line_search_stage();
     void read_status();
 
     unsigned n_ = 0, n_surf_ = 0, nf_ = 0, ne_ = 0, nh_ = 0;
@@ -180,7 +182,14 @@ class Solver {
     PieceBuffers pieces();
     DevBuf<IterStatus> st_;
     IterStatus *st_host_ = nullptr;
-    DevBuf<float> rescale_;
+    // the line-search stage captured as a CUDA graph, keyed on the scene
+    cudaGraphExec_t ls_graph_ = nullptr;
+    unsigned long long scene_version_ = 0, ls_key_ = ~0ull;
+    float ls_max_t_ = 0.0f, ls_max_dx_ = 0.0f, ls_ccd_eps_ = 0.0f;
+    unsigned ls_launches_ = 0;
+  public:
+    unsigned long long ls_replays_ = 0; // graph launches of the line-search stage
+  private:
     DevBuf<PpfIntersectionRecord> isect_;
     std::vector<PpfIntersectionRecord> isect_host_;
     unsigned isect_count_ = 0;

@@ -158,10 +158,14 @@ def test_stacked_sheets_first_contact_system(binding, product_lib):
     assert res["diag_max_err"] <= 1e-5, res
     assert st_g == 0 and st_o == 0
     assert rr_g.value < 1e-3 and rr_o < 1e-3
+    # the solutions solve the oracle's system to the tolerance: both stop at
+    # a 1e-3 recursive float32 residual, whose gap to the true (float64)
+    # residual the GPU's solution may show as much as the oracle's own
     b = so["force"].astype(np.float64).reshape(-1)
-    r_g = b - parity.apply_system(so, dx_g)
-    rel = np.abs(r_g).sum() / np.abs(b).sum()
-    assert rel < 2e-3, rel
+    rel = np.abs(b - parity.apply_system(so, dx_g)).sum() / np.abs(b).sum()
+    rel_o = np.abs(b - parity.apply_system(so, dx_o)).sum() / np.abs(b).sum()
+    print(f"true residuals: GPU {rel:.3e}, oracle {rel_o:.3e}")
+    assert rel < max(2e-3, 1.5 * rel_o), (rel, rel_o)
 
 
 def test_intersection_check_reports_a_tilted_sheet(binding, product_lib, ref_pipeline_or_none):
