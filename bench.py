@@ -57,6 +57,8 @@ WORKLOADS = {
                          "vertices), the small case for DRAM counters"),
     "twisted_tube": ("twisted_tube: a 256 x 512 tube (131,072 vertices), both end rings pinned "
                      "and turned at +-2 rad/s"),
+    "cloth_sphere": ("cloth_sphere: one 64x64 cloth (4,096 vertices) dropped from 1 m onto a "
+                     "fixed sphere of radius 0.3 m"),
 }
 WORKLOAD = WORKLOADS["stacked_sheets"]
 L2_FLUSH_BYTES = 256 << 20
@@ -167,6 +169,8 @@ def build_scene(seed: int = 0, workload: str = "stacked_sheets"):
         return scenes.sphere_field(512, 50, seed=seed, dt=0.01)
     if workload == "twisted_tube":
         return scenes.twisted_tube(256, 512)
+    if workload == "cloth_sphere":
+        return scenes.cloth_sphere(64, dt=0.01)
     return scenes.stacked_sheets(128, 8, seed=seed, dt=0.01)
 
 
@@ -293,10 +297,11 @@ def run_ours(args, rank, local_rank, world):
     pcg_ms_total = sum(pcg_ms_all)
     achieved = pcg_bytes / (pcg_ms_total / 1e3) / 1e9 if pcg_ms_total > 0 else 0.0
     traffic = None
-    tname = ("pcg_stacked_sheets_traffic.json" if args.workload == "stacked_sheets"
-             else "pcg_sphere_field_traffic.json")
+    tname = {"stacked_sheets": "pcg_stacked_sheets_traffic.json",
+             "sphere_field": "pcg_sphere_field_traffic.json",
+             "sphere_field_512": "pcg_sphere_field_traffic.json"}.get(args.workload, "")
     tfile = ROOT / "profiles" / tname
-    if tfile.exists() and pcg_iters_all:
+    if tname and tfile.is_file() and pcg_iters_all:
         # DRAM bytes per iteration from one ncu capture of this workload (the
         # sphere fields: of the 512 x 512 drop, scaled by vertices), times the
         # mean iterations per launch of this run
@@ -572,7 +577,8 @@ def main():
     ap.add_argument("--batch-count", type=int, default=256,
                     help="uneven drops of the batched-PCG comparison (0: skip)")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="stacked_sheets",
-                    help="stacked_sheets (the headline) or sphere_field (one 1M-vertex cloth)")
+                    help="stacked_sheets (the headline), sphere_field (one 1M-vertex cloth), "
+                         "twisted_tube or cloth_sphere (the 64x64 drop)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
