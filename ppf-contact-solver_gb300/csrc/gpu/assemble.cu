@@ -321,7 +321,9 @@ __global__ void k_detect_edge(Scene s, BvhView eb, const float *x, PairLists pl,
         EdgeQueryOp op{s, x, e, pl, st, 0u};
         // a lane without an exclusion box gets one that overlaps nothing
         if (!excl) xmin.w = 0.0f;
-        warp_query(eb, act, qmin, qmax, op, &st->status, &xmin, &xmax);
+        // the edge-edge test is light next to the walk: leaves are tested on
+        // the spot (warp rounds measured 2.7x slower here)
+        warp_query<LeafTests::kImmediate>(eb, act, qmin, qmax, op, &st->status, &xmin, &xmax);
         if (op.found) atomicAdd(&st->n_contact, op.found);
     }
 }

@@ -51,10 +51,46 @@ template <class T> struct HasPre {
     static constexpr bool value = sizeof(test<T>(0)) == sizeof(char);
 };
 
-template <class Op>
+//
+// Leaf tests taken in warp rounds pay off where the narrow phase is heavy and
+// diverges (the CCD sweeps). Where it is light, the rounds cost more than
+// they save: each round lasts as long as the lane whose next leaf is
+// farthest along its walk, so a warp walks up to the sum over rounds of the
+// longest step instead of the longest walk. kImmediate keeps the stackless
+// walk and tests each leaf on the spot, lane by lane.
+enum class LeafTests { kWarpRounds, kImmediate };
+
+template <LeafTests MODE = LeafTests::kWarpRounds, class Op>
 __device__ void warp_query(const BvhView &b, bool active, const float4 &qmin,
                            const float4 &qmax, Op &op, unsigned *status,
                            const float4 *xmin = nullptr, const float4 *xmax = nullptr) {
+    if constexpr (MODE == LeafTests::kImmediate) {
+        unsigned cur = (active && b.n != 0u && qmin.w != 0.0f) ? b.root : kLinkEnd;
+        const unsigned bound = 4u * b.n + 64u;
+        unsigned steps = 0;
+        while (cur != kLinkEnd) {
+            const float4 lo = b.bmin[cur], hi = b.bmax[cur];
+            const uint2 ln = b.link[cur];
+            if (++steps > bound) {
+                atomicOr(status, STATUS_BVH_STACK_OVERFLOW);
+                break;
+            }
+            if (box_overlap(lo, hi, qmin, qmax)) {
+                if (!(ln.x & kLinkLeaf)) {
+                    cur = ln.x;
+                    continue;
+                }
+                cur = ln.y;
+                const unsigned prim = ln.x & ~kLinkLeaf;
+                bool take = !xmin || !box_overlap(lo, hi, *xmin, *xmax);
+                if constexpr (HasPre<Op>::value) take = take && op.pre(prim);
+                if (take) op(prim);
+            } else {
+                cur = ln.y;
+            }
+        }
+        return;
+    }
     unsigned cur = (active && b.n != 0u && qmin.w != 0.0f) ? b.root : kLinkEnd;
     const unsigned bound = 4u * b.n + 64u;
     unsigned steps = 0;
