@@ -296,62 +296,6 @@ __device__ __forceinline__ void join_halves(Vec3 &acc, Vec3 &abssum) {
     }
 }
 
-// Ap(j) += u as one vector reduction in L2 (no return value).
-__device__ __forceinline__ void red_add4(float4 *dst, const Vec3 &u) {
-    asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst),
-                 "f"(u[0]), "f"(u[1]), "f"(u[2]), "f"(0.0f)
-                 : "memory");
-}
-
-// The upper segment of row (32 slice + r) (its diagonal block, then the
-// blocks right of it), slots of one parity, applied both ways: a block B at
-// column j adds B p_j to the row and, for j != row, B^T p_row to row j by a
-// reduction into Ap(j). p_row is the row's own value (every lane of the row
-// forms the same bits). xa and xb collect the transposed terms' share of
-// p^T A p and of its round-off scale: p_j . (B^T p_row) and
-// |p_j| . |B^T p_row|. Reads each stored block once, where the both-triangle
-// walk reads the block and its transposed copy.
-template <class G>
-__device__ __forceinline__ void sell_half_row_upper(const SellMatrix &M, unsigned slice,
-                                                    unsigned r, unsigned par, bool valid,
-                                                    unsigned row, const Vec3 &p_row,
-                                                    const G &gather, float4 *Ap, Vec3 &acc,
-                                                    Vec3 &abssum, float &xa, float &xb) {
-    const unsigned s0 = __ldg(M.slice_mid + slice), s1 = __ldg(M.slice_off + slice + 1);
-    auto term = [&](unsigned s, unsigned j) {
-        const float *a = M.val + (size_t)s * 9 * kSliceRows + r;
-        float m[9];
-#pragma unroll
-        for (int e = 0; e < 9; ++e) m[e] = __ldg(a + e * kSliceRows);
-        const Vec3 v = gather(j);
-        Vec3 t;
-        t[0] = m[0] * v[0] + m[3] * v[1] + m[6] * v[2];
-        t[1] = m[1] * v[0] + m[4] * v[1] + m[7] * v[2];
-        t[2] = m[2] * v[0] + m[5] * v[1] + m[8] * v[2];
-        acc += t;
-        abssum += t.cwise_abs();
-        if (valid && j != row) {
-            Vec3 u;
-            u[0] = m[0] * p_row[0] + m[1] * p_row[1] + m[2] * p_row[2];
-            u[1] = m[3] * p_row[0] + m[4] * p_row[1] + m[5] * p_row[2];
-            u[2] = m[6] * p_row[0] + m[7] * p_row[1] + m[8] * p_row[2];
-            red_add4(Ap + j, u);
-            xa += v.dot(u);
-            xb += fabsf(v[0]) * fabsf(u[0]) + fabsf(v[1]) * fabsf(u[1]) +
-                  fabsf(v[2]) * fabsf(u[2]);
-        }
-    };
-    unsigned s = s0 + par;
-    for (; s + 6 < s1; s += 8) {
-        unsigned j[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) j[q] = __ldg(M.col + (size_t)(s + 2 * q) * kSliceRows + r);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) term(s + 2 * q, j[q]);
-    }
-    for (; s < s1; s += 2) term(s, __ldg(M.col + (size_t)s * kSliceRows + r));
-}
-
 __device__ __forceinline__ Mat3 load_inv(const float *inv, unsigned slice, unsigned lane) {
     Mat3 P;
     const float *a = inv + (size_t)slice * 9 * kSliceRows + lane;
@@ -469,15 +413,10 @@ __device__ __forceinline__ Vec3 row_product(const PcgArgs &g, unsigned i) {
 // The epilogue gets (row, A-part, |terms|) on the lanes that own a result.
 // `vals` are the value arrays the slots are read from: the operator's own
 // (fixed, contact, overflow) or a factor's parallel ones.
-// With UPPER, the fixed part walks only the upper segment and scatters the
-// transposed products into g.Ap (sell_half_row_upper); its epilogue then gets
-// the row's own part, which it must add into g.Ap, and xa / xb get the
-// transposed terms' share of p^T A p and of its scale.
-template <int MASK, bool UPPER = false, class V, class G, class E>
+template <int MASK, class V, class G, class E>
 __device__ __forceinline__ void product_task(const PcgArgs &g, const V *const vals[3],
                                              unsigned task, unsigned lane, const G &gather,
-                                             E &&epilogue, float *xa = nullptr,
-                                             float *xb = nullptr) {
+                                             E &&epilogue) {
     const PcgOperator &A = g.A;
     // task order: overflow rows, contact half slices, fixed half slices (the
     // long and uneven items first, so the common pool at the end of the
@@ -497,14 +436,7 @@ __device__ __forceinline__ void product_task(const PcgArgs &g, const V *const va
             if (fixed) row = q < A.n ? q : 0xFFFFFFFFu;
             else row = q < A.contact.rows ? __ldg(A.contact.perm + q) : 0xFFFFFFFFu;
         }
-        if (UPPER && fixed) {
-            const bool valid = q < A.n;
-            const Vec3 p_row = valid ? gather(q) : Vec3::zero();
-            sell_half_row_upper(M, sl, r, par, valid, q, p_row, gather, g.Ap, acc, ab, *xa,
-                                *xb);
-        } else {
-            sell_half_row<MASK>(M, val, sl, r, par, row, gather, acc, ab);
-        }
+        sell_half_row<MASK>(M, val, sl, r, par, row, gather, acc, ab);
         join_halves(acc, ab);
         if (par == 0u) {
             if (fixed) {
@@ -539,33 +471,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
     __shared__ unsigned s_next;
     BlockTasks bt{&s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
                   g.task_start[gridDim.x], g.n_tasks, g.dyn_ctr, g.n_ctr};
-    // A x0 (fixed part reduced into Ap, which the launch zeroed: each upper
-    // block applied both ways; contact parts to Ap_c, overflow to Ap_ovf) ...
+    // A x0 (slice part to Ap, overflow part to Ap_ovf) ...
     bt.start();
     {
         const GatherPlain gx{g.x};
         float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
         const float *const vals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
-        float xa = 0.0f, xb = 0.0f;
         for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-            product_task<kAllSlots, true>(
-                g, vals, task, lane, gx,
-                [&](unsigned, unsigned part, unsigned slot, const Vec3 &acc, const Vec3 &) {
-                    if (part == 0u) red_add4(g.Ap + slot, acc);
-                    else st4(dst[part], slot, acc);
-                },
-                &xa, &xb);
+            product_task<kAllSlots>(g, vals, task, lane, gx,
+                         [&](unsigned, unsigned part, unsigned slot, const Vec3 &acc, const Vec3 &) {
+                             st4(dst[part], slot, acc);
+                         });
     }
     a = b = 0.0f;
     if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
-    // ... then r = b - A x0, z = P r, p_0 = 0; err0 = |r|_1, rz0 = r^T z; Ap
-    // zeroed for the first product phase
+    // ... then r = b - A x0, z = P r, p_0 = 0; err0 = |r|_1, rz0 = r^T z
     a = b = 0.0f;
     for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
         const unsigned i = sl * kSliceRows + lane;
         if (i >= A.n) continue;
         Vec3 ri = ldcg3(g.r, i) - row_product(g, i);
-        st4(g.Ap, i, Vec3::zero());
         Vec3 zi = load_inv(A.inv_diag, sl, lane) * ri;
         st3(g.r, i, ri);
         st_record(g.R, i, zi, Vec3::zero());
@@ -586,29 +511,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
         int broke = 0;
         float break_val = 0.0f;
         for (unsigned iter = 1;; ++iter) {
-            // S: A p_k with p_k = z + beta p_{k-1}; the fixed part reduced
-            // into Ap (zeroed by the previous update phase)
+            // S: A p_k with p_k = z + beta p_{k-1}
             a = b = 0.0f; // p^T A p, sum |p_i| |terms|
             const GatherCombined gp{g.R, beta};
             bt.start();
             float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
             const float *const vals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
             for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-                product_task<kAllSlots, true>(
-                    g, vals, task, lane, gp,
-                    [&](unsigned row, unsigned part, unsigned slot, const Vec3 &acc,
-                        const Vec3 &ab) {
-                        const Vec3 pi = gp(row);
-                        if (part == 0u) {
-                            st4(g.p, row, pi);
-                            red_add4(g.Ap + slot, acc);
-                        } else {
-                            st4(dst[part], slot, acc);
-                        }
-                        a += pi.dot(acc);
-                        b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] + fabsf(pi[2]) * ab[2];
-                    },
-                    &a, &b);
+                product_task<kAllSlots>(g, vals, task, lane, gp,
+                             [&](unsigned row, unsigned part, unsigned slot, const Vec3 &acc,
+                                 const Vec3 &ab) {
+                                 const Vec3 pi = gp(row);
+                                 if (part == 0u) st4(g.p, row, pi);
+                                 st4(dst[part], slot, acc);
+                                 a += pi.dot(acc);
+                                 b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] +
+                                      fabsf(pi[2]) * ab[2];
+                             });
             if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
             const float pAp = a, bound = kCurvatureSlack * kFloatEps * b;
             float alpha;
@@ -627,7 +546,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
                 const unsigned i = sl * kSliceRows + lane;
                 if (i >= A.n) continue;
                 Vec3 pi = ld4(g.p, i), api = row_product(g, i);
-                st4(g.Ap, i, Vec3::zero()); // for the next product phase
                 Vec3 xi = ldcg3(g.x, i), ri = ldcg3(g.r, i);
                 for (int k = 0; k < 3; ++k) {
                     xi[k] += alpha * pi[k];
@@ -1268,8 +1186,7 @@ __global__ void k_contact_fill(unsigned max_slices, const unsigned *off, const u
 // walks half its slots per lane; an overflow row walks its entries 32 at a
 // time. The constant covers the per-task epilogue. Task order: fixed half
 // slices, contact half slices, overflow rows.
-__global__ void k_task_cost(unsigned n_slices, const unsigned *fixed_off,
-                            const unsigned *fixed_mid, unsigned c_slices,
+__global__ void k_task_cost(unsigned n_slices, const unsigned *fixed_off, unsigned c_slices,
                             const unsigned *contact_off, unsigned n_ovf,
                             const uint2 *ovf_range, unsigned *cost) {
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1281,10 +1198,6 @@ __global__ void k_task_cost(unsigned n_slices, const unsigned *fixed_off,
     } else if (t < t2) {
         unsigned sl = (t - t1) >> 1;
         c = (contact_off[sl + 1] - contact_off[sl] + 1) / 2;
-    } else if (fixed_mid) {
-        // the upper segment only, each slot with its transposed reduction
-        unsigned sl = (t - t2) >> 1;
-        c = fixed_off[sl + 1] - fixed_mid[sl];
     } else {
         unsigned sl = (t - t2) >> 1;
         c = (fixed_off[sl + 1] - fixed_off[sl] + 1) / 2;
@@ -1481,11 +1394,7 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     ws.task_off.reserve(T + 1);
     ws.task_start.reserve(ws.grid + 1);
     ws.scan_tmp.reserve(scan_tmp_size(T + 1));
-    // the block-Jacobi kernel walks the fixed part's upper segment only
-    const bool upper = !A.schwarz.n_agg && !A.factor.diag;
-    if (upper) PPF_CUDA(cudaMemsetAsync(ws.Ap.data(), 0, (size_t)A.n * sizeof(float4), q));
     k_task_cost<<<div_up(T, 256u), 256, 0, q>>>(A.fixed.n_slices, A.fixed.slice_off,
-                                                upper ? A.fixed.slice_mid : nullptr,
                                                 A.contact.sell.n_slices, A.contact.sell.slice_off,
                                                 A.ovf.count, A.ovf.range, ws.task_cost.data());
     PPF_LAUNCH_CHECK();
