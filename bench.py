@@ -376,7 +376,8 @@ def run_ours(args, rank, local_rank, world):
 def compare_preconditioners(restart, sc, lib, stream, steps):
     """The same first `steps` time steps from t = 0 with each preconditioner:
     block-Jacobi (the reference's default and the headline's), the
-    reference's aggregate additive Schwarz (ParamSet precond = 1), the
+    reference's aggregate additive Schwarz (ParamSet precond = 1) with its
+    default two levels and with one, the
     first-order and FSAI factored preconditioners and, when the package holds
     trained weights, the learned one. Each solve runs to the same 1e-3
     relative residual. Device time per step from CUDA events on the
@@ -387,19 +388,23 @@ def compare_preconditioners(restart, sc, lib, stream, steps):
 
     from ppf_gb300 import learned
 
-    kinds = [("block_jacobi", 0, abi.PRECOND_BLOCK_JACOBI),
-             ("schwarz", 1, abi.PRECOND_BLOCK_JACOBI),
-             ("first_order_factor", 0, abi.PRECOND_FIRST_ORDER),
-             ("fsai", 0, abi.PRECOND_FSAI)]
+    # (name, ParamSet precond, extension kind, ParamSet schwarz_levels)
+    kinds = [("block_jacobi", 0, abi.PRECOND_BLOCK_JACOBI, 2),
+             ("schwarz_two_level", 1, abi.PRECOND_BLOCK_JACOBI, 2),
+             ("schwarz_one_level", 1, abi.PRECOND_BLOCK_JACOBI, 1),
+             ("first_order_factor", 0, abi.PRECOND_FIRST_ORDER, 2),
+             ("fsai", 0, abi.PRECOND_FSAI, 2)]
     out = {"steps": steps, "from": "t = 0", "tolerance": "1e-3 relative L1 residual"}
     if learned.WEIGHTS_FILE.exists():
         learned.use_weights()
-        kinds.append(("learned", 0, abi.PRECOND_LEARNED))
+        kinds.append(("learned", 0, abi.PRECOND_LEARNED, 2))
         out["learned_weights"] = learned.WEIGHTS_FILE.name
-    for name, precond, kind in kinds:
+    for name, precond, kind, levels in kinds:
         sc.param.contents.precond = precond
+        sc.param.contents.schwarz_levels = levels
         s = restart()
         sc.param.contents.precond = precond
+        sc.param.contents.schwarz_levels = levels
         s.set_preconditioner(kind, 0.5)
         ev = []
         newton, fallbacks, ms, iters = 0, 0, [], []
@@ -423,6 +428,7 @@ def compare_preconditioners(restart, sc, lib, stream, steps):
         finally:
             s.set_preconditioner(abi.PRECOND_BLOCK_JACOBI)
             sc.param.contents.precond = 0
+            sc.param.contents.schwarz_levels = 2
         total = sum(a.elapsed_time(b) for a, b in ev)
         ms.sort()
         it = sorted(iters)

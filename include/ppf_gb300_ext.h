@@ -274,6 +274,17 @@ int ppf_batch_autotune(unsigned n_sys, const unsigned *row_off, const unsigned *
  * returns the number of aggregates. */
 unsigned ppf_schwarz_aggregate(unsigned n, const unsigned *off, const unsigned *col,
                                const float *wgt, unsigned kmax, unsigned *agg);
+/* The Schwarz coarse level on the host (the reference's two-level form,
+ * schwarz/schwarz.cu:1225-1327 and 1416-1470): for the same CSR with the 9
+ * values of every block (column-major, 9 floats per entry) and the
+ * aggregation agg (n entries, n_agg aggregates), the Galerkin blocks of
+ * distinct aggregate pairs summed in float32 (rows in order, each row's
+ * entries in order), grouped by the aggregation above with their Frobenius
+ * norms as weights. Writes the domain of each aggregate to dom (n_agg) and
+ * returns the number of domains. */
+unsigned ppf_schwarz_coarsen(unsigned n, const unsigned *off, const unsigned *col,
+                             const float *blocks, const unsigned *agg, unsigned n_agg,
+                             unsigned kmax, unsigned *dom);
 
 /* The CUDA stream (cudaStream_t, as void*) every kernel of advance() runs
  * on, so a host can time the step with its own events on that stream. NULL
@@ -310,15 +321,26 @@ void ppf_debug_system_sizes(unsigned *sizes);
  * columns, values), the per-vertex diagonal (9n), the right-hand side (3n)
  * and the pair lists (pf: 2 u32, pe / pp: 3 u32 with the multiplicity and the
  * friction flag in bit 31, ee: 2 u32 per pair). Any pointer may be NULL. */
+void ppf_debug_system(unsigned *f_off, unsigned *f_col, float *f_val,
+                      unsigned *d_off, unsigned *d_col, float *d_val,
+                      float *diag, float *force, unsigned *pf, unsigned *pe,
+                      unsigned *pp, unsigned *ee);
 /* The vertex masses (n floats) and Dirichlet mask (n u32, nonzero = pinned)
  * of the initialized scene, and the diagonal blocks G(i,i) (9n floats,
  * column-major) of the last factor a factored preconditioner built. */
 void ppf_debug_vertex_info(float *mass, unsigned *dof_mask);
 void ppf_debug_factor_diag(float *out);
-void ppf_debug_system(unsigned *f_off, unsigned *f_col, float *f_val,
-                      unsigned *d_off, unsigned *d_col, float *d_val,
-                      float *diag, float *force, unsigned *pf, unsigned *pe,
-                      unsigned *pp, unsigned *ee);
+/* Solves the operator of the last ppf_debug_newton_system, with the same
+ * preconditioner, for the right-hand side b (3n floats) from x = 0 with at
+ * most max_iter iterations; writes x (3n floats). With max_iter = 1,
+ * x = alpha P b: the direction of the preconditioner's first output.
+ * Returns the PCG state. */
+int ppf_debug_pcg(const float *b, float *x, unsigned max_iter, unsigned *iters, float *resid);
+/* The Schwarz layout of the last solve: sizes[3] = {aggregates, coarse
+ * domains, levels} (zeros when no Schwarz solve ran), the aggregate of each
+ * vertex (n) and the domain of each aggregate (sizes[0], written when there
+ * are domains). Either array may be NULL. */
+void ppf_debug_schwarz_layout(unsigned *sizes, unsigned *agg, unsigned *dom);
 
 #ifdef __cplusplus
 }

@@ -282,6 +282,15 @@ unsigned ppf_schwarz_aggregate(unsigned n, const unsigned *off, const unsigned *
     return n_agg;
 }
 
+unsigned ppf_schwarz_coarsen(unsigned n, const unsigned *off, const unsigned *col,
+                             const float *blocks, const unsigned *agg, unsigned n_agg,
+                             unsigned kmax, unsigned *dom) {
+    std::vector<unsigned> o(off, off + n + 1), c(col, col + off[n]), a(agg, agg + n), d;
+    const unsigned n_dom = ppf::gpu::schwarz_coarsen(n, o, c, blocks, a, n_agg, kmax, d);
+    std::copy(d.begin(), d.end(), dom);
+    return n_dom;
+}
+
 int ppf_set_preconditioner(int kind, float param) {
     return solver_instance().set_preconditioner(kind, param) ? 0 : -1;
 }
@@ -346,6 +355,29 @@ void ppf_debug_vertex_info(float *mass, unsigned *dof_mask) {
         solver_instance().debug_vertex_info(m, d);
         if (mass) std::memcpy(mass, m.data(), m.size() * sizeof(float));
         if (dof_mask) std::memcpy(dof_mask, d.data(), d.size() * sizeof(unsigned));
+    } catch (const FatalError &e) {
+        fatal(e);
+    }
+}
+
+int ppf_debug_pcg(const float *b, float *x, unsigned max_iter, unsigned *iters, float *resid) {
+    try {
+        std::vector<float> v;
+        const int state = solver_instance().debug_pcg(b, v, max_iter, *iters, *resid);
+        std::memcpy(x, v.data(), v.size() * sizeof(float));
+        return state;
+    } catch (const FatalError &e) {
+        fatal(e);
+        return -1;
+    }
+}
+
+void ppf_debug_schwarz_layout(unsigned *sizes, unsigned *agg, unsigned *dom) {
+    try {
+        std::vector<unsigned> a, d;
+        solver_instance().debug_schwarz(sizes, a, d);
+        if (agg && !a.empty()) std::memcpy(agg, a.data(), a.size() * 4);
+        if (dom && !d.empty()) std::memcpy(dom, d.data(), d.size() * 4);
     } catch (const FatalError &e) {
         fatal(e);
     }

@@ -315,7 +315,7 @@ struct PcgArgs {
     float *R;            // 8 floats per vertex: {z, p} records
     float4 *p, *Ap, *Ap_c, *Ap_ovf;
     float4 *Y;   // G r of the factored preconditioner
-    float *part; // 2 buffers of 2 floats per block
+    float *part; // 2 buffers of 2 floats per block, then 1 float per block
     unsigned *bar;
     float tol;
     unsigned max_iter;
@@ -827,7 +827,8 @@ constexpr unsigned kSchwarzWarpFloats = 4 * kSchwarzDim + kSchwarzTri;
 
 // One Schwarz aggregate, by one warp: the update of its member rows
 // (`init`: r = r - A x0 and p = 0; otherwise x += alpha p, r -= alpha A p),
-// then z = G^T (G r) on the aggregate, and the members' {z, p} records.
+// with the coarse level the aggregate's residual sum rc, then
+// z = G^T (G r) on the aggregate, and the members' {z, p} records.
 // Adds r^T z to `a` and |r|_1 to `b`. `seg` is the warp's shared region
 // (kSchwarzWarpFloats, 16-byte aligned); the packed factor is staged there
 // with 16-byte loads and both triangular products read it from there.
@@ -862,6 +863,15 @@ __device__ __forceinline__ void schwarz_segment(const PcgArgs &g, unsigned ag, u
         }
         b += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
     }
+    __syncwarp();
+    if (S.n_dom && lane < 3u) { // C r: the aggregate's residual sum, members in order
+        float sum = 0.0f;
+        for (unsigned k = 0; k < m; ++k) sum += sr[3 * k + lane];
+        sy[lane] = sum;
+    }
+    __syncwarp();
+    if (S.n_dom && lane == 0) S.rc[ag] = make_float4(sy[0], sy[1], sy[2], 0.0f);
+    __syncwarp();
     {
         const float4 *G4 = reinterpret_cast<const float4 *>(S.ainv + __ldg(S.ainv_off + ag));
         float4 *s4 = reinterpret_cast<float4 *>(sG);
@@ -892,9 +902,72 @@ __device__ __forceinline__ void schwarz_segment(const PcgArgs &g, unsigned ag, u
     __syncwarp();
 }
 
+// One coarse domain, by one warp: rc of its nodes (written by the fine
+// phase), e = G1^T (G1 rc) with the domain's staged packed factor, then
+// z_i += w e(node of i) in the records of every member vertex of every node
+// (each vertex is reached by exactly one warp). Adds w rc . e, the coarse
+// part of r^T z, to `a`.
+__device__ __forceinline__ void schwarz_coarse(const PcgArgs &g, unsigned dm, unsigned lane,
+                                               float *seg, float &a) {
+    const SchwarzView &S = g.A.schwarz;
+    constexpr unsigned D = kSchwarzDim;
+    float *sr = seg, *sy = seg + D, *sz = seg + 2 * D;
+    float *sG = seg + 4 * D;
+    const unsigned base = __ldg(S.dom_off + dm), m = __ldg(S.dom_off + dm + 1) - base;
+    const unsigned d = 3u * m;
+    for (unsigned k = lane; k < m; k += 32u) {
+        const float4 v = __ldcg(S.rc + __ldg(S.dom_members + base + k));
+        sr[3 * k] = v.x;
+        sr[3 * k + 1] = v.y;
+        sr[3 * k + 2] = v.z;
+    }
+    {
+        const float4 *G4 = reinterpret_cast<const float4 *>(S.ainv1 + __ldg(S.ainv1_off + dm));
+        float4 *s4 = reinterpret_cast<float4 *>(sG);
+        const unsigned n4 = (d * (d + 1u) / 2u + 3u) / 4u;
+        for (unsigned e = lane; e < n4; e += 32u) s4[e] = __ldg(G4 + e);
+    }
+    __syncwarp();
+    for (unsigned p = lane; p < d; p += 32u) { // y = G1 rc
+        const float *row = sG + p * (p + 1u) / 2u;
+        float acc = 0.0f;
+        for (unsigned q = 0; q <= p; ++q) acc += row[q] * sr[q];
+        sy[p] = acc;
+    }
+    __syncwarp();
+    for (unsigned p = lane; p < d; p += 32u) { // e = G1^T y, weighted
+        float acc = 0.0f;
+        for (unsigned q = p; q < d; ++q) acc += sG[q * (q + 1u) / 2u + p] * sy[q];
+        sz[p] = S.weight * acc;
+        a += sr[p] * sz[p];
+    }
+    __syncwarp();
+    // prolongation: two nodes per pass, 16 lanes over each node's members
+    const unsigned half = lane >> 4, t = lane & 15u;
+    for (unsigned k0 = 0; k0 < m; k0 += 2u) {
+        const unsigned k = k0 + half;
+        if (k < m) {
+            const unsigned node = __ldg(S.dom_members + base + k);
+            const unsigned mb = __ldg(S.agg_off + node), mm = __ldg(S.agg_off + node + 1) - mb;
+            for (unsigned u = t; u < mm; u += 16u) {
+                float4 *rec = reinterpret_cast<float4 *>(g.R + 8 * (size_t)__ldg(S.members + mb + u));
+                float4 v = __ldcg(rec);
+                v.x += sz[3 * k];
+                v.y += sz[3 * k + 1];
+                v.z += sz[3 * k + 2];
+                *rec = v;
+            }
+        }
+    }
+    __syncwarp();
+}
+
 // PCG with the aggregate-Schwarz preconditioner: the recurrence, verdicts and
 // checks of k_pcg, with the update phase walking aggregates instead of
-// slices. A non-positive (or non-finite) r^T z ends the solve as failed with
+// slices. With the coarse level, the update phase also restricts r into rc,
+// and after its reduction a coarse phase (one warp per domain) adds the
+// coarse correction to z and its part of r^T z, reduced by a third grid
+// barrier. A non-positive (or non-finite) r^T z ends the solve as failed with
 // break cause 2, the reference's cue to solve again with block-Jacobi
 // (solver/solver.cu:1627-1676).
 __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
@@ -903,9 +976,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
     const unsigned lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
     const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
-    const unsigned n_agg = A.schwarz.n_agg;
+    const unsigned n_agg = A.schwarz.n_agg, n_dom = A.schwarz.n_dom;
     unsigned *abort = g.bar + 2;
-    float *part0 = g.part, *part1 = g.part + 2 * nb;
+    float *part0 = g.part, *part1 = g.part + 2 * nb, *part2 = g.part + 4 * nb;
     float a, b;
     extern __shared__ float4 s_dyn4[];
     float *seg = reinterpret_cast<float *>(s_dyn4) + (size_t)wib * kSchwarzWarpFloats;
@@ -930,6 +1003,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
     for (unsigned ag = warp; ag < n_agg; ag += nwarps)
         schwarz_segment(g, ag, lane, true, 0.0f, seg, a, b);
     if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+    if (n_dom) { // coarse correction, then its part of r^T z
+        float c[1] = {0.0f};
+        for (unsigned dm = warp; dm < n_dom; dm += nwarps) schwarz_coarse(g, dm, lane, seg, c[0]);
+        if (!grid_sum<1>(c, part2, g.bar, nb, abort)) goto aborted;
+        a += c[0];
+    }
     {
         const float err0 = b;
         float rz0 = a;
@@ -981,6 +1060,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
             for (unsigned ag = warp; ag < n_agg; ag += nwarps)
                 schwarz_segment(g, ag, lane, false, alpha, seg, a, b);
             if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+            if (n_dom) {
+                float c[1] = {0.0f};
+                for (unsigned dm = warp; dm < n_dom; dm += nwarps)
+                    schwarz_coarse(g, dm, lane, seg, c[0]);
+                if (!grid_sum<1>(c, part2, g.bar, nb, abort)) goto aborted;
+                a += c[0];
+            }
             const float rz_new = a, err_now = b;
             const bool rz_bad = !(rz_new > 0.0f);
             beta = rz_new / rz0;
@@ -1240,7 +1326,7 @@ void PcgWorkspace::reserve(unsigned n) {
         grid = (unsigned)(sms * per_sm);
         threads = kThreads;
     }
-    partials.reserve(4 * (size_t)grid + 4);
+    partials.reserve(6 * (size_t)grid + 4);
     barrier.reserve(4);
     result.reserve(1);
 }

@@ -89,10 +89,20 @@ constexpr unsigned kSchwarzMaxMembers = 16; // vertices per Schwarz aggregate
 // Aggregate additive-Schwarz preconditioner (schwarz.cuh); n_agg == 0 when
 // unused. Aggregate g holds members[agg_off[g] .. agg_off[g+1]) and its
 // factor G = L^{-1} packed row-major lower-triangular at ainv + ainv_off[g].
+// With the coarse level (n_dom > 0) the aggregates are the coarse nodes:
+// domain D holds the nodes dom_members[dom_off[D] .. dom_off[D+1]) and the
+// packed factor of its Galerkin block at ainv1 + ainv1_off[D]; rc holds the
+// restricted residual, one float4 per aggregate; weight damps the coarse
+// correction.
 struct SchwarzView {
     unsigned n_agg;
     const unsigned *agg_off, *members, *ainv_off;
     const float *ainv;
+    unsigned n_dom;
+    const unsigned *dom_off, *dom_members, *ainv1_off;
+    const float *ainv1;
+    float4 *rc;
+    float weight;
 };
 
 // A = fixed part (elastic + inertia + per-vertex terms, diagonal included)

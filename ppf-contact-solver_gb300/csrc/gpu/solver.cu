@@ -809,7 +809,12 @@ void Solver::assemble(float dt) {
     if (schwarz_active_) {
         PcgOperator A{n_, sell_view(fixed_sell_), contact_view(dyn_layout_),
                       overflow_view(dyn_layout_), inv_diag_.data(), PcgFactor{}, SchwarzView{}};
-        if (!schwarz_.ready || schwarz_.n != n_) schwarz_setup(A, schwarz_, q_);
+        // levels as the reference reads ParamSet::schwarz_levels (0: unset,
+        // 2), built up to kSchwarzMaxLevels (schwarz.cu:1650-1666)
+        unsigned levels = param->schwarz_levels ? param->schwarz_levels : 2u;
+        levels = std::min(levels, kSchwarzMaxLevels);
+        if (!schwarz_.ready || schwarz_.n != n_ || schwarz_.levels_req != levels)
+            schwarz_setup(A, schwarz_, levels, q_);
         launch_schwarz_factor(A, schwarz_, &st_.data()->status, q_);
     }
 }
@@ -1262,6 +1267,37 @@ int Solver::debug_assemble_solve(std::vector<float> &dx, unsigned &iters, float 
     iters = res.iter;
     resid = res.resid;
     return res.state;
+}
+
+int Solver::debug_pcg(const float *b, std::vector<float> &x, unsigned max_iter, unsigned &iters,
+                      float &resid) {
+    const size_t n3 = 3 * (size_t)n_;
+    PPF_CUDA(cudaMemcpyAsync(r_.data(), b, n3 * sizeof(float), cudaMemcpyHostToDevice, q_));
+    PPF_CUDA(cudaMemsetAsync(dx_.data(), 0, n3 * sizeof(float), q_));
+    PcgOperator A = pcg_operator();
+    launch_pcg(A, dx_.data(), r_.data(), param->cg_tol, max_iter, pcg_, q_);
+    PcgResult res;
+    PPF_CUDA(cudaMemcpyAsync(&res, pcg_.result.data(), sizeof(PcgResult), cudaMemcpyDeviceToHost, q_));
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    x.resize(n3);
+    PPF_CUDA(cudaMemcpy(x.data(), dx_.data(), n3 * sizeof(float), cudaMemcpyDeviceToHost));
+    iters = res.iter;
+    resid = res.resid;
+    return res.state;
+}
+
+void Solver::debug_schwarz(unsigned *sizes, std::vector<unsigned> &agg,
+                           std::vector<unsigned> &dom) {
+    const SchwarzLayout &S = schwarz_;
+    sizes[0] = S.ready ? S.n_agg : 0u;
+    sizes[1] = S.ready ? S.n_dom : 0u;
+    sizes[2] = S.ready ? S.levels : 0u;
+    agg.assign(S.ready ? S.n : 0u, 0u);
+    dom.assign(sizes[1] ? S.n_agg : 0u, 0u);
+    if (!agg.empty())
+        PPF_CUDA(cudaMemcpy(agg.data(), S.agg.data(), agg.size() * 4, cudaMemcpyDeviceToHost));
+    if (!dom.empty())
+        PPF_CUDA(cudaMemcpy(dom.data(), S.dom.data(), dom.size() * 4, cudaMemcpyDeviceToHost));
 }
 
 void Solver::release() {

@@ -76,6 +76,13 @@ class Solver {
                      std::vector<unsigned> &pp, std::vector<unsigned> &ee);
     // one assembly + solve at the current positions, without line search
     int debug_assemble_solve(std::vector<float> &dx, unsigned &iters, float &resid);
+    // Solves the operator (and preconditioner) of the last debug_assemble_solve
+    // with right-hand side b from x = 0, at most max_iter iterations.
+    int debug_pcg(const float *b, std::vector<float> &x, unsigned max_iter, unsigned &iters,
+                  float &resid);
+    // The Schwarz layout of the last solve: sizes {n_agg, n_dom, levels},
+    // the aggregate of each vertex and the domain of each aggregate.
+    void debug_schwarz(unsigned *sizes, std::vector<unsigned> &agg, std::vector<unsigned> &dom);
     void release();
 
     PpfDataSet *host = nullptr;

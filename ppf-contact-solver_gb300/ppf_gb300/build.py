@@ -37,10 +37,11 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 # -fmad=false: every single-precision operation rounds on its own, so the
 # kernels compute the same bits as the CPU oracle built with
 # -ffp-contract=off. Where the reference's contraction is part of the
-# arithmetic (the swept leaf box), the kernels call fmaf explicitly.
+# arithmetic (the swept leaf box), the kernels call fmaf explicitly. Host
+# code of the CUDA sources is not contracted either.
 NVCC_FLAGS = [
     "-std=c++17", "-O3", "-lineinfo", GENCODE, "-fmad=false",
-    "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+    "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
     "-Xptxas", "-warn-spills",
 ]
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off"]

@@ -13,11 +13,12 @@ from ppf_gb300 import meshes, scenes
 from ppf_gb300.session import Scene
 
 
-def two_sheets(side: int = 12, gap: float = 6e-4, seed: int = 3):
+def two_sheets(side: int = 12, gap: float = 6e-4, seed: int = 3, pinned: bool = True):
     """Two sheets inside each other's contact gap at t = 0, the upper one
-    rotated and moving, the lower one pinned at two corners, over a floor
-    within reach: point-face, point-edge, point-point, edge-edge pairs, a
-    floor constraint and Dirichlet rows in the first Newton system."""
+    rotated and moving, the lower one pinned at two corners (unless not
+    `pinned`), over a floor within reach: point-face, point-edge, point-point,
+    edge-edge pairs, a floor constraint and Dirichlet rows in the first Newton
+    system."""
     rng = np.random.default_rng(seed)
     mat = scenes.cloth_material()
     sc = Scene()
@@ -43,7 +44,8 @@ def two_sheets(side: int = 12, gap: float = 6e-4, seed: int = 3):
     vel = np.zeros((n, 3), np.float32)
     vel[b0:b0 + len(vb)] = (0.2, -0.3, 0.1)
     sc.set_velocity(vel)
-    sc.pin([a0, a0 + side - 1])
+    if pinned:
+        sc.pin([a0, a0 + side - 1])
     sc.add_floor((0.0, 0.5 - 8e-4, 0.0), contact_gap=1e-3, friction=0.5)
     return sc.build(scenes._param(0.01)), None
 

@@ -4,10 +4,16 @@ CPU: the product's aggregation equals the oracle's restatement of the
 reference's heavy-edge aggregation on seeded graphs, with every aggregate at
 most kmax vertices and connected in the graph.
 
+CPU: the coarse level's domains (Galerkin blocks of the aggregates grouped
+by the same growth on their norms) equal the restatement's.
+
 GPU: a Schwarz-preconditioned solve solves the oracle's Newton system to the
 same relative residual as block-Jacobi in fewer iterations; a trajectory run
 with it keeps the invariants; one step from an identical state agrees with
-the oracle's block-Jacobi step within 1e-5 relative.
+the oracle's block-Jacobi step within 1e-5 relative. On a contact system the
+PCG's aggregation and coarse domains equal the restatement's bit for bit,
+its first iteration is alpha P b for the restated one- and two-level
+operators, and both forms solve the system to the tolerance.
 """
 import ctypes as C
 
@@ -161,3 +167,191 @@ def test_schwarz_step_matches_oracle(binding):
     xg, xo = s.positions(), o.positions()[0]
     err = np.abs(xg - xo).max()
     assert err <= 1e-5 * np.abs(xo).max(), err
+
+
+def _block_graph(rng, side, extra):
+    """The grid graph of _graph with a seeded 3 x 3 block per entry,
+    block(j, i) = block(i, j)^T (column-major, 9 floats per entry)."""
+    off, col, _ = _graph(rng, side, extra)
+    n = len(off) - 1
+    upper = {}
+    blocks = np.zeros((len(col), 9), np.float32)
+    for i in range(n):
+        for k in range(off[i], off[i + 1]):
+            j = int(col[k])
+            key = (min(i, j), max(i, j))
+            if key not in upper:
+                upper[key] = rng.uniform(-1.0, 1.0, (3, 3)).astype(np.float32)
+            B = upper[key] if i <= j else upper[key].T
+            blocks[k] = B.T.reshape(9)  # column-major
+    wgt = np.array([np.float32(np.sqrt(np.float32(np.sum(b * b)))) for b in blocks], np.float32)
+    return off, col, blocks, wgt
+
+
+@pytest.mark.parametrize("seed,side,extra,kmax", [(0, 16, 0, 4), (1, 21, 60, 6), (2, 12, 150, 3)])
+def test_coarse_domains_match_restatement(product_lib, seed, side, extra, kmax):
+    """The coarse level (Galerkin blocks of the aggregates, grouped by the
+    same heavy-edge growth on their norms) equals the restatement."""
+    from oracle.schwarz import galerkin_domains, hem_aggregate
+
+    off, col, blocks, wgt = _block_graph(np.random.default_rng(seed), side, extra)
+    n = len(off) - 1
+    agg, n_agg = hem_aggregate(off, col, wgt, kmax)
+    lib = product_lib
+    lib.ppf_schwarz_coarsen.restype = C.c_uint
+    lib.ppf_schwarz_coarsen.argtypes = [C.c_uint, u32p, u32p, f32p, u32p, C.c_uint, C.c_uint,
+                                        u32p]
+    dom = np.zeros(n_agg, np.uint32)
+    n_dom = lib.ppf_schwarz_coarsen(n, off, col, blocks.reshape(-1), agg, n_agg, kmax, dom)
+    ref, n_ref = galerkin_domains(off, col, blocks, agg, n_agg, kmax)
+    assert n_dom == n_ref and 1 <= n_dom < n_agg
+    assert np.array_equal(dom, ref)
+    assert np.bincount(dom, minlength=n_dom).max() <= kmax
+
+
+def _operator_rows(sysm):
+    """Every off-diagonal block of each row of the product's kept system, as
+    the PCG's slice layout holds it (the upper blocks and, below the
+    diagonal, their transposes), sorted by column: CSR offsets, columns,
+    column-major blocks and Frobenius norms in float32."""
+    n = len(sysm["f_off"]) - 1
+    rows = [[] for _ in range(n)]
+    for off, col, val in ((sysm["f_off"], sysm["f_col"], sysm["f_val"]),
+                          (sysm["d_off"], sysm["d_col"], sysm["d_val"])):
+        for i in range(n):
+            for k in range(off[i], off[i + 1]):
+                j = int(col[k])
+                if j == i:
+                    continue
+                v = np.asarray(val[k], np.float32)
+                rows[i].append((j, v))
+                rows[j].append((i, v.reshape(3, 3).T.reshape(9)))
+    r_off, r_col, r_blk = [0], [], []
+    for i in range(n):
+        cols = [j for j, _ in rows[i]]
+        assert len(cols) == len(set(cols)), i  # fixed and contact patterns are disjoint
+        for j, v in sorted(rows[i], key=lambda e: e[0]):
+            r_col.append(j)
+            r_blk.append(v)
+        r_off.append(len(r_col))
+    blk = np.array(r_blk, np.float32).reshape(-1, 9)
+    wgt = np.zeros(len(blk), np.float32)
+    for k, b in enumerate(blk):
+        w = np.float32(0.0)
+        for q in range(9):
+            w = np.float32(w + np.float32(b[q] * b[q]))
+        wgt[k] = np.sqrt(w)
+    return np.array(r_off, np.uint32), np.array(r_col, np.uint32), blk, wgt
+
+
+def _full_operator(sysm):
+    """The kept system as a both-triangle float64 scipy matrix (3n x 3n)."""
+    import scipy.sparse as sp
+
+    n = len(sysm["f_off"]) - 1
+    R, Cc, V = [], [], []
+    for off, col, val in ((sysm["f_off"], sysm["f_col"], sysm["f_val"]),
+                          (sysm["d_off"], sysm["d_col"], sysm["d_val"])):
+        rows = np.repeat(np.arange(n), np.diff(off.astype(np.int64)))
+        cols = col.astype(np.int64)
+        B = val.astype(np.float64).reshape(-1, 3, 3).transpose(0, 2, 1)  # row-major
+        for a in range(3):
+            for b in range(3):
+                R.append(3 * rows + a)
+                Cc.append(3 * cols + b)
+                V.append(B[:, a, b])
+                low = rows != cols
+                R.append(3 * cols[low] + b)
+                Cc.append(3 * rows[low] + a)
+                V.append(B[low, a, b])
+    return sp.csr_matrix((np.concatenate(V), (np.concatenate(R), np.concatenate(Cc))),
+                         shape=(3 * n, 3 * n))
+
+
+def _schwarz_system(lib, levels, side=16):
+    """The first Newton system of the unpinned two-sheet scene, solved with
+    the Schwarz preconditioner at `levels`; returns (scene size, kept system,
+    layout sizes, aggregate per vertex, domain per aggregate)."""
+    from oracle.binding import product_system
+
+    sc, _ = step_scenes.two_sheets(side=side, pinned=False)
+    n = sc.vertex_count
+    sc.param.contents.precond = 1
+    sc.param.contents.schwarz_levels = levels
+    try:
+        Session(sc)
+        st, _, _, _ = _debug_solve(lib, n)
+    finally:
+        sc.param.contents.precond = 0
+        sc.param.contents.schwarz_levels = 2
+    assert st == 0
+    sysm = product_system(lib, n)
+    lib.ppf_debug_schwarz_layout.argtypes = [u32p, u32p, u32p]
+    sizes = np.zeros(3, np.uint32)
+    agg = np.zeros(n, np.uint32)
+    dom = np.zeros(n, np.uint32)  # n_agg <= n
+    lib.ppf_debug_schwarz_layout(sizes, agg, dom)
+    return n, sysm, sizes, agg, dom[:sizes[0]]
+
+
+def _debug_pcg(lib, b, max_iter):
+    lib.ppf_debug_pcg.argtypes = [f32p, f32p, C.c_uint, C.POINTER(C.c_uint),
+                                  C.POINTER(C.c_float)]
+    x = np.zeros_like(b)
+    it, rr = C.c_uint(), C.c_float()
+    st = lib.ppf_debug_pcg(b, x, max_iter, C.byref(it), C.byref(rr))
+    return st, x, it.value, rr.value
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("levels", [1, 2])
+def test_schwarz_layout_and_first_direction_match_restatement(product_lib, levels):
+    """On a contact system: the aggregation and (two levels) the coarse
+    domains equal the restatement's on the operator the PCG holds, bit for
+    bit; one PCG iteration from x = 0 gives x = alpha P b with P the
+    restated one- or two-level Schwarz operator applied in float64."""
+    from oracle.schwarz import galerkin_domains, hem_aggregate, schwarz_apply
+
+    lib = product_lib
+    n, sysm, sizes, agg, dom = _schwarz_system(lib, levels)
+    assert sysm["d_col"].size > 0  # contact blocks in the system
+    off, col, blk, wgt = _operator_rows(sysm)
+    ref_agg, n_agg = hem_aggregate(off, col, wgt, 16)
+    assert sizes[0] == n_agg and np.array_equal(agg, ref_agg)
+    assert sizes[2] == levels
+    if levels == 2:
+        ref_dom, n_dom = galerkin_domains(off, col, blk, agg, n_agg, 16)
+        assert sizes[1] == n_dom and n_dom > 1
+        assert np.array_equal(dom, ref_dom)
+    else:
+        assert sizes[1] == 0
+    A = _full_operator(sysm)
+    rng = np.random.default_rng(11)
+    b = rng.standard_normal(3 * n).astype(np.float32)
+    st, x, it, _ = _debug_pcg(lib, b, 1)
+    assert it == 1
+    z = schwarz_apply(A, agg, b, dom if levels == 2 else None)
+    alpha = float(b.astype(np.float64) @ z) / float(z @ (A @ z))
+    want = alpha * z
+    err = np.abs(x - want).max() / np.abs(want).max()
+    print(f"levels {levels}: first direction error {err:.2e}")
+    assert err < 1e-3, err
+
+
+@pytest.mark.gpu
+def test_two_level_solve_reaches_tolerance(product_lib):
+    """Solved to the 1e-3 relative L1 residual with one and with two levels
+    on the same contact system: both solutions solve the system in float64
+    to that tolerance (with float32 slack)."""
+    lib = product_lib
+    iters = {}
+    for levels in (1, 2):
+        n, sysm, _, _, _ = _schwarz_system(lib, levels)
+        A = _full_operator(sysm)
+        b = sysm["force"].reshape(-1).astype(np.float32)
+        st, x, it, rr = _debug_pcg(lib, b, 10000)
+        assert st == 0, (levels, st, rr)
+        res = np.abs(b - A @ x.astype(np.float64)).sum() / np.abs(b).sum()
+        assert res < 2e-3, (levels, res)
+        iters[levels] = it
+    print("PCG iterations by Schwarz levels:", iters)
