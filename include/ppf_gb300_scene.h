@@ -7,9 +7,9 @@
  * build() and make_param(), crates/ppf-cts-solver/src/scene.rs make_props(),
  * crates/ppf-cts-solver/src/mesh.rs Mesh::new, and the face-edge props of
  * crates/ppf-cts-solver/src/main.rs:205-250). Covered: shells (any model
- * field, Baraff-Witkin evaluated), fix pins (static or kinematic), pull pins,
- * analytic spheres and floors. Not covered: rods, tets, stitches, collision
- * meshes, PDRD bodies, sand grains, UV anisotropy.
+ * field, Baraff-Witkin evaluated), rods, fix pins (static or kinematic), pull
+ * pins, analytic spheres and floors, static collision meshes. Not covered:
+ * tets, stitches, PDRD bodies, sand grains, UV anisotropy.
  *
  * Edge and hinge order: the reference extracts them from a hash map, whose
  * iteration order is not reproducible; here they are listed in first-seen
@@ -42,6 +42,22 @@ typedef struct {
     float friction;
 } PpfShellMaterial;
 
+/* Per-object rod material (the reference scene's rod-* parameters,
+ * scene.rs:1540-1660). */
+typedef struct {
+    float density;        /* kg/m: edge mass = density x rest length */
+    float young_mod;      /* stretch stiffness, scaled by the edge mass */
+    float bend;           /* bending stiffness (0: none) */
+    float length_factor;  /* rest length = factor x initial length */
+    float strain_limit;   /* 0 disables */
+    float contact_gap;    /* ghat */
+    float contact_offset;
+    float friction;
+    float deform_damping; /* Rayleigh damping of the stretch */
+    float bend_damping;   /* Rayleigh damping of the bending */
+    int bend_rest_from_geometry; /* rest bend angle from the initial shape */
+} PpfRodMaterial;
+
 PpfScene *ppf_scene_create(void);
 void ppf_scene_destroy(PpfScene *scene);
 
@@ -62,6 +78,12 @@ unsigned ppf_scene_add_shell_faces(PpfScene *scene, const float *vertices, unsig
                                    const unsigned *faces, unsigned nf,
                                    const unsigned *face_material,
                                    const PpfShellMaterial *materials, unsigned n_materials);
+/* Appends a rod object: nv vertices and ne edges (2 vertex indices each,
+ * local to this object). Rod edges come first in the DataSet's edge list
+ * (mesh.rs:188-229), so the rods of every added object precede the shells'
+ * edges. Returns the global index of the first vertex. */
+unsigned ppf_scene_add_rod(PpfScene *scene, const float *vertices, unsigned nv,
+                           const unsigned *edges, unsigned ne, const PpfRodMaterial *mat);
 /* Initial velocity of every vertex (3 floats each); prev = curr - v dt. */
 void ppf_scene_set_velocity(PpfScene *scene, const float *velocity);
 /* Fix pins at the vertices' current positions. kinematic != 0 marks pins
@@ -108,9 +130,13 @@ void ppf_scene_set_positions(PpfScene *scene, const float *curr,
  * inv_rest2x2 (4 f32 per face, column-major); fixed_offset, fixed_index
  * (the upper-triangle fixed pattern, u32); transpose_offset, transpose (u32
  * (row, slot) pairs per lower entry); face_slots (9 u32 per face),
- * hinge_slots (16 u32 per hinge); edge_face_offset, edge_face (u32); and f32
- * per element: vertex_mass, vertex_area, face_area, face_mass, edge_length,
- * hinge_length, hinge_area, face_mu, face_lambda, hinge_bend. */
+ * hinge_slots (16 u32 per hinge); edge_slots (4 u32 per rod edge),
+ * rod_bend_slots (9 u32 per vertex); edge_face_offset, edge_face (u32); and
+ * f32 per element: vertex_mass, vertex_area, face_area, face_mass,
+ * edge_length, edge_initial_length, edge_mass, edge_stiffness, edge_bend,
+ * rest_bend_angle (per vertex), hinge_length, hinge_area, face_mu,
+ * face_lambda, hinge_bend; vertex_ghat, vertex_offset, vertex_friction (the
+ * contact parameters of each vertex's param). */
 size_t ppf_scene_array(PpfScene *scene, const char *name, void *out);
 
 #ifdef __cplusplus

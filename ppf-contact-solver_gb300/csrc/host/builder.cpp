@@ -12,6 +12,7 @@
 #include "../../../include/ppf_gb300_scene.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -76,6 +77,9 @@ struct PpfScene {
     std::vector<unsigned> faces;          // 3 F
     std::vector<unsigned> face_material;  // per face
     std::vector<PpfShellMaterial> materials;
+    std::vector<unsigned> rods;           // 2 R, global vertex indices
+    std::vector<unsigned> rod_material;   // per rod edge
+    std::vector<PpfRodMaterial> rod_materials;
     std::vector<unsigned> pin_index;
     std::vector<unsigned char> pin_kinematic;
     std::vector<std::pair<unsigned, float>> pulls;
@@ -108,7 +112,7 @@ struct PpfScene {
     VecVecStore fixed_table;
     std::vector<PpfVec2u> transpose_data;
     std::vector<unsigned> transpose_offset;
-    std::vector<unsigned> face_slots, hinge_slots;
+    std::vector<unsigned> face_slots, hinge_slots, edge_slots, rod_bend_slots;
     std::vector<PpfVec3f> cm_vertex;
     std::vector<PpfVec3u> cm_face;
     std::vector<PpfVec2u> cm_edge;
@@ -184,6 +188,19 @@ unsigned ppf_scene_add_shell(PpfScene *s, const float *v, unsigned nv,
     s->materials.push_back(*mat);
     for (unsigned i = 0; i < 3 * nf; ++i) s->faces.push_back(base + f[i]);
     s->face_material.insert(s->face_material.end(), nf, mi);
+    s->built = false;
+    return base;
+}
+
+unsigned ppf_scene_add_rod(PpfScene *s, const float *v, unsigned nv, const unsigned *e,
+                           unsigned ne, const PpfRodMaterial *mat) {
+    unsigned base = (unsigned)s->x.size() / 3;
+    s->x.insert(s->x.end(), v, v + 3 * nv);
+    s->vel.insert(s->vel.end(), 3 * nv, 0.0f);
+    unsigned mi = (unsigned)s->rod_materials.size();
+    s->rod_materials.push_back(*mat);
+    for (unsigned i = 0; i < 2 * ne; ++i) s->rods.push_back(base + e[i]);
+    s->rod_material.insert(s->rod_material.end(), ne, mi);
     s->built = false;
     return base;
 }
@@ -277,10 +294,13 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     for (unsigned i = 0; i < nf; ++i)
         for (int k = 0; k < 3; ++k) s->face[i].v[k] = s->faces[3 * i + k];
 
-    // edges in first-seen order with their incident faces (mesh.rs:188-229)
+    // edges (mesh.rs:188-229): the rod edges as given, then the face edges in
+    // first-seen order with their incident faces
+    const unsigned nr = (unsigned)s->rods.size() / 2;
     std::map<std::pair<unsigned, unsigned>, unsigned> edge_id;
-    std::vector<std::vector<unsigned>> edge_faces;
+    std::vector<std::vector<unsigned>> edge_faces(nr);
     s->edge.clear();
+    for (unsigned i = 0; i < nr; ++i) s->edge.push_back({{s->rods[2 * i], s->rods[2 * i + 1]}});
     for (unsigned i = 0; i < nf; ++i)
         for (int j = 0; j < 3; ++j) {
             unsigned a = s->faces[3 * i + j], b = s->faces[3 * i + (j + 1) % 3];
@@ -337,6 +357,8 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
         for (int k = 0; k < 4; ++k) vh[s->hinge[i].v[k]].push_back(i);
     for (unsigned i = 0; i < ne; ++i)
         for (int k = 0; k < 2; ++k) ve[s->edge[i].v[k]].push_back(i);
+    for (unsigned i = 0; i < nr; ++i)
+        for (int k = 0; k < 2; ++k) vr[s->edge[i].v[k]].push_back(i);
     s->nb_vface.from(vf);
     s->nb_vhinge.from(vh);
     s->nb_vedge.from(ve);
@@ -399,21 +421,79 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
         s->fprop[i] = pr;
     }
 
-    // vertex props (builder.rs:560-720) and params (builder.rs:780-870)
+    // rod edge props / params (scene.rs:1540-1655): mass from the initial
+    // length, rest length scaled by the length factor; fixed when both ends
+    // are pinned (builder.rs:409-419)
+    s->eparam.clear();
+    s->eprop.assign(ne, PpfEdgeProp{});
+    for (unsigned i = 0; i < nr; ++i) {
+        const PpfRodMaterial &m = s->rod_materials[s->rod_material[i]];
+        const float len = nrm(sub(X(s->edge[i].v[1]), X(s->edge[i].v[0])));
+        PpfEdgeParam ep{};
+        ep.stiffness = m.young_mod;
+        ep.bend = m.bend;
+        ep.ghat = m.contact_gap;
+        ep.offset = m.contact_offset;
+        ep.friction = m.friction;
+        ep.strainlimit = m.strain_limit;
+        ep.bend_rest_from_geometry = m.bend_rest_from_geometry != 0;
+        ep.deform_damping = m.deform_damping;
+        ep.bend_damping = m.bend_damping;
+        PpfEdgeProp pr{};
+        pr.length = len * m.length_factor;
+        pr.initial_length = len;
+        pr.mass = m.density * len;
+        pr.fixed = fixed_v[s->edge[i].v[0]] && fixed_v[s->edge[i].v[1]];
+        pr.param_index = dedup(s->eparam, ep);
+        s->eprop[i] = pr;
+    }
+
+    // vertex props (builder.rs:476-720) and params (builder.rs:780-870)
     s->vprop.assign(n, PpfVertexProp{});
     for (unsigned i = 0; i < n; ++i) s->vprop[i].rest_bend_angle = 3.14159265358979323846f;
     for (size_t i = 0; i < s->fix.size(); ++i) s->vprop[s->fix[i].index].fix_index = (unsigned)i + 1;
     for (size_t i = 0; i < s->pull.size(); ++i) s->vprop[s->pull[i].index].pull_index = (unsigned)i + 1;
+    // rest bend angle of an interior rod vertex (two rod edges, no face)
+    // whose edges ask for it from the initial shape (builder.rs:521-569)
+    for (unsigned j = 0; j < n; ++j) {
+        std::vector<unsigned> re;
+        for (unsigned ei : ve[j])
+            if (ei < nr) re.push_back(ei);
+        if (re.size() != 2 || !vf[j].empty()) continue;
+        if (!s->eparam[s->eprop[re[0]].param_index].bend_rest_from_geometry &&
+            !s->eparam[s->eprop[re[1]].param_index].bend_rest_from_geometry)
+            continue;
+        const PpfVec2u &a = s->edge[re[0]], &b = s->edge[re[1]];
+        const unsigned o0 = a.v[0] == j ? a.v[1] : a.v[0], o1 = b.v[0] == j ? b.v[1] : b.v[0];
+        V3 e0 = sub(X(o0), X(j)), e1 = sub(X(o1), X(j));
+        float n0 = nrm(e0), n1 = nrm(e1);
+        if (n0 <= 0.0f || n1 <= 0.0f) continue;
+        float c = dot(e0, e1) / (n0 * n1);
+        c = std::min(1.0f, std::max(-1.0f, c));
+        s->vprop[j].rest_bend_angle = std::acos(c);
+    }
     for (unsigned i = 0; i < nf; ++i)
         for (int k = 0; k < 3; ++k) s->vprop[s->face[i].v[k]].area += s->fprop[i].area / 3.0f;
     for (unsigned i = 0; i < nf; ++i)
         for (int k = 0; k < 3; ++k) s->vprop[s->face[i].v[k]].mass += s->fprop[i].mass / 3.0f;
+    for (unsigned i = 0; i < nr; ++i)
+        for (int k = 0; k < 2; ++k) s->vprop[s->edge[i].v[k]].mass += s->eprop[i].mass / 2.0f;
     s->vparam.clear();
     for (unsigned j = 0; j < n; ++j) {
+        // faces weighted by area, rod edges by rest length
         float gs = 0, os = 0, fs = 0, ws = 0;
         for (unsigned fi : vf[j]) {
             const PpfFaceParam &p = s->fparam[s->fprop[fi].param_index];
             float w = s->fprop[fi].area;
+            gs += w * p.ghat;
+            os += w * p.offset;
+            fs += w * p.friction;
+            ws += w;
+        }
+        for (unsigned ei : ve[j]) {
+            if (ei >= nr) continue;
+            const PpfEdgeParam &p = s->eparam[s->eprop[ei].param_index];
+            float w = s->eprop[ei].length;
             gs += w * p.ghat;
             os += w * p.offset;
             fs += w * p.friction;
@@ -458,9 +538,7 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     }
 
     // face-edge props (main.rs:205-250): zero mass, area-averaged contact
-    s->eparam.clear();
-    s->eprop.assign(ne, PpfEdgeProp{});
-    for (unsigned i = 0; i < ne; ++i) {
+    for (unsigned i = nr; i < ne; ++i) {
         float gs = 0, os = 0, fs = 0, as = 0;
         for (unsigned fi : edge_faces[i]) {
             const PpfFaceParam &p = s->fparam[s->fprop[fi].param_index];
@@ -525,6 +603,17 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     for (auto &h : s->hinge)
         for (int a = 0; a < 4; ++a)
             for (int b = 0; b < 4; ++b) insert(h.v[a], h.v[b]);
+    // rod-bend stencil (j, i, k) of every vertex with two edges and no face
+    // (builder.rs:1289-1313)
+    std::vector<std::array<unsigned, 3>> bend_stencil(n, {{0xFFFFFFFFu, 0u, 0u}});
+    for (unsigned i = 0; i < n; ++i) {
+        if (ve[i].size() != 2 || !vf[i].empty()) continue;
+        const PpfVec2u &a = s->edge[ve[i][0]], &b = s->edge[ve[i][1]];
+        const unsigned j = a.v[0] == i ? a.v[1] : a.v[0], k = b.v[0] == i ? b.v[1] : b.v[0];
+        bend_stencil[i] = {{j, i, k}};
+        for (unsigned x : bend_stencil[i])
+            for (unsigned y : bend_stencil[i]) insert(x, y);
+    }
     s->fixed_table.from(rows);
     std::vector<std::vector<PpfVec2u>> tr(n);
     unsigned base = 0;
@@ -555,6 +644,22 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
         for (int a = 0; a < 4; ++a)
             for (int b = 0; b < 4; ++b) s->hinge_slots.push_back(slot_of(r[a], r[b]));
     }
+    // rod edges: 4 blocks each; rod-bend stencils: 9 per vertex (sentinels
+    // where a vertex has none), builder.rs:1424-1466
+    s->edge_slots.clear();
+    for (unsigned i = 0; i < nr; ++i)
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b)
+                s->edge_slots.push_back(slot_of(s->edge[i].v[a], s->edge[i].v[b]));
+    s->rod_bend_slots.assign(nr ? 9 * (size_t)n : 0, 0xFFFFFFFFu);
+    if (nr)
+        for (unsigned i = 0; i < n; ++i) {
+            if (bend_stencil[i][0] == 0xFFFFFFFFu) continue;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b)
+                    s->rod_bend_slots[9 * (size_t)i + 3 * a + b] =
+                        slot_of(bend_stencil[i][a], bend_stencil[i][b]);
+        }
 
     // assemble the DataSet view
     PpfDataSet &ds = s->ds;
@@ -655,11 +760,14 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     ds.transpose_table.nnz = (unsigned)s->transpose_data.size();
     ds.transpose_table.nnz_allocated = ds.transpose_table.nnz;
     ds.transpose_table.offset_allocated = n + 1;
-    ds.rod_count = 0;
+    ds.rod_count = nr;
     ds.shell_face_count = nf;
     ds.surface_vert_count = n;
     set_vec(ds.face_hess_slots.data, ds.face_hess_slots.size, ds.face_hess_slots.allocated, s->face_slots);
     set_vec(ds.hinge_hess_slots.data, ds.hinge_hess_slots.size, ds.hinge_hess_slots.allocated, s->hinge_slots);
+    set_vec(ds.edge_hess_slots.data, ds.edge_hess_slots.size, ds.edge_hess_slots.allocated, s->edge_slots);
+    set_vec(ds.rod_bend_hess_slots.data, ds.rod_bend_hess_slots.size,
+            ds.rod_bend_hess_slots.allocated, s->rod_bend_slots);
     s->built = true;
     return 0;
 }
@@ -703,7 +811,24 @@ size_t ppf_scene_array(PpfScene *s, const char *name, void *out) {
     else if (n == "vertex_area") per(s->vprop, [](const PpfVertexProp &p) { return p.area; });
     else if (n == "face_area") per(s->fprop, [](const PpfFaceProp &p) { return p.area; });
     else if (n == "face_mass") per(s->fprop, [](const PpfFaceProp &p) { return p.mass; });
+    else if (n == "edge_slots") take(s->edge_slots);
+    else if (n == "rod_bend_slots") take(s->rod_bend_slots);
     else if (n == "edge_length") per(s->eprop, [](const PpfEdgeProp &p) { return p.length; });
+    else if (n == "edge_initial_length")
+        per(s->eprop, [](const PpfEdgeProp &p) { return p.initial_length; });
+    else if (n == "edge_mass") per(s->eprop, [](const PpfEdgeProp &p) { return p.mass; });
+    else if (n == "edge_stiffness")
+        per(s->eprop, [&](const PpfEdgeProp &p) { return s->eparam[p.param_index].stiffness; });
+    else if (n == "edge_bend")
+        per(s->eprop, [&](const PpfEdgeProp &p) { return s->eparam[p.param_index].bend; });
+    else if (n == "rest_bend_angle")
+        per(s->vprop, [](const PpfVertexProp &p) { return p.rest_bend_angle; });
+    else if (n == "vertex_ghat")
+        per(s->vprop, [&](const PpfVertexProp &p) { return s->vparam.empty() ? 0.0f : s->vparam[p.param_index].ghat; });
+    else if (n == "vertex_offset")
+        per(s->vprop, [&](const PpfVertexProp &p) { return s->vparam.empty() ? 0.0f : s->vparam[p.param_index].offset; });
+    else if (n == "vertex_friction")
+        per(s->vprop, [&](const PpfVertexProp &p) { return s->vparam.empty() ? 0.0f : s->vparam[p.param_index].friction; });
     else if (n == "hinge_length") per(s->hprop, [](const PpfHingeProp &p) { return p.length; });
     else if (n == "hinge_area") per(s->hprop, [](const PpfHingeProp &p) { return p.area; });
     else if (n == "face_mu")

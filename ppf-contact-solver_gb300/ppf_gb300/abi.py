@@ -93,6 +93,22 @@ class ShellMaterial(C.Structure):
     ]
 
 
+class RodMaterial(C.Structure):
+    _fields_ = [
+        ("density", C.c_float),
+        ("young_mod", C.c_float),
+        ("bend", C.c_float),
+        ("length_factor", C.c_float),
+        ("strain_limit", C.c_float),
+        ("contact_gap", C.c_float),
+        ("contact_offset", C.c_float),
+        ("friction", C.c_float),
+        ("deform_damping", C.c_float),
+        ("bend_damping", C.c_float),
+        ("bend_rest_from_geometry", C.c_int),
+    ]
+
+
 class StepStats(C.Structure):
     _fields_ = [
         ("newton_iters", C.c_uint),

@@ -37,6 +37,9 @@ def _declare(lib):
     lib.ppf_scene_add_shell.restype = C.c_uint
     lib.ppf_scene_add_shell.argtypes = [P, _f32, C.c_uint, _u32, C.c_uint,
                                         C.POINTER(abi.ShellMaterial)]
+    lib.ppf_scene_add_rod.restype = C.c_uint
+    lib.ppf_scene_add_rod.argtypes = [P, _f32, C.c_uint, _u32, C.c_uint,
+                                      C.POINTER(abi.RodMaterial)]
     lib.ppf_scene_set_velocity.argtypes = [P, _f32]
     lib.ppf_scene_pin.argtypes = [P, _u32, C.c_uint, C.c_int]
     lib.ppf_scene_pull.argtypes = [P, _u32, C.c_uint, C.c_float]
@@ -121,6 +124,30 @@ class Material:
                                  self.contact_offset, self.friction)
 
 
+@dataclass
+class RodMaterial:
+    """Rod material in the reference's units (scene.rs rod parameters):
+    density in kg/m, young_mod the stretch stiffness per unit edge mass."""
+
+    density: float = 1.0
+    young_mod: float = 1000.0
+    bend: float = 0.0
+    length_factor: float = 1.0
+    strain_limit: float = 0.0
+    contact_gap: float = 1e-3
+    contact_offset: float = 0.0
+    friction: float = 0.0
+    deform_damping: float = 0.0
+    bend_damping: float = 0.0
+    bend_rest_from_geometry: bool = False
+
+    def to_c(self) -> abi.RodMaterial:
+        return abi.RodMaterial(self.density, self.young_mod, self.bend, self.length_factor,
+                               self.strain_limit, self.contact_gap, self.contact_offset,
+                               self.friction, self.deform_damping, self.bend_damping,
+                               1 if self.bend_rest_from_geometry else 0)
+
+
 class Scene:
     """A scene under construction, then the built DataSet that owns the host
     arrays initialize() reads and fetch() writes."""
@@ -147,6 +174,13 @@ class Scene:
         m = material.to_c()
         return int(self.lib.ppf_scene_add_shell(self.h, v, v.size // 3, f, f.size // 3,
                                                 C.byref(m)))
+
+    def add_rod(self, vertices, edges, material: RodMaterial) -> int:
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1)
+        e = np.ascontiguousarray(edges, np.uint32).reshape(-1)
+        m = material.to_c()
+        return int(self.lib.ppf_scene_add_rod(self.h, v, v.size // 3, e, e.size // 2,
+                                              C.byref(m)))
 
     def set_velocity(self, velocity):
         v = np.ascontiguousarray(velocity, np.float32).reshape(-1)
