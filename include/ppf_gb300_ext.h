@@ -336,6 +336,11 @@ void ppf_debug_factor_diag(float *out);
  * x = alpha P b: the direction of the preconditioner's first output.
  * Returns the PCG state. */
 int ppf_debug_pcg(const float *b, float *x, unsigned max_iter, unsigned *iters, float *resid);
+/* The strain-limit line search of faces and rod edges (strainlimiting.cu:
+ * 192-305) on the initialized scene, from positions x0 to x1 (3n floats
+ * each): the fraction of x1 - x0 it admits (its time of impact divided by
+ * line_search_max_t, as the reference returns it). */
+float ppf_debug_strain_line_search(const float *x0, const float *x1);
 /* The Schwarz layout of the last solve: sizes[3] = {aggregates, coarse
  * domains, levels} (zeros when no Schwarz solve ran), the aggregate of each
  * vertex (n) and the domain of each aggregate (sizes[0], written when there

@@ -40,6 +40,8 @@ typedef struct {
     float contact_gap;    /* ghat */
     float contact_offset;
     float friction;
+    float deform_damping; /* Rayleigh damping of the membrane (0: none) */
+    float bend_damping;   /* Rayleigh damping of the bending (0: none) */
 } PpfShellMaterial;
 
 /* Per-object rod material (the reference scene's rod-* parameters,

@@ -73,6 +73,8 @@ def reference_pipeline():
         lib.refpipe_line_search.argtypes = [f32p, f32p, C.POINTER(C.c_uint), C.POINTER(C.c_int)]
         lib.refpipe_strain_line_search.restype = C.c_float
         lib.refpipe_strain_line_search.argtypes = [f32p, f32p]
+        lib.refpipe_rod_strain_line_search.restype = C.c_float
+        lib.refpipe_rod_strain_line_search.argtypes = [f32p, f32p]
         lib.refpipe_check_intersection.restype = C.c_bool
         lib.refpipe_check_intersection.argtypes = [f32p]
         _REF_PIPE = lib

@@ -9,6 +9,7 @@
 #include "../ppf-contact-solver_gb300/csrc/physics/bw.cuh"
 #include "../ppf-contact-solver_gb300/csrc/physics/contact_local.cuh"
 #include "../ppf-contact-solver_gb300/csrc/physics/hinge.cuh"
+#include "../ppf-contact-solver_gb300/csrc/physics/rod.cuh"
 #include "../ppf-contact-solver_gb300/csrc/physics/strainlimit.cuh"
 
 #include <cstring>
@@ -109,6 +110,22 @@ void orc_hinge(const float *x12, float rest, float *angle, float *force12,
     *angle = hinge::dihedral_angle(X0, X1, X2, X3);
     put(force12, f);
     put(hess144, h);
+}
+void orc_hook(const float *x0, const float *x1, float l0, float weight, float *grad6,
+              float *hess36) {
+    Mat3x2 g;
+    Mat6 h;
+    rod::stretch(v3(x0), v3(x1), l0, weight, g, h);
+    put(grad6, g);
+    put(hess36, h);
+}
+void orc_strand(const float *x0, const float *x1, const float *x2, float rest, float *f9,
+                float *h81) {
+    Mat3 f;
+    Mat9 h;
+    rod::bend(v3(x0), v3(x1), v3(x2), rest, f, h);
+    put(f9, f);
+    put(h81, h);
 }
 void orc_symm2(const float *A4, float *val, float *vec) {
     Vec2 v;

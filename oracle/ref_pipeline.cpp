@@ -505,6 +505,9 @@ unsigned refpipe_assemble(const float *eval_x, const float *target, float dt) {
     if (p.data.shell_face_count > 0)
         strainlimiting::embed_strainlimiting_force_hessian(p.data, ex, force, p.tmp_fixed,
                                                            p.fixed, p.prm);
+    if (p.data.rod_count > 0)
+        strainlimiting::embed_rod_strainlimiting_force_hessian(p.data, ex, force, p.tmp_fixed,
+                                                               p.fixed, p.prm);
     unsigned num = 0;
     if (!p.prm.disable_contact) {
         p.build_trees(p.eval_x, p.eval_x, 1.0f);
@@ -574,6 +577,17 @@ float refpipe_strain_line_search(const float *a, const float *b) {
     Vec<float> tmp_v = RefPipe::view(tmp);
     return strainlimiting::line_search(p.data, RefPipe::view(p.x1), RefPipe::view(p.x0), tmp_v,
                                        p.prm);
+}
+
+// main.cu:1336-1341: the rods' strain-limit line search from x0 to x1.
+float refpipe_rod_strain_line_search(const float *a, const float *b) {
+    RefPipe &p = *g_pipe;
+    load3(p.x0, a, p.n);
+    load3(p.x1, b, p.n);
+    std::vector<float> tmp(std::max(1u, p.data.rod_count));
+    Vec<float> tmp_v = RefPipe::view(tmp);
+    return strainlimiting::rod_line_search(p.data, RefPipe::view(p.x1), RefPipe::view(p.x0),
+                                           tmp_v, p.prm);
 }
 
 // main.cu:1519-1536: trees at x, then the intersection check.

@@ -48,6 +48,7 @@ inline unsigned atomicAdd(unsigned *p, unsigned v) {
 #include "energy/model/baraffwitkin.hpp"
 #include "energy/model/dihedral_angle.hpp"
 #include "energy/model/friction.hpp"
+#include "energy/model/hook.hpp"
 #include "energy/model/push.hpp"
 #include "linalg/eigsolve.hpp"
 #include "utility/utility.cu"
@@ -113,7 +114,7 @@ ParamSet ccd_param(float max_t, float eps) {
 
 extern "C" {
 
-int ref_wrap_version() { return 2; }
+int ref_wrap_version() { return 3; }
 
 void ref_pe_coeff(const float *p, const float *a, const float *b, float *out) {
     Vec2f c = distance::point_edge_distance_coeff<float, float>(v3(p), v3(a), v3(b));
@@ -239,6 +240,24 @@ void ref_hinge(const float *x12, float rest, float *angle, float *force12,
     *angle = dihedral_angle::face_dihedral_angle(xs[rh[0]], xs[rh[1]], xs[rh[2]], xs[rh[3]]);
     put(force12, f.m, 12);
     put(hess144, h.m, 144);
+}
+// hook.hpp:21-37: rod stretch gradient (3 x 2) and Hessian (6 x 6).
+void ref_hook(const float *x0, const float *x1, float l0, float weight, float *grad6,
+              float *hess36) {
+    Mat3x2f g;
+    Mat6x6f h;
+    hook::make_diff_table(v3(x0), v3(x1), l0, weight, g, h);
+    put(grad6, g.m, 6);
+    put(hess36, h.m, 36);
+}
+// dihedral_angle.hpp:451-541: rod bend force (3 x 3) and projected Hessian.
+void ref_strand(const float *x0, const float *x1, const float *x2, float rest, float *f9,
+                float *h81) {
+    Mat3x3f f;
+    Mat9x9f h;
+    dihedral_angle::strand_compute_force_hessian(v3(x0), v3(x1), v3(x2), rest, f, h);
+    put(f9, f.m, 9);
+    put(h81, h.m, 81);
 }
 void ref_symm2(const float *A4, float *val, float *vec) {
     Mat2x2f A;

@@ -192,6 +192,8 @@ PpfShellMaterial face_material(const std::map<std::string, std::vector<float>> &
     m.contact_gap = get("contact-gap", 1e-3f);
     m.contact_offset = get("contact-offset", 0.0f);
     m.friction = get("friction", 0.0f);
+    m.deform_damping = get("deformation-damping", 0.0f);
+    m.bend_damping = get("bending-damping", 0.0f);
     return m;
 }
 

@@ -372,6 +372,15 @@ int ppf_debug_pcg(const float *b, float *x, unsigned max_iter, unsigned *iters, 
     }
 }
 
+float ppf_debug_strain_line_search(const float *x0, const float *x1) {
+    try {
+        return solver_instance().debug_strain_line_search(x0, x1);
+    } catch (const FatalError &e) {
+        fatal(e);
+        return -1.0f;
+    }
+}
+
 void ppf_debug_schwarz_layout(unsigned *sizes, unsigned *agg, unsigned *dom) {
     try {
         std::vector<unsigned> a, d;

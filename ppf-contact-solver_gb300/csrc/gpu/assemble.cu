@@ -7,6 +7,7 @@
 // the CPU oracle); these kernels gather, evaluate and scatter.
 #include "../physics/bw.cuh"
 #include "../physics/hinge.cuh"
+#include "../physics/rod.cuh"
 #include "../physics/strainlimit.cuh"
 #include "assemble.cuh"
 
@@ -103,7 +104,35 @@ __global__ void k_vertex_energy(Scene s, StepParams p, AssemblyBuffers b) {
 }
 
 // ---- Baraff-Witkin membrane (energy.cu:304-364) ----------------------------
-__global__ void k_face_energy(Scene s, AssemblyBuffers b) {
+// Displacement of an element's N vertices over the step, x - x_start.
+template <int N>
+__device__ __forceinline__ Vec<3 * N> step_displacement(const AssemblyBuffers &b,
+                                                         const unsigned (&v)[N]) {
+    Vec<3 * N> u;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const Vec3 d = X(b.x, v[k]) - X(b.x0, v[k]);
+        u[3 * k] = d[0];
+        u[3 * k + 1] = d[1];
+        u[3 * k + 2] = d[2];
+    }
+    return u;
+}
+
+// Scatters an element's N x N Hessian blocks through its slot table
+// (sentinel: a lower-triangle block, which the upper pattern does not hold).
+template <int N>
+__device__ __forceinline__ void scatter_blocks(float *fixed_val, const unsigned *slot,
+                                               const Mat<3 * N, 3 * N> &H) {
+    for (int a = 0; a < N; ++a)
+        for (int c = 0; c < N; ++c) {
+            const unsigned sl = slot[N * a + c];
+            if (sl != kSentinel)
+                atomic_add_block(fixed_val + 9 * (size_t)sl, H.template block<3, 3>(3 * a, 3 * c));
+        }
+}
+
+__global__ void k_face_energy(Scene s, StepParams p, AssemblyBuffers b) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.nf) return;
     const PpfFaceProp &pr = s.fprop[i];
@@ -115,6 +144,10 @@ __global__ void k_face_energy(Scene s, AssemblyBuffers b) {
     Mat9 H;
     bw::membrane(X(b.x, f[0]), X(b.x, f[1]), X(b.x, f[2]),
                  load_inv_rest(s.inv_rest + 4 * i), fp.mu, fp.lambda, pr.mass, dedx, H);
+    if (fp.deform_damping > 0.0f) { // energy.cu:359-360
+        const unsigned v[3] = {f[0], f[1], f[2]};
+        damping::stiffness<3>(fp.deform_damping, p.dt, step_displacement<3>(b, v), dedx, H);
+    }
     for (int a = 0; a < 3; ++a) atomic_add3(b.force + 3 * f[a], dedx.col(a));
     const unsigned *slot = s.face_slot + 9 * i;
     for (int a = 0; a < 3; ++a)
@@ -126,7 +159,7 @@ __global__ void k_face_energy(Scene s, AssemblyBuffers b) {
 }
 
 // ---- dihedral bending (energy.cu:448-553) ----------------------------------
-__global__ void k_hinge_energy(Scene s, AssemblyBuffers b) {
+__global__ void k_hinge_energy(Scene s, StepParams p, AssemblyBuffers b) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.nh) return;
     const PpfHingeProp &pr = s.hprop[i];
@@ -153,6 +186,14 @@ __global__ void k_hinge_energy(Scene s, AssemblyBuffers b) {
                          pr.rest_angle, dedx, H);
     dedx *= k;
     H *= k;
+    if (hp.bend_damping > 0.0f) { // lagged, at the start-of-step positions (energy.cu:528-540)
+        Mat3x4 f_lag;
+        Mat12 K_lag;
+        hinge::force_hessian(X(b.x0, r[0]), X(b.x0, r[1]), X(b.x0, r[2]), X(b.x0, r[3]),
+                             pr.rest_angle, f_lag, K_lag);
+        K_lag *= k;
+        damping::lagged<4>(hp.bend_damping, p.dt, step_displacement<4>(b, r), K_lag, dedx, H);
+    }
     for (int a = 0; a < 4; ++a) atomic_add3(b.force + 3 * r[a], dedx.col(a));
     const unsigned *slot = s.hinge_slot + 16 * i;
     for (int a = 0; a < 4; ++a)
@@ -161,6 +202,56 @@ __global__ void k_hinge_energy(Scene s, AssemblyBuffers b) {
             if (sl != kSentinel)
                 atomic_add_block(b.fixed_val + 9 * (size_t)sl, H.block<3, 3>(3 * a, 3 * c));
         }
+}
+
+// ---- rod stretch (energy.cu:272-302) ---------------------------------------
+__global__ void k_rod_energy(Scene s, StepParams p, AssemblyBuffers b) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.nr) return;
+    const PpfEdgeProp &pr = s.eprop[i];
+    if (pr.fixed) return;
+    const PpfEdgeParam &ep = s.eparam[pr.param_index];
+    if (!(ep.stiffness > 0.0f)) return;
+    const unsigned v[2] = {s.edge[2 * i], s.edge[2 * i + 1]};
+    Mat3x2 dedx;
+    Mat6 H;
+    rod::stretch(X(b.x, v[0]), X(b.x, v[1]), pr.length, ep.stiffness * pr.mass, dedx, H);
+    if (ep.deform_damping > 0.0f)
+        damping::stiffness<2>(ep.deform_damping, p.dt, step_displacement<2>(b, v), dedx, H);
+    for (int a = 0; a < 2; ++a) atomic_add3(b.force + 3 * v[a], dedx.col(a));
+    scatter_blocks<2>(b.fixed_val, s.edge_slot + 4 * i, H);
+}
+
+// ---- rod bending at an interior rod vertex (energy.cu:555-641) -------------
+__global__ void k_rod_bend(Scene s, StepParams p, AssemblyBuffers b) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n_surf) return;
+    const PpfVertexProp &vp = s.vprop[i];
+    if (vp.fix_index != 0) return;
+    if (s.ve_off[i + 1] - s.ve_off[i] != 2 || s.vf_off[i + 1] != s.vf_off[i]) return;
+    const unsigned e0 = s.ve[s.ve_off[i]], e1 = s.ve[s.ve_off[i] + 1];
+    const PpfEdgeParam &p0 = s.eparam[s.eprop[e0].param_index];
+    const PpfEdgeParam &p1 = s.eparam[s.eprop[e1].param_index];
+    const float bend = 0.5f * (p0.bend + p1.bend);
+    const float bend_damping = 0.5f * (p0.bend_damping + p1.bend_damping);
+    const float k = rod::bend_stiffness(bend, vp.mass, s.eprop[e0].length, s.eprop[e1].length);
+    if (!(vp.mass > 0.0f && k > 0.0f)) return;
+    const unsigned *E0 = s.edge + 2 * e0, *E1 = s.edge + 2 * e1;
+    const unsigned v[3] = {E0[0] == i ? E0[1] : E0[0], i, E1[0] == i ? E1[1] : E1[0]};
+    Mat3 dedx;
+    Mat9 H;
+    rod::bend(X(b.x, v[0]), X(b.x, v[1]), X(b.x, v[2]), vp.rest_bend_angle, dedx, H);
+    dedx *= k;
+    H *= k;
+    if (bend_damping > 0.0f) {
+        Mat3 f_lag;
+        Mat9 K_lag;
+        rod::bend(X(b.x0, v[0]), X(b.x0, v[1]), X(b.x0, v[2]), vp.rest_bend_angle, f_lag, K_lag);
+        K_lag *= k;
+        damping::lagged<3>(bend_damping, p.dt, step_displacement<3>(b, v), K_lag, dedx, H);
+    }
+    for (int a = 0; a < 3; ++a) atomic_add3(b.force + 3 * v[a], dedx.col(a));
+    scatter_blocks<3>(b.fixed_val, s.bend_slot + 9 * (size_t)i, H);
 }
 
 // ---- strain-limit barrier (strainlimiting.cu:46-98) -------------------------
@@ -196,6 +287,34 @@ __global__ void k_strain_limit(Scene s, StepParams p, AssemblyBuffers b) {
             if (sl != kSentinel)
                 atomic_add_block(b.fixed_val + 9 * (size_t)sl, kH.block<3, 3>(3 * a, 3 * c));
         }
+}
+
+// ---- rod strain-limit barrier (strainlimiting.cu:122-190) --------------------
+__global__ void k_rod_strain_limit(Scene s, StepParams p, AssemblyBuffers b) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.nr) return;
+    const PpfEdgeProp &pr = s.eprop[i];
+    const PpfEdgeParam &ep = s.eparam[pr.param_index];
+    if (pr.fixed || !(ep.strainlimit > 0.0f)) return;
+    const float l0 = pr.initial_length;
+    if (l0 <= 0.0f) return;
+    const unsigned v[2] = {s.edge[2 * i], s.edge[2 * i + 1]};
+    float g;
+    Vec6 f;
+    Mat6 H;
+    if (!rod::strain_barrier(X(b.x, v[0]), X(b.x, v[1]), l0, ep.strainlimit, p.barrier, g, f, H))
+        return;
+    Mat6 local;
+    for (int a = 0; a < 2; ++a)
+        for (int c = 0; c < 2; ++c)
+            local.set_block<3, 3>(3 * a, 3 * c, fixed_block(s, b.fixed_tmp, v[a], v[c]));
+    const float k = rod::strain_stiffness(X(b.x0, v[0]), X(b.x0, v[1]), local, pr.mass, g,
+                                          ep.strainlimit);
+    H = k * H;
+    f = k * f;
+    atomic_add3(b.force + 3 * v[0], vec3(f[0], f[1], f[2]));
+    atomic_add3(b.force + 3 * v[1], vec3(f[3], f[4], f[5]));
+    scatter_blocks<2>(b.fixed_val, s.edge_slot + 4 * i, H);
 }
 
 // ---- contact detection (contact.cu:1398-1787, stage 0) ----------------------
@@ -942,22 +1061,32 @@ void launch_vertex_energy(const Scene &s, const StepParams &p, const AssemblyBuf
 
 void launch_elastic(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
                     cudaStream_t q) {
-    (void)p;
+    if (s.nr) {
+        k_rod_bend<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, p, b);
+        PPF_LAUNCH_CHECK();
+        k_rod_energy<<<div_up(s.nr, kB), kB, 0, q>>>(s, p, b);
+        PPF_LAUNCH_CHECK();
+    }
     if (s.nf) {
-        k_face_energy<<<div_up(s.nf, kB), kB, 0, q>>>(s, b);
+        k_face_energy<<<div_up(s.nf, kB), kB, 0, q>>>(s, p, b);
         PPF_LAUNCH_CHECK();
     }
     if (s.nh) {
-        k_hinge_energy<<<div_up(s.nh, kB), kB, 0, q>>>(s, b);
+        k_hinge_energy<<<div_up(s.nh, kB), kB, 0, q>>>(s, p, b);
         PPF_LAUNCH_CHECK();
     }
 }
 
 void launch_strain_limit(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
                          cudaStream_t q) {
-    if (!s.nf) return;
-    k_strain_limit<<<div_up(s.nf, kB), kB, 0, q>>>(s, p, b);
-    PPF_LAUNCH_CHECK();
+    if (s.nf) {
+        k_strain_limit<<<div_up(s.nf, kB), kB, 0, q>>>(s, p, b);
+        PPF_LAUNCH_CHECK();
+    }
+    if (s.nr) {
+        k_rod_strain_limit<<<div_up(s.nr, kB), kB, 0, q>>>(s, p, b);
+        PPF_LAUNCH_CHECK();
+    }
 }
 
 void launch_edge_pieces(const Scene &s, const BvhView &eb, const float *x, const float *x1,

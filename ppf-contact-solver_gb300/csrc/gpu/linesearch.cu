@@ -3,6 +3,7 @@
 // functions of ../physics/accd.cuh.
 #include "../physics/accd.cuh"
 #include "../physics/bw.cuh"
+#include "../physics/rod.cuh"
 #include "../physics/strainlimit.cuh"
 #include "assemble.cuh"
 #include "linesearch.cuh"
@@ -420,6 +421,22 @@ __global__ void k_strain_ls(Scene s, LineSearchArgs a) {
     atomicMin(&a.st->sl_toi_bits, __float_as_uint(t));
 }
 
+// Rod edges (strainlimiting.cu:192-245): a.x0 the previous iterate, a.x1 the
+// candidate, as for the faces.
+__global__ void k_rod_strain_ls(Scene s, LineSearchArgs a) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.nr) return;
+    float t = a.max_t;
+    const PpfEdgeProp &pr = s.eprop[i];
+    const PpfEdgeParam &ep = s.eparam[pr.param_index];
+    if (!pr.fixed && ep.strainlimit > 0.0f && pr.initial_length > 0.0f) {
+        const unsigned *e = s.edge + 2 * i;
+        t = rod::strain_line_search(X(a.x0, e[1]) - X(a.x0, e[0]), X(a.x1, e[1]) - X(a.x1, e[0]),
+                                    pr.initial_length, ep.strainlimit, a.max_t);
+    }
+    atomicMin(&a.st->sl_toi_bits, __float_as_uint(t));
+}
+
 struct FaceEdgeIsectOp {
     const Scene &s;
     const float *x;
@@ -601,9 +618,14 @@ void launch_constraint_line_search(const Scene &s, const LineSearchArgs &a, cuda
 }
 
 void launch_strain_line_search(const Scene &s, const LineSearchArgs &a, cudaStream_t q) {
-    if (!s.nf) return;
-    k_strain_ls<<<div_up(s.nf, kB), kB, 0, q>>>(s, a);
-    PPF_LAUNCH_CHECK();
+    if (s.nf) {
+        k_strain_ls<<<div_up(s.nf, kB), kB, 0, q>>>(s, a);
+        PPF_LAUNCH_CHECK();
+    }
+    if (s.nr) {
+        k_rod_strain_ls<<<div_up(s.nr, kB), kB, 0, q>>>(s, a);
+        PPF_LAUNCH_CHECK();
+    }
 }
 
 void launch_intersection_check(const Scene &s, const BvhView &fb, const BvhView &eb,

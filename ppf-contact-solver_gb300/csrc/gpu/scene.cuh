@@ -45,6 +45,7 @@ struct CsrView {
 // Everything a kernel needs to read the scene (device pointers, by value).
 struct Scene {
     unsigned n, n_surf, nf, ne, nh;
+    unsigned nr; // rod edges: edges 0 .. nr-1
     const unsigned *face;
     const unsigned *edge;
     const unsigned *hinge;
@@ -66,6 +67,8 @@ struct Scene {
     const unsigned *fixed_diag; // slot of (i, i)
     const unsigned *face_slot;  // 9 per face
     const unsigned *hinge_slot; // 16 per hinge, remapped order
+    const unsigned *edge_slot;  // 4 per rod edge
+    const unsigned *bend_slot;  // 9 per vertex: rod-bend stencil (j, i, k), or sentinels
     const unsigned *dof_mask;   // 1 = Dirichlet vertex
     const PpfFixPair *fix;
     unsigned nfix;

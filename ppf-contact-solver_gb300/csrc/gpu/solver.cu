@@ -195,6 +195,7 @@ Scene Solver::scene() const {
     s.nf = nf_;
     s.ne = ne_;
     s.nh = nh_;
+    s.nr = nr_;
     s.face = face_.data();
     s.edge = edge_.data();
     s.hinge = hinge_.data();
@@ -220,6 +221,8 @@ Scene Solver::scene() const {
     s.fixed_diag = fixed_diag_.data();
     s.face_slot = face_slot_.data();
     s.hinge_slot = hinge_slot_.data();
+    s.edge_slot = edge_slot_.data();
+    s.bend_slot = bend_slot_.data();
     s.dof_mask = dof_mask_.data();
     s.fix = fix_.data();
     s.nfix = nfix_;
@@ -427,6 +430,11 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     nf_ = ds->mesh.mesh.face.size;
     ne_ = ds->mesh.mesh.edge.size;
     nh_ = ds->mesh.mesh.hinge.size;
+    nr_ = std::min(ds->rod_count, ne_);
+    if (ds->mesh.mesh.tet.size)
+        throw FatalError(4, "tets are not simulated by this library");
+    if (ds->constraint.stitch.size)
+        throw FatalError(4, "stitches are not simulated by this library");
     if (!q_) PPF_CUDA(cudaStreamCreateWithFlags(&q_, cudaStreamNonBlocking));
     if (!ev0_) {
         PPF_CUDA(cudaEventCreate(&ev0_));
@@ -500,6 +508,35 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     }
     upload(face_slot_, fs);
     upload(hinge_slot_, hs);
+    // rod edges: 4 blocks each; the rod-bend stencil (j, i, k) of every vertex
+    // with two edges and no face (energy.cu:555-565): 9 blocks, else sentinels
+    const unsigned *E = (const unsigned *)ds->mesh.mesh.edge.data;
+    std::vector<unsigned> es(4 * (size_t)nr_), bs;
+    for (unsigned e = 0; e < nr_; ++e)
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b) es[4 * e + 2 * a + b] = slot_of(E[2 * e + a], E[2 * e + b]);
+    if (nr_) {
+        bs.assign(9 * (size_t)n_, kSentinel);
+        const PpfVecVecU32 &ve = ds->mesh.neighbor.vertex.edge, &vf = ds->mesh.neighbor.vertex.face;
+        auto count = [&](const PpfVecVecU32 &v, unsigned i) -> unsigned {
+            return (v.offset && i < v.size) ? v.offset[i + 1] - v.offset[i] : 0u;
+        };
+        for (unsigned i = 0; i < n_surf_; ++i) {
+            if (count(ve, i) != 2 || count(vf, i) != 0) continue;
+            const unsigned e0 = ve.data[ve.offset[i]], e1 = ve.data[ve.offset[i] + 1];
+            const unsigned st[3] = {E[2 * e0] == i ? E[2 * e0 + 1] : E[2 * e0], i,
+                                    E[2 * e1] == i ? E[2 * e1 + 1] : E[2 * e1]};
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    const unsigned sl = slot_of(st[a], st[b]);
+                    if (st[a] <= st[b] && sl == kSentinel)
+                        throw FatalError(4, "fixed pattern lacks a rod-bend block");
+                    bs[9 * (size_t)i + 3 * a + b] = sl;
+                }
+        }
+    }
+    upload(edge_slot_, es);
+    upload(bend_slot_, bs);
     // per-primitive margins 0.5 ghat + offset
     std::vector<float> mf(nf_), me(ne_), mv(n_);
     for (unsigned i = 0; i < nf_; ++i) {
@@ -1284,6 +1321,24 @@ int Solver::debug_pcg(const float *b, std::vector<float> &x, unsigned max_iter, 
     iters = res.iter;
     resid = res.resid;
     return res.state;
+}
+
+float Solver::debug_strain_line_search(const float *x0, const float *x1) {
+    const size_t n3 = 3 * (size_t)n_;
+    const float max_t = param->line_search_max_t;
+    PPF_CUDA(cudaMemcpyAsync(target_.data(), x0, n3 * sizeof(float), cudaMemcpyHostToDevice, q_));
+    PPF_CUDA(cudaMemcpyAsync(eval_x_.data(), x1, n3 * sizeof(float), cudaMemcpyHostToDevice, q_));
+    const unsigned bits = __builtin_bit_cast(unsigned, max_t);
+    PPF_CUDA(cudaMemcpyAsync(&st_.data()->sl_toi_bits, &bits, sizeof(unsigned),
+                             cudaMemcpyHostToDevice, q_));
+    LineSearchArgs la{target_.data(), eval_x_.data(), curr_.data(), st_.data(), max_t,
+                      param->ccd_eps};
+    launch_strain_line_search(scene(), la, q_);
+    unsigned out = 0;
+    PPF_CUDA(cudaMemcpyAsync(&out, &st_.data()->sl_toi_bits, sizeof(unsigned),
+                             cudaMemcpyDeviceToHost, q_));
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    return __builtin_bit_cast(float, out) / max_t;
 }
 
 void Solver::debug_schwarz(unsigned *sizes, std::vector<unsigned> &agg,

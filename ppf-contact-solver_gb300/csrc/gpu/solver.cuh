@@ -80,6 +80,9 @@ class Solver {
     // with right-hand side b from x = 0, at most max_iter iterations.
     int debug_pcg(const float *b, std::vector<float> &x, unsigned max_iter, unsigned &iters,
                   float &resid);
+    // The strain-limit line search (faces and rods) from x0 to x1, as the
+    // fraction of x1 - x0 it admits (the time of impact over max_t).
+    float debug_strain_line_search(const float *x0, const float *x1);
     // The Schwarz layout of the last solve: sizes {n_agg, n_dom, levels},
     // the aggregate of each vertex and the domain of each aggregate.
     void debug_schwarz(unsigned *sizes, std::vector<unsigned> &agg, std::vector<unsigned> &dom);
@@ -103,7 +106,7 @@ class Solver {
     void line_search_stage();
     void read_status();
 
-    unsigned n_ = 0, n_surf_ = 0, nf_ = 0, ne_ = 0, nh_ = 0;
+    unsigned n_ = 0, n_surf_ = 0, nf_ = 0, ne_ = 0, nh_ = 0, nr_ = 0;
     cudaStream_t q_ = nullptr;
     // topology / props / params
     DevBuf<unsigned> face_, edge_, hinge_;
@@ -119,7 +122,7 @@ class Solver {
     DevBuf<unsigned> vf_off_, vf_, ve_off_, ve_, ef_off_, ef_;
     DevBuf<unsigned> fixed_off_, fixed_col_, fixed_tr_off_, fixed_diag_;
     DevBuf<uint2> fixed_tr_;
-    DevBuf<unsigned> face_slot_, hinge_slot_, dof_mask_;
+    DevBuf<unsigned> face_slot_, hinge_slot_, edge_slot_, bend_slot_, dof_mask_;
     DevBuf<PpfFixPair> fix_;
     DevBuf<PpfPullPair> pull_;
     DevBuf<PpfSphere> sphere_;

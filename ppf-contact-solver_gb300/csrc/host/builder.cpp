@@ -412,6 +412,8 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
         fp.strainlimit = m.strain_limit;
         fp.shrink_x = 1.0f;
         fp.shrink_y = 1.0f;
+        fp.deform_damping = m.deform_damping;
+        fp.bend_damping = m.bend_damping;
         PpfFaceProp pr{};
         pr.area = area;
         pr.mass = m.density * area;
@@ -511,7 +513,7 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     for (unsigned i = 0; i < nh; ++i) {
         const PpfVec4u &h = s->hinge[i];
         float length = nrm(sub(X(h.v[0]), X(h.v[1])));
-        float os = 0, gs = 0, bs = 0, as = 0;
+        float os = 0, gs = 0, bs = 0, ds = 0, as = 0;
         bool all_fixed = true;
         for (unsigned fi : hinge_faces[i]) {
             const PpfFaceParam &p = s->fparam[s->fprop[fi].param_index];
@@ -520,10 +522,12 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
             os += a * p.offset;
             gs += a * p.ghat;
             bs += a * p.bend;
+            ds += a * p.bend_damping;
             as += a;
         }
         PpfHingeParam hp{};
         hp.bend = all_fixed ? 0.0f : bs / as;
+        hp.bend_damping = all_fixed ? 0.0f : ds / as;
         hp.ghat = gs / as;
         hp.offset = os / as;
         PpfHingeProp pr{};

@@ -90,6 +90,8 @@ class ShellMaterial(C.Structure):
         ("contact_gap", C.c_float),
         ("contact_offset", C.c_float),
         ("friction", C.c_float),
+        ("deform_damping", C.c_float),
+        ("bend_damping", C.c_float),
     ]
 
 

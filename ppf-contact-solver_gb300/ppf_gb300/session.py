@@ -117,11 +117,14 @@ class Material:
     contact_offset: float = 0.0
     friction: float = 0.0
     model: int = abi.MODEL_BARAFF_WITKIN
+    deform_damping: float = 0.0
+    bend_damping: float = 0.0
 
     def to_c(self) -> abi.ShellMaterial:
         return abi.ShellMaterial(self.model, self.density, self.young_mod, self.poiss_rat,
                                  self.bend, self.strain_limit, self.contact_gap,
-                                 self.contact_offset, self.friction)
+                                 self.contact_offset, self.friction, self.deform_damping,
+                                 self.bend_damping)
 
 
 @dataclass
@@ -160,6 +163,9 @@ class Scene:
         self.n_spheres = 0
         self.n_floors = 0
         self.n_collision_vertices = 0
+        self._rod_count = 0
+        self._rod_mats = []
+        self._vert_inputs = []
         self.built = False
 
     def __del__(self):
@@ -172,6 +178,7 @@ class Scene:
         v = np.ascontiguousarray(vertices, np.float32).reshape(-1)
         f = np.ascontiguousarray(faces, np.uint32).reshape(-1)
         m = material.to_c()
+        self._vert_inputs.append(v.reshape(-1, 3).copy())
         return int(self.lib.ppf_scene_add_shell(self.h, v, v.size // 3, f, f.size // 3,
                                                 C.byref(m)))
 
@@ -179,6 +186,9 @@ class Scene:
         v = np.ascontiguousarray(vertices, np.float32).reshape(-1)
         e = np.ascontiguousarray(edges, np.uint32).reshape(-1)
         m = material.to_c()
+        self._rod_count += e.size // 2
+        self._rod_mats.extend([material] * (e.size // 2))
+        self._vert_inputs.append(v.reshape(-1, 3).copy())
         return int(self.lib.ppf_scene_add_rod(self.h, v, v.size // 3, e, e.size // 2,
                                               C.byref(m)))
 
@@ -218,6 +228,12 @@ class Scene:
         self.lib.ppf_scene_add_collision_mesh(self.h, v, v.size // 3, f, f.size // 3,
                                               contact_gap, contact_offset, friction)
         self.n_collision_vertices += v.size // 3
+
+    @property
+    def _rest_positions(self) -> np.ndarray:
+        """The vertex positions the objects were added with (the builder's
+        rest shape), in vertex order."""
+        return np.concatenate(self._vert_inputs) if self._vert_inputs else np.zeros((0, 3))
 
     @property
     def vertex_count(self) -> int:
@@ -270,7 +286,11 @@ class Scene:
                      "face_mass": np.float32, "edge_length": np.float32,
                      "hinge_length": np.float32, "hinge_area": np.float32,
                      "face_mu": np.float32, "face_lambda": np.float32,
-                     "hinge_bend": np.float32}
+                     "hinge_bend": np.float32, "edge_initial_length": np.float32,
+                     "edge_mass": np.float32, "edge_stiffness": np.float32,
+                     "edge_bend": np.float32, "rest_bend_angle": np.float32,
+                     "vertex_ghat": np.float32, "vertex_offset": np.float32,
+                     "vertex_friction": np.float32}
 
     def array(self, name: str) -> np.ndarray:
         """A named array of the built DataSet (ppf_scene_array): topology

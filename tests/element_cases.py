@@ -128,6 +128,33 @@ def gen_hinge(rng, n):
     return out
 
 
+def gen_rod(rng, n):
+    """Rod edges stretched and compressed against their rest length, and rod
+    vertices bent from straight (including exactly and nearly collinear
+    triples) to folded, with straight and bent rest angles."""
+    out = []
+    for i in range(n):
+        x0 = rng.normal(0, 0.01, 3)
+        d = rng.normal(0, 1, 3)
+        d /= np.linalg.norm(d)
+        l0 = rng.uniform(0.005, 0.02)
+        x1 = x0 + d * l0 * rng.uniform(0.7, 1.3)
+        ang = [np.pi, np.pi - 1e-4, rng.uniform(0.3, np.pi)][i % 3]
+        a = rng.normal(0, 1, 3)
+        a /= np.linalg.norm(a)
+        b = np.cross(a, rng.normal(0, 1, 3))
+        b /= np.linalg.norm(b)
+        la, lb = rng.uniform(0.005, 0.02, 2)
+        c = rng.normal(0, 0.01, 3)
+        p0 = c + la * a
+        p2 = c + lb * (np.cos(ang) * a + np.sin(ang) * b)
+        rest = [np.pi, rng.uniform(1.0, np.pi), rng.uniform(0.5, 2.5)][i % 3]
+        out.append({"x0": x0.astype(f32), "x1": x1.astype(f32), "l0": f32(l0),
+                    "w": f32(10 ** rng.uniform(-2, 3)),
+                    "b": np.stack([p0, c, p2]).astype(f32), "rest": f32(rest)})
+    return out
+
+
 def gen_sym(rng, n):
     out = []
     for i in range(n):
@@ -306,6 +333,17 @@ def evaluate(lib, prefix, rng_seed=7, n=64):
         f.restype = C.c_int
         r = f(_ptr(c["e"][0]), _ptr(c["e"][1]), _ptr(c["t"][0]), _ptr(c["t"][1]), _ptr(c["t"][2]))
         rec("isect", i, hit=[float(r)])
+    for i, c in enumerate(gen_rod(rng, n)):
+        g6, h36 = np.zeros(6, f32), np.zeros(36, f32)
+        f = fn("hook")
+        f.argtypes = [C.POINTER(C.c_float)] * 2 + [C.c_float] * 2 + [C.POINTER(C.c_float)] * 2
+        f(_ptr(c["x0"]), _ptr(c["x1"]), c["l0"], c["w"], _ptr(g6), _ptr(h36))
+        f9, h81 = np.zeros(9, f32), np.zeros(81, f32)
+        f = fn("strand")
+        f.argtypes = [C.POINTER(C.c_float)] * 3 + [C.c_float] + [C.POINTER(C.c_float)] * 2
+        bx = np.ascontiguousarray(c["b"])
+        f(_ptr(bx[0]), _ptr(bx[1]), _ptr(bx[2]), c["rest"], _ptr(f9), _ptr(h81))
+        rec("rod", i, stretch_g=g6, stretch_h=h36, bend_f=f9, bend_h=h81)
     return {k: np.stack(v) for k, v in res.items()}
 
 

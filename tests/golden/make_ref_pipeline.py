@@ -1,5 +1,6 @@
 """Freezes the reference's own Newton-system assembly, line searches and
-intersection checks on the two-sheets scene.
+intersection checks on the two-sheets scene, and its assembly and rod
+strain-limit line search on the rods-and-sheet scene (ref_rods.npz).
 
 Builds oracle/_ref/libppfref_pipe.so from the reference sources
 (oracle/Makefile), drives it through the states of
@@ -50,6 +51,33 @@ def main():
     path = Path(__file__).parent / "ref_pipeline.npz"
     np.savez_compressed(path, **out)
     print("wrote", len(out), "arrays,", path.stat().st_size, "bytes")
+    rods(ref)
+
+
+def rods(ref):
+    """The rods-and-sheet scene's first Newton system at its start state, as
+    the reference assembles it (rod stretch, bending and strain limit with
+    damping, shell membrane and bending with damping, contact), and the rod
+    strain-limit line search toward a 3 % stretch of rod A."""
+    sc, info = step_scenes.rods_and_sheet()
+    prm = sc.param.contents
+    assert ref.refpipe_init(sc.dataset, C.byref(prm))
+    curr, prev = (a.reshape(-1).copy() for a in sc.positions())
+    target = rpc.step_target(sc, curr, prev)
+    dt = float(np.float32(prm.dt) * np.float32(prm.playback))
+    keys, blocks, force, count = rpc.reference_first_system(ref, curr, prev, prm, target, dt)
+    out = {"keys": keys, "blocks": blocks.astype(np.float32), "force": force,
+           "contacts": np.uint32(count), "target": target}
+    a0, na = info["rod_a"]
+    x1 = curr.reshape(-1, 3).copy()
+    c = x1[a0:a0 + na].mean(axis=0)
+    x1[a0:a0 + na] = c + 1.03 * (x1[a0:a0 + na] - c)
+    x1 = x1.reshape(-1).astype(np.float32)
+    out["rod_ls"] = np.array([ref.refpipe_rod_strain_line_search(curr, x1)], np.float32)
+    out["rod_ls_x1"] = x1
+    path = Path(__file__).parent / "ref_rods.npz"
+    np.savez_compressed(path, **out)
+    print("wrote", len(out), "arrays,", path.stat().st_size, "bytes", "contacts", count)
 
 
 if __name__ == "__main__":

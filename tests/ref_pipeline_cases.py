@@ -69,6 +69,23 @@ def oracle_first_system(o):
             blocks, sysd["force"].reshape(-1).copy())
 
 
+def step_target(sc, curr, prev):
+    """The inertial target of a step from (curr, prev) as the library and the
+    reference compute it in float32 (main.cu:491-511): x + (x - x_prev)
+    dt / dt_prev + dt^2 g for free vertices (the scenes used here have no
+    pins)."""
+    p = sc.param.contents
+    f32 = np.float32
+    dt = f32(p.dt) * f32(p.playback)
+    tr = dt / f32(p.prev_dt)
+    h2 = dt * dt
+    g = np.array([p.gravity.v[0], p.gravity.v[1], p.gravity.v[2]], f32)
+    x1 = curr.reshape(-1, 3).astype(f32)
+    x0 = prev.reshape(-1, 3).astype(f32)
+    y = (x1 - x0) * tr + h2 * g
+    return (x1 + y).reshape(-1).astype(f32)
+
+
 def reference_first_system(lib, curr, prev, prm, target, dt):
     lib.refpipe_state(curr, prev, C.byref(prm))
     count = lib.refpipe_assemble(curr, target, dt)

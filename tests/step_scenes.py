@@ -94,3 +94,64 @@ def strain_of(x, rest, faces):
     Ds = np.stack([x[f[:, 1]] - x[f[:, 0]], x[f[:, 2]] - x[f[:, 0]]], 2)  # [F,3,2]
     F = Ds @ np.linalg.inv(Dm)
     return np.linalg.svd(F, compute_uv=False)[:, 0]
+
+
+def rod_material(**kw):
+    from ppf_gb300.session import RodMaterial
+
+    base = dict(density=0.01, young_mod=1e4, bend=0.5, contact_gap=1e-3, friction=0.3,
+                strain_limit=0.01)
+    base.update(kw)
+    return RodMaterial(**base)
+
+
+def rods_and_sheet(seed: int = 4):
+    """Three rods and a sheet, every rod term active in the first Newton
+    system: rod A lies across the sheet inside its contact gap, stretched
+    0.4 % (the rod strain limit is 1 %) and damped; rod B is a zigzag that
+    keeps its bent rest shape, crossing rod A within the gap and falling;
+    rod C hangs off the sheet's edge with bending damping. The sheet has
+    membrane and bending damping. No pins: the system before and after the
+    Dirichlet elimination is the same."""
+    rng = np.random.default_rng(seed)
+    mat = scenes.cloth_material()
+    mat.deform_damping = 0.05
+    mat.bend_damping = 0.02
+    sc = Scene()
+    v, f = meshes.grid(10, 10, 0.2, 0.2)
+    v = v.astype(np.float64)
+    v[:, 1] = 0.5 + rng.uniform(-2e-5, 2e-5, len(v))
+    sc.add_shell(v.astype(np.float32), f, mat)
+    # rod A: along x across the sheet, 6e-4 above it
+    na = 24
+    xa = np.stack([np.linspace(-0.12, 0.12, na), np.full(na, 0.5 + 6e-4),
+                   np.linspace(-0.01, 0.013, na)], 1)
+    ea = np.stack([np.arange(na - 1), np.arange(1, na)], 1)
+    a0 = sc.add_rod(xa.astype(np.float32), ea, rod_material(deform_damping=0.1))
+    # rod B: zigzag along z, crossing rod A 7e-4 above it
+    nb = 16
+    zb = np.linspace(-0.08, 0.08, nb)
+    xb = np.stack([0.01 + 0.006 * (np.arange(nb) % 2), np.full(nb, 0.5 + 13e-4), zb], 1)
+    eb = np.stack([np.arange(nb - 1), np.arange(1, nb)], 1)
+    b0 = sc.add_rod(xb.astype(np.float32), eb,
+                    rod_material(bend=2.0, bend_rest_from_geometry=True, bend_damping=0.05))
+    # rod C: off the sheet's edge, bent downward
+    nc = 12
+    t = np.linspace(0.0, 1.0, nc)
+    xc = np.stack([0.105 + 0.05 * t, 0.5 - 0.03 * t * t, np.full(nc, 0.02)], 1)
+    ec = np.stack([np.arange(nc - 1), np.arange(1, nc)], 1)
+    sc.add_rod(xc.astype(np.float32), ec, rod_material(bend=1.0, bend_damping=0.1))
+    n = sc.vertex_count
+    vel = np.zeros((n, 3), np.float32)
+    vel[b0:b0 + nb] = (0.0, -0.2, 0.05)
+    vel[:a0] = (0.0, -0.05, 0.0)
+    sc.set_velocity(vel)
+    sc.add_floor((0.0, 0.3, 0.0), contact_gap=1e-3, friction=0.5)
+    built = sc.build(scenes._param(0.01))
+    # stretch rod A by 0.4 % about its centre (its strain barrier is active)
+    curr, prev = built.positions()
+    c = curr[a0:a0 + na].mean(axis=0)
+    curr[a0:a0 + na] = c + 1.004 * (curr[a0:a0 + na] - c)
+    prev[a0:a0 + na] = c + 1.004 * (prev[a0:a0 + na] - c)
+    built.set_positions(curr, prev)
+    return built, {"rod_a": (a0, na), "rod_b": (b0, nb)}
