@@ -86,6 +86,14 @@ unsigned ppf_scene_add_shell_faces(PpfScene *scene, const float *vertices, unsig
  * edges. Returns the global index of the first vertex. */
 unsigned ppf_scene_add_rod(PpfScene *scene, const float *vertices, unsigned nv,
                            const unsigned *edges, unsigned ne, const PpfRodMaterial *mat);
+/* Rod edges between vertices already added (global indices, 2 per edge),
+ * edge i with materials[edge_material[i]]: the reference scene's rod.bin and
+ * per-rod rod-* parameter arrays over its shared vertex array
+ * (scene.rs:512-719, 1540-1655). Returns 0, or -1 when an index is out of
+ * range (nothing is added then). */
+int ppf_scene_add_rod_edges(PpfScene *scene, const unsigned *edges, unsigned ne,
+                            const unsigned *edge_material, const PpfRodMaterial *materials,
+                            unsigned n_materials);
 /* Initial velocity of every vertex (3 floats each); prev = curr - v dt. */
 void ppf_scene_set_velocity(PpfScene *scene, const float *velocity);
 /* Fix pins at the vertices' current positions. kinematic != 0 marks pins

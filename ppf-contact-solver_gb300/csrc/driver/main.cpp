@@ -246,9 +246,9 @@ Loaded load_scene(const std::string &path) {
     auto count = [&](const char *k) { return (unsigned)num(info, C, k, 0.0, true); };
     const unsigned n_vert = count("vert"), n_tri = count("tri"), n_sv = count("static_vert"),
                    n_st = count("static_tri"), n_pin = count("pin_block"),
-                   n_wall = count("wall"), n_sphere = count("sphere");
-    if (count("rod") || count("tet") || count("stitch"))
-        die("rods, tets and stitches are not simulated by this library");
+                   n_wall = count("wall"), n_sphere = count("sphere"), n_rod = count("rod");
+    if (count("tet") || count("stitch"))
+        die("tets and stitches are not simulated by this library");
     const double ws = num(prm, "param", "world_scaling", 1.0);
     if (!(ws > 0.0)) die("world_scaling must be > 0");
     L.world_scaling = (float)ws;
@@ -299,12 +299,54 @@ Loaded load_scene(const std::string &path) {
     }
     L.scene = ppf_scene_create();
     L.n_vert = n_vert;
-    if (n_tri) {
-        if (ppf_scene_add_shell_faces(L.scene, x.data(), n_vert, tri.data(), n_tri, fmat.data(),
-                                      mats.data(), (unsigned)mats.size()) == 0xFFFFFFFFu)
-            die("bad face material table");
-    } else {
-        die("the scene has no shell faces");
+    if (!n_tri && !n_rod) die("the scene has neither shell faces nor rods");
+    // every vertex is added with the shells (faces may be none)
+    if (ppf_scene_add_shell_faces(L.scene, x.data(), n_vert, tri.data(), n_tri, fmat.data(),
+                                  mats.data(), (unsigned)mats.size()) == 0xFFFFFFFFu)
+        die("bad face material table");
+    if (n_rod) {
+        // rods over the shared vertex array: bin/rod.bin and the per-rod
+        // bin/param/rod-<name>.bin arrays (scene.rs:512-719, 1540-1655)
+        const auto rod64 = read_bin<uint64_t>(B + "rod.bin");
+        if (rod64.size() != 2 * (size_t)n_rod) die("rod.bin does not match count.rod");
+        std::vector<unsigned> rod(rod64.begin(), rod64.end());
+        std::map<std::string, std::vector<float>> rp;
+        for (const char *k : {"density", "young-mod", "bend", "length-factor", "strain-limit",
+                              "contact-gap", "contact-offset", "friction", "deformation-damping",
+                              "bending-damping", "bend-rest-from-geometry"}) {
+            auto v = read_bin<float>(B + "param/rod-" + k + ".bin", false);
+            if (!v.empty()) {
+                if (v.size() != n_rod) die(std::string("rod-") + k + ".bin does not match count.rod");
+                rp[k] = v;
+            }
+        }
+        std::vector<PpfRodMaterial> rmats;
+        std::vector<unsigned> rmat(n_rod);
+        for (unsigned i = 0; i < n_rod; ++i) {
+            auto get = [&](const char *name, float dflt) {
+                auto it = rp.find(name);
+                return it == rp.end() ? dflt : it->second[i];
+            };
+            PpfRodMaterial m{};
+            m.density = get("density", 1.0f);
+            m.young_mod = get("young-mod", 1000.0f);
+            m.bend = get("bend", 0.0f);
+            m.length_factor = get("length-factor", 1.0f);
+            m.strain_limit = get("strain-limit", 0.0f);
+            m.contact_gap = get("contact-gap", 1e-3f);
+            m.contact_offset = get("contact-offset", 0.0f);
+            m.friction = get("friction", 0.0f);
+            m.deform_damping = get("deformation-damping", 0.0f);
+            m.bend_damping = get("bending-damping", 0.0f);
+            m.bend_rest_from_geometry = get("bend-rest-from-geometry", 0.0f) != 0.0f;
+            unsigned k = 0;
+            while (k < rmats.size() && std::memcmp(&rmats[k], &m, sizeof(m)) != 0) ++k;
+            if (k == rmats.size()) rmats.push_back(m);
+            rmat[i] = k;
+        }
+        if (ppf_scene_add_rod_edges(L.scene, rod.data(), n_rod, rmat.data(), rmats.data(),
+                                    (unsigned)rmats.size()) != 0)
+            die("rod.bin names a vertex past count.vert");
     }
     std::vector<float> v3(vel.begin(), vel.end());
     for (float &c : v3) c = (float)(c * ws);
@@ -504,11 +546,12 @@ int main(int argc, char **argv) {
     if (describe) {
         // the scene as read, without a GPU: one "key value" per line
         const PpfConstraint &c = ds->constraint;
-        std::printf("vertices %u\nfaces %u\nedges %u\nhinges %u\nfix %u\npull %u\n"
+        std::printf("vertices %u\nfaces %u\nrods %u\nedges %u\nhinges %u\nfix %u\npull %u\n"
                     "spheres %u\nfloors %u\ncollision_vertices %u\ncollision_faces %u\n"
                     "face_params %u\ndt %.9g\nframes %d\nfps %.9g\nauto_save %d\n"
                     "gravity %.9g %.9g %.9g\ncg_tol %.9g\n",
-                    ds->vertex.curr.size, ds->mesh.mesh.face.size, ds->mesh.mesh.edge.size,
+                    ds->vertex.curr.size, ds->mesh.mesh.face.size, ds->rod_count,
+                    ds->mesh.mesh.edge.size,
                     ds->mesh.mesh.hinge.size, c.fix.size, c.pull.size, c.sphere.size,
                     c.floor.size, c.mesh.vertex.size, c.mesh.face.size,
                     ds->param_arrays.face.size, param->dt, L.frames, L.fps, L.auto_save,

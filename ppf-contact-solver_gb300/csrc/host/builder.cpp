@@ -205,10 +205,24 @@ unsigned ppf_scene_add_rod(PpfScene *s, const float *v, unsigned nv, const unsig
     return base;
 }
 
+int ppf_scene_add_rod_edges(PpfScene *s, const unsigned *e, unsigned ne,
+                            const unsigned *edge_material, const PpfRodMaterial *materials,
+                            unsigned n_materials) {
+    const unsigned n = (unsigned)s->x.size() / 3;
+    for (unsigned i = 0; i < ne; ++i)
+        if (e[2 * i] >= n || e[2 * i + 1] >= n || edge_material[i] >= n_materials) return -1;
+    const unsigned base = (unsigned)s->rod_materials.size();
+    s->rod_materials.insert(s->rod_materials.end(), materials, materials + n_materials);
+    s->rods.insert(s->rods.end(), e, e + 2 * ne);
+    for (unsigned i = 0; i < ne; ++i) s->rod_material.push_back(base + edge_material[i]);
+    s->built = false;
+    return 0;
+}
+
 unsigned ppf_scene_add_shell_faces(PpfScene *s, const float *v, unsigned nv, const unsigned *f,
                                    unsigned nf, const unsigned *face_material,
                                    const PpfShellMaterial *materials, unsigned n_materials) {
-    if (n_materials == 0) return 0xFFFFFFFFu;
+    if (n_materials == 0 && nf > 0) return 0xFFFFFFFFu;
     for (unsigned i = 0; i < nf; ++i)
         if (face_material[i] >= n_materials) return 0xFFFFFFFFu;
     unsigned base = (unsigned)s->x.size() / 3;

@@ -4,7 +4,8 @@ solver executable (csrc/driver/main.cpp).
 `write_session` writes the subset of the layout the reference's frontend
 exports (frontend/_scene_.py:806-1000, read back by crates/ppf-cts-solver/
 src/scene.rs:443-1110) that this library simulates: shells with per-face
-materials, fix and pull pins without operations, one-keyframe walls and
+materials, rods with per-rod materials, fix and pull pins without
+operations, one-keyframe walls and
 spheres, and a static collision mesh; info.toml and param.toml as the
 frontend writes them. `read_frame` reads a vert_<n>.bin the executable
 wrote.
@@ -51,6 +52,8 @@ class SessionScene:
     static_tri: np.ndarray | None = None
     static_params: dict = field(default_factory=dict)  # name -> (Fs,) float32
     param: dict = field(default_factory=dict)          # [param] keys of param.toml
+    rod: np.ndarray | None = None        # (R, 2) vertex indices of rod edges
+    rod_params: dict = field(default_factory=dict)     # name -> (R,) float32, e.g. "bend"
 
 
 def _toml_value(v):
@@ -68,9 +71,10 @@ def write_session(path, sc: SessionScene) -> Path:
     b = path / "bin"
     (b / "param").mkdir(parents=True, exist_ok=True)
     n, nf = len(sc.vert), len(sc.tri)
+    nr = 0 if sc.rod is None else len(sc.rod)
     ns = 0 if sc.static_vert is None else len(sc.static_vert)
     nst = 0 if sc.static_tri is None else len(sc.static_tri)
-    lines = ["[count]", f"vert = {n}", "rod = 0", f"tri = {nf}", "tet = 0",
+    lines = ["[count]", f"vert = {n}", f"rod = {nr}", f"tri = {nf}", "tet = 0",
              f"static_vert = {ns}", f"static_tri = {nst}", f"pin_block = {len(sc.pins)}",
              f"wall = {len(sc.walls)}", f"sphere = {len(sc.spheres)}", "stitch = 0",
              "rod_vert_start = 0", "rod_vert_end = 0", "shell_vert_start = 0",
@@ -108,6 +112,10 @@ def write_session(path, sc: SessionScene) -> Path:
             np.asarray(v, np.uint8).tofile(b / "param" / "tri-model.bin")
         else:
             np.asarray(v, np.float32).tofile(b / "param" / f"tri-{k}.bin")
+    if nr:
+        np.asarray(sc.rod, np.uint64).tofile(b / "rod.bin")
+        for k, v in sc.rod_params.items():
+            np.asarray(v, np.float32).tofile(b / "param" / f"rod-{k}.bin")
     if ns:
         np.asarray(sc.static_vert, np.float64).tofile(b / "static_vert.bin")
         np.zeros(ns, np.uint32).tofile(b / "static_vert_dmap.bin")

@@ -177,3 +177,69 @@ def test_driver_resumes_from_a_checkpoint(driver, tmp_path):
     # --load -1 resumes from the latest checkpoint
     r = _run(["--path", path, "--output", resumed, "--load", "-1"])
     assert r.returncode == 0, r.stderr
+
+
+def _rod_session(tmp_path, frames=6):
+    """A sheet and a rod above it, written with per-rod parameter arrays."""
+    v, f = _scene_arrays(8)
+    nr = 10
+    rv = np.stack([np.linspace(-0.2, 0.2, nr), np.full(nr, 0.47), np.full(nr, 0.01)], 1)
+    verts = np.concatenate([v, rv])
+    rod = np.stack([np.arange(nr - 1), np.arange(1, nr)], 1) + len(v)
+    mat = scenes.cloth_material()
+    nf = len(f)
+    fp = {"density": np.full(nf, mat.density), "young-mod": np.full(nf, mat.young_mod),
+          "poiss-rat": np.full(nf, mat.poiss_rat), "bend": np.full(nf, mat.bend),
+          "strain-limit": np.full(nf, mat.strain_limit),
+          "contact-gap": np.full(nf, mat.contact_gap), "friction": np.full(nf, mat.friction)}
+    r = nr - 1
+    rp = {"density": np.full(r, 0.01), "young-mod": np.full(r, 1e4), "bend": np.full(r, 0.5),
+          "length-factor": np.full(r, 1.0), "strain-limit": np.full(r, 0.01),
+          "contact-gap": np.full(r, 1e-3), "friction": np.full(r, 0.3)}
+    sc = session_io.SessionScene(
+        vert=verts, tri=f, face_params=fp, rod=rod, rod_params=rp,
+        walls=[session_io.Wall(position=(0.0, 0.0, 0.0), contact_gap=1e-3, friction=0.5)],
+        param={"dt": 0.01, "frames": frames, "fps": FPS, "auto_save": 0,
+               "gravity": [0.0, -9.8, 0.0], "cg_tol": 1e-3})
+    return session_io.write_session(tmp_path / "rods", sc), verts, f, rod
+
+
+def test_driver_reads_rods(driver, tmp_path):
+    path, verts, f, rod = _rod_session(tmp_path)
+    r = _run(["--path", path, "--describe"])
+    assert r.returncode == 0, r.stderr
+    d = dict(line.split(maxsplit=1) for line in r.stdout.splitlines())
+    assert int(d["vertices"]) == len(verts) and int(d["faces"]) == len(f)
+    assert int(d["rods"]) == len(rod)
+    assert int(d["edges"]) > len(rod)  # the rod edges, then the faces' edges
+
+
+@pytest.mark.gpu
+def test_driver_rod_frames_follow_the_library(driver, tmp_path):
+    """A session with a rod: the executable's frames are the library's
+    trajectory of the same scene built through the Python API."""
+    from ppf_gb300.session import RodMaterial
+
+    path, verts, f, rod = _rod_session(tmp_path, frames=6)
+    out = tmp_path / "out"
+    r = _run(["--path", path, "--output", out])
+    assert r.returncode == 0, r.stderr + r.stdout
+    sc = Scene()
+    v, _ = _scene_arrays(8)
+    sc.add_shell(v.astype(np.float32), f, scenes.cloth_material())
+    sc.add_rod(verts[len(v):].astype(np.float32), rod - len(v),
+               RodMaterial(density=0.01, young_mod=1e4, bend=0.5, strain_limit=0.01,
+                           contact_gap=1e-3, friction=0.3))
+    sc.add_floor((0.0, 0.0, 0.0), contact_gap=1e-3, friction=0.5)
+    sc.build(scenes._param(0.01))
+    s = Session(sc)
+    traj, times = [sc.positions()[0].copy()], [0.0]
+    while times[-1] < 6 / FPS:
+        assert s.step().success()
+        traj.append(s.positions().copy())
+        times.append(s.time)
+    for k in range(7):
+        got = session_io.read_frame(out, k)
+        want = _interp(traj, times, k / FPS)
+        moved = float(np.abs(want - traj[0]).max())
+        assert np.abs(got - want).max() <= 1e-3 * moved + 1e-7, (k, np.abs(got - want).max())
