@@ -8,8 +8,8 @@
  * crates/ppf-cts-solver/src/mesh.rs Mesh::new, and the face-edge props of
  * crates/ppf-cts-solver/src/main.rs:205-250). Covered: shells (any model
  * field, Baraff-Witkin evaluated), rods, fix pins (static or kinematic), pull
- * pins, analytic spheres and floors, static collision meshes. Not covered:
- * tets, stitches, PDRD bodies, sand grains, UV anisotropy.
+ * pins, analytic spheres and floors, static collision meshes, solids (tets).
+ * Not covered: stitches, PDRD bodies, sand grains, UV anisotropy.
  *
  * Edge and hinge order: the reference extracts them from a hash map, whose
  * iteration order is not reproducible; here they are listed in first-seen
@@ -43,6 +43,19 @@ typedef struct {
     float deform_damping; /* Rayleigh damping of the membrane (0: none) */
     float bend_damping;   /* Rayleigh damping of the bending (0: none) */
 } PpfShellMaterial;
+
+/* Per-object solid material (the reference scene's tet parameters,
+ * scene.rs:1840-1921). */
+typedef struct {
+    int model;            /* PPF_MODEL_ARAP / STVK / SNHK */
+    float density;        /* kg/m^3 */
+    float young_mod;      /* Young's modulus (pre-divided by density, as shells) */
+    float poiss_rat;      /* (0, 0.5) */
+    float contact_gap;    /* ghat of the boundary faces */
+    float contact_offset;
+    float friction;
+    float deform_damping; /* Rayleigh damping (0: none) */
+} PpfSolidMaterial;
 
 /* Per-object rod material (the reference scene's rod-* parameters,
  * scene.rs:1540-1660). */
@@ -94,6 +107,16 @@ unsigned ppf_scene_add_rod(PpfScene *scene, const float *vertices, unsigned nv,
 int ppf_scene_add_rod_edges(PpfScene *scene, const unsigned *edges, unsigned ne,
                             const unsigned *edge_material, const PpfRodMaterial *materials,
                             unsigned n_materials);
+/* Appends a solid object: nv vertices and nt tets (4 vertex indices each,
+ * local, positively oriented). Its boundary faces (the tet faces no other
+ * tet shares, outward) become contact faces after every shell face
+ * (shell_face_count stays the shells'); the vertices only tets use become
+ * the DataSet's last vertices (surface_vert_count counts the rest,
+ * mesh.rs:78-95). Vertex indices in this API stay in the order vertices were
+ * added; "vertex_order" (ppf_scene_array) maps them to DataSet indices.
+ * Returns the index of the first vertex. */
+unsigned ppf_scene_add_solid(PpfScene *scene, const float *vertices, unsigned nv,
+                             const unsigned *tets, unsigned nt, const PpfSolidMaterial *mat);
 /* Initial velocity of every vertex (3 floats each); prev = curr - v dt. */
 void ppf_scene_set_velocity(PpfScene *scene, const float *velocity);
 /* Fix pins at the vertices' current positions. kinematic != 0 marks pins
@@ -127,9 +150,10 @@ void ppf_scene_set_pin_targets(PpfScene *scene, const float *position,
                                const float *step_delta);
 unsigned ppf_scene_vertex_count(PpfScene *scene);
 /* Host copies of the built DataSet's vertex.curr / vertex.prev (3 floats per
- * vertex). fetch() writes the device state into these arrays, so after it
- * ppf_scene_positions returns the solver's state; ppf_scene_set_positions
- * overwrites them before initialize(). Either pointer may be NULL. */
+ * vertex, in the order the vertices were added). fetch() writes the device
+ * state into these arrays, so after it ppf_scene_positions returns the
+ * solver's state; ppf_scene_set_positions overwrites them before
+ * initialize(). Either pointer may be NULL. */
 void ppf_scene_positions(PpfScene *scene, float *curr, float *prev);
 void ppf_scene_set_positions(PpfScene *scene, const float *curr,
                              const float *prev);
@@ -145,6 +169,10 @@ void ppf_scene_set_positions(PpfScene *scene, const float *curr,
  * f32 per element: vertex_mass, vertex_area, face_area, face_mass,
  * edge_length, edge_initial_length, edge_mass, edge_stiffness, edge_bend,
  * rest_bend_angle (per vertex), hinge_length, hinge_area, face_mu,
+ * tet (4 u32 per tet), tet_slots (16 u32 per tet), inv_rest3x3 (9 f32 per
+ * tet, column-major), tet_mass, tet_volume, vertex_volume (f32),
+ * vertex_order (u32: DataSet index of each added vertex), face_type,
+ * hinge_type (u8, bit 0: a solid's boundary face / a hinge next to one),
  * face_lambda, hinge_bend; vertex_ghat, vertex_offset, vertex_friction (the
  * contact parameters of each vertex's param). */
 size_t ppf_scene_array(PpfScene *scene, const char *name, void *out);

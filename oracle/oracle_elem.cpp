@@ -8,6 +8,7 @@
 #include "../ppf-contact-solver_gb300/csrc/physics/accd.cuh"
 #include "../ppf-contact-solver_gb300/csrc/physics/bw.cuh"
 #include "../ppf-contact-solver_gb300/csrc/physics/contact_local.cuh"
+#include "../ppf-contact-solver_gb300/csrc/physics/elastic.cuh"
 #include "../ppf-contact-solver_gb300/csrc/physics/hinge.cuh"
 #include "../ppf-contact-solver_gb300/csrc/physics/rod.cuh"
 #include "../ppf-contact-solver_gb300/csrc/physics/strainlimit.cuh"
@@ -124,6 +125,44 @@ void orc_strand(const float *x0, const float *x1, const float *x2, float rest, f
     Mat3 f;
     Mat9 h;
     rod::bend(v3(x0), v3(x1), v3(x2), rest, f, h);
+    put(f9, f);
+    put(h81, h);
+}
+void orc_model_table(int model, int dim, const float *a, float mu, float lmd, float *deda,
+                     float *d2) {
+    if (dim == 2) {
+        elastic::Table<2> t;
+        elastic::table<2>(model, vec2(a[0], a[1]), mu, lmd, t);
+        put(deda, t.deda);
+        put(d2, t.d2);
+    } else {
+        elastic::Table<3> t;
+        elastic::table<3>(model, vec3(a[0], a[1], a[2]), mu, lmd, t);
+        put(deda, t.deda);
+        put(d2, t.d2);
+    }
+}
+void orc_svd33(const float *F9, float *U9, float *S3, float *Vt9) {
+    elastic::Svd33 s = elastic::svd3x3_rv(get<3, 3>(F9));
+    put(U9, s.U);
+    put(S3, s.S);
+    put(Vt9, s.Vt);
+}
+void orc_tet(const float *x12, const float *inv9, int model, float mu, float lmd, float mass,
+             float eps, float *f12, float *h144) {
+    Mat3x4 f;
+    Mat12 h;
+    elastic::tet(v3(x12), v3(x12 + 3), v3(x12 + 6), v3(x12 + 9), get<3, 3>(inv9), model, mu, lmd,
+                 mass, eps, f, h);
+    put(f12, f);
+    put(h144, h);
+}
+void orc_shell_model(const float *x9, const float *inv4, int model, float mu, float lmd,
+                     float mass, float eps, float *f9, float *h81) {
+    Mat3 f;
+    Mat9 h;
+    elastic::shell(v3(x9), v3(x9 + 3), v3(x9 + 6), get<2, 2>(inv4), model, mu, lmd, mass, eps, f,
+                   h);
     put(f9, f);
     put(h81, h);
 }

@@ -49,6 +49,9 @@ inline unsigned atomicAdd(unsigned *p, unsigned v) {
 #include "energy/model/dihedral_angle.hpp"
 #include "energy/model/friction.hpp"
 #include "energy/model/hook.hpp"
+#include "energy/model/arap.hpp"
+#include "energy/model/snhk.hpp"
+#include "energy/model/stvk.hpp"
 #include "energy/model/push.hpp"
 #include "linalg/eigsolve.hpp"
 #include "utility/utility.cu"
@@ -114,7 +117,7 @@ ParamSet ccd_param(float max_t, float eps) {
 
 extern "C" {
 
-int ref_wrap_version() { return 3; }
+int ref_wrap_version() { return 4; }
 
 void ref_pe_coeff(const float *p, const float *a, const float *b, float *out) {
     Vec2f c = distance::point_edge_distance_coeff<float, float>(v3(p), v3(a), v3(b));
@@ -257,6 +260,76 @@ void ref_strand(const float *x0, const float *x1, const float *x2, float rest, f
     Mat9x9f h;
     dihedral_angle::strand_compute_force_hessian(v3(x0), v3(x1), v3(x2), rest, f, h);
     put(f9, f.m, 9);
+    put(h81, h.m, 81);
+}
+// energy/model/{arap,stvk,snhk}.hpp: singular-value tables (dim 2 or 3).
+void ref_model_table(int model, int dim, const float *a, float mu, float lmd, float *deda,
+                     float *d2) {
+    if (dim == 2) {
+        Vec2f v(a[0], a[1]);
+        DiffTable2 t = model == 0 ? ARAP::make_diff_table2(v, mu, lmd)
+                       : model == 1 ? StVK::make_diff_table2(v, mu, lmd)
+                                    : SNHk::make_diff_table2(v, mu, lmd);
+        put(deda, t.deda.m, 2);
+        put(d2, t.d2ed2a.m, 4);
+    } else {
+        Vec3f v(a[0], a[1], a[2]);
+        DiffTable3 t = model == 0 ? ARAP::make_diff_table3(v, mu, lmd)
+                       : model == 1 ? StVK::make_diff_table3(v, mu, lmd)
+                                    : SNHk::make_diff_table3(v, mu, lmd);
+        put(deda, t.deda.m, 3);
+        put(d2, t.d2ed2a.m, 9);
+    }
+}
+// utility.cu:167-183: rotation-variant 3x3 SVD.
+void ref_svd33(const float *F9, float *U9, float *S3, float *Vt9) {
+    Mat3x3f F;
+    put(F.m, F9, 9);
+    Svd3x3 s = utility::svd3x3_rv(F);
+    put(U9, s.U.m, 9);
+    put(S3, s.S.m, 3);
+    put(Vt9, s.Vt.m, 9);
+}
+// energy.cu:395-446 without damping: the tet element's force and Hessian.
+void ref_tet(const float *x12, const float *inv9, int model, float mu, float lmd, float mass,
+             float eps, float *f12, float *h144) {
+    Mat3x4f X;
+    for (int k = 0; k < 4; ++k)
+        for (int d = 0; d < 3; ++d) X(d, k) = x12[3 * k + d];
+    Mat3x3f inv;
+    put(inv.m, inv9, 9);
+    Mat3x3f F = utility::compute_deformation_grad(X, inv);
+    Svd3x3 svd = utility::svd3x3_rv(F);
+    DiffTable3 table = model == 0 ? ARAP::make_diff_table3(svd.S, mu, lmd)
+                       : model == 1 ? StVK::make_diff_table3(svd.S, mu, lmd)
+                                    : SNHk::make_diff_table3(svd.S, mu, lmd);
+    Mat3x3f dedF = eigenanalysis::compute_force(table, svd);
+    Mat3x4f dedx = Mat3x4f::Zero();
+    Mat12x12f h = Mat12x12f::Zero();
+    dedx += mass * utility::convert_force(dedF, inv);
+    eigenanalysis::accumulate_hessian_tet_fused(table, svd, eps, inv, mass, h);
+    put(f12, dedx.m, 12);
+    put(h144, h.m, 144);
+}
+// energy.cu:336-355: a shell face under ARAP / StVK / SNHk.
+void ref_shell_model(const float *x9, const float *inv4, int model, float mu, float lmd,
+                     float mass, float eps, float *f9, float *h81) {
+    Mat3x3f X;
+    put(X.m, x9, 9);
+    Mat2x2f inv;
+    put(inv.m, inv4, 4);
+    Mat3x2f F = utility::compute_deformation_grad(X, inv);
+    const Svd3x2 svd = utility::svd3x2(F);
+    DiffTable2 table = model == 0 ? ARAP::make_diff_table2(svd.S, mu, lmd)
+                       : model == 1 ? StVK::make_diff_table2(svd.S, mu, lmd)
+                                    : SNHk::make_diff_table2(svd.S, mu, lmd);
+    Mat3x2f dedF = eigenanalysis::compute_force(table, svd);
+    Mat6x6f d2edF2 = eigenanalysis::compute_hessian(table, svd, eps);
+    Mat3x3f dedx = Mat3x3f::Zero();
+    Mat9x9f h = Mat9x9f::Zero();
+    dedx += mass * utility::convert_force(dedF, inv);
+    h += mass * utility::convert_hessian(d2edF2, inv);
+    put(f9, dedx.m, 9);
     put(h81, h.m, 81);
 }
 void ref_symm2(const float *A4, float *val, float *vec) {

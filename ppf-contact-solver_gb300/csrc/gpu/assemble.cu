@@ -6,6 +6,7 @@
 // -> Dirichlet elimination. Element formulas live in ../physics (shared with
 // the CPU oracle); these kernels gather, evaluate and scatter.
 #include "../physics/bw.cuh"
+#include "../physics/elastic.cuh"
 #include "../physics/hinge.cuh"
 #include "../physics/rod.cuh"
 #include "../physics/strainlimit.cuh"
@@ -134,7 +135,7 @@ __device__ __forceinline__ void scatter_blocks(float *fixed_val, const unsigned 
 
 __global__ void k_face_energy(Scene s, StepParams p, AssemblyBuffers b) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= s.nf) return;
+    if (i >= s.nf_shell) return;
     const PpfFaceProp &pr = s.fprop[i];
     if (pr.fixed || pr.rest_excluded || pr.collider) return;
     const PpfFaceParam &fp = s.fparam[pr.param_index];
@@ -142,8 +143,14 @@ __global__ void k_face_energy(Scene s, StepParams p, AssemblyBuffers b) {
     const unsigned *f = s.face + 3 * i;
     Mat3 dedx;
     Mat9 H;
-    bw::membrane(X(b.x, f[0]), X(b.x, f[1]), X(b.x, f[2]),
-                 load_inv_rest(s.inv_rest + 4 * i), fp.mu, fp.lambda, pr.mass, dedx, H);
+    if (fp.model == PPF_MODEL_BARAFF_WITKIN) {
+        bw::membrane(X(b.x, f[0]), X(b.x, f[1]), X(b.x, f[2]),
+                     load_inv_rest(s.inv_rest + 4 * i), fp.mu, fp.lambda, pr.mass, dedx, H);
+    } else if (!elastic::shell(X(b.x, f[0]), X(b.x, f[1]), X(b.x, f[2]),
+                               load_inv_rest(s.inv_rest + 4 * i), fp.model, fp.mu, fp.lambda,
+                               pr.mass, p.eiganalysis_eps, dedx, H)) {
+        return;
+    }
     if (fp.deform_damping > 0.0f) { // energy.cu:359-360
         const unsigned v[3] = {f[0], f[1], f[2]};
         damping::stiffness<3>(fp.deform_damping, p.dt, step_displacement<3>(b, v), dedx, H);
@@ -163,7 +170,7 @@ __global__ void k_hinge_energy(Scene s, StepParams p, AssemblyBuffers b) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.nh) return;
     const PpfHingeProp &pr = s.hprop[i];
-    if (pr.fixed || pr.collider) return;
+    if (pr.fixed || pr.collider || (s.hinge_type[i] & 1u)) return;
     const PpfHingeParam &hp = s.hparam[pr.param_index];
     const unsigned *h = s.hinge + 4 * i;
     float rho = 0.0f;
@@ -254,10 +261,31 @@ __global__ void k_rod_bend(Scene s, StepParams p, AssemblyBuffers b) {
     scatter_blocks<3>(b.fixed_val, s.bend_slot + 9 * (size_t)i, H);
 }
 
+// ---- solids (energy.cu:395-446) ------------------------------------------------
+__global__ void k_tet_energy(Scene s, StepParams p, AssemblyBuffers b) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.nt) return;
+    const PpfTetProp &pr = s.tprop[i];
+    if (pr.fixed || pr.rest_excluded) return;
+    const PpfTetParam &tp = s.tparam[pr.param_index];
+    if (!(tp.mu > 0.0f)) return;
+    const unsigned v[4] = {s.tet[4 * i], s.tet[4 * i + 1], s.tet[4 * i + 2], s.tet[4 * i + 3]};
+    const Mat3 inv = load_mat3(s.inv_rest3 + 9 * (size_t)i);
+    Mat3x4 dedx;
+    Mat12 H;
+    if (!elastic::tet(X(b.x, v[0]), X(b.x, v[1]), X(b.x, v[2]), X(b.x, v[3]), inv, tp.model,
+                      tp.mu, tp.lambda, pr.mass, p.eiganalysis_eps, dedx, H))
+        return;
+    if (tp.deform_damping > 0.0f)
+        damping::stiffness<4>(tp.deform_damping, p.dt, step_displacement<4>(b, v), dedx, H);
+    for (int a = 0; a < 4; ++a) atomic_add3(b.force + 3 * v[a], dedx.col(a));
+    scatter_blocks<4>(b.fixed_val, s.tet_slot + 16 * (size_t)i, H);
+}
+
 // ---- strain-limit barrier (strainlimiting.cu:46-98) -------------------------
 __global__ void k_strain_limit(Scene s, StepParams p, AssemblyBuffers b) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= s.nf) return;
+    if (i >= s.nf_shell) return;
     const PpfFaceProp &pr = s.fprop[i];
     const PpfFaceParam &fp = s.fparam[pr.param_index];
     if (pr.fixed || pr.rest_excluded || !(fp.strainlimit > 0.0f)) return;
@@ -1067,8 +1095,12 @@ void launch_elastic(const Scene &s, const StepParams &p, const AssemblyBuffers &
         k_rod_energy<<<div_up(s.nr, kB), kB, 0, q>>>(s, p, b);
         PPF_LAUNCH_CHECK();
     }
-    if (s.nf) {
-        k_face_energy<<<div_up(s.nf, kB), kB, 0, q>>>(s, p, b);
+    if (s.nf_shell) {
+        k_face_energy<<<div_up(s.nf_shell, kB), kB, 0, q>>>(s, p, b);
+        PPF_LAUNCH_CHECK();
+    }
+    if (s.nt) {
+        k_tet_energy<<<div_up(s.nt, kB), kB, 0, q>>>(s, p, b);
         PPF_LAUNCH_CHECK();
     }
     if (s.nh) {
@@ -1079,8 +1111,8 @@ void launch_elastic(const Scene &s, const StepParams &p, const AssemblyBuffers &
 
 void launch_strain_limit(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
                          cudaStream_t q) {
-    if (s.nf) {
-        k_strain_limit<<<div_up(s.nf, kB), kB, 0, q>>>(s, p, b);
+    if (s.nf_shell) {
+        k_strain_limit<<<div_up(s.nf_shell, kB), kB, 0, q>>>(s, p, b);
         PPF_LAUNCH_CHECK();
     }
     if (s.nr) {

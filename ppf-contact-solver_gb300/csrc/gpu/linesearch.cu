@@ -403,7 +403,7 @@ __global__ void k_fold_vertex_toi(IterStatus *st) {
 
 __global__ void k_strain_ls(Scene s, LineSearchArgs a) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= s.nf) return;
+    if (i >= s.nf_shell) return;
     float t = a.max_t;
     const PpfFaceProp &pr = s.fprop[i];
     const PpfFaceParam &fp = s.fparam[pr.param_index];
@@ -618,8 +618,8 @@ void launch_constraint_line_search(const Scene &s, const LineSearchArgs &a, cuda
 }
 
 void launch_strain_line_search(const Scene &s, const LineSearchArgs &a, cudaStream_t q) {
-    if (s.nf) {
-        k_strain_ls<<<div_up(s.nf, kB), kB, 0, q>>>(s, a);
+    if (s.nf_shell) {
+        k_strain_ls<<<div_up(s.nf_shell, kB), kB, 0, q>>>(s, a);
         PPF_LAUNCH_CHECK();
     }
     if (s.nr) {

@@ -45,7 +45,15 @@ struct CsrView {
 // Everything a kernel needs to read the scene (device pointers, by value).
 struct Scene {
     unsigned n, n_surf, nf, ne, nh;
-    unsigned nr; // rod edges: edges 0 .. nr-1
+    unsigned nr;       // rod edges: edges 0 .. nr-1
+    unsigned nf_shell; // shell faces: faces 0 .. nf_shell-1 (then solids' boundary faces)
+    unsigned nt;       // tets
+    const unsigned *tet;          // 4 per tet
+    const PpfTetProp *tprop;
+    const PpfTetParam *tparam;
+    const float *inv_rest3;       // 9 per tet, column-major
+    const unsigned *tet_slot;     // 16 per tet
+    const unsigned char *hinge_type; // bit 0: next to a solid's face (no bending)
     const unsigned *face;
     const unsigned *edge;
     const unsigned *hinge;

@@ -196,6 +196,14 @@ Scene Solver::scene() const {
     s.ne = ne_;
     s.nh = nh_;
     s.nr = nr_;
+    s.nf_shell = nf_shell_;
+    s.nt = nt_;
+    s.tet = tet_.data();
+    s.tprop = tprop_.data();
+    s.tparam = tparam_.data();
+    s.inv_rest3 = inv_rest3_.data();
+    s.tet_slot = tet_slot_.data();
+    s.hinge_type = hinge_type_.data();
     s.face = face_.data();
     s.edge = edge_.data();
     s.hinge = hinge_.data();
@@ -431,8 +439,10 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     ne_ = ds->mesh.mesh.edge.size;
     nh_ = ds->mesh.mesh.hinge.size;
     nr_ = std::min(ds->rod_count, ne_);
-    if (ds->mesh.mesh.tet.size)
-        throw FatalError(4, "tets are not simulated by this library");
+    nf_shell_ = std::min(ds->shell_face_count, nf_);
+    nt_ = ds->mesh.mesh.tet.size;
+    if (nt_ && ds->inv_rest3x3.size != nt_)
+        throw FatalError(4, "inv_rest3x3 does not match the tets");
     if (ds->constraint.stitch.size)
         throw FatalError(4, "stitches are not simulated by this library");
     if (!q_) PPF_CUDA(cudaStreamCreateWithFlags(&q_, cudaStreamNonBlocking));
@@ -537,6 +547,29 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     }
     upload(edge_slot_, es);
     upload(bend_slot_, bs);
+    // tets: topology, props, params, inverse rest matrices, 16 slots each
+    {
+        const unsigned *T = (const unsigned *)ds->mesh.mesh.tet.data;
+        upload(tet_, T, 4 * (size_t)nt_);
+        upload(tprop_, ds->prop.tet.data, nt_);
+        upload(tparam_, ds->param_arrays.tet.data, ds->param_arrays.tet.size);
+        upload(inv_rest3_, (const float *)ds->inv_rest3x3.data, 9 * (size_t)nt_);
+        std::vector<unsigned> ts(16 * (size_t)nt_);
+        for (unsigned t = 0; t < nt_; ++t)
+            for (int a = 0; a < 4; ++a)
+                for (int b = 0; b < 4; ++b) {
+                    const unsigned sl = slot_of(T[4 * t + a], T[4 * t + b]);
+                    if (T[4 * t + a] <= T[4 * t + b] && sl == kSentinel)
+                        throw FatalError(4, "fixed pattern lacks a tet block");
+                    ts[16 * t + 4 * a + b] = sl;
+                }
+        upload(tet_slot_, ts);
+        std::vector<unsigned char> ht(nh_, 0);
+        const PpfVecChar &hty = ds->mesh.type.hinge;
+        for (unsigned h = 0; h < nh_ && hty.data && h < hty.size; ++h)
+            ht[h] = (unsigned char)hty.data[h];
+        upload(hinge_type_, ht);
+    }
     // per-primitive margins 0.5 ghat + offset
     std::vector<float> mf(nf_), me(ne_), mv(n_);
     for (unsigned i = 0; i < nf_; ++i) {
@@ -667,6 +700,14 @@ void Solver::update_constraint(const PpfConstraint *c) {
     for (unsigned i = 0; i < nh_; ++i)
         h_hprop_[i].fixed = fixed(H[4 * i]) && fixed(H[4 * i + 1]) && fixed(H[4 * i + 2]) &&
                             fixed(H[4 * i + 3]);
+    if (nt_) {
+        const unsigned *T = (const unsigned *)host->mesh.mesh.tet.data;
+        PpfTetProp *tp = host->prop.tet.data;
+        for (unsigned i = 0; i < nt_; ++i)
+            tp[i].fixed = fixed(T[4 * i]) && fixed(T[4 * i + 1]) && fixed(T[4 * i + 2]) &&
+                          fixed(T[4 * i + 3]);
+        upload(tprop_, tp, nt_);
+    }
     upload_props();
     // mirror into the host DataSet props, as the reference does
     std::memcpy(host->prop.vertex.data, h_vprop_.data(), n_ * sizeof(PpfVertexProp));
@@ -685,6 +726,18 @@ void Solver::update_rest_shape(const PpfRestShapeUpdate *u) {
         for (unsigned i = 0; i < u->exclude_face.size && i < nf_; ++i)
             h_fprop_[i].rest_excluded = u->exclude_face.data[i] != 0;
         upload(fprop_, h_fprop_);
+    }
+    if (u->inv_rest3x3.size && nt_) {
+        const size_t k = std::min<size_t>(u->inv_rest3x3.size, nt_);
+        PPF_CUDA(cudaMemcpy(inv_rest3_.data(), u->inv_rest3x3.data, k * sizeof(PpfMat3x3f),
+                            cudaMemcpyHostToDevice));
+        g_h2d_bytes += k * sizeof(PpfMat3x3f);
+    }
+    if (u->exclude_tet.size && nt_) {
+        PpfTetProp *tp = host->prop.tet.data;
+        for (unsigned i = 0; i < u->exclude_tet.size && i < nt_; ++i)
+            tp[i].rest_excluded = u->exclude_tet.data[i] != 0;
+        upload(tprop_, tp, nt_);
     }
 }
 

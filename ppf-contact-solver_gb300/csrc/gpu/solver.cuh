@@ -106,7 +106,7 @@ class Solver {
     void line_search_stage();
     void read_status();
 
-    unsigned n_ = 0, n_surf_ = 0, nf_ = 0, ne_ = 0, nh_ = 0, nr_ = 0;
+    unsigned n_ = 0, n_surf_ = 0, nf_ = 0, ne_ = 0, nh_ = 0, nr_ = 0, nf_shell_ = 0, nt_ = 0;
     cudaStream_t q_ = nullptr;
     // topology / props / params
     DevBuf<unsigned> face_, edge_, hinge_;
@@ -122,7 +122,11 @@ class Solver {
     DevBuf<unsigned> vf_off_, vf_, ve_off_, ve_, ef_off_, ef_;
     DevBuf<unsigned> fixed_off_, fixed_col_, fixed_tr_off_, fixed_diag_;
     DevBuf<uint2> fixed_tr_;
-    DevBuf<unsigned> face_slot_, hinge_slot_, edge_slot_, bend_slot_, dof_mask_;
+    DevBuf<unsigned> face_slot_, hinge_slot_, edge_slot_, bend_slot_, dof_mask_, tet_, tet_slot_;
+    DevBuf<PpfTetProp> tprop_;
+    DevBuf<PpfTetParam> tparam_;
+    DevBuf<float> inv_rest3_;
+    DevBuf<unsigned char> hinge_type_;
     DevBuf<PpfFixPair> fix_;
     DevBuf<PpfPullPair> pull_;
     DevBuf<PpfSphere> sphere_;

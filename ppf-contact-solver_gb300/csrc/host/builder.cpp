@@ -80,6 +80,19 @@ struct PpfScene {
     std::vector<unsigned> rods;           // 2 R, global vertex indices
     std::vector<unsigned> rod_material;   // per rod edge
     std::vector<PpfRodMaterial> rod_materials;
+    std::vector<unsigned> tets;           // 4 T, global vertex indices
+    std::vector<unsigned> tet_material;   // per tet
+    std::vector<PpfSolidMaterial> solid_materials;
+    std::vector<unsigned> solid_faces;    // 3 per boundary face of the solids
+    std::vector<unsigned> solid_face_material;
+
+    // vertex order of the built DataSet (mesh.rs:78-95): vpos maps an added
+    // vertex to its DataSet index, vorder the reverse; identity unless a
+    // solid has interior vertices, which go last
+    std::vector<unsigned> vpos, vorder;
+    unsigned n_interior = 0;
+    std::vector<float> bx, bvel;          // positions / velocities in DataSet order
+    std::vector<unsigned> bfaces, brods, btets;
     std::vector<unsigned> pin_index;
     std::vector<unsigned char> pin_kinematic;
     std::vector<std::pair<unsigned, float>> pulls;
@@ -112,7 +125,11 @@ struct PpfScene {
     VecVecStore fixed_table;
     std::vector<PpfVec2u> transpose_data;
     std::vector<unsigned> transpose_offset;
-    std::vector<unsigned> face_slots, hinge_slots, edge_slots, rod_bend_slots;
+    std::vector<unsigned> face_slots, hinge_slots, edge_slots, rod_bend_slots, tet_slots;
+    std::vector<PpfVec4u> tet;
+    std::vector<PpfTetProp> tprop;
+    std::vector<PpfTetParam> tparam;
+    std::vector<PpfMat3x3f> inv_rest3;
     std::vector<PpfVec3f> cm_vertex;
     std::vector<PpfVec3u> cm_face;
     std::vector<PpfVec2u> cm_edge;
@@ -133,14 +150,24 @@ PpfScene *ppf_scene_create(void) { return new PpfScene(); }
 void ppf_scene_destroy(PpfScene *s) { delete s; }
 unsigned ppf_scene_vertex_count(PpfScene *s) { return (unsigned)s->x.size() / 3; }
 
+// Host copies of curr / prev in the order the vertices were added (the
+// DataSet holds a solid's interior vertices last).
 void ppf_scene_positions(PpfScene *s, float *curr, float *prev) {
-    if (curr && !s->curr.empty()) std::memcpy(curr, s->curr.data(), s->curr.size() * sizeof(PpfVec3f));
-    if (prev && !s->prev.empty()) std::memcpy(prev, s->prev.data(), s->prev.size() * sizeof(PpfVec3f));
+    const size_t n = s->curr.size();
+    for (size_t i = 0; i < n && s->vpos.size() == n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            if (curr) curr[3 * i + d] = s->curr[s->vpos[i]].v[d];
+            if (prev) prev[3 * i + d] = s->prev[s->vpos[i]].v[d];
+        }
 }
 
 void ppf_scene_set_positions(PpfScene *s, const float *curr, const float *prev) {
-    if (curr && !s->curr.empty()) std::memcpy(s->curr.data(), curr, s->curr.size() * sizeof(PpfVec3f));
-    if (prev && !s->prev.empty()) std::memcpy(s->prev.data(), prev, s->prev.size() * sizeof(PpfVec3f));
+    const size_t n = s->curr.size();
+    for (size_t i = 0; i < n && s->vpos.size() == n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            if (curr) s->curr[s->vpos[i]].v[d] = curr[3 * i + d];
+            if (prev) s->prev[s->vpos[i]].v[d] = prev[3 * i + d];
+        }
 }
 
 void ppf_scene_default_param(PpfParamSet *p) {
@@ -201,6 +228,47 @@ unsigned ppf_scene_add_rod(PpfScene *s, const float *v, unsigned nv, const unsig
     s->rod_materials.push_back(*mat);
     for (unsigned i = 0; i < 2 * ne; ++i) s->rods.push_back(base + e[i]);
     s->rod_material.insert(s->rod_material.end(), ne, mi);
+    s->built = false;
+    return base;
+}
+
+unsigned ppf_scene_add_solid(PpfScene *s, const float *v, unsigned nv, const unsigned *t,
+                             unsigned nt, const PpfSolidMaterial *mat) {
+    unsigned base = (unsigned)s->x.size() / 3;
+    s->x.insert(s->x.end(), v, v + 3 * (size_t)nv);
+    s->vel.insert(s->vel.end(), 3 * (size_t)nv, 0.0f);
+    const unsigned mi = (unsigned)s->solid_materials.size();
+    s->solid_materials.push_back(*mat);
+    // boundary faces: the tet faces that no other tet shares, oriented away
+    // from the tet's fourth vertex
+    std::map<std::array<unsigned, 3>, std::pair<int, std::array<unsigned, 3>>> faces;
+    for (unsigned i = 0; i < nt; ++i) {
+        const unsigned a = base + t[4 * i], b = base + t[4 * i + 1], c = base + t[4 * i + 2],
+                       d = base + t[4 * i + 3];
+        s->tets.insert(s->tets.end(), {a, b, c, d});
+        s->tet_material.push_back(mi);
+        const std::array<unsigned, 3> fs[4] = {{b, c, d}, {a, d, c}, {a, b, d}, {a, c, b}};
+        for (const auto &f : fs) {
+            std::array<unsigned, 3> key = f;
+            std::sort(key.begin(), key.end());
+            auto it = faces.find(key);
+            if (it == faces.end()) faces.emplace(key, std::make_pair(1, f));
+            else ++it->second.first;
+        }
+    }
+    // in tet order, so the surface is deterministic
+    for (unsigned i = 0; i < nt; ++i) {
+        const unsigned a = base + t[4 * i], b = base + t[4 * i + 1], c = base + t[4 * i + 2],
+                       d = base + t[4 * i + 3];
+        const std::array<unsigned, 3> fs[4] = {{b, c, d}, {a, d, c}, {a, b, d}, {a, c, b}};
+        for (const auto &f : fs) {
+            std::array<unsigned, 3> key = f;
+            std::sort(key.begin(), key.end());
+            if (faces[key].first != 1) continue;
+            s->solid_faces.insert(s->solid_faces.end(), f.begin(), f.end());
+            s->solid_face_material.push_back(mi);
+        }
+    }
     s->built = false;
     return base;
 }
@@ -289,8 +357,47 @@ void ppf_scene_add_floor(PpfScene *s, const float *g, const float *up, float gap
 
 int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     const unsigned n = (unsigned)s->x.size() / 3;
-    const unsigned nf = (unsigned)s->faces.size() / 3;
-    auto X = [&](unsigned i) { return V3{s->x[3 * i], s->x[3 * i + 1], s->x[3 * i + 2]}; };
+    s->n_interior = 0;
+    // vertex order (mesh.rs:78-95): every vertex a face or rod uses, then the
+    // vertices only tets use (a solid's interior), each group in added order
+    {
+        std::vector<char> surf(n, 0), in_tet(n, 0);
+        for (unsigned v : s->faces) surf[v] = 1;
+        for (unsigned v : s->solid_faces) surf[v] = 1;
+        for (unsigned v : s->rods) surf[v] = 1;
+        for (unsigned v : s->tets) in_tet[v] = 1;
+        s->vpos.assign(n, 0u);
+        s->vorder.clear();
+        for (int pass = 0; pass < 2; ++pass)
+            for (unsigned i = 0; i < n; ++i) {
+                const bool interior = in_tet[i] && !surf[i];
+                if (interior == (pass == 1)) {
+                    s->vpos[i] = (unsigned)s->vorder.size();
+                    s->vorder.push_back(i);
+                    s->n_interior += interior ? 1u : 0u;
+                }
+            }
+        s->bx.resize(3 * (size_t)n);
+        s->bvel.resize(3 * (size_t)n);
+        for (unsigned k = 0; k < n; ++k)
+            for (int d = 0; d < 3; ++d) {
+                s->bx[3 * k + d] = s->x[3 * s->vorder[k] + d];
+                s->bvel[3 * k + d] = s->vel[3 * s->vorder[k] + d];
+            }
+        auto remap = [&](const std::vector<unsigned> &in, std::vector<unsigned> &out) {
+            out.resize(in.size());
+            for (size_t k = 0; k < in.size(); ++k) out[k] = s->vpos[in[k]];
+        };
+        std::vector<unsigned> all_faces(s->faces);
+        all_faces.insert(all_faces.end(), s->solid_faces.begin(), s->solid_faces.end());
+        remap(all_faces, s->bfaces);
+        remap(s->rods, s->brods);
+        remap(s->tets, s->btets);
+    }
+    const unsigned nf_shell = (unsigned)s->faces.size() / 3;
+    const unsigned nf = (unsigned)s->bfaces.size() / 3;
+    const unsigned nt = (unsigned)s->btets.size() / 4;
+    auto X = [&](unsigned i) { return V3{s->bx[3 * i], s->bx[3 * i + 1], s->bx[3 * i + 2]}; };
     s->param = *prm;
     const float dt = prm->dt;
 
@@ -299,25 +406,25 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     s->prev.resize(n);
     for (unsigned i = 0; i < n; ++i)
         for (int d = 0; d < 3; ++d) {
-            s->curr[i].v[d] = s->x[3 * i + d];
-            s->prev[i].v[d] = s->x[3 * i + d] - s->vel[3 * i + d] * dt;
+            s->curr[i].v[d] = s->bx[3 * i + d];
+            s->prev[i].v[d] = s->bx[3 * i + d] - s->bvel[3 * i + d] * dt;
         }
 
     // faces
     s->face.resize(nf);
     for (unsigned i = 0; i < nf; ++i)
-        for (int k = 0; k < 3; ++k) s->face[i].v[k] = s->faces[3 * i + k];
+        for (int k = 0; k < 3; ++k) s->face[i].v[k] = s->bfaces[3 * i + k];
 
     // edges (mesh.rs:188-229): the rod edges as given, then the face edges in
     // first-seen order with their incident faces
-    const unsigned nr = (unsigned)s->rods.size() / 2;
+    const unsigned nr = (unsigned)s->brods.size() / 2;
     std::map<std::pair<unsigned, unsigned>, unsigned> edge_id;
     std::vector<std::vector<unsigned>> edge_faces(nr);
     s->edge.clear();
-    for (unsigned i = 0; i < nr; ++i) s->edge.push_back({{s->rods[2 * i], s->rods[2 * i + 1]}});
+    for (unsigned i = 0; i < nr; ++i) s->edge.push_back({{s->brods[2 * i], s->brods[2 * i + 1]}});
     for (unsigned i = 0; i < nf; ++i)
         for (int j = 0; j < 3; ++j) {
-            unsigned a = s->faces[3 * i + j], b = s->faces[3 * i + (j + 1) % 3];
+            unsigned a = s->bfaces[3 * i + j], b = s->bfaces[3 * i + (j + 1) % 3];
             auto key = std::make_pair(std::min(a, b), std::max(a, b));
             auto it = edge_id.find(key);
             if (it == edge_id.end()) {
@@ -338,8 +445,8 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     std::vector<HingeAcc> hacc;
     for (unsigned i = 0; i < nf; ++i)
         for (int j = 0; j < 3; ++j) {
-            unsigned a = s->faces[3 * i + j], b = s->faces[3 * i + (j + 1) % 3],
-                     c = s->faces[3 * i + (j + 2) % 3];
+            unsigned a = s->bfaces[3 * i + j], b = s->bfaces[3 * i + (j + 1) % 3],
+                     c = s->bfaces[3 * i + (j + 2) % 3];
             auto key = std::make_pair(std::min(a, b), std::max(a, b));
             auto it = hinge_key.find(key);
             if (it == hinge_key.end()) {
@@ -379,17 +486,24 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     s->nb_vrod.from(vr);
     s->nb_hface.from(hinge_faces);
     s->nb_eface.from(edge_faces);
+    // element types (builder.rs:1497-1518): bit 0 marks a solid's boundary
+    // face, a tet vertex, and a hinge next to a solid face (no bending)
     s->type_face.assign(nf, 0);
     s->type_vertex.assign(n, 0);
     s->type_hinge.assign(nh, 0);
+    for (unsigned i = nf_shell; i < nf; ++i) s->type_face[i] = 1;
+    for (unsigned v : s->btets) s->type_vertex[v] = 1;
+    for (unsigned i = 0; i < nh; ++i)
+        for (unsigned f : hinge_faces[i])
+            if (f >= nf_shell) s->type_hinge[i] = 1;
 
     // pins
     std::vector<char> fixed_v(n, 0);
     s->fix.clear();
     for (size_t i = 0; i < s->pin_index.size(); ++i) {
-        unsigned v = s->pin_index[i];
+        unsigned v = s->vpos[s->pin_index[i]];
         PpfFixPair fp{};
-        for (int d = 0; d < 3; ++d) fp.position.v[d] = s->x[3 * v + d];
+        for (int d = 0; d < 3; ++d) fp.position.v[d] = s->bx[3 * v + d];
         fp.ghat = 1e-3f;
         fp.index = v;
         fp.kinematic = s->pin_kinematic[i] != 0;
@@ -399,9 +513,10 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     s->pull.clear();
     for (auto &p : s->pulls) {
         PpfPullPair pp{};
-        for (int d = 0; d < 3; ++d) pp.position.v[d] = s->x[3 * p.first + d];
+        const unsigned v = s->vpos[p.first];
+        for (int d = 0; d < 3; ++d) pp.position.v[d] = s->bx[3 * v + d];
         pp.weight = p.second;
-        pp.index = p.first;
+        pp.index = v;
         s->pull.push_back(pp);
     }
 
@@ -409,7 +524,29 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     s->fparam.clear();
     s->fprop.assign(nf, PpfFaceProp{});
     std::vector<float> face_area(nf);
-    for (unsigned i = 0; i < nf; ++i) {
+    for (unsigned i = nf_shell; i < nf; ++i) {
+        // a solid's boundary face: contact parameters of its solid, no
+        // membrane energy (energy.cu:748-760 runs over the shell faces only)
+        const PpfSolidMaterial &m = s->solid_materials[s->solid_face_material[i - nf_shell]];
+        V3 a = X(s->face[i].v[0]), b = X(s->face[i].v[1]), c = X(s->face[i].v[2]);
+        const float area = 0.5f * nrm(crs(sub(b, a), sub(c, a)));
+        face_area[i] = area;
+        PpfFaceParam fp{};
+        fp.model = m.model;
+        fp.friction = m.friction;
+        fp.ghat = m.contact_gap;
+        fp.offset = m.contact_offset;
+        fp.shrink_x = 1.0f;
+        fp.shrink_y = 1.0f;
+        PpfFaceProp pr{};
+        pr.area = area;
+        pr.mass = m.density * area;
+        pr.fixed = fixed_v[s->face[i].v[0]] && fixed_v[s->face[i].v[1]] &&
+                   fixed_v[s->face[i].v[2]];
+        pr.param_index = dedup(s->fparam, fp);
+        s->fprop[i] = pr;
+    }
+    for (unsigned i = 0; i < nf_shell; ++i) {
         const PpfShellMaterial &m = s->materials[s->face_material[i]];
         V3 a = X(s->face[i].v[0]), b = X(s->face[i].v[1]), c = X(s->face[i].v[2]);
         float area = 0.5f * nrm(crs(sub(b, a), sub(c, a)));
@@ -490,10 +627,42 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     }
     for (unsigned i = 0; i < nf; ++i)
         for (int k = 0; k < 3; ++k) s->vprop[s->face[i].v[k]].area += s->fprop[i].area / 3.0f;
-    for (unsigned i = 0; i < nf; ++i)
+    // mass: shell faces (not a solid's boundary faces), rod edges, tets
+    // (builder.rs:589-660)
+    for (unsigned i = 0; i < nf_shell; ++i)
         for (int k = 0; k < 3; ++k) s->vprop[s->face[i].v[k]].mass += s->fprop[i].mass / 3.0f;
     for (unsigned i = 0; i < nr; ++i)
         for (int k = 0; k < 2; ++k) s->vprop[s->edge[i].v[k]].mass += s->eprop[i].mass / 2.0f;
+    // tets (scene.rs:1840-1921): volume |(e0 x e1) . e2| / 6, mass density x
+    // volume, Lame parameters from (E, nu); a quarter of each to its vertices
+    s->tet.resize(nt);
+    s->tprop.assign(nt, PpfTetProp{});
+    s->tparam.clear();
+    for (unsigned i = 0; i < nt; ++i) {
+        const unsigned *t = &s->btets[4 * i];
+        s->tet[i] = {{t[0], t[1], t[2], t[3]}};
+        const PpfSolidMaterial &m = s->solid_materials[s->tet_material[i]];
+        const V3 x0 = X(t[0]);
+        const float vol = std::fabs(dot(crs(sub(X(t[1]), x0), sub(X(t[2]), x0)), sub(X(t[3]), x0))) / 6.0f;
+        PpfTetParam tp{};
+        tp.model = m.model;
+        const float E = m.young_mod, nu = m.poiss_rat;
+        tp.mu = E / (2.0f * (1.0f + nu));
+        tp.lambda = E * nu / ((1.0f + nu) * (1.0f - 2.0f * nu));
+        tp.shrink = 1.0f;
+        tp.deform_damping = m.deform_damping;
+        PpfTetProp pr{};
+        pr.mass = m.density * vol;
+        pr.volume = vol;
+        pr.fixed = fixed_v[t[0]] && fixed_v[t[1]] && fixed_v[t[2]] && fixed_v[t[3]];
+        pr.param_index = dedup(s->tparam, tp);
+        s->tprop[i] = pr;
+    }
+    for (unsigned i = 0; i < nt; ++i)
+        for (int k = 0; k < 4; ++k) {
+            s->vprop[s->tet[i].v[k]].mass += s->tprop[i].mass / 4.0f;
+            s->vprop[s->tet[i].v[k]].volume += s->tprop[i].volume / 4.0f;
+        }
     s->vparam.clear();
     for (unsigned j = 0; j < n; ++j) {
         // faces weighted by area, rod edges by rest length
@@ -579,9 +748,32 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
         s->eprop[i] = pr;
     }
 
-    // inverse rest matrices in the face's tangent frame (builder.rs:157-230)
-    s->inv_rest.resize(nf);
-    for (unsigned i = 0; i < nf; ++i) {
+    // inverse rest matrices of the tets: [x1-x0, x2-x0, x3-x0]^-1 (builder.rs:
+    // 232-262, shrink 1), by cofactors, column-major
+    s->inv_rest3.resize(nt);
+    for (unsigned i = 0; i < nt; ++i) {
+        const unsigned *t = &s->btets[4 * i];
+        const V3 x0 = X(t[0]);
+        const V3 c[3] = {sub(X(t[1]), x0), sub(X(t[2]), x0), sub(X(t[3]), x0)};
+        // m(r, k) = c[k] component r
+        auto m = [&](int r, int k) { return r == 0 ? c[k].x : r == 1 ? c[k].y : c[k].z; };
+        const float det = m(0, 0) * (m(1, 1) * m(2, 2) - m(1, 2) * m(2, 1)) -
+                          m(0, 1) * (m(1, 0) * m(2, 2) - m(1, 2) * m(2, 0)) +
+                          m(0, 2) * (m(1, 0) * m(2, 1) - m(1, 1) * m(2, 0));
+        if (!(std::fabs(det) > 0.0f)) return 1;
+        PpfMat3x3f inv;
+        for (int r = 0; r < 3; ++r)
+            for (int k = 0; k < 3; ++k) {
+                // inverse(r, k) = cofactor(k, r) / det
+                const int r1 = (k + 1) % 3, r2 = (k + 2) % 3, c1 = (r + 1) % 3, c2 = (r + 2) % 3;
+                inv.m[r + 3 * k] = (m(r1, c1) * m(r2, c2) - m(r1, c2) * m(r2, c1)) / det;
+            }
+        s->inv_rest3[i] = inv;
+    }
+    // inverse rest matrices in the face's tangent frame (builder.rs:157-230),
+    // shell faces only
+    s->inv_rest.resize(nf_shell);
+    for (unsigned i = 0; i < nf_shell; ++i) {
         V3 x0 = X(s->face[i].v[0]), x1 = X(s->face[i].v[1]), x2 = X(s->face[i].v[2]);
         V3 d0 = sub(x1, x0), d1 = sub(x2, x0);
         V3 nn = crs(d0, d1);
@@ -621,6 +813,9 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     for (auto &h : s->hinge)
         for (int a = 0; a < 4; ++a)
             for (int b = 0; b < 4; ++b) insert(h.v[a], h.v[b]);
+    for (auto &t : s->tet)
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) insert(t.v[a], t.v[b]);
     // rod-bend stencil (j, i, k) of every vertex with two edges and no face
     // (builder.rs:1289-1313)
     std::vector<std::array<unsigned, 3>> bend_stencil(n, {{0xFFFFFFFFu, 0u, 0u}});
@@ -662,6 +857,10 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
         for (int a = 0; a < 4; ++a)
             for (int b = 0; b < 4; ++b) s->hinge_slots.push_back(slot_of(r[a], r[b]));
     }
+    s->tet_slots.clear();
+    for (auto &t : s->tet)
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) s->tet_slots.push_back(slot_of(t.v[a], t.v[b]));
     // rod edges: 4 blocks each; rod-bend stencils: 9 per vertex (sentinels
     // where a vertex has none), builder.rs:1424-1466
     s->edge_slots.clear();
@@ -779,8 +978,15 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     ds.transpose_table.nnz_allocated = ds.transpose_table.nnz;
     ds.transpose_table.offset_allocated = n + 1;
     ds.rod_count = nr;
-    ds.shell_face_count = nf;
-    ds.surface_vert_count = n;
+    ds.shell_face_count = nf_shell;
+    ds.surface_vert_count = n - s->n_interior;
+    set_vec(ds.mesh.mesh.tet.data, ds.mesh.mesh.tet.size, ds.mesh.mesh.tet.allocated, s->tet);
+    set_vec(ds.prop.tet.data, ds.prop.tet.size, ds.prop.tet.allocated, s->tprop);
+    set_vec(ds.param_arrays.tet.data, ds.param_arrays.tet.size, ds.param_arrays.tet.allocated,
+            s->tparam);
+    set_vec(ds.inv_rest3x3.data, ds.inv_rest3x3.size, ds.inv_rest3x3.allocated, s->inv_rest3);
+    set_vec(ds.tet_hess_slots.data, ds.tet_hess_slots.size, ds.tet_hess_slots.allocated,
+            s->tet_slots);
     set_vec(ds.face_hess_slots.data, ds.face_hess_slots.size, ds.face_hess_slots.allocated, s->face_slots);
     set_vec(ds.hinge_hess_slots.data, ds.hinge_hess_slots.size, ds.hinge_hess_slots.allocated, s->hinge_slots);
     set_vec(ds.edge_hess_slots.data, ds.edge_hess_slots.size, ds.edge_hess_slots.allocated, s->edge_slots);
@@ -829,6 +1035,15 @@ size_t ppf_scene_array(PpfScene *s, const char *name, void *out) {
     else if (n == "vertex_area") per(s->vprop, [](const PpfVertexProp &p) { return p.area; });
     else if (n == "face_area") per(s->fprop, [](const PpfFaceProp &p) { return p.area; });
     else if (n == "face_mass") per(s->fprop, [](const PpfFaceProp &p) { return p.mass; });
+    else if (n == "vertex_order") take(s->vpos);
+    else if (n == "tet") take(s->tet);
+    else if (n == "tet_slots") take(s->tet_slots);
+    else if (n == "inv_rest3x3") take(s->inv_rest3);
+    else if (n == "tet_mass") per(s->tprop, [](const PpfTetProp &p) { return p.mass; });
+    else if (n == "tet_volume") per(s->tprop, [](const PpfTetProp &p) { return p.volume; });
+    else if (n == "vertex_volume") per(s->vprop, [](const PpfVertexProp &p) { return p.volume; });
+    else if (n == "face_type") take(s->type_face);
+    else if (n == "hinge_type") take(s->type_hinge);
     else if (n == "edge_slots") take(s->edge_slots);
     else if (n == "rod_bend_slots") take(s->rod_bend_slots);
     else if (n == "edge_length") per(s->eprop, [](const PpfEdgeProp &p) { return p.length; });

@@ -95,6 +95,19 @@ class ShellMaterial(C.Structure):
     ]
 
 
+class SolidMaterial(C.Structure):
+    _fields_ = [
+        ("model", C.c_int),
+        ("density", C.c_float),
+        ("young_mod", C.c_float),
+        ("poiss_rat", C.c_float),
+        ("contact_gap", C.c_float),
+        ("contact_offset", C.c_float),
+        ("friction", C.c_float),
+        ("deform_damping", C.c_float),
+    ]
+
+
 class RodMaterial(C.Structure):
     _fields_ = [
         ("density", C.c_float),

@@ -52,6 +52,33 @@ def box(side: float, center=(0.0, 0.0, 0.0)):
     return v.astype(np.float32), f
 
 
+def tet_box(n: int, side: float, center=(0.0, 0.0, 0.0)):
+    """Solid cube of (n+1)^3 vertices, each of its n^3 cells split into six
+    tets along the main diagonal (one per axis order), all positively
+    oriented. Returns (vertices [(n+1)^3, 3] f32, tets [6 n^3, 4] u32)."""
+    g = np.linspace(-0.5 * side, 0.5 * side, n + 1)
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    v = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1) + np.asarray(center, np.float64)
+    idx = np.arange((n + 1) ** 3).reshape(n + 1, n + 1, n + 1)
+    unit = np.eye(3, dtype=int)
+    orders = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    tets = []
+    for i in range(n):
+        for j in range(n):
+            for k in range(n):
+                c = np.array([i, j, k])
+                for o in orders:
+                    p1 = c + unit[o[0]]
+                    p2 = p1 + unit[o[1]]
+                    t = [idx[tuple(c)], idx[tuple(p1)], idx[tuple(p2)], idx[tuple(c + 1)]]
+                    d = np.linalg.det(np.stack([v[t[1]] - v[t[0]], v[t[2]] - v[t[0]],
+                                                v[t[3]] - v[t[0]]], 1))
+                    if d < 0:
+                        t[1], t[2] = t[2], t[1]
+                    tets.append(t)
+    return v.astype(np.float32), np.asarray(tets, np.uint32)
+
+
 def edges_of(faces: np.ndarray) -> np.ndarray:
     """Unique undirected edges in first-seen order (face order, then corner
     order j -> j+1), each as (first-seen endpoint, next endpoint)."""

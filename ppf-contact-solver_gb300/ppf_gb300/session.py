@@ -40,6 +40,9 @@ def _declare(lib):
     lib.ppf_scene_add_rod.restype = C.c_uint
     lib.ppf_scene_add_rod.argtypes = [P, _f32, C.c_uint, _u32, C.c_uint,
                                       C.POINTER(abi.RodMaterial)]
+    lib.ppf_scene_add_solid.restype = C.c_uint
+    lib.ppf_scene_add_solid.argtypes = [P, _f32, C.c_uint, _u32, C.c_uint,
+                                        C.POINTER(abi.SolidMaterial)]
     lib.ppf_scene_set_velocity.argtypes = [P, _f32]
     lib.ppf_scene_pin.argtypes = [P, _u32, C.c_uint, C.c_int]
     lib.ppf_scene_pull.argtypes = [P, _u32, C.c_uint, C.c_float]
@@ -128,6 +131,26 @@ class Material:
 
 
 @dataclass
+class SolidMaterial:
+    """Solid (tet) material in the reference's units (scene.rs tet
+    parameters): density in kg/m^3, young_mod pre-divided by density."""
+
+    density: float = 1000.0
+    young_mod: float = 500.0
+    poiss_rat: float = 0.35
+    model: int = abi.MODEL_ARAP
+    contact_gap: float = 1e-3
+    contact_offset: float = 0.0
+    friction: float = 0.0
+    deform_damping: float = 0.0
+
+    def to_c(self) -> abi.SolidMaterial:
+        return abi.SolidMaterial(self.model, self.density, self.young_mod, self.poiss_rat,
+                                 self.contact_gap, self.contact_offset, self.friction,
+                                 self.deform_damping)
+
+
+@dataclass
 class RodMaterial:
     """Rod material in the reference's units (scene.rs rod parameters):
     density in kg/m, young_mod the stretch stiffness per unit edge mass."""
@@ -166,6 +189,7 @@ class Scene:
         self._rod_count = 0
         self._rod_mats = []
         self._vert_inputs = []
+        self._solids = []
         self.built = False
 
     def __del__(self):
@@ -191,6 +215,16 @@ class Scene:
         self._vert_inputs.append(v.reshape(-1, 3).copy())
         return int(self.lib.ppf_scene_add_rod(self.h, v, v.size // 3, e, e.size // 2,
                                               C.byref(m)))
+
+    def add_solid(self, vertices, tets, material: SolidMaterial) -> int:
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1)
+        t = np.ascontiguousarray(tets, np.uint32).reshape(-1)
+        m = material.to_c()
+        self._vert_inputs.append(v.reshape(-1, 3).copy())
+        self._solids.append((len(np.concatenate(self._vert_inputs)) - v.size // 3,
+                             t.reshape(-1, 4).copy(), material))
+        return int(self.lib.ppf_scene_add_solid(self.h, v, v.size // 3, t, t.size // 4,
+                                                C.byref(m)))
 
     def set_velocity(self, velocity):
         v = np.ascontiguousarray(velocity, np.float32).reshape(-1)
@@ -290,7 +324,10 @@ class Scene:
                      "edge_mass": np.float32, "edge_stiffness": np.float32,
                      "edge_bend": np.float32, "rest_bend_angle": np.float32,
                      "vertex_ghat": np.float32, "vertex_offset": np.float32,
-                     "vertex_friction": np.float32}
+                     "vertex_friction": np.float32, "inv_rest3x3": np.float32,
+                     "tet_mass": np.float32, "tet_volume": np.float32,
+                     "vertex_volume": np.float32, "face_type": np.uint8,
+                     "hinge_type": np.uint8}
 
     def array(self, name: str) -> np.ndarray:
         """A named array of the built DataSet (ppf_scene_array): topology

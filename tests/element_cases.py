@@ -155,6 +155,32 @@ def gen_rod(rng, n):
     return out
 
 
+def gen_solid(rng, n):
+    """Tets and shell faces deformed around their rest shape (some inverted,
+    so the rotation-variant SVD flips a sign), under ARAP, StVK and SNHk."""
+    out = []
+    for i in range(n):
+        rest = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float64) * 0.02
+        rest += rng.normal(0, 0.003, rest.shape)
+        D = (rest[1:] - rest[0]).T
+        inv = np.linalg.inv(D)
+        A = np.eye(3) + rng.normal(0, 0.15, (3, 3))
+        if i % 5 == 0:
+            A[:, 2] *= -0.3  # inverted
+        x = rest[0] + (A @ (rest - rest[0]).T).T + rng.normal(0, 0.01, 3)
+        F = (A + rng.normal(0, 0.05, (3, 3))).astype(f32)
+        tri = x[:3].copy()
+        d2 = np.stack([tri[1] - tri[0], tri[2] - tri[0]], 1)
+        inv2 = np.linalg.inv(np.array([[np.linalg.norm(d2[:, 0]), 0.0],
+                                       [0.0, np.linalg.norm(d2[:, 1])]]) + rng.normal(0, 0.01, (2, 2)))
+        out.append({"model": [0, 1, 3][i % 3], "mu": f32(10 ** rng.uniform(2, 4)),
+                    "lmd": f32(10 ** rng.uniform(2, 4)), "mass": f32(rng.uniform(0.01, 1.0)),
+                    "x": x.astype(f32).reshape(-1), "inv": inv.T.astype(f32).reshape(-1),
+                    "F": F.T.reshape(-1).copy(), "a3": (1.0 + rng.normal(0, 0.2, 3)).astype(f32),
+                    "tri": tri.astype(f32).reshape(-1), "inv2": inv2.T.astype(f32).reshape(-1)})
+    return out
+
+
 def gen_sym(rng, n):
     out = []
     for i in range(n):
@@ -344,6 +370,28 @@ def evaluate(lib, prefix, rng_seed=7, n=64):
         bx = np.ascontiguousarray(c["b"])
         f(_ptr(bx[0]), _ptr(bx[1]), _ptr(bx[2]), c["rest"], _ptr(f9), _ptr(h81))
         rec("rod", i, stretch_g=g6, stretch_h=h36, bend_f=f9, bend_h=h81)
+    for i, c in enumerate(gen_solid(rng, n)):
+        ft = fn("model_table")
+        ft.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_float), C.c_float, C.c_float,
+                       C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        d2a, d2b = np.zeros(2, f32), np.zeros(4, f32)
+        ft(c["model"], 2, _ptr(c["a3"]), c["mu"], c["lmd"], _ptr(d2a), _ptr(d2b))
+        d3a, d3b = np.zeros(3, f32), np.zeros(9, f32)
+        ft(c["model"], 3, _ptr(c["a3"]), c["mu"], c["lmd"], _ptr(d3a), _ptr(d3b))
+        U9, S3, Vt9 = np.zeros(9, f32), np.zeros(3, f32), np.zeros(9, f32)
+        fn("svd33")(_ptr(c["F"]), _ptr(U9), _ptr(S3), _ptr(Vt9))
+        f12, h144 = np.zeros(12, f32), np.zeros(144, f32)
+        f = fn("tet")
+        f.argtypes = [C.POINTER(C.c_float)] * 2 + [C.c_int] + [C.c_float] * 4 + [C.POINTER(C.c_float)] * 2
+        f(_ptr(c["x"]), _ptr(c["inv"]), c["model"], c["mu"], c["lmd"], c["mass"], f32(1e-4),
+          _ptr(f12), _ptr(h144))
+        f9, h81 = np.zeros(9, f32), np.zeros(81, f32)
+        f = fn("shell_model")
+        f.argtypes = [C.POINTER(C.c_float)] * 2 + [C.c_int] + [C.c_float] * 4 + [C.POINTER(C.c_float)] * 2
+        f(_ptr(c["tri"]), _ptr(c["inv2"]), c["model"], c["mu"], c["lmd"], c["mass"], f32(1e-4),
+          _ptr(f9), _ptr(h81))
+        rec("solid", i, table2_g=d2a, table2_h=d2b, table3_g=d3a, table3_h=d3b, svd_U=U9,
+            svd_S=S3, svd_Vt=Vt9, tet_f=f12, tet_h=h144, shell_f=f9, shell_h=h81)
     return {k: np.stack(v) for k, v in res.items()}
 
 

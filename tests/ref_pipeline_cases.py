@@ -69,6 +69,18 @@ def oracle_first_system(o):
             blocks, sysd["force"].reshape(-1).copy())
 
 
+def dataset_positions(sc):
+    """(curr, prev) of a built scene in the DataSet's vertex order (which puts
+    a solid's interior vertices last), flattened."""
+    curr, prev = sc.positions()
+    order = sc.array("vertex_order")
+    c = np.empty_like(curr)
+    p = np.empty_like(prev)
+    c[order] = curr
+    p[order] = prev
+    return c.reshape(-1).copy(), p.reshape(-1).copy()
+
+
 def step_target(sc, curr, prev):
     """The inertial target of a step from (curr, prev) as the library and the
     reference compute it in float32 (main.cu:491-511): x + (x - x_prev)

@@ -155,3 +155,42 @@ def rods_and_sheet(seed: int = 4):
     prev[a0:a0 + na] = c + 1.004 * (prev[a0:a0 + na] - c)
     built.set_positions(curr, prev)
     return built, {"rod_a": (a0, na), "rod_b": (b0, nb)}
+
+
+def solids_and_sheet(seed: int = 6):
+    """Two solids and a sheet, every solid term active in the first Newton
+    system: an ARAP block (3^3 cells, eight interior vertices, sheared and
+    damped) with a sheet lying 6e-4 above its top face, and a falling SNHk
+    block (2^3 cells) whose corner is within the gap of the first's side; an
+    StVK sheet membrane exercises the shell models. No pins."""
+    from ppf_gb300.session import SolidMaterial
+
+    rng = np.random.default_rng(seed)
+    sc = Scene()
+    va, ta = meshes.tet_box(3, 0.1, center=(0.0, 0.45, 0.0))
+    a0 = sc.add_solid(va, ta, SolidMaterial(model=0, density=500.0, young_mod=800.0,
+                                            poiss_rat=0.3, contact_gap=1e-3, friction=0.4,
+                                            deform_damping=0.05))
+    vb, tb = meshes.tet_box(2, 0.05, center=(0.0778, 0.47, 0.03))
+    vb = vb + rng.uniform(-2e-4, 2e-4, vb.shape).astype(np.float32)
+    b0 = sc.add_solid(vb, tb, SolidMaterial(model=3, density=800.0, young_mod=600.0,
+                                            poiss_rat=0.35, contact_gap=1e-3, friction=0.2))
+    mat = scenes.cloth_material()
+    mat.model = 1  # StVK
+    vs, fs = meshes.grid(8, 8, 0.12, 0.12)
+    vs = vs.astype(np.float64)
+    vs[:, 1] = 0.5 + 6e-4 + rng.uniform(-2e-5, 2e-5, len(vs))
+    sc.add_shell(vs.astype(np.float32), fs, mat)
+    n = sc.vertex_count
+    vel = np.zeros((n, 3), np.float32)
+    vel[b0:b0 + len(vb)] = (0.0, -0.3, 0.0)
+    sc.set_velocity(vel)
+    sc.add_floor((0.0, 0.3, 0.0), contact_gap=1e-3, friction=0.5)
+    built = sc.build(scenes._param(0.01))
+    # shear block A by 3 % (curr and prev alike: its elastic force is active)
+    curr, prev = built.positions()
+    for arr in (curr, prev):
+        blk = arr[a0:a0 + len(va)]
+        blk[:, 0] += 0.03 * (blk[:, 1] - 0.45)
+    built.set_positions(curr, prev)
+    return built, {"block_a": (a0, len(va)), "block_b": (b0, len(vb))}

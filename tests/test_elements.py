@@ -35,7 +35,7 @@ def _compare(ref, got, exact):
 
 def test_golden_covers_every_output():
     g = np.load(GOLDEN)
-    assert len(g.files) == 44
+    assert len(g.files) == 55
 
 
 def test_element_math_matches_golden(oracle_lib):
