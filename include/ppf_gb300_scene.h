@@ -8,8 +8,8 @@
  * crates/ppf-cts-solver/src/mesh.rs Mesh::new, and the face-edge props of
  * crates/ppf-cts-solver/src/main.rs:205-250). Covered: shells (any model
  * field, Baraff-Witkin evaluated), rods, fix pins (static or kinematic), pull
- * pins, analytic spheres and floors, static collision meshes, solids (tets).
- * Not covered: stitches, PDRD bodies, sand grains, UV anisotropy.
+ * pins, analytic spheres and floors, static collision meshes, solids (tets),
+ * stitches. Not covered: PDRD bodies, sand grains, UV anisotropy.
  *
  * Edge and hinge order: the reference extracts them from a hash map, whose
  * iteration order is not reproducible; here they are listed in first-seen
@@ -117,6 +117,14 @@ int ppf_scene_add_rod_edges(PpfScene *scene, const unsigned *edges, unsigned ne,
  * Returns the index of the first vertex. */
 unsigned ppf_scene_add_solid(PpfScene *scene, const float *vertices, unsigned nv,
                              const unsigned *tets, unsigned nt, const PpfSolidMaterial *mat);
+/* A stitch (Constraint::stitch, energy.cu:796-884): a spring between the
+ * barycentric point index[0..2] / weight[0..2] and index[3..5] /
+ * weight[3..5] (vertex indices as added; weights of each side sum to 1; a
+ * single vertex s is {s, s, s} with {1, 0, 0}), rest length half the
+ * weighted contact gap, with the given stiffness. Returns 0, or -1 for an
+ * index out of range. */
+int ppf_scene_add_stitch(PpfScene *scene, const unsigned *index, const float *weight,
+                         float stiffness);
 /* Initial velocity of every vertex (3 floats each); prev = curr - v dt. */
 void ppf_scene_set_velocity(PpfScene *scene, const float *velocity);
 /* Fix pins at the vertices' current positions. kinematic != 0 marks pins
@@ -169,6 +177,7 @@ void ppf_scene_set_positions(PpfScene *scene, const float *curr,
  * f32 per element: vertex_mass, vertex_area, face_area, face_mass,
  * edge_length, edge_initial_length, edge_mass, edge_stiffness, edge_bend,
  * rest_bend_angle (per vertex), hinge_length, hinge_area, face_mu,
+ * stitch (the DataSet's stitches), stitch_slots (36 u32 per stitch),
  * tet (4 u32 per tet), tet_slots (16 u32 per tet), inv_rest3x3 (9 f32 per
  * tet, column-major), tet_mass, tet_volume, vertex_volume (f32),
  * vertex_order (u32: DataSet index of each added vertex), face_type,

@@ -482,8 +482,9 @@ void refpipe_state(const float *curr, const float *prev, const ParamSet *param) 
 }
 
 // One Newton system at eval_x (main.cu:713-874, the scene features in
-// scope): inertia and per-vertex terms, elastic, strain limit, contact over
-// trees at eval_x, analytic constraints. Returns the contact count.
+// scope): inertia and per-vertex terms, elastic, stitches, strain limit,
+// contact over trees at eval_x, analytic constraints. Returns the contact
+// count.
 unsigned refpipe_assemble(const float *eval_x, const float *target, float dt) {
     RefPipe &p = *g_pipe;
     load3(p.eval_x, eval_x, p.n);
@@ -501,6 +502,8 @@ unsigned refpipe_assemble(const float *eval_x, const float *target, float dt) {
     energy::compute_torque_groups(p.data, ex, torque_v);
     energy::embed_momentum_force_hessian(p.data, ex, vel, dt, tg, force, diag, p.prm, torque_v);
     energy::embed_elastic_force_hessian(p.data, ex, force, p.fixed, dt, p.prm);
+    if (p.data.constraint.stitch.size)
+        energy::embed_stitch_force_hessian(p.data, ex, force, p.fixed, p.prm);
     p.tmp_fixed.copy(p.fixed);
     if (p.data.shell_face_count > 0)
         strainlimiting::embed_strainlimiting_force_hessian(p.data, ex, force, p.tmp_fixed,

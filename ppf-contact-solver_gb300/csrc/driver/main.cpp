@@ -247,8 +247,8 @@ Loaded load_scene(const std::string &path) {
     const unsigned n_vert = count("vert"), n_tri = count("tri"), n_sv = count("static_vert"),
                    n_st = count("static_tri"), n_pin = count("pin_block"),
                    n_wall = count("wall"), n_sphere = count("sphere"), n_rod = count("rod");
-    if (count("tet") || count("stitch"))
-        die("tets and stitches are not simulated by this library");
+    const unsigned n_stitch = count("stitch");
+    if (count("tet")) die("tets are not read by this executable");
     const double ws = num(prm, "param", "world_scaling", 1.0);
     if (!(ws > 0.0)) die("world_scaling must be > 0");
     L.world_scaling = (float)ws;
@@ -347,6 +347,23 @@ Loaded load_scene(const std::string &path) {
         if (ppf_scene_add_rod_edges(L.scene, rod.data(), n_rod, rmat.data(), rmats.data(),
                                     (unsigned)rmats.size()) != 0)
             die("rod.bin names a vertex past count.vert");
+    }
+    if (n_stitch) {
+        // stitches (scene.rs:504-520, 748-756): six indices and weights each,
+        // and a per-stitch stiffness (1 where the file is absent)
+        const auto ind = read_bin<uint64_t>(B + "stitch_ind.bin");
+        const auto w = read_bin<float>(B + "stitch_w.bin");
+        auto k = read_bin<float>(B + "stitch_stiffness.bin", false);
+        if (ind.size() != 6 * (size_t)n_stitch || w.size() != 6 * (size_t)n_stitch)
+            die("stitch_ind.bin / stitch_w.bin do not match count.stitch");
+        if (k.empty()) k.assign(n_stitch, 1.0f);
+        if (k.size() != n_stitch) die("stitch_stiffness.bin does not match count.stitch");
+        for (unsigned i = 0; i < n_stitch; ++i) {
+            unsigned idx[6];
+            for (int a = 0; a < 6; ++a) idx[a] = (unsigned)ind[6 * i + a];
+            if (ppf_scene_add_stitch(L.scene, idx, &w[6 * i], k[i]) != 0)
+                die("stitch_ind.bin names a vertex past count.vert");
+        }
     }
     std::vector<float> v3(vel.begin(), vel.end());
     for (float &c : v3) c = (float)(c * ws);
@@ -546,11 +563,12 @@ int main(int argc, char **argv) {
     if (describe) {
         // the scene as read, without a GPU: one "key value" per line
         const PpfConstraint &c = ds->constraint;
-        std::printf("vertices %u\nfaces %u\nrods %u\nedges %u\nhinges %u\nfix %u\npull %u\n"
+        std::printf("vertices %u\nfaces %u\nrods %u\nstitches %u\nedges %u\nhinges %u\nfix %u\npull %u\n"
                     "spheres %u\nfloors %u\ncollision_vertices %u\ncollision_faces %u\n"
                     "face_params %u\ndt %.9g\nframes %d\nfps %.9g\nauto_save %d\n"
                     "gravity %.9g %.9g %.9g\ncg_tol %.9g\n",
                     ds->vertex.curr.size, ds->mesh.mesh.face.size, ds->rod_count,
+                    c.stitch.size,
                     ds->mesh.mesh.edge.size,
                     ds->mesh.mesh.hinge.size, c.fix.size, c.pull.size, c.sphere.size,
                     c.floor.size, c.mesh.vertex.size, c.mesh.face.size,

@@ -261,6 +261,33 @@ __global__ void k_rod_bend(Scene s, StepParams p, AssemblyBuffers b) {
     scatter_blocks<3>(b.fixed_val, s.bend_slot + 9 * (size_t)i, H);
 }
 
+// ---- stitches (energy.cu:796-884) ---------------------------------------------
+__global__ void k_stitch_energy(Scene s, StepParams p, AssemblyBuffers b) {
+    unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.nstitch) return;
+    const PpfStitch &st = s.stitch[i];
+    Vec3 x[6];
+    float w[6], ghat = 0.0f;
+    float off_src = -INFINITY, off_tgt = -INFINITY;
+    for (int a = 0; a < 6; ++a) {
+        const unsigned v = st.index.v[a];
+        x[a] = X(b.x, v);
+        w[a] = st.weight.v[a];
+        const PpfVertexParam &vp = s.vparam[s.vprop[v].param_index];
+        ghat += w[a] * vp.ghat;
+        if (a < 3) off_src = a ? fmaxf(off_src, vp.offset) : vp.offset;
+        else off_tgt = a > 3 ? fmaxf(off_tgt, vp.offset) : vp.offset;
+    }
+    const float l0 = ghat / 2.0f;
+    const float l_cap = p.stitch_length_factor * l0 + off_src + off_tgt;
+    Mat<3, 6> dedx;
+    Mat<18, 18> H;
+    stitch::spring(x, w, l0, l_cap, dedx, H);
+    for (int a = 0; a < 6; ++a) atomic_add3(b.force + 3 * st.index.v[a], st.stiffness * dedx.col(a));
+    H *= st.stiffness;
+    scatter_blocks<6>(b.fixed_val, s.stitch_slot + 36 * (size_t)i, H);
+}
+
 // ---- solids (energy.cu:395-446) ------------------------------------------------
 __global__ void k_tet_energy(Scene s, StepParams p, AssemblyBuffers b) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1105,6 +1132,10 @@ void launch_elastic(const Scene &s, const StepParams &p, const AssemblyBuffers &
     }
     if (s.nh) {
         k_hinge_energy<<<div_up(s.nh, kB), kB, 0, q>>>(s, p, b);
+        PPF_LAUNCH_CHECK();
+    }
+    if (s.nstitch) { // after the elastic terms, before the copy (main.cu:794-797)
+        k_stitch_energy<<<div_up(s.nstitch, kB), kB, 0, q>>>(s, p, b);
         PPF_LAUNCH_CHECK();
     }
 }

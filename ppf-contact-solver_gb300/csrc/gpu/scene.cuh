@@ -54,6 +54,9 @@ struct Scene {
     const float *inv_rest3;       // 9 per tet, column-major
     const unsigned *tet_slot;     // 16 per tet
     const unsigned char *hinge_type; // bit 0: next to a solid's face (no bending)
+    unsigned nstitch;
+    const PpfStitch *stitch;
+    const unsigned *stitch_slot;  // 36 per stitch
     const unsigned *face;
     const unsigned *edge;
     const unsigned *hinge;
@@ -112,6 +115,7 @@ struct StepParams {
     int barrier, friction_mode;
     int inactive_momentum;
     float fix_xz;
+    float stitch_length_factor;
 };
 
 // Per-iteration scalars reduced on the device and read by the host once per

@@ -204,6 +204,9 @@ Scene Solver::scene() const {
     s.inv_rest3 = inv_rest3_.data();
     s.tet_slot = tet_slot_.data();
     s.hinge_type = hinge_type_.data();
+    s.nstitch = nstitch_;
+    s.stitch = stitch_.data();
+    s.stitch_slot = stitch_slot_.data();
     s.face = face_.data();
     s.edge = edge_.data();
     s.hinge = hinge_.data();
@@ -318,6 +321,7 @@ StepParams Solver::step_params(float dt) const {
     p.friction_mode = param->friction_mode;
     p.inactive_momentum = param->inactive_momentum ? 1 : 0;
     p.fix_xz = param->fix_xz;
+    p.stitch_length_factor = param->stitch_length_factor;
     return p;
 }
 
@@ -443,8 +447,6 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     nt_ = ds->mesh.mesh.tet.size;
     if (nt_ && ds->inv_rest3x3.size != nt_)
         throw FatalError(4, "inv_rest3x3 does not match the tets");
-    if (ds->constraint.stitch.size)
-        throw FatalError(4, "stitches are not simulated by this library");
     if (!q_) PPF_CUDA(cudaStreamCreateWithFlags(&q_, cudaStreamNonBlocking));
     if (!ev0_) {
         PPF_CUDA(cudaEventCreate(&ev0_));
@@ -564,6 +566,22 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
                     ts[16 * t + 4 * a + b] = sl;
                 }
         upload(tet_slot_, ts);
+        // stitches: 36 slots each over the six indices (builder.rs:1314-1320);
+        // update_constraint may change their weights and stiffness, not
+        // their vertices
+        nstitch_ = ds->constraint.stitch.size;
+        std::vector<unsigned> ss(36 * (size_t)nstitch_);
+        for (unsigned k = 0; k < nstitch_; ++k) {
+            const unsigned *I = ds->constraint.stitch.data[k].index.v;
+            for (int a = 0; a < 6; ++a)
+                for (int b = 0; b < 6; ++b) {
+                    const unsigned sl = slot_of(I[a], I[b]);
+                    if (I[a] <= I[b] && sl == kSentinel)
+                        throw FatalError(4, "fixed pattern lacks a stitch block");
+                    ss[36 * k + 6 * a + b] = sl;
+                }
+        }
+        upload(stitch_slot_, ss);
         std::vector<unsigned char> ht(nh_, 0);
         const PpfVecChar &hty = ds->mesh.type.hinge;
         for (unsigned h = 0; h < nh_ && hty.data && h < hty.size; ++h)
@@ -672,6 +690,9 @@ void Solver::update_constraint(const PpfConstraint *c) {
     upload(pull_, c->pull.data, npull_);
     upload(sphere_, c->sphere.data, nsphere_);
     upload(floor_, c->floor.data, nfloor_);
+    if (c->stitch.size != nstitch_ && !h_vprop_.empty())
+        throw FatalError(4, "update_constraint changed the number of stitches");
+    upload(stitch_, c->stitch.data, c->stitch.size);
     if (h_vprop_.empty()) return;
     // rebuild fix/pull indices and element `fixed` flags (main.cu:2012-2077).
     // The reference re-uploads every prop array on each call; when the pinned

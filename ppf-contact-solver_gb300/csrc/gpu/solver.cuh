@@ -127,6 +127,9 @@ class Solver {
     DevBuf<PpfTetParam> tparam_;
     DevBuf<float> inv_rest3_;
     DevBuf<unsigned char> hinge_type_;
+    DevBuf<PpfStitch> stitch_;
+    DevBuf<unsigned> stitch_slot_;
+    unsigned nstitch_ = 0;
     DevBuf<PpfFixPair> fix_;
     DevBuf<PpfPullPair> pull_;
     DevBuf<PpfSphere> sphere_;

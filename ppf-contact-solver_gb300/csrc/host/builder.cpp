@@ -83,6 +83,8 @@ struct PpfScene {
     std::vector<unsigned> tets;           // 4 T, global vertex indices
     std::vector<unsigned> tet_material;   // per tet
     std::vector<PpfSolidMaterial> solid_materials;
+    std::vector<PpfStitch> seams;         // stitches, indices as added
+    std::vector<PpfStitch> stitch;        // the DataSet's, indices in DataSet order
     std::vector<unsigned> solid_faces;    // 3 per boundary face of the solids
     std::vector<unsigned> solid_face_material;
 
@@ -125,7 +127,8 @@ struct PpfScene {
     VecVecStore fixed_table;
     std::vector<PpfVec2u> transpose_data;
     std::vector<unsigned> transpose_offset;
-    std::vector<unsigned> face_slots, hinge_slots, edge_slots, rod_bend_slots, tet_slots;
+    std::vector<unsigned> face_slots, hinge_slots, edge_slots, rod_bend_slots, tet_slots,
+        stitch_slots;
     std::vector<PpfVec4u> tet;
     std::vector<PpfTetProp> tprop;
     std::vector<PpfTetParam> tparam;
@@ -273,6 +276,21 @@ unsigned ppf_scene_add_solid(PpfScene *s, const float *v, unsigned nv, const uns
     return base;
 }
 
+int ppf_scene_add_stitch(PpfScene *s, const unsigned *index, const float *weight,
+                         float stiffness) {
+    const unsigned n = (unsigned)s->x.size() / 3;
+    PpfStitch st{};
+    for (int k = 0; k < 6; ++k) {
+        if (index[k] >= n) return -1;
+        st.index.v[k] = index[k];
+        st.weight.v[k] = weight[k];
+    }
+    st.stiffness = stiffness;
+    s->seams.push_back(st);
+    s->built = false;
+    return 0;
+}
+
 int ppf_scene_add_rod_edges(PpfScene *s, const unsigned *e, unsigned ne,
                             const unsigned *edge_material, const PpfRodMaterial *materials,
                             unsigned n_materials) {
@@ -393,6 +411,9 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
         remap(all_faces, s->bfaces);
         remap(s->rods, s->brods);
         remap(s->tets, s->btets);
+        s->stitch = s->seams;
+        for (auto &st : s->stitch)
+            for (int k = 0; k < 6; ++k) st.index.v[k] = s->vpos[st.index.v[k]];
     }
     const unsigned nf_shell = (unsigned)s->faces.size() / 3;
     const unsigned nf = (unsigned)s->bfaces.size() / 3;
@@ -816,6 +837,9 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     for (auto &t : s->tet)
         for (int a = 0; a < 4; ++a)
             for (int b = 0; b < 4; ++b) insert(t.v[a], t.v[b]);
+    for (auto &st : s->stitch) // builder.rs:1314-1320
+        for (int a = 0; a < 6; ++a)
+            for (int b = 0; b < 6; ++b) insert(st.index.v[a], st.index.v[b]);
     // rod-bend stencil (j, i, k) of every vertex with two edges and no face
     // (builder.rs:1289-1313)
     std::vector<std::array<unsigned, 3>> bend_stencil(n, {{0xFFFFFFFFu, 0u, 0u}});
@@ -857,6 +881,11 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
         for (int a = 0; a < 4; ++a)
             for (int b = 0; b < 4; ++b) s->hinge_slots.push_back(slot_of(r[a], r[b]));
     }
+    s->stitch_slots.clear();
+    for (auto &st : s->stitch)
+        for (int a = 0; a < 6; ++a)
+            for (int b = 0; b < 6; ++b)
+                s->stitch_slots.push_back(slot_of(st.index.v[a], st.index.v[b]));
     s->tet_slots.clear();
     for (auto &t : s->tet)
         for (int a = 0; a < 4; ++a)
@@ -987,6 +1016,10 @@ int ppf_scene_build(PpfScene *s, const PpfParamSet *prm) {
     set_vec(ds.inv_rest3x3.data, ds.inv_rest3x3.size, ds.inv_rest3x3.allocated, s->inv_rest3);
     set_vec(ds.tet_hess_slots.data, ds.tet_hess_slots.size, ds.tet_hess_slots.allocated,
             s->tet_slots);
+    set_vec(ds.constraint.stitch.data, ds.constraint.stitch.size, ds.constraint.stitch.allocated,
+            s->stitch);
+    set_vec(ds.stitch_hess_slots.data, ds.stitch_hess_slots.size,
+            ds.stitch_hess_slots.allocated, s->stitch_slots);
     set_vec(ds.face_hess_slots.data, ds.face_hess_slots.size, ds.face_hess_slots.allocated, s->face_slots);
     set_vec(ds.hinge_hess_slots.data, ds.hinge_hess_slots.size, ds.hinge_hess_slots.allocated, s->hinge_slots);
     set_vec(ds.edge_hess_slots.data, ds.edge_hess_slots.size, ds.edge_hess_slots.allocated, s->edge_slots);
@@ -1038,6 +1071,8 @@ size_t ppf_scene_array(PpfScene *s, const char *name, void *out) {
     else if (n == "vertex_order") take(s->vpos);
     else if (n == "tet") take(s->tet);
     else if (n == "tet_slots") take(s->tet_slots);
+    else if (n == "stitch_slots") take(s->stitch_slots);
+    else if (n == "stitch") take(s->stitch);
     else if (n == "inv_rest3x3") take(s->inv_rest3);
     else if (n == "tet_mass") per(s->tprop, [](const PpfTetProp &p) { return p.mass; });
     else if (n == "tet_volume") per(s->tprop, [](const PpfTetProp &p) { return p.volume; });

@@ -11,6 +11,7 @@
 //   stretch strain-limit barrier and stiffness strainlimiting/strainlimiting.cu:100-190
 //   stretch strain-limit line search          strainlimiting/strainlimiting.cu:192-245
 //   stiffness-proportional damping            energy/energy.cu:90-181
+//   stitch spring                             energy/energy.cu:796-884
 #pragma once
 
 #include "barrier.cuh"
@@ -203,6 +204,42 @@ PPF_HD float strain_line_search(const Vec3 &d0, const Vec3 &d1, float l0, float 
 }
 
 } // namespace rod
+
+namespace stitch {
+
+// A stitch spring between the barycentric points sum w_a x_a (a < 3) and
+// sum w_a x_a (a >= 3), taken about their centroid, stretched against rest
+// length l0 with the length capped at l_cap (energy.cu:822-876): gradient
+// (3 x 6, one column per index) and Hessian (18 x 18), before the stitch's
+// stiffness scale.
+PPF_HD void spring(const Vec3 (&x)[6], const float (&w)[6], float l0, float l_cap,
+                   Mat<3, 6> &grad, Mat<18, 18> &hess) {
+    const float s = 1.0f / 6.0f;
+    Vec3 cog = s * x[0];
+    for (int a = 1; a < 6; ++a) cog = cog + s * x[a];
+    const Vec3 z0 = (w[0] * (x[0] - cog) + w[1] * (x[1] - cog)) + w[2] * (x[2] - cog);
+    const Vec3 z1 = (w[3] * (x[3] - cog) + w[4] * (x[4] - cog)) + w[5] * (x[5] - cog);
+    const Vec3 t = z0 - z1;
+    const float l = fminf(l_cap, t.norm());
+    const Vec3 n = t / l;
+    float coef[6];
+    for (int a = 0; a < 6; ++a) coef[a] = a < 3 ? w[a] : -w[a];
+    const Vec3 dedt = (l / l0 - 1.0f) * n;
+    float g[18];
+    for (int a = 0; a < 6; ++a)
+        for (int k = 0; k < 3; ++k) g[3 * a + k] = coef[a] * n[k];
+    const float r = (l - l0) / l;
+    const float c0 = fmaxf(0.0f, 1.0f - r) / l0;
+    const float c1 = fmaxf(0.0f, r / l0);
+    for (int a = 0; a < 6; ++a) grad.set_col(a, coef[a] * dedt);
+    for (int j = 0; j < 18; ++j)
+        for (int i = 0; i < 18; ++i) {
+            const float jj = (i % 3 == j % 3) ? (c1 * coef[i / 3]) * coef[j / 3] : 0.0f;
+            hess(i, j) = (c0 * g[i]) * g[j] + jj;
+        }
+}
+
+} // namespace stitch
 
 namespace damping {
 

@@ -43,6 +43,8 @@ def _declare(lib):
     lib.ppf_scene_add_solid.restype = C.c_uint
     lib.ppf_scene_add_solid.argtypes = [P, _f32, C.c_uint, _u32, C.c_uint,
                                         C.POINTER(abi.SolidMaterial)]
+    lib.ppf_scene_add_stitch.restype = C.c_int
+    lib.ppf_scene_add_stitch.argtypes = [P, _u32, _f32, C.c_float]
     lib.ppf_scene_set_velocity.argtypes = [P, _f32]
     lib.ppf_scene_pin.argtypes = [P, _u32, C.c_uint, C.c_int]
     lib.ppf_scene_pull.argtypes = [P, _u32, C.c_uint, C.c_float]
@@ -225,6 +227,14 @@ class Scene:
                              t.reshape(-1, 4).copy(), material))
         return int(self.lib.ppf_scene_add_solid(self.h, v, v.size // 3, t, t.size // 4,
                                                 C.byref(m)))
+
+    def add_stitch(self, index, weight, stiffness: float = 1.0) -> None:
+        """A stitch between the barycentric points index[0:3] / weight[0:3]
+        and index[3:6] / weight[3:6] (vertex indices as added)."""
+        i = np.ascontiguousarray(index, np.uint32).reshape(6)
+        w = np.ascontiguousarray(weight, np.float32).reshape(6)
+        if self.lib.ppf_scene_add_stitch(self.h, i, w, float(stiffness)) != 0:
+            raise ValueError("stitch index out of range")
 
     def set_velocity(self, velocity):
         v = np.ascontiguousarray(velocity, np.float32).reshape(-1)

@@ -4,7 +4,7 @@ solver executable (csrc/driver/main.cpp).
 `write_session` writes the subset of the layout the reference's frontend
 exports (frontend/_scene_.py:806-1000, read back by crates/ppf-cts-solver/
 src/scene.rs:443-1110) that this library simulates: shells with per-face
-materials, rods with per-rod materials, fix and pull pins without
+materials, rods with per-rod materials, stitches, fix and pull pins without
 operations, one-keyframe walls and
 spheres, and a static collision mesh; info.toml and param.toml as the
 frontend writes them. `read_frame` reads a vert_<n>.bin the executable
@@ -54,6 +54,9 @@ class SessionScene:
     param: dict = field(default_factory=dict)          # [param] keys of param.toml
     rod: np.ndarray | None = None        # (R, 2) vertex indices of rod edges
     rod_params: dict = field(default_factory=dict)     # name -> (R,) float32, e.g. "bend"
+    stitch_ind: np.ndarray | None = None  # (M, 6) vertex indices
+    stitch_w: np.ndarray | None = None    # (M, 6) barycentric weights
+    stitch_stiffness: np.ndarray | None = None  # (M,)
 
 
 def _toml_value(v):
@@ -72,11 +75,12 @@ def write_session(path, sc: SessionScene) -> Path:
     (b / "param").mkdir(parents=True, exist_ok=True)
     n, nf = len(sc.vert), len(sc.tri)
     nr = 0 if sc.rod is None else len(sc.rod)
+    n_seam = 0 if sc.stitch_ind is None else len(sc.stitch_ind)
     ns = 0 if sc.static_vert is None else len(sc.static_vert)
     nst = 0 if sc.static_tri is None else len(sc.static_tri)
     lines = ["[count]", f"vert = {n}", f"rod = {nr}", f"tri = {nf}", "tet = 0",
              f"static_vert = {ns}", f"static_tri = {nst}", f"pin_block = {len(sc.pins)}",
-             f"wall = {len(sc.walls)}", f"sphere = {len(sc.spheres)}", "stitch = 0",
+             f"wall = {len(sc.walls)}", f"sphere = {len(sc.spheres)}", f"stitch = {n_seam}",
              "rod_vert_start = 0", "rod_vert_end = 0", "shell_vert_start = 0",
              f"shell_vert_end = {n}", "rod_count = 0", "shell_count = 1", ""]
     for i, (ind, pull) in enumerate(sc.pins):
@@ -112,6 +116,11 @@ def write_session(path, sc: SessionScene) -> Path:
             np.asarray(v, np.uint8).tofile(b / "param" / "tri-model.bin")
         else:
             np.asarray(v, np.float32).tofile(b / "param" / f"tri-{k}.bin")
+    if n_seam:
+        np.asarray(sc.stitch_ind, np.uint64).tofile(b / "stitch_ind.bin")
+        np.asarray(sc.stitch_w, np.float32).tofile(b / "stitch_w.bin")
+        if sc.stitch_stiffness is not None:
+            np.asarray(sc.stitch_stiffness, np.float32).tofile(b / "stitch_stiffness.bin")
     if nr:
         np.asarray(sc.rod, np.uint64).tofile(b / "rod.bin")
         for k, v in sc.rod_params.items():

@@ -1,7 +1,8 @@
 """Freezes the reference's own Newton-system assembly, line searches and
 intersection checks on the two-sheets scene, and its assembly and rod
 strain-limit line search on the rods-and-sheet scene (ref_rods.npz), and its
-assembly on the solids-and-sheet scene (ref_solids.npz).
+assembly on the solids-and-sheet scene (ref_solids.npz) and the stitched
+sheets (ref_stitches.npz).
 
 Builds oracle/_ref/libppfref_pipe.so from the reference sources
 (oracle/Makefile), drives it through the states of
@@ -53,25 +54,29 @@ def main():
     np.savez_compressed(path, **out)
     print("wrote", len(out), "arrays,", path.stat().st_size, "bytes")
     rods(ref)
-    solids(ref)
+    for name, make in (("solids", step_scenes.solids_and_sheet),
+                       ("stitches", step_scenes.stitched_sheets)):
+        sc, _ = make()
+        out = first_system(ref, sc)
+        path = Path(__file__).parent / f"ref_{name}.npz"
+        np.savez_compressed(path, **out)
+        print("wrote", len(out), "arrays,", path.stat().st_size, "bytes",
+              "contacts", int(out["contacts"]))
 
 
-def solids(ref):
-    """The solids-and-sheet scene's first Newton system at its start state
-    (ARAP and SNHk tets with damping, an StVK sheet, contact between the
-    solids' boundary faces and the sheet), as the reference assembles it."""
-    sc, info = step_scenes.solids_and_sheet()
+def first_system(ref, sc):
+    """A scene's first Newton system at its start state as the reference
+    assembles it: the solids-and-sheet scene (ARAP and SNHk tets with
+    damping, an StVK sheet, contact on the solids' boundary faces) and the
+    stitched sheets (vertex-to-face and vertex-to-vertex stitches)."""
     prm = sc.param.contents
     assert ref.refpipe_init(sc.dataset, C.byref(prm))
     curr, prev = rpc.dataset_positions(sc)
     target = rpc.step_target(sc, curr, prev)
     dt = float(np.float32(prm.dt) * np.float32(prm.playback))
     keys, blocks, force, count = rpc.reference_first_system(ref, curr, prev, prm, target, dt)
-    out = {"keys": keys, "blocks": blocks.astype(np.float32), "force": force,
-           "contacts": np.uint32(count), "target": target}
-    path = Path(__file__).parent / "ref_solids.npz"
-    np.savez_compressed(path, **out)
-    print("wrote", len(out), "arrays,", path.stat().st_size, "bytes", "contacts", count)
+    return {"keys": keys, "blocks": blocks.astype(np.float32), "force": force,
+            "contacts": np.uint32(count), "target": target}
 
 
 def rods(ref):

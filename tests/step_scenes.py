@@ -194,3 +194,38 @@ def solids_and_sheet(seed: int = 6):
         blk[:, 0] += 0.03 * (blk[:, 1] - 0.45)
     built.set_positions(curr, prev)
     return built, {"block_a": (a0, len(va)), "block_b": (b0, len(vb))}
+
+
+def stitched_sheets(seed: int = 8):
+    """Two sheets side by side, 2 mm apart, stitched along their facing
+    edges: each of sheet A's edge vertices to the barycentric point of the
+    nearest face of sheet B (vertex-to-face stitches), and B's corner
+    vertices to A's (vertex-to-vertex), with two stiffnesses. No pins."""
+    rng = np.random.default_rng(seed)
+    mat = scenes.cloth_material()
+    sc = Scene()
+    side = 8
+    va, fa = meshes.grid(side, side, 0.1, 0.1)
+    va = va.astype(np.float64)
+    va[:, 0] -= 0.051
+    va[:, 1] = 0.5 + rng.uniform(-1e-5, 1e-5, len(va))
+    vb = va.copy()
+    vb[:, 0] += 0.102
+    a0 = sc.add_shell(va.astype(np.float32), fa, mat)
+    b0 = sc.add_shell(vb.astype(np.float32), fa, mat)
+    # A's right edge (x max) to B's left-edge faces
+    right = [j * side + side - 1 for j in range(side)]
+    left_faces = [k for k, f in enumerate(fa) if min(vb[f][:, 0]) < vb[:, 0].min() + 1e-9]
+    for v in right:
+        f = fa[left_faces[min(range(len(left_faces)),
+                               key=lambda k: np.linalg.norm(vb[fa[left_faces[k]]].mean(0) - va[v]))]]
+        w = rng.dirichlet([4.0, 4.0, 4.0]).astype(np.float32)
+        sc.add_stitch([a0 + v] * 3 + [b0 + int(t) for t in f], [1.0, 0.0, 0.0, *w], 0.8)
+    for v in (0, (side - 1) * side):
+        sc.add_stitch([b0 + v] * 3 + [a0 + v + side - 1] * 3, [1.0, 0.0, 0.0, 1.0, 0.0, 0.0],
+                      1.5)
+    n = sc.vertex_count
+    vel = np.zeros((n, 3), np.float32)
+    vel[b0:] = (0.05, -0.02, 0.0)
+    sc.set_velocity(vel)
+    return sc.build(scenes._param(0.01)), None

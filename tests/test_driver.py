@@ -196,8 +196,14 @@ def _rod_session(tmp_path, frames=6):
     rp = {"density": np.full(r, 0.01), "young-mod": np.full(r, 1e4), "bend": np.full(r, 0.5),
           "length-factor": np.full(r, 1.0), "strain-limit": np.full(r, 0.01),
           "contact-gap": np.full(r, 1e-3), "friction": np.full(r, 0.3)}
+    # the rod's ends stitched to the sheet's nearest vertices
+    ends = [len(v), len(v) + nr - 1]
+    near = [int(np.argmin(np.linalg.norm(v - verts[e], axis=1))) for e in ends]
+    sind = np.array([[e, e, e, m, m, m] for e, m in zip(ends, near)], np.uint64)
+    sw = np.tile(np.array([1, 0, 0, 1, 0, 0], np.float32), (2, 1))
     sc = session_io.SessionScene(
         vert=verts, tri=f, face_params=fp, rod=rod, rod_params=rp,
+        stitch_ind=sind, stitch_w=sw, stitch_stiffness=np.full(2, 0.5, np.float32),
         walls=[session_io.Wall(position=(0.0, 0.0, 0.0), contact_gap=1e-3, friction=0.5)],
         param={"dt": 0.01, "frames": frames, "fps": FPS, "auto_save": 0,
                "gravity": [0.0, -9.8, 0.0], "cg_tol": 1e-3})
@@ -210,7 +216,7 @@ def test_driver_reads_rods(driver, tmp_path):
     assert r.returncode == 0, r.stderr
     d = dict(line.split(maxsplit=1) for line in r.stdout.splitlines())
     assert int(d["vertices"]) == len(verts) and int(d["faces"]) == len(f)
-    assert int(d["rods"]) == len(rod)
+    assert int(d["rods"]) == len(rod) and int(d["stitches"]) == 2
     assert int(d["edges"]) > len(rod)  # the rod edges, then the faces' edges
 
 
@@ -231,6 +237,10 @@ def test_driver_rod_frames_follow_the_library(driver, tmp_path):
                RodMaterial(density=0.01, young_mod=1e4, bend=0.5, strain_limit=0.01,
                            contact_gap=1e-3, friction=0.3))
     sc.add_floor((0.0, 0.0, 0.0), contact_gap=1e-3, friction=0.5)
+    ends = [len(v), len(v) + len(rod)]
+    for e in ends:
+        m = int(np.argmin(np.linalg.norm(v - verts[e], axis=1)))
+        sc.add_stitch([e, e, e, m, m, m], [1, 0, 0, 1, 0, 0], 0.5)
     sc.build(scenes._param(0.01))
     s = Session(sc)
     traj, times = [sc.positions()[0].copy()], [0.0]
