@@ -286,6 +286,22 @@ unsigned ppf_schwarz_coarsen(unsigned n, const unsigned *off, const unsigned *co
                              const float *blocks, const unsigned *agg, unsigned n_agg,
                              unsigned kmax, unsigned *dom);
 
+/* The project's autotuner for the traversal kernels (no counterpart in the
+ * reference). Each of the six traversal kernels (vertex and edge proximity
+ * detection, vertex, collision-mesh vertex and edge CCD, the intersection
+ * check) tests the leaves its stackless walk reaches either in warp rounds
+ * (0: the leaves the lanes found are tested together) or on the spot (1).
+ * Both forms find the same pairs and times of impact; which is faster depends
+ * on the scene. ppf_autotune times both forms of each on the initialized
+ * scene's current state (three runs each, the minimum kept: detection at the
+ * positions, the CCD over the inertial step, the intersection check), keeps
+ * the faster and writes the six choices to modes (may be NULL); it returns
+ * 0, or -1 on a fatal error. ppf_get_tuning / ppf_set_tuning read and set
+ * the six choices (set returns -1 for a value other than 0 or 1). Defaults:
+ * 0 1 0 0 0 0. */
+int ppf_autotune(unsigned char *modes);
+void ppf_get_tuning(unsigned char *modes);
+int ppf_set_tuning(const unsigned char *modes);
 /* The CUDA stream (cudaStream_t, as void*) every kernel of advance() runs
  * on, so a host can time the step with its own events on that stream. NULL
  * before initialize(). */

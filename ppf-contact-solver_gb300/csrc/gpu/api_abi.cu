@@ -372,6 +372,44 @@ int ppf_debug_pcg(const float *b, float *x, unsigned max_iter, unsigned *iters, 
     }
 }
 
+namespace {
+void tuning_out(const ppf::gpu::Tuning &t, unsigned char *m) {
+    m[0] = t.detect_vertex;
+    m[1] = t.detect_edge;
+    m[2] = t.ccd_vertex;
+    m[3] = t.ccd_mesh_vertex;
+    m[4] = t.ccd_edge;
+    m[5] = t.isect;
+}
+} // namespace
+
+int ppf_autotune(unsigned char *modes) {
+    try {
+        const ppf::gpu::Tuning t = solver_instance().autotune();
+        if (modes) tuning_out(t, modes);
+        return 0;
+    } catch (const FatalError &e) {
+        fatal(e);
+        return -1;
+    }
+}
+
+void ppf_get_tuning(unsigned char *modes) { tuning_out(solver_instance().tuning(), modes); }
+
+int ppf_set_tuning(const unsigned char *m) {
+    for (int k = 0; k < 6; ++k)
+        if (m[k] > 1) return -1;
+    ppf::gpu::Tuning t;
+    t.detect_vertex = m[0];
+    t.detect_edge = m[1];
+    t.ccd_vertex = m[2];
+    t.ccd_mesh_vertex = m[3];
+    t.ccd_edge = m[4];
+    t.isect = m[5];
+    solver_instance().set_tuning(t);
+    return 0;
+}
+
 float ppf_debug_strain_line_search(const float *x0, const float *x1) {
     try {
         return solver_instance().debug_strain_line_search(x0, x1);

@@ -427,6 +427,7 @@ struct VertexQueryOp {
 
 // One lane per surface vertex, in the vertex tree's Morton order, so a warp's
 // queries are neighbours in space; all lanes of a warp query together.
+template <LeafTests M>
 __global__ void k_detect_vertex(Scene s, BvhView fb, BvhView eb, BvhView vb,
                                 const float *x, PairLists pl, IterStatus *st) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -440,11 +441,11 @@ __global__ void k_detect_vertex(Scene s, BvhView fb, BvhView eb, BvhView vb,
         qmax = make_float4(p[0] + m, p[1] + m, p[2] + m, 0.0f);
     }
     VertexQueryOp op{s, x, v, 0, pl, st, 0u};
-    warp_query(fb, act, qmin, qmax, op, &st->status);
+    warp_query<M>(fb, act, qmin, qmax, op, &st->status);
     op.kind = 1;
-    warp_query(eb, act, qmin, qmax, op, &st->status);
+    warp_query<M>(eb, act, qmin, qmax, op, &st->status);
     op.kind = 2;
-    warp_query(vb, act, qmin, qmax, op, &st->status);
+    warp_query<M>(vb, act, qmin, qmax, op, &st->status);
     if (op.found) atomicAdd(&st->n_contact, op.found);
 }
 
@@ -469,6 +470,7 @@ struct EdgeQueryOp {
 // One work item per edge piece (edges in the tree's Morton order).
 // Work items (edge pieces in the tree's Morton order) are taken a warp at a
 // time; a piece after the first excludes the leaves its predecessor reports.
+template <LeafTests M>
 __global__ void k_detect_edge(Scene s, BvhView eb, const float *x, PairLists pl,
                               IterStatus *st, EdgePieces ep) {
     const unsigned total = ep.off[ep.n];
@@ -495,9 +497,7 @@ __global__ void k_detect_edge(Scene s, BvhView eb, const float *x, PairLists pl,
         EdgeQueryOp op{s, x, e, pl, st, 0u};
         // a lane without an exclusion box gets one that overlaps nothing
         if (!excl) xmin.w = 0.0f;
-        // the edge-edge test is light next to the walk: leaves are tested on
-        // the spot (warp rounds measured 2.7x slower here)
-        warp_query<LeafTests::kImmediate>(eb, act, qmin, qmax, op, &st->status, &xmin, &xmax);
+        warp_query<M>(eb, act, qmin, qmax, op, &st->status, &xmin, &xmax);
         if (op.found) atomicAdd(&st->n_contact, op.found);
     }
 }
@@ -1168,11 +1168,22 @@ void launch_detect(const Scene &s, const BvhView &fb, const BvhView &eb,
                    const BvhView &vb, const AssemblyBuffers &b, PairLists &pl,
                    const PieceBuffers &pb, cudaStream_t q) {
     if (s.n_surf) {
-        k_detect_vertex<<<div_up(s.n_surf, 128u), 128, 0, q>>>(s, fb, eb, vb, b.x, pl, b.st);
+        if (s.tune.detect_vertex)
+            k_detect_vertex<LeafTests::kImmediate>
+                <<<div_up(s.n_surf, 128u), 128, 0, q>>>(s, fb, eb, vb, b.x, pl, b.st);
+        else
+            k_detect_vertex<LeafTests::kWarpRounds>
+                <<<div_up(s.n_surf, 128u), 128, 0, q>>>(s, fb, eb, vb, b.x, pl, b.st);
         PPF_LAUNCH_CHECK();
     }
     if (s.ne) {
-        k_detect_edge<<<piece_grid(s.ne, 128u), 128, 0, q>>>(s, eb, b.x, pl, b.st,
+        if (s.tune.detect_edge)
+            k_detect_edge<LeafTests::kImmediate>
+                <<<piece_grid(s.ne, 128u), 128, 0, q>>>(s, eb, b.x, pl, b.st,
+                                                            EdgePieces{pb.off, s.ne});
+        else
+            k_detect_edge<LeafTests::kWarpRounds>
+                <<<piece_grid(s.ne, 128u), 128, 0, q>>>(s, eb, b.x, pl, b.st,
                                                             EdgePieces{pb.off, s.ne});
         PPF_LAUNCH_CHECK();
     }

@@ -245,6 +245,7 @@ __device__ __forceinline__ void warp_min_toi(unsigned *bits, float toi) {
     if ((threadIdx.x & 31u) == 0u) atomicMin(bits, __float_as_uint(toi));
 }
 
+template <LeafTests M>
 __global__ void k_ccd_mesh_vertex(Scene s, BvhView fb, LineSearchArgs a) {
     const unsigned cv = blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = cv < s.ncv;
@@ -257,12 +258,13 @@ __global__ void k_ccd_mesh_vertex(Scene s, BvhView fb, LineSearchArgs a) {
         qmax = make_float4(y[0] + m, y[1] + m, y[2] + m, 0.0f);
     }
     MeshVertexCcdOp op{s, a, act ? cv : 0u, a.max_t};
-    warp_query(fb, act, qmin, qmax, op, &a.st->status);
+    warp_query<M>(fb, act, qmin, qmax, op, &a.st->status);
     warp_min_toi(&a.st->toi_vf_bits, op.toi);
 }
 
 // One lane per surface vertex in the vertex tree's Morton order; the warp's
 // lanes walk the face, vertex and collision-face trees together.
+template <LeafTests M>
 __global__ void k_ccd_vertex(Scene s, BvhView fb, BvhView vb, LineSearchArgs a) {
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = t < s.n_surf;
@@ -282,13 +284,13 @@ __global__ void k_ccd_vertex(Scene s, BvhView fb, BvhView vb, LineSearchArgs a) 
         mesh = s.ncf && vp.fix_index == 0 && vp.mass > 0.0f;
     }
     PointFaceCcdOp pf{s, a, v, a.max_t};
-    warp_query(fb, act, qmin, qmax, pf, &a.st->status);
+    warp_query<M>(fb, act, qmin, qmax, pf, &a.st->status);
     PointPointCcdOp pp{s, a, v, a.max_t};
-    warp_query(vb, act, qmin, qmax, pp, &a.st->status);
+    warp_query<M>(vb, act, qmin, qmax, pp, &a.st->status);
     toi = fminf(toi, fminf(pf.toi, pp.toi));
     if (s.ncf) {
         MeshPointFaceCcdOp mf{s, a, v, a.max_t};
-        warp_query(s.cm_face_bvh, mesh, qmin, qmax, mf, &a.st->status);
+        warp_query<M>(s.cm_face_bvh, mesh, qmin, qmax, mf, &a.st->status);
         toi = fminf(toi, mf.toi);
     }
     warp_min_toi(&a.st->toi_vf_bits, toi);
@@ -349,6 +351,7 @@ struct EdgeEdgeCcdOp {
 // One work item per edge piece: the piece swept from the previous iterate to
 // the vertex/face seed time. A leaf found by two pieces is tested twice;
 // the result is a minimum, so that changes nothing.
+template <LeafTests M>
 __global__ void k_ccd_edge(Scene s, BvhView eb, LineSearchArgs a, EdgePieces ep) {
     const unsigned total = ep.off[ep.n];
     const float seed = __uint_as_float(a.st->toi_vf_bits);
@@ -379,10 +382,10 @@ __global__ void k_ccd_edge(Scene s, BvhView eb, LineSearchArgs a, EdgePieces ep)
             mesh = s.nce && !s.eprop[e].fixed && s.eprop[e].mass > 0.0f;
         }
         EdgeEdgeCcdOp op{s, a, e, seed};
-        warp_query(eb, act, qmin, qmax, op, &a.st->status);
+        warp_query<M>(eb, act, qmin, qmax, op, &a.st->status);
         if (s.nce) {
             MeshEdgeCcdOp me{s, a, e, op.toi};
-            warp_query(s.cm_edge_bvh, mesh, qmin, qmax, me, &a.st->status);
+            warp_query<M>(s.cm_edge_bvh, mesh, qmin, qmax, me, &a.st->status);
             op.toi = me.toi;
         }
         warp_min_toi(&a.st->toi_bits, op.toi);
@@ -550,6 +553,7 @@ struct MeshFaceEdgeIsectOp {
     }
 };
 
+template <LeafTests M>
 __global__ void k_isect(Scene s, BvhView fb, BvhView eb, const float *x,
                         PpfIntersectionRecord *rec, IterStatus *st, EdgePieces ep) {
     const unsigned total = ep.off[ep.n];
@@ -579,12 +583,12 @@ __global__ void k_isect(Scene s, BvhView fb, BvhView eb, const float *x,
             mesh = s.ncf && s.eprop[e].mass > 0.0f;
         }
         FaceEdgeIsectOp op{s, x, e, rec, st};
-        warp_query(fb, act, qmin, qmax, op, &st->status, &xmin, &xmax);
+        warp_query<M>(fb, act, qmin, qmax, op, &st->status, &xmin, &xmax);
         EdgeEdgeIsectOp op2{s, x, e, rec, st};
-        warp_query(eb, act, qmin, qmax, op2, &st->status, &xmin, &xmax);
+        warp_query<M>(eb, act, qmin, qmax, op2, &st->status, &xmin, &xmax);
         if (s.ncf) {
             MeshFaceEdgeIsectOp op3{s, x, e, rec, st};
-            warp_query(s.cm_face_bvh, mesh, qmin, qmax, op3, &st->status, &xmin, &xmax);
+            warp_query<M>(s.cm_face_bvh, mesh, qmin, qmax, op3, &st->status, &xmin, &xmax);
         }
     }
 }
@@ -595,16 +599,26 @@ void launch_contact_line_search(const Scene &s, const BvhView &fb, const BvhView
                                 const BvhView &vb, const LineSearchArgs &a, float piece_len,
                                 PieceBuffers &pb, cudaStream_t q) {
     if (s.n_surf) {
-        k_ccd_vertex<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, fb, vb, a);
+        if (s.tune.ccd_vertex)
+            k_ccd_vertex<LeafTests::kImmediate><<<div_up(s.n_surf, kB), kB, 0, q>>>(s, fb, vb, a);
+        else
+            k_ccd_vertex<LeafTests::kWarpRounds><<<div_up(s.n_surf, kB), kB, 0, q>>>(s, fb, vb, a);
         PPF_LAUNCH_CHECK();
     }
     if (s.ncv) { // before the edge seed is read
-        k_ccd_mesh_vertex<<<div_up(s.ncv, kB), kB, 0, q>>>(s, fb, a);
+        if (s.tune.ccd_mesh_vertex)
+            k_ccd_mesh_vertex<LeafTests::kImmediate><<<div_up(s.ncv, kB), kB, 0, q>>>(s, fb, a);
+        else
+            k_ccd_mesh_vertex<LeafTests::kWarpRounds><<<div_up(s.ncv, kB), kB, 0, q>>>(s, fb, a);
         PPF_LAUNCH_CHECK();
     }
     if (s.ne) {
         launch_edge_pieces(s, eb, a.x0, a.x1, &a.st->toi_vf_bits, piece_len, pb, q);
-        k_ccd_edge<<<piece_grid(s.ne, kB), kB, 0, q>>>(s, eb, a, EdgePieces{pb.off, s.ne});
+        const EdgePieces ep{pb.off, s.ne};
+        if (s.tune.ccd_edge)
+            k_ccd_edge<LeafTests::kImmediate><<<piece_grid(s.ne, kB), kB, 0, q>>>(s, eb, a, ep);
+        else
+            k_ccd_edge<LeafTests::kWarpRounds><<<piece_grid(s.ne, kB), kB, 0, q>>>(s, eb, a, ep);
         PPF_LAUNCH_CHECK();
     }
     k_fold_vertex_toi<<<1, 1, 0, q>>>(a.st);
@@ -633,8 +647,13 @@ void launch_intersection_check(const Scene &s, const BvhView &fb, const BvhView 
                                float piece_len, PieceBuffers &pb, cudaStream_t q) {
     if (!s.ne) return;
     launch_edge_pieces(s, eb, x, nullptr, nullptr, piece_len, pb, q);
-    k_isect<<<piece_grid(s.ne, kB), kB, 0, q>>>(s, fb, eb, x, records, st,
-                                               EdgePieces{pb.off, s.ne});
+    const EdgePieces ep{pb.off, s.ne};
+    if (s.tune.isect)
+        k_isect<LeafTests::kImmediate>
+            <<<piece_grid(s.ne, kB), kB, 0, q>>>(s, fb, eb, x, records, st, ep);
+    else
+        k_isect<LeafTests::kWarpRounds>
+            <<<piece_grid(s.ne, kB), kB, 0, q>>>(s, fb, eb, x, records, st, ep);
     PPF_LAUNCH_CHECK();
 }
 

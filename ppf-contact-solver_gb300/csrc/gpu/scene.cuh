@@ -42,6 +42,15 @@ struct CsrView {
     const uint2 *tr; // (row, block index)
 };
 
+// How each traversal kernel tests the leaves its walk reaches: 0 in warp
+// rounds (the leaves the lanes found are tested together), 1 on the spot.
+// Both give the same pairs and times of impact; the faster form depends on
+// the scene (ppf_autotune times them).
+struct Tuning {
+    unsigned char detect_vertex = 0, detect_edge = 1, ccd_vertex = 0, ccd_mesh_vertex = 0,
+                  ccd_edge = 0, isect = 0;
+};
+
 // Everything a kernel needs to read the scene (device pointers, by value).
 struct Scene {
     unsigned n, n_surf, nf, ne, nh;
@@ -57,6 +66,7 @@ struct Scene {
     unsigned nstitch;
     const PpfStitch *stitch;
     const unsigned *stitch_slot;  // 36 per stitch
+    Tuning tune;
     const unsigned *face;
     const unsigned *edge;
     const unsigned *hinge;

@@ -204,6 +204,7 @@ Scene Solver::scene() const {
     s.inv_rest3 = inv_rest3_.data();
     s.tet_slot = tet_slot_.data();
     s.hinge_type = hinge_type_.data();
+    s.tune = tune_;
     s.nstitch = nstitch_;
     s.stitch = stitch_.data();
     s.stitch_slot = stitch_slot_.data();
@@ -1413,6 +1414,86 @@ float Solver::debug_strain_line_search(const float *x0, const float *x1) {
                              cudaMemcpyDeviceToHost, q_));
     PPF_CUDA(cudaStreamSynchronize(q_));
     return __builtin_bit_cast(float, out) / max_t;
+}
+
+void Solver::set_tuning(const Tuning &t) {
+    tune_ = t;
+    ++scene_version_; // the line-search graph holds the kernels it chose
+}
+
+Tuning Solver::autotune() {
+    const size_t n3 = 3 * (size_t)n_;
+    const float max_t = param->line_search_max_t;
+    pcg_.reserve(n_); // k_init_ls copies the last solve's result block
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    // min of three timed runs of `run` on the solver's stream, in ms
+    auto time = [&](auto &&run) {
+        float best = 1e30f;
+        for (int k = 0; k < 3; ++k) {
+            PPF_CUDA(cudaEventRecord(ev0_, q_));
+            run();
+            PPF_CUDA(cudaEventRecord(ev1_, q_));
+            PPF_CUDA(cudaEventSynchronize(ev1_));
+            float ms = 0.0f;
+            PPF_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+            best = std::min(best, ms);
+        }
+        return best;
+    };
+    // each field in turn, the others held: the kernels run one after another
+    // and do not interact, so the per-field choices compose
+    auto pick = [&](unsigned char &field, auto &&run) {
+        float t[2];
+        for (unsigned char v = 0; v < 2; ++v) {
+            field = v;
+            t[v] = time(run);
+        }
+        field = t[1] < t[0] ? 1 : 0;
+    };
+    if (!param->disable_contact && n_surf_) {
+        build_trees(curr_.data(), curr_.data(), 1.0f, true);
+        PPF_CUDA(cudaMemcpyAsync(eval_x_.data(), curr_.data(), n3 * sizeof(float),
+                                 cudaMemcpyDeviceToDevice, q_));
+        AssemblyBuffers b = abuf();
+        auto detect = [&]() {
+            PPF_CUDA(cudaMemsetAsync(st_.data(), 0, sizeof(IterStatus), q_));
+            PieceBuffers pb = pieces();
+            const Scene sc = scene();
+            launch_edge_pieces(sc, view(bvh_edge_), eval_x_.data(), nullptr, nullptr, piece_len_,
+                               pb, q_);
+            launch_detect(sc, view(bvh_face_), view(bvh_edge_), view(bvh_vert_), b, pairs_, pb,
+                          q_);
+        };
+        pick(tune_.detect_vertex, detect);
+        pick(tune_.detect_edge, detect);
+        // the CCD over the inertial step from the current positions
+        compute_target(param->dt * param->playback);
+        build_trees(curr_.data(), target_.data(), max_t, false);
+        LineSearchArgs la{curr_.data(), target_.data(), curr_.data(), st_.data(), max_t,
+                          param->ccd_eps};
+        auto ccd = [&]() {
+            k_init_ls<<<1, 1, 0, q_>>>(st_.data(), max_t, pcg_.result.data());
+            PPF_LAUNCH_CHECK();
+            PieceBuffers pb = pieces();
+            launch_contact_line_search(scene(), view(bvh_face_), view(bvh_edge_),
+                                       view(bvh_vert_), la, piece_len_, pb, q_);
+        };
+        pick(tune_.ccd_vertex, ccd);
+        if (ncv_) pick(tune_.ccd_mesh_vertex, ccd);
+        pick(tune_.ccd_edge, ccd);
+        build_trees(curr_.data(), curr_.data(), 1.0f, false);
+        auto isect = [&]() {
+            PPF_CUDA(cudaMemsetAsync(&st_.data()->n_isect, 0, sizeof(unsigned), q_));
+            PieceBuffers pb = pieces();
+            launch_intersection_check(scene(), view(bvh_face_), view(bvh_edge_), curr_.data(),
+                                      isect_.data(), st_.data(), piece_len_, pb, q_);
+        };
+        pick(tune_.isect, isect);
+    }
+    PPF_CUDA(cudaMemsetAsync(st_.data(), 0, sizeof(IterStatus), q_));
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    ++scene_version_;
+    return tune_;
 }
 
 void Solver::debug_schwarz(unsigned *sizes, std::vector<unsigned> &agg,

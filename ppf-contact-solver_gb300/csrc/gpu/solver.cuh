@@ -86,6 +86,12 @@ class Solver {
     // The Schwarz layout of the last solve: sizes {n_agg, n_dom, levels},
     // the aggregate of each vertex and the domain of each aggregate.
     void debug_schwarz(unsigned *sizes, std::vector<unsigned> &agg, std::vector<unsigned> &dom);
+    // Times both leaf-test forms of every traversal kernel on the current
+    // state (detection at the positions, the CCD over the inertial step, the
+    // intersection check) and keeps the faster of each; returns the choice.
+    Tuning autotune();
+    Tuning tuning() const { return tune_; }
+    void set_tuning(const Tuning &t);
     void release();
 
     PpfDataSet *host = nullptr;
@@ -202,6 +208,7 @@ class Solver {
     // the line-search stage captured as a CUDA graph, keyed on the scene
     cudaGraphExec_t ls_graph_ = nullptr;
     unsigned long long scene_version_ = 0, ls_key_ = ~0ull;
+    Tuning tune_;
     float ls_max_t_ = 0.0f, ls_max_dx_ = 0.0f, ls_ccd_eps_ = 0.0f;
     unsigned ls_launches_ = 0;
   public:

@@ -1,0 +1,84 @@
+"""The traversal autotuner (ppf_autotune, ppf_get_tuning, ppf_set_tuning).
+
+Each traversal kernel tests the leaves of its stackless walk in warp rounds
+or on the spot; the two forms must find the same pairs and the same times of
+impact, so the choice is free for speed. GPU: on the two-sheet scene (every
+contact kind) and the rods-and-sheet scene, the first Newton system's pair
+lists are the same sets under both forms of every kernel, and one step ends
+at the same positions within the PCG tolerance; the autotuner returns a
+valid choice and the scene steps under it.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import step_scenes
+from ppf_gb300.session import Session
+
+ALL_ROUNDS = (0, 0, 0, 0, 0, 0)
+ALL_SPOT = (1, 1, 1, 1, 1, 1)
+
+
+def _set(lib, modes):
+    lib.ppf_set_tuning.argtypes = [C.POINTER(C.c_ubyte)]
+    m = (C.c_ubyte * 6)(*modes)
+    assert lib.ppf_set_tuning(m) == 0
+
+
+def _pairs(lib, sc):
+    from oracle.binding import product_system
+
+    n = sc.vertex_count
+    dx = np.zeros(3 * n, np.float32)
+    it, rr = C.c_uint(), C.c_float()
+    assert lib.ppf_debug_newton_system(dx, C.byref(it), C.byref(rr)) == 0
+    sysm = product_system(lib, n)
+    return {k: sorted(map(tuple, sysm[k].tolist())) for k in ("pf", "pe", "pp", "ee")}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("make", [step_scenes.two_sheets, step_scenes.rods_and_sheet])
+def test_leaf_test_forms_agree(product_lib, make):
+    lib = product_lib
+    sc, _ = make()
+    curr0, prev0 = sc.positions()
+    res = {}
+    for modes in (ALL_ROUNDS, ALL_SPOT):
+        sc.set_positions(curr0, prev0)
+        sc.param.contents.time = 0.0
+        s = Session(sc)
+        _set(lib, modes)
+        res[modes] = _pairs(lib, sc)
+        sc.set_positions(curr0, prev0)
+        s = Session(sc)
+        _set(lib, modes)
+        r = s.step()
+        assert r.success()
+        res[modes, "x"] = s.positions().copy()
+    a, b = res[ALL_ROUNDS], res[ALL_SPOT]
+    assert sum(len(v) for v in a.values()) > 0
+    for k in a:
+        assert a[k] == b[k], k
+    xa, xb = res[ALL_ROUNDS, "x"], res[ALL_SPOT, "x"]
+    scale = np.abs(xa).max()
+    assert np.abs(xa - xb).max() <= 1e-5 * scale, np.abs(xa - xb).max()
+
+
+@pytest.mark.gpu
+def test_autotune_choice_is_valid(product_lib):
+    lib = product_lib
+    sc, _ = step_scenes.two_sheets()
+    s = Session(sc)
+    lib.ppf_autotune.argtypes = [C.POINTER(C.c_ubyte)]
+    m = (C.c_ubyte * 6)()
+    assert lib.ppf_autotune(m) == 0
+    modes = list(m)
+    assert all(v in (0, 1) for v in modes)
+    g = (C.c_ubyte * 6)()
+    lib.ppf_get_tuning.argtypes = [C.POINTER(C.c_ubyte)]
+    lib.ppf_get_tuning(g)
+    assert list(g) == modes
+    for _ in range(3):
+        assert s.step().success()
+    _set(lib, (0, 1, 0, 0, 0, 0))  # the defaults back for the tests after this one
