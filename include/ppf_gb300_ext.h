@@ -352,6 +352,12 @@ void ppf_debug_factor_diag(float *out);
  * x = alpha P b: the direction of the preconditioner's first output.
  * Returns the PCG state. */
 int ppf_debug_pcg(const float *b, float *x, unsigned max_iter, unsigned *iters, float *resid);
+/* The contact line search (contact.cu:2472-2740: vertex, edge and
+ * collision-mesh CCD over trees swept from x0 to x1, 3n floats each) on the
+ * initialized scene: the fraction of x1 - x0 it admits (its time of impact
+ * over line_search_max_t); overlap (may be NULL) is set when a pair starts
+ * inside its offset. */
+float ppf_debug_contact_line_search(const float *x0, const float *x1, unsigned *overlap);
 /* The strain-limit line search of faces and rod edges (strainlimiting.cu:
  * 192-305) on the initialized scene, from positions x0 to x1 (3n floats
  * each): the fraction of x1 - x0 it admits (its time of impact divided by

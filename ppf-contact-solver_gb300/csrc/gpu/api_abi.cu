@@ -410,6 +410,18 @@ int ppf_set_tuning(const unsigned char *m) {
     return 0;
 }
 
+float ppf_debug_contact_line_search(const float *x0, const float *x1, unsigned *overlap) {
+    try {
+        unsigned ov = 0;
+        const float t = solver_instance().debug_contact_line_search(x0, x1, ov);
+        if (overlap) *overlap = ov;
+        return t;
+    } catch (const FatalError &e) {
+        fatal(e);
+        return -1.0f;
+    }
+}
+
 float ppf_debug_strain_line_search(const float *x0, const float *x1) {
     try {
         return solver_instance().debug_strain_line_search(x0, x1);

@@ -86,6 +86,10 @@ __device__ __forceinline__ void st_relaxed(unsigned *p, unsigned v) {
 // The wait is bounded in wall time: a timeout (or an abort latched by
 // another block) sets STATUS_PCG_BREAKDOWN in `abort`, and every block
 // leaves the solve instead of waiting again.
+// partials a lane folds with its loads in flight together (grids up to
+// 32 * kFoldLoads blocks)
+constexpr unsigned kFoldLoads = 5;
+
 template <int N>
 __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
                          unsigned *abort) {
@@ -135,9 +139,26 @@ __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
         if (ok) {
 #pragma unroll
             for (int q = 0; q < N; ++q) x[q] = 0.0f;
-            for (unsigned k = lane; k < nb; k += 32)
+            if (nb <= 32u * kFoldLoads) {
+                // every partial loaded before the first add, so the loads are
+                // in flight together; added in the same order as the loop
+                float pv[kFoldLoads][N];
 #pragma unroll
-                for (int q = 0; q < N; ++q) x[q] += __ldcg(part + N * k + q);
+                for (unsigned j = 0; j < kFoldLoads; ++j) {
+                    const unsigned k = lane + 32u * j;
+#pragma unroll
+                    for (int q = 0; q < N; ++q) pv[j][q] = k < nb ? __ldcg(part + N * k + q) : 0.0f;
+                }
+#pragma unroll
+                for (unsigned j = 0; j < kFoldLoads; ++j)
+                    if (lane + 32u * j < nb)
+#pragma unroll
+                        for (int q = 0; q < N; ++q) x[q] += pv[j][q];
+            } else {
+                for (unsigned k = lane; k < nb; k += 32)
+#pragma unroll
+                    for (int q = 0; q < N; ++q) x[q] += __ldcg(part + N * k + q);
+            }
             for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
                 for (int q = 0; q < N; ++q) x[q] += __shfl_down_sync(0xffffffffu, x[q], off);

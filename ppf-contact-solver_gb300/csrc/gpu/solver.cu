@@ -1496,6 +1496,29 @@ Tuning Solver::autotune() {
     return tune_;
 }
 
+float Solver::debug_contact_line_search(const float *x0, const float *x1, unsigned &overlap) {
+    const size_t n3 = 3 * (size_t)n_;
+    const float max_t = param->line_search_max_t;
+    pcg_.reserve(n_); // k_init_ls copies the last solve's result block
+    PPF_CUDA(cudaMemcpyAsync(target_.data(), x0, n3 * sizeof(float), cudaMemcpyHostToDevice, q_));
+    PPF_CUDA(cudaMemcpyAsync(eval_x_.data(), x1, n3 * sizeof(float), cudaMemcpyHostToDevice, q_));
+    PPF_CUDA(cudaMemsetAsync(st_.data(), 0, sizeof(IterStatus), q_));
+    build_trees(target_.data(), target_.data(), 1.0f, true);
+    build_trees(target_.data(), eval_x_.data(), max_t, false);
+    k_init_ls<<<1, 1, 0, q_>>>(st_.data(), max_t, pcg_.result.data());
+    PPF_LAUNCH_CHECK();
+    LineSearchArgs la{target_.data(), eval_x_.data(), curr_.data(), st_.data(), max_t,
+                      param->ccd_eps};
+    PieceBuffers pb = pieces();
+    launch_contact_line_search(scene(), view(bvh_face_), view(bvh_edge_), view(bvh_vert_), la,
+                               piece_len_, pb, q_);
+    IterStatus st;
+    PPF_CUDA(cudaMemcpyAsync(&st, st_.data(), sizeof(IterStatus), cudaMemcpyDeviceToHost, q_));
+    PPF_CUDA(cudaStreamSynchronize(q_));
+    overlap = st.overlap;
+    return bits_to_float(st.toi_bits) / max_t;
+}
+
 void Solver::debug_schwarz(unsigned *sizes, std::vector<unsigned> &agg,
                            std::vector<unsigned> &dom) {
     const SchwarzLayout &S = schwarz_;

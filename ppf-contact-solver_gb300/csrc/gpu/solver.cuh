@@ -83,6 +83,9 @@ class Solver {
     // The strain-limit line search (faces and rods) from x0 to x1, as the
     // fraction of x1 - x0 it admits (the time of impact over max_t).
     float debug_strain_line_search(const float *x0, const float *x1);
+    // The contact line search (CCD over trees swept from x0 to x1), as the
+    // fraction of x1 - x0 it admits; `overlap` reports a start inside an offset.
+    float debug_contact_line_search(const float *x0, const float *x1, unsigned &overlap);
     // The Schwarz layout of the last solve: sizes {n_agg, n_dom, levels},
     // the aggregate of each vertex and the domain of each aggregate.
     void debug_schwarz(unsigned *sizes, std::vector<unsigned> &agg, std::vector<unsigned> &dom);

@@ -4,9 +4,9 @@ Each traversal kernel tests the leaves of its stackless walk in warp rounds
 or on the spot; the two forms must find the same pairs and the same times of
 impact, so the choice is free for speed. GPU: on the two-sheet scene (every
 contact kind) and the rods-and-sheet scene, the first Newton system's pair
-lists are the same sets under both forms of every kernel, and one step ends
-at the same positions within the PCG tolerance; the autotuner returns a
-valid choice and the scene steps under it.
+lists are the same sets under both forms of every kernel, and the contact
+line search returns the same time of impact bit for bit; the autotuner
+returns a valid choice and the scene steps under it.
 """
 import ctypes as C
 
@@ -37,32 +37,53 @@ def _pairs(lib, sc):
     return {k: sorted(map(tuple, sysm[k].tolist())) for k in ("pf", "pe", "pp", "ee")}
 
 
+def _line_search(lib, x0, x1):
+    lib.ppf_debug_contact_line_search.restype = C.c_float
+    lib.ppf_debug_contact_line_search.argtypes = [C.POINTER(C.c_float)] * 2 + [
+        C.POINTER(C.c_uint)]
+    ov = C.c_uint()
+    a = np.ascontiguousarray(x0, np.float32).reshape(-1)
+    b = np.ascontiguousarray(x1, np.float32).reshape(-1)
+    t = lib.ppf_debug_contact_line_search(a.ctypes.data_as(C.POINTER(C.c_float)),
+                                          b.ctypes.data_as(C.POINTER(C.c_float)), C.byref(ov))
+    return t, ov.value
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("make", [step_scenes.two_sheets, step_scenes.rods_and_sheet])
 def test_leaf_test_forms_agree(product_lib, make):
+    """Pair sets equal, and the contact line search's time of impact equal
+    bit for bit, under either form of every kernel: the Newton direction of
+    the first system and a sweep that drives the upper object through the
+    lower one."""
     lib = product_lib
     sc, _ = make()
-    curr0, prev0 = sc.positions()
+    n = sc.vertex_count
+    x0 = sc.positions()[0].copy()
+    order = sc.array("vertex_order")
+    s = Session(sc)
     res = {}
     for modes in (ALL_ROUNDS, ALL_SPOT):
-        sc.set_positions(curr0, prev0)
-        sc.param.contents.time = 0.0
-        s = Session(sc)
         _set(lib, modes)
         res[modes] = _pairs(lib, sc)
-        sc.set_positions(curr0, prev0)
-        s = Session(sc)
-        _set(lib, modes)
-        r = s.step()
-        assert r.success()
-        res[modes, "x"] = s.positions().copy()
+        dx = np.zeros(3 * n, np.float32)
+        it, rr = C.c_uint(), C.c_float()
+        lib.ppf_debug_newton_system(dx, C.byref(it), C.byref(rr))
+        xd = np.empty_like(x0)
+        xd[order] = x0  # the DataSet's vertex order
+        down = xd.copy()
+        down[:, 1] -= 4e-3 * np.linspace(0.0, 1.0, n)
+        res[modes, "ls"] = (_line_search(lib, xd, xd - dx.reshape(-1, 3)),
+                            _line_search(lib, xd, down))
     a, b = res[ALL_ROUNDS], res[ALL_SPOT]
     assert sum(len(v) for v in a.values()) > 0
     for k in a:
         assert a[k] == b[k], k
-    xa, xb = res[ALL_ROUNDS, "x"], res[ALL_SPOT, "x"]
-    scale = np.abs(xa).max()
-    assert np.abs(xa - xb).max() <= 1e-5 * scale, np.abs(xa - xb).max()
+    assert res[ALL_ROUNDS, "ls"] == res[ALL_SPOT, "ls"], (res[ALL_ROUNDS, "ls"],
+                                                         res[ALL_SPOT, "ls"])
+    assert res[ALL_ROUNDS, "ls"][1][0] < 1.0  # the sweep meets a contact
+    _set(lib, (0, 1, 0, 0, 0, 0))
+    del s
 
 
 @pytest.mark.gpu

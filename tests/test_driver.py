@@ -242,16 +242,28 @@ def test_driver_rod_frames_follow_the_library(driver, tmp_path):
         m = int(np.argmin(np.linalg.norm(v - verts[e], axis=1)))
         sc.add_stitch([e, e, e, m, m, m], [1, 0, 0, 1, 0, 0], 0.5)
     sc.build(scenes._param(0.01))
-    s = Session(sc)
-    traj, times = [sc.positions()[0].copy()], [0.0]
-    while times[-1] < 6 / FPS:
-        assert s.step().success()
-        traj.append(s.positions().copy())
-        times.append(s.time)
+    curr0, prev0 = sc.positions()
+
+    def trajectory():
+        sc.set_positions(curr0, prev0)
+        sc.param.contents.time = 0.0
+        s = Session(sc)
+        traj, times = [curr0.copy()], [0.0]
+        while times[-1] < 6 / FPS:
+            assert s.step().success()
+            traj.append(s.positions().copy())
+            times.append(s.time)
+        return traj, times
+
     # the rod rests 1.5 mm above the sheet, its ends stitched to it: contacts
-    # and stitches switch on near their thresholds, where one last bit can
-    # move a decision, so frames agree to a tenth of the contact gap
+    # and stitches switch on near their thresholds, where the order of the
+    # assembly's atomic sums moves decisions, so two runs of the library part
+    # by up to ~1 mm over these frames. The executable's frames must stay
+    # within twice that run-to-run spread of the library's trajectory.
+    (t1, s1), (t2, s2) = trajectory(), trajectory()
     for k in range(7):
         got = session_io.read_frame(out, k)
-        want = _interp(traj, times, k / FPS)
-        assert np.abs(got - want).max() <= 1e-4, (k, np.abs(got - want).max())
+        a, b = _interp(t1, s1, k / FPS), _interp(t2, s2, k / FPS)
+        spread = float(np.abs(a - b).max())
+        d = float(min(np.abs(got - a).max(), np.abs(got - b).max()))
+        assert d <= 2.0 * spread + 1e-5, (k, d, spread)
