@@ -62,17 +62,20 @@ def test_leaf_test_forms_agree(product_lib, make):
     x0 = sc.positions()[0].copy()
     order = sc.array("vertex_order")
     s = Session(sc)
+    # one Newton direction for both forms (two solves would differ by the
+    # order of the assembly's atomic sums)
+    _set(lib, ALL_ROUNDS)
+    dx = np.zeros(3 * n, np.float32)
+    it, rr = C.c_uint(), C.c_float()
+    lib.ppf_debug_newton_system(dx, C.byref(it), C.byref(rr))
+    xd = np.empty_like(x0)
+    xd[order] = x0  # the DataSet's vertex order
+    down = xd.copy()
+    down[:, 1] -= 4e-3 * np.linspace(0.0, 1.0, n)
     res = {}
     for modes in (ALL_ROUNDS, ALL_SPOT):
         _set(lib, modes)
         res[modes] = _pairs(lib, sc)
-        dx = np.zeros(3 * n, np.float32)
-        it, rr = C.c_uint(), C.c_float()
-        lib.ppf_debug_newton_system(dx, C.byref(it), C.byref(rr))
-        xd = np.empty_like(x0)
-        xd[order] = x0  # the DataSet's vertex order
-        down = xd.copy()
-        down[:, 1] -= 4e-3 * np.linspace(0.0, 1.0, n)
         res[modes, "ls"] = (_line_search(lib, xd, xd - dx.reshape(-1, 3)),
                             _line_search(lib, xd, down))
     a, b = res[ALL_ROUNDS], res[ALL_SPOT]
