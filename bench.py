@@ -71,6 +71,14 @@ def _env_rank():
             int(os.environ.get("WORLD_SIZE", "1")))
 
 
+def _iteration_graph_stats(lib):
+    import ctypes as C
+
+    out = (C.c_ulonglong * 4)()
+    lib.ppf_iteration_graph_stats(out)
+    return [int(v) for v in out]
+
+
 def _peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -230,6 +238,7 @@ def run_ours(args, rank, local_rank, world):
     torch.cuda.synchronize()
     sampler.start()
     launches0 = lib.ppf_kernel_launches()
+    graph0 = _iteration_graph_stats(lib)
     for k in range(args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
@@ -252,6 +261,8 @@ def run_ours(args, rank, local_rank, world):
                               int(st.dyn_blocks[i])])
     torch.cuda.synchronize()
     launches = int(lib.ppf_kernel_launches() - launches0)
+    graph = {k: b - a for k, a, b in zip(("direct", "captures", "replays", "repeats"), graph0,
+                                         _iteration_graph_stats(lib))}
     clocks = sampler.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
@@ -359,6 +370,10 @@ def run_ours(args, rank, local_rank, world):
                          "(ppf_transfer_bytes), mean per timed step",
                 "path": "update_constraint + advance + fetch (C ABI, host DataSet)"},
         "gpu_launches": launches,
+        # Newton iterations of the timed steps as one CUDA graph each: run
+        # directly under a new capture key, captured, replayed, repeated
+        # after a capacity overran
+        "iteration_graph": graph,
         "clocks": clocks,
         "tuning": tuning,
     }

@@ -309,13 +309,36 @@ void *ppf_stream(void);
 /* Number of kernels this library has launched since it was loaded (the
  * kernels of a replayed CUDA graph count each time). */
 unsigned long long ppf_kernel_launches(void);
-/* Replays of the CUDA graph that holds a Newton iteration's line-search stage
+/* Launches of a CUDA graph that holds a Newton iteration's line-search stage
  * (the rescaled step, the swept-box refits, the contact and strain-limit line
- * searches and the status copy): one per Newton iteration. The graph is
- * captured at the first iteration after initialize, update_constraint or a
- * change of the active collision windows. No counterpart in the reference
- * (which captures its PCG iteration, solver/solver.cu:1195-1244). */
+ * searches and the status copy): the whole-iteration graph below, or, for an
+ * iteration that runs outside it, a graph of that stage alone. No counterpart
+ * in the reference (which captures its PCG iteration,
+ * solver/solver.cu:1195-1244). */
 unsigned long long ppf_graph_launches(void);
+/* The whole Newton iteration as one CUDA graph: status reset, assembly
+ * (elastic terms, detection, contact blocks, the PCG's operator layout and
+ * preconditioner), the PCG solve, the line search and the status copy, with
+ * no read-back until the status copy. Its launches are sized by capacities
+ * (the pair lists and a contact-block capacity) and read the counts on the
+ * device; an iteration whose counts overran a capacity changes nothing and
+ * is repeated after the host grows it. The first iteration under a new
+ * capture key (scene, parameters but the clock, capacities, device buffers)
+ * runs its launches directly, the next captures them, later ones replay the
+ * graph. It serves block-Jacobi and (once its layout is set up) Schwarz
+ * solves; the factored preconditioners size their builds on the host and run
+ * outside it. On by default; ppf_set_iteration_graph(0) turns it off (the
+ * assembly then reads the counts back and sizes to them, and the line-search
+ * stage alone is a graph). ppf_iteration_graph_stats writes four counts since
+ * the library was loaded: iterations run directly, graphs captured, graph
+ * replays, iterations repeated after an overrun. */
+void ppf_set_iteration_graph(int enable);
+void ppf_iteration_graph_stats(unsigned long long *out);
+/* Debug: caps the pair lists at pair_cap entries each and the iteration
+ * graph's contact-block capacity at block_cap (0 leaves one as it is), to
+ * exercise the overrun-and-repeat path. The capacities grow again as counts
+ * require. */
+void ppf_debug_set_contact_capacity(unsigned pair_cap, unsigned block_cap);
 /* Bytes copied host -> device and device -> host by the library since it was
  * loaded, counted at the copies of the per-step path: update_constraint's
  * uploads, the status and count reads inside advance(), intersection

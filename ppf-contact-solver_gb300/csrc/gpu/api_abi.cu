@@ -298,7 +298,20 @@ int ppf_set_preconditioner(int kind, float param) {
 void *ppf_stream(void) { return (void *)solver_instance().stream(); }
 
 unsigned long long ppf_kernel_launches(void) { return ppf::gpu::g_kernel_launches; }
-unsigned long long ppf_graph_launches(void) { return solver_instance().ls_replays_; }
+unsigned long long ppf_graph_launches(void) {
+    return solver_instance().ls_replays_ + solver_instance().graph_stats_.replays;
+}
+void ppf_set_iteration_graph(int enable) { solver_instance().graph_enabled_ = enable != 0; }
+void ppf_iteration_graph_stats(unsigned long long *out) {
+    const auto &g = solver_instance().graph_stats_;
+    out[0] = g.direct;
+    out[1] = g.captures;
+    out[2] = g.replays;
+    out[3] = g.repeats;
+}
+void ppf_debug_set_contact_capacity(unsigned pair_cap, unsigned block_cap) {
+    solver_instance().set_contact_capacity(pair_cap, block_cap);
+}
 void ppf_transfer_bytes(unsigned long long *h2d, unsigned long long *d2h) {
     if (h2d) *h2d = ppf::gpu::g_h2d_bytes;
     if (d2h) *d2h = ppf::gpu::g_d2h_bytes;

@@ -40,7 +40,8 @@ __device__ __forceinline__ Mat2 load_inv_rest(const float *p) {
 }
 
 // ---- inertia, air drag, pull pins (energy.cu:182-270, 700-716) ------------
-__global__ void k_vertex_energy(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_vertex_energy(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.n) return;
     const PpfVertexProp &vp = s.vprop[i];
@@ -133,7 +134,8 @@ __device__ __forceinline__ void scatter_blocks(float *fixed_val, const unsigned 
         }
 }
 
-__global__ void k_face_energy(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_face_energy(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.nf_shell) return;
     const PpfFaceProp &pr = s.fprop[i];
@@ -166,7 +168,8 @@ __global__ void k_face_energy(Scene s, StepParams p, AssemblyBuffers b) {
 }
 
 // ---- dihedral bending (energy.cu:448-553) ----------------------------------
-__global__ void k_hinge_energy(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_hinge_energy(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.nh) return;
     const PpfHingeProp &pr = s.hprop[i];
@@ -212,7 +215,8 @@ __global__ void k_hinge_energy(Scene s, StepParams p, AssemblyBuffers b) {
 }
 
 // ---- rod stretch (energy.cu:272-302) ---------------------------------------
-__global__ void k_rod_energy(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_rod_energy(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.nr) return;
     const PpfEdgeProp &pr = s.eprop[i];
@@ -230,7 +234,8 @@ __global__ void k_rod_energy(Scene s, StepParams p, AssemblyBuffers b) {
 }
 
 // ---- rod bending at an interior rod vertex (energy.cu:555-641) -------------
-__global__ void k_rod_bend(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_rod_bend(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.n_surf) return;
     const PpfVertexProp &vp = s.vprop[i];
@@ -262,7 +267,8 @@ __global__ void k_rod_bend(Scene s, StepParams p, AssemblyBuffers b) {
 }
 
 // ---- stitches (energy.cu:796-884) ---------------------------------------------
-__global__ void k_stitch_energy(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_stitch_energy(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.nstitch) return;
     const PpfStitch &st = s.stitch[i];
@@ -289,7 +295,8 @@ __global__ void k_stitch_energy(Scene s, StepParams p, AssemblyBuffers b) {
 }
 
 // ---- solids (energy.cu:395-446) ------------------------------------------------
-__global__ void k_tet_energy(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_tet_energy(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.nt) return;
     const PpfTetProp &pr = s.tprop[i];
@@ -310,7 +317,8 @@ __global__ void k_tet_energy(Scene s, StepParams p, AssemblyBuffers b) {
 }
 
 // ---- strain-limit barrier (strainlimiting.cu:46-98) -------------------------
-__global__ void k_strain_limit(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_strain_limit(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.nf_shell) return;
     const PpfFaceProp &pr = s.fprop[i];
@@ -345,7 +353,8 @@ __global__ void k_strain_limit(Scene s, StepParams p, AssemblyBuffers b) {
 }
 
 // ---- rod strain-limit barrier (strainlimiting.cu:122-190) --------------------
-__global__ void k_rod_strain_limit(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_rod_strain_limit(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.nr) return;
     const PpfEdgeProp &pr = s.eprop[i];
@@ -535,6 +544,10 @@ __device__ __forceinline__ unsigned hash_key(unsigned long long k) {
 }
 
 __device__ void hash_insert(DynMatrix &dm, unsigned long long key, IterStatus *st) {
+    // past the block capacity the iteration is repeated with a larger one:
+    // stop inserting (the table, sized at least twice the capacity plus the
+    // threads in flight, never fills)
+    if (*(volatile unsigned *)&st->n_dyn > dm.cap) return;
     unsigned mask = dm.hcap - 1u;
     unsigned h = hash_key(key) & mask;
     for (unsigned probe = 0; probe < dm.hcap; ++probe) {
@@ -546,7 +559,8 @@ __device__ void hash_insert(DynMatrix &dm, unsigned long long key, IterStatus *s
         if (prev == key) return;
         h = (h + 1u) & mask;
     }
-    atomicOr(&st->status, STATUS_BLOCK_OVERFLOW);
+    // a full table: more blocks than the capacity it was sized for
+    atomicOr(&st->status, STATUS_PAIR_OVERFLOW);
 }
 
 __device__ unsigned hash_find(const DynMatrix &dm, unsigned long long key) {
@@ -596,48 +610,85 @@ __device__ __forceinline__ void pair_indices_ee(const Scene &s, uint2 pr, unsign
     idx[3] = c[1];
 }
 
-__global__ void k_dyn_insert(Scene s, PairLists pl, unsigned n_pf, unsigned n_pe,
-                             unsigned n_pp, unsigned n_ee, DynMatrix dm, IterStatus *st) {
+// Pair counts as detected, clamped to the lists' capacities; none in an
+// iteration flagged for a repeat (a list or the block capacity overran).
+struct PairCounts {
+    unsigned pf = 0, pe = 0, pp = 0, ee = 0;
+    __device__ __forceinline__ PairCounts(const PairLists &pl, const IterStatus *st) {
+        if (st->status & STATUS_PAIR_OVERFLOW) return;
+        pf = min(st->n_pf, pl.cap_pf);
+        pe = min(st->n_pe, pl.cap_pe);
+        pp = min(st->n_pp, pl.cap_pp);
+        ee = min(st->n_ee, pl.cap_ee);
+    }
+};
+
+__global__ void k_dyn_insert(Scene s, PairLists pl, DynMatrix dm, IterStatus *st) {
+    const PairCounts n(pl, st);
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n_pf) {
+    if (t < n.pf) {
         unsigned idx[4];
         pair_indices_pf(s, pl.pf[t], idx);
         insert_pair_keys<4>(s, dm, idx, st);
         return;
     }
-    t -= n_pf;
-    if (t < n_pe) {
+    t -= n.pf;
+    if (t < n.pe) {
         unsigned idx[3];
         pair_indices_pe(s, pl.pe[t], idx);
         insert_pair_keys<3>(s, dm, idx, st);
         return;
     }
-    t -= n_pe;
-    if (t < n_pp) {
+    t -= n.pe;
+    if (t < n.pp) {
         unsigned idx[2] = {pl.pp[t].x, pl.pp[t].y};
         insert_pair_keys<2>(s, dm, idx, st);
         return;
     }
-    t -= n_pp;
-    if (t < n_ee) {
+    t -= n.pp;
+    if (t < n.ee) {
         unsigned idx[4];
         pair_indices_ee(s, pl.ee[t], idx);
         insert_pair_keys<4>(s, dm, idx, st);
     }
 }
 
-__global__ void k_dyn_count(DynMatrix dm) {
+// Zeroes the values of the n_dyn unique contact blocks (grid-stride).
+__global__ void k_zero_dyn_val(DynMatrix dm, const IterStatus *st) {
+    const size_t m = 9 * (size_t)min(st->n_dyn, dm.cap);
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < m;
+         e += (size_t)gridDim.x * blockDim.x)
+        dm.val[e] = 0.0f;
+}
+
+// Marks an iteration whose pair lists were too short for what detection
+// found: its pair sets were cut at the capacities, so the host grows the
+// lists and repeats the iteration (the step's rescale turns it into a no-op).
+__global__ void k_pair_capacity(PairLists pl, IterStatus *st) {
+    if (st->n_pf > pl.cap_pf || st->n_pe > pl.cap_pe || st->n_pp > pl.cap_pp ||
+        st->n_ee > pl.cap_ee)
+        atomicOr(&st->status, STATUS_PAIR_OVERFLOW);
+}
+
+// More unique contact blocks than the block capacity: flag the iteration for
+// a repeat with a larger one, and leave the contact CSR empty (the counts and
+// the fill below skip a flagged iteration, the pair kernels see no pairs).
+__global__ void k_dyn_capacity(DynMatrix dm, IterStatus *st) {
+    if (st->n_dyn > dm.cap) atomicOr(&st->status, STATUS_PAIR_OVERFLOW);
+}
+
+__global__ void k_dyn_count(DynMatrix dm, const IterStatus *st) {
     unsigned h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= dm.hcap) return;
+    if (h >= dm.hcap || (st->status & STATUS_PAIR_OVERFLOW)) return;
     unsigned long long k = dm.hkey[h];
     if (k == kEmptyKey) return;
     atomicAdd(&dm.cnt[(unsigned)(k >> 32)], 1u);
     atomicAdd(&dm.cnt2[(unsigned)k], 1u);
 }
 
-__global__ void k_dyn_fill(DynMatrix dm) {
+__global__ void k_dyn_fill(DynMatrix dm, const IterStatus *st) {
     unsigned h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= dm.hcap) return;
+    if (h >= dm.hcap || (st->status & STATUS_PAIR_OVERFLOW)) return;
     unsigned long long k = dm.hkey[h];
     if (k == kEmptyKey) return;
     unsigned r = (unsigned)(k >> 32), c = (unsigned)k;
@@ -677,10 +728,11 @@ __device__ void scatter_pair(const Scene &s, const AssemblyBuffers &b, const Dyn
 }
 
 template <int N>
-__device__ void assemble_pair(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+__device__ void assemble_pair(const Scene &s, const AssemblyBuffers &b,
                               const DynMatrix &dm, const unsigned (&idx)[N],
                               const float (&w)[N], float ghat, float offset, float mu,
                               bool friction_on, float count) {
+    const StepParams &p = *b.params;
     Vec3 x[N], x0[N];
     float mass[N];
     Mat<3 * N, 3 * N> local;
@@ -702,10 +754,10 @@ __device__ void assemble_pair(const Scene &s, const StepParams &p, const Assembl
     scatter_pair<N>(s, b, dm, idx, f, H, b.st);
 }
 
-__global__ void k_assemble_pf(Scene s, StepParams p, AssemblyBuffers b, PairLists pl,
-                              unsigned n, DynMatrix dm) {
+__global__ void k_assemble_pf(Scene s, AssemblyBuffers b, PairLists pl, DynMatrix dm) {
+    const StepParams &p = *b.params;
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
+    if (t >= PairCounts(pl, b.st).pf) return;
     uint2 pr = pl.pf[t];
     unsigned idx[4];
     pair_indices_pf(s, pr, idx);
@@ -717,13 +769,13 @@ __global__ void k_assemble_pf(Scene s, StepParams p, AssemblyBuffers b, PairList
     float offset = vp.offset + fp.offset;
     float ghat = 0.5f * (vp.ghat + fp.ghat);
     float mu = contact::combine_friction(vp.friction, fp.friction, p.friction_mode);
-    assemble_pair<4>(s, p, b, dm, idx, w, ghat, offset, mu, true, 1.0f);
+    assemble_pair<4>(s, b, dm, idx, w, ghat, offset, mu, true, 1.0f);
 }
 
-__global__ void k_assemble_pe(Scene s, StepParams p, AssemblyBuffers b, PairLists pl,
-                              unsigned n, DynMatrix dm) {
+__global__ void k_assemble_pe(Scene s, AssemblyBuffers b, PairLists pl, DynMatrix dm) {
+    const StepParams &p = *b.params;
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
+    if (t >= PairCounts(pl, b.st).pe) return;
     uint3 pr = pl.pe[t];
     unsigned idx[3];
     pair_indices_pe(s, pr, idx);
@@ -736,13 +788,13 @@ __global__ void k_assemble_pe(Scene s, StepParams p, AssemblyBuffers b, PairList
     float mu = contact::combine_friction(vp.friction, ep.friction, p.friction_mode);
     bool fr = (pr.z & 0x80000000u) != 0u;
     float count = (float)(pr.z & 0x7fffffffu);
-    assemble_pair<3>(s, p, b, dm, idx, w, ghat, offset, mu, fr, count);
+    assemble_pair<3>(s, b, dm, idx, w, ghat, offset, mu, fr, count);
 }
 
-__global__ void k_assemble_pp(Scene s, StepParams p, AssemblyBuffers b, PairLists pl,
-                              unsigned n, DynMatrix dm) {
+__global__ void k_assemble_pp(Scene s, AssemblyBuffers b, PairLists pl, DynMatrix dm) {
+    const StepParams &p = *b.params;
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
+    if (t >= PairCounts(pl, b.st).pp) return;
     uint3 pr = pl.pp[t];
     unsigned idx[2] = {pr.x, pr.y};
     float w[2] = {1.0f, -1.0f};
@@ -753,13 +805,13 @@ __global__ void k_assemble_pp(Scene s, StepParams p, AssemblyBuffers b, PairList
     float mu = contact::combine_friction(a.friction, c.friction, p.friction_mode);
     bool fr = (pr.z & 0x80000000u) != 0u;
     float count = (float)(pr.z & 0x7fffffffu);
-    assemble_pair<2>(s, p, b, dm, idx, w, ghat, offset, mu, fr, count);
+    assemble_pair<2>(s, b, dm, idx, w, ghat, offset, mu, fr, count);
 }
 
-__global__ void k_assemble_ee(Scene s, StepParams p, AssemblyBuffers b, PairLists pl,
-                              unsigned n, DynMatrix dm) {
+__global__ void k_assemble_ee(Scene s, AssemblyBuffers b, PairLists pl, DynMatrix dm) {
+    const StepParams &p = *b.params;
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
+    if (t >= PairCounts(pl, b.st).ee) return;
     uint2 pr = pl.ee[t];
     unsigned idx[4];
     pair_indices_ee(s, pr, idx);
@@ -771,11 +823,12 @@ __global__ void k_assemble_ee(Scene s, StepParams p, AssemblyBuffers b, PairList
     float offset = pa.offset + pb.offset;
     float ghat = 0.5f * (pa.ghat + pb.ghat);
     float mu = contact::combine_friction(pa.friction, pb.friction, p.friction_mode);
-    assemble_pair<4>(s, p, b, dm, idx, w, ghat, offset, mu, true, 1.0f);
+    assemble_pair<4>(s, b, dm, idx, w, ghat, offset, mu, true, 1.0f);
 }
 
 // ---- analytic sphere / floor (contact.cu:1154-1381) --------------------------
-__global__ void k_vertex_constraints(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_vertex_constraints(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.n_surf) return;
     const PpfVertexProp &vp = s.vprop[i];
@@ -844,7 +897,8 @@ struct MeshFaceOp {
     }
 };
 
-__global__ void k_mesh_vertex_face(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_mesh_vertex_face(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     const unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = v < s.n_surf;
     if (act) act = s.vprop[v].fix_index == 0 && s.vprop[v].mass > 0.0f;
@@ -909,7 +963,8 @@ struct MeshVertexOp {
     }
 };
 
-__global__ void k_mesh_face_vertex(Scene s, StepParams p, AssemblyBuffers b, BvhView fb) {
+__global__ void k_mesh_face_vertex(Scene s, AssemblyBuffers b, BvhView fb) {
+    const StepParams &p = *b.params;
     const unsigned cv = blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = cv < s.ncv;
     float4 qmin = make_float4(0.0f, 0.0f, 0.0f, 0.0f), qmax = qmin;
@@ -964,7 +1019,8 @@ struct MeshEdgeOp {
     }
 };
 
-__global__ void k_mesh_edge_edge(Scene s, StepParams p, AssemblyBuffers b) {
+__global__ void k_mesh_edge_edge(Scene s, AssemblyBuffers b) {
+    const StepParams &p = *b.params;
     const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = e < s.ne;
     if (act) act = !s.eprop[e].fixed && s.eprop[e].mass > 0.0f;
@@ -1107,47 +1163,47 @@ void exclusive_scan(const unsigned *in, unsigned *out, unsigned n, unsigned *tmp
     PPF_LAUNCH_CHECK();
 }
 
-void launch_vertex_energy(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+void launch_vertex_energy(const Scene &s, const AssemblyBuffers &b,
                           cudaStream_t q) {
     if (!s.n) return;
-    k_vertex_energy<<<div_up(s.n, kB), kB, 0, q>>>(s, p, b);
+    k_vertex_energy<<<div_up(s.n, kB), kB, 0, q>>>(s, b);
     PPF_LAUNCH_CHECK();
 }
 
-void launch_elastic(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+void launch_elastic(const Scene &s, const AssemblyBuffers &b,
                     cudaStream_t q) {
     if (s.nr) {
-        k_rod_bend<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, p, b);
+        k_rod_bend<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, b);
         PPF_LAUNCH_CHECK();
-        k_rod_energy<<<div_up(s.nr, kB), kB, 0, q>>>(s, p, b);
+        k_rod_energy<<<div_up(s.nr, kB), kB, 0, q>>>(s, b);
         PPF_LAUNCH_CHECK();
     }
     if (s.nf_shell) {
-        k_face_energy<<<div_up(s.nf_shell, kB), kB, 0, q>>>(s, p, b);
+        k_face_energy<<<div_up(s.nf_shell, kB), kB, 0, q>>>(s, b);
         PPF_LAUNCH_CHECK();
     }
     if (s.nt) {
-        k_tet_energy<<<div_up(s.nt, kB), kB, 0, q>>>(s, p, b);
+        k_tet_energy<<<div_up(s.nt, kB), kB, 0, q>>>(s, b);
         PPF_LAUNCH_CHECK();
     }
     if (s.nh) {
-        k_hinge_energy<<<div_up(s.nh, kB), kB, 0, q>>>(s, p, b);
+        k_hinge_energy<<<div_up(s.nh, kB), kB, 0, q>>>(s, b);
         PPF_LAUNCH_CHECK();
     }
     if (s.nstitch) { // after the elastic terms, before the copy (main.cu:794-797)
-        k_stitch_energy<<<div_up(s.nstitch, kB), kB, 0, q>>>(s, p, b);
+        k_stitch_energy<<<div_up(s.nstitch, kB), kB, 0, q>>>(s, b);
         PPF_LAUNCH_CHECK();
     }
 }
 
-void launch_strain_limit(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+void launch_strain_limit(const Scene &s, const AssemblyBuffers &b,
                          cudaStream_t q) {
     if (s.nf_shell) {
-        k_strain_limit<<<div_up(s.nf_shell, kB), kB, 0, q>>>(s, p, b);
+        k_strain_limit<<<div_up(s.nf_shell, kB), kB, 0, q>>>(s, b);
         PPF_LAUNCH_CHECK();
     }
     if (s.nr) {
-        k_rod_strain_limit<<<div_up(s.nr, kB), kB, 0, q>>>(s, p, b);
+        k_rod_strain_limit<<<div_up(s.nr, kB), kB, 0, q>>>(s, b);
         PPF_LAUNCH_CHECK();
     }
 }
@@ -1190,67 +1246,72 @@ void launch_detect(const Scene &s, const BvhView &fb, const BvhView &eb,
 }
 
 void launch_dyn_build(const Scene &s, const AssemblyBuffers &b, const PairLists &pl,
-                      const unsigned counts[4], DynMatrix &dm, unsigned n_dyn_max,
-                      unsigned *d_scan_tmp, cudaStream_t q) {
-    (void)n_dyn_max;
+                      const unsigned bound[4], DynMatrix &dm, unsigned *d_scan_tmp,
+                      cudaStream_t q) {
     PPF_CUDA(cudaMemsetAsync(dm.hkey, 0xff, (size_t)dm.hcap * sizeof(unsigned long long), q));
     PPF_CUDA(cudaMemsetAsync(dm.cnt, 0, s.n * sizeof(unsigned), q));
     PPF_CUDA(cudaMemsetAsync(dm.cnt2, 0, s.n * sizeof(unsigned), q));
-    unsigned total = counts[0] + counts[1] + counts[2] + counts[3];
+    const unsigned total = bound[0] + bound[1] + bound[2] + bound[3];
     if (total) {
-        k_dyn_insert<<<div_up(total, kB), kB, 0, q>>>(s, pl, counts[0], counts[1], counts[2],
-                                                      counts[3], dm, b.st);
+        k_dyn_insert<<<div_up(total, kB), kB, 0, q>>>(s, pl, dm, b.st);
         PPF_LAUNCH_CHECK();
     }
-    k_dyn_count<<<div_up(dm.hcap, kB), kB, 0, q>>>(dm);
+    k_dyn_capacity<<<1, 1, 0, q>>>(dm, b.st);
+    PPF_LAUNCH_CHECK();
+    k_dyn_count<<<div_up(dm.hcap, kB), kB, 0, q>>>(dm, b.st);
     PPF_LAUNCH_CHECK();
     exclusive_scan(dm.cnt, dm.off, s.n, d_scan_tmp, q);
     exclusive_scan(dm.cnt2, dm.tr_off, s.n, d_scan_tmp, q);
     PPF_CUDA(cudaMemsetAsync(dm.cnt, 0, s.n * sizeof(unsigned), q));
     PPF_CUDA(cudaMemsetAsync(dm.cnt2, 0, s.n * sizeof(unsigned), q));
-    k_dyn_fill<<<div_up(dm.hcap, kB), kB, 0, q>>>(dm);
+    k_dyn_fill<<<div_up(dm.hcap, kB), kB, 0, q>>>(dm, b.st);
+    PPF_LAUNCH_CHECK();
+    k_zero_dyn_val<<<2 * kNumSMs, kB, 0, q>>>(dm, b.st);
     PPF_LAUNCH_CHECK();
 }
 
-void launch_contact_assemble(const Scene &s, const StepParams &p,
-                             const AssemblyBuffers &b, const PairLists &pl,
-                             const unsigned counts[4], DynMatrix &dm, cudaStream_t q) {
-    if (counts[0]) {
-        k_assemble_pf<<<div_up(counts[0], 128u), 128, 0, q>>>(s, p, b, pl, counts[0], dm);
+void launch_pair_capacity(const PairLists &pl, IterStatus *st, cudaStream_t q) {
+    k_pair_capacity<<<1, 1, 0, q>>>(pl, st);
+    PPF_LAUNCH_CHECK();
+}
+
+void launch_contact_assemble(const Scene &s, const AssemblyBuffers &b, const PairLists &pl,
+                             const unsigned bound[4], DynMatrix &dm, cudaStream_t q) {
+    if (bound[0]) {
+        k_assemble_pf<<<div_up(bound[0], 128u), 128, 0, q>>>(s, b, pl, dm);
         PPF_LAUNCH_CHECK();
     }
-    if (counts[1]) {
-        k_assemble_pe<<<div_up(counts[1], 128u), 128, 0, q>>>(s, p, b, pl, counts[1], dm);
+    if (bound[1]) {
+        k_assemble_pe<<<div_up(bound[1], 128u), 128, 0, q>>>(s, b, pl, dm);
         PPF_LAUNCH_CHECK();
     }
-    if (counts[2]) {
-        k_assemble_pp<<<div_up(counts[2], 128u), 128, 0, q>>>(s, p, b, pl, counts[2], dm);
+    if (bound[2]) {
+        k_assemble_pp<<<div_up(bound[2], 128u), 128, 0, q>>>(s, b, pl, dm);
         PPF_LAUNCH_CHECK();
     }
-    if (counts[3]) {
-        k_assemble_ee<<<div_up(counts[3], 128u), 128, 0, q>>>(s, p, b, pl, counts[3], dm);
+    if (bound[3]) {
+        k_assemble_ee<<<div_up(bound[3], 128u), 128, 0, q>>>(s, b, pl, dm);
         PPF_LAUNCH_CHECK();
     }
 }
 
-void launch_vertex_constraints(const Scene &s, const StepParams &p,
-                               const AssemblyBuffers &b, cudaStream_t q) {
+void launch_vertex_constraints(const Scene &s, const AssemblyBuffers &b, cudaStream_t q) {
     if (!s.n_surf || (s.nsphere == 0 && s.nfloor == 0)) return;
-    k_vertex_constraints<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, p, b);
+    k_vertex_constraints<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, b);
     PPF_LAUNCH_CHECK();
 }
 
-void launch_collision_mesh(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+void launch_collision_mesh(const Scene &s, const AssemblyBuffers &b,
                            const BvhView &fb, cudaStream_t q) {
     if (!s.ncv) return;
     if (s.ncf && s.n_surf) {
-        k_mesh_vertex_face<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, p, b);
+        k_mesh_vertex_face<<<div_up(s.n_surf, kB), kB, 0, q>>>(s, b);
         PPF_LAUNCH_CHECK();
     }
-    k_mesh_face_vertex<<<div_up(s.ncv, kB), kB, 0, q>>>(s, p, b, fb);
+    k_mesh_face_vertex<<<div_up(s.ncv, kB), kB, 0, q>>>(s, b, fb);
     PPF_LAUNCH_CHECK();
     if (s.nce && s.ne) {
-        k_mesh_edge_edge<<<div_up(s.ne, kB), kB, 0, q>>>(s, p, b);
+        k_mesh_edge_edge<<<div_up(s.ne, kB), kB, 0, q>>>(s, b);
         PPF_LAUNCH_CHECK();
     }
 }

@@ -37,13 +37,14 @@ struct AssemblyBuffers {
     const float *x0;    // vertex.curr (start of step)
     const float *target;
     IterStatus *st;
+    const StepParams *params; // device copy of the step's parameters
 };
 
-void launch_vertex_energy(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+void launch_vertex_energy(const Scene &s, const AssemblyBuffers &b,
                           cudaStream_t q);
-void launch_elastic(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+void launch_elastic(const Scene &s, const AssemblyBuffers &b,
                     cudaStream_t q);
-void launch_strain_limit(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+void launch_strain_limit(const Scene &s, const AssemblyBuffers &b,
                          cudaStream_t q);
 // Per-edge piece counts for split edge queries (see contact_rules.cuh).
 struct PieceBuffers {
@@ -60,18 +61,21 @@ unsigned piece_grid(unsigned ne, unsigned block);
 void launch_detect(const Scene &s, const BvhView &fb, const BvhView &eb,
                    const BvhView &vb, const AssemblyBuffers &b, PairLists &pl,
                    const PieceBuffers &pb, cudaStream_t q);
-// Dedupes the contact blocks outside the fixed pattern and lays them out.
+// Dedupes the contact blocks outside the fixed pattern, lays them out and
+// zeroes their values. The pair counts are read on the device (clamped to
+// the lists' capacities); `bound` is an upper bound of each count (the
+// counts themselves, or the capacities) that only sizes the grids.
 void launch_dyn_build(const Scene &s, const AssemblyBuffers &b, const PairLists &pl,
-                      const unsigned counts[4], DynMatrix &dm, unsigned n_dyn_max,
-                      unsigned *d_scan_tmp, cudaStream_t q);
-void launch_contact_assemble(const Scene &s, const StepParams &p,
-                             const AssemblyBuffers &b, const PairLists &pl,
-                             const unsigned counts[4], DynMatrix &dm, cudaStream_t q);
-void launch_vertex_constraints(const Scene &s, const StepParams &p,
-                               const AssemblyBuffers &b, cudaStream_t q);
+                      const unsigned bound[4], DynMatrix &dm, unsigned *d_scan_tmp,
+                      cudaStream_t q);
+// Sets STATUS_PAIR_OVERFLOW when detection found more pairs than a list holds.
+void launch_pair_capacity(const PairLists &pl, IterStatus *st, cudaStream_t q);
+void launch_contact_assemble(const Scene &s, const AssemblyBuffers &b, const PairLists &pl,
+                             const unsigned bound[4], DynMatrix &dm, cudaStream_t q);
+void launch_vertex_constraints(const Scene &s, const AssemblyBuffers &b, cudaStream_t q);
 // Contacts against the static collision mesh (contact/contact.cu:1834-1947);
 // fb is the free faces' tree of this Newton iteration.
-void launch_collision_mesh(const Scene &s, const StepParams &p, const AssemblyBuffers &b,
+void launch_collision_mesh(const Scene &s, const AssemblyBuffers &b,
                            const BvhView &fb, cudaStream_t q);
 void launch_dirichlet(const Scene &s, const AssemblyBuffers &b, const DynMatrix &dm,
                       float *dx, cudaStream_t q);

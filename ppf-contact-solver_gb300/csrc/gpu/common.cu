@@ -24,6 +24,12 @@ namespace gpu {
 
 unsigned long long g_kernel_launches = 0;
 unsigned long long g_h2d_bytes = 0, g_d2h_bytes = 0;
+unsigned long long g_buffer_epoch = 0;
+bool g_capturing = false;
+
+void buffer_grow_during_capture() {
+    throw FatalError(4, "a device buffer had to grow while a Newton iteration was being captured");
+}
 
 void check_cuda(cudaError_t err, const char *what, const char *file, int line) {
     if (err == cudaSuccess) return;

@@ -37,6 +37,15 @@ extern unsigned long long g_kernel_launches;
 // loaded, counted at the copies of the per-step path (uploads, status reads,
 // contact-layout totals, intersection records, fetch).
 extern unsigned long long g_h2d_bytes, g_d2h_bytes;
+// Bumped whenever a DevBuf is allocated anew or released: a captured CUDA
+// graph holds raw device pointers, so it is valid only while this count is
+// the one it was captured under.
+extern unsigned long long g_buffer_epoch;
+// Set while the solver's stream is being captured into a graph; a DevBuf that
+// would have to grow then reports a host error instead of allocating (an
+// allocation would end the capture).
+extern bool g_capturing;
+void buffer_grow_during_capture();
 #define PPF_CUDA(x) ::ppf::gpu::check_cuda((x), #x, __FILE__, __LINE__)
 #define PPF_LAUNCH_CHECK()                                                              \
     (++::ppf::gpu::g_kernel_launches,                                                   \
@@ -83,13 +92,18 @@ template <class T> struct DevBuf {
     size_t cap = 0;
     void reserve(size_t n) {
         if (n <= cap) return;
+        if (g_capturing) buffer_grow_during_capture();
+        ++g_buffer_epoch;
         if (ptr) PPF_CUDA(cudaFree(ptr));
         size_t c = n < 16 ? 16 : n;
         PPF_CUDA(cudaMalloc(&ptr, c * sizeof(T)));
         cap = c;
     }
     void release() {
-        if (ptr) cudaFree(ptr);
+        if (ptr) {
+            ++g_buffer_epoch;
+            cudaFree(ptr);
+        }
         ptr = nullptr;
         cap = 0;
     }

@@ -329,7 +329,6 @@ struct PcgArgs {
     PcgOperator A;
     const unsigned *task_start; // grid + 1: each block's static range of product
                                 // tasks; task_start[grid] starts the common pool
-    unsigned n_tasks;
     unsigned *dyn_ctr;          // one zeroed counter per product phase
     unsigned n_ctr;
     float *x, *r;
@@ -429,20 +428,40 @@ __device__ __forceinline__ Vec3 row_product(const PcgArgs &g, unsigned i) {
     return ap;
 }
 
+// The product task list of one solve: overflow rows [0, t1), contact half
+// slices [t1, t2), fixed half slices [t2, total). The contact row and
+// overflow row counts are read from the device when the layout carries
+// them, so a solve launched before they are known (a captured iteration)
+// partitions the same list.
+struct TaskSpace {
+    unsigned t1, t2, total, c_rows;
+    __device__ __forceinline__ explicit TaskSpace(const PcgOperator &A) {
+        unsigned rows = A.contact.rows, n_ovf = A.ovf.count;
+        if (A.contact.sizes) {
+            rows = __ldg(A.contact.sizes);
+            n_ovf = __ldg(A.contact.sizes + 1);
+        }
+        c_rows = rows;
+        t1 = n_ovf;
+        t2 = t1 + 2 * ((rows + kSliceRows - 1) / kSliceRows);
+        total = t2 + 2 * A.fixed.n_slices;
+    }
+};
+
 // One product task of warp `lane`s: the fixed part of a half slice, the
 // contact part of a half slice of sorted contact rows, or an overflow row.
 // The epilogue gets (row, A-part, |terms|) on the lanes that own a result.
 // `vals` are the value arrays the slots are read from: the operator's own
 // (fixed, contact, overflow) or a factor's parallel ones.
 template <int MASK, class V, class G, class E>
-__device__ __forceinline__ void product_task(const PcgArgs &g, const V *const vals[3],
-                                             unsigned task, unsigned lane, const G &gather,
-                                             E &&epilogue) {
+__device__ __forceinline__ void product_task(const PcgArgs &g, const TaskSpace &ts,
+                                             const V *const vals[3], unsigned task,
+                                             unsigned lane, const G &gather, E &&epilogue) {
     const PcgOperator &A = g.A;
     // task order: overflow rows, contact half slices, fixed half slices (the
     // long and uneven items first, so the common pool at the end of the
     // order holds short, even ones)
-    const unsigned t1 = A.ovf.count, t2 = t1 + 2 * A.contact.sell.n_slices;
+    const unsigned t1 = ts.t1, t2 = ts.t2;
     const unsigned par = lane >> 4;
     Vec3 acc = Vec3::zero(), ab = Vec3::zero();
     if (task >= t1) {
@@ -455,14 +474,14 @@ __device__ __forceinline__ void product_task(const PcgArgs &g, const V *const va
         unsigned row = 0xFFFFFFFFu;
         if (MASK != kAllSlots) {
             if (fixed) row = q < A.n ? q : 0xFFFFFFFFu;
-            else row = q < A.contact.rows ? __ldg(A.contact.perm + q) : 0xFFFFFFFFu;
+            else row = q < ts.c_rows ? __ldg(A.contact.perm + q) : 0xFFFFFFFFu;
         }
         sell_half_row<MASK>(M, val, sl, r, par, row, gather, acc, ab);
         join_halves(acc, ab);
         if (par == 0u) {
             if (fixed) {
                 if (q < A.n) epilogue(q, 0u, q, acc, ab);
-            } else if (q < A.contact.rows) {
+            } else if (q < ts.c_rows) {
                 epilogue(__ldg(A.contact.perm + q), 1u, q, acc, ab);
             }
         }
@@ -490,8 +509,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
     // then one warp per overflow row of the contact part
 
     __shared__ unsigned s_next;
+    const TaskSpace ts(A);
     BlockTasks bt{&s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
-                  g.task_start[gridDim.x], g.n_tasks, g.dyn_ctr, g.n_ctr};
+                  g.task_start[gridDim.x], ts.total, g.dyn_ctr, g.n_ctr};
     // A x0 (slice part to Ap, overflow part to Ap_ovf) ...
     bt.start();
     {
@@ -499,7 +519,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
         float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
         const float *const vals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
         for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-            product_task<kAllSlots>(g, vals, task, lane, gx,
+            product_task<kAllSlots>(g, ts, vals, task, lane, gx,
                          [&](unsigned, unsigned part, unsigned slot, const Vec3 &acc, const Vec3 &) {
                              st4(dst[part], slot, acc);
                          });
@@ -539,7 +559,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
             const float *const vals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
             for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-                product_task<kAllSlots>(g, vals, task, lane, gp,
+                product_task<kAllSlots>(g, ts, vals, task, lane, gp,
                              [&](unsigned row, unsigned part, unsigned slot, const Vec3 &acc,
                                  const Vec3 &ab) {
                                  const Vec3 pi = gp(row);
@@ -617,12 +637,13 @@ aborted:
 __device__ bool factor_y(const PcgArgs &g, BlockTasks &bt, unsigned lane, float *part,
                          unsigned *abort) {
     const PcgOperator &A = g.A;
+    const TaskSpace ts(A);
     const bf16_t *const vals[3] = {A.factor.fixed, A.factor.contact, A.factor.ovf};
     bt.start();
     {
         const GatherPlain gr{g.r};
         for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-            product_task<kBelow>(g, vals, task, lane, gr,
+            product_task<kBelow>(g, ts, vals, task, lane, gr,
                                  [&](unsigned row, unsigned part, unsigned, Vec3 acc, const Vec3 &) {
                                      if (part == 0u)
                                          acc += load_mat3(A.factor.diag + 9 * (size_t)row) *
@@ -640,13 +661,14 @@ __device__ bool factor_y(const PcgArgs &g, BlockTasks &bt, unsigned lane, float 
 __device__ bool factor_z(const PcgArgs &g, BlockTasks &bt, unsigned lane, float *part,
                          unsigned *abort, float &rz) {
     const PcgOperator &A = g.A;
+    const TaskSpace ts(A);
     const bf16_t *const vals[3] = {A.factor.fixed, A.factor.contact, A.factor.ovf};
     bt.start();
     float a = 0.0f;
     {
         const GatherY gy{g.Y};
         for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-            product_task<kAbove>(g, vals, task, lane, gy,
+            product_task<kAbove>(g, ts, vals, task, lane, gy,
                                  [&](unsigned row, unsigned part, unsigned, Vec3 acc, const Vec3 &) {
                                      const Vec3 ri = ldcg3(g.r, row);
                                      if (part == 0u) {
@@ -683,11 +705,12 @@ struct GatherAp {
 // barrier), so y needs no barrier of its own. No barrier here.
 __device__ void factor_y_update(const PcgArgs &g, BlockTasks &bt, unsigned lane, float alpha) {
     const PcgOperator &A = g.A;
+    const TaskSpace ts(A);
     const bf16_t *const vals[3] = {A.factor.fixed, A.factor.contact, A.factor.ovf};
     bt.start();
     const GatherAp gap{&g};
     for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-        product_task<kBelow>(g, vals, task, lane, gap,
+        product_task<kBelow>(g, ts, vals, task, lane, gap,
                              [&](unsigned row, unsigned part, unsigned, Vec3 acc, const Vec3 &) {
                                  if (part == 0u)
                                      acc += load_mat3(A.factor.diag + 9 * (size_t)row) *
@@ -720,8 +743,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
     float a, b;
 
     __shared__ unsigned s_next;
+    const TaskSpace ts(A);
     BlockTasks bt{&s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
-                  g.task_start[gridDim.x], g.n_tasks, g.dyn_ctr, g.n_ctr};
+                  g.task_start[gridDim.x], ts.total, g.dyn_ctr, g.n_ctr};
     const float *const avals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
     // A x0
     bt.start();
@@ -729,7 +753,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
         const GatherPlain gx{g.x};
         float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
         for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-            product_task<kAllSlots>(g, avals, task, lane, gx,
+            product_task<kAllSlots>(g, ts, avals, task, lane, gx,
                                     [&](unsigned, unsigned part, unsigned slot, const Vec3 &acc,
                                         const Vec3 &) { st4(dst[part], slot, acc); });
     }
@@ -768,7 +792,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
             bt.start();
             float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
             for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-                product_task<kAllSlots>(g, avals, task, lane, gp,
+                product_task<kAllSlots>(g, ts, avals, task, lane, gp,
                                         [&](unsigned row, unsigned part, unsigned slot,
                                             const Vec3 &acc, const Vec3 &ab) {
                                             const Vec3 pi = gp(row);
@@ -1005,15 +1029,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
     float *seg = reinterpret_cast<float *>(s_dyn4) + (size_t)wib * kSchwarzWarpFloats;
 
     __shared__ unsigned s_next;
+    const TaskSpace ts(A);
     BlockTasks bt{&s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
-                  g.task_start[gridDim.x], g.n_tasks, g.dyn_ctr, g.n_ctr};
+                  g.task_start[gridDim.x], ts.total, g.dyn_ctr, g.n_ctr};
     const float *const avals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
     bt.start();
     {
         const GatherPlain gx{g.x};
         float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
         for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-            product_task<kAllSlots>(g, avals, task, lane, gx,
+            product_task<kAllSlots>(g, ts, avals, task, lane, gx,
                                     [&](unsigned, unsigned part, unsigned slot, const Vec3 &acc,
                                         const Vec3 &) { st4(dst[part], slot, acc); });
     }
@@ -1054,7 +1079,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
             bt.start();
             float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
             for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-                product_task<kAllSlots>(g, avals, task, lane, gp,
+                product_task<kAllSlots>(g, ts, avals, task, lane, gp,
                                         [&](unsigned row, unsigned part, unsigned slot,
                                             const Vec3 &acc, const Vec3 &ab) {
                                             const Vec3 pi = gp(row);
@@ -1206,6 +1231,29 @@ __global__ void k_contact_slice_k(unsigned max_slices, const unsigned *n_rows,
     slice_k[sl] = k;
 }
 
+// The contact layout's sizes from its scans. A layout sized for bounds that
+// the totals would overrun (which the bounds rule out), or one whose row sort
+// timed out, is left empty and flagged, so no later kernel writes past it.
+__global__ void k_dyn_sizes(unsigned n, unsigned max_slices, const unsigned *counters,
+                            const unsigned *slice_off, const unsigned *ovf_off,
+                            const unsigned *flag_off, unsigned slot_cap, unsigned entry_cap,
+                            unsigned *sizes, unsigned *status) {
+    unsigned rows = counters[0], n_ovf = flag_off[n];
+    const unsigned slots = slice_off[max_slices], entries = ovf_off[n];
+    unsigned bad = 0u;
+    if (counters[1]) bad |= STATUS_SORT_LOOKBACK_TIMEOUT;
+    if (slots > slot_cap || entries > entry_cap) bad |= STATUS_BLOCK_OVERFLOW;
+    if (bad) {
+        rows = 0u;
+        n_ovf = 0u;
+        if (status) atomicOr(status, bad);
+    }
+    sizes[0] = rows;
+    sizes[1] = n_ovf;
+    sizes[2] = slots;
+    sizes[3] = entries;
+}
+
 __device__ __forceinline__ void put_slot(unsigned *out_col, float *out_val, unsigned s,
                                          unsigned lane, unsigned j, const float (&m)[9]) {
     out_col[(size_t)s * kSliceRows + lane] = j;
@@ -1291,23 +1339,25 @@ __global__ void k_contact_fill(unsigned max_slices, const unsigned *off, const u
 
 // Estimated cost of each product task, in warp slot-steps: a half slice
 // walks half its slots per lane; an overflow row walks its entries 32 at a
-// time. The constant covers the per-task epilogue. Task order: fixed half
-// slices, contact half slices, overflow rows.
-__global__ void k_task_cost(unsigned n_slices, const unsigned *fixed_off, unsigned c_slices,
-                            const unsigned *contact_off, unsigned n_ovf,
-                            const uint2 *ovf_range, unsigned *cost) {
+// time. The constant covers the per-task epilogue. Task order: overflow
+// rows, contact half slices, fixed half slices (TaskSpace); entries past the
+// solve's task count, up to the launch's bound, cost nothing.
+__global__ void k_task_cost(PcgOperator A, unsigned bound, unsigned *cost) {
     unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned t1 = n_ovf, t2 = t1 + 2 * c_slices;
-    if (t >= t2 + 2 * n_slices) return;
+    if (t >= bound) return;
+    const TaskSpace ts(A);
     unsigned c;
-    if (t < t1) {
-        c = (ovf_range[t].y + 31) / 32;
-    } else if (t < t2) {
-        unsigned sl = (t - t1) >> 1;
-        c = (contact_off[sl + 1] - contact_off[sl] + 1) / 2;
+    if (t >= ts.total) {
+        cost[t] = 0u;
+        return;
+    } else if (t < ts.t1) {
+        c = (A.ovf.range[t].y + 31) / 32;
+    } else if (t < ts.t2) {
+        unsigned sl = (t - ts.t1) >> 1;
+        c = (A.contact.sell.slice_off[sl + 1] - A.contact.sell.slice_off[sl] + 1) / 2;
     } else {
-        unsigned sl = (t - t2) >> 1;
-        c = (fixed_off[sl + 1] - fixed_off[sl] + 1) / 2;
+        unsigned sl = (t - ts.t2) >> 1;
+        c = (A.fixed.slice_off[sl + 1] - A.fixed.slice_off[sl] + 1) / 2;
     }
     cost[t] = c + 2u;
 }
@@ -1315,10 +1365,11 @@ __global__ void k_task_cost(unsigned n_slices, const unsigned *fixed_off, unsign
 // Block b takes the tasks whose cost prefix falls in [b Ws / nb,
 // (b+1) Ws / nb), Ws the static share of the total cost W; start[nb] is the
 // first task of the common pool.
-__global__ void k_task_split(unsigned T, const unsigned *cost_off, unsigned nb,
+__global__ void k_task_split(PcgOperator A, const unsigned *cost_off, unsigned nb,
                              unsigned *start) {
     unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b > nb) return;
+    const unsigned T = TaskSpace(A).total;
     const unsigned long long W = (unsigned long long)cost_off[T] * kStaticSixteenths / 16u;
     const unsigned long long target = W * b / nb;
     unsigned lo = 0, hi = T; // first t with cost_off[t] >= target
@@ -1416,7 +1467,7 @@ void sell_pack_fixed(SellLayout &L, const float *upper_val, cudaStream_t q) {
 
 void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const float *val,
                     const unsigned *tr_off, const uint2 *tr, const unsigned *dof_mask,
-                    DynLayout &D, cudaStream_t q) {
+                    DynLayout &D, cudaStream_t q, unsigned block_cap, unsigned *d_status) {
     const unsigned max_slices = (n + kSliceRows - 1) / kSliceRows;
     SellLayout &out = D.sell;
     out.slice_off.reserve(max_slices + 1);
@@ -1430,7 +1481,27 @@ void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const 
     D.flag_off.reserve(n + 1);
     D.ovf_index.reserve(n + 1);
     D.counters.reserve(4);
+    D.sizes.reserve(4);
     D.scan_tmp.reserve(scan_tmp_size(n + 1));
+    // Bounds for a layout sized before its totals are known: each contact
+    // block sits in two rows, so the rows hold at most 2 block_cap entries;
+    // with rows in order of decreasing count every slice after the first is
+    // at most as wide as the mean of the 32 rows before it, so the slots are
+    // at most one capped slice plus 2 block_cap / 32.
+    const unsigned long long entry_cap = 2ull * block_cap;
+    const unsigned long long slot_cap = kDynSliceCap + (entry_cap + kSliceRows - 1) / kSliceRows;
+    if (block_cap) {
+        if (slot_cap * kSliceRows * 9 >= 0xFFFFFFFFull || entry_cap * 9 >= 0xFFFFFFFFull)
+            throw FatalError(4, "contact layout bound exceeds 32-bit indexing");
+        out.col.reserve(slot_cap * kSliceRows + 1);
+        out.val.reserve(slot_cap * kSliceRows * 9 + 1);
+        out.src.reserve(slot_cap * kSliceRows + 1);
+        D.ovf_src.reserve(entry_cap + 1);
+        D.ovf_col.reserve(entry_cap + 1);
+        D.ovf_val.reserve(9 * entry_cap + 1);
+        D.ovf_row.reserve(n + 1);
+        D.ovf_range.reserve(n + 1);
+    }
     PPF_CUDA(cudaMemsetAsync(D.counters.data(), 0, 4 * sizeof(unsigned), q));
     k_contact_rows<<<div_up(n, 256u), 256, 0, q>>>(n, off, col, tr_off, tr, dof_mask,
                                                    D.key.data(), D.perm.data(),
@@ -1446,34 +1517,48 @@ void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const 
     exclusive_scan(D.slice_k.data(), out.slice_off.data(), max_slices, D.scan_tmp.data(), q);
     exclusive_scan(D.row_ovf.data(), D.ovf_off.data(), n, D.scan_tmp.data(), q);
     exclusive_scan(D.row_flag.data(), D.flag_off.data(), n, D.scan_tmp.data(), q);
-    unsigned totals[5] = {0, 0, 0, 0, 0};
-    PPF_CUDA(cudaMemcpyAsync(&totals[0], D.counters.data(), 2 * sizeof(unsigned),
-                             cudaMemcpyDeviceToHost, q));
-    PPF_CUDA(cudaMemcpyAsync(&totals[2], out.slice_off.data() + max_slices, sizeof(unsigned),
-                             cudaMemcpyDeviceToHost, q));
-    PPF_CUDA(cudaMemcpyAsync(&totals[3], D.ovf_off.data() + n, sizeof(unsigned),
-                             cudaMemcpyDeviceToHost, q));
-    PPF_CUDA(cudaMemcpyAsync(&totals[4], D.flag_off.data() + n, sizeof(unsigned),
-                             cudaMemcpyDeviceToHost, q));
-    PPF_CUDA(cudaStreamSynchronize(q));
-    g_d2h_bytes += sizeof(totals);
-    if (totals[1]) throw FatalError(4, "contact-row sort look-back timed out");
-    D.rows = totals[0];
-    out.n_slices = (D.rows + kSliceRows - 1) / kSliceRows;
-    out.slots = totals[2];
-    D.ovf_entries = totals[3];
-    D.n_ovf = totals[4];
-    out.col.reserve((size_t)out.slots * kSliceRows + 1);
-    out.val.reserve((size_t)out.slots * kSliceRows * 9 + 1);
-    out.src.reserve((size_t)out.slots * kSliceRows + 1);
-    D.ovf_src.reserve(D.ovf_entries + 1);
-    D.ovf_col.reserve(D.ovf_entries + 1);
-    D.ovf_val.reserve(9 * (size_t)D.ovf_entries + 1);
-    D.ovf_row.reserve(D.n_ovf + 1);
-    D.ovf_range.reserve(D.n_ovf + 1);
-    if (!D.rows) return;
+    k_dyn_sizes<<<1, 1, 0, q>>>(n, max_slices, D.counters.data(), out.slice_off.data(),
+                                D.ovf_off.data(), D.flag_off.data(),
+                                block_cap ? (unsigned)slot_cap : 0xFFFFFFFFu,
+                                block_cap ? (unsigned)entry_cap : 0xFFFFFFFFu, D.sizes.data(),
+                                d_status);
+    PPF_LAUNCH_CHECK();
+    if (block_cap) {
+        D.rows = n;
+        out.n_slices = max_slices;
+        out.slots = (unsigned)slot_cap;
+        D.ovf_entries = (unsigned)entry_cap;
+        D.n_ovf = n;
+    } else {
+        unsigned totals[5] = {0, 0, 0, 0, 0};
+        PPF_CUDA(cudaMemcpyAsync(&totals[0], D.counters.data(), 2 * sizeof(unsigned),
+                                 cudaMemcpyDeviceToHost, q));
+        PPF_CUDA(cudaMemcpyAsync(&totals[2], out.slice_off.data() + max_slices,
+                                 sizeof(unsigned), cudaMemcpyDeviceToHost, q));
+        PPF_CUDA(cudaMemcpyAsync(&totals[3], D.ovf_off.data() + n, sizeof(unsigned),
+                                 cudaMemcpyDeviceToHost, q));
+        PPF_CUDA(cudaMemcpyAsync(&totals[4], D.flag_off.data() + n, sizeof(unsigned),
+                                 cudaMemcpyDeviceToHost, q));
+        PPF_CUDA(cudaStreamSynchronize(q));
+        g_d2h_bytes += sizeof(totals);
+        if (totals[1]) throw FatalError(4, "contact-row sort look-back timed out");
+        D.rows = totals[0];
+        out.n_slices = (D.rows + kSliceRows - 1) / kSliceRows;
+        out.slots = totals[2];
+        D.ovf_entries = totals[3];
+        D.n_ovf = totals[4];
+        out.col.reserve((size_t)out.slots * kSliceRows + 1);
+        out.val.reserve((size_t)out.slots * kSliceRows * 9 + 1);
+        out.src.reserve((size_t)out.slots * kSliceRows + 1);
+        D.ovf_src.reserve(D.ovf_entries + 1);
+        D.ovf_col.reserve(D.ovf_entries + 1);
+        D.ovf_val.reserve(9 * (size_t)D.ovf_entries + 1);
+        D.ovf_row.reserve(D.n_ovf + 1);
+        D.ovf_range.reserve(D.n_ovf + 1);
+        if (!D.rows) return;
+    }
     DynFillOut o{out.slice_off.data(), D.ovf_off.data(), D.flag_off.data(), D.perm.data(),
-                 D.counters.data(),    out.col.data(),   out.val.data(),    D.index.data(),
+                 D.sizes.data(),       out.col.data(),   out.val.data(),    D.index.data(),
                  D.ovf_row.data(),     D.ovf_col.data(), D.ovf_index.data(), D.ovf_range.data(),
                  D.ovf_val.data(),     out.src.data(),   D.ovf_src.data()};
     k_contact_fill<<<div_up(out.n_slices * kSliceRows, 256u), 256, 0, q>>>(
@@ -1495,18 +1580,17 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     PPF_CUDA(cudaMemsetAsync(ws.barrier.data(), 0, 4 * sizeof(unsigned), q));
     ws.Ap_ovf.reserve(A.ovf.count + 1);
     ws.Ap_c.reserve(A.contact.rows + 1);
-    // balanced task ranges per block
+    // balanced task ranges per block; the contact counts are an upper bound
+    // here, the task kernels read the solve's own from the layout
     const unsigned T = 2 * A.fixed.n_slices + 2 * A.contact.sell.n_slices + A.ovf.count;
     ws.task_cost.reserve(T + 1);
     ws.task_off.reserve(T + 1);
     ws.task_start.reserve(ws.grid + 1);
     ws.scan_tmp.reserve(scan_tmp_size(T + 1));
-    k_task_cost<<<div_up(T, 256u), 256, 0, q>>>(A.fixed.n_slices, A.fixed.slice_off,
-                                                A.contact.sell.n_slices, A.contact.sell.slice_off,
-                                                A.ovf.count, A.ovf.range, ws.task_cost.data());
+    k_task_cost<<<div_up(T, 256u), 256, 0, q>>>(A, T, ws.task_cost.data());
     PPF_LAUNCH_CHECK();
     exclusive_scan(ws.task_cost.data(), ws.task_off.data(), T, ws.scan_tmp.data(), q);
-    k_task_split<<<div_up(ws.grid + 1, 256u), 256, 0, q>>>(T, ws.task_off.data(), ws.grid,
+    k_task_split<<<div_up(ws.grid + 1, 256u), 256, 0, q>>>(A, ws.task_off.data(), ws.grid,
                                                           ws.task_start.data());
     PPF_LAUNCH_CHECK();
     // one counter per product phase: the initial product, then one (block-
@@ -1516,7 +1600,6 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     PPF_CUDA(cudaMemsetAsync(ws.dyn_ctr.data(), 0, n_ctr * sizeof(unsigned), q));
     PcgArgs g{A,
               ws.task_start.data(),
-              T,
               ws.dyn_ctr.data(),
               n_ctr,
               x,

@@ -59,10 +59,13 @@ struct OverflowRows {
 // decreasing block count, cut into SELL-32 slices over that order (lane l of
 // slice s is row perm[32 s + l]), so rows of like length share a slice.
 struct ContactRows {
-    unsigned rows;          // rows with contact blocks
+    unsigned rows;          // rows with contact blocks (an upper bound when sizes is set)
     SellMatrix sell;        // n_slices = ceil(rows / 32)
     const unsigned *perm;   // sorted position -> row
     const unsigned *index;  // n: row -> sorted position, or 0xffffffff
+    // null, or the device's {rows, overflow rows}: the PCG's task kernels
+    // read these, so the host fields above need only bound them
+    const unsigned *sizes;
 };
 
 typedef __nv_bfloat16 bf16_t;
@@ -166,6 +169,7 @@ struct DynLayout {
     SellLayout sell; // over the sorted contact rows
     DevBuf<unsigned> key, perm, index, slice_k, row_ovf, row_flag, ovf_off, flag_off;
     DevBuf<unsigned> scan_tmp, counters;
+    DevBuf<unsigned> sizes; // {rows, overflow rows, slots, overflow entries}
     DevBuf<unsigned> ovf_row, ovf_col, ovf_index, ovf_src;
     DevBuf<uint2> ovf_range;
     DevBuf<float> ovf_val;
@@ -185,17 +189,23 @@ void sell_pack_fixed(SellLayout &L, const float *upper_val, cudaStream_t q);
 // Contact part, rebuilt per Newton iteration from the deduplicated upper CSR
 // (off, col, val) and its transpose list (tr_off, tr), leaving out the blocks
 // of Dirichlet vertices (dof_mask, zero after elimination). Rows are sorted
-// by block count with the stable radix sort; four totals are read back to
-// the host (one synchronization) to size the layout.
+// by block count with the stable radix sort. The device writes the layout's
+// sizes to out.sizes. With block_cap == 0 four totals are read back to the
+// host (one synchronization) and the layout is sized to them; otherwise it
+// is sized for at most block_cap contact blocks (upper triangle) with no
+// read-back, and its host counts are those bounds. A sort time-out or an
+// overrun bound empties the layout and sets a bit of *d_status.
 void sell_build_dyn(unsigned n, const unsigned *off, const unsigned *col, const float *val,
                     const unsigned *tr_off, const uint2 *tr, const unsigned *dof_mask,
-                    DynLayout &out, cudaStream_t q);
+                    DynLayout &out, cudaStream_t q, unsigned block_cap = 0,
+                    unsigned *d_status = nullptr);
 inline SellMatrix sell_view(const SellLayout &L) {
     return SellMatrix{L.n_slices, L.slice_off.data(), L.col.data(), L.val.data(),
                       L.slice_mid.data()};
 }
 inline ContactRows contact_view(const DynLayout &D) {
-    return ContactRows{D.rows, sell_view(D.sell), D.perm.data(), D.index.data()};
+    return ContactRows{D.rows, sell_view(D.sell), D.perm.data(), D.index.data(),
+                       D.sizes.data()};
 }
 inline OverflowRows overflow_view(const DynLayout &D) {
     return OverflowRows{D.n_ovf, D.ovf_row.data(), D.ovf_range.data(), D.ovf_col.data(),

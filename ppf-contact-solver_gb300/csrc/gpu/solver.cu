@@ -84,9 +84,12 @@ __global__ void k_max_dx(unsigned n, const float *dx, IterStatus *st) {
 }
 
 // target <- eval_x; eval_x -= min(1, max_dx / |dx|_max) dx (main.cu:1142-1188)
+// An iteration flagged for a repeat (a pair list or the contact-block
+// capacity overran) leaves both untouched.
 __global__ void k_apply_dx(unsigned n, float *x, float *target, const float *dx,
                            IterStatus *st, float max_dx_param) {
     unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (st->status & STATUS_PAIR_OVERFLOW) return;
     float mdx = __uint_as_float(st->max_dx_bits);
     float rescale = fminf(1.0f, max_dx_param / mdx);
     if (i == 0) st->rescale = rescale;
@@ -336,6 +339,7 @@ AssemblyBuffers Solver::abuf() {
     b.x0 = curr_.data();
     b.target = target_.data();
     b.st = st_.data();
+    b.params = sp_dev_.data();
     return b;
 }
 
@@ -642,6 +646,7 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     fixed_val_.reserve(9 * (size_t)nnz_fixed_);
     fixed_tmp_.reserve(9 * (size_t)nnz_fixed_);
     st_.reserve(1);
+    sp_dev_.reserve(1);
     isect_.reserve(PPF_MAX_INTERSECTION_RECORDS);
     if (!st_host_) PPF_CUDA(cudaMallocHost(&st_host_, sizeof(IterStatus)));
     // pair lists and contact-block buffers start at a size proportional to the
@@ -820,10 +825,47 @@ void Solver::read_status() {
     g_d2h_bytes += sizeof(IterStatus);
 }
 
+__global__ void k_set_step_params(StepParams p, StepParams *dst) { *dst = p; }
+
+// The step's parameters to their device copy, by a kernel argument: the
+// assembly kernels read them there, so a captured iteration serves every
+// step (their time step and clock change per step).
+void Solver::upload_step_params(float dt) {
+    sp_dev_.reserve(1);
+    k_set_step_params<<<1, 1, 0, q_>>>(step_params(dt), sp_dev_.data());
+    PPF_LAUNCH_CHECK();
+}
+
+void Solver::grow_pairs(const unsigned counts[4]) {
+    auto grow_to = [](unsigned c) { return std::max(1u << 14, (unsigned)(2ull * c)); };
+    if (counts[0] > pairs_.cap_pf) pf_buf_.reserve(grow_to(counts[0]));
+    if (counts[1] > pairs_.cap_pe) pe_buf_.reserve(grow_to(counts[1]));
+    if (counts[2] > pairs_.cap_pp) pp_buf_.reserve(grow_to(counts[2]));
+    if (counts[3] > pairs_.cap_ee) ee_buf_.reserve(grow_to(counts[3]));
+    pairs_.pf = pf_buf_.data();
+    pairs_.pe = pe_buf_.data();
+    pairs_.pp = pp_buf_.data();
+    pairs_.ee = ee_buf_.data();
+    pairs_.cap_pf = (unsigned)pf_buf_.cap;
+    pairs_.cap_pe = (unsigned)pe_buf_.cap;
+    pairs_.cap_pp = (unsigned)pp_buf_.cap;
+    pairs_.cap_ee = (unsigned)ee_buf_.cap;
+}
+
 // Assembly of the Newton system at eval_x (main.cu:713-1049).
 void Solver::assemble(float dt) {
+    upload_step_params(dt);
+    assemble_stage(false);
+}
+
+// The assembly launches. With `capacity` false the pair counts and the
+// contact layout's totals are read back to size the launches and buffers
+// (two synchronizations); with it true everything is sized by capacities
+// (the pair lists' and dyn_cap_ contact blocks), no value is read back, and
+// an iteration whose counts overran them is flagged (STATUS_PAIR_OVERFLOW)
+// for the host to grow them and repeat it.
+void Solver::assemble_stage(bool capacity) {
     const Scene s = scene();
-    const StepParams p = step_params(dt);
     const size_t n3 = 3 * (size_t)n_;
     PPF_CUDA(cudaMemsetAsync(force_.data(), 0, n3 * sizeof(float), q_));
     PPF_CUDA(cudaMemsetAsync(diag_.data(), 0, 9 * (size_t)n_ * sizeof(float), q_));
@@ -833,54 +875,64 @@ void Solver::assemble(float dt) {
                                             dx_.data());
     PPF_LAUNCH_CHECK();
     AssemblyBuffers b = abuf();
-    launch_vertex_energy(s, p, b, q_);
-    launch_elastic(s, p, b, q_);
+    launch_vertex_energy(s, b, q_);
+    launch_elastic(s, b, q_);
     PPF_CUDA(cudaMemcpyAsync(fixed_tmp_.data(), fixed_val_.data(),
                              9 * (size_t)nnz_fixed_ * sizeof(float), cudaMemcpyDeviceToDevice, q_));
-    launch_strain_limit(s, p, b, q_);
-    unsigned counts[4] = {0, 0, 0, 0};
+    launch_strain_limit(s, b, q_);
+    unsigned bound[4] = {0, 0, 0, 0};
     if (!param->disable_contact) {
         // tight boxes at the evaluated positions for the proximity queries
         build_trees(eval_x_.data(), eval_x_.data(), 1.0f, false);
-        for (int attempt = 0; attempt < 3; ++attempt) {
+        if (capacity) {
             PPF_CUDA(cudaMemsetAsync(st_.data(), 0, 4 * sizeof(unsigned), q_));
             PieceBuffers pb = pieces();
             launch_edge_pieces(s, view(bvh_edge_), eval_x_.data(), nullptr, nullptr, piece_len_,
                                pb, q_);
             launch_detect(s, view(bvh_face_), view(bvh_edge_), view(bvh_vert_), b, pairs_, pb, q_);
-            read_status();
-            counts[0] = st_host_->n_pf;
-            counts[1] = st_host_->n_pe;
-            counts[2] = st_host_->n_pp;
-            counts[3] = st_host_->n_ee;
-            bool grow = counts[0] > pairs_.cap_pf || counts[1] > pairs_.cap_pe ||
-                        counts[2] > pairs_.cap_pp || counts[3] > pairs_.cap_ee;
-            if (!grow) break;
-            auto grow_to = [](unsigned c) { return std::max(1u << 14, (unsigned)(2ull * c)); };
-            pf_buf_.reserve(grow_to(counts[0]));
-            pe_buf_.reserve(grow_to(counts[1]));
-            pp_buf_.reserve(grow_to(counts[2]));
-            ee_buf_.reserve(grow_to(counts[3]));
-            pairs_.pf = pf_buf_.data();
-            pairs_.pe = pe_buf_.data();
-            pairs_.pp = pp_buf_.data();
-            pairs_.ee = ee_buf_.data();
-            pairs_.cap_pf = (unsigned)pf_buf_.cap;
-            pairs_.cap_pe = (unsigned)pe_buf_.cap;
-            pairs_.cap_pp = (unsigned)pp_buf_.cap;
-            pairs_.cap_ee = (unsigned)ee_buf_.cap;
-            PPF_CUDA(cudaMemsetAsync(&st_.data()->n_contact, 0, sizeof(unsigned), q_));
+            launch_pair_capacity(pairs_, st_.data(), q_);
+            bound[0] = pairs_.cap_pf;
+            bound[1] = pairs_.cap_pe;
+            bound[2] = pairs_.cap_pp;
+            bound[3] = pairs_.cap_ee;
+        } else {
+            for (int attempt = 0; attempt < 3; ++attempt) {
+                PPF_CUDA(cudaMemsetAsync(st_.data(), 0, 4 * sizeof(unsigned), q_));
+                PieceBuffers pb = pieces();
+                launch_edge_pieces(s, view(bvh_edge_), eval_x_.data(), nullptr, nullptr,
+                                   piece_len_, pb, q_);
+                launch_detect(s, view(bvh_face_), view(bvh_edge_), view(bvh_vert_), b, pairs_, pb,
+                              q_);
+                read_status();
+                bound[0] = st_host_->n_pf;
+                bound[1] = st_host_->n_pe;
+                bound[2] = st_host_->n_pp;
+                bound[3] = st_host_->n_ee;
+                bool grow = bound[0] > pairs_.cap_pf || bound[1] > pairs_.cap_pe ||
+                            bound[2] > pairs_.cap_pp || bound[3] > pairs_.cap_ee;
+                if (!grow) break;
+                grow_pairs(bound);
+                PPF_CUDA(cudaMemsetAsync(&st_.data()->n_contact, 0, sizeof(unsigned), q_));
+            }
+            if (bound[0] > pairs_.cap_pf || bound[1] > pairs_.cap_pe ||
+                bound[2] > pairs_.cap_pp || bound[3] > pairs_.cap_ee)
+                throw FatalError(4, "contact pair lists still overflow after growing them");
         }
-        if (counts[0] > pairs_.cap_pf || counts[1] > pairs_.cap_pe ||
-            counts[2] > pairs_.cap_pp || counts[3] > pairs_.cap_ee)
-            throw FatalError(4, "contact pair lists still overflow after growing them");
     }
-    // contact blocks outside the fixed pattern
-    unsigned long long keys = 6ull * counts[0] + 3ull * counts[1] + counts[2] + 6ull * counts[3];
-    unsigned hcap = next_pow2(2 * keys + 16);
+    // contact blocks outside the fixed pattern: at most 6, 3, 1, 6 per pair
+    // (upper triangle); the hash table is kept at most half full
+    unsigned hcap, dcap;
+    if (capacity) {
+        dcap = dyn_cap_;
+        hcap = next_pow2(4ull * dcap);
+    } else {
+        unsigned long long keys =
+            6ull * bound[0] + 3ull * bound[1] + bound[2] + 6ull * bound[3];
+        hcap = next_pow2(2 * keys + 16);
+        dcap = (unsigned)std::max<unsigned long long>(keys, 16ull);
+    }
     hkey_buf_.reserve(hcap);
     hval_buf_.reserve(hcap);
-    unsigned dcap = (unsigned)std::max<unsigned long long>(keys, 16ull);
     dcol_buf_.reserve(dcap);
     dtr_buf_.reserve(dcap);
     dval_buf_.reserve(9 * (size_t)dcap);
@@ -896,12 +948,11 @@ void Solver::assemble(float dt) {
     dyn_.cnt2 = dcnt2_buf_.data();
     dyn_.cap = dcap;
     PPF_CUDA(cudaMemsetAsync(&st_.data()->n_dyn, 0, sizeof(unsigned), q_));
-    launch_dyn_build(s, b, pairs_, counts, dyn_, dcap, scan_tmp_.data(), q_);
+    launch_dyn_build(s, b, pairs_, bound, dyn_, scan_tmp_.data(), q_);
     carried_ = false;
-    PPF_CUDA(cudaMemsetAsync(dval_buf_.data(), 0, 9 * (size_t)dcap * sizeof(float), q_));
-    launch_contact_assemble(s, p, b, pairs_, counts, dyn_, q_);
-    launch_vertex_constraints(s, p, b, q_);
-    if (!param->disable_contact) launch_collision_mesh(s, p, b, view(bvh_face_), q_);
+    launch_contact_assemble(s, b, pairs_, bound, dyn_, q_);
+    launch_vertex_constraints(s, b, q_);
+    if (!param->disable_contact) launch_collision_mesh(s, b, view(bvh_face_), q_);
     launch_dirichlet(s, b, dyn_, dx_.data(), q_);
     k_fold_diag<<<div_up(n_, kB), kB, 0, q_>>>(n_, fixed_diag_.data(), diag_.data(),
                                               fixed_val_.data());
@@ -909,26 +960,174 @@ void Solver::assemble(float dt) {
     // the operator in the PCG's slice layout, and its block-Jacobi inverse
     sell_pack_fixed(fixed_sell_, fixed_val_.data(), q_);
     sell_build_dyn(n_, dyn_.off, dyn_.col, dyn_.val, dyn_.tr_off, dyn_.tr, dof_mask_.data(),
-                   dyn_layout_, q_);
+                   dyn_layout_, q_, capacity ? dcap : 0u, &st_.data()->status);
     launch_block_jacobi(n_, fixed_val_.data(), fixed_diag_.data(), inv_diag_.data(),
                         &st_.data()->status, q_);
     // the factored preconditioner once a block-Jacobi solve has set the
-    // iteration count it must stay within
-    factor_active_ = precond_kind_ != 0 && (plain_iters_ != 0 || force_factor_);
+    // iteration count it must stay within (never in a capacity-sized
+    // iteration: its build reads the layout's sizes on the host)
+    factor_active_ = !capacity && precond_kind_ != 0 && (plain_iters_ != 0 || force_factor_);
     if (factor_active_) build_factor();
     // the reference's aggregate Schwarz when the scene asks for it
     schwarz_active_ = precond_kind_ == 0 && param->precond == 1;
     if (schwarz_active_) {
         PcgOperator A{n_, sell_view(fixed_sell_), contact_view(dyn_layout_),
                       overflow_view(dyn_layout_), inv_diag_.data(), PcgFactor{}, SchwarzView{}};
-        // levels as the reference reads ParamSet::schwarz_levels (0: unset,
-        // 2), built up to kSchwarzMaxLevels (schwarz.cu:1650-1666)
-        unsigned levels = param->schwarz_levels ? param->schwarz_levels : 2u;
-        levels = std::min(levels, kSchwarzMaxLevels);
-        if (!schwarz_.ready || schwarz_.n != n_ || schwarz_.levels_req != levels)
-            schwarz_setup(A, schwarz_, levels, q_);
+        if (!schwarz_ready()) {
+            if (capacity) throw FatalError(4, "Schwarz layout not set up before a captured iteration");
+            schwarz_setup(A, schwarz_, schwarz_levels(), q_);
+        }
         launch_schwarz_factor(A, schwarz_, &st_.data()->status, q_);
     }
+}
+
+// Levels as the reference reads ParamSet::schwarz_levels (0: unset, 2), built
+// up to kSchwarzMaxLevels (schwarz.cu:1650-1666).
+unsigned Solver::schwarz_levels() const {
+    unsigned levels = param->schwarz_levels ? param->schwarz_levels : 2u;
+    return std::min(levels, kSchwarzMaxLevels);
+}
+
+bool Solver::schwarz_ready() const {
+    return schwarz_.ready && schwarz_.n == n_ && schwarz_.levels_req == schwarz_levels();
+}
+
+void Solver::record_event(cudaEvent_t ev, bool capturing) {
+    if (capturing) PPF_CUDA(cudaEventRecordWithFlags(ev, q_, cudaEventRecordExternal));
+    else PPF_CUDA(cudaEventRecord(ev, q_));
+}
+
+// The linear solve of the assembled system, bracketed by the PCG timing
+// events. A factored or Schwarz solve runs first; block-Jacobi solves again
+// from the same start if it stalled or reached the block-Jacobi count (a
+// factored one), or if r^T z <= 0 (a Schwarz one, solver/solver.cu:1627-1676),
+// decided on the device.
+void Solver::enqueue_solve(bool capturing) {
+    const size_t n3 = 3 * (size_t)n_;
+    PPF_CUDA(cudaMemcpyAsync(r_.data(), force_.data(), n3 * sizeof(float),
+                             cudaMemcpyDeviceToDevice, q_));
+    PcgOperator A = pcg_operator();
+    record_event(ev0_, capturing);
+    if (factor_active_ || schwarz_active_) {
+        dx0_.reserve(n3);
+        run_plain_.reserve(1);
+        PPF_CUDA(cudaMemcpyAsync(dx0_.data(), dx_.data(), n3 * sizeof(float),
+                                 cudaMemcpyDeviceToDevice, q_));
+        launch_pcg(A, dx_.data(), r_.data(), param->cg_tol,
+                   factor_active_ ? std::min(plain_iters_, param->cg_max_iter)
+                                  : param->cg_max_iter,
+                   pcg_, q_);
+        k_factor_verdict<<<div_up(n3, (size_t)kB), kB, 0, q_>>>(
+            (unsigned)n3, pcg_.result.data(), factor_active_ ? 1 : 0, force_.data(),
+            dx0_.data(), r_.data(), dx_.data(), run_plain_.data(), st_.data());
+        PPF_LAUNCH_CHECK();
+        A.schwarz = SchwarzView{};
+        PcgOperator J = A;
+        J.factor = PcgFactor{};
+        launch_pcg(J, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_,
+                   run_plain_.data());
+    } else {
+        launch_pcg(A, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_);
+    }
+    record_event(ev1_, capturing);
+}
+
+// Everything a captured iteration bakes in: the scene's arrays and counts,
+// the parameters (but the per-step clock), the pair lists, the contact-block
+// capacity, the fixed operator's and the Schwarz layout's sizes, and the
+// buffer epoch (every device pointer). A constraint update that rewrites the
+// device arrays in place leaves it as it is.
+Solver::IterKey Solver::iteration_key() const {
+    IterKey k;
+    memset(&k, 0, sizeof(k));
+    const Scene sc = scene();
+    memcpy(&k.scene, &sc, sizeof(Scene));
+    memcpy(&k.param, param, sizeof(PpfParamSet));
+    k.param.time = 0.0;
+    k.param.prev_dt = 0.0f;
+    memcpy(&k.pairs, &pairs_, sizeof(PairLists));
+    k.piece_len = piece_len_;
+    k.dyn_cap = dyn_cap_;
+    k.use_active = use_active_ ? 1u : 0u;
+    k.schwarz = schwarz_ready() ? 1u : 0u;
+    k.nnz_fixed = nnz_fixed_;
+    k.fixed_slices = fixed_sell_.n_slices;
+    k.fixed_slots = fixed_sell_.slots;
+    if (k.schwarz) {
+        k.agg[0] = schwarz_.n;
+        k.agg[1] = schwarz_.n_agg;
+        k.agg[2] = schwarz_.max_members;
+        k.agg[3] = schwarz_.levels;
+        k.agg[4] = schwarz_.n_dom;
+        k.agg[5] = schwarz_.max_dom_members;
+    }
+    k.epoch = g_buffer_epoch;
+    return k;
+}
+
+// A Newton iteration can be captured when its assembly needs no read-back:
+// block-Jacobi, or Schwarz once its layout is set up.
+bool Solver::iteration_graph_ok() const {
+    if (!graph_enabled_ || precond_kind_ != 0) return false;
+    return param->precond != 1 || schwarz_ready();
+}
+
+// The iteration's launches, sized by capacities, in stream order: status
+// reset, assembly, solve, line search, status copy to the host.
+void Solver::enqueue_iteration(bool capturing) {
+    PPF_CUDA(cudaMemsetAsync(st_.data(), 0, sizeof(IterStatus), q_));
+    assemble_stage(true);
+    enqueue_solve(capturing);
+    enqueue_line_search();
+}
+
+// One Newton iteration through its CUDA graph. The first iteration under a
+// new key runs its launches directly (sizing every buffer for the current
+// capacities), the next one captures them, and later ones replay the graph.
+void Solver::iteration_graph(float dt) {
+    upload_step_params(dt);
+    IterKey key = iteration_key();
+    if (it_graph_ && memcmp(&key, &it_key_, sizeof(IterKey)) == 0) {
+        PPF_CUDA(cudaGraphLaunch(it_graph_, q_));
+        g_kernel_launches += it_launches_;
+        ++graph_stats_.replays;
+        return;
+    }
+    if (it_graph_) {
+        PPF_CUDA(cudaGraphExecDestroy(it_graph_));
+        it_graph_ = nullptr;
+    }
+    if (!it_eager_valid_ || memcmp(&key, &it_eager_key_, sizeof(IterKey)) != 0) {
+        enqueue_iteration(false);
+        it_eager_key_ = iteration_key();
+        it_eager_valid_ = true;
+        ++graph_stats_.direct;
+        return;
+    }
+    cudaGraph_t graph = nullptr;
+    const unsigned long long l0 = g_kernel_launches;
+    PPF_CUDA(cudaStreamBeginCapture(q_, cudaStreamCaptureModeThreadLocal));
+    g_capturing = true;
+    try {
+        enqueue_iteration(true);
+    } catch (...) {
+        g_capturing = false;
+        cudaGraph_t aborted = nullptr;
+        cudaStreamEndCapture(q_, &aborted);
+        if (aborted) cudaGraphDestroy(aborted);
+        throw;
+    }
+    g_capturing = false;
+    PPF_CUDA(cudaStreamEndCapture(q_, &graph));
+    it_launches_ = (unsigned)(g_kernel_launches - l0);
+    g_kernel_launches = l0;
+    PPF_CUDA(cudaGraphInstantiate(&it_graph_, graph, 0ull));
+    PPF_CUDA(cudaGraphDestroy(graph));
+    it_key_ = key;
+    ++graph_stats_.captures;
+    PPF_CUDA(cudaGraphLaunch(it_graph_, q_));
+    g_kernel_launches += it_launches_;
+    ++graph_stats_.replays;
 }
 
 // The line-search stage of a Newton iteration (main.cu:1142-1354): the
@@ -1014,62 +1213,63 @@ PpfStepResult Solver::advance() {
     double toi_advanced = 0.0;
     unsigned step = 1;
     bool final_step = false;
-    const Scene s = scene();
+    bool repeat = false;   // the last iteration overran a capacity: run it again
+    unsigned repeats = 0;
     while (true) {
-        if (!final_step && param->max_newton_steps > 0 && step >= param->max_newton_steps) {
-            result.newton_progress = false;
-            return result;
-        }
-        if (final_step) {
-            if (toi_advanced < 1.0 && nfix_) {
-                k_rewind_fix<<<div_up(nfix_, kB), kB, 0, q_>>>(nfix_, fix_.data(),
-                                                               1.0f - (float)toi_advanced);
-                PPF_LAUNCH_CHECK();
+        if (!repeat) {
+            if (!final_step && param->max_newton_steps > 0 &&
+                step >= param->max_newton_steps) {
+                result.newton_progress = false;
+                return result;
             }
-            dt *= (float)toi_advanced;
-            compute_target(dt);
+            if (final_step) {
+                if (toi_advanced < 1.0 && nfix_) {
+                    k_rewind_fix<<<div_up(nfix_, kB), kB, 0, q_>>>(nfix_, fix_.data(),
+                                                                   1.0f - (float)toi_advanced);
+                    PPF_LAUNCH_CHECK();
+                }
+                dt *= (float)toi_advanced;
+                compute_target(dt);
+            }
         }
-        PPF_CUDA(cudaMemsetAsync(st_.data(), 0, sizeof(IterStatus), q_));
-        assemble(dt);
-        // linear solve
-        PPF_CUDA(cudaMemcpyAsync(r_.data(), force_.data(), n3 * sizeof(float),
-                                 cudaMemcpyDeviceToDevice, q_));
-        PcgOperator A = pcg_operator();
-        PPF_CUDA(cudaEventRecord(ev0_, q_));
-        if (factor_active_ || schwarz_active_) {
-            // factored solve within the block-Jacobi count, then block-Jacobi
-            // from the same start if it stalled or reached that count; a
-            // Schwarz solve goes back to block-Jacobi only when r^T z <= 0
-            // (solver/solver.cu:1627-1676)
-            dx0_.reserve(n3);
-            run_plain_.reserve(1);
-            PPF_CUDA(cudaMemcpyAsync(dx0_.data(), dx_.data(), n3 * sizeof(float),
-                                     cudaMemcpyDeviceToDevice, q_));
-            launch_pcg(A, dx_.data(), r_.data(), param->cg_tol,
-                       factor_active_ ? std::min(plain_iters_, param->cg_max_iter)
-                                      : param->cg_max_iter,
-                       pcg_, q_);
-            k_factor_verdict<<<div_up(n3, (size_t)kB), kB, 0, q_>>>(
-                (unsigned)n3, pcg_.result.data(), factor_active_ ? 1 : 0, force_.data(),
-                dx0_.data(), r_.data(), dx_.data(), run_plain_.data(), st_.data());
-            PPF_LAUNCH_CHECK();
-            A.schwarz = SchwarzView{};
-            PcgOperator J = A;
-            J.factor = PcgFactor{};
-            launch_pcg(J, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_,
-                       run_plain_.data());
+        repeat = false;
+        const bool graphed = iteration_graph_ok();
+        if (graphed) {
+            // assembly, solve and line search as one CUDA graph, sized by
+            // capacities, with no read-back before the status copy
+            iteration_graph(dt);
         } else {
-            launch_pcg(A, dx_.data(), r_.data(), param->cg_tol, param->cg_max_iter, pcg_, q_);
+            PPF_CUDA(cudaMemsetAsync(st_.data(), 0, sizeof(IterStatus), q_));
+            assemble(dt);
+            enqueue_solve(false);
+            // rescaled Newton step, swept boxes, line search, status to the
+            // host: a fixed sequence of launches over this scene's buffers,
+            // replayed as one CUDA graph
+            line_search_stage();
         }
-        PPF_CUDA(cudaEventRecord(ev1_, q_));
-        // rescaled Newton step, swept boxes, line search, status to the host:
-        // a fixed sequence of launches over this scene's buffers, replayed as
-        // one CUDA graph
-        line_search_stage();
         PPF_CUDA(cudaStreamSynchronize(q_));
         g_d2h_bytes += sizeof(IterStatus);
         const float rescale = st_host_->rescale;
         const IterStatus st = *st_host_;
+        if (st.status & STATUS_PAIR_OVERFLOW) {
+            // a capacity-sized iteration found more pairs or contact blocks
+            // than it could hold; it changed nothing, so grow and repeat it
+            if (!graphed || ++repeats > 8)
+                throw FatalError(4, "contact capacities still overflow after growing them");
+            const unsigned counts[4] = {st.n_pf, st.n_pe, st.n_pp, st.n_ee};
+            const bool lists = st.n_pf > pairs_.cap_pf || st.n_pe > pairs_.cap_pe ||
+                               st.n_pp > pairs_.cap_pp || st.n_ee > pairs_.cap_ee;
+            if (lists) {
+                // the blocks were not counted: grow the lists first
+                grow_pairs(counts);
+            } else {
+                dyn_cap_ = (unsigned)std::min<unsigned long long>(
+                    2ull * std::max(st.n_dyn, dyn_cap_), 0x3FFFFFFFull);
+            }
+            ++graph_stats_.repeats;
+            repeat = true;
+            continue;
+        }
         float pcg_ms = 0.0f;
         PPF_CUDA(cudaEventElapsedTime(&pcg_ms, ev0_, ev1_));
         stats_.newton_iters++;
@@ -1414,6 +1614,16 @@ float Solver::debug_strain_line_search(const float *x0, const float *x1) {
                              cudaMemcpyDeviceToHost, q_));
     PPF_CUDA(cudaStreamSynchronize(q_));
     return __builtin_bit_cast(float, out) / max_t;
+}
+
+void Solver::set_contact_capacity(unsigned pair_cap, unsigned block_cap) {
+    if (pair_cap) {
+        pairs_.cap_pf = std::min<unsigned>(pair_cap, (unsigned)pf_buf_.cap);
+        pairs_.cap_pe = std::min<unsigned>(pair_cap, (unsigned)pe_buf_.cap);
+        pairs_.cap_pp = std::min<unsigned>(pair_cap, (unsigned)pp_buf_.cap);
+        pairs_.cap_ee = std::min<unsigned>(pair_cap, (unsigned)ee_buf_.cap);
+    }
+    if (block_cap) dyn_cap_ = std::max(block_cap, 16u);
 }
 
 void Solver::set_tuning(const Tuning &t) {

@@ -95,6 +95,10 @@ class Solver {
     Tuning autotune();
     Tuning tuning() const { return tune_; }
     void set_tuning(const Tuning &t);
+    // Caps the pair lists at pair_cap entries each and a capacity-sized
+    // iteration at block_cap contact blocks (0 leaves one as it is); larger
+    // counts then take the overrun-and-repeat path.
+    void set_contact_capacity(unsigned pair_cap, unsigned block_cap);
     void release();
 
     PpfDataSet *host = nullptr;
@@ -109,7 +113,14 @@ class Solver {
     void build_trees(const float *x0, const float *x1, float extrap, bool rebuild);
     BvhView view(const Lbvh &b) const;
     void compute_target(float dt);
+    void upload_step_params(float dt);
+    void grow_pairs(const unsigned counts[4]);
     void assemble(float dt);
+    void assemble_stage(bool capacity);
+    unsigned schwarz_levels() const;
+    bool schwarz_ready() const;
+    void record_event(cudaEvent_t ev, bool capturing);
+    void enqueue_solve(bool capturing);
     bool check_intersection(const float *x);
     void enqueue_line_search();
     void line_search_stage();
@@ -216,7 +227,38 @@ class Solver {
     unsigned ls_launches_ = 0;
   public:
     unsigned long long ls_replays_ = 0; // graph launches of the line-search stage
+    // Newton iterations run through the iteration graph: directly (the first
+    // under a new key), captured, replayed, and repeated after a capacity
+    // overran
+    struct GraphStats {
+        unsigned long long direct = 0, captures = 0, replays = 0, repeats = 0;
+    } graph_stats_;
+    // the whole Newton iteration as one CUDA graph (on by default; off runs
+    // the sized-by-read-back assembly and the line-search graph alone)
+    bool graph_enabled_ = true;
   private:
+    struct IterKey {
+        Scene scene;
+        PpfParamSet param;
+        PairLists pairs;
+        float piece_len;
+        unsigned dyn_cap, use_active, schwarz;
+        unsigned nnz_fixed, fixed_slices, fixed_slots;
+        unsigned agg[6]; // Schwarz: n, n_agg, max_members, levels, n_dom, max_dom_members
+        unsigned long long epoch;
+    };
+    IterKey iteration_key() const;
+    bool iteration_graph_ok() const;
+    void enqueue_iteration(bool capturing);
+    void iteration_graph(float dt);
+    cudaGraphExec_t it_graph_ = nullptr;
+    IterKey it_key_{}, it_eager_key_{};
+    bool it_eager_valid_ = false;
+    unsigned it_launches_ = 0;
+    // contact blocks a capacity-sized iteration holds; doubled past the count
+    // an overrun iteration reached
+    unsigned dyn_cap_ = 1u << 18;
+    DevBuf<StepParams> sp_dev_;
     DevBuf<PpfIntersectionRecord> isect_;
     std::vector<PpfIntersectionRecord> isect_host_;
     unsigned isect_count_ = 0;
