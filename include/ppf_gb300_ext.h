@@ -300,6 +300,20 @@ unsigned ppf_schwarz_coarsen(unsigned n, const unsigned *off, const unsigned *co
  * the six choices (set returns -1 for a value other than 0 or 1). Defaults:
  * 0 1 0 0 0 0. */
 int ppf_autotune(unsigned char *modes);
+/* The PCG's team. Each solve is one persistent launch: over the whole grid
+ * (one 1024-thread block per SM, a cooperative launch whose two reductions
+ * per iteration meet at grid barriers through L2), or as one thread-block
+ * cluster of up to 16 CTAs, whose hardware barrier stands for the grid
+ * barrier. A small system's iterations are bound by those reductions, so it
+ * solves faster on one cluster. ppf_set_pcg_team(-1) (the default) picks one
+ * cluster of the largest size the device runs for scenes up to 16,384
+ * vertices and the whole grid above, at each initialize; 0 sets the whole
+ * grid; 2 to 16 one cluster of that many CTAs (returns -1 for a size the
+ * device cannot run). ppf_autotune also times the whole grid against the
+ * largest cluster and half of it on the current Newton system and keeps the
+ * fastest. ppf_pcg_team returns the current team (0: the whole grid). */
+int ppf_set_pcg_team(int ctas);
+int ppf_pcg_team(void);
 void ppf_get_tuning(unsigned char *modes);
 int ppf_set_tuning(const unsigned char *modes);
 /* The CUDA stream (cudaStream_t, as void*) every kernel of advance() runs

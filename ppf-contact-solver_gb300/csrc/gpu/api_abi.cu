@@ -301,6 +301,15 @@ unsigned long long ppf_kernel_launches(void) { return ppf::gpu::g_kernel_launche
 unsigned long long ppf_graph_launches(void) {
     return solver_instance().ls_replays_ + solver_instance().graph_stats_.replays;
 }
+int ppf_set_pcg_team(int ctas) {
+    try {
+        return solver_instance().set_pcg_team(ctas) ? 0 : -1;
+    } catch (const ppf::FatalError &e) {
+        ppf::set_fatal(e.code, e.what());
+        return -1;
+    }
+}
+int ppf_pcg_team(void) { return (int)solver_instance().pcg_team(); }
 void ppf_set_iteration_graph(int enable) { solver_instance().graph_enabled_ = enable != 0; }
 void ppf_iteration_graph_stats(unsigned long long *out) {
     const auto &g = solver_instance().graph_stats_;

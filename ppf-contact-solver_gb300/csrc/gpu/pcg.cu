@@ -90,9 +90,20 @@ __device__ __forceinline__ void st_relaxed(unsigned *p, unsigned v) {
 // 32 * kFoldLoads blocks)
 constexpr unsigned kFoldLoads = 5;
 
+// Arrival at and wait on the cluster's hardware barrier by every thread,
+// release and acquire at cluster scope (orders the partials stored before it
+// for the other CTAs' L2 loads after it).
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+// With `cluster` set the launch is one thread-block cluster (all its CTAs
+// co-scheduled by the hardware) and the grid barrier is the cluster's
+// barrier, which every thread of the block passes; there is no wait to bound
+// and no abort.
 template <int N>
 __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
-                         unsigned *abort) {
+                         unsigned *abort, bool cluster) {
     __shared__ float s_w[N][kWarps];
     __shared__ float s_res[N];
     __shared__ int s_ok;
@@ -104,36 +115,41 @@ __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
 #pragma unroll
         for (int q = 0; q < N; ++q) s_w[q][w] = v[q];
     __syncthreads();
+    float x[N];
+    int ok = 1;
     if (w == 0) {
-        float x[N];
 #pragma unroll
         for (int q = 0; q < N; ++q) x[q] = s_w[q][lane]; // kWarps == 32
         for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
             for (int q = 0; q < N; ++q) x[q] += __shfl_down_sync(0xffffffffu, x[q], off);
-        int ok = 1;
         if (lane == 0) {
 #pragma unroll
             for (int q = 0; q < N; ++q) part[N * blockIdx.x + q] = x[q];
-            unsigned *count = bar, *gen = bar + 1;
-            const unsigned g0 = ld_relaxed(gen);
-            if (atom_add_acq_rel(count, 1u) == nb - 1) {
-                st_relaxed(count, 0u);
-                red_add_release(gen, 1u);
-            } else {
-                const unsigned long long t0 = global_ns();
-                for (unsigned spin = 0; ld_acquire(gen) == g0; ++spin) {
-                    if ((spin & 63u) == 63u) {
-                        if (ld_relaxed(abort) || global_ns() - t0 > kBarrierTimeoutNs) {
-                            atomicOr(abort, STATUS_PCG_BREAKDOWN);
-                            ok = 0;
-                            break;
+            if (!cluster) {
+                unsigned *count = bar, *gen = bar + 1;
+                const unsigned g0 = ld_relaxed(gen);
+                if (atom_add_acq_rel(count, 1u) == nb - 1) {
+                    st_relaxed(count, 0u);
+                    red_add_release(gen, 1u);
+                } else {
+                    const unsigned long long t0 = global_ns();
+                    for (unsigned spin = 0; ld_acquire(gen) == g0; ++spin) {
+                        if ((spin & 63u) == 63u) {
+                            if (ld_relaxed(abort) || global_ns() - t0 > kBarrierTimeoutNs) {
+                                atomicOr(abort, STATUS_PCG_BREAKDOWN);
+                                ok = 0;
+                                break;
+                            }
                         }
                     }
                 }
+                if (ok && ld_relaxed(abort)) ok = 0;
             }
-            if (ok && ld_relaxed(abort)) ok = 0;
         }
+    }
+    if (cluster) cluster_barrier();
+    if (w == 0) {
         ok = __shfl_sync(0xffffffffu, ok, 0);
         __syncwarp();
         if (ok) {
@@ -176,9 +192,9 @@ __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
 }
 
 __device__ bool grid_sum2(float &a, float &b, float *part, unsigned *bar, unsigned nb,
-                          unsigned *abort) {
+                          unsigned *abort, bool cluster) {
     float v[2] = {a, b};
-    const bool ok = grid_sum<2>(v, part, bar, nb, abort);
+    const bool ok = grid_sum<2>(v, part, bar, nb, abort, cluster);
     a = v[0];
     b = v[1];
     return ok;
@@ -337,6 +353,7 @@ struct PcgArgs {
     float4 *Y;   // G r of the factored preconditioner
     float *part; // 2 buffers of 2 floats per block, then 1 float per block
     unsigned *bar;
+    unsigned cluster; // nonzero: the launch is one cluster of this many CTAs
     float tol;
     unsigned max_iter;
     PcgResult *res;
@@ -525,7 +542,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
                          });
     }
     a = b = 0.0f;
-    if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
+    if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster)) goto aborted;
     // ... then r = b - A x0, z = P r, p_0 = 0; err0 = |r|_1, rz0 = r^T z
     a = b = 0.0f;
     for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
@@ -538,7 +555,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
         a += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
         b += ri.dot(zi);
     }
-    if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+    if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
     {
         const float err0 = a;
         float rz0 = b;
@@ -569,7 +586,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
                                  b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] +
                                       fabsf(pi[2]) * ab[2];
                              });
-            if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
+            if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster)) goto aborted;
             const float pAp = a, bound = kCurvatureSlack * kFloatEps * b;
             float alpha;
             if (pAp > bound) {
@@ -599,7 +616,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
                 a += ri.dot(zi);
                 b += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
             }
-            if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+            if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
             const float rz_new = a, err_now = b;
             beta = rz_new / rz0;
             rz0 = rz_new;
@@ -655,7 +672,7 @@ __device__ bool factor_y(const PcgArgs &g, BlockTasks &bt, unsigned lane, float 
                                  });
     }
     float a = 0.0f, b = 0.0f;
-    return grid_sum2(a, b, part, g.bar, gridDim.x, abort);
+    return grid_sum2(a, b, part, g.bar, gridDim.x, abort, g.cluster);
 }
 
 __device__ bool factor_z(const PcgArgs &g, BlockTasks &bt, unsigned lane, float *part,
@@ -688,7 +705,7 @@ __device__ bool factor_z(const PcgArgs &g, BlockTasks &bt, unsigned lane, float 
                                  });
     }
     float b = 0.0f;
-    if (!grid_sum2(a, b, part, g.bar, gridDim.x, abort)) return false;
+    if (!grid_sum2(a, b, part, g.bar, gridDim.x, abort, g.cluster)) return false;
     rz = a;
     return true;
 }
@@ -758,7 +775,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
                                         const Vec3 &) { st4(dst[part], slot, acc); });
     }
     a = b = 0.0f;
-    if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
+    if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster)) goto aborted;
     // r = b - A x0, err0 = |r|_1; records {0, 0}, Y = 0
     a = b = 0.0f;
     for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
@@ -770,7 +787,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
         st4(g.Y, i, Vec3::zero());
         a += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
     }
-    if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+    if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
     {
         const float err0 = a;
         if (err0 == 0.0f) {
@@ -802,7 +819,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
                                             b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] +
                                                  fabsf(pi[2]) * ab[2];
                                         });
-            if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
+            if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster)) goto aborted;
             const float pAp = a, bound = kCurvatureSlack * kFloatEps * b;
             float alpha;
             if (pAp > bound) {
@@ -835,7 +852,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
                 b += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
             }
             if (!refresh) factor_y_update(g, bt, lane, alpha);
-            if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+            if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
             const float err_now = b;
             float rz_new;
             if (refresh && !factor_y(g, bt, lane, part1, abort)) goto aborted;
@@ -1043,16 +1060,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
                                         const Vec3 &) { st4(dst[part], slot, acc); });
     }
     a = b = 0.0f;
-    if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
+    if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster)) goto aborted;
     // r = b - A x0, z = P r, p_0 = 0; rz0, err0
     a = b = 0.0f;
     for (unsigned ag = warp; ag < n_agg; ag += nwarps)
         schwarz_segment(g, ag, lane, true, 0.0f, seg, a, b);
-    if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+    if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
     if (n_dom) { // coarse correction, then its part of r^T z
         float c[1] = {0.0f};
         for (unsigned dm = warp; dm < n_dom; dm += nwarps) schwarz_coarse(g, dm, lane, seg, c[0]);
-        if (!grid_sum<1>(c, part2, g.bar, nb, abort)) goto aborted;
+        if (!grid_sum<1>(c, part2, g.bar, nb, abort, g.cluster)) goto aborted;
         a += c[0];
     }
     {
@@ -1089,7 +1106,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
                                             b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] +
                                                  fabsf(pi[2]) * ab[2];
                                         });
-            if (!grid_sum2(a, b, part1, g.bar, nb, abort)) goto aborted;
+            if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster)) goto aborted;
             const float pAp = a, bound = kCurvatureSlack * kFloatEps * b;
             float alpha;
             if (pAp > bound) {
@@ -1105,12 +1122,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
             a = b = 0.0f;
             for (unsigned ag = warp; ag < n_agg; ag += nwarps)
                 schwarz_segment(g, ag, lane, false, alpha, seg, a, b);
-            if (!grid_sum2(a, b, part0, g.bar, nb, abort)) goto aborted;
+            if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
             if (n_dom) {
                 float c[1] = {0.0f};
                 for (unsigned dm = warp; dm < n_dom; dm += nwarps)
                     schwarz_coarse(g, dm, lane, seg, c[0]);
-                if (!grid_sum<1>(c, part2, g.bar, nb, abort)) goto aborted;
+                if (!grid_sum<1>(c, part2, g.bar, nb, abort, g.cluster)) goto aborted;
                 a += c[0];
             }
             const float rz_new = a, err_now = b;
@@ -1397,6 +1414,42 @@ void PcgWorkspace::reserve(unsigned n) {
         if (per_sm > 1) per_sm = 1;
         grid = (unsigned)(sms * per_sm);
         threads = kThreads;
+        // the largest cluster the kernels can run as (one CTA per SM, so
+        // the CTAs of a GPC): 16 when the device allows clusters that large
+        const size_t schwarz_smem = (size_t)kWarps * kSchwarzWarpFloats * sizeof(float);
+        PPF_CUDA(cudaFuncSetAttribute((const void *)k_pcg_schwarz,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)schwarz_smem));
+        max_cluster = 16;
+        for (const void *kf : {(const void *)k_pcg, (const void *)k_pcg_factor,
+                               (const void *)k_pcg_schwarz}) {
+            if (cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                cudaSuccess) {
+                cudaGetLastError();
+                max_cluster = std::min(max_cluster, 8u);
+                continue;
+            }
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(16);
+            cfg.blockDim = dim3(kThreads);
+            cfg.dynamicSmemBytes = kf == (const void *)k_pcg_schwarz ? schwarz_smem : 0;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = 16;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int size = 0;
+            if (cudaOccupancyMaxPotentialClusterSize(&size, kf, &cfg) != cudaSuccess) {
+                cudaGetLastError();
+                size = 0;
+            }
+            unsigned c = 1;
+            while (2 * c <= (unsigned)std::max(size, 1)) c *= 2;
+            max_cluster = std::min(max_cluster, c);
+        }
+        if (max_cluster < 2) max_cluster = 0;
     }
     partials.reserve(6 * (size_t)grid + 4);
     barrier.reserve(4);
@@ -1590,8 +1643,11 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     k_task_cost<<<div_up(T, 256u), 256, 0, q>>>(A, T, ws.task_cost.data());
     PPF_LAUNCH_CHECK();
     exclusive_scan(ws.task_cost.data(), ws.task_off.data(), T, ws.scan_tmp.data(), q);
-    k_task_split<<<div_up(ws.grid + 1, 256u), 256, 0, q>>>(A, ws.task_off.data(), ws.grid,
-                                                          ws.task_start.data());
+    // the whole grid (a cooperative launch), or one cluster of ws.cluster CTAs
+    const unsigned nb =
+        ws.cluster >= 2 && ws.cluster <= ws.max_cluster ? ws.cluster : ws.grid;
+    k_task_split<<<div_up(nb + 1, 256u), 256, 0, q>>>(A, ws.task_off.data(), nb,
+                                                     ws.task_start.data());
     PPF_LAUNCH_CHECK();
     // one counter per product phase: the initial product, then one (block-
     // Jacobi) or three (factored) per iteration, plus the factored start
@@ -1612,6 +1668,7 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
               ws.Y.data(),
               ws.partials.data(),
               ws.barrier.data(),
+              nb == ws.grid ? 0u : nb,
               tol,
               max_iter,
               ws.result.data(),
@@ -1620,19 +1677,26 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     const void *kernel = A.schwarz.n_agg ? (const void *)k_pcg_schwarz
                          : A.factor.diag ? (const void *)k_pcg_factor
                                          : (const void *)k_pcg;
-    size_t dyn_smem = 0;
-    if (A.schwarz.n_agg) {
-        dyn_smem = (size_t)kWarps * kSchwarzWarpFloats * sizeof(float);
-        static bool attr_set = false;
-        if (!attr_set) {
-            PPF_CUDA(cudaFuncSetAttribute((const void *)k_pcg_schwarz,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)dyn_smem));
-            attr_set = true;
-        }
+    const size_t dyn_smem =
+        A.schwarz.n_agg ? (size_t)kWarps * kSchwarzWarpFloats * sizeof(float) : 0;
+    if (nb == ws.grid) {
+        PPF_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(nb), dim3(ws.threads), args, dyn_smem,
+                                             q));
+    } else {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(nb);
+        cfg.blockDim = dim3(ws.threads);
+        cfg.dynamicSmemBytes = dyn_smem;
+        cfg.stream = q;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = nb;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        PPF_CUDA(cudaLaunchKernelExC(&cfg, kernel, args));
     }
-    PPF_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(ws.grid), dim3(ws.threads), args, dyn_smem,
-                                         q));
     ++g_kernel_launches;
 }
 

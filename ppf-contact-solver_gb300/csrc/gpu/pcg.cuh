@@ -142,6 +142,10 @@ struct PcgWorkspace {
     DevBuf<unsigned> barrier;
     DevBuf<PcgResult> result;
     unsigned grid = 0, threads = 0;
+    // 0: each solve runs on the whole grid (one block per SM, grid-wide
+    // barriers through L2); 2 to max_cluster: on one thread-block cluster of
+    // that many CTAs, whose hardware barrier stands for the grid barrier
+    unsigned cluster = 0, max_cluster = 0;
     void reserve(unsigned n);
 };
 

@@ -49,6 +49,8 @@ struct CsrView {
 struct Tuning {
     unsigned char detect_vertex = 0, detect_edge = 1, ccd_vertex = 0, ccd_mesh_vertex = 0,
                   ccd_edge = 0, isect = 0;
+    // the PCG's team: 0 the whole grid, else one cluster of this many CTAs
+    unsigned char pcg_cluster = 0;
 };
 
 // Everything a kernel needs to read the scene (device pointers, by value).

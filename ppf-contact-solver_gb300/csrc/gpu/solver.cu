@@ -667,6 +667,8 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     dcnt2_buf_.reserve(n_ + 1);
     scan_tmp_.reserve(scan_tmp_size(n_ + 1));
     pcg_.reserve(n_);
+    if (pcg_team_auto_) tune_.pcg_cluster = auto_pcg_team();
+    pcg_.cluster = tune_.pcg_cluster;
     upload_collision_mesh(ds->constraint.mesh);
     initialized_ = true;
     carried_ = false;
@@ -1007,6 +1009,7 @@ void Solver::enqueue_solve(bool capturing) {
     PPF_CUDA(cudaMemcpyAsync(r_.data(), force_.data(), n3 * sizeof(float),
                              cudaMemcpyDeviceToDevice, q_));
     PcgOperator A = pcg_operator();
+    pcg_.cluster = tune_.pcg_cluster;
     record_event(ev0_, capturing);
     if (factor_active_ || schwarz_active_) {
         dx0_.reserve(n3);
@@ -1627,7 +1630,9 @@ void Solver::set_contact_capacity(unsigned pair_cap, unsigned block_cap) {
 }
 
 void Solver::set_tuning(const Tuning &t) {
+    const unsigned char team = tune_.pcg_cluster;
     tune_ = t;
+    tune_.pcg_cluster = team;
     ++scene_version_; // the line-search graph holds the kernels it chose
 }
 
@@ -1700,10 +1705,65 @@ Tuning Solver::autotune() {
         };
         pick(tune_.isect, isect);
     }
+    // the PCG's team, by the time of 40 iterations on the Newton system at
+    // the current positions (tolerance 0: no early exit), block-Jacobi
+    if (pcg_.max_cluster >= 2 && n_) {
+        const float dt = param->dt * param->playback;
+        PPF_CUDA(cudaMemcpyAsync(eval_x_.data(), curr_.data(), n3 * sizeof(float),
+                                 cudaMemcpyDeviceToDevice, q_));
+        compute_target(dt);
+        PPF_CUDA(cudaMemsetAsync(st_.data(), 0, sizeof(IterStatus), q_));
+        assemble(dt);
+        PcgOperator A = pcg_operator();
+        A.factor = PcgFactor{};
+        A.schwarz = SchwarzView{};
+        auto solve = [&]() {
+            PPF_CUDA(cudaMemcpyAsync(r_.data(), force_.data(), n3 * sizeof(float),
+                                     cudaMemcpyDeviceToDevice, q_));
+            PPF_CUDA(cudaMemsetAsync(dx_.data(), 0, n3 * sizeof(float), q_));
+            launch_pcg(A, dx_.data(), r_.data(), 0.0f, 40u, pcg_, q_);
+        };
+        float best = 1e30f;
+        unsigned char choice = 0;
+        for (unsigned c : {0u, pcg_.max_cluster, pcg_.max_cluster / 2}) {
+            if (c == 1) continue;
+            pcg_.cluster = c;
+            const float t = time(solve);
+            if (t < best) {
+                best = t;
+                choice = (unsigned char)c;
+            }
+        }
+        tune_.pcg_cluster = choice;
+        pcg_.cluster = choice;
+        pcg_team_auto_ = false;
+    }
     PPF_CUDA(cudaMemsetAsync(st_.data(), 0, sizeof(IterStatus), q_));
     PPF_CUDA(cudaStreamSynchronize(q_));
     ++scene_version_;
     return tune_;
+}
+
+bool Solver::set_pcg_team(int ctas) {
+    pcg_.reserve(std::max(n_, 1u));
+    if (ctas < 0) {
+        pcg_team_auto_ = true;
+        tune_.pcg_cluster = auto_pcg_team();
+    } else if (ctas == 0 || (ctas >= 2 && (unsigned)ctas <= pcg_.max_cluster)) {
+        pcg_team_auto_ = false;
+        tune_.pcg_cluster = (unsigned char)ctas;
+    } else {
+        return false;
+    }
+    pcg_.cluster = tune_.pcg_cluster;
+    return true;
+}
+
+// Systems up to kClusterPcgRows vertices solve on one cluster: their
+// iterations are bound by the two reductions, which a cluster's hardware
+// barrier makes several times cheaper than a grid barrier through L2.
+unsigned char Solver::auto_pcg_team() const {
+    return n_ <= kClusterPcgRows && pcg_.max_cluster >= 2 ? (unsigned char)pcg_.max_cluster : 0;
 }
 
 float Solver::debug_contact_line_search(const float *x0, const float *x1, unsigned &overlap) {

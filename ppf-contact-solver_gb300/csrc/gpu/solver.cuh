@@ -13,6 +13,8 @@
 namespace ppf {
 namespace gpu {
 
+constexpr unsigned kClusterPcgRows = 16384;
+
 // Per-step statistics (GB300 extension, ppf_step_stats in ppf_gb300_ext.h).
 struct StepStats {
     unsigned newton_iters = 0;
@@ -94,7 +96,14 @@ class Solver {
     // intersection check) and keeps the faster of each; returns the choice.
     Tuning autotune();
     Tuning tuning() const { return tune_; }
+    // the traversal leaf-test forms (the PCG team is kept)
     void set_tuning(const Tuning &t);
+    // The PCG's team: -1 automatic (one cluster up to kClusterPcgRows
+    // vertices, else the whole grid), 0 the whole grid, 2 to the largest
+    // cluster the device runs: one cluster of that many CTAs. False for a
+    // size the device cannot run.
+    bool set_pcg_team(int ctas);
+    unsigned pcg_team() const { return tune_.pcg_cluster; }
     // Caps the pair lists at pair_cap entries each and a capacity-sized
     // iteration at block_cap contact blocks (0 leaves one as it is); larger
     // counts then take the overrun-and-repeat path.
@@ -259,6 +268,8 @@ class Solver {
     // an overrun iteration reached
     unsigned dyn_cap_ = 1u << 18;
     DevBuf<StepParams> sp_dev_;
+    bool pcg_team_auto_ = true;
+    unsigned char auto_pcg_team() const;
     DevBuf<PpfIntersectionRecord> isect_;
     std::vector<PpfIntersectionRecord> isect_host_;
     unsigned isect_count_ = 0;

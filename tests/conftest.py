@@ -77,7 +77,8 @@ def rng():
 def _block_jacobi_after_each_test(request):
     """The library keeps its preconditioner choice across sessions (it is a
     process-wide setting, like the rest of its state): put block-Jacobi, the
-    reference's, back after every GPU test, so no test inherits another's."""
+    reference's, back after every GPU test, so no test inherits another's
+    (the same for the PCG team and the iteration graph)."""
     yield
     if request.node.get_closest_marker("gpu") is None:
         return
@@ -87,3 +88,6 @@ def _block_jacobi_after_each_test(request):
 
     if _lib._PRODUCT is not None:
         _lib._PRODUCT.ppf_set_preconditioner(ctypes.c_int(0), ctypes.c_float(0.0))
+        # and the default PCG team and Newton-iteration graph
+        _lib._PRODUCT.ppf_set_pcg_team(ctypes.c_int(-1))
+        _lib._PRODUCT.ppf_set_iteration_graph(ctypes.c_int(1))
