@@ -97,13 +97,80 @@ __device__ __forceinline__ void cluster_barrier() {
     asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
 }
 
-// With `cluster` set the launch is one thread-block cluster (all its CTAs
-// co-scheduled by the hardware) and the grid barrier is the cluster's
-// barrier, which every thread of the block passes; there is no wait to bound
-// and no abort.
+// Folds the first n of the N-value partials at p (lane k holds entries k,
+// k + 32, ...), the loads in flight together, in a fixed order: every block
+// that folds the same partials gets the same bits. Result on lane 0.
+template <int N>
+__device__ __forceinline__ void fold_partials(const float *p, unsigned n, unsigned lane,
+                                              float (&x)[N]) {
+#pragma unroll
+    for (int q = 0; q < N; ++q) x[q] = 0.0f;
+    if (n <= 32u * kFoldLoads) {
+        float pv[kFoldLoads][N];
+#pragma unroll
+        for (unsigned j = 0; j < kFoldLoads; ++j) {
+            const unsigned k = lane + 32u * j;
+#pragma unroll
+            for (int q = 0; q < N; ++q) pv[j][q] = k < n ? __ldcg(p + N * k + q) : 0.0f;
+        }
+#pragma unroll
+        for (unsigned j = 0; j < kFoldLoads; ++j)
+            if (lane + 32u * j < n)
+#pragma unroll
+                for (int q = 0; q < N; ++q) x[q] += pv[j][q];
+    } else {
+        for (unsigned k = lane; k < n; k += 32)
+#pragma unroll
+            for (int q = 0; q < N; ++q) x[q] += __ldcg(p + N * k + q);
+    }
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int q = 0; q < N; ++q) x[q] += __shfl_down_sync(0xffffffffu, x[q], off);
+}
+
+// Arrival of lane 0 of warp 0 at the grid barrier through L2 among `count`
+// arrivers (acquire-release), and its bounded wait. Returns 0 when the wait
+// timed out or another block latched an abort.
+__device__ __forceinline__ int grid_arrive_wait(unsigned *bar, unsigned count, unsigned *abort) {
+    int ok = 1;
+    unsigned *ctr = bar, *gen = bar + 1;
+    const unsigned g0 = ld_relaxed(gen);
+    if (atom_add_acq_rel(ctr, 1u) == count - 1) {
+        st_relaxed(ctr, 0u);
+        red_add_release(gen, 1u);
+    } else {
+        const unsigned long long t0 = global_ns();
+        for (unsigned spin = 0; ld_acquire(gen) == g0; ++spin) {
+            if ((spin & 63u) == 63u) {
+                if (ld_relaxed(abort) || global_ns() - t0 > kBarrierTimeoutNs) {
+                    atomicOr(abort, STATUS_PCG_BREAKDOWN);
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+    }
+    if (ok && ld_relaxed(abort)) ok = 0;
+    return ok;
+}
+
+// The barrier has three forms, by `cluster` (the launch's cluster size):
+//   0          every block's lane 0 arrives at the grid barrier through L2
+//              and folds all blocks' partials;
+//   gridDim.x  the launch is one cluster (all its CTAs co-scheduled by the
+//              hardware): the cluster's barrier, passed by every thread,
+//              stands for the grid barrier; there is no wait to bound;
+//   otherwise  a cooperative launch in clusters: the CTAs of a cluster meet
+//              at its barrier, its first CTA folds their partials (in block
+//              order) and alone arrives at the grid barrier, folds the
+//              clusters' partials and hands the sum (and the verdict) back
+//              through L2 behind a second cluster barrier: gridDim.x /
+//              cluster arrivals instead of gridDim.x.
+// `part` holds 5 gridDim.x floats: the block partials, then, in clusters,
+// the cluster partials and the per-cluster results.
 template <int N>
 __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
-                         unsigned *abort, bool cluster) {
+                         unsigned *abort, unsigned cluster) {
     __shared__ float s_w[N][kWarps];
     __shared__ float s_res[N];
     __shared__ int s_ok;
@@ -116,73 +183,58 @@ __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
         for (int q = 0; q < N; ++q) s_w[q][w] = v[q];
     __syncthreads();
     float x[N];
-    int ok = 1;
     if (w == 0) {
 #pragma unroll
         for (int q = 0; q < N; ++q) x[q] = s_w[q][lane]; // kWarps == 32
         for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
             for (int q = 0; q < N; ++q) x[q] += __shfl_down_sync(0xffffffffu, x[q], off);
-        if (lane == 0) {
+        if (lane == 0)
 #pragma unroll
             for (int q = 0; q < N; ++q) part[N * blockIdx.x + q] = x[q];
-            if (!cluster) {
-                unsigned *count = bar, *gen = bar + 1;
-                const unsigned g0 = ld_relaxed(gen);
-                if (atom_add_acq_rel(count, 1u) == nb - 1) {
-                    st_relaxed(count, 0u);
-                    red_add_release(gen, 1u);
-                } else {
-                    const unsigned long long t0 = global_ns();
-                    for (unsigned spin = 0; ld_acquire(gen) == g0; ++spin) {
-                        if ((spin & 63u) == 63u) {
-                            if (ld_relaxed(abort) || global_ns() - t0 > kBarrierTimeoutNs) {
-                                atomicOr(abort, STATUS_PCG_BREAKDOWN);
-                                ok = 0;
-                                break;
-                            }
-                        }
-                    }
-                }
-                if (ok && ld_relaxed(abort)) ok = 0;
-            }
-        }
     }
-    if (cluster) cluster_barrier();
-    if (w == 0) {
-        ok = __shfl_sync(0xffffffffu, ok, 0);
-        __syncwarp();
-        if (ok) {
-#pragma unroll
-            for (int q = 0; q < N; ++q) x[q] = 0.0f;
-            if (nb <= 32u * kFoldLoads) {
-                // every partial loaded before the first add, so the loads are
-                // in flight together; added in the same order as the loop
-                float pv[kFoldLoads][N];
-#pragma unroll
-                for (unsigned j = 0; j < kFoldLoads; ++j) {
-                    const unsigned k = lane + 32u * j;
-#pragma unroll
-                    for (int q = 0; q < N; ++q) pv[j][q] = k < nb ? __ldcg(part + N * k + q) : 0.0f;
-                }
-#pragma unroll
-                for (unsigned j = 0; j < kFoldLoads; ++j)
-                    if (lane + 32u * j < nb)
-#pragma unroll
-                        for (int q = 0; q < N; ++q) x[q] += pv[j][q];
-            } else {
-                for (unsigned k = lane; k < nb; k += 32)
-#pragma unroll
-                    for (int q = 0; q < N; ++q) x[q] += __ldcg(part + N * k + q);
-            }
-            for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-                for (int q = 0; q < N; ++q) x[q] += __shfl_down_sync(0xffffffffu, x[q], off);
+    if (cluster == 0 || cluster == nb) {
+        int ok = 1;
+        if (cluster == 0) {
+            if (w == 0 && lane == 0) ok = grid_arrive_wait(bar, nb, abort);
+        } else {
+            cluster_barrier();
         }
-        if (lane == 0) {
+        if (w == 0) {
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (ok) fold_partials<N>(part, nb, lane, x);
+            if (lane == 0) {
 #pragma unroll
-            for (int q = 0; q < N; ++q) s_res[q] = x[q];
-            s_ok = ok;
+                for (int q = 0; q < N; ++q) s_res[q] = x[q];
+                s_ok = ok;
+            }
+        }
+    } else {
+        const unsigned ncl = nb / cluster, cid = blockIdx.x / cluster;
+        float *cpart = part + N * nb, *cres = cpart + N * ncl + (N + 1) * cid;
+        cluster_barrier();
+        if (blockIdx.x % cluster == 0 && w == 0) {
+            float y[N];
+            fold_partials<N>(part + N * cid * cluster, cluster, lane, y);
+            int ok = 1;
+            if (lane == 0) {
+#pragma unroll
+                for (int q = 0; q < N; ++q) cpart[N * cid + q] = y[q];
+                ok = grid_arrive_wait(bar, ncl, abort);
+            }
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (ok) fold_partials<N>(cpart, ncl, lane, x);
+            if (lane == 0) {
+#pragma unroll
+                for (int q = 0; q < N; ++q) cres[q] = ok ? x[q] : 0.0f;
+                cres[N] = ok ? 1.0f : 0.0f;
+            }
+        }
+        cluster_barrier();
+        if (w == 0 && lane == 0) {
+#pragma unroll
+            for (int q = 0; q < N; ++q) s_res[q] = __ldcg(cres + q);
+            s_ok = __ldcg(cres + N) != 0.0f;
         }
     }
     __syncthreads();
@@ -192,7 +244,7 @@ __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
 }
 
 __device__ bool grid_sum2(float &a, float &b, float *part, unsigned *bar, unsigned nb,
-                          unsigned *abort, bool cluster) {
+                          unsigned *abort, unsigned cluster) {
     float v[2] = {a, b};
     const bool ok = grid_sum<2>(v, part, bar, nb, abort, cluster);
     a = v[0];
@@ -351,9 +403,9 @@ struct PcgArgs {
     float *R;            // 8 floats per vertex: {z, p} records
     float4 *p, *Ap, *Ap_c, *Ap_ovf;
     float4 *Y;   // G r of the factored preconditioner
-    float *part; // 2 buffers of 2 floats per block, then 1 float per block
+    float *part; // 3 buffers of 5 floats per block (grid_sum)
     unsigned *bar;
-    unsigned cluster; // nonzero: the launch is one cluster of this many CTAs
+    unsigned cluster; // the launch's cluster size (0: none; gridDim.x: one cluster)
     float tol;
     unsigned max_iter;
     PcgResult *res;
@@ -519,7 +571,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
     const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
     const unsigned n_slices = A.fixed.n_slices;
     unsigned *abort = g.bar + 2;
-    float *part0 = g.part, *part1 = g.part + 2 * nb;
+    float *part0 = g.part, *part1 = g.part + 5 * nb;
     float a, b;
 
     // work items of the products: half slices (16 rows, two lanes per row),
@@ -756,7 +808,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
     const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
     const unsigned n_slices = A.fixed.n_slices;
     unsigned *abort = g.bar + 2;
-    float *part0 = g.part, *part1 = g.part + 2 * nb;
+    float *part0 = g.part, *part1 = g.part + 5 * nb;
     float a, b;
 
     __shared__ unsigned s_next;
@@ -1040,7 +1092,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
     const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
     const unsigned n_agg = A.schwarz.n_agg, n_dom = A.schwarz.n_dom;
     unsigned *abort = g.bar + 2;
-    float *part0 = g.part, *part1 = g.part + 2 * nb, *part2 = g.part + 4 * nb;
+    float *part0 = g.part, *part1 = g.part + 5 * nb, *part2 = g.part + 10 * nb;
     float a, b;
     extern __shared__ float4 s_dyn4[];
     float *seg = reinterpret_cast<float *>(s_dyn4) + (size_t)wib * kSchwarzWarpFloats;
@@ -1450,8 +1502,39 @@ void PcgWorkspace::reserve(unsigned n) {
             max_cluster = std::min(max_cluster, c);
         }
         if (max_cluster < 2) max_cluster = 0;
+        // the whole grid in clusters: the largest size that divides the
+        // grid and whose clusters all fit on the device at once
+        grid_cluster = 0;
+        for (unsigned c : {8u, 4u, 2u}) {
+            if (grid % c) continue;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(grid);
+            cfg.blockDim = dim3(kThreads);
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = c;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int fit = 0, fit_s = 0;
+            if (cudaOccupancyMaxActiveClusters(&fit, (const void *)k_pcg, &cfg) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            cfg.dynamicSmemBytes = schwarz_smem;
+            if (cudaOccupancyMaxActiveClusters(&fit_s, (const void *)k_pcg_schwarz, &cfg) !=
+                cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            if ((unsigned)std::min(fit, fit_s) * c >= grid) {
+                grid_cluster = c;
+                break;
+            }
+        }
     }
-    partials.reserve(6 * (size_t)grid + 4);
+    partials.reserve(15 * (size_t)grid + 4);
     barrier.reserve(4);
     result.reserve(1);
 }
@@ -1643,9 +1726,12 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     k_task_cost<<<div_up(T, 256u), 256, 0, q>>>(A, T, ws.task_cost.data());
     PPF_LAUNCH_CHECK();
     exclusive_scan(ws.task_cost.data(), ws.task_off.data(), T, ws.scan_tmp.data(), q);
-    // the whole grid (a cooperative launch), or one cluster of ws.cluster CTAs
-    const unsigned nb =
-        ws.cluster >= 2 && ws.cluster <= ws.max_cluster ? ws.cluster : ws.grid;
+    // the whole grid (a cooperative launch, in clusters of ws.grid_cluster
+    // CTAs when asked and possible), or one cluster of ws.cluster CTAs
+    const bool one_cluster = ws.cluster >= 2 && ws.cluster <= ws.max_cluster;
+    const unsigned nb = one_cluster ? ws.cluster : ws.grid;
+    const unsigned launch_cluster =
+        one_cluster ? nb : (ws.cluster == 1 && ws.grid_cluster >= 2 ? ws.grid_cluster : 0u);
     k_task_split<<<div_up(nb + 1, 256u), 256, 0, q>>>(A, ws.task_off.data(), nb,
                                                      ws.task_start.data());
     PPF_LAUNCH_CHECK();
@@ -1668,7 +1754,7 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
               ws.Y.data(),
               ws.partials.data(),
               ws.barrier.data(),
-              nb == ws.grid ? 0u : nb,
+              launch_cluster,
               tol,
               max_iter,
               ws.result.data(),
@@ -1679,7 +1765,7 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
                                          : (const void *)k_pcg;
     const size_t dyn_smem =
         A.schwarz.n_agg ? (size_t)kWarps * kSchwarzWarpFloats * sizeof(float) : 0;
-    if (nb == ws.grid) {
+    if (launch_cluster == 0) {
         PPF_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(nb), dim3(ws.threads), args, dyn_smem,
                                              q));
     } else {
@@ -1688,14 +1774,27 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
         cfg.blockDim = dim3(ws.threads);
         cfg.dynamicSmemBytes = dyn_smem;
         cfg.stream = q;
-        cudaLaunchAttribute attr[1];
+        cudaLaunchAttribute attr[2];
         attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = nb;
+        attr[0].val.clusterDim.x = launch_cluster;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
+        attr[1].id = cudaLaunchAttributeCooperative;
+        attr[1].val.cooperative = 1;
         cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        PPF_CUDA(cudaLaunchKernelExC(&cfg, kernel, args));
+        cfg.numAttrs = one_cluster ? 1 : 2;
+        const cudaError_t e = cudaLaunchKernelExC(&cfg, kernel, args);
+        if (e != cudaSuccess && !one_cluster) {
+            // a cooperative launch in clusters the device refuses: the whole
+            // grid without clusters from now on
+            cudaGetLastError();
+            ws.grid_cluster = 0;
+            g.cluster = 0;
+            PPF_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(nb), dim3(ws.threads), args,
+                                                 dyn_smem, q));
+        } else {
+            PPF_CUDA(e);
+        }
     }
     ++g_kernel_launches;
 }
