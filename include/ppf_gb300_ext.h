@@ -305,16 +305,13 @@ int ppf_autotune(unsigned char *modes);
  * per iteration meet at grid barriers through L2), or as one thread-block
  * cluster of up to 16 CTAs, whose hardware barrier stands for the grid
  * barrier. A small system's iterations are bound by those reductions, so it
- * solves faster on one cluster. The whole grid can also run in clusters of
- * 2 to 8 CTAs: a cluster's CTAs meet at its barrier and one of them arrives
- * at the grid barrier for all. ppf_set_pcg_team(-1) (the default) picks one
+ * solves faster on one cluster. ppf_set_pcg_team(-1) (the default) picks one
  * cluster of the largest size the device runs for scenes up to 16,384
  * vertices and the whole grid above, at each initialize; 0 sets the whole
- * grid; 1 the whole grid in clusters; 2 to 16 one cluster of that many CTAs
- * (returns -1 for a form the device cannot run). ppf_autotune also times the
- * whole grid (both forms) against the largest cluster and half of it on the
- * current Newton system and keeps the fastest. ppf_pcg_team returns the
- * current team. */
+ * grid; 2 to 16 one cluster of that many CTAs (returns -1 for a size the
+ * device cannot run). ppf_autotune also times the whole grid against the
+ * largest cluster and half of it on the current Newton system and keeps the
+ * fastest. ppf_pcg_team returns the current team (0: the whole grid). */
 int ppf_set_pcg_team(int ctas);
 int ppf_pcg_team(void);
 void ppf_get_tuning(unsigned char *modes);

@@ -154,20 +154,13 @@ __device__ __forceinline__ int grid_arrive_wait(unsigned *bar, unsigned count, u
     return ok;
 }
 
-// The barrier has three forms, by `cluster` (the launch's cluster size):
+// The barrier has two forms, by `cluster` (the launch's cluster size):
 //   0          every block's lane 0 arrives at the grid barrier through L2
 //              and folds all blocks' partials;
 //   gridDim.x  the launch is one cluster (all its CTAs co-scheduled by the
 //              hardware): the cluster's barrier, passed by every thread,
-//              stands for the grid barrier; there is no wait to bound;
-//   otherwise  a cooperative launch in clusters: the CTAs of a cluster meet
-//              at its barrier, its first CTA folds their partials (in block
-//              order) and alone arrives at the grid barrier, folds the
-//              clusters' partials and hands the sum (and the verdict) back
-//              through L2 behind a second cluster barrier: gridDim.x /
-//              cluster arrivals instead of gridDim.x.
-// `part` holds 5 gridDim.x floats: the block partials, then, in clusters,
-// the cluster partials and the per-cluster results.
+//              stands for the grid barrier; there is no wait to bound.
+// `part` holds 2 gridDim.x floats: the block partials.
 template <int N>
 __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
                          unsigned *abort, unsigned cluster) {
@@ -193,48 +186,19 @@ __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
 #pragma unroll
             for (int q = 0; q < N; ++q) part[N * blockIdx.x + q] = x[q];
     }
-    if (cluster == 0 || cluster == nb) {
-        int ok = 1;
-        if (cluster == 0) {
-            if (w == 0 && lane == 0) ok = grid_arrive_wait(bar, nb, abort);
-        } else {
-            cluster_barrier();
-        }
-        if (w == 0) {
-            ok = __shfl_sync(0xffffffffu, ok, 0);
-            if (ok) fold_partials<N>(part, nb, lane, x);
-            if (lane == 0) {
-#pragma unroll
-                for (int q = 0; q < N; ++q) s_res[q] = x[q];
-                s_ok = ok;
-            }
-        }
+    int ok = 1;
+    if (cluster == 0) {
+        if (w == 0 && lane == 0) ok = grid_arrive_wait(bar, nb, abort);
     } else {
-        const unsigned ncl = nb / cluster, cid = blockIdx.x / cluster;
-        float *cpart = part + N * nb, *cres = cpart + N * ncl + (N + 1) * cid;
         cluster_barrier();
-        if (blockIdx.x % cluster == 0 && w == 0) {
-            float y[N];
-            fold_partials<N>(part + N * cid * cluster, cluster, lane, y);
-            int ok = 1;
-            if (lane == 0) {
+    }
+    if (w == 0) {
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (ok) fold_partials<N>(part, nb, lane, x);
+        if (lane == 0) {
 #pragma unroll
-                for (int q = 0; q < N; ++q) cpart[N * cid + q] = y[q];
-                ok = grid_arrive_wait(bar, ncl, abort);
-            }
-            ok = __shfl_sync(0xffffffffu, ok, 0);
-            if (ok) fold_partials<N>(cpart, ncl, lane, x);
-            if (lane == 0) {
-#pragma unroll
-                for (int q = 0; q < N; ++q) cres[q] = ok ? x[q] : 0.0f;
-                cres[N] = ok ? 1.0f : 0.0f;
-            }
-        }
-        cluster_barrier();
-        if (w == 0 && lane == 0) {
-#pragma unroll
-            for (int q = 0; q < N; ++q) s_res[q] = __ldcg(cres + q);
-            s_ok = __ldcg(cres + N) != 0.0f;
+            for (int q = 0; q < N; ++q) s_res[q] = x[q];
+            s_ok = ok;
         }
     }
     __syncthreads();
@@ -403,7 +367,7 @@ struct PcgArgs {
     float *R;            // 8 floats per vertex: {z, p} records
     float4 *p, *Ap, *Ap_c, *Ap_ovf;
     float4 *Y;   // G r of the factored preconditioner
-    float *part; // 3 buffers of 5 floats per block (grid_sum)
+    float *part; // 2 buffers of 2 floats per block, then 1 float per block
     unsigned *bar;
     unsigned cluster; // the launch's cluster size (0: none; gridDim.x: one cluster)
     float tol;
@@ -455,7 +419,8 @@ constexpr unsigned kStaticSixteenths = 12;
 // pool [dyn0, total) through the phase's global counter. Each product phase
 // of a solve has its own counter (zeroed before the launch).
 struct BlockTasks {
-    unsigned *next;       // shared
+    unsigned *next;       // shared: [0] the static range's next task, [1] set
+                          // once the common pool ran dry for this block
     unsigned begin, end;  // this block's static range
     unsigned dyn0, total; // the common pool
     unsigned *ctrs;       // one per phase
@@ -466,18 +431,26 @@ struct BlockTasks {
     __device__ __forceinline__ void start() {
         ctr = phase < n_ctrs ? ctrs + phase : nullptr;
         ++phase;
-        if (threadIdx.x == 0) *next = begin;
+        if (threadIdx.x == 0) {
+            next[0] = begin;
+            next[1] = 0u;
+        }
         __syncthreads();
     }
+    // The block's warps stop asking the pool's global counter once one of
+    // them found it empty, so an empty pool costs about one atomic per block
+    // rather than one per warp.
     __device__ __forceinline__ unsigned take(unsigned lane) const {
         unsigned t = 0;
         if (lane == 0u) {
             t = atomicAdd(next, 1u);
             if (t >= end) {
                 t = kNoTask;
-                if (ctr) {
+                volatile unsigned *drained = next + 1;
+                if (ctr && !*drained) {
                     const unsigned d = atomicAdd(ctr, 1u);
                     if (d < total - dyn0) t = dyn0 + d;
+                    else *drained = 1u;
                 }
             }
         }
@@ -571,15 +544,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
     const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
     const unsigned n_slices = A.fixed.n_slices;
     unsigned *abort = g.bar + 2;
-    float *part0 = g.part, *part1 = g.part + 5 * nb;
+    float *part0 = g.part, *part1 = g.part + 2 * nb;
     float a, b;
 
     // work items of the products: half slices (16 rows, two lanes per row),
     // then one warp per overflow row of the contact part
 
-    __shared__ unsigned s_next;
+    __shared__ unsigned s_next[2];
     const TaskSpace ts(A);
-    BlockTasks bt{&s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
+    BlockTasks bt{s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
                   g.task_start[gridDim.x], ts.total, g.dyn_ctr, g.n_ctr};
     // A x0 (slice part to Ap, overflow part to Ap_ovf) ...
     bt.start();
@@ -808,12 +781,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
     const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
     const unsigned n_slices = A.fixed.n_slices;
     unsigned *abort = g.bar + 2;
-    float *part0 = g.part, *part1 = g.part + 5 * nb;
+    float *part0 = g.part, *part1 = g.part + 2 * nb;
     float a, b;
 
-    __shared__ unsigned s_next;
+    __shared__ unsigned s_next[2];
     const TaskSpace ts(A);
-    BlockTasks bt{&s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
+    BlockTasks bt{s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
                   g.task_start[gridDim.x], ts.total, g.dyn_ctr, g.n_ctr};
     const float *const avals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
     // A x0
@@ -1092,14 +1065,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
     const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
     const unsigned n_agg = A.schwarz.n_agg, n_dom = A.schwarz.n_dom;
     unsigned *abort = g.bar + 2;
-    float *part0 = g.part, *part1 = g.part + 5 * nb, *part2 = g.part + 10 * nb;
+    float *part0 = g.part, *part1 = g.part + 2 * nb, *part2 = g.part + 4 * nb;
     float a, b;
     extern __shared__ float4 s_dyn4[];
     float *seg = reinterpret_cast<float *>(s_dyn4) + (size_t)wib * kSchwarzWarpFloats;
 
-    __shared__ unsigned s_next;
+    __shared__ unsigned s_next[2];
     const TaskSpace ts(A);
-    BlockTasks bt{&s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
+    BlockTasks bt{s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
                   g.task_start[gridDim.x], ts.total, g.dyn_ctr, g.n_ctr};
     const float *const avals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
     bt.start();
@@ -1502,39 +1475,8 @@ void PcgWorkspace::reserve(unsigned n) {
             max_cluster = std::min(max_cluster, c);
         }
         if (max_cluster < 2) max_cluster = 0;
-        // the whole grid in clusters: the largest size that divides the
-        // grid and whose clusters all fit on the device at once
-        grid_cluster = 0;
-        for (unsigned c : {8u, 4u, 2u}) {
-            if (grid % c) continue;
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3(grid);
-            cfg.blockDim = dim3(kThreads);
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeClusterDimension;
-            attr[0].val.clusterDim.x = c;
-            attr[0].val.clusterDim.y = 1;
-            attr[0].val.clusterDim.z = 1;
-            cfg.attrs = attr;
-            cfg.numAttrs = 1;
-            int fit = 0, fit_s = 0;
-            if (cudaOccupancyMaxActiveClusters(&fit, (const void *)k_pcg, &cfg) != cudaSuccess) {
-                cudaGetLastError();
-                continue;
-            }
-            cfg.dynamicSmemBytes = schwarz_smem;
-            if (cudaOccupancyMaxActiveClusters(&fit_s, (const void *)k_pcg_schwarz, &cfg) !=
-                cudaSuccess) {
-                cudaGetLastError();
-                continue;
-            }
-            if ((unsigned)std::min(fit, fit_s) * c >= grid) {
-                grid_cluster = c;
-                break;
-            }
-        }
     }
-    partials.reserve(15 * (size_t)grid + 4);
+    partials.reserve(6 * (size_t)grid + 4);
     barrier.reserve(4);
     result.reserve(1);
 }
@@ -1726,12 +1668,10 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     k_task_cost<<<div_up(T, 256u), 256, 0, q>>>(A, T, ws.task_cost.data());
     PPF_LAUNCH_CHECK();
     exclusive_scan(ws.task_cost.data(), ws.task_off.data(), T, ws.scan_tmp.data(), q);
-    // the whole grid (a cooperative launch, in clusters of ws.grid_cluster
-    // CTAs when asked and possible), or one cluster of ws.cluster CTAs
+    // the whole grid (a cooperative launch), or one cluster of ws.cluster CTAs
     const bool one_cluster = ws.cluster >= 2 && ws.cluster <= ws.max_cluster;
     const unsigned nb = one_cluster ? ws.cluster : ws.grid;
-    const unsigned launch_cluster =
-        one_cluster ? nb : (ws.cluster == 1 && ws.grid_cluster >= 2 ? ws.grid_cluster : 0u);
+    const unsigned launch_cluster = one_cluster ? nb : 0u;
     k_task_split<<<div_up(nb + 1, 256u), 256, 0, q>>>(A, ws.task_off.data(), nb,
                                                      ws.task_start.data());
     PPF_LAUNCH_CHECK();
@@ -1774,27 +1714,14 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
         cfg.blockDim = dim3(ws.threads);
         cfg.dynamicSmemBytes = dyn_smem;
         cfg.stream = q;
-        cudaLaunchAttribute attr[2];
+        cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = launch_cluster;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
-        attr[1].id = cudaLaunchAttributeCooperative;
-        attr[1].val.cooperative = 1;
         cfg.attrs = attr;
-        cfg.numAttrs = one_cluster ? 1 : 2;
-        const cudaError_t e = cudaLaunchKernelExC(&cfg, kernel, args);
-        if (e != cudaSuccess && !one_cluster) {
-            // a cooperative launch in clusters the device refuses: the whole
-            // grid without clusters from now on
-            cudaGetLastError();
-            ws.grid_cluster = 0;
-            g.cluster = 0;
-            PPF_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(nb), dim3(ws.threads), args,
-                                                 dyn_smem, q));
-        } else {
-            PPF_CUDA(e);
-        }
+        cfg.numAttrs = 1;
+        PPF_CUDA(cudaLaunchKernelExC(&cfg, kernel, args));
     }
     ++g_kernel_launches;
 }

@@ -143,11 +143,9 @@ struct PcgWorkspace {
     DevBuf<PcgResult> result;
     unsigned grid = 0, threads = 0;
     // 0: each solve runs on the whole grid (one block per SM, grid-wide
-    // barriers through L2); 1: on the whole grid in clusters of grid_cluster
-    // CTAs (one arrival per cluster at the grid barrier; as 0 when
-    // grid_cluster is 0); 2 to max_cluster: on one thread-block cluster of
+    // barriers through L2); 2 to max_cluster: on one thread-block cluster of
     // that many CTAs, whose hardware barrier stands for the grid barrier
-    unsigned cluster = 0, max_cluster = 0, grid_cluster = 0;
+    unsigned cluster = 0, max_cluster = 0;
     void reserve(unsigned n);
 };
 

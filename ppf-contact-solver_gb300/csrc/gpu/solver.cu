@@ -1725,10 +1725,8 @@ Tuning Solver::autotune() {
         };
         float best = 1e30f;
         unsigned char choice = 0;
-        for (unsigned c : {0u, pcg_.grid_cluster >= 2 ? 1u : 0u, pcg_.max_cluster,
-                           pcg_.max_cluster / 2}) {
-            if (c == 1 && pcg_.grid_cluster < 2) continue;
-            if (c >= 2 && c > pcg_.max_cluster) continue;
+        for (unsigned c : {0u, pcg_.max_cluster, pcg_.max_cluster / 2}) {
+            if (c == 1) continue;
             pcg_.cluster = c;
             const float t = time(solve);
             if (t < best) {
@@ -1751,8 +1749,7 @@ bool Solver::set_pcg_team(int ctas) {
     if (ctas < 0) {
         pcg_team_auto_ = true;
         tune_.pcg_cluster = auto_pcg_team();
-    } else if (ctas == 0 || (ctas == 1 && pcg_.grid_cluster >= 2) ||
-               (ctas >= 2 && (unsigned)ctas <= pcg_.max_cluster)) {
+    } else if (ctas == 0 || (ctas >= 2 && (unsigned)ctas <= pcg_.max_cluster)) {
         pcg_team_auto_ = false;
         tune_.pcg_cluster = (unsigned char)ctas;
     } else {

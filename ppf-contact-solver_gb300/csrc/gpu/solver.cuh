@@ -99,9 +99,9 @@ class Solver {
     // the traversal leaf-test forms (the PCG team is kept)
     void set_tuning(const Tuning &t);
     // The PCG's team: -1 automatic (one cluster up to kClusterPcgRows
-    // vertices, else the whole grid), 0 the whole grid, 1 the whole grid in
-    // clusters, 2 to the largest cluster the device runs: one cluster of
-    // that many CTAs. False for a form the device cannot run.
+    // vertices, else the whole grid), 0 the whole grid, 2 to the largest
+    // cluster the device runs: one cluster of that many CTAs. False for a
+    // size the device cannot run.
     bool set_pcg_team(int ctas);
     unsigned pcg_team() const { return tune_.pcg_cluster; }
     // Caps the pair lists at pair_cap entries each and a capacity-sized

@@ -1,11 +1,10 @@
-"""The PCG's teams: the whole grid, the whole grid in clusters, one cluster.
+"""The PCG on one thread-block cluster against the whole grid.
 
 Each solve is one persistent launch: over the whole grid (grid barriers
-through L2), over the whole grid in clusters (one arrival per cluster at the
-grid barrier) or as one cluster of up to 16 CTAs (the cluster's hardware
+through L2) or as one cluster of up to 16 CTAs (the cluster's hardware
 barrier). The recurrence is the same; only the fold of the per-block
-partial sums differs, so the forms stop within a few iterations of each
-other and solve the system to the same tolerance.
+partial sums differs (16 against 152 partials), so the two stop within a
+few iterations of each other and solve the system to the same tolerance.
 """
 import ctypes as C
 
@@ -80,9 +79,7 @@ def test_cluster_and_grid_solve_the_same_system(lib):
         big //= 2
     assert big >= 2
     xs, its = [], []
-    for team in (0, 1, big, 2):
-        if team == 1 and lib.ppf_set_pcg_team(1) != 0:
-            continue  # the device runs no cooperative launch in clusters
+    for team in (0, big, 2):
         assert lib.ppf_set_pcg_team(team) == 0
         x = np.zeros_like(b)
         st = lib.ppf_debug_pcg(b, x, 10000, C.byref(it), C.byref(rr))
