@@ -348,6 +348,28 @@ unsigned long long ppf_graph_launches(void);
  * replays, iterations repeated after an overrun. */
 void ppf_set_iteration_graph(int enable);
 void ppf_iteration_graph_stats(unsigned long long *out);
+/* ---- many scenes stepped together -------------------------------------------
+ * No counterpart in the reference, whose backend holds one scene per process.
+ * ppf_multi_create initializes one solver per scene (its own stream, device
+ * buffers and Newton-iteration graph; datasets[i] and params[i] stay owned by
+ * the caller and must outlive the handle), `threads` host threads at a time.
+ * ppf_multi_advance steps every scene by one time step (advance()), the
+ * scenes taken by the host threads as they come free, so their launches
+ * overlap on the device; results may be NULL. A scene up to 16,384 vertices
+ * solves its PCG on one cluster sized to it (2 to 16 CTAs). The others
+ * mirror update_constraint, fetch and ppf_step_stats for scene i. Each
+ * returns 0, or -1 on a fatal error (ppf_fatal_code / ppf_fatal_detail; the
+ * handle of a failed create is NULL). The single-scene entry points keep
+ * their own solver. */
+typedef struct PpfMulti PpfMulti;
+PpfMulti *ppf_multi_create(unsigned count, PpfDataSet *const *datasets,
+                           PpfParamSet *const *params, unsigned threads);
+int ppf_multi_advance(PpfMulti *m, PpfStepResult *results);
+int ppf_multi_update_constraint(PpfMulti *m, unsigned i, const PpfConstraint *constraint);
+int ppf_multi_fetch(PpfMulti *m, unsigned i);
+int ppf_multi_step_stats(PpfMulti *m, unsigned i, PpfStepStats *out);
+int ppf_multi_pcg_team(PpfMulti *m, unsigned i);
+void ppf_multi_destroy(PpfMulti *m);
 /* Debug: caps the pair lists at pair_cap entries each and the iteration
  * graph's contact-block capacity at block_cap (0 leaves one as it is), to
  * exercise the overrun-and-repeat path. The capacities grow again as counts

@@ -6,6 +6,7 @@
 #include "learned.cuh"
 #include "schwarz.cuh"
 #include "solver.cuh"
+#include "stats.cuh"
 
 #include <cmath>
 #include <cstdio>
@@ -245,8 +246,13 @@ void set_log_path(const char *data_dir) {
 }
 
 // ---- extensions -------------------------------------------------------------
-void ppf_step_stats(PpfStepStats *out) {
-    const ppf::gpu::StepStats &s = solver_instance().stats();
+void ppf_step_stats(PpfStepStats *out) { ppf::gpu::fill_step_stats(solver_instance(), out); }
+}
+
+namespace ppf {
+namespace gpu {
+void fill_step_stats(const Solver &solver, PpfStepStats *out) {
+    const ppf::gpu::StepStats &s = solver.stats();
     std::memset(out, 0, sizeof(*out));
     out->newton_iters = s.newton_iters;
     out->pcg_iters_total = s.pcg_iters_total;
@@ -262,9 +268,9 @@ void ppf_step_stats(PpfStepStats *out) {
         out->toi[i] = i < s.toi.size() ? s.toi[i] : 0.0f;
         out->dyn_blocks[i] = i < s.dyn_blocks.size() ? s.dyn_blocks[i] : 0u;
     }
-    out->fixed_blocks = solver_instance().fixed_blocks();
-    out->vertices = solver_instance().vertices();
-    out->precond_kind = (unsigned)solver_instance().preconditioner();
+    out->fixed_blocks = solver.fixed_blocks();
+    out->vertices = solver.vertices();
+    out->precond_kind = (unsigned)solver.preconditioner();
     out->fallbacks = s.fallbacks;
     out->factor_iters_total = s.factor_iters_total;
     out->last_pcg_state = s.last_state;
@@ -272,6 +278,10 @@ void ppf_step_stats(PpfStepStats *out) {
     out->last_pcg_resid = s.last_resid;
     out->last_break_val = s.last_break_val;
 }
+} // namespace gpu
+} // namespace ppf
+
+extern "C" {
 
 unsigned ppf_schwarz_aggregate(unsigned n, const unsigned *off, const unsigned *col,
                                const float *wgt, unsigned kmax, unsigned *agg) {

@@ -645,7 +645,7 @@ cudaError_t launch_teams(const BatchArgs &g, unsigned systems, unsigned ctas, cu
     if (!systems) return cudaSuccess;
     if (ctas == 1) {
         k_batch_pcg<false><<<systems, kBT, 0, q>>>(g);
-        ++g_kernel_launches;
+        count_launches();
         return cudaGetLastError();
     }
     static bool non_portable = false;
@@ -666,7 +666,7 @@ cudaError_t launch_teams(const BatchArgs &g, unsigned systems, unsigned ctas, cu
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    ++g_kernel_launches;
+    count_launches();
     return cudaLaunchKernelEx(&cfg, k_batch_pcg<true>, g);
 }
 

@@ -22,10 +22,11 @@ void set_fatal(unsigned char code, const char *detail) {
 
 namespace gpu {
 
-unsigned long long g_kernel_launches = 0;
-unsigned long long g_h2d_bytes = 0, g_d2h_bytes = 0;
-unsigned long long g_buffer_epoch = 0;
-bool g_capturing = false;
+std::atomic<unsigned long long> g_kernel_launches{0};
+thread_local unsigned long long t_kernel_launches = 0;
+std::atomic<unsigned long long> g_h2d_bytes{0}, g_d2h_bytes{0};
+std::atomic<unsigned long long> g_buffer_epoch{0};
+thread_local bool g_capturing = false;
 
 void buffer_grow_during_capture() {
     throw FatalError(4, "a device buffer had to grow while a Newton iteration was being captured");

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <atomic>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -31,24 +33,36 @@ enum StatusBits : unsigned {
 
 void check_cuda(cudaError_t err, const char *what, const char *file, int line);
 // Kernels launched by this library since it was loaded (every launch site
-// ends in PPF_LAUNCH_CHECK or counts itself).
-extern unsigned long long g_kernel_launches;
+// ends in PPF_LAUNCH_CHECK or counts itself with count_launches), in all
+// host threads, and by the calling thread alone (what a stream capture on
+// that thread recorded).
+extern std::atomic<unsigned long long> g_kernel_launches;
+extern thread_local unsigned long long t_kernel_launches;
+inline void count_launches(unsigned long long k = 1) {
+    g_kernel_launches += k;
+    t_kernel_launches += k;
+}
+// A capture's launches run when its graph is replayed, not when captured.
+inline void uncount_launches(unsigned long long k) {
+    g_kernel_launches -= k;
+    t_kernel_launches -= k;
+}
 // Bytes the library has copied host -> device and device -> host since it was
 // loaded, counted at the copies of the per-step path (uploads, status reads,
 // contact-layout totals, intersection records, fetch).
-extern unsigned long long g_h2d_bytes, g_d2h_bytes;
+extern std::atomic<unsigned long long> g_h2d_bytes, g_d2h_bytes;
 // Bumped whenever a DevBuf is allocated anew or released: a captured CUDA
 // graph holds raw device pointers, so it is valid only while this count is
 // the one it was captured under.
-extern unsigned long long g_buffer_epoch;
-// Set while the solver's stream is being captured into a graph; a DevBuf that
-// would have to grow then reports a host error instead of allocating (an
-// allocation would end the capture).
-extern bool g_capturing;
+extern std::atomic<unsigned long long> g_buffer_epoch;
+// Set while this host thread captures a solver's stream into a graph; a
+// DevBuf that would have to grow then reports a host error instead of
+// allocating (an allocation would end the capture).
+extern thread_local bool g_capturing;
 void buffer_grow_during_capture();
 #define PPF_CUDA(x) ::ppf::gpu::check_cuda((x), #x, __FILE__, __LINE__)
 #define PPF_LAUNCH_CHECK()                                                              \
-    (++::ppf::gpu::g_kernel_launches,                                                   \
+    (::ppf::gpu::count_launches(),                                                      \
      ::ppf::gpu::check_cuda(cudaGetLastError(), "kernel launch", __FILE__, __LINE__))
 
 constexpr unsigned kNumSMs = 152; // GB300: 2 dies x 76 SMs
@@ -90,6 +104,10 @@ __device__ __forceinline__ void atomic_add3(float *p, const Vec3 &v) {
 template <class T> struct DevBuf {
     T *ptr = nullptr;
     size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
     void reserve(size_t n) {
         if (n <= cap) return;
         if (g_capturing) buffer_grow_during_capture();

@@ -1723,7 +1723,7 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
         cfg.numAttrs = 1;
         PPF_CUDA(cudaLaunchKernelExC(&cfg, kernel, args));
     }
-    ++g_kernel_launches;
+    count_launches();
 }
 
 } // namespace gpu

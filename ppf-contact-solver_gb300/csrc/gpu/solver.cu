@@ -1092,7 +1092,7 @@ void Solver::iteration_graph(float dt) {
     IterKey key = iteration_key();
     if (it_graph_ && memcmp(&key, &it_key_, sizeof(IterKey)) == 0) {
         PPF_CUDA(cudaGraphLaunch(it_graph_, q_));
-        g_kernel_launches += it_launches_;
+        count_launches(it_launches_);
         ++graph_stats_.replays;
         return;
     }
@@ -1108,7 +1108,7 @@ void Solver::iteration_graph(float dt) {
         return;
     }
     cudaGraph_t graph = nullptr;
-    const unsigned long long l0 = g_kernel_launches;
+    const unsigned long long l0 = t_kernel_launches;
     PPF_CUDA(cudaStreamBeginCapture(q_, cudaStreamCaptureModeThreadLocal));
     g_capturing = true;
     try {
@@ -1122,14 +1122,14 @@ void Solver::iteration_graph(float dt) {
     }
     g_capturing = false;
     PPF_CUDA(cudaStreamEndCapture(q_, &graph));
-    it_launches_ = (unsigned)(g_kernel_launches - l0);
-    g_kernel_launches = l0;
+    it_launches_ = (unsigned)(t_kernel_launches - l0);
+    uncount_launches(it_launches_);
     PPF_CUDA(cudaGraphInstantiate(&it_graph_, graph, 0ull));
     PPF_CUDA(cudaGraphDestroy(graph));
     it_key_ = key;
     ++graph_stats_.captures;
     PPF_CUDA(cudaGraphLaunch(it_graph_, q_));
-    g_kernel_launches += it_launches_;
+    count_launches(it_launches_);
     ++graph_stats_.replays;
 }
 
@@ -1174,7 +1174,7 @@ void Solver::line_search_stage() {
             ls_graph_ = nullptr;
         }
         cudaGraph_t graph = nullptr;
-        const unsigned long long l0 = g_kernel_launches;
+        const unsigned long long l0 = t_kernel_launches;
         PPF_CUDA(cudaStreamBeginCapture(q_, cudaStreamCaptureModeThreadLocal));
         try {
             enqueue_line_search();
@@ -1185,8 +1185,8 @@ void Solver::line_search_stage() {
             throw;
         }
         PPF_CUDA(cudaStreamEndCapture(q_, &graph));
-        ls_launches_ = (unsigned)(g_kernel_launches - l0);
-        g_kernel_launches = l0;
+        ls_launches_ = (unsigned)(t_kernel_launches - l0);
+        uncount_launches(ls_launches_);
         PPF_CUDA(cudaGraphInstantiate(&ls_graph_, graph, 0ull));
         PPF_CUDA(cudaGraphDestroy(graph));
         ls_key_ = key;
@@ -1195,7 +1195,7 @@ void Solver::line_search_stage() {
         ls_ccd_eps_ = param->ccd_eps;
     }
     PPF_CUDA(cudaGraphLaunch(ls_graph_, q_));
-    g_kernel_launches += ls_launches_;
+    count_launches(ls_launches_);
     ++ls_replays_;
 }
 
@@ -1801,6 +1801,16 @@ void Solver::debug_schwarz(unsigned *sizes, std::vector<unsigned> &agg,
         PPF_CUDA(cudaMemcpy(agg.data(), S.agg.data(), agg.size() * 4, cudaMemcpyDeviceToHost));
     if (!dom.empty())
         PPF_CUDA(cudaMemcpy(dom.data(), S.dom.data(), dom.size() * 4, cudaMemcpyDeviceToHost));
+}
+
+Solver::~Solver() {
+    if (q_) cudaStreamSynchronize(q_);
+    if (it_graph_) cudaGraphExecDestroy(it_graph_);
+    if (ls_graph_) cudaGraphExecDestroy(ls_graph_);
+    for (cudaEvent_t e : {ev0_, ev1_, evs0_, evs1_})
+        if (e) cudaEventDestroy(e);
+    if (st_host_) cudaFreeHost(st_host_);
+    if (q_) cudaStreamDestroy(q_);
 }
 
 void Solver::release() {

@@ -37,6 +37,12 @@ struct StepStats {
 
 class Solver {
   public:
+    Solver() = default;
+    Solver(const Solver &) = delete;
+    Solver &operator=(const Solver &) = delete;
+    // its stream, graphs, events and pinned status (device buffers free
+    // themselves)
+    ~Solver();
     bool initialize(PpfDataSet *ds, PpfParamSet *param);
     PpfStepResult advance();
     void fetch();
