@@ -1,0 +1,65 @@
+"""Many scenes stepped together (ppf_multi_*): each scene's trajectory is
+the one the same scene takes stepped alone, up to the order of the float
+atomics in the assembly; every scene gets the PCG team its size asks for."""
+import numpy as np
+import pytest
+
+from ppf_gb300 import scenes
+from ppf_gb300.multi import MultiSession
+from ppf_gb300.session import Session
+
+pytestmark = pytest.mark.gpu
+
+DROPS = scenes.uneven_drops(8, seed=3)
+
+
+def _build(p):
+    side, height, collider, size = p
+    sc, _ = scenes.cloth_drop(side, height, collider, size)
+    return sc
+
+
+def test_multi_matches_scenes_stepped_alone(product_lib):
+    steps = 12
+    alone = []
+    for p in DROPS:
+        sc = _build(p)
+        s = Session(sc)
+        for _ in range(steps):
+            assert s.step(fetch=False).success()
+        s.step()
+        alone.append(s.positions().copy())
+        del s, sc
+    built = [_build(p) for p in DROPS]
+    m = MultiSession(built, threads=4)
+    for k in range(steps + 1):
+        res = m.step()
+        assert all(r.success() for r in res), k
+    for i, p in enumerate(DROPS):
+        x = m.positions(i)
+        assert np.abs(x - alone[i]).max() <= 1e-5 * np.abs(alone[i]).max(), (i, p)
+        st = m.stats(i)
+        assert st.newton_iters >= 1 and st.vertices == built[i].vertex_count
+        n = built[i].vertex_count
+        want = 2 if n <= 2048 else 4 if n <= 4096 else 8 if n <= 8192 else 16
+        assert m.pcg_team(i) == want, (n, m.pcg_team(i))
+    m.close()
+
+
+def test_multi_rejects_an_intersecting_scene(product_lib):
+    """A scene that starts self-intersecting fails its create; the handle is
+    not made and the fatal detail names the scene."""
+    from ppf_gb300 import meshes
+
+    good = _build(DROPS[0])
+    v, f = meshes.grid(8, 8, 1.0, 1.0)
+    v2 = v.copy()
+    v2[:, 1] = 0.0
+    v3 = v.copy()
+    v3[:, [0, 1, 2]] = v3[:, [1, 0, 2]]  # a vertical sheet through the first
+    sc = scenes.Scene()
+    sc.add_shell(np.concatenate([v2, v3]), np.concatenate([f, f + len(v)]),
+                 scenes.cloth_material())
+    bad, _ = sc.build(scenes._param(0.01)), None
+    with pytest.raises(Exception):
+        MultiSession([good, bad], threads=2)
