@@ -27,6 +27,9 @@ advance()), with PCG ms-to-tolerance (relative L1 residual 1e-3) per solve.
   16-96, sphere or box colliders). Their Newton systems are solved in one
   launch per autotuned team size, against one launch per system
   (ppf_gb300.batch).
+* batched_steps: the same drops stepped whole for --batch-steps time steps
+  from t = 0, one solver per scene, overlapped by host threads
+  (ppf_gb300.multi), against one scene after another on the first steps.
 * N > 1 (torchrun): replicas only. Each rank steps its own copy of the
   scene (seed = rank); value = Newton iterations of all ranks / max time.
 """
@@ -387,6 +390,11 @@ def run_ours(args, rank, local_rank, world):
         from ppf_gb300 import batch
 
         out["batched_pcg"] = batch.run_bench(args.batch_count, seed=0, reps=3)
+        # the same drops stepped whole (every stage), together: one solver
+        # and iteration graph per scene, host threads overlapping them
+        from ppf_gb300 import multi
+
+        out["batched_steps"] = multi.run_bench(args.batch_count, steps=args.batch_steps, seed=0)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"], first_o = cpu_baseline(sc, curr0, prev0, param0,
                                                     CPU_SAMPLE_SECONDS)
@@ -605,6 +613,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precond-steps", type=int, default=24,
                     help="time steps of the preconditioner comparison (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=100,
+                    help="time steps of the batched drops stepped together")
     ap.add_argument("--batch-count", type=int, default=256,
                     help="uneven drops of the batched-PCG comparison (0: skip)")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="stacked_sheets",

@@ -83,3 +83,72 @@ class MultiSession:
             self.close()
         except Exception:
             pass
+
+
+def run_bench(count: int = 256, steps: int = 100, seed: int = 0, threads: int = 16,
+              compare_steps: int = 10) -> dict:
+    """The uneven drops (scenes.uneven_drops) stepped together for `steps`
+    time steps from t = 0, and the first `compare_steps` of them also one
+    scene after another through the single-scene solver; returns the
+    figures (host wall clock around the steps; scene construction and
+    initialize outside it)."""
+    import time
+
+    from . import scenes
+    from .session import Session
+
+    drops = scenes.uneven_drops(count, seed)
+
+    def build():
+        return [scenes.cloth_drop(*p)[0] for p in drops]
+
+    def together(n_steps):
+        built = build()
+        m = MultiSession(built, threads=threads)
+        newton, pcg_iters, walls = 0, np.zeros(count, np.int64), []
+        for _ in range(n_steps):
+            t0 = time.perf_counter()
+            res = m.step()
+            walls.append(time.perf_counter() - t0)
+            if not all(r.success() for r in res):
+                bad = [i for i, r in enumerate(res) if not r.success()]
+                raise SolverError(f"scenes {bad[:8]} failed a step")
+            for i in range(count):
+                st = m.stats(i)
+                newton += st.newton_iters
+                pcg_iters[i] += st.pcg_iters_total
+        teams = [m.pcg_team(i) for i in range(count)]
+        m.close()
+        return newton, float(np.sum(walls)), pcg_iters, teams
+
+    newton, wall, pcg_iters, teams = together(steps)
+    n_cmp, w_cmp, _, _ = together(compare_steps)
+    one_newton, one_wall = 0, 0.0
+    for sc in build():
+        s = Session(sc)
+        for _ in range(compare_steps):
+            t0 = time.perf_counter()
+            if not s.step(fetch=False).success():
+                raise SolverError("a drop failed a step stepped alone")
+            one_wall += time.perf_counter() - t0
+            one_newton += s.stats().newton_iters
+        del s
+    verts = [d[0] * d[0] for d in drops]
+    it = np.sort(pcg_iters)
+    return {
+        "workload": (f"{count} uneven cloth drops (sides 16-96 log-uniform, heights 0.2-1.0 m, "
+                     "sphere or box colliders; seeded), each with its own solver, stepped "
+                     f"together by {threads} host threads (ppf_multi_advance)"),
+        "scenes": count, "vertices_total": int(sum(verts)),
+        "steps": steps, "from": "t = 0",
+        "newton_iters": newton, "wall_s": round(wall, 3),
+        "newton_iters_per_s": round(newton / wall, 1),
+        "scene_steps_per_s": round(count * steps / wall, 1),
+        "pcg_iters_per_scene_median": int(it[len(it) // 2]),
+        "pcg_iters_per_scene_p90": int(it[int(0.9 * (len(it) - 1))]),
+        "pcg_teams": {str(t): teams.count(t) for t in sorted(set(teams))},
+        "first_steps": {"steps": compare_steps,
+                        "together_newton_iters_per_s": round(n_cmp / w_cmp, 1),
+                        "one_by_one_newton_iters_per_s": round(one_newton / one_wall, 1),
+                        "speedup": round((n_cmp / w_cmp) / (one_newton / one_wall), 2)},
+    }
