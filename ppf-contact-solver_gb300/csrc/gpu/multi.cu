@@ -86,7 +86,10 @@ PpfMulti *ppf_multi_create(unsigned count, PpfDataSet *const *datasets,
     std::unique_ptr<PpfMulti> m(new PpfMulti);
     m->threads = threads ? threads : 1;
     m->solvers.resize(count);
-    for (auto &s : m->solvers) s.reset(new ppf::gpu::Solver);
+    for (auto &s : m->solvers) {
+        s.reset(new ppf::gpu::Solver);
+        s->blocking_sync_ = true;
+    }
     const int rc = run_all(count, m->threads, [&](unsigned i) {
         ppf::gpu::Solver &s = *m->solvers[i];
         if (!s.initialize(datasets[i], params[i])) {

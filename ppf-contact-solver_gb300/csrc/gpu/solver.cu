@@ -805,7 +805,7 @@ bool Solver::check_intersection(const float *x) {
     unsigned cnt = 0;
     PPF_CUDA(cudaMemcpyAsync(&cnt, &st_.data()->n_isect, sizeof(unsigned),
                              cudaMemcpyDeviceToHost, q_));
-    PPF_CUDA(cudaStreamSynchronize(q_));
+    wait();
     isect_count_ = std::min(cnt, (unsigned)PPF_MAX_INTERSECTION_RECORDS);
     isect_host_.resize(isect_count_);
     if (isect_count_)
@@ -821,9 +821,24 @@ unsigned Solver::fetch_intersection_records(PpfIntersectionRecord *out, unsigned
     return c;
 }
 
+// Waits for the solver's stream: spinning (the default, lowest latency), or
+// with blocking_sync_ by an event the thread sleeps on, so that more host
+// threads than cores can each wait on their own scene.
+void Solver::wait() {
+    if (blocking_sync_) {
+        if (!ev_done_)
+            PPF_CUDA(cudaEventCreateWithFlags(&ev_done_,
+                                              cudaEventBlockingSync | cudaEventDisableTiming));
+        PPF_CUDA(cudaEventRecord(ev_done_, q_));
+        PPF_CUDA(cudaEventSynchronize(ev_done_));
+    } else {
+        PPF_CUDA(cudaStreamSynchronize(q_));
+    }
+}
+
 void Solver::read_status() {
     PPF_CUDA(cudaMemcpyAsync(st_host_, st_.data(), sizeof(IterStatus), cudaMemcpyDeviceToHost, q_));
-    PPF_CUDA(cudaStreamSynchronize(q_));
+    wait();
     g_d2h_bytes += sizeof(IterStatus);
 }
 
@@ -1250,7 +1265,7 @@ PpfStepResult Solver::advance() {
             // replayed as one CUDA graph
             line_search_stage();
         }
-        PPF_CUDA(cudaStreamSynchronize(q_));
+        wait();
         g_d2h_bytes += sizeof(IterStatus);
         const float rescale = st_host_->rescale;
         const IterStatus st = *st_host_;
@@ -1352,7 +1367,7 @@ PpfStepResult Solver::advance() {
                              cudaMemcpyDeviceToDevice, q_));
     PPF_CUDA(cudaMemcpyAsync(curr_.data(), eval_x_.data(), n3 * sizeof(float),
                              cudaMemcpyDeviceToDevice, q_));
-    PPF_CUDA(cudaStreamSynchronize(q_));
+    wait();
     result.time = param->time;
     stats_.step_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() -
                                                               t_start)
@@ -1807,7 +1822,7 @@ Solver::~Solver() {
     if (q_) cudaStreamSynchronize(q_);
     if (it_graph_) cudaGraphExecDestroy(it_graph_);
     if (ls_graph_) cudaGraphExecDestroy(ls_graph_);
-    for (cudaEvent_t e : {ev0_, ev1_, evs0_, evs1_})
+    for (cudaEvent_t e : {ev0_, ev1_, evs0_, evs1_, ev_done_})
         if (e) cudaEventDestroy(e);
     if (st_host_) cudaFreeHost(st_host_);
     if (q_) cudaStreamDestroy(q_);

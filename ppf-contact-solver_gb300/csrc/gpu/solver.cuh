@@ -140,6 +140,8 @@ class Solver {
     void enqueue_line_search();
     void line_search_stage();
     void read_status();
+    void wait();
+    cudaEvent_t ev_done_ = nullptr;
 
     unsigned n_ = 0, n_surf_ = 0, nf_ = 0, ne_ = 0, nh_ = 0, nr_ = 0, nf_shell_ = 0, nt_ = 0;
     cudaStream_t q_ = nullptr;
@@ -251,6 +253,9 @@ class Solver {
     // the whole Newton iteration as one CUDA graph (on by default; off runs
     // the sized-by-read-back assembly and the line-search graph alone)
     bool graph_enabled_ = true;
+    // waits for the stream sleep on an event instead of spinning (many
+    // solvers stepped by more host threads than cores)
+    bool blocking_sync_ = false;
   private:
     struct IterKey {
         Scene scene;
