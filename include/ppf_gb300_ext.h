@@ -314,6 +314,11 @@ int ppf_autotune(unsigned char *modes);
  * fastest. ppf_pcg_team returns the current team (0: the whole grid). */
 int ppf_set_pcg_team(int ctas);
 int ppf_pcg_team(void);
+/* The share of a PCG product phase's work, in sixteenths of its estimated
+ * cost, that is split into one contiguous range per block; the rest is a
+ * common pool taken by whichever warps finish first. 0 restores the default
+ * (12); returns -1 above 16. */
+int ppf_set_pcg_static_share(unsigned sixteenths);
 void ppf_get_tuning(unsigned char *modes);
 int ppf_set_tuning(const unsigned char *modes);
 /* The CUDA stream (cudaStream_t, as void*) every kernel of advance() runs

@@ -320,6 +320,11 @@ int ppf_set_pcg_team(int ctas) {
     }
 }
 int ppf_pcg_team(void) { return (int)solver_instance().pcg_team(); }
+int ppf_set_pcg_static_share(unsigned sixteenths) {
+    if (sixteenths > 16) return -1;
+    solver_instance().set_pcg_static_share(sixteenths);
+    return 0;
+}
 void ppf_set_iteration_graph(int enable) { solver_instance().graph_enabled_ = enable != 0; }
 void ppf_iteration_graph_stats(unsigned long long *out) {
     const auto &g = solver_instance().graph_stats_;

@@ -412,7 +412,7 @@ constexpr unsigned kNoTask = 0xFFFFFFFFu;
 // Share of the product work (in sixteenths of its cost) split statically
 // among the blocks; the rest, the last tasks in order (fixed half slices,
 // short and even), goes to whichever warps finish first.
-constexpr unsigned kStaticSixteenths = 12;
+constexpr unsigned kStaticSixteenths = 12; // the default (PcgWorkspace::static_sixteenths)
 
 // The product tasks of one phase: first the block's static range, handed to
 // its warps one at a time through a shared counter, then tasks of the common
@@ -1408,11 +1408,11 @@ __global__ void k_task_cost(PcgOperator A, unsigned bound, unsigned *cost) {
 // (b+1) Ws / nb), Ws the static share of the total cost W; start[nb] is the
 // first task of the common pool.
 __global__ void k_task_split(PcgOperator A, const unsigned *cost_off, unsigned nb,
-                             unsigned *start) {
+                             unsigned sixteenths, unsigned *start) {
     unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b > nb) return;
     const unsigned T = TaskSpace(A).total;
-    const unsigned long long W = (unsigned long long)cost_off[T] * kStaticSixteenths / 16u;
+    const unsigned long long W = (unsigned long long)cost_off[T] * sixteenths / 16u;
     const unsigned long long target = W * b / nb;
     unsigned lo = 0, hi = T; // first t with cost_off[t] >= target
     while (lo < hi) {
@@ -1672,8 +1672,9 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     const bool one_cluster = ws.cluster >= 2 && ws.cluster <= ws.max_cluster;
     const unsigned nb = one_cluster ? ws.cluster : ws.grid;
     const unsigned launch_cluster = one_cluster ? nb : 0u;
-    k_task_split<<<div_up(nb + 1, 256u), 256, 0, q>>>(A, ws.task_off.data(), nb,
-                                                     ws.task_start.data());
+    k_task_split<<<div_up(nb + 1, 256u), 256, 0, q>>>(
+        A, ws.task_off.data(), nb, ws.static_sixteenths ? ws.static_sixteenths : kStaticSixteenths,
+        ws.task_start.data());
     PPF_LAUNCH_CHECK();
     // one counter per product phase: the initial product, then one (block-
     // Jacobi) or three (factored) per iteration, plus the factored start

@@ -146,6 +146,9 @@ struct PcgWorkspace {
     // barriers through L2); 2 to max_cluster: on one thread-block cluster of
     // that many CTAs, whose hardware barrier stands for the grid barrier
     unsigned cluster = 0, max_cluster = 0;
+    // share of the product work, in sixteenths of its cost, split into the
+    // blocks' static ranges (the rest is the common pool); 0: the default 12
+    unsigned static_sixteenths = 0;
     void reserve(unsigned n);
 };
 

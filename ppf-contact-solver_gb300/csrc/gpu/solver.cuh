@@ -110,6 +110,9 @@ class Solver {
     // size the device cannot run.
     bool set_pcg_team(int ctas);
     unsigned pcg_team() const { return tune_.pcg_cluster; }
+    // the PCG's static share of the product work, in sixteenths (1 to 16;
+    // 0 the default)
+    void set_pcg_static_share(unsigned sixteenths) { pcg_.static_sixteenths = sixteenths; }
     // Caps the pair lists at pair_cap entries each and a capacity-sized
     // iteration at block_cap contact blocks (0 leaves one as it is); larger
     // counts then take the overrun-and-repeat path.
