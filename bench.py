@@ -46,6 +46,8 @@ import time
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parent
+# hardware work queues for the batched scenes' streams, before CUDA starts
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 sys.path.insert(0, str(ROOT / "ppf-contact-solver_gb300"))
 sys.path.insert(0, str(ROOT))
 

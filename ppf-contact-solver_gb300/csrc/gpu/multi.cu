@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -24,6 +25,14 @@ struct PpfMulti {
 };
 
 namespace {
+
+// A host that loads the library before it touches CUDA (the solver
+// executable, a C program) gets 32 hardware work queues, so that the scenes'
+// streams do not share queues (the CUDA default is 8); a value already in the
+// environment is kept, and a context created earlier keeps its count.
+__attribute__((constructor)) void more_work_queues() {
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
+}
 
 // f(i) for every i in [0, count) on up to `threads` host threads, each
 // taking the next index when it is free. The first error any call raised is

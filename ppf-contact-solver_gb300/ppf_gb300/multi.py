@@ -33,7 +33,7 @@ class MultiSession:
     """Built scenes stepped together: step() advances every scene by one time
     step; positions(i) and stats(i) read scene i."""
 
-    def __init__(self, scenes: list[Scene], threads: int = 16):
+    def __init__(self, scenes: list[Scene], threads: int = 32):
         if not scenes or not all(sc.built for sc in scenes):
             raise ValueError("build the scenes first")
         self.scenes = list(scenes)
@@ -85,7 +85,7 @@ class MultiSession:
             pass
 
 
-def run_bench(count: int = 256, steps: int = 100, seed: int = 0, threads: int = 16,
+def run_bench(count: int = 256, steps: int = 100, seed: int = 0, threads: int = 32,
               compare_steps: int = 10) -> dict:
     """The uneven drops (scenes.uneven_drops) stepped together for `steps`
     time steps from t = 0, and the first `compare_steps` of them also one
