@@ -361,8 +361,9 @@ void ppf_iteration_graph_stats(unsigned long long *out);
  * ppf_multi_advance steps every scene by one time step (advance()), the
  * scenes taken by the host threads as they come free, so their launches
  * overlap on the device; results may be NULL. A scene up to 16,384 vertices
- * solves its PCG on one cluster sized to it (2 to 16 CTAs). The others
- * mirror update_constraint, fetch and ppf_step_stats for scene i. Each
+ * solves its PCG on one cluster sized to it (2 to 16 CTAs; set per scene with
+ * ppf_multi_set_pcg_team, as ppf_set_pcg_team). The others mirror
+ * update_constraint, fetch and ppf_step_stats for scene i. Each
  * returns 0, or -1 on a fatal error (ppf_fatal_code / ppf_fatal_detail; the
  * handle of a failed create is NULL). The single-scene entry points keep
  * their own solver. */
@@ -373,6 +374,7 @@ int ppf_multi_advance(PpfMulti *m, PpfStepResult *results);
 int ppf_multi_update_constraint(PpfMulti *m, unsigned i, const PpfConstraint *constraint);
 int ppf_multi_fetch(PpfMulti *m, unsigned i);
 int ppf_multi_step_stats(PpfMulti *m, unsigned i, PpfStepStats *out);
+int ppf_multi_set_pcg_team(PpfMulti *m, unsigned i, int ctas);
 int ppf_multi_pcg_team(PpfMulti *m, unsigned i);
 void ppf_multi_destroy(PpfMulti *m);
 /* Debug: caps the pair lists at pair_cap entries each and the iteration

@@ -149,6 +149,11 @@ int ppf_multi_step_stats(PpfMulti *m, unsigned i, PpfStepStats *out) {
     return 0;
 }
 
+int ppf_multi_set_pcg_team(PpfMulti *m, unsigned i, int ctas) {
+    if (!m || i >= m->solvers.size()) return -1;
+    return m->solvers[i]->set_pcg_team(ctas) ? 0 : -1;
+}
+
 int ppf_multi_pcg_team(PpfMulti *m, unsigned i) {
     if (!m || i >= m->solvers.size()) return -1;
     return (int)m->solvers[i]->pcg_team();

@@ -26,6 +26,7 @@ def _declare(lib):
     lib.ppf_multi_fetch.argtypes = [P, C.c_uint]
     lib.ppf_multi_step_stats.argtypes = [P, C.c_uint, C.POINTER(abi.StepStats)]
     lib.ppf_multi_pcg_team.argtypes = [P, C.c_uint]
+    lib.ppf_multi_set_pcg_team.argtypes = [P, C.c_uint, C.c_int]
     lib.ppf_multi_destroy.argtypes = [P]
 
 
@@ -72,6 +73,12 @@ class MultiSession:
 
     def pcg_team(self, i: int) -> int:
         return int(self.lib.ppf_multi_pcg_team(self.h, int(i)))
+
+    def set_pcg_team(self, i: int, ctas: int) -> None:
+        """As ppf_set_pcg_team for scene i (-1 automatic, 0 the whole grid,
+        2 to 16 one cluster)."""
+        if self.lib.ppf_multi_set_pcg_team(self.h, int(i), int(ctas)) != 0:
+            raise ValueError(f"PCG team {ctas} is not available")
 
     def close(self) -> None:
         if self.h:
