@@ -221,9 +221,15 @@ def run_ours(args, rank, local_rank, world):
     # the project's autotuner picks each traversal kernel's leaf-test form on
     # the warmed-up state (outside the timed region)
     tune_modes = (C.c_ubyte * 6)()
-    lib.ppf_autotune.argtypes = [C.POINTER(C.c_ubyte)]
-    if lib.ppf_autotune(tune_modes) != 0:
-        raise RuntimeError("autotune failed")
+    if args.no_autotune:
+        # the library's defaults (profiling runs: under a profiler the
+        # autotuner's timings say nothing about the real choice)
+        lib.ppf_get_tuning.argtypes = [C.POINTER(C.c_ubyte)]
+        lib.ppf_get_tuning(tune_modes)
+    else:
+        lib.ppf_autotune.argtypes = [C.POINTER(C.c_ubyte)]
+        if lib.ppf_autotune(tune_modes) != 0:
+            raise RuntimeError("autotune failed")
     tuning = dict(zip(("detect_vertex", "detect_edge", "ccd_vertex", "ccd_mesh_vertex",
                        "ccd_edge", "isect"),
                       ("on the spot" if m else "warp rounds" for m in tune_modes)))
@@ -613,6 +619,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the library's default traversal forms and PCG team")
     ap.add_argument("--precond-steps", type=int, default=24,
                     help="time steps of the preconditioner comparison (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=100,
