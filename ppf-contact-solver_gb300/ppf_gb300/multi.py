@@ -34,10 +34,15 @@ class MultiSession:
     """Built scenes stepped together: step() advances every scene by one time
     step; positions(i) and stats(i) read scene i."""
 
-    def __init__(self, scenes: list[Scene], threads: int = 32):
+    def __init__(self, scenes: list[Scene], threads: int = 32, pin_motions=None):
+        """`pin_motions`: None, or per scene None or the pin motion its
+        builder returned (as Session takes it)."""
         if not scenes or not all(sc.built for sc in scenes):
             raise ValueError("build the scenes first")
         self.scenes = list(scenes)
+        self.pin_motions = list(pin_motions) if pin_motions else [None] * len(self.scenes)
+        if len(self.pin_motions) != len(self.scenes):
+            raise ValueError("one pin motion (or None) per scene")
         self.lib = self.scenes[0].lib
         _declare(self.lib)
         n = len(self.scenes)
@@ -57,6 +62,15 @@ class MultiSession:
         return len(self.scenes)
 
     def step(self) -> list[abi.StepResult]:
+        for i, motion in enumerate(self.pin_motions):
+            if motion is None:
+                continue
+            sc = self.scenes[i]
+            prm = sc.param.contents
+            pos, delta = motion(float(prm.time) + prm.dt, prm.dt)
+            sc.set_pin_targets(pos, delta)
+            if self.lib.ppf_multi_update_constraint(self.h, i, sc.constraint) != 0:
+                raise SolverError(self._fatal("ppf_multi_update_constraint"))
         if self.lib.ppf_multi_advance(self.h, self.results) != 0:
             raise SolverError(self._fatal("ppf_multi_advance"))
         return list(self.results)

@@ -63,3 +63,28 @@ def test_multi_rejects_an_intersecting_scene(product_lib):
     bad, _ = sc.build(scenes._param(0.01)), None
     with pytest.raises(Exception):
         MultiSession([good, bad], threads=2)
+
+
+def test_multi_pinned_moving_scenes(product_lib):
+    """Twisted tubes (both end rings pinned and turned) stepped together with
+    their pin motions follow the same tubes stepped alone."""
+    steps = 6
+    makers = [lambda: scenes.twisted_tube(16, 24), lambda: scenes.twisted_tube(24, 32)]
+    alone = []
+    for make in makers:
+        sc, motion = make()
+        s = Session(sc, motion)
+        for _ in range(steps):
+            assert s.step(fetch=False).success()
+        s.step()
+        alone.append(s.positions().copy())
+        del s, sc
+    built = [make() for make in makers]
+    m = MultiSession([b[0] for b in built], threads=2, pin_motions=[b[1] for b in built])
+    for _ in range(steps + 1):
+        assert all(r.success() for r in m.step())
+    for i in range(len(makers)):
+        x = m.positions(i)
+        assert np.abs(x - alone[i]).max() <= 1e-5 * np.abs(alone[i]).max(), i
+    m.close()
+
