@@ -123,36 +123,42 @@ def run_bench(count: int = 256, steps: int = 100, seed: int = 0, threads: int = 
     def build():
         return [scenes.cloth_drop(*p)[0] for p in drops]
 
-    def together(n_steps):
+    def together(n_steps, failures):
         built = build()
         m = MultiSession(built, threads=threads)
         newton, pcg_iters, walls = 0, np.zeros(count, np.int64), []
-        for _ in range(n_steps):
+        for k in range(n_steps):
             t0 = time.perf_counter()
             res = m.step()
             walls.append(time.perf_counter() - t0)
-            if not all(r.success() for r in res):
-                bad = [i for i, r in enumerate(res) if not r.success()]
-                raise SolverError(f"scenes {bad[:8]} failed a step")
             for i in range(count):
                 st = m.stats(i)
                 newton += st.newton_iters
                 pcg_iters[i] += st.pcg_iters_total
+                if not res[i].success():
+                    # a failed step leaves the scene where it was (advance()
+                    # returns before it commits); it is stepped again with
+                    # the others
+                    failures.append({"scene": i, "step": k, "drop": list(drops[i]),
+                                     "result": res[i].as_dict(),
+                                     "pcg_state": int(st.last_pcg_state),
+                                     "pcg_break_cause": int(st.last_break_cause)})
         teams = [m.pcg_team(i) for i in range(count)]
         m.close()
         return newton, float(np.sum(walls)), pcg_iters, teams
 
-    newton, wall, pcg_iters, teams = together(steps)
-    n_cmp, w_cmp, _, _ = together(compare_steps)
-    one_newton, one_wall = 0, 0.0
+    failures, cmp_failures = [], []
+    newton, wall, pcg_iters, teams = together(steps, failures)
+    n_cmp, w_cmp, _, _ = together(compare_steps, cmp_failures)
+    one_newton, one_wall, one_failed = 0, 0.0, 0
     for sc in build():
         s = Session(sc)
         for _ in range(compare_steps):
             t0 = time.perf_counter()
-            if not s.step(fetch=False).success():
-                raise SolverError("a drop failed a step stepped alone")
+            ok = s.step(fetch=False).success()
             one_wall += time.perf_counter() - t0
             one_newton += s.stats().newton_iters
+            one_failed += 0 if ok else 1
         del s
     verts = [d[0] * d[0] for d in drops]
     it = np.sort(pcg_iters)
@@ -168,8 +174,10 @@ def run_bench(count: int = 256, steps: int = 100, seed: int = 0, threads: int = 
         "pcg_iters_per_scene_median": int(it[len(it) // 2]),
         "pcg_iters_per_scene_p90": int(it[int(0.9 * (len(it) - 1))]),
         "pcg_teams": {str(t): teams.count(t) for t in sorted(set(teams))},
+        "failed_scene_steps": len(failures), "failures": failures[:8],
         "first_steps": {"steps": compare_steps,
                         "together_newton_iters_per_s": round(n_cmp / w_cmp, 1),
                         "one_by_one_newton_iters_per_s": round(one_newton / one_wall, 1),
-                        "speedup": round((n_cmp / w_cmp) / (one_newton / one_wall), 2)},
+                        "speedup": round((n_cmp / w_cmp) / (one_newton / one_wall), 2),
+                        "failed_scene_steps": [len(cmp_failures), one_failed]},
     }

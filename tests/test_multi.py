@@ -1,6 +1,9 @@
 """Many scenes stepped together (ppf_multi_*): each scene's trajectory is
-the one the same scene takes stepped alone, up to the order of the float
-atomics in the assembly; every scene gets the PCG team its size asks for."""
+the one the same scene takes stepped alone with the same PCG team, up to the
+order of the float atomics in the assembly; every scene gets the PCG team
+its size asks for."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -19,12 +22,26 @@ def _build(p):
     return sc
 
 
+def _team(n):
+    """The PCG team ppf_multi_create gives a scene of n vertices."""
+    return 2 if n <= 2048 else 4 if n <= 4096 else 8 if n <= 8192 else 16 if n <= 16384 else 0
+
+
+def _alone(sc, motion=None):
+    """A session on the scene with the PCG team the multi-scene solver gives
+    it, so the two run the same reductions."""
+    s = Session(sc, motion) if motion is not None else Session(sc)
+    s.lib.ppf_set_pcg_team.argtypes = [C.c_int]
+    assert s.lib.ppf_set_pcg_team(_team(sc.vertex_count)) == 0
+    return s
+
+
 def test_multi_matches_scenes_stepped_alone(product_lib):
     steps = 12
     alone = []
     for p in DROPS:
         sc = _build(p)
-        s = Session(sc)
+        s = _alone(sc)
         for _ in range(steps):
             assert s.step(fetch=False).success()
         s.step()
@@ -40,9 +57,7 @@ def test_multi_matches_scenes_stepped_alone(product_lib):
         assert np.abs(x - alone[i]).max() <= 1e-5 * np.abs(alone[i]).max(), (i, p)
         st = m.stats(i)
         assert st.newton_iters >= 1 and st.vertices == built[i].vertex_count
-        n = built[i].vertex_count
-        want = 2 if n <= 2048 else 4 if n <= 4096 else 8 if n <= 8192 else 16
-        assert m.pcg_team(i) == want, (n, m.pcg_team(i))
+        assert m.pcg_team(i) == _team(built[i].vertex_count)
     m.close()
 
 
@@ -73,7 +88,7 @@ def test_multi_pinned_moving_scenes(product_lib):
     alone = []
     for make in makers:
         sc, motion = make()
-        s = Session(sc, motion)
+        s = _alone(sc, motion)
         for _ in range(steps):
             assert s.step(fetch=False).success()
         s.step()
