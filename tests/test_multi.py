@@ -36,17 +36,33 @@ def _alone(sc, motion=None):
     return s
 
 
-def test_multi_matches_scenes_stepped_alone(product_lib):
-    steps = 12
-    alone = []
-    for p in DROPS:
-        sc = _build(p)
-        s = _alone(sc)
+def _alone_runs(make, steps, runs=3):
+    """Positions after steps + 1 steps of `runs` sessions on the same scene,
+    each alone with the multi-scene PCG team, and their largest pairwise
+    difference: the library's own run-to-run spread (the assembly's float
+    atomics add in an order that varies from run to run)."""
+    xs = []
+    for _ in range(runs):
+        sc, motion = make()
+        s = _alone(sc, motion)
         for _ in range(steps):
             assert s.step(fetch=False).success()
         s.step()
-        alone.append(s.positions().copy())
+        xs.append(s.positions().copy())
         del s, sc
+    spread = max(np.abs(a - b).max() for i, a in enumerate(xs) for b in xs[i + 1:])
+    return xs[0], spread
+
+
+def _close(x, ref, spread):
+    # within a few times the run-to-run spread, never tighter than 1e-5
+    # relative
+    return np.abs(x - ref).max() <= max(3.0 * spread, 1e-5 * np.abs(ref).max())
+
+
+def test_multi_matches_scenes_stepped_alone(product_lib):
+    steps = 12
+    alone = [_alone_runs(lambda p=p: (_build(p), None), steps) for p in DROPS]
     built = [_build(p) for p in DROPS]
     m = MultiSession(built, threads=4)
     for k in range(steps + 1):
@@ -54,7 +70,8 @@ def test_multi_matches_scenes_stepped_alone(product_lib):
         assert all(r.success() for r in res), k
     for i, p in enumerate(DROPS):
         x = m.positions(i)
-        assert np.abs(x - alone[i]).max() <= 1e-5 * np.abs(alone[i]).max(), (i, p)
+        ref, spread = alone[i]
+        assert _close(x, ref, spread), (i, p, np.abs(x - ref).max(), spread)
         st = m.stats(i)
         assert st.newton_iters >= 1 and st.vertices == built[i].vertex_count
         assert m.pcg_team(i) == _team(built[i].vertex_count)
@@ -85,21 +102,13 @@ def test_multi_pinned_moving_scenes(product_lib):
     their pin motions follow the same tubes stepped alone."""
     steps = 6
     makers = [lambda: scenes.twisted_tube(16, 24), lambda: scenes.twisted_tube(24, 32)]
-    alone = []
-    for make in makers:
-        sc, motion = make()
-        s = _alone(sc, motion)
-        for _ in range(steps):
-            assert s.step(fetch=False).success()
-        s.step()
-        alone.append(s.positions().copy())
-        del s, sc
+    alone = [_alone_runs(make, steps) for make in makers]
     built = [make() for make in makers]
     m = MultiSession([b[0] for b in built], threads=2, pin_motions=[b[1] for b in built])
     for _ in range(steps + 1):
         assert all(r.success() for r in m.step())
     for i in range(len(makers)):
         x = m.positions(i)
-        assert np.abs(x - alone[i]).max() <= 1e-5 * np.abs(alone[i]).max(), i
+        ref, spread = alone[i]
+        assert _close(x, ref, spread), (i, np.abs(x - ref).max(), spread)
     m.close()
-
