@@ -163,18 +163,32 @@ __global__ void k_karras(const unsigned *keys, const unsigned *vals, unsigned n,
     if (t == 0) parent[self] = self;
 }
 
+// One tree's arrays for a refit.
+struct RefitTree {
+    PrimKind kind;
+    const unsigned *prims;
+    const float *margin;
+    const unsigned char *active;
+    unsigned n;
+    const uint2 *node;
+    const unsigned *parent;
+    float4 *bmin, *bmax;
+    unsigned *visit;
+    unsigned root;
+};
+
 // Leaf box of the sweep x0 -> x0 + e (x1 - x0), widened by the primitive's
 // margin (lbvh.cu:623-731), then the climb to the root: the second child to
 // arrive at a node merges both boxes (active-aware, lbvh.cu:778-823).
-__global__ void k_leaf_refit(PrimKind kind, const unsigned *prims,
-                             const float *margin, const unsigned char *active,
-                             const float *x0, const float *x1, float e,
-                             unsigned n, const uint2 *node,
-                             const unsigned *parent, float4 *bmin, float4 *bmax,
-                             unsigned *visit, unsigned root,
-                             unsigned *status) {
-    unsigned leaf = blockIdx.x * blockDim.x + threadIdx.x;
-    if (leaf >= n) return;
+__device__ void refit_leaf(const RefitTree &t, unsigned leaf, const float *x0, const float *x1,
+                           float e, unsigned *status) {
+    const PrimKind kind = t.kind;
+    const unsigned *prims = t.prims;
+    const unsigned n = t.n, root = t.root;
+    const uint2 *node = t.node;
+    const unsigned *parent = t.parent;
+    float4 *bmin = t.bmin, *bmax = t.bmax;
+    unsigned *visit = t.visit;
     unsigned prim = node[leaf].x - 1u;
     unsigned v[3];
     int nv;
@@ -191,7 +205,7 @@ __global__ void k_leaf_refit(PrimKind kind, const unsigned *prims,
         nv = 1;
         v[0] = prims ? prims[prim] : prim;
     }
-    float mg = margin[prim];
+    float mg = t.margin[prim];
     float lo[3], hi[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -208,7 +222,7 @@ __global__ void k_leaf_refit(PrimKind kind, const unsigned *prims,
         lo[d] = fminf(a0, a1) - mg;
         hi[d] = fmaxf(b0, b1) + mg;
     }
-    float act = (active && !active[prim]) ? 0.0f : 1.0f;
+    float act = (t.active && !t.active[prim]) ? 0.0f : 1.0f;
     bmin[leaf] = make_float4(lo[0], lo[1], lo[2], act);
     bmax[leaf] = make_float4(hi[0], hi[1], hi[2], 0.0f);
 
@@ -251,6 +265,26 @@ __global__ void k_leaf_refit(PrimKind kind, const unsigned *prims,
             atomicOr(status, STATUS_REFIT_CYCLE);
             return;
         }
+    }
+}
+
+// Up to three trees refit in one launch: thread t takes leaf t of the first
+// tree, then the second's, then the third's, so the climbs of all three run
+// together instead of one launch after another.
+struct RefitTrees {
+    RefitTree tree[3];
+    unsigned count;
+};
+
+__global__ void k_leaf_refit(RefitTrees ts, const float *x0, const float *x1, float e,
+                             unsigned *status) {
+    unsigned leaf = blockIdx.x * blockDim.x + threadIdx.x;
+    for (unsigned k = 0; k < ts.count; ++k) {
+        if (leaf < ts.tree[k].n) {
+            refit_leaf(ts.tree[k], leaf, x0, x1, e, status);
+            return;
+        }
+        leaf -= ts.tree[k].n;
     }
 }
 
@@ -317,7 +351,7 @@ void Lbvh::release() {
 
 void lbvh_build(Lbvh &bvh, const PrimSet &ps, const float *x_tree,
                 const float *x0, const float *x1, float extrapolate,
-                RadixSortWorkspace &ws, unsigned *d_status, cudaStream_t s) {
+                RadixSortWorkspace &ws, unsigned *d_status, cudaStream_t s, bool refit) {
     unsigned n = ps.count;
     bvh.reserve(n);
     bvh.n = n;
@@ -350,17 +384,34 @@ void lbvh_build(Lbvh &bvh, const PrimSet &ps, const float *x_tree,
                                                              bvh.link.data(), d_status);
         PPF_LAUNCH_CHECK();
     }
-    lbvh_refit(bvh, ps, x0, x1, extrapolate, d_status, s);
+    if (refit) lbvh_refit(bvh, ps, x0, x1, extrapolate, d_status, s);
 }
+
+namespace {
+RefitTree refit_tree(Lbvh &bvh, const PrimSet &ps) {
+    return RefitTree{ps.kind,           ps.prims,          ps.margin,         ps.active,
+                     bvh.n,             bvh.node.data(),   bvh.parent.data(), bvh.bmin.data(),
+                     bvh.bmax.data(),   bvh.visit.data(),  bvh.root};
+}
+} // namespace
 
 void lbvh_refit(Lbvh &bvh, const PrimSet &ps, const float *x0, const float *x1,
                 float extrapolate, unsigned *d_status, cudaStream_t s) {
-    unsigned n = bvh.n;
-    if (n == 0) return;
-    k_leaf_refit<<<div_up(n, kBlock), kBlock, 0, s>>>(
-        ps.kind, ps.prims, ps.margin, ps.active, x0, x1, extrapolate, n,
-        bvh.node.data(), bvh.parent.data(), bvh.bmin.data(), bvh.bmax.data(),
-        bvh.visit.data(), bvh.root, d_status);
+    Lbvh *trees[1] = {&bvh};
+    lbvh_refit_many(trees, &ps, 1, x0, x1, extrapolate, d_status, s);
+}
+
+void lbvh_refit_many(Lbvh *const *trees, const PrimSet *ps, unsigned count, const float *x0,
+                     const float *x1, float extrapolate, unsigned *d_status, cudaStream_t s) {
+    RefitTrees ts{};
+    unsigned total = 0;
+    for (unsigned k = 0; k < count && k < 3; ++k) {
+        if (trees[k]->n == 0) continue;
+        ts.tree[ts.count++] = refit_tree(*trees[k], ps[k]);
+        total += trees[k]->n;
+    }
+    if (total == 0) return;
+    k_leaf_refit<<<div_up(total, kBlock), kBlock, 0, s>>>(ts, x0, x1, extrapolate, d_status);
     PPF_LAUNCH_CHECK();
 }
 

@@ -57,11 +57,15 @@ struct PrimSet {
 // -> leaf boxes of the sweep x0 -> x0 + extrapolate (x1 - x0) -> refit.
 void lbvh_build(Lbvh &bvh, const PrimSet &ps, const float *x_tree,
                 const float *x0, const float *x1, float extrapolate,
-                RadixSortWorkspace &ws, unsigned *d_status, cudaStream_t s);
+                RadixSortWorkspace &ws, unsigned *d_status, cudaStream_t s,
+                bool refit = true);
 
 // Box-only update on the existing topology (lbvh.cu:1032-1097).
 void lbvh_refit(Lbvh &bvh, const PrimSet &ps, const float *x0, const float *x1,
                 float extrapolate, unsigned *d_status, cudaStream_t s);
+// Up to three trees (built over the same positions) refit in one launch.
+void lbvh_refit_many(Lbvh *const *trees, const PrimSet *ps, unsigned count, const float *x0,
+                     const float *x1, float extrapolate, unsigned *d_status, cudaStream_t s);
 
 } // namespace gpu
 } // namespace ppf

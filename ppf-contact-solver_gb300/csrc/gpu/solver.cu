@@ -779,14 +779,14 @@ void Solver::build_trees(const float *x0, const float *x1, float extrap, bool re
                use_active_ ? vert_active_.data() : nullptr};
     unsigned *status = &st_.data()->status;
     if (rebuild) {
-        lbvh_build(bvh_face_, pf, x1, x0, x1, extrap, sort_ws_, status, q_);
-        lbvh_build(bvh_edge_, pe, x1, x0, x1, extrap, sort_ws_, status, q_);
-        lbvh_build(bvh_vert_, pv, x1, x0, x1, extrap, sort_ws_, status, q_);
-    } else {
-        lbvh_refit(bvh_face_, pf, x0, x1, extrap, status, q_);
-        lbvh_refit(bvh_edge_, pe, x0, x1, extrap, status, q_);
-        lbvh_refit(bvh_vert_, pv, x0, x1, extrap, status, q_);
+        lbvh_build(bvh_face_, pf, x1, x0, x1, extrap, sort_ws_, status, q_, false);
+        lbvh_build(bvh_edge_, pe, x1, x0, x1, extrap, sort_ws_, status, q_, false);
+        lbvh_build(bvh_vert_, pv, x1, x0, x1, extrap, sort_ws_, status, q_, false);
     }
+    // the three trees' boxes and climbs in one launch
+    Lbvh *trees[3] = {&bvh_face_, &bvh_edge_, &bvh_vert_};
+    const PrimSet sets[3] = {pf, pe, pv};
+    lbvh_refit_many(trees, sets, 3, x0, x1, extrap, status, q_);
 }
 
 void Solver::compute_target(float dt) {
