@@ -88,6 +88,7 @@ extern "C" {
 
 PpfMulti *ppf_multi_create(unsigned count, PpfDataSet *const *datasets,
                            PpfParamSet *const *params, unsigned threads) {
+    ppf::set_fatal(0, ""); // as initialize: a new handle starts without a fatal report
     if (!count || !datasets || !params) {
         ppf::set_fatal(5, "ppf_multi_create: no scenes");
         return nullptr;

@@ -65,3 +65,25 @@ def test_ctypes_mirrors_match_headers():
         out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
     got = {k: int(v) for k, v in (line.split() for line in out.strip().splitlines())}
     assert got == expect
+
+
+def test_host_side_argument_checks(product_lib):
+    """Entry points that reject their arguments before touching the device
+    (these run without a GPU)."""
+    import ctypes as C
+
+    lib = product_lib
+    lib.ppf_multi_create.restype = C.c_void_p
+    lib.ppf_multi_create.argtypes = [C.c_uint, C.c_void_p, C.c_void_p, C.c_uint]
+    assert lib.ppf_multi_create(0, None, None, 4) is None
+    assert lib.ppf_fatal_code() != 0
+    lib.ppf_multi_advance.argtypes = [C.c_void_p, C.c_void_p]
+    assert lib.ppf_multi_advance(None, None) == -1
+    lib.ppf_multi_fetch.argtypes = [C.c_void_p, C.c_uint]
+    assert lib.ppf_multi_fetch(None, 0) == -1
+    lib.ppf_set_pcg_static_share.argtypes = [C.c_uint]
+    assert lib.ppf_set_pcg_static_share(17) == -1
+    assert lib.ppf_set_pcg_static_share(0) == 0
+    stats = (C.c_ulonglong * 4)()
+    lib.ppf_iteration_graph_stats(stats)
+    assert all(v >= 0 for v in stats)
