@@ -319,6 +319,10 @@ int ppf_pcg_team(void);
  * common pool taken by whichever warps finish first. 0 restores the default
  * (12); returns -1 above 16. */
 int ppf_set_pcg_static_share(unsigned sixteenths);
+/* Threads per CTA of a one-cluster block-Jacobi solve: 256, 512 or 1024 (0:
+ * 1024, the default); smaller CTAs let several solves share an SM. Returns
+ * -1 for another value. */
+int ppf_set_pcg_cta_threads(unsigned threads);
 void ppf_get_tuning(unsigned char *modes);
 int ppf_set_tuning(const unsigned char *modes);
 /* The CUDA stream (cudaStream_t, as void*) every kernel of advance() runs
@@ -375,6 +379,7 @@ int ppf_multi_update_constraint(PpfMulti *m, unsigned i, const PpfConstraint *co
 int ppf_multi_fetch(PpfMulti *m, unsigned i);
 int ppf_multi_step_stats(PpfMulti *m, unsigned i, PpfStepStats *out);
 int ppf_multi_set_pcg_team(PpfMulti *m, unsigned i, int ctas);
+int ppf_multi_set_pcg_cta_threads(PpfMulti *m, unsigned i, unsigned threads);
 int ppf_multi_pcg_team(PpfMulti *m, unsigned i);
 void ppf_multi_destroy(PpfMulti *m);
 /* Debug: caps the pair lists at pair_cap entries each and the iteration

@@ -320,6 +320,9 @@ int ppf_set_pcg_team(int ctas) {
     }
 }
 int ppf_pcg_team(void) { return (int)solver_instance().pcg_team(); }
+int ppf_set_pcg_cta_threads(unsigned threads) {
+    return solver_instance().set_pcg_cta_threads(threads) ? 0 : -1;
+}
 int ppf_set_pcg_static_share(unsigned sixteenths) {
     if (sixteenths > 16) return -1;
     solver_instance().set_pcg_static_share(sixteenths);

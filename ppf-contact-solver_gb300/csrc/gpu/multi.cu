@@ -155,6 +155,11 @@ int ppf_multi_set_pcg_team(PpfMulti *m, unsigned i, int ctas) {
     return m->solvers[i]->set_pcg_team(ctas) ? 0 : -1;
 }
 
+int ppf_multi_set_pcg_cta_threads(PpfMulti *m, unsigned i, unsigned threads) {
+    if (!m || i >= m->solvers.size()) return -1;
+    return m->solvers[i]->set_pcg_cta_threads(threads) ? 0 : -1;
+}
+
 int ppf_multi_pcg_team(PpfMulti *m, unsigned i) {
     if (!m || i >= m->solvers.size()) return -1;
     return (int)m->solvers[i]->pcg_team();

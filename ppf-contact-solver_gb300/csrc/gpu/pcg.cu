@@ -33,7 +33,8 @@ namespace gpu {
 
 namespace {
 
-constexpr unsigned kThreads = 1024; // one block per SM
+constexpr unsigned kThreads = 1024; // one block per SM (the largest block; a
+                                    // one-cluster solve may run smaller ones)
 constexpr unsigned kWarps = kThreads / 32;
 static_assert(kWarps == 32, "the block fold reads one partial per lane of warp 0");
 constexpr float kCurvatureSlack = 256.0f;
@@ -178,7 +179,7 @@ __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
     float x[N];
     if (w == 0) {
 #pragma unroll
-        for (int q = 0; q < N; ++q) x[q] = s_w[q][lane]; // kWarps == 32
+        for (int q = 0; q < N; ++q) x[q] = lane < (blockDim.x >> 5) ? s_w[q][lane] : 0.0f;
         for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
             for (int q = 0; q < N; ++q) x[q] += __shfl_down_sync(0xffffffffu, x[q], off);
@@ -1712,7 +1713,9 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     } else {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(nb);
-        cfg.blockDim = dim3(ws.threads);
+        cfg.blockDim = dim3(kernel == (const void *)k_pcg && ws.cluster_threads
+                                ? ws.cluster_threads
+                                : ws.threads);
         cfg.dynamicSmemBytes = dyn_smem;
         cfg.stream = q;
         cudaLaunchAttribute attr[1];

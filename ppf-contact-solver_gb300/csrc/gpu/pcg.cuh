@@ -146,6 +146,9 @@ struct PcgWorkspace {
     // barriers through L2); 2 to max_cluster: on one thread-block cluster of
     // that many CTAs, whose hardware barrier stands for the grid barrier
     unsigned cluster = 0, max_cluster = 0;
+    // threads per CTA of a one-cluster block-Jacobi solve (256, 512 or
+    // 1024; 0: 1024): smaller CTAs share an SM with other solves'
+    unsigned cluster_threads = 0;
     // share of the product work, in sixteenths of its cost, split into the
     // blocks' static ranges (the rest is the common pool); 0: the default 12
     unsigned static_sixteenths = 0;

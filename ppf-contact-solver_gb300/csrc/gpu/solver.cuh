@@ -113,6 +113,13 @@ class Solver {
     // the PCG's static share of the product work, in sixteenths (1 to 16;
     // 0 the default)
     void set_pcg_static_share(unsigned sixteenths) { pcg_.static_sixteenths = sixteenths; }
+    // threads per CTA of a one-cluster block-Jacobi solve: 256, 512 or 1024
+    // (0: 1024); false for another value
+    bool set_pcg_cta_threads(unsigned threads) {
+        if (threads != 0 && threads != 256 && threads != 512 && threads != 1024) return false;
+        pcg_.cluster_threads = threads;
+        return true;
+    }
     // Caps the pair lists at pair_cap entries each and a capacity-sized
     // iteration at block_cap contact blocks (0 leaves one as it is); larger
     // counts then take the overrun-and-repeat path.

@@ -27,6 +27,7 @@ def _declare(lib):
     lib.ppf_multi_step_stats.argtypes = [P, C.c_uint, C.POINTER(abi.StepStats)]
     lib.ppf_multi_pcg_team.argtypes = [P, C.c_uint]
     lib.ppf_multi_set_pcg_team.argtypes = [P, C.c_uint, C.c_int]
+    lib.ppf_multi_set_pcg_cta_threads.argtypes = [P, C.c_uint, C.c_uint]
     lib.ppf_multi_destroy.argtypes = [P]
 
 
@@ -93,6 +94,11 @@ class MultiSession:
         2 to 16 one cluster)."""
         if self.lib.ppf_multi_set_pcg_team(self.h, int(i), int(ctas)) != 0:
             raise ValueError(f"PCG team {ctas} is not available")
+
+    def set_pcg_cta_threads(self, i: int, threads: int) -> None:
+        """Threads per CTA of scene i's one-cluster solves (256, 512, 1024)."""
+        if self.lib.ppf_multi_set_pcg_cta_threads(self.h, int(i), int(threads)) != 0:
+            raise ValueError(f"{threads} threads per CTA are not available")
 
     def close(self) -> None:
         if self.h:

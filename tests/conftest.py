@@ -90,4 +90,5 @@ def _block_jacobi_after_each_test(request):
         _lib._PRODUCT.ppf_set_preconditioner(ctypes.c_int(0), ctypes.c_float(0.0))
         # and the default PCG team and Newton-iteration graph
         _lib._PRODUCT.ppf_set_pcg_team(ctypes.c_int(-1))
+        _lib._PRODUCT.ppf_set_pcg_cta_threads(ctypes.c_uint(0))
         _lib._PRODUCT.ppf_set_iteration_graph(ctypes.c_int(1))

@@ -88,6 +88,20 @@ def test_cluster_and_grid_solve_the_same_system(lib):
         assert np.abs(r).sum() / np.abs(b).sum() < 2e-3, team
         xs.append(x.astype(np.float64))
         its.append(it.value)
+    # one cluster of smaller CTAs (several solves can then share an SM)
+    lib.ppf_set_pcg_cta_threads.argtypes = [C.c_uint]
+    assert lib.ppf_set_pcg_cta_threads(300) == -1
+    for threads in (256, 512):
+        assert lib.ppf_set_pcg_cta_threads(threads) == 0
+        assert lib.ppf_set_pcg_team(big) == 0
+        x = np.zeros_like(b)
+        st = lib.ppf_debug_pcg(b, x, 10000, C.byref(it), C.byref(rr))
+        assert st == 0 and rr.value < 1e-3, (threads, st, rr.value)
+        r = b.astype(np.float64) - _apply(sysm, x)
+        assert np.abs(r).sum() / np.abs(b).sum() < 2e-3, threads
+        xs.append(x.astype(np.float64))
+        its.append(it.value)
+    assert lib.ppf_set_pcg_cta_threads(0) == 0
     for x in xs[1:]:
         assert np.linalg.norm(x - xs[0]) / np.linalg.norm(xs[0]) < 2e-2, its
     assert max(its) <= 1.2 * min(its) + 4, its
