@@ -365,8 +365,9 @@ void ppf_iteration_graph_stats(unsigned long long *out);
  * ppf_multi_advance steps every scene by one time step (advance()), the
  * scenes taken by the host threads as they come free, so their launches
  * overlap on the device; results may be NULL. A scene up to 16,384 vertices
- * solves its PCG on one cluster sized to it (2 to 16 CTAs; set per scene with
- * ppf_multi_set_pcg_team, as ppf_set_pcg_team). The others mirror
+ * solves its PCG on one cluster sized to it (2 to 16 CTAs of 512 threads; set
+ * per scene with ppf_multi_set_pcg_team and ppf_multi_set_pcg_cta_threads, as
+ * their single-scene forms). The others mirror
  * update_constraint, fetch and ppf_step_stats for scene i. Each
  * returns 0, or -1 on a fatal error (ppf_fatal_code / ppf_fatal_detail; the
  * handle of a failed create is NULL). The single-scene entry points keep
