@@ -28,11 +28,13 @@ def _team(n):
 
 
 def _alone(sc, motion=None):
-    """A session on the scene with the PCG team the multi-scene solver gives
-    it, so the two run the same reductions."""
+    """A session on the scene with the PCG team (and CTA size) the
+    multi-scene solver gives it, so the two run the same reductions."""
     s = Session(sc, motion) if motion is not None else Session(sc)
     s.lib.ppf_set_pcg_team.argtypes = [C.c_int]
+    s.lib.ppf_set_pcg_cta_threads.argtypes = [C.c_uint]
     assert s.lib.ppf_set_pcg_team(_team(sc.vertex_count)) == 0
+    assert s.lib.ppf_set_pcg_cta_threads(512) == 0
     return s
 
 
