@@ -28,18 +28,11 @@
 
 #include <algorithm>
 
-#include <cooperative_groups.h>
-
-namespace cg = cooperative_groups;
-
 namespace ppf {
 namespace gpu {
 
 namespace {
 
-// A one-cluster block-Jacobi solve keeps its records in shared memory when
-// each CTA holds at most this many (32 bytes each).
-constexpr unsigned kClusterRecordRows = 2048;
 constexpr unsigned kThreads = 1024; // one block per SM (the largest block; a
                                     // one-cluster solve may run smaller ones)
 constexpr unsigned kWarps = kThreads / 32;
@@ -542,64 +535,7 @@ __device__ __forceinline__ void product_task(const PcgArgs &g, const TaskSpace &
     }
 }
 
-// Where the {z, p} records of the block-Jacobi PCG live.
-//
-// GlobalRecords: one 32-byte record per vertex in global memory, gathered
-// through L2.
-struct GlobalRecords {
-    float *R;
-    __device__ __forceinline__ void store(unsigned i, const Vec3 &z, const Vec3 &p) const {
-        st_record(R, i, z, p);
-    }
-    __device__ __forceinline__ void leave() const {}
-    struct Gather {
-        const GlobalRecords &rec;
-        float beta;
-        __device__ __forceinline__ Vec3 operator()(unsigned j) const {
-            Vec3 z, p;
-            ld_record(rec.R, j, z, p);
-            return z + beta * p;
-        }
-    };
-};
-
-// ClusterRecords (a one-cluster solve of a small system): each record lives
-// in the shared memory of the CTA whose warp updates the vertex (slice sl is
-// updated by warp sl mod nwarps, the m-th slice of that warp, m = sl /
-// nwarps), and the products gather them from there through distributed
-// shared memory instead of L2. The update phase writes its own CTA's records.
-struct ClusterRecords {
-    float *smem;            // this CTA's records, 8 floats each
-    unsigned nwarps, wpc;   // warps of the launch and of one CTA
-    __device__ __forceinline__ unsigned slot(unsigned i, unsigned &cta) const {
-        const unsigned sl = i >> 5, w = sl % nwarps;
-        cta = w / wpc;
-        return ((sl / nwarps) * wpc + (w % wpc)) * 32u + (i & 31u);
-    }
-    __device__ __forceinline__ void store(unsigned i, const Vec3 &z, const Vec3 &p) const {
-        unsigned cta;
-        float4 *d = reinterpret_cast<float4 *>(smem + 8 * (size_t)slot(i, cta));
-        d[0] = make_float4(z[0], z[1], z[2], p[0]);
-        d[1] = make_float4(p[1], p[2], 0.0f, 0.0f);
-    }
-    // the others may still read this CTA's records: the cluster meets once
-    // more before any CTA leaves (every thread leaves at the same point)
-    __device__ __forceinline__ void leave() const { cluster_barrier(); }
-    struct Gather {
-        const ClusterRecords &rec;
-        float beta;
-        __device__ __forceinline__ Vec3 operator()(unsigned j) const {
-            unsigned cta;
-            const unsigned k = rec.slot(j, cta);
-            const float4 *r = reinterpret_cast<const float4 *>(
-                cg::this_cluster().map_shared_rank(rec.smem + 8 * (size_t)k, cta));
-            const float4 a = r[0], b = r[1];
-            return vec3(a.x, a.y, a.z) + beta * vec3(a.w, b.x, b.y);
-        }
-    };
-};
-
-template <class Rec> __device__ __forceinline__ void pcg_body(const PcgArgs &g, const Rec &rec) {
+__global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
     // a conditional solve that is not needed leaves everything as it is
     if (g.run_if && *g.run_if == 0u) return;
     const PcgOperator &A = g.A;
@@ -641,7 +577,7 @@ template <class Rec> __device__ __forceinline__ void pcg_body(const PcgArgs &g, 
         Vec3 ri = ldcg3(g.r, i) - row_product(g, i);
         Vec3 zi = load_inv(A.inv_diag, sl, lane) * ri;
         st3(g.r, i, ri);
-        rec.store(i, zi, Vec3::zero());
+        st_record(g.R, i, zi, Vec3::zero());
         a += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
         b += ri.dot(zi);
     }
@@ -652,7 +588,6 @@ template <class Rec> __device__ __forceinline__ void pcg_body(const PcgArgs &g, 
         if (err0 == 0.0f) {
             if (blockIdx.x == 0 && threadIdx.x == 0)
                 *g.res = PcgResult{1u, 0.0f, 0, 0, 0.0f, 0.0f, 0u};
-            rec.leave();
             return;
         }
         float beta = 0.0f;
@@ -662,7 +597,7 @@ template <class Rec> __device__ __forceinline__ void pcg_body(const PcgArgs &g, 
         for (unsigned iter = 1;; ++iter) {
             // S: A p_k with p_k = z + beta p_{k-1}
             a = b = 0.0f; // p^T A p, sum |p_i| |terms|
-            const typename Rec::Gather gp{rec, beta};
+            const GatherCombined gp{g.R, beta};
             bt.start();
             float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
             const float *const vals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
@@ -703,7 +638,7 @@ template <class Rec> __device__ __forceinline__ void pcg_body(const PcgArgs &g, 
                 Vec3 zi = load_inv(A.inv_diag, sl, lane) * ri;
                 st3(g.x, i, xi);
                 st3(g.r, i, ri);
-                rec.store(i, zi, pi);
+                st_record(g.R, i, zi, pi);
                 a += ri.dot(zi);
                 b += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
             }
@@ -721,7 +656,6 @@ template <class Rec> __device__ __forceinline__ void pcg_body(const PcgArgs &g, 
                 else if (!isfinite(reresid) || at_cap) out.state = 2;
                 if (out.state >= 0) {
                     if (blockIdx.x == 0 && threadIdx.x == 0) *g.res = out;
-                    rec.leave();
                     return;
                 }
                 if (reresid < 8.0f * g.tol) stride = 1;
@@ -732,19 +666,6 @@ template <class Rec> __device__ __forceinline__ void pcg_body(const PcgArgs &g, 
 aborted:
     if (blockIdx.x == 0 && threadIdx.x == 0)
         *g.res = PcgResult{0u, 0.0f, 2, 0, 0.0f, 0.0f, STATUS_PCG_BREAKDOWN};
-    rec.leave();
-}
-
-__global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
-    pcg_body(g, GlobalRecords{g.R});
-}
-
-// The same solve with the records in the cluster's shared memory (a
-// one-cluster launch whose CTAs hold at most kClusterRecordRows records).
-__global__ void __launch_bounds__(kThreads, 1) k_pcg_cluster(PcgArgs g) {
-    extern __shared__ float4 s_records[];
-    pcg_body(g, ClusterRecords{reinterpret_cast<float *>(s_records),
-                               (gridDim.x * blockDim.x) >> 5, blockDim.x >> 5});
 }
 
 // The factored preconditioner's two products (P = G^T G + eps D^{-1}):
@@ -1526,11 +1447,8 @@ void PcgWorkspace::reserve(unsigned n) {
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)schwarz_smem));
         max_cluster = 16;
-        PPF_CUDA(cudaFuncSetAttribute((const void *)k_pcg_cluster,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(kClusterRecordRows * 32u)));
         for (const void *kf : {(const void *)k_pcg, (const void *)k_pcg_factor,
-                               (const void *)k_pcg_schwarz, (const void *)k_pcg_cluster}) {
+                               (const void *)k_pcg_schwarz}) {
             if (cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
                 cudaSuccess) {
                 cudaGetLastError();
@@ -1540,9 +1458,7 @@ void PcgWorkspace::reserve(unsigned n) {
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(16);
             cfg.blockDim = dim3(kThreads);
-            cfg.dynamicSmemBytes = kf == (const void *)k_pcg_schwarz    ? schwarz_smem
-                                   : kf == (const void *)k_pcg_cluster ? kClusterRecordRows * 32u
-                                                                        : 0;
+            cfg.dynamicSmemBytes = kf == (const void *)k_pcg_schwarz ? schwarz_smem : 0;
             cudaLaunchAttribute attr[1];
             attr[0].id = cudaLaunchAttributeClusterDimension;
             attr[0].val.clusterDim.x = 16;
@@ -1789,25 +1705,15 @@ void launch_pcg(const PcgOperator &A, float *x, float *r, float tol, unsigned ma
     const void *kernel = A.schwarz.n_agg ? (const void *)k_pcg_schwarz
                          : A.factor.diag ? (const void *)k_pcg_factor
                                          : (const void *)k_pcg;
-    size_t dyn_smem = A.schwarz.n_agg ? (size_t)kWarps * kSchwarzWarpFloats * sizeof(float) : 0;
-    if (one_cluster && kernel == (const void *)k_pcg) {
-        // the records in the cluster's shared memory when each CTA's share fits
-        const unsigned threads = ws.cluster_threads ? ws.cluster_threads : ws.threads;
-        const unsigned wpc = threads / 32u, nwarps = nb * wpc;
-        const unsigned rows = div_up(A.fixed.n_slices, nwarps) * wpc * 32u;
-        if (rows <= kClusterRecordRows) {
-            kernel = (const void *)k_pcg_cluster;
-            dyn_smem = (size_t)rows * 32u;
-        }
-    }
+    const size_t dyn_smem =
+        A.schwarz.n_agg ? (size_t)kWarps * kSchwarzWarpFloats * sizeof(float) : 0;
     if (launch_cluster == 0) {
         PPF_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(nb), dim3(ws.threads), args, dyn_smem,
                                              q));
     } else {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(nb);
-        cfg.blockDim = dim3((kernel == (const void *)k_pcg ||
-                             kernel == (const void *)k_pcg_cluster) && ws.cluster_threads
+        cfg.blockDim = dim3(kernel == (const void *)k_pcg && ws.cluster_threads
                                 ? ws.cluster_threads
                                 : ws.threads);
         cfg.dynamicSmemBytes = dyn_smem;
