@@ -4,7 +4,7 @@ sizes, through the C ABI.
 * The 64 x 64 cloth on the r = 0.3 sphere, 60 steps (the small plain
   configuration): at every step both the GPU and the oracle advance from the
   GPU's state (lockstep), and the positions must agree within 1e-5 relative
-  to the coordinate scale, the benchmark spec's one-step bar. Every frame is
+  to the coordinate scale, the one-step parity bar. Every frame is
   intersection-free by the oracle's own check and strain-limited; Newton
   iteration counts match and PCG iteration counts agree within what the 1e-3
   relative residual lets the stopping iteration move.
