@@ -129,30 +129,19 @@ __device__ __forceinline__ void fold_partials(const float *p, unsigned n, unsign
         for (int q = 0; q < N; ++q) x[q] += __shfl_down_sync(0xffffffffu, x[q], off);
 }
 
-// Arrival of lane 0 of warp 0 at the grid barrier through L2 among `count`
-// arrivers (acquire-release), and its bounded wait. Returns 0 when the wait
-// timed out or another block latched an abort.
-__device__ __forceinline__ int grid_arrive_wait(unsigned *bar, unsigned count, unsigned *abort) {
-    int ok = 1;
-    unsigned *ctr = bar, *gen = bar + 1;
-    const unsigned g0 = ld_relaxed(gen);
-    if (atom_add_acq_rel(ctr, 1u) == count - 1) {
-        st_relaxed(ctr, 0u);
-        red_add_release(gen, 1u);
-    } else {
-        const unsigned long long t0 = global_ns();
-        for (unsigned spin = 0; ld_acquire(gen) == g0; ++spin) {
-            if ((spin & 63u) == 63u) {
-                if (ld_relaxed(abort) || global_ns() - t0 > kBarrierTimeoutNs) {
-                    atomicOr(abort, STATUS_PCG_BREAKDOWN);
-                    ok = 0;
-                    break;
-                }
+// The bounded wait for the generation word to move past g0. Returns 0 when
+// it timed out or another block latched an abort.
+__device__ __forceinline__ int grid_wait(unsigned *gen, unsigned g0, unsigned *abort) {
+    const unsigned long long t0 = global_ns();
+    for (unsigned spin = 0; ld_acquire(gen) == g0; ++spin) {
+        if ((spin & 63u) == 63u) {
+            if (ld_relaxed(abort) || global_ns() - t0 > kBarrierTimeoutNs) {
+                atomicOr(abort, STATUS_PCG_BREAKDOWN);
+                return 0;
             }
         }
     }
-    if (ok && ld_relaxed(abort)) ok = 0;
-    return ok;
+    return 1;
 }
 
 // The barrier has two forms, by `cluster` (the launch's cluster size):
@@ -162,9 +151,16 @@ __device__ __forceinline__ int grid_arrive_wait(unsigned *bar, unsigned count, u
 //              hardware): the cluster's barrier, passed by every thread,
 //              stands for the grid barrier; there is no wait to bound.
 // `part` holds 2 gridDim.x floats: the block partials.
-template <int N>
+// Loads a caller issues while its block waits at the grid barrier (none by
+// default): anything that does not depend on the sum, so its latency hides
+// behind the wait.
+struct NoPrefetch {
+    __device__ __forceinline__ void operator()() const {}
+};
+
+template <int N, class Pre = NoPrefetch>
 __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
-                         unsigned *abort, unsigned cluster) {
+                         unsigned *abort, unsigned cluster, const Pre &pre = Pre()) {
     __shared__ float s_w[N][kWarps];
     __shared__ float s_res[N];
     __shared__ int s_ok;
@@ -189,8 +185,23 @@ __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
     }
     int ok = 1;
     if (cluster == 0) {
-        if (w == 0 && lane == 0) ok = grid_arrive_wait(bar, nb, abort);
+        unsigned g0 = 0;
+        bool last = false;
+        if (w == 0 && lane == 0) {
+            g0 = ld_relaxed(bar + 1);
+            last = atom_add_acq_rel(bar, 1u) == nb - 1;
+            if (last) {
+                st_relaxed(bar, 0u);
+                red_add_release(bar + 1, 1u);
+            }
+        }
+        pre();
+        if (w == 0 && lane == 0) {
+            if (!last) ok = grid_wait(bar + 1, g0, abort);
+            if (ok && ld_relaxed(abort)) ok = 0;
+        }
     } else {
+        pre();
         cluster_barrier();
     }
     if (w == 0) {
@@ -208,10 +219,11 @@ __device__ bool grid_sum(float (&v)[N], float *part, unsigned *bar, unsigned nb,
     return s_ok != 0;
 }
 
+template <class Pre = NoPrefetch>
 __device__ bool grid_sum2(float &a, float &b, float *part, unsigned *bar, unsigned nb,
-                          unsigned *abort, unsigned cluster) {
+                          unsigned *abort, unsigned cluster, const Pre &pre = Pre()) {
     float v[2] = {a, b};
-    const bool ok = grid_sum<2>(v, part, bar, nb, abort, cluster);
+    const bool ok = grid_sum<2>(v, part, bar, nb, abort, cluster, pre);
     a = v[0];
     b = v[1];
     return ok;
@@ -459,10 +471,14 @@ struct BlockTasks {
     }
 };
 
+constexpr unsigned kNoIndex = 0xFFFFFFFEu; // row_product: look the contact row up
+
 // (A v)(i): the row's fixed part, plus its contact and overflow parts, if any.
-__device__ __forceinline__ Vec3 row_product(const PcgArgs &g, unsigned i) {
+// `c` is the row's contact position when the caller already loaded it.
+__device__ __forceinline__ Vec3 row_product(const PcgArgs &g, unsigned i,
+                                            unsigned c = kNoIndex) {
     Vec3 ap = ld4(g.Ap, i);
-    const unsigned c = __ldg(g.A.contact.index + i);
+    if (c == kNoIndex) c = __ldg(g.A.contact.index + i);
     if (c != 0xFFFFFFFFu) {
         ap += ld4(g.Ap_c, c);
         const unsigned k = __ldg(g.A.ovf.index + i);
@@ -612,7 +628,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
                                  b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] +
                                       fabsf(pi[2]) * ab[2];
                              });
-            if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster)) goto aborted;
+            // the update phase's first slice: what it reads that no other
+            // warp writes in this phase, loaded while the block waits
+            const unsigned i0 = warp * kSliceRows + lane;
+            const bool has0 = warp < n_slices && i0 < A.n;
+            Vec3 x0v = Vec3::zero(), r0v = Vec3::zero();
+            unsigned c0 = 0xFFFFFFFFu;
+            const auto pre = [&]() {
+                if (has0) {
+                    x0v = ldcg3(g.x, i0);
+                    r0v = ldcg3(g.r, i0);
+                    c0 = __ldg(A.contact.index + i0);
+                }
+            };
+            if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster, pre)) goto aborted;
             const float pAp = a, bound = kCurvatureSlack * kFloatEps * b;
             float alpha;
             if (pAp > bound) {
@@ -629,8 +658,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
                 const unsigned i = sl * kSliceRows + lane;
                 if (i >= A.n) continue;
-                Vec3 pi = ld4(g.p, i), api = row_product(g, i);
-                Vec3 xi = ldcg3(g.x, i), ri = ldcg3(g.r, i);
+                const bool first = sl == warp;
+                Vec3 pi = ld4(g.p, i), api = row_product(g, i, first ? c0 : kNoIndex);
+                Vec3 xi = first ? x0v : ldcg3(g.x, i), ri = first ? r0v : ldcg3(g.r, i);
                 for (int k = 0; k < 3; ++k) {
                     xi[k] += alpha * pi[k];
                     ri[k] = ri[k] - alpha * api[k];
