@@ -633,14 +633,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             const unsigned i0 = warp * kSliceRows + lane;
             const bool has0 = warp < n_slices && i0 < A.n;
             Vec3 x0v = Vec3::zero(), r0v = Vec3::zero();
-            Mat3 P0 = Mat3::zero();
             unsigned c0 = 0xFFFFFFFFu;
             const auto pre = [&]() {
                 if (has0) {
                     x0v = ldcg3(g.x, i0);
                     r0v = ldcg3(g.r, i0);
                     c0 = __ldg(A.contact.index + i0);
-                    P0 = load_inv(A.inv_diag, warp, lane);
                 }
             };
             if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster, pre)) goto aborted;
@@ -667,7 +665,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
                     xi[k] += alpha * pi[k];
                     ri[k] = ri[k] - alpha * api[k];
                 }
-                Vec3 zi = (first ? P0 : load_inv(A.inv_diag, sl, lane)) * ri;
+                Vec3 zi = load_inv(A.inv_diag, sl, lane) * ri;
                 st3(g.x, i, xi);
                 st3(g.r, i, ri);
                 st_record(g.R, i, zi, pi);
