@@ -440,22 +440,15 @@ struct BlockTasks {
     unsigned n_ctrs;
     unsigned phase = 0;
     unsigned *ctr = nullptr;
-    // Starts a product phase (every thread of the block calls it). With
-    // `preassigned`, warp w of the block takes task begin + w first
-    // (first()), and the shared counter hands out the tasks after those.
-    __device__ __forceinline__ void start(bool preassigned = false) {
+    // Starts a product phase (every thread of the block calls it).
+    __device__ __forceinline__ void start() {
         ctr = phase < n_ctrs ? ctrs + phase : nullptr;
         ++phase;
         if (threadIdx.x == 0) {
-            next[0] = begin + (preassigned ? blockDim.x >> 5 : 0u);
+            next[0] = begin;
             next[1] = 0u;
         }
         __syncthreads();
-    }
-    // This warp's preassigned task, or kNoTask.
-    __device__ __forceinline__ unsigned first() const {
-        const unsigned t = begin + (threadIdx.x >> 5);
-        return t < end ? t : kNoTask;
     }
     // The block's warps stop asking the pool's global counter once one of
     // them found it empty, so an empty pool costs about one atomic per block
@@ -578,26 +571,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
     const TaskSpace ts(A);
     BlockTasks bt{s_next, g.task_start[blockIdx.x], g.task_start[blockIdx.x + 1],
                   g.task_start[gridDim.x], ts.total, g.dyn_ctr, g.n_ctr};
-    // While a block waits at the barrier before a product phase, warps 1 to
-    // 31 bring their first task's column indices and blocks (its first eight
-    // slots) into L1; the operator is read-only, so the lines stay valid.
-    const auto pre_task = [&]() {
-        if ((threadIdx.x >> 5) == 0u) return; // warp 0 waits at the barrier
-        const unsigned t = bt.first();
-        if (t == kNoTask || t < ts.t1) return; // none, or an overflow row
-        const bool fixed = t >= ts.t2;
-        const SellMatrix &M = fixed ? A.fixed : A.contact.sell;
-        const unsigned u = fixed ? t - ts.t2 : t - ts.t1, sl = u >> 1;
-        const unsigned s0 = __ldg(M.slice_off + sl), s1 = __ldg(M.slice_off + sl + 1);
-        const unsigned nslot = min(s1 - s0, 8u), half = (u & 1u) * 16u;
-        for (unsigned k = lane; k < nslot * 10u; k += 32u) {
-            const unsigned slot = s0 + k / 10u, e = k % 10u;
-            const void *ptr = e == 0u ? (const void *)(M.col + (size_t)slot * kSliceRows + half)
-                                      : (const void *)(M.val + ((size_t)slot * 9 + (e - 1u)) *
-                                                                   kSliceRows + half);
-            asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
-        }
-    };
     // A x0 (slice part to Ap, overflow part to Ap_ovf) ...
     bt.start();
     {
@@ -624,7 +597,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
         a += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
         b += ri.dot(zi);
     }
-    if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster, pre_task)) goto aborted;
+    if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
     {
         const float err0 = a;
         float rz0 = b;
@@ -641,12 +614,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             // S: A p_k with p_k = z + beta p_{k-1}
             a = b = 0.0f; // p^T A p, sum |p_i| |terms|
             const GatherCombined gp{g.R, beta};
-            bt.start(true);
+            bt.start();
             float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
             const float *const vals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
-            unsigned first = bt.first();
-            if (first == kNoTask) first = bt.take(lane);
-            for (unsigned task = first; task != kNoTask; task = bt.take(lane))
+            for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
                 product_task<kAllSlots>(g, ts, vals, task, lane, gp,
                              [&](unsigned row, unsigned part, unsigned slot, const Vec3 &acc,
                                  const Vec3 &ab) {
@@ -701,7 +672,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
                 a += ri.dot(zi);
                 b += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
             }
-            if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster, pre_task)) goto aborted;
+            if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
             const float rz_new = a, err_now = b;
             beta = rz_new / rz0;
             rz0 = rz_new;
