@@ -512,10 +512,7 @@ struct TaskSpace {
 // The epilogue gets (row, A-part, |terms|) on the lanes that own a result.
 // `vals` are the value arrays the slots are read from: the operator's own
 // (fixed, contact, overflow) or a factor's parallel ones.
-// With kRowValue the lanes that own a result gather their row's own value
-// before the slots (its load in flight with theirs) and hand it to the
-// epilogue as a sixth argument.
-template <int MASK, bool kRowValue = false, class V, class G, class E>
+template <int MASK, class V, class G, class E>
 __device__ __forceinline__ void product_task(const PcgArgs &g, const TaskSpace &ts,
                                              const V *const vals[3], unsigned task,
                                              unsigned lane, const G &gather, E &&epilogue) {
@@ -526,10 +523,6 @@ __device__ __forceinline__ void product_task(const PcgArgs &g, const TaskSpace &
     const unsigned t1 = ts.t1, t2 = ts.t2;
     const unsigned par = lane >> 4;
     Vec3 acc = Vec3::zero(), ab = Vec3::zero();
-    auto finish = [&](unsigned row, unsigned part, unsigned slot, const Vec3 &rv) {
-        if constexpr (kRowValue) epilogue(row, part, slot, acc, ab, rv);
-        else epilogue(row, part, slot, acc, ab);
-    };
     if (task >= t1) {
         const bool fixed = task >= t2;
         const unsigned u = fixed ? task - t2 : task - t1;
@@ -537,30 +530,24 @@ __device__ __forceinline__ void product_task(const PcgArgs &g, const TaskSpace &
         const unsigned q = sl * kSliceRows + r;
         const SellMatrix &M = fixed ? A.fixed : A.contact.sell;
         const V *val = vals[fixed ? 0 : 1];
-        const bool owns = fixed ? q < A.n : q < ts.c_rows;
         unsigned row = 0xFFFFFFFFu;
-        if (MASK != kAllSlots || kRowValue) {
-            if (owns) row = fixed ? q : __ldg(A.contact.perm + q);
+        if (MASK != kAllSlots) {
+            if (fixed) row = q < A.n ? q : 0xFFFFFFFFu;
+            else row = q < ts.c_rows ? __ldg(A.contact.perm + q) : 0xFFFFFFFFu;
         }
-        Vec3 rv = Vec3::zero();
-        if constexpr (kRowValue) {
-            if (par == 0u && owns) rv = gather(row);
-        }
-        sell_half_row<MASK>(M, val, sl, r, par, MASK != kAllSlots ? row : 0xFFFFFFFFu, gather,
-                            acc, ab);
+        sell_half_row<MASK>(M, val, sl, r, par, row, gather, acc, ab);
         join_halves(acc, ab);
-        if (par == 0u && owns) finish(row == 0xFFFFFFFFu ? (fixed ? q : __ldg(A.contact.perm + q))
-                                                         : row,
-                                      fixed ? 0u : 1u, q, rv);
+        if (par == 0u) {
+            if (fixed) {
+                if (q < A.n) epilogue(q, 0u, q, acc, ab);
+            } else if (q < ts.c_rows) {
+                epilogue(__ldg(A.contact.perm + q), 1u, q, acc, ab);
+            }
+        }
     } else {
         const unsigned k = task;
-        Vec3 rv = Vec3::zero();
-        const unsigned orow = __ldg(A.ovf.row + k);
-        if constexpr (kRowValue) {
-            if (lane == 0u) rv = gather(orow);
-        }
         overflow_row<MASK>(A.ovf, vals[2], k, lane, gather, acc, ab);
-        if (lane == 0u) finish(orow, 2u, k, rv);
+        if (lane == 0u) epilogue(__ldg(A.ovf.row + k), 2u, k, acc, ab);
     }
 }
 
@@ -631,9 +618,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
             const float *const vals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
             for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
-                product_task<kAllSlots, true>(g, ts, vals, task, lane, gp,
+                product_task<kAllSlots>(g, ts, vals, task, lane, gp,
                              [&](unsigned row, unsigned part, unsigned slot, const Vec3 &acc,
-                                 const Vec3 &ab, const Vec3 &pi) {
+                                 const Vec3 &ab) {
+                                 const Vec3 pi = gp(row);
                                  if (part == 0u) st4(g.p, row, pi);
                                  st4(dst[part], slot, acc);
                                  a += pi.dot(acc);
