@@ -950,9 +950,22 @@ constexpr unsigned kSchwarzWarpFloats = 4 * kSchwarzDim + kSchwarzTri;
 // Adds r^T z to `a` and |r|_1 to `b`. `seg` is the warp's shared region
 // (kSchwarzWarpFloats, 16-byte aligned); the packed factor is staged there
 // with 16-byte loads and both triangular products read it from there.
+// Copies aggregate ag's packed factor into the warp's shared segment.
+__device__ __forceinline__ void schwarz_stage(const PcgArgs &g, unsigned ag, unsigned lane,
+                                              float *seg) {
+    const SchwarzView &S = g.A.schwarz;
+    const unsigned m = __ldg(S.agg_off + ag + 1) - __ldg(S.agg_off + ag), d = 3u * m;
+    const float4 *G4 = reinterpret_cast<const float4 *>(S.ainv + __ldg(S.ainv_off + ag));
+    float4 *s4 = reinterpret_cast<float4 *>(seg + 4 * kSchwarzDim);
+    const unsigned n4 = (d * (d + 1u) / 2u + 3u) / 4u;
+    for (unsigned e = lane; e < n4; e += 32u) s4[e] = __ldg(G4 + e);
+}
+
+// `staged`: the aggregate's factor is already in the segment (the caller
+// staged it while its block waited at the grid barrier).
 __device__ __forceinline__ void schwarz_segment(const PcgArgs &g, unsigned ag, unsigned lane,
                                                 bool init, float alpha, float *seg, float &a,
-                                                float &b) {
+                                                float &b, bool staged = false) {
     const SchwarzView &S = g.A.schwarz;
     constexpr unsigned D = kSchwarzDim;
     float *sr = seg, *sy = seg + D, *sz = seg + 2 * D, *sp = seg + 3 * D;
@@ -990,12 +1003,7 @@ __device__ __forceinline__ void schwarz_segment(const PcgArgs &g, unsigned ag, u
     __syncwarp();
     if (S.n_dom && lane == 0) S.rc[ag] = make_float4(sy[0], sy[1], sy[2], 0.0f);
     __syncwarp();
-    {
-        const float4 *G4 = reinterpret_cast<const float4 *>(S.ainv + __ldg(S.ainv_off + ag));
-        float4 *s4 = reinterpret_cast<float4 *>(sG);
-        const unsigned n4 = (d * (d + 1u) / 2u + 3u) / 4u;
-        for (unsigned e = lane; e < n4; e += 32u) s4[e] = __ldg(G4 + e);
-    }
+    if (!staged) schwarz_stage(g, ag, lane, seg);
     __syncwarp();
     for (unsigned p = lane; p < d; p += 32u) { // y = G r
         const float *row = sG + p * (p + 1u) / 2u;
@@ -1162,7 +1170,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
                                             b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] +
                                                  fabsf(pi[2]) * ab[2];
                                         });
-            if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster)) goto aborted;
+            // the warp's first aggregate's factor staged while the block
+            // waits (warp 0 of each block, which waits for it, excepted)
+            const bool staged0 = wib != 0u && warp < n_agg;
+            const auto pre = [&]() {
+                if (staged0) schwarz_stage(g, warp, lane, seg);
+            };
+            if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster, pre)) goto aborted;
             const float pAp = a, bound = kCurvatureSlack * kFloatEps * b;
             float alpha;
             if (pAp > bound) {
@@ -1177,7 +1191,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
             // U: per aggregate, x += alpha p, r -= alpha A p, z = P r
             a = b = 0.0f;
             for (unsigned ag = warp; ag < n_agg; ag += nwarps)
-                schwarz_segment(g, ag, lane, false, alpha, seg, a, b);
+                schwarz_segment(g, ag, lane, false, alpha, seg, a, b, staged0 && ag == warp);
             if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
             if (n_dom) {
                 float c[1] = {0.0f};
