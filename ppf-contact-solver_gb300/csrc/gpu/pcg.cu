@@ -961,32 +961,11 @@ __device__ __forceinline__ void schwarz_stage(const PcgArgs &g, unsigned ag, uns
     for (unsigned e = lane; e < n4; e += 32u) s4[e] = __ldg(G4 + e);
 }
 
-// A lane's member of an aggregate (m <= 32) with the values of it that no
-// other warp writes, loaded ahead (while the block waits at the barrier).
-struct SchwarzMember {
-    unsigned i = 0xFFFFFFFFu;
-    Vec3 x, r;
-};
-__device__ __forceinline__ SchwarzMember schwarz_member(const PcgArgs &g, unsigned ag,
-                                                        unsigned lane) {
-    const SchwarzView &S = g.A.schwarz;
-    SchwarzMember mb;
-    const unsigned base = __ldg(S.agg_off + ag), m = __ldg(S.agg_off + ag + 1) - base;
-    if (lane < m) {
-        mb.i = __ldg(S.members + base + lane);
-        mb.x = ldcg3(g.x, mb.i);
-        mb.r = ldcg3(g.r, mb.i);
-    }
-    return mb;
-}
-
 // `staged`: the aggregate's factor is already in the segment (the caller
-// staged it while its block waited at the grid barrier); `pre`, when not
-// null, the lane's member with its x and r loaded then.
+// staged it while its block waited at the grid barrier).
 __device__ __forceinline__ void schwarz_segment(const PcgArgs &g, unsigned ag, unsigned lane,
                                                 bool init, float alpha, float *seg, float &a,
-                                                float &b, bool staged = false,
-                                                const SchwarzMember *pre = nullptr) {
+                                                float &b, bool staged = false) {
     const SchwarzView &S = g.A.schwarz;
     constexpr unsigned D = kSchwarzDim;
     float *sr = seg, *sy = seg + D, *sz = seg + 2 * D, *sp = seg + 3 * D;
@@ -994,14 +973,14 @@ __device__ __forceinline__ void schwarz_segment(const PcgArgs &g, unsigned ag, u
     const unsigned base = __ldg(S.agg_off + ag), m = __ldg(S.agg_off + ag + 1) - base;
     const unsigned d = 3u * m;
     for (unsigned k = lane; k < m; k += 32u) {
-        const unsigned i = pre ? pre->i : __ldg(S.members + base + k);
-        Vec3 ri = pre ? pre->r : ldcg3(g.r, i), pi = Vec3::zero();
+        const unsigned i = __ldg(S.members + base + k);
+        Vec3 ri = ldcg3(g.r, i), pi = Vec3::zero();
         const Vec3 api = row_product(g, i);
         if (init) {
             ri = ri - api;
         } else {
             pi = ld4(g.p, i);
-            Vec3 xi = pre ? pre->x : ldcg3(g.x, i);
+            Vec3 xi = ldcg3(g.x, i);
             for (int c = 0; c < 3; ++c) {
                 xi[c] += alpha * pi[c];
                 ri[c] = ri[c] - alpha * api[c];
@@ -1194,9 +1173,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
             // the warp's first aggregate's factor staged while the block
             // waits (warp 0 of each block, which waits for it, excepted)
             const bool staged0 = wib != 0u && warp < n_agg;
-            SchwarzMember mb0;
             const auto pre = [&]() {
-                if (warp < n_agg) mb0 = schwarz_member(g, warp, lane);
                 if (staged0) schwarz_stage(g, warp, lane, seg);
             };
             if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster, pre)) goto aborted;
@@ -1214,8 +1191,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_schwarz(PcgArgs g) {
             // U: per aggregate, x += alpha p, r -= alpha A p, z = P r
             a = b = 0.0f;
             for (unsigned ag = warp; ag < n_agg; ag += nwarps)
-                schwarz_segment(g, ag, lane, false, alpha, seg, a, b, staged0 && ag == warp,
-                                ag == warp ? &mb0 : nullptr);
+                schwarz_segment(g, ag, lane, false, alpha, seg, a, b, staged0 && ag == warp);
             if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
             if (n_dom) {
                 float c[1] = {0.0f};
