@@ -875,7 +875,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
                                             b += fabsf(pi[0]) * ab[0] + fabsf(pi[1]) * ab[1] +
                                                  fabsf(pi[2]) * ab[2];
                                         });
-            if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster)) goto aborted;
+            // the update phase's first slice: x, r and the contact position,
+            // which no other warp writes, loaded while the block waits
+            const unsigned i0 = warp * kSliceRows + lane;
+            const bool has0 = warp < n_slices && i0 < A.n;
+            Vec3 x0v = Vec3::zero(), r0v = Vec3::zero();
+            unsigned c0 = 0xFFFFFFFFu;
+            const auto pre = [&]() {
+                if (has0) {
+                    x0v = ldcg3(g.x, i0);
+                    r0v = ldcg3(g.r, i0);
+                    c0 = __ldg(A.contact.index + i0);
+                }
+            };
+            if (!grid_sum2(a, b, part1, g.bar, nb, abort, g.cluster, pre)) goto aborted;
             const float pAp = a, bound = kCurvatureSlack * kFloatEps * b;
             float alpha;
             if (pAp > bound) {
@@ -895,8 +908,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg_factor(PcgArgs g) {
             for (unsigned sl = warp; sl < n_slices; sl += nwarps) {
                 const unsigned i = sl * kSliceRows + lane;
                 if (i >= A.n) continue;
-                Vec3 pi = ld4(g.p, i), api = row_product(g, i);
-                Vec3 xi = ldcg3(g.x, i), ri = ldcg3(g.r, i);
+                const bool first = sl == warp;
+                Vec3 pi = ld4(g.p, i), api = row_product(g, i, first ? c0 : kNoIndex);
+                Vec3 xi = first ? x0v : ldcg3(g.x, i), ri = first ? r0v : ldcg3(g.r, i);
                 for (int k = 0; k < 3; ++k) {
                     xi[k] += alpha * pi[k];
                     ri[k] = ri[k] - alpha * api[k];
