@@ -440,20 +440,6 @@ struct BlockTasks {
     unsigned n_ctrs;
     unsigned phase = 0;
     unsigned *ctr = nullptr;
-    // Resets the shared counters of the next product phase; the caller
-    // orders it before that phase's first take() with a block barrier (the
-    // one ending the grid sum the reset runs in).
-    __device__ __forceinline__ void reset_next() const {
-        if (threadIdx.x == 0) {
-            next[0] = begin;
-            next[1] = 0u;
-        }
-    }
-    // Starts a phase whose counters reset_next() already set: no barrier.
-    __device__ __forceinline__ void start_reset() {
-        ctr = phase < n_ctrs ? ctrs + phase : nullptr;
-        ++phase;
-    }
     // Starts a product phase (every thread of the block calls it).
     __device__ __forceinline__ void start() {
         ctr = phase < n_ctrs ? ctrs + phase : nullptr;
@@ -611,9 +597,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
         a += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
         b += ri.dot(zi);
     }
-    // the next product phase's task counters reset inside this sum's wait
-    if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster, [&]() { bt.reset_next(); }))
-        goto aborted;
+    if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
     {
         const float err0 = a;
         float rz0 = b;
@@ -630,7 +614,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
             // S: A p_k with p_k = z + beta p_{k-1}
             a = b = 0.0f; // p^T A p, sum |p_i| |terms|
             const GatherCombined gp{g.R, beta};
-            bt.start_reset();
+            bt.start();
             float4 *dst[3] = {g.Ap, g.Ap_c, g.Ap_ovf};
             const float *const vals[3] = {A.fixed.val, A.contact.sell.val, A.ovf.val};
             for (unsigned task = bt.take(lane); task != kNoTask; task = bt.take(lane))
@@ -688,8 +672,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_pcg(PcgArgs g) {
                 a += ri.dot(zi);
                 b += fabsf(ri[0]) + fabsf(ri[1]) + fabsf(ri[2]);
             }
-            if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster, [&]() { bt.reset_next(); }))
-                goto aborted;
+            if (!grid_sum2(a, b, part0, g.bar, nb, abort, g.cluster)) goto aborted;
             const float rz_new = a, err_now = b;
             beta = rz_new / rz0;
             rz0 = rz_new;
