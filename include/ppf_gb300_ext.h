@@ -319,9 +319,10 @@ int ppf_pcg_team(void);
  * common pool taken by whichever warps finish first. 0 restores the default
  * (12); returns -1 above 16. */
 int ppf_set_pcg_static_share(unsigned sixteenths);
-/* Threads per CTA of a one-cluster block-Jacobi solve: 256, 512 or 1024 (0:
- * 1024, the default); smaller CTAs let several solves share an SM. Returns
- * -1 for another value. */
+/* Threads per CTA of a one-cluster block-Jacobi solve: 256, 512 or 1024; 0
+ * (the default) picks 512 up to 6,144 vertices and 1024 above, at each
+ * initialize. Smaller CTAs let several solves share an SM. Returns -1 for
+ * another value. */
 int ppf_set_pcg_cta_threads(unsigned threads);
 void ppf_get_tuning(unsigned char *modes);
 int ppf_set_tuning(const unsigned char *modes);

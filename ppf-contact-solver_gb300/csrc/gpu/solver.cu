@@ -669,6 +669,7 @@ bool Solver::initialize(PpfDataSet *ds, PpfParamSet *prm) {
     pcg_.reserve(n_);
     if (pcg_team_auto_) tune_.pcg_cluster = auto_pcg_team();
     pcg_.cluster = tune_.pcg_cluster;
+    if (cta_auto_) pcg_.cluster_threads = auto_cta_threads();
     upload_collision_mesh(ds->constraint.mesh);
     initialized_ = true;
     carried_ = false;

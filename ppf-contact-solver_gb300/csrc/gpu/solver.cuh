@@ -14,6 +14,10 @@ namespace ppf {
 namespace gpu {
 
 constexpr unsigned kClusterPcgRows = 16384;
+// One-cluster solves of systems up to this size run on 512-thread CTAs (per
+// PCG iteration on the 64 x 64 cloth: 8.0 against 10.1 us with 1024; at
+// 96 x 96 and above 1024 is faster)
+constexpr unsigned kSmallCtaRows = 6144;
 
 // Per-step statistics (GB300 extension, ppf_step_stats in ppf_gb300_ext.h).
 struct StepStats {
@@ -113,11 +117,13 @@ class Solver {
     // the PCG's static share of the product work, in sixteenths (1 to 16;
     // 0 the default)
     void set_pcg_static_share(unsigned sixteenths) { pcg_.static_sixteenths = sixteenths; }
-    // threads per CTA of a one-cluster block-Jacobi solve: 256, 512 or 1024
-    // (0: 1024); false for another value
+    // threads per CTA of a one-cluster block-Jacobi solve: 256, 512 or 1024;
+    // 0 restores the automatic choice (512 up to kSmallCtaRows vertices, else
+    // 1024); false for another value
     bool set_pcg_cta_threads(unsigned threads) {
         if (threads != 0 && threads != 256 && threads != 512 && threads != 1024) return false;
-        pcg_.cluster_threads = threads;
+        cta_auto_ = threads == 0;
+        pcg_.cluster_threads = cta_auto_ ? auto_cta_threads() : threads;
         return true;
     }
     // Caps the pair lists at pair_cap entries each and a capacity-sized
@@ -291,6 +297,8 @@ class Solver {
     DevBuf<StepParams> sp_dev_;
     bool pcg_team_auto_ = true;
     unsigned char auto_pcg_team() const;
+    bool cta_auto_ = true;
+    unsigned auto_cta_threads() const { return n_ <= kSmallCtaRows ? 512u : 0u; }
     DevBuf<PpfIntersectionRecord> isect_;
     std::vector<PpfIntersectionRecord> isect_host_;
     unsigned isect_count_ = 0;
