@@ -220,8 +220,8 @@ unsigned ppf_learned_tc_status(void);
  * Many independent Newton systems (one per scene of a batch of uneven scenes)
  * solved by the reference's block-Jacobi PCG (solver/solver.cu:357-400,
  * 431-571, 1002-1278; x0 = 0, relative L1 residual tol, the same check
- * schedule and curvature verdict) in ONE launch: one 1024-thread CTA per
- * system with block barriers only, so each system stops on its own iteration
+ * schedule and curvature verdict) in ONE launch: one 512-thread CTA (or a
+ * cluster of them) per system with block barriers only, so each system stops on its own iteration
  * count. No counterpart in the reference, which solves one scene per process.
  *   row_off   n_sys + 1 vertex-row offsets: system s owns rows
  *             [row_off[s], row_off[s+1])
