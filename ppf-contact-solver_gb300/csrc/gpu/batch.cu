@@ -30,8 +30,8 @@ namespace {
 namespace cg = cooperative_groups;
 
 // Threads per CTA of a team. 512: two CTAs share an SM, and a small
-// system's iteration is shorter than on 1024 (the 256 drops one launch per
-// system: 578 against 751 ms; batched 26.7 against 28.9 ms).
+// system's iteration is shorter than on 1024 (the 256 uneven drops, one
+// launch per system: 578 against 751 ms).
 constexpr unsigned kBT = 512;
 // Rows of the first size bucket (then doubling).
 constexpr unsigned kBucketRows = 1024;
