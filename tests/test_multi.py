@@ -7,6 +7,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
+import step_scenes
 from ppf_gb300 import scenes
 from ppf_gb300.multi import MultiSession
 from ppf_gb300.session import Session
@@ -117,4 +118,33 @@ def test_multi_pinned_moving_scenes(product_lib):
         x = m.positions(i)
         ref, bound = alone[i]
         assert _close(x, ref, bound), (i, np.abs(x - ref).max(), bound)
+    m.close()
+
+
+def test_multi_step_matches_the_oracle(product_lib):
+    """Two contact scenes (the two sheets after three oracle steps, and the
+    same sheets unpinned) stepped together: each scene's step matches the
+    oracle's step from the same state within 1e-5 relative, as a scene
+    stepped alone does."""
+    from oracle.binding import OracleSession
+
+    built, oracles = [], []
+    for pinned in (True, False):
+        sc, _ = step_scenes.two_sheets(pinned=pinned)
+        orc = OracleSession(sc)
+        for _ in range(3):
+            assert orc.step().success()
+        curr, prev = orc.positions()
+        sc.set_positions(curr, prev)
+        sc.param.contents.time = orc.time
+        built.append(sc)
+        oracles.append(OracleSession(sc))
+    m = MultiSession(built, threads=2)
+    res = m.step()
+    assert all(r.success() for r in res)
+    for i, o in enumerate(oracles):
+        ro = o.step()
+        assert ro.success()
+        xg, xo = m.positions(i), o.positions()[0]
+        assert np.abs(xg - xo).max() <= 1e-5 * np.abs(xo).max(), i
     m.close()
