@@ -122,29 +122,38 @@ def test_multi_pinned_moving_scenes(product_lib):
 
 
 def test_multi_step_matches_the_oracle(product_lib):
-    """Two contact scenes (the two sheets after three oracle steps, and the
-    same sheets unpinned) stepped together: each scene's step matches the
-    oracle's step from the same state within 1e-5 relative, as a scene
-    stepped alone does."""
+    """Two contact scenes (the two sheets after three oracle steps, pinned and
+    unpinned) stepped together: each scene's step matches the oracle's step
+    from the same state within 1e-5 relative, as a scene stepped alone does.
+    The oracle holds one scene at a time, so each scene's oracle step is
+    taken before the next scene is built."""
     from oracle.binding import OracleSession
 
-    built, oracles = [], []
+    states, expect = [], []
     for pinned in (True, False):
         sc, _ = step_scenes.two_sheets(pinned=pinned)
         orc = OracleSession(sc)
         for _ in range(3):
             assert orc.step().success()
         curr, prev = orc.positions()
+        t = orc.time
         sc.set_positions(curr, prev)
-        sc.param.contents.time = orc.time
+        sc.param.contents.time = t
+        o = OracleSession(sc)
+        assert o.step().success()
+        expect.append(o.positions()[0].copy())
+        states.append((pinned, curr.copy(), prev.copy(), t))
+        del o, orc, sc
+    built = []
+    for pinned, curr, prev, t in states:
+        sc, _ = step_scenes.two_sheets(pinned=pinned)
+        sc.set_positions(curr, prev)
+        sc.param.contents.time = t
         built.append(sc)
-        oracles.append(OracleSession(sc))
     m = MultiSession(built, threads=2)
     res = m.step()
     assert all(r.success() for r in res)
-    for i, o in enumerate(oracles):
-        ro = o.step()
-        assert ro.success()
-        xg, xo = m.positions(i), o.positions()[0]
-        assert np.abs(xg - xo).max() <= 1e-5 * np.abs(xo).max(), i
+    for i, xo in enumerate(expect):
+        xg = m.positions(i)
+        assert np.abs(xg - xo).max() <= 1e-5 * np.abs(xo).max(), (i, np.abs(xg - xo).max())
     m.close()
